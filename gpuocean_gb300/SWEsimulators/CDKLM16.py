@@ -1,0 +1,402 @@
+"""CDKLM16 rotating shallow-water simulator on GB300 (drop-in for ``SWEsimulators/CDKLM16.py``).
+
+Same constructor, ``step``, ``download``, ``updateDt`` ... as the reference
+(S/ = src/gpuocean/SWEsimulators, S/CDKLM16.py:43-895).  The differences are
+in how the work reaches the GPU:
+
+* all kernels are prebuilt for sm_103a and called through ``libgpuocean_gb300``;
+  physical parameters are runtime arguments, not ``#define``s;
+* an RK2 step is one fused launch (both stages and the periodic ghost fill);
+  the two buffer sets are swapped after each step, so ``gpu_data.h0`` is the
+  latest state and ``gpu_data.h1`` the previous time step;
+* the CFL reduction covers every interior cell.
+"""
+from __future__ import annotations
+
+import ctypes
+import gc
+import logging
+
+import numpy as np
+
+from .. import _lib
+from ..utils import AtmosphericPressure, Common, WindStress
+from .Simulator import Simulator
+
+
+def subsample_texture(data, factor):
+    """Bilinear re-sampling of a texture to (max(2, ny//factor), max(2, nx//factor)).
+
+    Same sample positions as S/CDKLM16.py:181-192; the result is returned in
+    [y, x] order, which is how the step kernel reads it.
+    """
+    from scipy.interpolate import RectBivariateSpline
+    ny, nx = data.shape
+    dx, dy = 1 / nx, 1 / ny
+    spline = RectBivariateSpline(np.linspace(0.5 * dx, 1 - 0.5 * dx, nx),
+                                 np.linspace(0.5 * dy, 1 - 0.5 * dy, ny), data.T, kx=1, ky=1)
+    new_nx, new_ny = max(2, nx // factor), max(2, ny // factor)
+    ndx, ndy = 1 / new_nx, 1 / new_ny
+    x_new = np.linspace(0.5 * ndx, 1 - 0.5 * ndx, new_nx)
+    y_new = np.linspace(0.5 * ndy, 1 - 0.5 * ndy, new_ny)
+    return np.ascontiguousarray(spline(x_new, y_new).T)
+
+
+def calcCoriolisParams(lat):
+    """f and beta of a latitude (rad): f = 2 Omega sin(lat), beta = 2 Omega cos(lat)/a."""
+    omega = 7.2921e-5
+    a = 6371008.8
+    return [2.0 * omega * np.sin(lat), 2.0 * omega * np.cos(lat) / a]
+
+
+class CDKLM16(Simulator):
+    """Chertock, Dudzinski, Kurganov & Lukacova-Medvidova (2016) well-balanced
+    central-upwind scheme for the rotating shallow-water equations."""
+
+    def __init__(self, gpu_ctx, eta0, hu0, hv0, H, nx, ny, dx, dy, dt, g, f, r,
+                 subsample_f=10, angle=np.array([[0]], dtype=np.float32), subsample_angle=10,
+                 latitude=None, rho_o=1025.0, t=0.0, theta=1.8, rk_order=2, coriolis_beta=0.0,
+                 max_wind_direction_perturbation=0, wind=None, wind_stress_factor=1.0,
+                 atmospheric_pressure=None, boundary_conditions=None, boundary_conditions_data=None,
+                 model_time_step=None, reportGeostrophicEquilibrium=False, write_netcdf=False,
+                 comm=None, local_particle_id=0, super_dir_name=None, netcdf_filename=None,
+                 ignore_ghostcells=False, courant_number=0.8, offset_x=0, offset_y=0,
+                 flux_slope_eps=1.0e-1, desingularization_eps=1.0e-1, depth_cutoff=1.0e-5,
+                 one_dimensional=False, flux_balancer=0.8, block_width=12, block_height=32,
+                 num_threads_dt=256, use_direct_lookup=False):
+        self.logger = logging.getLogger(__name__)
+        assert rk_order in (1, 2, 3), "Only 1st, 2nd and 3rd order Runge Kutta supported"
+        if rk_order == 3:
+            assert r == 0.0, "3rd order Runge Kutta supported only without friction"
+        if write_netcdf:
+            raise NotImplementedError("NetCDF output is not part of this package")
+        if use_direct_lookup:
+            raise NotImplementedError("use_direct_lookup is not supported; pressure is always interpolated")
+        wind = WindStress.WindStress() if wind is None else wind
+        atmospheric_pressure = AtmosphericPressure.AtmosphericPressure() if atmospheric_pressure is None else atmospheric_pressure
+        boundary_conditions = Common.BoundaryConditions() if boundary_conditions is None else boundary_conditions
+        if boundary_conditions.isSponge():
+            raise NotImplementedError("sponge boundary conditions (3, 4) are not supported")
+        angle = np.asarray(angle)
+        ghost_cells_x = ghost_cells_y = 2
+        self.boundary_conditions = boundary_conditions
+        # compensate f for the reference cell (S/CDKLM16.py:147-149)
+        north = np.array([np.sin(angle.flat[0]), np.cos(angle.flat[0])])
+        f = f - coriolis_beta * (ghost_cells_x * dx * north[0] + ghost_cells_y * dy * north[1])
+        self.max_wind_direction_perturbation = max_wind_direction_perturbation
+        super().__init__(gpu_ctx, nx, ny, ghost_cells_x, ghost_cells_y, dx, dy, dt, g, f, r, None, t,
+                         theta, rk_order, coriolis_beta, 0, wind, atmospheric_pressure, write_netcdf,
+                         ignore_ghostcells, offset_x, offset_y, comm, block_width, block_height,
+                         local_particle_id=local_particle_id)
+        self.interior_domain_indices = np.array([-2, -2, 2, 2])
+
+        # Coriolis texture (S/CDKLM16.py:194-223)
+        eta0 = np.asarray(eta0) if not np.ma.isMaskedArray(eta0) else eta0
+        if latitude is not None:
+            if self.f != 0.0:
+                raise RuntimeError("Cannot specify both latitude and f. Make your mind up.")
+            coriolis_f, _ = calcCoriolisParams(latitude)
+            coriolis_f = np.asarray(coriolis_f, dtype=np.float32)
+        elif self.coriolis_beta != 0.0:
+            if angle.size != 1:
+                raise RuntimeError("non-constant angle cannot be combined with beta plane model (makes no sense)")
+            x = np.linspace((-ghost_cells_x + 0.5) * self.dx, (self.nx + ghost_cells_x - 0.5) * self.dx, self.nx + 2 * ghost_cells_x)
+            y = np.linspace((-ghost_cells_y + 0.5) * self.dy, (self.ny + ghost_cells_y - 0.5) * self.dy, self.ny + 2 * ghost_cells_x)
+            x, y = np.meshgrid(x, y)
+            n = x * np.sin(angle.flat[0]) + y * np.cos(angle.flat[0])
+            coriolis_f = self.f + self.coriolis_beta * n
+        elif np.size(self.f) == 1:
+            coriolis_f = np.array([[self.f]], dtype=np.float32)
+        elif np.shape(self.f) == eta0.shape:
+            coriolis_f = np.array(self.f, dtype=np.float32)
+        else:
+            raise RuntimeError("The shape of f should match up with eta or be scalar.")
+        coriolis_f = np.atleast_2d(coriolis_f)
+        if subsample_f and coriolis_f.size >= eta0.size:
+            coriolis_f = subsample_texture(coriolis_f, subsample_f)
+        self.coriolis_f_arr = Common.CUDAArray2D(self.gpu_stream, coriolis_f.shape[1], coriolis_f.shape[0], 0, 0, coriolis_f)
+        if subsample_angle and angle.size >= eta0.size:
+            angle = subsample_texture(angle, subsample_angle)
+        angle = np.atleast_2d(np.asarray(angle, dtype=np.float32))
+        if angle.size != 1:
+            raise NotImplementedError("only a constant north angle is supported by the GB300 step kernel")
+        self.angle_arr = Common.CUDAArray2D(self.gpu_stream, angle.shape[1], angle.shape[0], 0, 0, angle)
+
+        self.rho_o = np.float32(rho_o)
+        self.wind_stress_factor = np.float32(wind_stress_factor)
+        self.flux_slope_eps = np.float32(flux_slope_eps)
+        self.desingularization_eps = np.float32(desingularization_eps)
+        self.depth_cutoff = np.float32(depth_cutoff)
+        self.flux_balancer = np.float32(flux_balancer)
+        self.one_dimensional = bool(one_dimensional)
+
+        # bathymetry, dry-state clamp and the double-buffered state
+        self.bathymetry = Common.Bathymetry(gpu_ctx, self.gpu_stream, nx, ny, ghost_cells_x, ghost_cells_y, H,
+                                            boundary_conditions)
+        Hm = self.downloadBathymetry()[1]
+        eta0 = np.maximum(eta0, -Hm)
+        self.gpu_data = Common.SWEDataArakawaA(self.gpu_stream, nx, ny, ghost_cells_x, ghost_cells_y, eta0, hu0, hv0)
+        self.gpu_data_extra = None  # third buffer set for RK3
+
+        # CFL reduction buffers
+        self.num_threads_dt = num_threads_dt
+        n_part = _lib.load().goc_max_dt_partials(int(nx), int(ny))
+        self.device_dt = Common.DevicePtr(4 * n_part)
+        self.num_blocks_dt = np.int32(n_part)
+        self.max_dt_buffer = Common.DevicePtr(4)
+        self.courant_number = courant_number
+
+        self.reportGeostrophicEquilibrium = np.int32(reportGeostrophicEquilibrium)
+        self.constant_equilibrium_depth = np.max(H)
+        self.bc_kernel = Common.BoundaryConditionsArakawaA(gpu_ctx, self.gpu_stream, self.nx, self.ny,
+                                                           ghost_cells_x, ghost_cells_y, self.boundary_conditions,
+                                                           boundary_conditions_data)
+        self.model_error = None
+        self.model_time_step = model_time_step
+        self.total_time_steps = 0
+        if model_time_step is None:
+            self.model_time_step = self.dt
+        self._params = self._make_params()
+        if self.dt <= 0:
+            self.updateDt()
+
+    # ------------------------------------------------------------------
+    def _make_params(self):
+        p = _lib.GocCdklmParams()
+        p.nx, p.ny = int(self.nx), int(self.ny)
+        p.dx, p.dy, p.g, p.r = float(self.dx), float(self.dy), float(self.g), float(self.r)
+        p.theta = float(self.theta)
+        p.desing_eps = float(self.desingularization_eps)
+        p.flux_slope_eps = float(self.flux_slope_eps)
+        p.depth_cutoff = float(self.depth_cutoff)
+        p.flux_balancer = float(self.flux_balancer)
+        p.rho_o = float(self.rho_o)
+        p.wind_stress_factor = float(self.wind_stress_factor)
+        p.rk_order = int(self.rk_order)
+        p.one_dimensional = int(self.one_dimensional)
+        bc = self.boundary_conditions
+        p.bc_north, p.bc_east, p.bc_south, p.bc_west = int(bc.north), int(bc.east), int(bc.south), int(bc.west)
+        p.land_value = float(self.bathymetry.mask_value)
+        p.coriolis_f = self.coriolis_f_arr.ptr
+        p.coriolis_nx, p.coriolis_ny = self.coriolis_f_arr.nx_halo, self.coriolis_f_arr.ny_halo
+        p.angle = self.angle_arr.ptr
+        p.angle_nx, p.angle_ny = self.angle_arr.nx_halo, self.angle_arr.ny_halo
+        p.wind_x_cur, p.wind_x_next = self.wind_stress_x_current_arr.ptr, self.wind_stress_x_next_arr.ptr
+        p.wind_x_nx, p.wind_x_ny = self.wind_stress_x_current_arr.nx_halo, self.wind_stress_x_current_arr.ny_halo
+        p.wind_y_cur, p.wind_y_next = self.wind_stress_y_current_arr.ptr, self.wind_stress_y_next_arr.ptr
+        p.wind_y_nx, p.wind_y_ny = self.wind_stress_y_current_arr.nx_halo, self.wind_stress_y_current_arr.ny_halo
+        p.atm_p_cur, p.atm_p_next = self.atmospheric_pressure_current_arr.ptr, self.atmospheric_pressure_next_arr.ptr
+        p.atm_p_nx, p.atm_p_ny = self.atmospheric_pressure_current_arr.nx_halo, self.atmospheric_pressure_current_arr.ny_halo
+        return p
+
+    @property
+    def stream_handle(self):
+        return self.gpu_stream.handle
+
+    def cleanUp(self, do_gc=True):
+        if getattr(self, "gpu_data", None) is None:
+            return
+        if self.model_error is not None:
+            self.model_error.cleanUp(do_gc=False)
+        self.gpu_data.release()
+        if self.gpu_data_extra is not None:
+            self.gpu_data_extra.release()
+        self.bathymetry.release()
+        self.device_dt.free()
+        self.max_dt_buffer.free()
+        for a in (self.coriolis_f_arr, self.angle_arr, self.wind_stress_x_current_arr, self.wind_stress_y_current_arr,
+                  self.wind_stress_x_next_arr, self.wind_stress_y_next_arr, self.atmospheric_pressure_current_arr,
+                  self.atmospheric_pressure_next_arr):
+            a.release()
+        self.gpu_data = None
+        self.gpu_ctx = None
+        if do_gc:
+            gc.collect()
+
+    # ------------------------------------------------------------------
+    def _stage(self, src, dst, dt, rk_step, alt=None):
+        d = self.gpu_data
+        a = alt if alt is not None else (None, None, None)
+        _lib.call("goc_cdklm_stage", ctypes.byref(self._params), ctypes.c_float(dt), int(rk_step),
+                  src[0].ptr, src[1].ptr, src[2].ptr, dst[0].ptr, dst[1].ptr, dst[2].ptr,
+                  a[0].ptr if alt else None, a[1].ptr if alt else None, a[2].ptr if alt else None,
+                  int(d.h0.pitch), self.bathymetry.Bi.ptr, int(self.bathymetry.Bi.pitch), self.stream_handle)
+
+    def _rk_step(self, local_dt):
+        d = self.gpu_data
+        if self.rk_order == 2:
+            _lib.call("goc_cdklm_rk2_step", ctypes.byref(self._params), ctypes.c_float(local_dt),
+                      d.h0.ptr, d.hu0.ptr, d.hv0.ptr, d.h1.ptr, d.hu1.ptr, d.hv1.ptr, int(d.h0.pitch),
+                      self.bathymetry.Bi.ptr, int(self.bathymetry.Bi.pitch), self.stream_handle)
+            d.swap()
+        elif self.rk_order == 1:
+            self._stage((d.h0, d.hu0, d.hv0), (d.h1, d.hu1, d.hv1), local_dt, 0)
+            d.swap()
+            self.bc_kernel.boundaryCondition(self.gpu_stream, d.h0, d.hu0, d.hv0)
+        else:
+            if self.gpu_data_extra is None:
+                eta, hu, hv = self.download()
+                self.gpu_data_extra = Common.SWEDataArakawaA(self.gpu_stream, self.nx, self.ny, 2, 2, eta, hu, hv)
+            x = self.gpu_data_extra
+            q0, q1, q2 = (d.h0, d.hu0, d.hv0), (d.h1, d.hu1, d.hv1), (x.h0, x.hu0, x.hv0)
+            self._stage(q0, q1, local_dt, 0)
+            self.bc_kernel.boundaryCondition(self.gpu_stream, *q1)
+            self._stage(q1, q0, local_dt, 1, alt=q2)
+            self.bc_kernel.boundaryCondition(self.gpu_stream, *q2)
+            self._stage(q2, q0, local_dt, 2)
+            self.bc_kernel.boundaryCondition(self.gpu_stream, *q0)
+
+    def step(self, t_end=0.0, apply_stochastic_term=True, write_now=True, update_dt=False):
+        """Advance by ``t_end`` seconds in steps of at most ``self.dt``
+        (S/CDKLM16.py:477-584)."""
+        if self.t == 0:
+            self.bc_kernel.update_bc_values(self.gpu_stream, self.t)
+            self.bc_kernel.boundaryCondition(self.gpu_stream, self.gpu_data.h0, self.gpu_data.hu0, self.gpu_data.hv0)
+        t_now = 0.0
+        while t_now < t_end:
+            if update_dt:
+                self.updateDt()
+            local_dt = np.float32(min(self.dt, np.float32(t_end - t_now)))
+            self._params.wind_t = float(np.float32(self.update_wind_stress()))
+            self._params.atm_p_t = float(np.float32(self.update_atmospheric_pressure()))
+            self._rk_step(local_dt)
+            if self.model_error is not None and apply_stochastic_term:
+                self.perturbState()
+                self.bc_kernel.boundaryCondition(self.gpu_stream, self.gpu_data.h0, self.gpu_data.hu0,
+                                                 self.gpu_data.hv0)
+            self.drifterStep(local_dt)
+            self.t += np.float64(local_dt)
+            t_now += np.float64(local_dt)
+            self.num_iterations += 1
+        return self.t
+
+    # ------------------------------------------------------------------
+    def setSOARModelError(self, small_scale_perturbation_amplitude=None, small_scale_perturbation_interpolation_factor=1,
+                          use_lcg=False, xorwow_seed=None, block_width_model_error=16, block_height_model_error=16):
+        from . import OceanStateNoise
+        self.model_error = OceanStateNoise.OceanStateNoise.fromsim(
+            self, soar_q0=small_scale_perturbation_amplitude,
+            interpolation_factor=small_scale_perturbation_interpolation_factor,
+            use_lcg=use_lcg, xorwow_seed=xorwow_seed,
+            block_width=block_width_model_error, block_height=block_height_model_error)
+
+    def perturbState(self, perturbation_scale=1.0, update_random_field=True, q0_scale=1):
+        if q0_scale != 1:
+            perturbation_scale = q0_scale
+        if self.model_error is not None:
+            self.model_error.perturbSim(self, perturbation_scale=perturbation_scale,
+                                        update_random_field=update_random_field)
+
+    def perturbSimilarAs(self, otherSim, perturbation_scale=1.0):
+        self.model_error.perturbSimSimilarAs(self, modelError=otherSim.model_error,
+                                             perturbation_scale=perturbation_scale)
+
+    def applyBoundaryConditions(self):
+        self.bc_kernel.boundaryCondition(self.gpu_stream, self.gpu_data.h0, self.gpu_data.hu0, self.gpu_data.hv0)
+
+    def drifterStep(self, dt):
+        if self.hasCrossProductDrifter:
+            for d in range(len(self.CrossProductDrifter)):
+                if self.CPsims[d] is not None:
+                    o = self.CPsims[d]
+                    self.CrossProductDrifter[d].drift(o.gpu_data.h0, o.gpu_data.hu0, o.gpu_data.hv0, o.bathymetry.Bm,
+                                                      self.nx, self.ny, self.t, self.dx, self.dy, dt,
+                                                      np.int32(2), np.int32(2))
+                self.CrossProductDrifter[d].drift(self.gpu_data.h0, self.gpu_data.hu0, self.gpu_data.hv0,
+                                                  self.bathymetry.Bm, self.nx, self.ny, self.t, self.dx, self.dy, dt,
+                                                  np.int32(2), np.int32(2))
+            self.CPdrifter_t += dt
+        if self.hasDrifters:
+            self.drifters.driftFromSim(self, dt)
+            self.drifter_t += dt
+            return self.drifter_t
+
+    def dataAssimilationStep(self, observation_time, otherSim=None, model_error_final_step=True, write_now=True,
+                             courant_number=0.8):
+        """Run to ``observation_time`` with model error every ``model_time_step``
+        (S/CDKLM16.py:742-806)."""
+        full_model_time_steps = int(round(observation_time - self.t) / self.model_time_step)
+        leftover_step_size = observation_time - self.t - full_model_time_steps * self.model_time_step
+        if leftover_step_size / self.model_time_step < 0.1 and full_model_time_steps > 1:
+            leftover_step_size += self.model_time_step
+            full_model_time_steps -= 1
+        if leftover_step_size / self.model_time_step < 0.00001:
+            leftover_step_size = 0
+        assert full_model_time_steps > 0, "There is less than CDKLM16.model_time_step until the observation"
+        self.updateDt(courant_number=courant_number)
+        if otherSim is not None:
+            otherSim.updateDt(courant_number=courant_number)
+        for i in range(full_model_time_steps + 1):
+            if i == 0 and leftover_step_size == 0:
+                continue
+            elif i == 0:
+                self.step(leftover_step_size, apply_stochastic_term=False, write_now=False)
+                self.perturbState(perturbation_scale=np.sqrt(leftover_step_size / self.model_time_step))
+                if otherSim is not None:
+                    otherSim.step(leftover_step_size, apply_stochastic_term=False, write_now=False)
+                    otherSim.perturbSimilarAs(self, perturbation_scale=np.sqrt(leftover_step_size / self.model_time_step))
+            else:
+                self.step(self.model_time_step, apply_stochastic_term=False, write_now=False)
+                if (i < full_model_time_steps) or model_error_final_step:
+                    self.perturbState()
+                if otherSim is not None:
+                    otherSim.step(self.model_time_step, apply_stochastic_term=False, write_now=False)
+                    if (i < full_model_time_steps) or model_error_final_step:
+                        otherSim.perturbSimilarAs(self)
+            self.total_time_steps += 1
+            if self.total_time_steps % 5 == 0:
+                self.updateDt(courant_number=courant_number)
+        assert round(observation_time) == round(self.t), \
+            'The simulation time is not the same as observation time after dataAssimilationStep! \n' + \
+            '(self.t, observation_time, diff): ' + str((self.t, observation_time, self.t - observation_time))
+
+    def writeState(self):
+        return None
+
+    # ------------------------------------------------------------------
+    def downloadMaxDt(self):
+        """Launch the CFL reduction and return the limit before the Courant factor."""
+        d = self.gpu_data
+        _lib.call("goc_max_dt", int(self.nx), int(self.ny), ctypes.c_float(self.dx), ctypes.c_float(self.dy),
+                  ctypes.c_float(self.g), d.h0.ptr, d.hu0.ptr, d.hv0.ptr, int(d.h0.pitch),
+                  self.bathymetry.Bm.ptr, int(self.bathymetry.Bm.pitch), ctypes.c_float(self.bathymetry.mask_value),
+                  self.device_dt.ptr, int(self.num_blocks_dt), self.max_dt_buffer.ptr, self.stream_handle)
+        out = np.zeros(1, dtype=np.float32)
+        _lib.call("goc_memcpy_d2h_async", out.ctypes.data, self.max_dt_buffer.ptr, ctypes.c_size_t(4), self.stream_handle)
+        self.gpu_stream.synchronize()
+        return out[0]
+
+    def updateDt(self, courant_number=None):
+        """dt = courant_number * CFL limit (S/CDKLM16.py:814-841)."""
+        if courant_number is None:
+            courant_number = self.courant_number
+        self.dt = courant_number * self.downloadMaxDt()
+
+    def _getMaxTimestepHost(self, courant_number=0.8):
+        eta, hu, hv = self.download(interior_domain_only=True)
+        Hm = self.downloadBathymetry()[1][2:-2, 2:-2]
+        h = eta + Hm
+        gravityWaves = np.sqrt(self.g * h)
+        u = hu / h
+        v = hv / h
+        max_dt = 0.25 * min(self.dx / np.max(np.abs(u) + gravityWaves), self.dy / np.max(np.abs(v) + gravityWaves))
+        return courant_number * max_dt
+
+    def downloadBathymetry(self, interior_domain_only=False):
+        Bi, Bm = self.bathymetry.download(self.gpu_stream)
+        if interior_domain_only:
+            Bi = Bi[2:-2 + 1, 2:-2 + 1]
+            Bm = Bm[2:-2, 2:-2]
+        return [Bi, Bm]
+
+    def getLandMask(self, interior_domain_only=True):
+        if self.gpu_data.h0.mask is None:
+            return None
+        return self.gpu_data.h0.mask[2:-2, 2:-2] if interior_domain_only else self.gpu_data.h0.mask
+
+    def downloadDt(self):
+        out = np.zeros(int(self.num_blocks_dt), dtype=np.float32)
+        _lib.call("goc_memcpy_d2h_async", out.ctypes.data, self.device_dt.ptr, ctypes.c_size_t(out.nbytes),
+                  self.stream_handle)
+        self.gpu_stream.synchronize()
+        return out

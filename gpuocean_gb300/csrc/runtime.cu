@@ -1,0 +1,186 @@
+// Runtime plumbing of the C ABI: errors, device memory, streams, events,
+// CUDA graphs and the launch counter.
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "common.cuh"
+
+namespace goc {
+
+static thread_local std::string g_last_error;
+static std::atomic<int64_t> g_launches{0};
+
+int set_error(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int check_launch(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(GOC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    return GOC_OK;
+}
+
+void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+static int cuda_result(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) return set_error(GOC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    return GOC_OK;
+}
+
+}  // namespace goc
+
+using namespace goc;
+
+extern "C" {
+
+int goc_version(void) { return 1; }
+
+int goc_last_error(char* buf, int len) {
+    if (!buf || len <= 0) return GOC_ERR_ARG;
+    std::strncpy(buf, g_last_error.c_str(), (size_t)len - 1);
+    buf[len - 1] = '\0';
+    return GOC_OK;
+}
+
+int goc_device_count(int* count) {
+    if (!count) return set_error(GOC_ERR_ARG, "goc_device_count: null count");
+    return cuda_result(cudaGetDeviceCount(count), "cudaGetDeviceCount");
+}
+
+int goc_set_device(int device) { return cuda_result(cudaSetDevice(device), "cudaSetDevice"); }
+
+int goc_device_synchronize(void) { return cuda_result(cudaDeviceSynchronize(), "cudaDeviceSynchronize"); }
+
+int goc_malloc(void** ptr, size_t bytes) {
+    if (!ptr) return set_error(GOC_ERR_ARG, "goc_malloc: null out pointer");
+    *ptr = nullptr;
+    if (bytes == 0) return GOC_OK;
+    return cuda_result(cudaMalloc(ptr, bytes), "cudaMalloc");
+}
+
+int goc_free(void* ptr) {
+    if (!ptr) return GOC_OK;
+    return cuda_result(cudaFree(ptr), "cudaFree");
+}
+
+int goc_host_alloc(void** ptr, size_t bytes) {
+    if (!ptr) return set_error(GOC_ERR_ARG, "goc_host_alloc: null out pointer");
+    *ptr = nullptr;
+    if (bytes == 0) return GOC_OK;
+    return cuda_result(cudaMallocHost(ptr, bytes), "cudaMallocHost");
+}
+
+int goc_host_free(void* ptr) {
+    if (!ptr) return GOC_OK;
+    return cuda_result(cudaFreeHost(ptr), "cudaFreeHost");
+}
+
+int goc_memset_async(void* dst, int value, size_t bytes, void* stream) {
+    if (bytes == 0) return GOC_OK;
+    if (!dst) return set_error(GOC_ERR_ARG, "goc_memset_async: null destination");
+    return cuda_result(cudaMemsetAsync(dst, value, bytes, as_stream(stream)), "cudaMemsetAsync");
+}
+
+static int copy(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, void* stream,
+                const char* what) {
+    if (bytes == 0) return GOC_OK;
+    if (!dst || !src) return set_error(GOC_ERR_ARG, "%s: null pointer", what);
+    return cuda_result(cudaMemcpyAsync(dst, src, bytes, kind, as_stream(stream)), what);
+}
+
+int goc_memcpy_h2d_async(void* dst, const void* src, size_t bytes, void* stream) {
+    return copy(dst, src, bytes, cudaMemcpyHostToDevice, stream, "goc_memcpy_h2d_async");
+}
+
+int goc_memcpy_d2h_async(void* dst, const void* src, size_t bytes, void* stream) {
+    return copy(dst, src, bytes, cudaMemcpyDeviceToHost, stream, "goc_memcpy_d2h_async");
+}
+
+int goc_memcpy_d2d_async(void* dst, const void* src, size_t bytes, void* stream) {
+    return copy(dst, src, bytes, cudaMemcpyDeviceToDevice, stream, "goc_memcpy_d2d_async");
+}
+
+int goc_stream_create(void** stream) {
+    if (!stream) return set_error(GOC_ERR_ARG, "goc_stream_create: null out pointer");
+    cudaStream_t s = nullptr;
+    int rc = cuda_result(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+    *stream = s;
+    return rc;
+}
+
+int goc_stream_destroy(void* stream) {
+    if (!stream) return GOC_OK;
+    return cuda_result(cudaStreamDestroy(as_stream(stream)), "cudaStreamDestroy");
+}
+
+int goc_stream_synchronize(void* stream) {
+    return cuda_result(cudaStreamSynchronize(as_stream(stream)), "cudaStreamSynchronize");
+}
+
+int goc_event_create(void** event) {
+    if (!event) return set_error(GOC_ERR_ARG, "goc_event_create: null out pointer");
+    cudaEvent_t e = nullptr;
+    int rc = cuda_result(cudaEventCreate(&e), "cudaEventCreate");
+    *event = e;
+    return rc;
+}
+
+int goc_event_destroy(void* event) {
+    if (!event) return GOC_OK;
+    return cuda_result(cudaEventDestroy(reinterpret_cast<cudaEvent_t>(event)), "cudaEventDestroy");
+}
+
+int goc_event_record(void* event, void* stream) {
+    return cuda_result(cudaEventRecord(reinterpret_cast<cudaEvent_t>(event), as_stream(stream)),
+                       "cudaEventRecord");
+}
+
+int goc_event_elapsed_ms(void* start, void* stop, float* ms) {
+    if (!ms) return set_error(GOC_ERR_ARG, "goc_event_elapsed_ms: null out pointer");
+    return cuda_result(cudaEventElapsedTime(ms, reinterpret_cast<cudaEvent_t>(start),
+                                            reinterpret_cast<cudaEvent_t>(stop)),
+                       "cudaEventElapsedTime");
+}
+
+int goc_graph_begin_capture(void* stream) {
+    if (!stream) return set_error(GOC_ERR_ARG, "goc_graph_begin_capture: capture needs a non-default stream");
+    return cuda_result(cudaStreamBeginCapture(as_stream(stream), cudaStreamCaptureModeThreadLocal),
+                       "cudaStreamBeginCapture");
+}
+
+int goc_graph_end_capture(void* stream, void** graph_exec) {
+    if (!graph_exec) return set_error(GOC_ERR_ARG, "goc_graph_end_capture: null out pointer");
+    cudaGraph_t graph = nullptr;
+    int rc = cuda_result(cudaStreamEndCapture(as_stream(stream), &graph), "cudaStreamEndCapture");
+    if (rc) return rc;
+    cudaGraphExec_t exec = nullptr;
+    rc = cuda_result(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+    cudaGraphDestroy(graph);
+    *graph_exec = exec;
+    return rc;
+}
+
+int goc_graph_launch(void* graph_exec, void* stream) {
+    if (!graph_exec) return set_error(GOC_ERR_ARG, "goc_graph_launch: null graph");
+    return cuda_result(cudaGraphLaunch(reinterpret_cast<cudaGraphExec_t>(graph_exec), as_stream(stream)),
+                       "cudaGraphLaunch");
+}
+
+int goc_graph_destroy(void* graph_exec) {
+    if (!graph_exec) return GOC_OK;
+    return cuda_result(cudaGraphExecDestroy(reinterpret_cast<cudaGraphExec_t>(graph_exec)),
+                       "cudaGraphExecDestroy");
+}
+
+int64_t goc_kernel_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+}  // extern "C"
