@@ -1,0 +1,550 @@
+"""Benchmark: member-cell-steps/s of the batched CDKLM16 ensemble on one GB300.
+
+Workload (default ``c3``): 256 members on the double-jet domain
+(nx=512, ny=300, dx=dy=5 km, periodic in x, walls in y, beta plane,
+Gaussian-random bathymetry), 1000 drifters per member, stepped in blocks of
+one model time step (60 s, ~3 RK2 steps per member at the CFL limit).  One
+bench "step" is one such block for every member.  All inputs are synthetic
+(seeded), as the reference's configurations are.
+
+Output: one JSON line (rank 0).  ``--impl reference`` times the reference
+algorithm on the host cores instead (the reference has no CPU step of its
+own; the FP64 restatement under oracle/ stands in for it).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MODEL_TIME_STEP = 60.0
+NOISE_FACTOR = 8          # coarse grid every 8 cells
+NOISE_L_COARSE = 8.0      # SOAR length scale in coarse cells
+NOISE_STD = 0.003         # target std of the SOAR eta perturbation [m]
+
+
+def soar_q0(L_cells=NOISE_L_COARSE, std=NOISE_STD):
+    """q0 such that the SOAR field sum_{5x5} Q xi has standard deviation `std`
+    for unit normals: q0 = std / sqrt(sum s(d)^2), s(d) = (1 + d/L) exp(-d/L)."""
+    oy, ox = np.mgrid[-2:3, -2:3]
+    d = np.sqrt(ox ** 2 + oy ** 2) / L_cells
+    return std / np.sqrt(np.sum(((1 + d) * np.exp(-d)) ** 2))
+
+
+# ---------------------------------------------------------------------------
+# helpers
+# ---------------------------------------------------------------------------
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-reduction across torchrun ranks (no-op for one rank)."""
+
+    def __init__(self, world, backend):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as td
+            td.init_process_group(backend=backend)
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, v):
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        if self.td.get_backend() == "nccl":
+            t = t.cuda()
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# workload construction
+# ---------------------------------------------------------------------------
+
+def workload_spec(name, members):
+    if name == "c3":
+        return dict(name="c3", members=members, nx=512, ny=300, drifters=1000, noise=True)
+    if name == "c1":
+        return dict(name="c1", members=members, nx=256, ny=256, drifters=0, noise=False)
+    raise SystemExit("unknown workload " + name)
+
+
+def make_case(spec):
+    from gpuocean_gb300.utils import BenchmarkCases
+    if spec["name"] == "c3":
+        return BenchmarkCases.double_jet_case(nx=spec["nx"], ny=spec["ny"])
+    return BenchmarkCases.gaussian_bump_case(nx=spec["nx"], ny=spec["ny"])
+
+
+def build_members(ctx, spec, case):
+    from gpuocean_gb300.SWEsimulators import CDKLM16
+    from gpuocean_gb300.drifters import GPUDrifterCollection
+    from gpuocean_gb300.utils import Common
+    sims = []
+    bc = Common.BoundaryConditions(*case["boundary"])
+    for m in range(spec["members"]):
+        sim = CDKLM16.CDKLM16(ctx, case["eta0"], case["hu0"], case["hv0"], case["H"], case["nx"], case["ny"],
+                              case["dx"], case["dy"], 0.0, case["g"], case["f"], case["r"],
+                              coriolis_beta=case.get("coriolis_beta", 0.0), boundary_conditions=bc,
+                              model_time_step=MODEL_TIME_STEP)
+        if spec["drifters"]:
+            rng = np.random.default_rng(5000 + m)
+            d = GPUDrifterCollection.GPUDrifterCollection(
+                ctx, spec["drifters"], boundaryConditions=bc, domain_size_x=case["nx"] * case["dx"],
+                domain_size_y=case["ny"] * case["dy"], gpu_stream=sim.gpu_stream)
+            pos = np.stack([rng.uniform(0, case["nx"] * case["dx"], spec["drifters"]),
+                            rng.uniform(0, case["ny"] * case["dy"], spec["drifters"])], axis=1)
+            d.setDrifterPositions(pos)
+            d.setObservationPosition(np.array([0.5 * case["nx"] * case["dx"], 0.5 * case["ny"] * case["dy"]]))
+            sim.attachDrifters(d)
+        if spec.get("noise"):
+            from gpuocean_gb300.SWEsimulators.OceanStateNoise import OceanStateNoise
+            cdx = case["dx"] * NOISE_FACTOR
+            sim.model_error = OceanStateNoise.fromsim(sim, soar_q0=soar_q0(), soar_L=NOISE_L_COARSE * cdx,
+                                                      interpolation_factor=NOISE_FACTOR, strict_odd_factor=False)
+        sims.append(sim)
+    return sims
+
+
+def algorithmic_bytes_per_launch(sims, n_active, distinct_bathymetry):
+    """24 B per member-cell-step (read + write eta, hu, hv), 4 B per corner of
+    each distinct bathymetry, 16 B per drifter-step (read + write x, y)."""
+    cells = sum(int(s.nx) * int(s.ny) for s in sims[:n_active])
+    bathy = distinct_bathymetry * (int(sims[0].nx) + 5) * (int(sims[0].ny) + 5) * 4
+    drift = sum((s.drifters.getNumDrifters() + 1) * 16 for s in sims[:n_active] if s.hasDrifters)
+    return 24 * cells + bathy + drift
+
+
+# ---------------------------------------------------------------------------
+# the reference algorithm on the host (CPU baseline and the reference arm)
+# ---------------------------------------------------------------------------
+
+def _oracle_member_block(args):
+    spec, m, n_blocks = args
+    from oracle.cdklm16_oracle import BC, OracleCDKLM16
+    case = make_case(spec)
+    sim = OracleCDKLM16(case["eta0"], case["hu0"], case["hv0"], case["H"], case["nx"], case["ny"], case["dx"],
+                        case["dy"], 0.0, case["g"], case["f"], case["r"],
+                        coriolis_beta=case.get("coriolis_beta", 0.0), boundary_conditions=BC(*case["boundary"]))
+    t0 = time.perf_counter()
+    steps = 0
+    for _ in range(n_blocks):
+        before = sim.num_iterations
+        sim.step(MODEL_TIME_STEP)
+        steps += sim.num_iterations - before
+    return steps * case["nx"] * case["ny"], time.perf_counter() - t0
+
+
+def cpu_reference_rate(spec, n_members, n_blocks, cores):
+    """member-cell-steps/s of the FP64 oracle on `cores` processes."""
+    jobs = [(spec, m, n_blocks) for m in range(n_members)]
+    t0 = time.perf_counter()
+    if cores <= 1:
+        res = [_oracle_member_block(j) for j in jobs]
+    else:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(cores) as pool:
+            res = pool.map(_oracle_member_block, jobs)
+    wall = time.perf_counter() - t0
+    cells = sum(r[0] for r in res)
+    return cells / wall, wall
+
+
+def run_reference(args, spec, rank, world):
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    n_members = max(cores, 1)
+    rate, wall = cpu_reference_rate(spec, n_members, 1, cores)
+    rates = [rate]
+    for _ in range(max(0, args.steps - 1)):
+        if wall > 60:
+            break
+        r, _w = cpu_reference_rate(spec, n_members, 1, cores)
+        rates.append(r)
+    value = statistics.median(rates)
+    sample = (f"{n_members} members x 1 block of {MODEL_TIME_STEP:.0f} s of the {spec['name']} workload per step, "
+              f"FP64 NumPy restatement (the reference has no CPU step), one member per process")
+    line = {"metric": "member-cell-steps/s", "value": value, "unit": "member-cell-steps/s", "n_gpus": world,
+            "steps": len(rates), "warmup": 0, "ms_per_step": 1000.0 * wall, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": spec["name"], "members": n_members, "nx": spec["nx"], "ny": spec["ny"]},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "member-cell-steps/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "member-cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# uneven multi-level ensemble (512 x 64x128, 128 x 128x256, 32 x 256x512)
+# ---------------------------------------------------------------------------
+
+def run_multilevel(ctx, args, levels=((128, 64, 512), (256, 128, 128), (512, 256, 32)), blocks=5):
+    """All levels share one physical domain (2560 km x 1500 km) and the
+    double-jet physics with SOAR model error; every member of every level
+    advances in one persistent launch per RK2 step.  Returns the batched and
+    the member-by-member member-cell-steps/s."""
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
+    from gpuocean_gb300.SWEsimulators import CDKLM16
+    from gpuocean_gb300.SWEsimulators.OceanStateNoise import OceanStateNoise
+    from gpuocean_gb300.utils import BenchmarkCases, Common
+    Lx, Ly = 2560e3, 1500e3
+    sims = []
+    bc = Common.BoundaryConditions(1, 2, 1, 2)
+    for nx, ny, n in levels:
+        c = BenchmarkCases.double_jet_case(nx=nx, ny=ny, dx=Lx / nx, dy=Ly / ny)
+        for m in range(n):
+            s = CDKLM16.CDKLM16(ctx, c["eta0"], c["hu0"], c["hv0"], c["H"], nx, ny, c["dx"], c["dy"], 0.0, c["g"],
+                                c["f"], 0.0, coriolis_beta=c["coriolis_beta"], boundary_conditions=bc,
+                                model_time_step=MODEL_TIME_STEP)
+            s.model_error = OceanStateNoise.fromsim(s, soar_q0=soar_q0(), soar_L=NOISE_L_COARSE * c["dx"] * NOISE_FACTOR,
+                                                    interpolation_factor=NOISE_FACTOR, strict_odd_factor=False)
+            sims.append(s)
+    ens = BatchedEnsemble(sims)
+    ens.set_noise([s.model_error for s in sims], rng_seed=77)
+    ens.updateDt(courant_number=0.8)
+    for _ in range(2):
+        ens.step(MODEL_TIME_STEP, apply_stochastic_term=True)
+    ens.synchronize()
+    t0 = time.perf_counter()
+    cells = 0
+    for _ in range(blocks):
+        cells += ens.step(MODEL_TIME_STEP, apply_stochastic_term=True)
+    ens.synchronize()
+    batched = cells / (time.perf_counter() - t0)
+    ens.release()
+    # member by member: a sample of every level, stepped from Python
+    sample = [s for lv in range(len(levels)) for s in sims[sum(l[2] for l in levels[:lv]):][:8]]
+    for s in sample:
+        s.step(MODEL_TIME_STEP, apply_stochastic_term=False)
+        s.perturbState()
+    for s in sample:
+        s.gpu_stream.synchronize()
+    t0 = time.perf_counter()
+    pm = 0
+    for s in sample:
+        before = s.num_iterations
+        s.step(MODEL_TIME_STEP, apply_stochastic_term=False)
+        s.perturbState()
+        pm += (s.num_iterations - before) * int(s.nx) * int(s.ny)
+    for s in sample:
+        s.gpu_stream.synchronize()
+    per_member = pm / (time.perf_counter() - t0)
+    for s in sims:
+        s.cleanUp(do_gc=False)
+    return {"workload": "c4", "levels": [list(l) for l in levels], "members": len(sims),
+            "value": batched, "unit": "member-cell-steps/s", "blocks": blocks,
+            "per_member_baseline": per_member, "batched_over_per_member": batched / per_member,
+            "per_member_sample": len(sample)}
+
+
+# ---------------------------------------------------------------------------
+# main arm
+# ---------------------------------------------------------------------------
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c3", choices=["c3", "c1"])
+    ap.add_argument("--members", type=int, default=256)
+    ap.add_argument("--per-member-sample", type=int, default=16)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-multilevel", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    spec = workload_spec(args.workload, args.members if args.workload == "c3" else 1)
+    if args.impl == "reference":
+        run_reference(args, spec, rank, world)
+        return
+
+    from gpuocean_gb300 import _lib
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
+    from gpuocean_gb300.utils import Common
+    dist = Dist(world, "nccl" if world > 1 else "gloo")
+    ctx = Common.CUDAContext(device=local)
+    case = make_case(spec)
+    sims = build_members(ctx, spec, case)
+    ens = BatchedEnsemble(sims)
+    distinct_bathy = len(set(ens._bathy_owner))
+    noise = bool(spec.get("noise"))
+    if noise:
+        # model error drawn on the device (XORWOW) for every member, every block
+        ens.set_noise([s.model_error for s in sims], rng_seed=1000)
+    ens.updateDt(courant_number=0.8)
+    lib = _lib.load()
+    stream = ens.stream.handle
+
+    for _ in range(args.warmup):
+        ens.step(MODEL_TIME_STEP, apply_stochastic_term=noise)
+    ens.synchronize()
+
+    ev = [ctypes.c_void_p() for _ in range(2)]
+    for e in ev:
+        _lib.call("goc_event_create", ctypes.byref(e))
+    launches0 = ens.kernels_launched
+    cells = 0
+    clocks = ClockSampler(local)
+    dist.barrier()
+    ens.synchronize()
+    clocks.start()
+    wall0 = time.perf_counter()
+    _lib.call("goc_event_record", ev[0], stream)
+    for _ in range(args.steps):
+        cells += ens.step(MODEL_TIME_STEP, apply_stochastic_term=noise)
+    _lib.call("goc_event_record", ev[1], stream)
+    ens.synchronize()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    dist.barrier()
+    ms = ctypes.c_float()
+    _lib.call("goc_event_elapsed_ms", ev[0], ev[1], ctypes.byref(ms))
+    elapsed = dist.max(ms.value / 1000.0)
+    launches = ens.kernels_launched - launches0
+    value = cells * world / elapsed
+
+    # dominant kernel: per-launch CUDA-event times of the RK2 ensemble kernel
+    # on the launching stream, over a few eager blocks
+    sched = ens._schedule(MODEL_TIME_STEP)
+    n_active = [int((sched[2] > k).sum()) for k in range(sched[3])]
+    kev = [ctypes.c_void_p() for _ in range(2 * sched[3])]
+    for e in kev:
+        _lib.call("goc_event_create", ctypes.byref(e))
+    ens._sched_key = None
+    durations, bytes_k = [], []
+    for _ in range(3):
+        scheds, table, n, nsub = ens._schedule(MODEL_TIME_STEP)
+        _lib.call("goc_ensemble_set_schedule", ens._handle, table.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                  n.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), stream)
+        for k in range(nsub):
+            _lib.call("goc_event_record", kev[2 * k], stream)
+            _lib.call("goc_ensemble_rk2_substep", ens._handle, k, stream)
+            _lib.call("goc_event_record", kev[2 * k + 1], stream)
+        _lib.call("goc_ensemble_end_block", ens._handle, int(nsub), stream)
+        ens.synchronize()
+        for k in range(nsub):
+            t = ctypes.c_float()
+            _lib.call("goc_event_elapsed_ms", kev[2 * k], kev[2 * k + 1], ctypes.byref(t))
+            durations.append(t.value / 1000.0)
+            bytes_k.append(algorithmic_bytes_per_launch(sims, n_active[k], distinct_bathy))
+        for m, s in enumerate(sims):
+            for x in scheds[m]:
+                s.t += np.float64(x)
+            if len(scheds[m]) % 2:
+                s.gpu_data.swap()
+        ens._ptrs = ens._current_ptrs()
+    ens._sched_key = None
+    avg_bytes = float(np.mean(bytes_k))
+    avg_dur = float(np.mean(durations))
+    achieved = avg_bytes / avg_dur / 1e9
+    peak, peak_kind = measured_peaks()
+
+    # end to end through the public API: per block, upload from pinned host
+    # memory every member's observation position and (with model error) the
+    # block's N(0,1) draws, step, read back every member's drifter positions
+    n_d = spec["drifters"]
+    e2e = None
+    if n_d:
+        e2e_steps = max(2, args.steps // 2)
+        in_obs = 8 * len(sims)
+        rand_sizes = [int(s.model_error.rand_ny) * int(s.model_error.random_numbers.pitch) for s in sims] if noise else []
+        in_rand = sum(rand_sizes)
+        out_bytes = 8 * (n_d + 1) * len(sims)
+        host_in = ctypes.c_void_p()
+        host_out = ctypes.c_void_p()
+        _lib.call("goc_host_alloc", ctypes.byref(host_in), in_obs + e2e_steps * in_rand)
+        _lib.call("goc_host_alloc", ctypes.byref(host_out), out_bytes)
+        obs = np.ctypeslib.as_array(ctypes.cast(host_in, ctypes.POINTER(ctypes.c_float)), shape=(len(sims), 2))
+        obs[:, 0] = 0.5 * case["nx"] * case["dx"]
+        obs[:, 1] = 0.5 * case["ny"] * case["dy"]
+        pool = None
+        if noise:
+            draws = np.ctypeslib.as_array(ctypes.cast(host_in.value + in_obs, ctypes.POINTER(ctypes.c_float)),
+                                          shape=(e2e_steps * in_rand // 4,))
+            for m in range(len(sims)):
+                # member m's normals for every block: default_rng(1000 + m)
+                rng = np.random.default_rng(1000 + m)
+                off = sum(rand_sizes[:m]) // 4
+                for b in range(e2e_steps):
+                    draws[b * in_rand // 4 + off: b * in_rand // 4 + off + rand_sizes[m] // 4] = \
+                        rng.standard_normal(rand_sizes[m] // 4)
+            pool = Common.DevicePtr(in_rand)
+            ens.set_noise([s.model_error for s in sims], random_pool=pool)
+        ens.synchronize()
+        e2e_cells = 0
+        t0 = time.perf_counter()
+        for b in range(e2e_steps):
+            for m, s in enumerate(sims):
+                _lib.call("goc_memcpy_h2d_async", s.drifters.driftersDevice.ptr + 8 * n_d, host_in.value + 8 * m,
+                          8, stream)
+            if noise:
+                _lib.call("goc_memcpy_h2d_async", pool.ptr, host_in.value + in_obs + b * in_rand, in_rand, stream)
+            e2e_cells += ens.step(MODEL_TIME_STEP, apply_stochastic_term=noise)
+            for m, s in enumerate(sims):
+                _lib.call("goc_memcpy_d2h_async", host_out.value + 8 * (n_d + 1) * m, s.drifters.driftersDevice.ptr,
+                          8 * (n_d + 1), stream)
+        ens.synchronize()
+        e2e_wall = time.perf_counter() - t0
+        e2e = {"value": e2e_cells * world / dist.max(e2e_wall), "unit": "member-cell-steps/s",
+               "h2d_bytes_per_step": in_obs + in_rand, "d2h_bytes_per_step": out_bytes}
+        _lib.call("goc_host_free", host_in)
+        _lib.call("goc_host_free", host_out)
+
+    # per-member baseline: the plain simulator stepped member by member from
+    # Python, as the reference's ensembles do
+    pm_sims = sims[:max(1, min(args.per_member_sample, len(sims)))]
+    ens.synchronize()
+
+    def member_block(s):
+        # CDKLM16.dataAssimilationStep cadence: a block of steps, then the model error
+        s.step(MODEL_TIME_STEP, apply_stochastic_term=False)
+        if noise:
+            s.perturbState()
+
+    for s in pm_sims:
+        member_block(s)
+    for s in pm_sims:
+        s.gpu_stream.synchronize()
+    t0 = time.perf_counter()
+    pm_cells = 0
+    for s in pm_sims:
+        before = s.num_iterations
+        member_block(s)
+        pm_cells += (s.num_iterations - before) * int(s.nx) * int(s.ny)
+    for s in pm_sims:
+        s.gpu_stream.synchronize()
+    per_member_rate = pm_cells / (time.perf_counter() - t0)
+
+    multilevel = None if args.no_multilevel else run_multilevel(ctx, args)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        n_cpu_members = 2
+        rate, wall_cpu = cpu_reference_rate(spec, n_cpu_members, 1, 1)
+        cpu = {"value": rate, "unit": "member-cell-steps/s", "cores": 1, "kind": "port",
+               "sample": f"{n_cpu_members} members x 1 block of {MODEL_TIME_STEP:.0f} s ({wall_cpu:.1f} s), FP64 NumPy "
+                         f"restatement of the reference step on one core"}
+
+    if rank == 0:
+        line = {
+            "metric": "member-cell-steps/s", "value": value, "unit": "member-cell-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": spec["name"], "members": len(sims), "nx": spec["nx"], "ny": spec["ny"],
+                       "drifters_per_member": n_d, "block_seconds": MODEL_TIME_STEP,
+                       "model_error": (f"SOAR every {MODEL_TIME_STEP:.0f} s, coarse factor {NOISE_FACTOR}, "
+                                       f"L={NOISE_L_COARSE:g} coarse cells, std {NOISE_STD} m") if noise else None,
+                       "substeps_per_block": int(sched[3]), "l2": "inputs larger than L2"
+                       if 24 * sum(int(s.nx) * int(s.ny) for s in sims) > 129e6 else "inputs smaller than L2",
+                       "parallelism": f"replicas x{world}"},
+            "per_member_baseline": {"value": per_member_rate, "unit": "member-cell-steps/s",
+                                    "members_sampled": len(pm_sims),
+                                    "batched_over_per_member": value / world / per_member_rate},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": "ensemble_rk2_kernel",
+                         "peak_kind": peak_kind, "avg_launch_ms": 1000.0 * avg_dur,
+                         "algorithmic_bytes_per_launch": avg_bytes},
+            "e2e": e2e, "gpu_launches": launches, "clocks": clk, "cpu_baseline": cpu,
+            "multilevel": multilevel,
+            "wall_s": wall,
+        }
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

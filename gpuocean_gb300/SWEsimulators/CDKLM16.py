@@ -121,6 +121,13 @@ class CDKLM16(Simulator):
         if angle.size != 1:
             raise NotImplementedError("only a constant north angle is supported by the GB300 step kernel")
         self.angle_arr = Common.CUDAArray2D(self.gpu_stream, angle.shape[1], angle.shape[0], 0, 0, angle)
+        # a spatially varying texture is evaluated once per cell centre
+        self.coriolis_cell = None
+        if coriolis_f.size > 1:
+            self.coriolis_cell = Common.CUDAArray2D(self.gpu_stream, nx, ny, 2, 2,
+                                                    np.zeros((ny + 4, nx + 4), dtype=np.float32))
+            _lib.call("goc_cell_texture", self.coriolis_f_arr.ptr, int(coriolis_f.shape[1]), int(coriolis_f.shape[0]),
+                      int(nx), int(ny), self.coriolis_cell.ptr, int(self.coriolis_cell.pitch), self.gpu_stream.handle)
 
         self.rho_o = np.float32(rho_o)
         self.wind_stress_factor = np.float32(wind_stress_factor)
@@ -179,6 +186,8 @@ class CDKLM16(Simulator):
         p.land_value = float(self.bathymetry.mask_value)
         p.coriolis_f = self.coriolis_f_arr.ptr
         p.coriolis_nx, p.coriolis_ny = self.coriolis_f_arr.nx_halo, self.coriolis_f_arr.ny_halo
+        if self.coriolis_cell is not None:
+            p.coriolis_cell, p.coriolis_cell_pitch = self.coriolis_cell.ptr, int(self.coriolis_cell.pitch)
         p.angle = self.angle_arr.ptr
         p.angle_nx, p.angle_ny = self.angle_arr.nx_halo, self.angle_arr.ny_halo
         p.wind_x_cur, p.wind_x_next = self.wind_stress_x_current_arr.ptr, self.wind_stress_x_next_arr.ptr
@@ -204,6 +213,8 @@ class CDKLM16(Simulator):
         self.bathymetry.release()
         self.device_dt.free()
         self.max_dt_buffer.free()
+        if self.coriolis_cell is not None:
+            self.coriolis_cell.release()
         for a in (self.coriolis_f_arr, self.angle_arr, self.wind_stress_x_current_arr, self.wind_stress_y_current_arr,
                   self.wind_stress_x_next_arr, self.wind_stress_y_next_arr, self.atmospheric_pressure_current_arr,
                   self.atmospheric_pressure_next_arr):
@@ -220,14 +231,16 @@ class CDKLM16(Simulator):
         _lib.call("goc_cdklm_stage", ctypes.byref(self._params), ctypes.c_float(dt), int(rk_step),
                   src[0].ptr, src[1].ptr, src[2].ptr, dst[0].ptr, dst[1].ptr, dst[2].ptr,
                   a[0].ptr if alt else None, a[1].ptr if alt else None, a[2].ptr if alt else None,
-                  int(d.h0.pitch), self.bathymetry.Bi.ptr, int(self.bathymetry.Bi.pitch), self.stream_handle)
+                  int(d.h0.pitch), self.bathymetry.Bi.ptr, int(self.bathymetry.Bi.pitch),
+                  self.bathymetry.Bm.ptr, int(self.bathymetry.Bm.pitch), self.stream_handle)
 
     def _rk_step(self, local_dt):
         d = self.gpu_data
         if self.rk_order == 2:
             _lib.call("goc_cdklm_rk2_step", ctypes.byref(self._params), ctypes.c_float(local_dt),
                       d.h0.ptr, d.hu0.ptr, d.hv0.ptr, d.h1.ptr, d.hu1.ptr, d.hv1.ptr, int(d.h0.pitch),
-                      self.bathymetry.Bi.ptr, int(self.bathymetry.Bi.pitch), self.stream_handle)
+                      self.bathymetry.Bi.ptr, int(self.bathymetry.Bi.pitch),
+                      self.bathymetry.Bm.ptr, int(self.bathymetry.Bm.pitch), self.stream_handle)
             d.swap()
         elif self.rk_order == 1:
             self._stage((d.h0, d.hu0, d.hv0), (d.h1, d.hu1, d.hv1), local_dt, 0)

@@ -30,6 +30,7 @@ class GocCdklmParams(ctypes.Structure):
         ("bc_south", ctypes.c_int32), ("bc_west", ctypes.c_int32),
         ("land_value", c_float),
         ("coriolis_f", c_void_p), ("coriolis_nx", ctypes.c_int32), ("coriolis_ny", ctypes.c_int32),
+        ("coriolis_cell", c_void_p), ("coriolis_cell_pitch", ctypes.c_int32),
         ("angle", c_void_p), ("angle_nx", ctypes.c_int32), ("angle_ny", ctypes.c_int32),
         ("wind_x_cur", c_void_p), ("wind_x_next", c_void_p),
         ("wind_x_nx", ctypes.c_int32), ("wind_x_ny", ctypes.c_int32),
@@ -71,16 +72,42 @@ SIGNATURES = {
     "goc_kernel_launch_count": (c_i64, []),
     "goc_cdklm_rk2_step": (c_int, [ctypes.POINTER(GocCdklmParams), c_float,
                                    c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
-                                   c_void_p, c_int, c_void_p]),
+                                   c_void_p, c_int, c_void_p, c_int, c_void_p]),
     "goc_cdklm_stage": (c_int, [ctypes.POINTER(GocCdklmParams), c_float, c_int,
                                 c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
-                                c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p]),
+                                c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_int, c_void_p]),
+    "goc_cell_texture": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p]),
     "goc_periodic_ghosts": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     "goc_bathymetry_init": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_float,
                                     c_void_p, c_int, c_void_p, c_int, c_void_p]),
     "goc_max_dt_partials": (c_int, [c_int, c_int]),
     "goc_max_dt": (c_int, [c_int, c_int, c_float, c_float, c_float, c_void_p, c_void_p, c_void_p, c_int,
                            c_void_p, c_int, c_float, c_void_p, c_int, c_void_p, c_void_p]),
+    "goc_drift": (c_int, [c_int, c_int, c_float, c_float, c_float, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int,
+                          c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_float,
+                          c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_float, c_float, c_void_p]),
+    "goc_drift_enforce_boundary": (c_int, [c_float, c_float, c_int, c_int, c_int, c_void_p, c_int, c_void_p]),
+    "goc_ensemble_create": (c_int, [c_void_p, c_int, c_int, ctypes.POINTER(c_void_p)]),
+    "goc_ensemble_destroy": (c_int, [c_void_p]),
+    "goc_ensemble_size": (c_int, [c_void_p, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
+    "goc_ensemble_set_schedule": (c_int, [c_void_p, c_fp, ctypes.POINTER(c_int), c_void_p]),
+    "goc_ensemble_rk2_substep": (c_int, [c_void_p, c_int, c_void_p]),
+    "goc_ensemble_end_block": (c_int, [c_void_p, c_int, c_void_p]),
+    "goc_ensemble_get_member": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
+    "goc_ensemble_max_dt": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "goc_ensemble_set_drifters": (c_int, [c_void_p, c_void_p, ctypes.POINTER(c_int), c_float, c_void_p]),
+    "goc_lcg_fill": (c_int, [c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_int, c_void_p]),
+    "goc_xorwow_state_bytes": (c_size_t, [c_int]),
+    "goc_xorwow_init": (c_int, [c_void_p, c_int, ctypes.c_ulonglong, c_void_p]),
+    "goc_xorwow_normal": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, c_void_p]),
+    "goc_soar": (c_int, [c_void_p, c_float, c_int, c_void_p]),
+    "goc_perturb_ocean": (c_int, [c_void_p, c_int, c_int, c_float, c_float, c_void_p, c_void_p, c_void_p, c_int,
+                                  c_void_p, c_int, c_float, c_int, c_void_p]),
+    "goc_noise_batch_create": (c_int, [c_void_p, c_void_p, ctypes.POINTER(c_void_p)]),
+    "goc_noise_batch_destroy": (c_int, [c_void_p]),
+    "goc_noise_batch_perturb": (c_int, [c_void_p, c_void_p, c_float, c_int, c_void_p]),
+    "goc_noise_batch_seed": (c_int, [c_void_p, ctypes.c_ulonglong, c_void_p]),
+    "goc_noise_batch_generate": (c_int, [c_void_p, c_void_p, c_int, c_void_p]),
 }
 
 _lib = None

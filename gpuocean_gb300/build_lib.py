@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
           "--expt-relaxed-constexpr", "-ftz=true", "-prec-div=false", "-prec-sqrt=false"]
 # per-file extra flags
-EXTRA = {}
+EXTRA = {"noise.cu": ["-use_fast_math"]}
 
 
 def nvcc_path() -> str:

@@ -1,0 +1,757 @@
+// CDKLM16 step kernels for sm_103a.
+//
+// One CTA owns an output tile of TX x TY interior cells and stages a halo of
+// 2 cells per Runge-Kutta stage in shared memory:
+//   * the fused RK2 kernel (NSTAGE = 2) loads Q^n on the tile + 4 cells,
+//     recomputes the first stage on the tile + 2 cells (including the periodic
+//     ghost images and the mirrored wall ghosts), then the second stage on the
+//     tile, and writes Q^{n+1} (+ periodic ghost images) once.  One launch
+//     replaces two step launches and two periodic boundary launches per step
+//     (S/CDKLM16.py:519-572).
+//   * the single-stage kernel (NSTAGE = 1) evaluates one stage with the
+//     reference's buffer semantics (K/CDKLM16_kernel.cu:475-1090).
+// Every face flux is evaluated once per stage and shared by the two cells
+// beside it (the reference evaluates each face twice).
+//
+// The per-cell arithmetic follows the reference kernel:
+//   desingularisation          K/CDKLM16_kernel.cu:614-656, K/common.cu:664-666
+//   x slopes + Kx + wall fixes :673-737, adjustSlopes_x :160-203
+//   x face flux                computeFFaceFlux :260-340, CDKLM16_flux :104-151
+//   y slopes + Ly              :779-842, adjustSlopes_y :211-254
+//   y face flux                computeGFaceFlux :346-416
+//   sources, friction, RK      :874-1089
+// Constant divisions of the reference (/(2g), /DX, /DY, /(ap-am)) are
+// multiplications by precomputed reciprocals here.
+#pragma once
+
+#include "common.cuh"
+
+namespace goc {
+
+// Per-launch constants derived on the host.
+struct StepConst {
+    float inv_dx, inv_dy, inv_2g;
+    float half_g, two_g;
+    float theta_g;        // theta * g
+    float Vc, Uc;         // dx/(2g), dy/(2g)
+    float inv_atm_x, inv_atm_y;  // 1/(2 dx rho), 1/(2 dy rho)
+    int periodic_x, periodic_y;
+};
+
+template <int W, int H>
+struct TileSmem {
+    float D[3][H][W];    // (eta, u, v) after desingularisation
+    float Hmb[H][W];     // cell mean depth (initBm semantics)
+    float Fc[H][W];      // Coriolis f per cell
+    float Sx[3][H][W];   // u_x, v_x, dx*Kx at each cell
+    float Sy[3][H][W];   // u_y, v_y, dy*Ly at each cell
+    float Fx[3][H][W];   // flux through the east face of each cell
+    float Gy[3][H][W];   // flux through the north face of each cell
+    float Hi[H + 1][W + 1];  // corner depths, land -> kDryFlag
+};
+
+__device__ __forceinline__ float minmod_raw(float b, float c, float f) {
+    const float sb = copysignf(1.0f, b), sc = copysignf(1.0f, c), sf = copysignf(1.0f, f);
+    return 0.25f * sb * (sb + sc) * (sc + sf) * fminf(fminf(fabsf(b), fabsf(c)), fabsf(f));
+}
+
+__device__ __forceinline__ float minmod_slope(float l, float c, float r, float theta) {
+    return minmod_raw((c - l) * theta, (r - l) * 0.5f, (r - c) * theta);
+}
+
+// K/common.cu:664-666.  The reference's literal 0.5*eps is a double.
+__device__ __forceinline__ float desing(float h, float hu, float eps) {
+    const float a = (float)((double)(h * h / (2.0f * eps)) + 0.5 * (double)eps);
+    return hu / fmaxf(fminf(a, eps), fabsf(h));
+}
+
+// Desingularised (eta, u, v) of a raw state, K/CDKLM16_kernel.cu:614-656.
+__device__ __forceinline__ void desingularize_cell(const GocCdklmParams& p, float eta, float hu, float hv,
+                                                   float Hm, float& oe, float& ou, float& ov) {
+    const float h = eta + Hm;
+    if (fabsf(Hm - p.land_value) <= kDryEps) {
+        oe = kDryFlag; ou = 0.0f; ov = 0.0f;
+    } else if (h < p.desing_eps) {
+        if (h <= p.depth_cutoff) {
+            oe = -Hm + p.depth_cutoff; ou = 0.0f; ov = 0.0f;
+        } else {
+            oe = eta;
+            ou = desing(h, hu, p.desing_eps);
+            ov = desing(h, hv, p.desing_eps);
+        }
+    } else {
+        const float ih = 1.0f / h;
+        oe = eta; ou = hu * ih; ov = hv * ih;
+    }
+}
+
+// Central-upwind flux with the flux balancer, K/CDKLM16_kernel.cu:82-151.
+// Q = (eta, u_normal, v_transverse).
+__device__ __forceinline__ void cdklm_flux(const GocCdklmParams& p, const StepConst& k,
+                                           float em, float um_, float vm_, float ep, float up_, float vp_,
+                                           float H, float& F0, float& F1, float& F2) {
+    const float hp = ep + H;
+    const float hm = em + H;
+    float Fp0 = 0.f, Fp1 = 0.f, Fp2 = 0.f, up = 0.f, cp = 0.f;
+    if (hp > p.depth_cutoff) {
+        Fp0 = hp * up_;
+        Fp1 = hp * up_ * up_ + k.half_g * hp * hp;
+        Fp2 = hp * up_ * vp_;
+        up = up_;
+        cp = sqrtf(p.g * hp);
+    }
+    float Fm0 = 0.f, Fm1 = 0.f, Fm2 = 0.f, um = 0.f, cm = 0.f;
+    if (hm > p.depth_cutoff) {
+        Fm0 = hm * um_;
+        Fm1 = hm * um_ * um_ + k.half_g * hm * hm;
+        Fm2 = hm * um_ * vm_;
+        um = um_;
+        cm = sqrtf(p.g * hm);
+    }
+    const float am = fminf(fminf(um - cm, up - cp), 0.0f);
+    const float ap = fmaxf(fmaxf(um + cm, up + cp), 0.0f);
+    if (fabsf(ap - am) < p.flux_slope_eps) {
+        F0 = 0.f; F1 = 0.f; F2 = 0.f;
+        return;
+    }
+    const float inv = 1.0f / (ap - am);
+    const float apam = ap * am;
+    F0 = ((ap * Fm0 - am * Fp0) + apam * (ep - em)) * inv;
+    F1 = ((ap * Fm1 - am * Fp1) + apam * (Fp0 - Fm0)) * inv;
+    const float fb = p.flux_balancer;
+    float f2 = (um_ > -up_) ? fb * Fm2 : fb * Fp2;
+    f2 += (1.0f - fb) * (((ap * Fm2 - am * Fp2) + apam * (hp * vp_ - hm * vm_)) * inv);
+    F2 = f2;
+}
+
+template <int W, int H, int NT, bool BORDER>
+struct Tile {
+    TileSmem<W, H>& S;
+    const GocCdklmParams& p;
+    const StepConst& k;
+    int x0, y0;               // global cell of local (0,0)
+    float nX, nY;             // north vector (constant angle)
+    float f0;                 // Coriolis f of a 1x1 texture
+    float wind_X, wind_Y;     // scaled wind stress of 1x1 textures
+
+    __device__ float F(int j, int i, bool const_f) const { return const_f ? f0 : S.Fc[j][i]; }
+
+    // x slopes on [ux0-1, ux1+1) x [uy0, uy1) and y slopes on
+    // [ux0, ux1) x [uy0-1, uy1+1)
+    template <int UX0, int UX1, int UY0, int UY1, bool CONST_F>
+    __device__ void slopes() {
+        constexpr int NXS = UX1 - UX0 + 2, NYS = UY1 - UY0;
+        const float th = p.theta;
+        for (int idx = threadIdx.x; idx < NXS * NYS; idx += NT) {
+            const int i = UX0 - 1 + idx % NXS;
+            const int j = UY0 + idx / NXS;
+            const int gx = x0 + i;
+            const float eL = S.D[0][j][i - 1], eC = S.D[0][j][i], eR = S.D[0][j][i + 1];
+            const float uL = S.D[1][j][i - 1], uC = S.D[1][j][i], uR = S.D[1][j][i + 1];
+            const float vL = S.D[2][j][i - 1], vC = S.D[2][j][i], vR = S.D[2][j][i + 1];
+            S.Sx[0][j][i] = minmod_slope(uL, uC, uR, th);
+            S.Sx[1][j][i] = minmod_slope(vL, vC, vR, th);
+            float lv = vL, cv = vC, rv = vR;
+            if (BORDER) {
+                if (p.bc_west == 1) { if (gx < 3) lv = -lv; if (gx < 2) cv = -cv; }
+                if (p.bc_east == 1) { if (gx > p.nx) rv = -rv; if (gx > p.nx + 1) cv = -cv; }
+            }
+            const float fL = F(j, i - 1, CONST_F), fC = F(j, i, CONST_F), fR = F(j, i + 1, CONST_F);
+            const float lfv = (nX * uL + nY * lv) * fL;
+            const float cfv = (nX * uC + nY * cv) * fC;
+            const float rfv = (nX * uR + nY * rv) * fR;
+            const float back = k.theta_g * (eC - eL - k.Vc * (cfv + lfv));
+            const float cent = k.half_g * (eR - eL - k.Vc * (rfv + 2.0f * cfv + lfv));
+            const float fwd = k.theta_g * (eR - eC - k.Vc * (cfv + rfv));
+            float Kx = minmod_raw(back, cent, fwd);
+            float va = vC;
+            if (BORDER) {
+                if (p.bc_west == 1 && gx < 2) va = -va;
+                if (p.bc_east == 1 && gx > p.nx + 2) va = -va;
+            }
+            const float dxfv = p.dx * fC * va;
+            const float Hw = 0.5f * (S.Hi[j][i] + S.Hi[j + 1][i]);
+            const float He = 0.5f * (S.Hi[j][i + 1] + S.Hi[j + 1][i + 1]);
+            const float t = (Kx + dxfv) * k.inv_2g;
+            const float hw = eC + Hw - t;
+            const float he = eC + He + t;
+            Kx = (hw > 0.0f) ? Kx : -dxfv + k.two_g * (eC + Hw);
+            Kx = (he > 0.0f) ? Kx : -dxfv - k.two_g * (eC + He);
+            S.Sx[2][j][i] = Kx;
+        }
+        constexpr int NXY = UX1 - UX0, NYY = UY1 - UY0 + 2;
+        const float eX = nY, eY = -nX;  // east vector
+        for (int idx = threadIdx.x; idx < NXY * NYY; idx += NT) {
+            const int i = UX0 + idx % NXY;
+            const int j = UY0 - 1 + idx / NXY;
+            const int gy = y0 + j;
+            const float eL = S.D[0][j - 1][i], eC = S.D[0][j][i], eU = S.D[0][j + 1][i];
+            const float uL = S.D[1][j - 1][i], uC = S.D[1][j][i], uU = S.D[1][j + 1][i];
+            const float vL = S.D[2][j - 1][i], vC = S.D[2][j][i], vU = S.D[2][j + 1][i];
+            S.Sy[0][j][i] = minmod_slope(uL, uC, uU, th);
+            S.Sy[1][j][i] = minmod_slope(vL, vC, vU, th);
+            float lu = uL, cu = uC, uu = uU;
+            if (BORDER) {
+                if (p.bc_south == 1) { if (gy < 3) lu = -lu; if (gy < 2) cu = -cu; }
+                if (p.bc_north == 1) { if (gy > p.ny) uu = -uu; if (gy > p.ny + 1) cu = -cu; }
+            }
+            const float fL = F(j - 1, i, CONST_F), fC = F(j, i, CONST_F), fU = F(j + 1, i, CONST_F);
+            const float lfu = (eX * lu + eY * vL) * fL;
+            const float cfu = (eX * cu + eY * vC) * fC;
+            const float ufu = (eX * uu + eY * vU) * fU;
+            const float back = k.theta_g * (eC - eL + k.Uc * (cfu + lfu));
+            const float cent = k.half_g * (eU - eL + k.Uc * (ufu + 2.0f * cfu + lfu));
+            const float fwd = k.theta_g * (eU - eC + k.Uc * (cfu + ufu));
+            float Ly = minmod_raw(back, cent, fwd);
+            float ua = uC;
+            if (BORDER) {
+                if (p.bc_south == 1 && gy < 2) ua = -ua;
+                if (p.bc_north == 1 && gy > p.ny + 2) ua = -ua;
+            }
+            const float dyfu = p.dy * fC * ua;
+            const float Hs = 0.5f * (S.Hi[j][i] + S.Hi[j][i + 1]);
+            const float Hn = 0.5f * (S.Hi[j + 1][i] + S.Hi[j + 1][i + 1]);
+            const float t = (Ly - dyfu) * k.inv_2g;
+            const float hs = eC + Hs - t;
+            const float hn = eC + Hn + t;
+            Ly = (hs > 0.0f) ? Ly : dyfu + k.two_g * (eC + Hs);
+            Ly = (hn > 0.0f) ? Ly : dyfu - k.two_g * (eC + Hn);
+            S.Sy[2][j][i] = Ly;
+        }
+    }
+
+    // east faces of cells [ux0-1, ux1) x [uy0, uy1); north faces of cells
+    // [ux0, ux1) x [uy0-1, uy1)
+    template <int UX0, int UX1, int UY0, int UY1, bool CONST_F>
+    __device__ void faces() {
+        constexpr int NXF = UX1 - UX0 + 1, NYF = UY1 - UY0;
+        for (int idx = threadIdx.x; idx < NXF * NYF; idx += NT) {
+            const int i = UX0 - 1 + idx % NXF;
+            const int j = UY0 + idx / NXF;
+            const int gxp = x0 + i + 1;  // global column of the plus cell
+            const float ebm = S.D[0][j][i], ebp = S.D[0][j][i + 1];
+            float F0 = 0.f, F1 = 0.f, F2 = 0.f;
+            const bool dm = (ebm == kDryFlag), dp = (ebp == kDryFlag);
+            if (!(dm && dp)) {
+                const float um = S.D[1][j][i], up = S.D[1][j][i + 1];
+                float vm = S.D[2][j][i], vp = S.D[2][j][i + 1];
+                const float Rpx = up - 0.5f * S.Sx[0][j][i + 1];
+                const float Rpy = vp - 0.5f * S.Sx[1][j][i + 1];
+                const float Rmx = um + 0.5f * S.Sx[0][j][i];
+                const float Rmy = vm + 0.5f * S.Sx[1][j][i];
+                const float Hf = 0.5f * (S.Hi[j][i + 1] + S.Hi[j + 1][i + 1]);
+                if (BORDER) {
+                    if (p.bc_west == 1 && gxp == 2) vm = -vm;
+                    if (p.bc_east == 1 && gxp == p.nx + 2) vp = -vp;
+                }
+                const float vpn = up * nX + vp * nY;
+                const float vmn = um * nX + vm * nY;
+                const float etap = fmaxf(-Hf, ebp - (S.Sx[2][j][i + 1] + p.dx * F(j, i + 1, CONST_F) * vpn) * k.inv_2g);
+                const float etam = fmaxf(-Hf, ebm + (S.Sx[2][j][i] + p.dx * F(j, i, CONST_F) * vmn) * k.inv_2g);
+                if (dm) {
+                    F1 = k.half_g * (etap + Hf) * (etap + Hf);
+                } else if (dp) {
+                    F1 = k.half_g * (etam + Hf) * (etam + Hf);
+                } else {
+                    cdklm_flux(p, k, etam, Rmx, Rmy, etap, Rpx, Rpy, Hf, F0, F1, F2);
+                }
+            }
+            S.Fx[0][j][i] = F0; S.Fx[1][j][i] = F1; S.Fx[2][j][i] = F2;
+        }
+        constexpr int NXG = UX1 - UX0, NYG = UY1 - UY0 + 1;
+        const float eX = nY, eY = -nX;
+        for (int idx = threadIdx.x; idx < NXG * NYG; idx += NT) {
+            const int i = UX0 + idx % NXG;
+            const int j = UY0 - 1 + idx / NXG;
+            const int gyp = y0 + j + 1;
+            const float ebm = S.D[0][j][i], ebp = S.D[0][j + 1][i];
+            float G0 = 0.f, G1 = 0.f, G2 = 0.f;
+            const bool dm = (ebm == kDryFlag), dp = (ebp == kDryFlag);
+            if (!(dm && dp)) {
+                float um = S.D[1][j][i], up = S.D[1][j + 1][i];
+                const float vm = S.D[2][j][i], vp = S.D[2][j + 1][i];
+                const float Rpx = up - 0.5f * S.Sy[0][j + 1][i];
+                const float Rpy = vp - 0.5f * S.Sy[1][j + 1][i];
+                const float Rmx = um + 0.5f * S.Sy[0][j][i];
+                const float Rmy = vm + 0.5f * S.Sy[1][j][i];
+                const float Hf = 0.5f * (S.Hi[j + 1][i] + S.Hi[j + 1][i + 1]);
+                if (BORDER) {
+                    if (p.bc_south == 1 && gyp == 2) um = -um;
+                    if (p.bc_north == 1 && gyp == p.ny + 2) up = -up;
+                }
+                const float upe = up * eX + vp * eY;
+                const float ume = um * eX + vm * eY;
+                const float etap = fmaxf(-Hf, ebp - (S.Sy[2][j + 1][i] - p.dy * F(j + 1, i, CONST_F) * upe) * k.inv_2g);
+                const float etam = fmaxf(-Hf, ebm + (S.Sy[2][j][i] - p.dy * F(j, i, CONST_F) * ume) * k.inv_2g);
+                if (dm) {
+                    G2 = k.half_g * (etap + Hf) * (etap + Hf);
+                } else if (dp) {
+                    G2 = k.half_g * (etam + Hf) * (etam + Hf);
+                } else {
+                    // u and v swap roles along y
+                    float a0, a1, a2;
+                    cdklm_flux(p, k, etam, Rmy, Rmx, etap, Rpy, Rpx, Hf, a0, a1, a2);
+                    G0 = a0; G1 = a2; G2 = a1;
+                }
+            }
+            S.Gy[0][j][i] = G0; S.Gy[1][j][i] = G1; S.Gy[2][j][i] = G2;
+        }
+    }
+
+    // Right-hand side L(Q) of the cell (i,j) plus the quantities the RK
+    // combination needs; K/CDKLM16_kernel.cu:739-966.
+    template <bool CONST_F, bool SIMPLE_FORCING>
+    __device__ void rhs(int i, int j, int gxs, int gys, float& L1, float& L2, float& L3,
+                        float& ec, float& hu, float& hv, float& Hm, float& hsum) const {
+        ec = S.D[0][j][i];
+        const float uc = S.D[1][j][i], vc = S.D[2][j][i];
+        Hm = 0.25f * (S.Hi[j][i] + S.Hi[j + 1][i] + S.Hi[j][i + 1] + S.Hi[j + 1][i + 1]);
+        hsum = ec + Hm;
+        hu = 0.0f; hv = 0.0f;
+        if (hsum > p.depth_cutoff) { hu = uc * hsum; hv = vc * hsum; }
+        const float fc = F(j, i, CONST_F);
+        float fd0 = (S.Fx[0][j][i] - S.Fx[0][j][i - 1]) * k.inv_dx;
+        float fd1 = (S.Fx[1][j][i] - S.Fx[1][j][i - 1]) * k.inv_dx;
+        float fd2 = (S.Fx[2][j][i] - S.Fx[2][j][i - 1]) * k.inv_dx;
+        if (!p.one_dimensional) {
+            fd0 = fd0 + (S.Gy[0][j][i] - S.Gy[0][j - 1][i]) * k.inv_dy;
+            fd1 = fd1 + (S.Gy[1][j][i] - S.Gy[1][j - 1][i]) * k.inv_dy;
+            fd2 = fd2 + (S.Gy[2][j][i] - S.Gy[2][j - 1][i]) * k.inv_dy;
+        }
+        float st1 = 0.0f, st2 = 0.0f;
+        if (hsum >= p.depth_cutoff && ec != kDryFlag) {
+            const float tx = (S.Sx[2][j][i] + p.dx * fc * vc) * k.inv_2g;
+            const float ty = (S.Sy[2][j][i] - p.dy * fc * uc) * k.inv_2g;
+            const float eta_we = 0.5f * ((ec - tx) + (ec + tx));
+            const float eta_sn = 0.5f * ((ec + ty) + (ec - ty));
+            const float RHxp = 0.5f * (S.Hi[j][i + 1] + S.Hi[j + 1][i + 1]);
+            const float RHxm = 0.5f * (S.Hi[j][i] + S.Hi[j + 1][i]);
+            const float RHyp = 0.5f * (S.Hi[j + 1][i] + S.Hi[j + 1][i + 1]);
+            const float RHym = 0.5f * (S.Hi[j][i] + S.Hi[j][i + 1]);
+            const float eX = nY, eY = -nX;
+            const float hu_e = hu * eX + hv * eY;
+            const float hv_n = hu * nX + hv * nY;
+            const float hu_ec = fc * hv_n;
+            const float hv_nc = -fc * hu_e;
+            const float upx = -nX, upy = nY;
+            const float hu_cor = upy * hu_ec + (-upx) * hv_nc;
+            const float hv_cor = upx * hu_ec + upy * hv_nc;
+            float X, Y, ax = 0.0f, ay = 0.0f;
+            if (SIMPLE_FORCING) {
+                X = wind_X; Y = wind_Y;
+            } else {
+                const float s = ((float)gxs + 0.5f) / (float)(p.nx + 4);
+                const float t = ((float)gys + 0.5f) / (float)(p.ny + 4);
+                const float wxc = tex_bilinear(p.wind_x_cur, p.wind_x_nx, p.wind_x_ny, s, t);
+                const float wxn = tex_bilinear(p.wind_x_next, p.wind_x_nx, p.wind_x_ny, s, t);
+                const float wyc = tex_bilinear(p.wind_y_cur, p.wind_y_nx, p.wind_y_ny, s, t);
+                const float wyn = tex_bilinear(p.wind_y_next, p.wind_y_nx, p.wind_y_ny, s, t);
+                X = p.wind_stress_factor * (p.wind_t * wxn + (1.0f - p.wind_t) * wxc);
+                Y = p.wind_stress_factor * (p.wind_t * wyn + (1.0f - p.wind_t) * wyc);
+                if (p.atm_p_nx * p.atm_p_ny > 1) {
+                    const float dxn = 1.0f / (float)(p.nx + 4), dyn = 1.0f / (float)(p.ny + 4);
+                    const float pt = p.atm_p_t;
+                    auto P = [&](float ss, float tt) {
+                        const float c = tex_bilinear(p.atm_p_cur, p.atm_p_nx, p.atm_p_ny, ss, tt);
+                        const float n = tex_bilinear(p.atm_p_next, p.atm_p_nx, p.atm_p_ny, ss, tt);
+                        return pt * n + (1.0f - pt) * c;
+                    };
+                    const float pe = P(s + dxn, t), pw = P(s - dxn, t);
+                    const float pn = P(s, t + dyn), ps = P(s, t - dyn);
+                    ax = -(pe - pw) * hsum * k.inv_atm_x;
+                    ay = -(pn - ps) * hsum * k.inv_atm_y;
+                }
+            }
+            const float bath1 = p.g * (eta_we + Hm) * (RHxp - RHxm);
+            const float bath2 = p.g * (eta_sn + Hm) * (RHyp - RHym);
+            st1 = X + hu_cor + ax + bath1 * k.inv_dx;
+            st2 = Y + hv_cor + ay + bath2 * k.inv_dy;
+        }
+        L1 = -fd0;
+        L2 = -fd1 + st1;
+        L3 = -fd2 + st2;
+    }
+
+    // Semi-implicit friction coefficient C (K/CDKLM16_kernel.cu:971-983).
+    __device__ float friction(float dt, float hsum, float hu, float hv) const {
+        if (!(p.r > 0.0f) || p.rk_order >= 3) return 0.0f;
+        if (hsum < p.desing_eps) {
+            const float u = desing(hsum, hu, p.desing_eps);
+            const float v = desing(hsum, hv, p.desing_eps);
+            return dt * p.r * desing(hsum, sqrtf(u * u + v * v), p.desing_eps);
+        }
+        const float u = hu / hsum, v = hv / hsum;
+        return dt * p.r * sqrtf(u * u + v * v) / hsum;
+    }
+};
+
+// Final clamp of an updated state (K/CDKLM16_kernel.cu:1069-1088).
+__device__ __forceinline__ void finish_cell(const GocCdklmParams& p, float Hm, float& e, float& hu, float& hv) {
+    if (e + Hm <= p.depth_cutoff) {
+        e = -Hm + p.depth_cutoff; hu = 0.0f; hv = 0.0f;
+    }
+    e = fmaxf(-Hm + p.depth_cutoff, e);
+}
+
+__device__ __forceinline__ void store_with_images(const GocCdklmParams& p, const StepConst& k, float* e_out,
+                                                  float* hu_out, float* hv_out, int pitch, int gx, int gy,
+                                                  float e, float hu, float hv) {
+    int xs[2] = {gx, -1}, ys[2] = {gy, -1};
+    if (k.periodic_x) {
+        if (gx < 4) xs[1] = gx + p.nx;
+        else if (gx >= p.nx) xs[1] = gx - p.nx;
+    }
+    if (k.periodic_y) {
+        if (gy < 4) ys[1] = gy + p.ny;
+        else if (gy >= p.ny) ys[1] = gy - p.ny;
+    }
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        if (ys[a] < 0) continue;
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            if (xs[b] < 0) continue;
+            const size_t o = (size_t)ys[a] * pitch + xs[b];
+            e_out[o] = e; hu_out[o] = hu; hv_out[o] = hv;
+        }
+    }
+}
+
+// Launch constants of a parameter set.
+// IEEE division on host and device alike, so that launch constants do not
+// depend on where they were derived (device code is built with
+// -prec-div=false).
+__host__ __device__ inline float exact_div(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fdiv_rn(a, b);
+#else
+    return a / b;
+#endif
+}
+
+__host__ __device__ inline StepConst make_step_const(const GocCdklmParams& p) {
+    StepConst k;
+    k.inv_dx = exact_div(1.0f, p.dx);
+    k.inv_dy = exact_div(1.0f, p.dy);
+    k.inv_2g = exact_div(1.0f, 2.0f * p.g);
+    k.half_g = 0.5f * p.g;
+    k.two_g = 2.0f * p.g;
+    k.theta_g = p.theta * p.g;
+    k.Vc = exact_div(p.dx, 2.0f * p.g);
+    k.Uc = exact_div(p.dy, 2.0f * p.g);
+    k.inv_atm_x = exact_div(1.0f, 2.0f * p.dx * p.rho_o);
+    k.inv_atm_y = exact_div(1.0f, 2.0f * p.dy * p.rho_o);
+    k.periodic_x = (p.bc_east == 2);
+    k.periodic_y = (p.bc_north == 2);
+    return k;
+}
+
+// One output tile (tile_x, tile_y) of one stage (NSTAGE = 1) or of a full
+// fused RK2 step (NSTAGE = 2).  Called by the single-simulator kernel and by
+// the persistent ensemble kernel; the caller synchronises the block before
+// the shared memory is reused.
+template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING, bool BORDER>
+__device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const StepConst& k, float dt, int rk_step,
+                                                int tile_x, int tile_y,
+                                                const float* __restrict__ e_in, const float* __restrict__ hu_in,
+                                                const float* __restrict__ hv_in, float* e_out, float* hu_out,
+                                                float* hv_out, float* e_alt, float* hu_alt, float* hv_alt, int pitch,
+                                                const float* __restrict__ Hi_g, int hi_pitch,
+                                                const float* __restrict__ Hm_g, int hm_pitch, float* smem_raw) {
+    constexpr int HALO = 2 * NSTAGE;
+    constexpr int W = TX + 2 * HALO, H = TY + 2 * HALO;
+    TileSmem<W, H>& S = *reinterpret_cast<TileSmem<W, H>*>(smem_raw);
+
+    Tile<W, H, NT, BORDER> T{S, p, k, 2 + tile_x * TX - HALO, 2 + tile_y * TY - HALO, 0.f, 1.f, 0.f, 0.f, 0.f};
+    {
+        // uniform one-value textures are read once per thread
+        const float a = __ldg(p.angle);
+        T.nX = sinf(a);
+        T.nY = cosf(a);
+        if (CONST_F) T.f0 = __ldg(p.coriolis_f);
+        if (SIMPLE_FORCING) {
+            const float wt = p.wind_t;
+            T.wind_X = p.wind_stress_factor * (wt * __ldg(p.wind_x_next) + (1.0f - wt) * __ldg(p.wind_x_cur));
+            T.wind_Y = p.wind_stress_factor * (wt * __ldg(p.wind_y_next) + (1.0f - wt) * __ldg(p.wind_y_cur));
+        }
+    }
+    const int nx = p.nx, ny = p.ny;
+    const bool px = k.periodic_x, py = k.periodic_y;
+
+    // 1. corner depths, land marked with the dry flag (K/CDKLM16_kernel.cu:571-587)
+    for (int idx = threadIdx.x; idx < (H + 1) * (W + 1); idx += NT) {
+        const int i = idx % (W + 1), j = idx / (W + 1);
+        const int gc = T.x0 + i, gr = T.y0 + j;
+        const int cc = !BORDER ? gc : px ? wrap_interior(gc, nx) : clampi(gc, 0, nx + 4);
+        const int cr = !BORDER ? gr : py ? wrap_interior(gr, ny) : clampi(gr, 0, ny + 4);
+        float v = __ldg(Hi_g + (size_t)cr * hi_pitch + cc);
+        if (fabsf(v - p.land_value) < kDryEps) v = kDryFlag;
+        S.Hi[j][i] = v;
+    }
+    __syncthreads();
+
+    // 2. Q^n with wall mirrors and periodic images, desingularised with the
+    //    cell-mean depth of the (unmirrored) cell (K/CDKLM16_kernel.cu:614-656)
+    for (int idx = threadIdx.x; idx < H * W; idx += NT) {
+        const int i = idx % W, j = idx / W;
+        int gx = T.x0 + i, gy = T.y0 + j;
+        int mx = gx, my = gy;
+        float su = 1.0f, sv = 1.0f;
+        if (BORDER) {
+            if (px) gx = wrap_interior(gx, nx);
+            if (py) gy = wrap_interior(gy, ny);
+            const bool inx = (gx >= 2 && gx < nx + 2), iny = (gy >= 2 && gy < ny + 2);
+            mx = gx;
+            my = gy;
+            if (iny) {
+                if (p.bc_east == 1 && (gx == nx + 2 || gx == nx + 3)) { mx = 2 * nx + 3 - gx; su = -1.0f; }
+                if (p.bc_west == 1 && (gx == 0 || gx == 1)) { mx = 3 - gx; su = -1.0f; }
+            }
+            if (inx) {
+                if (p.bc_north == 1 && (gy == ny + 2 || gy == ny + 3)) { my = 2 * ny + 3 - gy; sv = -1.0f; }
+                if (p.bc_south == 1 && (gy == 0 || gy == 1)) { my = 3 - gy; sv = -1.0f; }
+            }
+            mx = clampi(mx, 0, nx + 3);
+            my = clampi(my, 0, ny + 3);
+            gx = clampi(gx, 0, nx + 3);
+            gy = clampi(gy, 0, ny + 3);
+        }
+        const size_t o = (size_t)my * pitch + mx;
+        const float e = __ldg(e_in + o);
+        const float hu = su * __ldg(hu_in + o);
+        const float hv = sv * __ldg(hv_in + o);
+        const float hmb = __ldg(Hm_g + (size_t)gy * hm_pitch + gx);
+        S.Hmb[j][i] = hmb;
+        float oe, ou, ov;
+        desingularize_cell(p, e, hu, hv, hmb, oe, ou, ov);
+        S.D[0][j][i] = oe; S.D[1][j][i] = ou; S.D[2][j][i] = ov;
+        if (!CONST_F) {
+            if (p.coriolis_cell) {
+                S.Fc[j][i] = __ldg(p.coriolis_cell + (size_t)gy * (p.coriolis_cell_pitch / 4) + gx);
+            } else {
+                const int fx = (BORDER && !px) ? T.x0 + i : gx, fy = (BORDER && !py) ? T.y0 + j : gy;
+                const float s = (fx + 0.5f) / (nx + 4.0f);
+                const float t = (fy + 0.5f) / (ny + 4.0f);
+                S.Fc[j][i] = tex_bilinear(p.coriolis_f, p.coriolis_nx, p.coriolis_ny, s, t);
+            }
+        }
+    }
+    __syncthreads();
+
+    if (NSTAGE == 2) {
+        // ---- stage 1 on the tile + 2 cells ----
+        T.template slopes<2, W - 2, 2, H - 2, CONST_F>();
+        __syncthreads();
+        T.template faces<2, W - 2, 2, H - 2, CONST_F>();
+        __syncthreads();
+        constexpr int NU = (W - 4) * (H - 4);
+        // Results are kept in registers until every thread has read its
+        // cell of D^n, then written as D* (each thread owns its cells).
+        constexpr int PER = (NU + NT - 1) / NT;
+        float qe[PER], qu[PER], qv[PER];
+#pragma unroll
+        for (int r = 0; r < PER; ++r) {
+            const int idx = threadIdx.x + r * NT;
+            qe[r] = 0.f; qu[r] = 0.f; qv[r] = 0.f;
+            if (idx >= NU) continue;
+            const int i = 2 + idx % (W - 4), j = 2 + idx / (W - 4);
+            int gx = T.x0 + i, gy = T.y0 + j;
+            const int gxs = (BORDER && px) ? wrap_interior(gx, nx) : gx;
+            const int gys = (BORDER && py) ? wrap_interior(gy, ny) : gy;
+            const bool ok = !BORDER || ((px || (gx >= 2 && gx < nx + 2)) && (py || (gy >= 2 && gy < ny + 2)));
+            if (!ok) continue;
+            float L1, L2, L3, ec, hu, hv, Hm, hsum;
+            T.template rhs<CONST_F, SIMPLE_FORCING>(i, j, gxs, gys, L1, L2, L3, ec, hu, hv, Hm, hsum);
+            const float C = T.friction(dt, hsum, hu, hv);
+            float ne = ec + dt * L1;
+            float nhu = (hu + dt * L2) / (1.0f + C);
+            float nhv = (hv + dt * L3) / (1.0f + C);
+            finish_cell(p, Hm, ne, nhu, nhv);
+            qe[r] = ne; qu[r] = nhu; qv[r] = nhv;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < PER; ++r) {
+            const int idx = threadIdx.x + r * NT;
+            if (idx >= NU) continue;
+            const int i = 2 + idx % (W - 4), j = 2 + idx / (W - 4);
+            const int gx = T.x0 + i, gy = T.y0 + j;
+            const bool okx = !BORDER || px || (gx >= 2 && gx < nx + 2);
+            const bool oky = !BORDER || py || (gy >= 2 && gy < ny + 2);
+            if (!(okx && oky)) continue;
+            float oe, ou, ov;
+            desingularize_cell(p, qe[r], qu[r], qv[r], S.Hmb[j][i], oe, ou, ov);
+            S.D[0][j][i] = oe; S.D[1][j][i] = ou; S.D[2][j][i] = ov;
+            if (BORDER) {
+                // wall ghosts of the stage result (K/CDKLM16_kernel.cu:420-470)
+                auto mirror = [&](int ii, int jj, float e, float hu, float hv) {
+                    if (ii < 2 || ii >= W - 2 || jj < 2 || jj >= H - 2) return;
+                    float me, mu, mv;
+                    desingularize_cell(p, e, hu, hv, S.Hmb[jj][ii], me, mu, mv);
+                    S.D[0][jj][ii] = me; S.D[1][jj][ii] = mu; S.D[2][jj][ii] = mv;
+                };
+                const int gxs = px ? wrap_interior(gx, nx) : gx;
+                const int gys = py ? wrap_interior(gy, ny) : gy;
+                if (p.bc_north == 1) {
+                    if (gys == ny + 1) mirror(i, j + 1, qe[r], qu[r], -qv[r]);
+                    if (gys == ny) mirror(i, j + 3, qe[r], qu[r], -qv[r]);
+                }
+                if (p.bc_south == 1) {
+                    if (gys == 2) mirror(i, j - 1, qe[r], qu[r], -qv[r]);
+                    if (gys == 3) mirror(i, j - 3, qe[r], qu[r], -qv[r]);
+                }
+                if (p.bc_east == 1) {
+                    if (gxs == nx + 1) mirror(i + 1, j, qe[r], -qu[r], qv[r]);
+                    if (gxs == nx) mirror(i + 3, j, qe[r], -qu[r], qv[r]);
+                }
+                if (p.bc_west == 1) {
+                    if (gxs == 2) mirror(i - 1, j, qe[r], -qu[r], qv[r]);
+                    if (gxs == 3) mirror(i - 3, j, qe[r], -qu[r], qv[r]);
+                }
+            }
+        }
+        __syncthreads();
+        // ---- stage 2 on the tile ----
+        T.template slopes<4, W - 4, 4, H - 4, CONST_F>();
+        __syncthreads();
+        T.template faces<4, W - 4, 4, H - 4, CONST_F>();
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < TX * TY; idx += NT) {
+            const int i = 4 + idx % TX, j = 4 + idx / TX;
+            const int gx = T.x0 + i, gy = T.y0 + j;
+            if (BORDER && (gx >= nx + 2 || gy >= ny + 2)) continue;
+            float L1, L2, L3, ec, hu, hv, Hm, hsum;
+            T.template rhs<CONST_F, SIMPLE_FORCING>(i, j, gx, gy, L1, L2, L3, ec, hu, hv, Hm, hsum);
+            const float C = T.friction(dt, hsum, hu, hv);
+            const size_t o = (size_t)gy * pitch + gx;
+            const float ea = __ldg(e_in + o), hua = __ldg(hu_in + o), hva = __ldg(hv_in + o);
+            float ne = 0.5f * (ea + (ec + dt * L1));
+            float nhu = 0.5f * (hua + (hu + dt * L2)) / (1.0f + 0.5f * C);
+            float nhv = 0.5f * (hva + (hv + dt * L3)) / (1.0f + 0.5f * C);
+            finish_cell(p, Hm, ne, nhu, nhv);
+            if (BORDER) {
+                store_with_images(p, k, e_out, hu_out, hv_out, pitch, gx, gy, ne, nhu, nhv);
+            } else {
+                e_out[o] = ne; hu_out[o] = nhu; hv_out[o] = nhv;
+            }
+        }
+    } else {
+        // ---- one stage with the reference's buffer semantics ----
+        T.template slopes<2, W - 2, 2, H - 2, CONST_F>();
+        __syncthreads();
+        T.template faces<2, W - 2, 2, H - 2, CONST_F>();
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < TX * TY; idx += NT) {
+            const int i = 2 + idx % TX, j = 2 + idx / TX;
+            const int gx = T.x0 + i, gy = T.y0 + j;
+            if (BORDER && (gx >= nx + 2 || gy >= ny + 2)) continue;
+            float L1, L2, L3, ec, hu, hv, Hm, hsum;
+            T.template rhs<CONST_F, SIMPLE_FORCING>(i, j, gx, gy, L1, L2, L3, ec, hu, hv, Hm, hsum);
+            const size_t o = (size_t)gy * pitch + gx;
+            float ne, nhu, nhv;
+            float* de = e_out; float* du = hu_out; float* dv = hv_out;
+            if (p.rk_order < 3) {
+                const float C = T.friction(dt, hsum, hu, hv);
+                if (rk_step == 0) {
+                    ne = ec + dt * L1;
+                    nhu = (hu + dt * L2) / (1.0f + C);
+                    nhv = (hv + dt * L3) / (1.0f + C);
+                } else {
+                    ne = 0.5f * (e_out[o] + (ec + dt * L1));
+                    nhu = 0.5f * (hu_out[o] + (hu + dt * L2)) / (1.0f + 0.5f * C);
+                    nhv = 0.5f * (hv_out[o] + (hv + dt * L3)) / (1.0f + 0.5f * C);
+                }
+            } else {
+                if (rk_step == 0) {
+                    ne = ec + dt * L1; nhu = hu + dt * L2; nhv = hv + dt * L3;
+                } else if (rk_step == 1) {
+                    ne = 0.75f * e_out[o] + 0.25f * (ec + dt * L1);
+                    nhu = 0.75f * hu_out[o] + 0.25f * (hu + dt * L2);
+                    nhv = 0.75f * hv_out[o] + 0.25f * (hv + dt * L3);
+                    de = e_alt; du = hu_alt; dv = hv_alt;
+                } else {
+                    ne = (e_out[o] + 2.0f * (ec + dt * L1)) / 3.0f;
+                    nhu = (hu_out[o] + 2.0f * (hu + dt * L2)) / 3.0f;
+                    nhv = (hv_out[o] + 2.0f * (hv + dt * L3)) / 3.0f;
+                }
+            }
+            finish_cell(p, Hm, ne, nhu, nhv);
+            de[o] = ne; du[o] = nhu; dv[o] = nhv;
+        }
+    }
+}
+
+// A tile needs the boundary logic (periodic wrap, wall mirrors, clamping,
+// periodic ghost images of the output) when its staged region reaches
+// outside the interior.
+template <int TX, int TY, int NSTAGE>
+__device__ __forceinline__ bool tile_on_border(const GocCdklmParams& p, int tile_x, int tile_y) {
+    constexpr int HALO = 2 * NSTAGE;
+    const int x0 = 2 + tile_x * TX - HALO, y0 = 2 + tile_y * TY - HALO;
+    return x0 < 2 || y0 < 2 || x0 + TX + 2 * HALO > p.nx + 2 || y0 + TY + 2 * HALO > p.ny + 2;
+}
+
+template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING>
+__device__ __forceinline__ void cdklm_tile(const GocCdklmParams& p, const StepConst& k, float dt, int rk_step,
+                                           int tile_x, int tile_y,
+                                           const float* __restrict__ e_in, const float* __restrict__ hu_in,
+                                           const float* __restrict__ hv_in, float* e_out, float* hu_out,
+                                           float* hv_out, float* e_alt, float* hu_alt, float* hv_alt, int pitch,
+                                           const float* __restrict__ Hi_g, int hi_pitch,
+                                           const float* __restrict__ Hm_g, int hm_pitch, float* smem_raw) {
+    if (tile_on_border<TX, TY, NSTAGE>(p, tile_x, tile_y))
+        cdklm_tile_body<TX, TY, NSTAGE, NT, CONST_F, SIMPLE_FORCING, true>(
+            p, k, dt, rk_step, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, e_alt, hu_alt, hv_alt,
+            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw);
+    else
+        cdklm_tile_body<TX, TY, NSTAGE, NT, CONST_F, SIMPLE_FORCING, false>(
+            p, k, dt, rk_step, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, e_alt, hu_alt, hv_alt,
+            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw);
+}
+
+template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING>
+__global__ void __launch_bounds__(NT, 3)
+cdklm_tile_kernel(const GocCdklmParams p, const StepConst k, float dt, int rk_step,
+                  const float* __restrict__ e_in, const float* __restrict__ hu_in,
+                  const float* __restrict__ hv_in, float* e_out, float* hu_out, float* hv_out,
+                  float* e_alt, float* hu_alt, float* hv_alt, int pitch,
+                  const float* __restrict__ Hi_g, int hi_pitch, const float* __restrict__ Hm_g, int hm_pitch) {
+    extern __shared__ __align__(16) float smem_raw[];
+    cdklm_tile<TX, TY, NSTAGE, NT, CONST_F, SIMPLE_FORCING>(p, k, dt, rk_step, blockIdx.x, blockIdx.y, e_in, hu_in,
+                                                            hv_in, e_out, hu_out, hv_out, e_alt, hu_alt, hv_alt,
+                                                            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw);
+}
+
+// Output tile of the step kernels and threads per CTA.
+constexpr int kTX = 32, kTY = 16, kNT = 256;
+
+// Host-side validation of a parameter set (shared by all entry points).
+inline int validate_params(const GocCdklmParams* p, const char* who) {
+    if (!p) return set_error(GOC_ERR_ARG, "%s: null params", who);
+    if (p->nx < 1 || p->ny < 1) return set_error(GOC_ERR_ARG, "%s: nx, ny must be >= 1 (got %d, %d)", who, p->nx, p->ny);
+    if (!(p->dx > 0.0f) || !(p->dy > 0.0f) || !(p->g > 0.0f))
+        return set_error(GOC_ERR_ARG, "%s: dx, dy, g must be positive", who);
+    if (p->rk_order < 1 || p->rk_order > 3) return set_error(GOC_ERR_ARG, "%s: rk_order must be 1, 2 or 3", who);
+    if (p->rk_order == 3 && p->r != 0.0f)
+        return set_error(GOC_ERR_ARG, "%s: 3rd order Runge Kutta supported only without friction", who);
+    const int b[4] = {p->bc_north, p->bc_east, p->bc_south, p->bc_west};
+    for (int i = 0; i < 4; ++i)
+        if (b[i] != 1 && b[i] != 2)
+            return set_error(GOC_ERR_UNSUPPORTED, "%s: boundary flag %d not supported (1 = wall, 2 = periodic)", who, b[i]);
+    if ((p->bc_north == 2) != (p->bc_south == 2) || (p->bc_east == 2) != (p->bc_west == 2))
+        return set_error(GOC_ERR_ARG, "%s: periodic boundaries must come in opposite pairs", who);
+    if (!p->coriolis_f || p->coriolis_nx < 1 || p->coriolis_ny < 1)
+        return set_error(GOC_ERR_ARG, "%s: Coriolis texture missing", who);
+    if (!p->angle || p->angle_nx != 1 || p->angle_ny != 1)
+        return set_error(GOC_ERR_UNSUPPORTED, "%s: only a constant (1x1) angle texture is supported", who);
+    if (!p->wind_x_cur || !p->wind_x_next || !p->wind_y_cur || !p->wind_y_next ||
+        p->wind_x_nx < 1 || p->wind_x_ny < 1 || p->wind_y_nx < 1 || p->wind_y_ny < 1)
+        return set_error(GOC_ERR_ARG, "%s: wind stress textures missing", who);
+    if (!p->atm_p_cur || !p->atm_p_next || p->atm_p_nx < 1 || p->atm_p_ny < 1)
+        return set_error(GOC_ERR_ARG, "%s: atmospheric pressure textures missing", who);
+    if ((p->bc_north == 2 && p->ny < 4) || (p->bc_east == 2 && p->nx < 4))
+        return set_error(GOC_ERR_ARG, "%s: periodic directions need at least 4 interior cells", who);
+    return GOC_OK;
+}
+
+}  // namespace goc

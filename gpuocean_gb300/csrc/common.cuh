@@ -20,6 +20,12 @@ int set_error(int code, const char* fmt, ...);
 int check_launch(const char* what);
 void count_launch(int n = 1);
 
+// Member tables of an ensemble handle (ensemble.cu): the descriptors as
+// created (host) and the device copy whose buffer set 0 is the current state.
+const GocMemberDesc* ensemble_host_members(void* ensemble, int* n_members);
+const GocMemberDesc* ensemble_device_members(void* ensemble);
+const int* ensemble_device_nsub(void* ensemble);
+
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // Clamped, texel-centred bilinear lookup in normalised coordinates, the

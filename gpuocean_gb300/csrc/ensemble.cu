@@ -1,0 +1,423 @@
+// Batched ensemble engine: every member of an ensemble (grids of any size)
+// advances in one persistent launch per RK2 step over a member/tile work
+// queue, instead of one Python-driven launch sequence per member
+// (E/OceanNoiseEnsemble.py:517-543, E/MultiLevelOceanEnsemble.py:95-141).
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "cdklm_tile.cuh"
+#include "cfl.cuh"
+#include "drift.cuh"
+
+namespace goc {
+
+struct Ensemble {
+    int n_members = 0;
+    int n_tiles = 0;
+    int max_substeps = 0;
+    int n_dt_items = 0;
+    bool const_f = true, simple = true;
+    std::vector<GocMemberDesc> host;      // descriptors as created (set 0 current)
+    GocMemberDesc* d_members = nullptr;   // device copy, buffers swapped on device
+    int4* d_tiles = nullptr;              // (member, tile_x, tile_y, 0)
+    float* d_dt = nullptr;                // n_members x max_substeps
+    int* d_nsub = nullptr;                // n_substeps per member
+    int4* d_dt_items = nullptr;           // CFL work: (member, bx, by, partial index)
+    int2* d_dt_ranges = nullptr;          // per member [first partial, count)
+    float* d_partials = nullptr;          // CFL scratch
+    // drifters: one (N_m + 1) x 2 position array per member
+    float** d_drift_pos = nullptr;        // per member, null = no drifters
+    int4* d_drift_chunks = nullptr;       // (member, first drifter, count, 0)
+    int n_drift_chunks = 0;
+    float drift_sensitivity = 1.0f;
+};
+
+constexpr int kDriftChunk = 256;
+
+__device__ __forceinline__ DriftGrid member_drift_grid(const GocMemberDesc& d, int set) {
+    return DriftGrid{d.p.nx, d.p.ny, d.p.dx, d.p.dy, 2, 2, d.eta[set], d.hu[set], d.hv[set], d.pitch / 4,
+                     d.Hm, d.Hm_pitch / 4, d.p.bc_north == 2, d.p.bc_east == 2};
+}
+
+// Advect one chunk of a member's drifters with the state of buffer set `set`.
+__device__ __forceinline__ void drift_chunk(const GocMemberDesc& d, float* pos, int first, int count, int set,
+                                           float dt, float sensitivity) {
+    const DriftGrid g = member_drift_grid(d, set);
+    for (int q = threadIdx.x; q < count; q += blockDim.x) {
+        float* p = pos + 2 * (size_t)(first + q);
+        float px = p[0], py = p[1];
+        drift_one(g, nullptr, dt, sensitivity, px, py);
+        p[0] = px;
+        p[1] = py;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+template <bool CONST_F, bool SIMPLE_FORCING>
+__global__ void __launch_bounds__(kNT, 3)
+ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __restrict__ tiles, int n_tiles,
+                    const float* __restrict__ dt_table, const int* __restrict__ nsub, int max_sub, int k,
+                    float* const* __restrict__ drift_pos, const int4* __restrict__ drift_chunks, int n_chunks,
+                    float sensitivity) {
+    extern __shared__ __align__(16) float smem_raw[];
+    __shared__ GocMemberDesc md;
+    __shared__ StepConst kc;
+    int cur = -1;
+    // Work items: the RK2 tiles of step k, then (for k >= 1) the drifter
+    // chunks of step k-1, which read the input state of step k (buffer set
+    // k % 2) that no tile of this launch writes.
+    const int n_items = n_tiles + (k >= 1 ? n_chunks : 0);
+    for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+        if (item >= n_tiles) {
+            const int4 c = drift_chunks[item - n_tiles];
+            if (k - 1 >= __ldg(nsub + c.x)) continue;
+            drift_chunk(members[c.x], drift_pos[c.x], c.y, c.z, k & 1,
+                        __ldg(dt_table + (size_t)c.x * max_sub + (k - 1)), sensitivity);
+            continue;
+        }
+        const int4 t = tiles[item];
+        const int m = t.x;
+        if (k >= __ldg(nsub + m)) continue;  // member already at the end of its block
+        if (m != cur) {
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                md = members[m];
+                kc = make_step_const(md.p);
+            }
+            __syncthreads();
+            cur = m;
+        }
+        const int in = k & 1, out = in ^ 1;
+        const float dt = __ldg(dt_table + (size_t)m * max_sub + k);
+        cdklm_tile<kTX, kTY, 2, kNT, CONST_F, SIMPLE_FORCING>(
+            md.p, kc, dt, 1, t.y, t.z, md.eta[in], md.hu[in], md.hv[in], md.eta[out], md.hu[out], md.hv[out],
+            nullptr, nullptr, nullptr, md.pitch / 4, md.Hi, md.Hi_pitch / 4, md.Hm, md.Hm_pitch / 4, smem_raw);
+        __syncthreads();
+    }
+}
+
+// Drift of the last step of members that ran all `n_launched` steps of the block.
+__global__ void ensemble_end_drift_kernel(const GocMemberDesc* __restrict__ members, const int* __restrict__ nsub,
+                                          const float* __restrict__ dt_table, int max_sub, int n_launched,
+                                          float* const* __restrict__ drift_pos, const int4* __restrict__ chunks,
+                                          float sensitivity) {
+    const int4 c = chunks[blockIdx.x];
+    if (nsub[c.x] != n_launched || n_launched == 0) return;
+    drift_chunk(members[c.x], drift_pos[c.x], c.y, c.z, n_launched & 1,
+                dt_table[(size_t)c.x * max_sub + (n_launched - 1)], sensitivity);
+}
+
+__global__ void ensemble_end_block_kernel(GocMemberDesc* members, const int* nsub, int n) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n || (nsub[m] & 1) == 0) return;
+    GocMemberDesc& d = members[m];
+    float* t;
+    t = d.eta[0]; d.eta[0] = d.eta[1]; d.eta[1] = t;
+    t = d.hu[0]; d.hu[0] = d.hu[1]; d.hu[1] = t;
+    t = d.hv[0]; d.hv[0] = d.hv[1]; d.hv[1] = t;
+}
+
+__global__ void __launch_bounds__(kDtBX * kDtBY)
+ensemble_dt_partials_kernel(const GocMemberDesc* __restrict__ members, const int4* __restrict__ items,
+                            float* __restrict__ partials) {
+    __shared__ float wmin[kDtBX * kDtBY / 32];
+    const int4 it = items[blockIdx.x];
+    const GocMemberDesc& d = members[it.x];
+    const int i = 2 + it.y * kDtBX + threadIdx.x;
+    const int j = 2 + it.z * kDtBY + threadIdx.y;
+    float v = cell_dt(d.p.nx, d.p.ny, d.p.dx, d.p.dy, d.p.g, d.eta[0], d.hu[0], d.hv[0], d.pitch / 4, d.Hm,
+                      d.Hm_pitch / 4, d.p.land_value, i, j);
+    v = warp_min(v);
+    const int tid = threadIdx.y * kDtBX + threadIdx.x;
+    if ((tid & 31) == 0) wmin[tid >> 5] = v;
+    __syncthreads();
+    if (tid < 32) {
+        float w = (tid < kDtBX * kDtBY / 32) ? wmin[tid] : kMaxDt;
+        w = warp_min(w);
+        if (tid == 0) partials[it.w] = w;
+    }
+}
+
+__global__ void __launch_bounds__(256) ensemble_dt_final_kernel(const float* __restrict__ partials,
+                                                                const int2* __restrict__ ranges,
+                                                                float* __restrict__ out) {
+    __shared__ float wmin[8];
+    const int2 r = ranges[blockIdx.x];
+    float v = kMaxDt;
+    for (int q = threadIdx.x; q < r.y; q += blockDim.x) v = fminf(v, partials[r.x + q]);
+    v = warp_min(v);
+    if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        v = (threadIdx.x < 8) ? wmin[threadIdx.x] : kMaxDt;
+        v = warp_min(v);
+        if (threadIdx.x == 0) out[blockIdx.x] = v;
+    }
+}
+
+// Kernel attributes and the persistent grid are set up once per variant,
+// outside any stream capture (goc_ensemble_create calls this).
+template <bool CF, bool SF>
+static int configure_ensemble_kernel(int* grid_out) {
+    constexpr size_t smem = sizeof(TileSmem<kTX + 8, kTY + 8>);
+    static int grid = 0;
+    if (grid == 0) {
+        auto kern = ensemble_rk2_kernel<CF, SF>;
+        cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(err));
+        int blocks = 0;
+        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, kNT, smem);
+        if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(err));
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        grid = std::max(1, sms) * std::max(1, blocks);
+    }
+    *grid_out = grid;
+    return GOC_OK;
+}
+
+template <bool CF, bool SF>
+static int launch_ensemble(Ensemble* e, int k, cudaStream_t st) {
+    constexpr size_t smem = sizeof(TileSmem<kTX + 8, kTY + 8>);
+    auto kern = ensemble_rk2_kernel<CF, SF>;
+    int full = 0;
+    int rc = configure_ensemble_kernel<CF, SF>(&full);
+    if (rc) return rc;
+    const int items = e->n_tiles + (k >= 1 ? e->n_drift_chunks : 0);
+    const int grid = std::min(items, full);
+    kern<<<grid, kNT, smem, st>>>(e->d_members, e->d_tiles, e->n_tiles, e->d_dt, e->d_nsub, e->max_substeps, k,
+                                  e->d_drift_pos, e->d_drift_chunks, e->n_drift_chunks, e->drift_sensitivity);
+    count_launch();
+    return check_launch("ensemble_rk2_kernel");
+}
+
+static void free_ensemble(Ensemble* e) {
+    cudaFree(e->d_members);
+    cudaFree(e->d_tiles);
+    cudaFree(e->d_dt);
+    cudaFree(e->d_nsub);
+    cudaFree(e->d_dt_items);
+    cudaFree(e->d_dt_ranges);
+    cudaFree(e->d_partials);
+    cudaFree(e->d_drift_pos);
+    cudaFree(e->d_drift_chunks);
+    delete e;
+}
+
+const GocMemberDesc* ensemble_host_members(void* ensemble, int* n_members) {
+    Ensemble* e = static_cast<Ensemble*>(ensemble);
+    if (n_members) *n_members = e->n_members;
+    return e->host.data();
+}
+
+const GocMemberDesc* ensemble_device_members(void* ensemble) { return static_cast<Ensemble*>(ensemble)->d_members; }
+
+const int* ensemble_device_nsub(void* ensemble) { return static_cast<Ensemble*>(ensemble)->d_nsub; }
+
+}  // namespace goc
+
+using namespace goc;
+
+extern "C" int goc_ensemble_create(const GocMemberDesc* members, int n_members, int max_substeps, void** out) {
+    if (!out) return set_error(GOC_ERR_ARG, "goc_ensemble_create: null out pointer");
+    *out = nullptr;
+    if (!members || n_members < 1) return set_error(GOC_ERR_ARG, "goc_ensemble_create: no members");
+    if (max_substeps < 1) return set_error(GOC_ERR_ARG, "goc_ensemble_create: max_substeps must be >= 1");
+    Ensemble* e = new Ensemble();
+    e->n_members = n_members;
+    e->max_substeps = max_substeps;
+    e->host.assign(members, members + n_members);
+    std::vector<int4> tiles, dt_items;
+    std::vector<int2> ranges;
+    for (int m = 0; m < n_members; ++m) {
+        const GocMemberDesc& d = members[m];
+        char who[64];
+        snprintf(who, sizeof(who), "goc_ensemble_create: member %d", m);
+        int rc = validate_params(&d.p, who);
+        if (!rc && d.p.rk_order != 2) rc = set_error(GOC_ERR_ARG, "%s: rk_order must be 2", who);
+        if (!rc && (!d.Hi || !d.Hm || !d.eta[0] || !d.eta[1] || !d.hu[0] || !d.hu[1] || !d.hv[0] || !d.hv[1]))
+            rc = set_error(GOC_ERR_ARG, "%s: null buffer", who);
+        if (!rc && (d.pitch < (d.p.nx + 4) * 4 || d.pitch % 4 || d.Hi_pitch < (d.p.nx + 5) * 4 || d.Hi_pitch % 4 ||
+                    d.Hm_pitch < (d.p.nx + 4) * 4 || d.Hm_pitch % 4))
+            rc = set_error(GOC_ERR_ARG, "%s: pitch too small", who);
+        if (!rc && (d.eta[0] == d.eta[1] || d.hu[0] == d.hu[1] || d.hv[0] == d.hv[1]))
+            rc = set_error(GOC_ERR_ARG, "%s: the two buffer sets must differ", who);
+        if (rc) {
+            delete e;
+            return rc;
+        }
+        e->const_f = e->const_f && d.p.coriolis_nx == 1 && d.p.coriolis_ny == 1;
+        e->simple = e->simple && d.p.wind_x_nx == 1 && d.p.wind_x_ny == 1 && d.p.wind_y_nx == 1 &&
+                    d.p.wind_y_ny == 1 && d.p.atm_p_nx == 1 && d.p.atm_p_ny == 1;
+        const int tx = (d.p.nx + kTX - 1) / kTX, ty = (d.p.ny + kTY - 1) / kTY;
+        for (int j = 0; j < ty; ++j)
+            for (int i = 0; i < tx; ++i) tiles.push_back(make_int4(m, i, j, 0));
+        const int bx = (d.p.nx + kDtBX - 1) / kDtBX, by = (d.p.ny + kDtBY - 1) / kDtBY;
+        ranges.push_back(make_int2((int)dt_items.size(), bx * by));
+        for (int j = 0; j < by; ++j)
+            for (int i = 0; i < bx; ++i) dt_items.push_back(make_int4(m, i, j, (int)dt_items.size()));
+    }
+    e->n_tiles = (int)tiles.size();
+    e->n_dt_items = (int)dt_items.size();
+    cudaError_t err = cudaSuccess;
+    auto alloc = [&](void** p, size_t bytes) {
+        if (err == cudaSuccess) err = cudaMalloc(p, bytes);
+    };
+    alloc((void**)&e->d_members, sizeof(GocMemberDesc) * n_members);
+    alloc((void**)&e->d_tiles, sizeof(int4) * tiles.size());
+    alloc((void**)&e->d_dt, sizeof(float) * (size_t)n_members * max_substeps);
+    alloc((void**)&e->d_nsub, sizeof(int) * n_members);
+    alloc((void**)&e->d_dt_items, sizeof(int4) * dt_items.size());
+    alloc((void**)&e->d_dt_ranges, sizeof(int2) * ranges.size());
+    alloc((void**)&e->d_partials, sizeof(float) * dt_items.size());
+    if (err == cudaSuccess)
+        err = cudaMemcpy(e->d_members, members, sizeof(GocMemberDesc) * n_members, cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMemcpy(e->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess)
+        err = cudaMemcpy(e->d_dt_items, dt_items.data(), sizeof(int4) * dt_items.size(), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess)
+        err = cudaMemcpy(e->d_dt_ranges, ranges.data(), sizeof(int2) * ranges.size(), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMemset(e->d_nsub, 0, sizeof(int) * n_members);
+    if (err == cudaSuccess) err = cudaMemset(e->d_dt, 0, sizeof(float) * (size_t)n_members * max_substeps);
+    if (err != cudaSuccess) {
+        free_ensemble(e);
+        return set_error(GOC_ERR_CUDA, "goc_ensemble_create: %s", cudaGetErrorString(err));
+    }
+    int grid = 0, rc = GOC_OK;
+    if (e->const_f && e->simple) rc = configure_ensemble_kernel<true, true>(&grid);
+    else if (e->const_f) rc = configure_ensemble_kernel<true, false>(&grid);
+    else if (e->simple) rc = configure_ensemble_kernel<false, true>(&grid);
+    else rc = configure_ensemble_kernel<false, false>(&grid);
+    if (rc) {
+        free_ensemble(e);
+        return rc;
+    }
+    *out = e;
+    return GOC_OK;
+}
+
+extern "C" int goc_ensemble_destroy(void* ensemble) {
+    if (!ensemble) return GOC_OK;
+    free_ensemble(static_cast<Ensemble*>(ensemble));
+    return GOC_OK;
+}
+
+extern "C" int goc_ensemble_size(void* ensemble, int* n_members, int* n_tiles) {
+    if (!ensemble) return set_error(GOC_ERR_ARG, "goc_ensemble_size: null handle");
+    Ensemble* e = static_cast<Ensemble*>(ensemble);
+    if (n_members) *n_members = e->n_members;
+    if (n_tiles) *n_tiles = e->n_tiles;
+    return GOC_OK;
+}
+
+extern "C" int goc_ensemble_set_schedule(void* ensemble, const float* dt_table, const int* n_substeps, void* stream) {
+    if (!ensemble || !dt_table || !n_substeps) return set_error(GOC_ERR_ARG, "goc_ensemble_set_schedule: null argument");
+    Ensemble* e = static_cast<Ensemble*>(ensemble);
+    for (int m = 0; m < e->n_members; ++m) {
+        if (n_substeps[m] < 0 || n_substeps[m] > e->max_substeps)
+            return set_error(GOC_ERR_ARG, "goc_ensemble_set_schedule: member %d has %d steps (max %d)", m,
+                             n_substeps[m], e->max_substeps);
+        for (int k = 0; k < n_substeps[m]; ++k)
+            if (!(dt_table[(size_t)m * e->max_substeps + k] >= 0.0f))
+                return set_error(GOC_ERR_ARG, "goc_ensemble_set_schedule: negative dt for member %d", m);
+    }
+    cudaStream_t st = as_stream(stream);
+    cudaError_t err = cudaMemcpyAsync(e->d_dt, dt_table, sizeof(float) * (size_t)e->n_members * e->max_substeps,
+                                      cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(e->d_nsub, n_substeps, sizeof(int) * e->n_members, cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);  // host arrays may be reused on return
+    if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_ensemble_set_schedule: %s", cudaGetErrorString(err));
+    return GOC_OK;
+}
+
+extern "C" int goc_ensemble_rk2_substep(void* ensemble, int k, void* stream) {
+    if (!ensemble) return set_error(GOC_ERR_ARG, "goc_ensemble_rk2_substep: null handle");
+    Ensemble* e = static_cast<Ensemble*>(ensemble);
+    if (k < 0 || k >= e->max_substeps) return set_error(GOC_ERR_ARG, "goc_ensemble_rk2_substep: k=%d out of range", k);
+    cudaStream_t st = as_stream(stream);
+    if (e->const_f && e->simple) return launch_ensemble<true, true>(e, k, st);
+    if (e->const_f) return launch_ensemble<true, false>(e, k, st);
+    if (e->simple) return launch_ensemble<false, true>(e, k, st);
+    return launch_ensemble<false, false>(e, k, st);
+}
+
+extern "C" int goc_ensemble_end_block(void* ensemble, int n_launched, void* stream) {
+    if (!ensemble) return set_error(GOC_ERR_ARG, "goc_ensemble_end_block: null handle");
+    Ensemble* e = static_cast<Ensemble*>(ensemble);
+    if (n_launched < 0 || n_launched > e->max_substeps)
+        return set_error(GOC_ERR_ARG, "goc_ensemble_end_block: %d steps launched, max %d", n_launched, e->max_substeps);
+    if (e->n_drift_chunks > 0 && n_launched > 0) {
+        ensemble_end_drift_kernel<<<e->n_drift_chunks, kDriftChunk, 0, as_stream(stream)>>>(
+            e->d_members, e->d_nsub, e->d_dt, e->max_substeps, n_launched, e->d_drift_pos, e->d_drift_chunks,
+            e->drift_sensitivity);
+        count_launch();
+        int rc = check_launch("ensemble_end_drift_kernel");
+        if (rc) return rc;
+    }
+    ensemble_end_block_kernel<<<(e->n_members + 127) / 128, 128, 0, as_stream(stream)>>>(e->d_members, e->d_nsub,
+                                                                                      e->n_members);
+    count_launch();
+    return check_launch("ensemble_end_block_kernel");
+}
+
+extern "C" int goc_ensemble_get_member(void* ensemble, int m, GocMemberDesc* out, void* stream) {
+    if (!ensemble || !out) return set_error(GOC_ERR_ARG, "goc_ensemble_get_member: null argument");
+    Ensemble* e = static_cast<Ensemble*>(ensemble);
+    if (m < 0 || m >= e->n_members) return set_error(GOC_ERR_ARG, "goc_ensemble_get_member: member %d out of range", m);
+    cudaStream_t st = as_stream(stream);
+    cudaError_t err = cudaMemcpyAsync(out, e->d_members + m, sizeof(GocMemberDesc), cudaMemcpyDeviceToHost, st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_ensemble_get_member: %s", cudaGetErrorString(err));
+    return GOC_OK;
+}
+
+extern "C" int goc_ensemble_max_dt(void* ensemble, float* dt_out, void* stream) {
+    if (!ensemble || !dt_out) return set_error(GOC_ERR_ARG, "goc_ensemble_max_dt: null argument");
+    Ensemble* e = static_cast<Ensemble*>(ensemble);
+    cudaStream_t st = as_stream(stream);
+    ensemble_dt_partials_kernel<<<e->n_dt_items, dim3(kDtBX, kDtBY), 0, st>>>(e->d_members, e->d_dt_items,
+                                                                             e->d_partials);
+    count_launch();
+    int rc = check_launch("ensemble_dt_partials_kernel");
+    if (rc) return rc;
+    ensemble_dt_final_kernel<<<e->n_members, 256, 0, st>>>(e->d_partials, e->d_dt_ranges, dt_out);
+    count_launch();
+    return check_launch("ensemble_dt_final_kernel");
+}
+
+extern "C" int goc_ensemble_set_drifters(void* ensemble, float* const* positions, const int* num_drifters,
+                                         float sensitivity, void* stream) {
+    if (!ensemble || !positions || !num_drifters) return set_error(GOC_ERR_ARG, "goc_ensemble_set_drifters: null argument");
+    Ensemble* e = static_cast<Ensemble*>(ensemble);
+    std::vector<int4> chunks;
+    for (int m = 0; m < e->n_members; ++m) {
+        if (!positions[m]) continue;
+        if (num_drifters[m] < 0) return set_error(GOC_ERR_ARG, "goc_ensemble_set_drifters: negative count");
+        const int n = num_drifters[m] + 1;  // with the observation row
+        for (int f = 0; f < n; f += kDriftChunk) chunks.push_back(make_int4(m, f, std::min(kDriftChunk, n - f), 0));
+    }
+    cudaStream_t st = as_stream(stream);
+    cudaError_t err = cudaStreamSynchronize(st);
+    cudaFree(e->d_drift_pos);
+    cudaFree(e->d_drift_chunks);
+    e->d_drift_pos = nullptr;
+    e->d_drift_chunks = nullptr;
+    e->n_drift_chunks = 0;
+    if (err == cudaSuccess) err = cudaMalloc(&e->d_drift_pos, sizeof(float*) * e->n_members);
+    if (err == cudaSuccess) err = cudaMemcpy(e->d_drift_pos, positions, sizeof(float*) * e->n_members, cudaMemcpyHostToDevice);
+    if (err == cudaSuccess && !chunks.empty()) {
+        err = cudaMalloc(&e->d_drift_chunks, sizeof(int4) * chunks.size());
+        if (err == cudaSuccess)
+            err = cudaMemcpy(e->d_drift_chunks, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice);
+    }
+    if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_ensemble_set_drifters: %s", cudaGetErrorString(err));
+    e->n_drift_chunks = (int)chunks.size();
+    e->drift_sensitivity = sensitivity;
+    return GOC_OK;
+}

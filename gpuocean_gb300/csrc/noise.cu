@@ -1,0 +1,517 @@
+// Stochastic model error: random numbers, SOAR-correlated coarse field and
+// its geostrophically balanced (bicubic) transfer to the ocean state.
+//
+// Semantics follow the reference kernels (K/ocean_noise.cu:126-666,
+// K/random_number_generators.cu:1-134, K/interpolation.cu) and their build
+// flags (--use_fast_math, S/OceanStateNoise.py:214-217): this translation
+// unit is compiled with -use_fast_math as well.
+#include <curand_kernel.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+
+namespace goc {
+
+// ---------------------------------------------------------------------------
+// random numbers
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned long long lcg_next(unsigned long long s) {
+    return (s * 1103515245ULL + 12345ULL) % 2147483647ULL;
+}
+
+// Two uniforms per seed (K/random_number_generators.cu:5-22); `normal`
+// applies Box-Muller with a redraw when the first uniform is 0 (:35-52).
+__global__ void lcg_kernel(int seed_nx, int seed_ny, int random_nx, unsigned long long* seeds, int seed_pitch,
+                           float* random, int random_pitch, int normal) {
+    const int ti = blockIdx.x * blockDim.x + threadIdx.x;
+    const int tj = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ti >= seed_nx || tj >= seed_ny) return;
+    unsigned long long* srow = seeds + (size_t)tj * seed_pitch;
+    float* rrow = random + (size_t)tj * random_pitch;
+    unsigned long long s = srow[ti];
+    s = lcg_next(s);
+    float u1 = (float)(s / 2147483648.0);
+    s = lcg_next(s);
+    float u2 = (float)(s / 2147483648.0);
+    float a = u1, b = u2;
+    if (normal) {
+        if (u1 == 0.0f) {
+            s = lcg_next(s);
+            u1 = (float)(s / 2147483648.0);
+            s = lcg_next(s);
+            u2 = (float)(s / 2147483648.0);
+        }
+        const float r = sqrtf(-2.0f * logf(u1));
+        a = r * cospif(2 * u2);
+        b = r * sinpif(2 * u2);
+    }
+    srow[ti] = s;
+    if (2 * ti < random_nx) rrow[2 * ti] = a;
+    if (2 * ti + 1 < random_nx) rrow[2 * ti + 1] = b;
+}
+
+__global__ void xorwow_init_kernel(curandStateXORWOW_t* states, int n, unsigned long long seed) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) curand_init(seed, (unsigned long long)i, 0ULL, states + i);
+}
+
+__global__ void xorwow_normal_kernel(curandStateXORWOW_t* states, int nx, int ny, float* random, int pitch) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nx * ny) return;
+    curandStateXORWOW_t st = states[i];
+    random[(size_t)(i / nx) * pitch + (i % nx)] = curand_normal(&st);
+    states[i] = st;
+}
+
+// ---------------------------------------------------------------------------
+// SOAR coarse field (K/ocean_noise.cu:126-247)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ float soar_cov(int ax, int ay, int bx, int by, float dx, float dy, float q0, float L) {
+    const float dist = sqrtf(dx * dx * (ax - bx) * (ax - bx) + dy * dy * (ay - by) * (ay - by));
+    return q0 * (1.0f + dist / L) * expf(-dist / L);
+}
+
+__device__ __forceinline__ void soar_cell(const GocNoiseDesc& d, float scale, int additive, int ti, int tj,
+                                          const float* __restrict__ random, float* coarse) {
+    const int cnx = d.coarse_nx, cny = d.coarse_ny;
+    if (ti >= cnx + 4 || tj >= cny + 4) return;
+    float q = 0.0f;
+    for (int b = 0; b < 5; ++b) {
+        // xi row read by stencil row b of coarse cell tj
+        const int r = d.periodic_ns ? ((tj + b - 4) % cny + cny) % cny : min(tj + b, cny + 7);
+        const float* row = random + (size_t)r * (d.random_pitch / 4);
+        for (int a = 0; a < 5; ++a) {
+            const int c = d.periodic_ew ? ((ti + a - 4) % cnx + cnx) % cnx : min(ti + a, cnx + 7);
+            q += soar_cov(2, 2, a, b, d.coarse_dx, d.coarse_dy, d.soar_q0, d.soar_L) * row[c];
+        }
+    }
+    float* out = coarse + (size_t)tj * (d.coarse_pitch / 4) + ti;
+    if (additive) *out += scale * q;
+    else *out = scale * q;
+}
+
+__global__ void soar_kernel(GocNoiseDesc d, float scale, int additive) {
+    soar_cell(d, scale, additive, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y,
+              d.random, d.coarse);
+}
+
+// ---------------------------------------------------------------------------
+// transfer to the ocean state
+// ---------------------------------------------------------------------------
+
+struct OceanRef {
+    int nx, ny;
+    float dx, dy;
+    float* eta; float* hu; float* hv; int pitch;    // floats
+    const float* Hi; int hi_pitch;                  // floats
+    float land;
+    int images_ns, images_ew;                       // write periodic ghost images
+};
+
+__device__ __forceinline__ OceanRef ocean_of(const GocMemberDesc& m, int images) {
+    return OceanRef{m.p.nx, m.p.ny, m.p.dx, m.p.dy, m.eta[0], m.hu[0], m.hv[0], m.pitch / 4, m.Hi, m.Hi_pitch / 4,
+                    m.p.land_value, images && m.p.bc_north == 2, images && m.p.bc_east == 2};
+}
+
+// Write a perturbed interior cell and, for periodic boundaries, its ghost
+// images (the boundary fill the reference runs after perturbState,
+// S/CDKLM16.py:571-572).
+__device__ __forceinline__ void store_cell(const OceanRef& o, int ti, int tj, float e, float u, float v) {
+    int xs[2] = {ti, -1}, ys[2] = {tj, -1};
+    if (o.images_ew) xs[1] = (ti < 4) ? ti + o.nx : (ti >= o.nx ? ti - o.nx : -1);
+    if (o.images_ns) ys[1] = (tj < 4) ? tj + o.ny : (tj >= o.ny ? tj - o.ny : -1);
+    for (int a = 0; a < 2; ++a) {
+        if (ys[a] < 0) continue;
+        for (int b = 0; b < 2; ++b) {
+            if (xs[b] < 0) continue;
+            const size_t k = (size_t)ys[a] * o.pitch + xs[b];
+            o.eta[k] = e; o.hu[k] = u; o.hv[k] = v;
+        }
+    }
+}
+
+__device__ __forceinline__ float noise_coriolis(const GocNoiseDesc& d, const OceanRef& o, int ti, int tj) {
+    float c = d.f + d.beta * ((ti + 0.5f) * o.dx * d.north_x + (tj + 0.5f) * o.dy * d.north_y);
+    if (d.f == 0.0f && d.coriolis_f) {
+        const float s = (ti + 0.5f) / (o.nx + 4.0f), t = (tj + 0.5f) / (o.ny + 4.0f);
+        c = tex_bilinear(d.coriolis_f, d.coriolis_nx, d.coriolis_ny, s, t);
+    }
+    return c;
+}
+
+__device__ __forceinline__ float coarse_at(const GocNoiseDesc& d, int j, int i) {
+    j = clampi(j, 0, d.coarse_ny + 3);
+    i = clampi(i, 0, d.coarse_nx + 3);
+    return d.coarse[(size_t)j * (d.coarse_pitch / 4) + i];
+}
+
+// Bicubic value of the coarse field at fine cell (ti, tj) (K/ocean_noise.cu:497-586)
+__device__ float bicubic_value(const GocNoiseDesc& d, const OceanRef& o, int ti, int tj) {
+    const float x = (ti - 2 + 0.5f + d.offset_i) * o.dx;
+    const float y = (tj - 2 + 0.5f + d.offset_j) * o.dy;
+    int ci = (int)floorf(x / d.coarse_dx + 2 - 0.5f);
+    int cj = (int)floorf(y / d.coarse_dy + 2 - 0.5f);
+    if (ci > d.coarse_nx + 1) ci -= 1;
+    if (cj > d.coarse_ny + 1) cj -= 1;
+    const float rx = (x - (ci - 2 + 0.5f) * d.coarse_dx) / d.coarse_dx;
+    const float ry = (y - (cj - 2 + 0.5f) * d.coarse_dy) / d.coarse_dy;
+    float c[4][4];  // c[row][col] = coarse[cj-1+row][ci-1+col]
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) c[r][q] = coarse_at(d, cj - 1 + r, ci - 1 + q);
+    // values, x/y derivatives and cross derivatives at the 4 corners
+    float F[4][4];
+    F[0][0] = c[1][1]; F[0][1] = c[2][1]; F[1][0] = c[1][2]; F[1][1] = c[2][2];
+    F[2][0] = (c[1][2] - c[1][0]) / 2.0f; F[2][1] = (c[2][2] - c[2][0]) / 2.0f;
+    F[3][0] = (c[1][3] - c[1][1]) / 2.0f; F[3][1] = (c[2][3] - c[2][1]) / 2.0f;
+    F[0][2] = (c[2][1] - c[0][1]) / 2.0f; F[0][3] = (c[3][1] - c[1][1]) / 2.0f;
+    F[1][2] = (c[2][2] - c[0][2]) / 2.0f; F[1][3] = (c[3][2] - c[1][2]) / 2.0f;
+    const float fy_10 = (c[2][0] - c[0][0]) / 2.0f, fy_11 = (c[3][0] - c[1][0]) / 2.0f;
+    const float fy20 = (c[2][3] - c[0][3]) / 2.0f, fy21 = (c[3][3] - c[1][3]) / 2.0f;
+    F[2][2] = (F[1][2] - fy_10) / 2.0f; F[2][3] = (F[1][3] - fy_11) / 2.0f;
+    F[3][2] = (fy20 - F[0][2]) / 2.0f; F[3][3] = (fy21 - F[0][3]) / 2.0f;
+    const float B[4][4] = {{1, 0, 0, 0}, {0, 0, 1, 0}, {-3, 3, -2, -1}, {2, -2, 1, 1}};
+    float FB[4][4], A[4][4];   // FB = F B^T, A = B FB
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            FB[r][q] = F[r][0] * B[q][0] + F[r][1] * B[q][1] + F[r][2] * B[q][2] + F[r][3] * B[q][3];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            A[r][q] = B[r][0] * FB[0][q] + B[r][1] * FB[1][q] + B[r][2] * FB[2][q] + B[r][3] * FB[3][q];
+    const float xv[4] = {1.0f, rx, rx * rx, rx * rx * rx};
+    const float yv[4] = {1.0f, ry, ry * ry, ry * ry * ry};
+    float v = 0.0f;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+        v += xv[r] * (A[r][0] * yv[0] + A[r][1] * yv[1] + A[r][2] * yv[2] + A[r][3] * yv[3]);
+    return v;
+}
+
+// Perturbation of interior cell (ti, tj).  `factor1`: the coarse grid is the
+// computational grid (geostrophicBalance, the state's own depth in h and land
+// cells zeroed); otherwise bicubic up-sampling (bicubicInterpolation, land
+// cells unperturbed).  `de(jj, ii)` gives the perturbation of eta.
+template <typename DE>
+__device__ __forceinline__ void perturb_cell(const GocNoiseDesc& d, const OceanRef& o, int ti, int tj, bool factor1,
+                                             DE de) {
+    const float* h0 = o.Hi + (size_t)tj * o.hi_pitch + ti;
+    const float* h1 = h0 + o.hi_pitch;
+    const bool dry = (h0[0] == o.land) || (h0[1] == o.land) || (h1[0] == o.land) || (h1[1] == o.land);
+    const float H_mid = 0.25f * (h0[0] + h0[1] + h1[0] + h1[1]);
+    const float cor = noise_coriolis(d, o, ti, tj);
+    const float dc = de(tj, ti);
+    const float ex = (de(tj, ti + 1) - de(tj, ti - 1)) / (2.0f * o.dx);
+    const float ey = (de(tj + 1, ti) - de(tj - 1, ti)) / (2.0f * o.dy);
+    const size_t k = (size_t)tj * o.pitch + ti;
+    float e = o.eta[k], u = o.hu[k], v = o.hv[k];
+    if (factor1) {
+        const float h_mid = dc + H_mid + e;
+        const float dhu = -(d.g / cor) * h_mid * ey;
+        const float dhv = (d.g / cor) * h_mid * ex;
+        if (dry) {
+            e = 0.0f; u = 0.0f; v = 0.0f;
+        } else {
+            e += dc; u += dhu; v += dhv;
+        }
+    } else if (!dry) {
+        e += dc;
+        u += -(d.g / cor) * (H_mid + dc) * ey;
+        v += (d.g / cor) * (H_mid + dc) * ex;
+    }
+    store_cell(o, ti, tj, e, u, v);
+}
+
+constexpr int kNB = 16;  // noise tile edge
+
+// One 16x16 tile of interior cells (tile origin bx, by in interior cells).
+__device__ void perturb_tile(const GocNoiseDesc& d, const OceanRef& o, int bx, int by) {
+    __shared__ float s_de[kNB + 2][kNB + 2];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const bool factor1 = d.interpolation_factor <= 1;
+    // d_eta on the tile + 1 ring (interior origin at ghost offset 2)
+    for (int j = ty; j < kNB + 2; j += kNB)
+        for (int i = tx; i < kNB + 2; i += kNB) {
+            const int gi = 2 + bx + i - 1, gj = 2 + by + j - 1;
+            s_de[j][i] = factor1 ? coarse_at(d, gj, gi) : bicubic_value(d, o, gi, gj);
+        }
+    __syncthreads();
+    const int ti = 2 + bx + tx, tj = 2 + by + ty;
+    if (ti < o.nx + 2 && tj < o.ny + 2)
+        perturb_cell(d, o, ti, tj, factor1,
+                     [&](int jj, int ii) { return s_de[jj - (2 + by) + 1][ii - (2 + bx) + 1]; });
+    __syncthreads();
+}
+
+__global__ void perturb_kernel(GocNoiseDesc d, OceanRef o) {
+    perturb_tile(d, o, blockIdx.x * kNB, blockIdx.y * kNB);
+}
+
+// ---------------------------------------------------------------------------
+// batched: all members of an ensemble in two launches
+// ---------------------------------------------------------------------------
+
+// substep < 0: between blocks, the state of member m is buffer set 0 of the
+// ensemble's device member table.  substep = k: right after RK2 step k of a
+// block, members that took step k hold their state in set (k + 1) % 2.
+__device__ __forceinline__ bool member_set(const int* nsub, int m, int substep, int* set) {
+    if (substep < 0) {
+        *set = 0;
+        return true;
+    }
+    if (substep >= nsub[m]) return false;
+    *set = (substep + 1) & 1;
+    return true;
+}
+
+__global__ void soar_batched_active_kernel(const GocNoiseDesc* __restrict__ nd, const int4* __restrict__ items,
+                                           const int* __restrict__ nsub, int substep, float scale) {
+    const int4 it = items[blockIdx.x];
+    int set;
+    if (!member_set(nsub, it.x, substep, &set)) return;
+    const GocNoiseDesc& d = nd[it.x];
+    soar_cell(d, scale, 0, it.y * kNB + threadIdx.x, it.z * kNB + threadIdx.y, d.random, d.coarse);
+}
+
+__global__ void perturb_batched_kernel(const GocNoiseDesc* __restrict__ nd, const GocMemberDesc* __restrict__ mem,
+                                       const int4* __restrict__ items, const int* __restrict__ nsub, int substep) {
+    const int4 it = items[blockIdx.x];
+    int set;
+    if (!member_set(nsub, it.x, substep, &set)) return;
+    const GocMemberDesc& m = mem[it.x];
+    const OceanRef o{m.p.nx, m.p.ny, m.p.dx, m.p.dy, m.eta[set], m.hu[set], m.hv[set], m.pitch / 4, m.Hi,
+                     m.Hi_pitch / 4, m.p.land_value, m.p.bc_north == 2, m.p.bc_east == 2};
+    perturb_tile(nd[it.x], o, it.y * kNB, it.z * kNB);
+}
+
+// XORWOW normals for every member's random field; one state per element.
+__global__ void xorwow_batched_kernel(const GocNoiseDesc* __restrict__ nd, const int4* __restrict__ chunks,
+                                      curandStateXORWOW_t* states, const int* __restrict__ nsub, int substep) {
+    const int4 c = chunks[blockIdx.x];   // (member, first element, count, first state)
+    int set;
+    if (!member_set(nsub, c.x, substep, &set)) return;
+    const GocNoiseDesc& d = nd[c.x];
+    const int rnx = d.periodic_ew ? d.coarse_nx : d.coarse_nx + 8;
+    for (int q = threadIdx.x; q < c.z; q += blockDim.x) {
+        const int e = c.y + q;
+        curandStateXORWOW_t st = states[c.w + q];
+        const float v = curand_normal(&st);
+        states[c.w + q] = st;
+        const_cast<float*>(d.random)[(size_t)(e / rnx) * (d.random_pitch / 4) + (e % rnx)] = v;
+    }
+}
+
+__global__ void xorwow_batched_init_kernel(curandStateXORWOW_t* states, int n, unsigned long long seed) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) curand_init(seed, (unsigned long long)i, 0ULL, states + i);
+}
+
+}  // namespace goc
+
+using namespace goc;
+
+static int check_noise(const GocNoiseDesc* d, const char* who) {
+    if (!d) return set_error(GOC_ERR_ARG, "%s: null noise descriptor", who);
+    if (d->coarse_nx < 1 || d->coarse_ny < 1 || !(d->coarse_dx > 0) || !(d->coarse_dy > 0) || !(d->soar_L > 0))
+        return set_error(GOC_ERR_ARG, "%s: bad coarse grid", who);
+    if (!d->random || !d->coarse) return set_error(GOC_ERR_ARG, "%s: null random/coarse buffer", who);
+    if (d->coarse_pitch < (d->coarse_nx + 4) * 4 || d->random_pitch < 4)
+        return set_error(GOC_ERR_ARG, "%s: pitch too small", who);
+    if (d->interpolation_factor < 1) return set_error(GOC_ERR_ARG, "%s: interpolation factor must be >= 1", who);
+    return GOC_OK;
+}
+
+extern "C" int goc_lcg_fill(int seed_nx, int seed_ny, int random_nx, unsigned long long* seeds, int seed_pitch,
+                            float* random, int random_pitch, int normal, void* stream) {
+    if (seed_nx < 1 || seed_ny < 1 || random_nx < 1 || random_nx > 2 * seed_nx || !seeds || !random ||
+        seed_pitch < seed_nx * 8 || random_pitch < random_nx * 4 || seed_pitch % 8 || random_pitch % 4)
+        return set_error(GOC_ERR_ARG, "goc_lcg_fill: bad arguments");
+    dim3 blk(16, 16), grd((seed_nx + 15) / 16, (seed_ny + 15) / 16);
+    lcg_kernel<<<grd, blk, 0, as_stream(stream)>>>(seed_nx, seed_ny, random_nx, seeds, seed_pitch / 8, random,
+                                                   random_pitch / 4, normal);
+    count_launch();
+    return check_launch("lcg_kernel");
+}
+
+extern "C" size_t goc_xorwow_state_bytes(int n) { return (size_t)(n > 0 ? n : 0) * sizeof(curandStateXORWOW_t); }
+
+extern "C" int goc_xorwow_init(void* states, int n, unsigned long long seed, void* stream) {
+    if (!states || n < 1) return set_error(GOC_ERR_ARG, "goc_xorwow_init: bad arguments");
+    xorwow_init_kernel<<<(n + 127) / 128, 128, 0, as_stream(stream)>>>((curandStateXORWOW_t*)states, n, seed);
+    count_launch();
+    return check_launch("xorwow_init_kernel");
+}
+
+extern "C" int goc_xorwow_normal(void* states, int nx, int ny, float* random, int random_pitch, void* stream) {
+    if (!states || !random || nx < 1 || ny < 1 || random_pitch < nx * 4 || random_pitch % 4)
+        return set_error(GOC_ERR_ARG, "goc_xorwow_normal: bad arguments");
+    const int n = nx * ny;
+    xorwow_normal_kernel<<<(n + 127) / 128, 128, 0, as_stream(stream)>>>((curandStateXORWOW_t*)states, nx, ny,
+                                                                         random, random_pitch / 4);
+    count_launch();
+    return check_launch("xorwow_normal_kernel");
+}
+
+extern "C" int goc_soar(const GocNoiseDesc* d, float perturbation_scale, int additive, void* stream) {
+    int rc = check_noise(d, "goc_soar");
+    if (rc) return rc;
+    dim3 blk(kNB, kNB), grd((d->coarse_nx + 4 + kNB - 1) / kNB, (d->coarse_ny + 4 + kNB - 1) / kNB);
+    soar_kernel<<<grd, blk, 0, as_stream(stream)>>>(*d, perturbation_scale, additive);
+    count_launch();
+    return check_launch("soar_kernel");
+}
+
+static int make_ocean(int nx, int ny, float dx, float dy, float* eta, float* hu, float* hv, int pitch,
+                      const float* Hi, int Hi_pitch, float land, int images_ns, int images_ew, OceanRef* o,
+                      const char* who) {
+    if (nx < 1 || ny < 1 || !eta || !hu || !hv || !Hi) return set_error(GOC_ERR_ARG, "%s: bad ocean arguments", who);
+    if (pitch < (nx + 4) * 4 || Hi_pitch < (nx + 5) * 4 || pitch % 4 || Hi_pitch % 4)
+        return set_error(GOC_ERR_ARG, "%s: pitch too small", who);
+    if ((images_ns && ny < 4) || (images_ew && nx < 4))
+        return set_error(GOC_ERR_ARG, "%s: periodic directions need at least 4 cells", who);
+    *o = OceanRef{nx, ny, dx, dy, eta, hu, hv, pitch / 4, Hi, Hi_pitch / 4, land, images_ns, images_ew};
+    return GOC_OK;
+}
+
+extern "C" int goc_perturb_ocean(const GocNoiseDesc* d, int nx, int ny, float dx, float dy, float* eta, float* hu,
+                                 float* hv, int pitch, const float* Hi, int Hi_pitch, float land_value,
+                                 int periodic_ghosts, void* stream) {
+    int rc = check_noise(d, "goc_perturb_ocean");
+    if (rc) return rc;
+    OceanRef o;
+    if ((rc = make_ocean(nx, ny, dx, dy, eta, hu, hv, pitch, Hi, Hi_pitch, land_value,
+                         periodic_ghosts && d->periodic_ns, periodic_ghosts && d->periodic_ew, &o, "goc_perturb_ocean")))
+        return rc;
+    dim3 blk(kNB, kNB), grd((nx + kNB - 1) / kNB, (ny + kNB - 1) / kNB);
+    perturb_kernel<<<grd, blk, 0, as_stream(stream)>>>(*d, o);
+    count_launch();
+    return check_launch("perturb_kernel");
+}
+
+// ---------------------------------------------------------------------------
+// batched handle
+// ---------------------------------------------------------------------------
+
+struct NoiseBatch {
+    int n = 0;
+    GocNoiseDesc* d_noise = nullptr;
+    int4* d_soar_items = nullptr;
+    int4* d_pert_items = nullptr;
+    int4* d_rng_chunks = nullptr;
+    curandStateXORWOW_t* d_states = nullptr;
+    int n_soar = 0, n_pert = 0, n_rng = 0, n_states = 0;
+};
+
+extern "C" int goc_noise_batch_create(void* ensemble, const GocNoiseDesc* noise, void** out) {
+    if (!out || !noise || !ensemble) return set_error(GOC_ERR_ARG, "goc_noise_batch_create: bad arguments");
+    *out = nullptr;
+    int n_members = 0;
+    const GocMemberDesc* members = ensemble_host_members(ensemble, &n_members);
+    NoiseBatch* b = new NoiseBatch();
+    b->n = n_members;
+    std::vector<int4> soar, pert, rng;
+    int states = 0;
+    for (int m = 0; m < n_members; ++m) {
+        int rc = check_noise(&noise[m], "goc_noise_batch_create");
+        const GocMemberDesc& md = members[m];
+        if (!rc && noise[m].interpolation_factor <= 1 &&
+            (noise[m].coarse_nx != md.p.nx || noise[m].coarse_ny != md.p.ny))
+            rc = set_error(GOC_ERR_ARG, "goc_noise_batch_create: member %d: factor 1 needs the coarse grid = the grid", m);
+        if (rc) {
+            delete b;
+            return rc;
+        }
+        for (int j = 0; j < (noise[m].coarse_ny + 4 + kNB - 1) / kNB; ++j)
+            for (int i = 0; i < (noise[m].coarse_nx + 4 + kNB - 1) / kNB; ++i) soar.push_back(make_int4(m, i, j, 0));
+        for (int j = 0; j < (md.p.ny + kNB - 1) / kNB; ++j)
+            for (int i = 0; i < (md.p.nx + kNB - 1) / kNB; ++i) pert.push_back(make_int4(m, i, j, 0));
+        const int rnx = noise[m].periodic_ew ? noise[m].coarse_nx : noise[m].coarse_nx + 8;
+        const int rny = noise[m].periodic_ns ? noise[m].coarse_ny : noise[m].coarse_ny + 8;
+        for (int f = 0; f < rnx * rny; f += 256) {
+            const int cnt = std::min(256, rnx * rny - f);
+            rng.push_back(make_int4(m, f, cnt, states));
+            states += cnt;
+        }
+    }
+    b->n_soar = (int)soar.size();
+    b->n_pert = (int)pert.size();
+    b->n_rng = (int)rng.size();
+    b->n_states = states;
+    cudaError_t e = cudaMalloc(&b->d_noise, sizeof(GocNoiseDesc) * n_members);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_soar_items, sizeof(int4) * soar.size());
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_pert_items, sizeof(int4) * pert.size());
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_rng_chunks, sizeof(int4) * rng.size());
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_noise, noise, sizeof(GocNoiseDesc) * n_members, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_soar_items, soar.data(), sizeof(int4) * soar.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_pert_items, pert.data(), sizeof(int4) * pert.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_rng_chunks, rng.data(), sizeof(int4) * rng.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(b->d_noise); cudaFree(b->d_soar_items); cudaFree(b->d_pert_items); cudaFree(b->d_rng_chunks);
+        delete b;
+        return set_error(GOC_ERR_CUDA, "goc_noise_batch_create: %s", cudaGetErrorString(e));
+    }
+    *out = b;
+    return GOC_OK;
+}
+
+extern "C" int goc_noise_batch_destroy(void* batch) {
+    if (!batch) return GOC_OK;
+    NoiseBatch* b = static_cast<NoiseBatch*>(batch);
+    cudaFree(b->d_noise);
+    cudaFree(b->d_soar_items);
+    cudaFree(b->d_pert_items);
+    cudaFree(b->d_rng_chunks);
+    cudaFree(b->d_states);
+    delete b;
+    return GOC_OK;
+}
+
+extern "C" int goc_noise_batch_seed(void* batch, unsigned long long seed, void* stream) {
+    if (!batch) return set_error(GOC_ERR_ARG, "goc_noise_batch_seed: null handle");
+    NoiseBatch* b = static_cast<NoiseBatch*>(batch);
+    if (!b->d_states) {
+        cudaError_t e = cudaMalloc(&b->d_states, sizeof(curandStateXORWOW_t) * (size_t)b->n_states);
+        if (e != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_noise_batch_seed: %s", cudaGetErrorString(e));
+    }
+    xorwow_batched_init_kernel<<<(b->n_states + 127) / 128, 128, 0, as_stream(stream)>>>(b->d_states, b->n_states, seed);
+    count_launch();
+    return check_launch("xorwow_batched_init_kernel");
+}
+
+extern "C" int goc_noise_batch_generate(void* batch, void* ensemble, int substep, void* stream) {
+    if (!batch || !ensemble) return set_error(GOC_ERR_ARG, "goc_noise_batch_generate: null handle");
+    NoiseBatch* b = static_cast<NoiseBatch*>(batch);
+    if (!b->d_states) return set_error(GOC_ERR_ARG, "goc_noise_batch_generate: call goc_noise_batch_seed first");
+    xorwow_batched_kernel<<<b->n_rng, 256, 0, as_stream(stream)>>>(b->d_noise, b->d_rng_chunks, b->d_states,
+                                                                 ensemble_device_nsub(ensemble), substep);
+    count_launch();
+    return check_launch("xorwow_batched_kernel");
+}
+
+extern "C" int goc_noise_batch_perturb(void* batch, void* ensemble, float perturbation_scale, int substep,
+                                       void* stream) {
+    if (!batch || !ensemble) return set_error(GOC_ERR_ARG, "goc_noise_batch_perturb: null handle");
+    NoiseBatch* b = static_cast<NoiseBatch*>(batch);
+    int n = 0;
+    ensemble_host_members(ensemble, &n);
+    if (n != b->n) return set_error(GOC_ERR_ARG, "goc_noise_batch_perturb: ensemble has %d members, batch %d", n, b->n);
+    cudaStream_t st = as_stream(stream);
+    const int* nsub = ensemble_device_nsub(ensemble);
+    soar_batched_active_kernel<<<b->n_soar, dim3(kNB, kNB), 0, st>>>(b->d_noise, b->d_soar_items, nsub, substep,
+                                                                     perturbation_scale);
+    count_launch();
+    int rc = check_launch("soar_batched_active_kernel");
+    if (rc) return rc;
+    perturb_batched_kernel<<<b->n_pert, dim3(kNB, kNB), 0, st>>>(b->d_noise, ensemble_device_members(ensemble),
+                                                                  b->d_pert_items, nsub, substep);
+    count_launch();
+    return check_launch("perturb_batched_kernel");
+}

@@ -1,0 +1,302 @@
+"""Batched ensemble engine over CDKLM16 members.
+
+The reference steps its ensembles member by member from Python
+(E/OceanNoiseEnsemble.py:517-543, E/OceanModelEnsemble.py:138-150,
+E/MultiLevelOceanEnsemble.py:95-141; E/ = src/gpuocean/ensembles), which
+costs (members x kernels) launches per time step.  Here every member - of
+any grid size - advances in one persistent launch per RK2 step over a
+member/tile work queue, and a block of steps is replayed as one CUDA graph.
+
+Per member the step sequence is exactly that of ``CDKLM16.step(t_end)``
+(S/CDKLM16.py:493-509): local_dt = float32(min(dt, float32(t_end - t_now))),
+t_now advanced in float64.  Members keep their own dt, so they may take
+different numbers of steps; a member whose block is done idles.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from .. import _lib
+from ..utils import Common
+
+
+class GocMemberDesc(ctypes.Structure):
+    """Mirror of ``GocMemberDesc`` in include/gpuocean_gb300.h."""
+    _fields_ = [
+        ("p", _lib.GocCdklmParams),
+        ("Hi", ctypes.c_void_p), ("Hi_pitch", ctypes.c_int32),
+        ("Hm", ctypes.c_void_p), ("Hm_pitch", ctypes.c_int32),
+        ("eta", ctypes.c_void_p * 2), ("hu", ctypes.c_void_p * 2), ("hv", ctypes.c_void_p * 2),
+        ("pitch", ctypes.c_int32),
+    ]
+
+
+def step_schedule(dt, t_end):
+    """The dt sequence of one ``step(t_end)`` call (S/CDKLM16.py:493-509)."""
+    out = []
+    t_now = 0.0
+    while t_now < t_end:
+        local_dt = np.float32(min(dt, np.float32(t_end - t_now)))
+        out.append(local_dt)
+        t_now += np.float64(local_dt)
+    return out
+
+
+class BatchedEnsemble:
+    """Steps a list of RK2 ``CDKLM16`` simulators together on one GPU stream.
+
+    share_bathymetry: point members with identical corner depths at one copy
+    (None = detect by comparing the device arrays once).
+    use_graph: replay each distinct block schedule as a CUDA graph.
+    """
+
+    def __init__(self, sims, share_bathymetry=None, use_graph=True, stream=None):
+        assert len(sims) > 0
+        for s in sims:
+            assert int(s.rk_order) == 2, "the batched engine runs the fused RK2 step"
+        self.sims = list(sims)
+        self.stream = stream if stream is not None else Common.Stream()
+        self.use_graph = use_graph
+        self.kernels_launched = 0
+        self._graphs = {}
+        self._handle = None
+        self._noise = None
+        self._noises = None
+        self._rng_seed = None
+        self._bathy_owner = list(range(len(sims)))
+        if share_bathymetry is None:
+            share_bathymetry = True
+        if share_bathymetry:
+            self._dedupe_bathymetry()
+        self._build()
+
+    # ------------------------------------------------------------------
+    def _dedupe_bathymetry(self):
+        seen = {}
+        for m, s in enumerate(self.sims):
+            Bi = np.ma.getdata(s.bathymetry.Bi.download(s.gpu_stream))
+            key = (Bi.shape, Bi.tobytes().__hash__(), int(s.boundary_conditions.north), int(s.boundary_conditions.east))
+            if key in seen and np.array_equal(seen[key][1], Bi):
+                self._bathy_owner[m] = seen[key][0]
+            else:
+                seen[key] = (m, Bi)
+
+    def _descs(self):
+        descs = (GocMemberDesc * len(self.sims))()
+        for m, s in enumerate(self.sims):
+            d = descs[m]
+            s._params = s._make_params()
+            d.p = s._params
+            b = self.sims[self._bathy_owner[m]].bathymetry
+            d.Hi, d.Hi_pitch = b.Bi.ptr, int(b.Bi.pitch)
+            d.Hm, d.Hm_pitch = b.Bm.ptr, int(b.Bm.pitch)
+            g = s.gpu_data
+            d.eta[0], d.eta[1] = g.h0.ptr, g.h1.ptr
+            d.hu[0], d.hu[1] = g.hu0.ptr, g.hu1.ptr
+            d.hv[0], d.hv[1] = g.hv0.ptr, g.hv1.ptr
+            d.pitch = int(g.h0.pitch)
+        return descs
+
+    def _current_ptrs(self):
+        return tuple(s.gpu_data.h0.ptr for s in self.sims)
+
+    def _build(self, max_substeps=8):
+        self.release()
+        self._descs_host = self._descs()
+        h = ctypes.c_void_p()
+        _lib.call("goc_ensemble_create", self._descs_host, len(self.sims), int(max_substeps), ctypes.byref(h))
+        self._handle = h.value
+        self.max_substeps = int(max_substeps)
+        self._ptrs = self._current_ptrs()
+        self._graphs = {}
+        self._sched_key = None
+        self._dt_dev = Common.DevicePtr(4 * len(self.sims))
+        self._attach_drifters()
+        if getattr(self, "_noises", None) is not None:
+            self.set_noise(self._noises, getattr(self, "_random_pool", None))
+
+    def _attach_drifters(self):
+        """Drifter collections attached to the members are advected inside
+        the batched step (wind drift is not applied there)."""
+        ptrs = (ctypes.c_void_p * len(self.sims))()
+        counts = np.zeros(len(self.sims), dtype=np.int32)
+        sens = 1.0
+        self.has_drifters = False
+        for m, s in enumerate(self.sims):
+            d = s.drifters if s.hasDrifters else None
+            if d is not None and hasattr(d, "driftersDevice"):
+                if d.wind_drift_factor:
+                    raise NotImplementedError("wind drift of drifters is not applied by the batched engine")
+                ptrs[m] = d.driftersDevice.ptr
+                counts[m] = d.getNumDrifters()
+                sens = d.sensitivity
+                self.has_drifters = True
+        if self.has_drifters:
+            _lib.call("goc_ensemble_set_drifters", self._handle, ptrs, counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                      ctypes.c_float(sens), self.stream.handle)
+
+    def release(self):
+        self.release_noise()
+        for g in getattr(self, "_graphs", {}).values():
+            _lib.load().goc_graph_destroy(g[0])
+        self._graphs = {}
+        if getattr(self, "_handle", None):
+            _lib.load().goc_ensemble_destroy(self._handle)
+            self._handle = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+    @property
+    def n_tiles(self):
+        nm, nt = ctypes.c_int(), ctypes.c_int()
+        _lib.call("goc_ensemble_size", self._handle, ctypes.byref(nm), ctypes.byref(nt))
+        return nt.value
+
+    # ------------------------------------------------------------------
+    def _schedule(self, t_end):
+        scheds = [step_schedule(s.dt, t_end) for s in self.sims]
+        nsub = max(len(x) for x in scheds)
+        if nsub > self.max_substeps or self._current_ptrs() != self._ptrs:
+            # members stepped on their own, or a longer block: rebuild the table
+            self._build(max_substeps=max(nsub, self.max_substeps))
+        table = np.zeros((len(self.sims), self.max_substeps), dtype=np.float32)
+        n = np.zeros(len(self.sims), dtype=np.int32)
+        for m, sc in enumerate(scheds):
+            table[m, :len(sc)] = sc
+            n[m] = len(sc)
+        return scheds, table, n, nsub
+
+    # ------------------------------------------------------------------
+    def set_noise(self, noises, random_pool=None, rng_seed=None):
+        """Model error of every member in two launches per perturbation.
+
+        noises: one OceanStateNoise per member.  random_pool: optional device
+        array holding every member's random field back to back (one upload
+        refreshes them all); by default each member's own buffer is used.
+        rng_seed: draw fresh XORWOW normals on the device before every
+        perturbation (otherwise the random fields are used as they are, e.g.
+        injected from the host).
+        """
+        from ..SWEsimulators.OceanStateNoise import GocNoiseDesc
+        assert len(noises) == len(self.sims)
+        descs = (GocNoiseDesc * len(self.sims))()
+        off = 0
+        for m, (n, s) in enumerate(zip(noises, self.sims)):
+            d = n.descriptor(s.f, s.coriolis_beta, s.g)
+            if random_pool is not None:
+                d.random = random_pool.ptr + off
+                off += int(n.rand_ny) * int(n.random_numbers.pitch)
+            descs[m] = d
+        if random_pool is not None:
+            assert off <= random_pool.nbytes, "random pool too small"
+        self._random_pool = random_pool
+        self.release_noise()
+        h = ctypes.c_void_p()
+        _lib.call("goc_noise_batch_create", self._handle, descs, ctypes.byref(h))
+        self._noise = h.value
+        self._noise_descs = descs
+        self._noises = noises
+        self._rng_seed = rng_seed
+        if rng_seed is not None:
+            _lib.call("goc_noise_batch_seed", self._noise, ctypes.c_ulonglong(int(rng_seed)), self.stream.handle)
+        for g in self._graphs.values():
+            _lib.load().goc_graph_destroy(g[0])
+        self._graphs = {}
+
+    def release_noise(self):
+        if getattr(self, "_noise", None):
+            _lib.load().goc_noise_batch_destroy(self._noise)
+            self._noise = None
+
+    def _noise_launch(self, substep, scale=1.0, update_random_field=True):
+        if update_random_field and self._rng_seed is not None:
+            _lib.call("goc_noise_batch_generate", self._noise, self._handle, int(substep), self.stream.handle)
+        _lib.call("goc_noise_batch_perturb", self._noise, self._handle, ctypes.c_float(scale), int(substep),
+                  self.stream.handle)
+
+    def perturb(self, perturbation_scale=1.0, update_random_field=True):
+        """Add the SOAR model error to every member's current state."""
+        before = _lib.load().goc_kernel_launch_count()
+        self._noise_launch(-1, perturbation_scale, update_random_field)
+        self.kernels_launched += _lib.load().goc_kernel_launch_count() - before
+
+    def _launch_block(self, nsub, noise=None):
+        """noise: None, "block" (once after the block) or "step" (after every
+        RK2 step of each member, before its drifters move)."""
+        before = _lib.load().goc_kernel_launch_count()
+        for k in range(nsub):
+            _lib.call("goc_ensemble_rk2_substep", self._handle, k, self.stream.handle)
+            if noise == "step":
+                self._noise_launch(k)
+        _lib.call("goc_ensemble_end_block", self._handle, int(nsub), self.stream.handle)
+        if noise == "block":
+            self._noise_launch(-1)
+        return _lib.load().goc_kernel_launch_count() - before
+
+    def step(self, t_end, apply_stochastic_term=False, noise_cadence="block"):
+        """Advance every member by ``t_end`` seconds (one block).  With
+        ``apply_stochastic_term`` the model error is added either once after
+        the block (``noise_cadence="block"``, the ``dataAssimilationStep``
+        cadence, S/CDKLM16.py:786-790) or after every RK2 step
+        (``"step"``, the cadence of ``CDKLM16.step``, S/CDKLM16.py:567-568).
+        Returns the number of member-cell-steps taken."""
+        assert noise_cadence in ("block", "step")
+        with_noise = noise_cadence if (apply_stochastic_term and getattr(self, "_noise", None) is not None) else None
+        for s in self.sims:
+            if s.t == 0:
+                s.bc_kernel.boundaryCondition(s.gpu_stream, s.gpu_data.h0, s.gpu_data.hu0, s.gpu_data.hv0)
+                s.gpu_stream.synchronize()
+        for s in self.sims:
+            if s.hasDrifters:
+                s.drifters.gpu_stream.synchronize()
+        scheds, table, n, nsub = self._schedule(t_end)
+        key = (n.tobytes(), table.tobytes())
+        if key != getattr(self, "_sched_key", None):
+            _lib.call("goc_ensemble_set_schedule", self._handle, table.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                      n.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), self.stream.handle)
+            self._sched_key = key
+        if self.use_graph:
+            entry = self._graphs.get((nsub, with_noise))
+            if entry is None:
+                _lib.call("goc_graph_begin_capture", self.stream.handle)
+                nodes = self._launch_block(nsub, with_noise)
+                gh = ctypes.c_void_p()
+                _lib.call("goc_graph_end_capture", self.stream.handle, ctypes.byref(gh))
+                entry = self._graphs[(nsub, with_noise)] = (gh.value, nodes)
+            _lib.call("goc_graph_launch", entry[0], self.stream.handle)
+            self.kernels_launched += entry[1]
+        else:
+            self.kernels_launched += self._launch_block(nsub, with_noise)
+        cells = 0
+        for m, s in enumerate(self.sims):
+            for local_dt in scheds[m]:
+                s.t += np.float64(local_dt)
+            s.num_iterations += len(scheds[m])
+            if s.hasDrifters:
+                s.drifter_t += sum(np.float64(x) for x in scheds[m])
+            if len(scheds[m]) % 2 == 1:
+                s.gpu_data.swap()
+            cells += len(scheds[m]) * int(s.nx) * int(s.ny)
+        self._ptrs = self._current_ptrs()
+        return cells
+
+    def synchronize(self):
+        self.stream.synchronize()
+
+    def updateDt(self, courant_number=None):
+        """Batched CFL limit of every member (one reduction launch pair)."""
+        _lib.call("goc_ensemble_max_dt", self._handle, self._dt_dev.ptr, self.stream.handle)
+        out = np.zeros(len(self.sims), dtype=np.float32)
+        _lib.call("goc_memcpy_d2h_async", out.ctypes.data, self._dt_dev.ptr, ctypes.c_size_t(out.nbytes),
+                  self.stream.handle)
+        self.stream.synchronize()
+        for s, v in zip(self.sims, out):
+            cn = s.courant_number if courant_number is None else courant_number
+            s.dt = cn * v
+        return out

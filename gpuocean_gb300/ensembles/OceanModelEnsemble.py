@@ -1,0 +1,139 @@
+"""Ensemble of CDKLM16 models built from simulator arguments
+(drop-in for ``ensembles/OceanModelEnsemble.py:34-218``).
+
+All members advance together through the batched engine: one persistent
+launch per RK2 step for the whole ensemble, SOAR model error for all members
+in two launches, drifters advected inside the step launch.
+"""
+from __future__ import annotations
+
+import logging
+
+import numpy as np
+
+from ..drifters.GPUDrifterCollection import GPUDrifterCollection
+from ..SWEsimulators import CDKLM16
+from .BatchedEnsemble import BatchedEnsemble
+
+
+class OceanModelEnsemble:
+    def __init__(self, gpu_ctx, sim_args, data_args, model_error_args, numParticles,
+                 observation_variance=0.01 ** 2, initialization_variance_factor_ocean_field=0.0,
+                 super_dir_name=None, netcdf_filename=None, rank=0, rng_seed=None):
+        self.logger = logging.getLogger(__name__)
+        self.gpu_ctx = gpu_ctx
+        self.sim_args, self.data_args = sim_args, data_args
+        self.numParticles = numParticles
+        self.observation_variance = observation_variance
+        self.initialization_variance_factor_ocean_field = initialization_variance_factor_ocean_field
+        if np.isscalar(observation_variance):
+            self.observation_cov = np.eye(2) * observation_variance
+            self.observation_cov_inverse = np.eye(2) * (1.0 / observation_variance)
+        else:
+            self.observation_cov = observation_variance
+            self.observation_cov_inverse = np.linalg.inv(observation_variance)
+        self.particles = [None] * numParticles
+        self.drifterForecast = [None] * numParticles
+        for i in range(numParticles):
+            self.particles[i] = CDKLM16.CDKLM16(gpu_ctx, **sim_args, **data_args, local_particle_id=i)
+            if 'small_scale_perturbation_amplitude' in model_error_args:
+                self.particles[i].setSOARModelError(**model_error_args)
+            elif model_error_args:
+                raise NotImplementedError("only SOAR model error is supported")
+            if initialization_variance_factor_ocean_field != 0.0:
+                self.particles[i].perturbState(q0_scale=initialization_variance_factor_ocean_field)
+        self.nx, self.ny = self.particles[0].nx, self.particles[0].ny
+        self.dx, self.dy = self.particles[0].dx, self.particles[0].dy
+        self.t = self.particles[0].t
+        self.particlesActive = [True] * numParticles
+        self.engine = None
+        self.rng_seed = rng_seed if rng_seed is not None else 1234 + 7919 * rank
+
+    def _engine(self):
+        if self.engine is None:
+            self.engine = BatchedEnsemble(self.particles)
+            if all(p.model_error is not None for p in self.particles):
+                self.engine.set_noise([p.model_error for p in self.particles], rng_seed=self.rng_seed)
+        return self.engine
+
+    def attachDrifters(self, drifter_positions):
+        for i in range(self.numParticles):
+            if len(drifter_positions) > 0:
+                d = GPUDrifterCollection(self.gpu_ctx, len(drifter_positions),
+                                         observation_variance=self.observation_variance,
+                                         boundaryConditions=self.data_args['boundary_conditions'],
+                                         domain_size_x=self.data_args['nx'] * self.data_args['dx'],
+                                         domain_size_y=self.data_args['ny'] * self.data_args['dy'])
+                d.setDrifterPositions(drifter_positions)
+                self.particles[i].attachDrifters(d)
+        if self.engine is not None:
+            self.engine._build(self.engine.max_substeps)
+
+    def cleanUp(self):
+        if self.engine is not None:
+            self.engine.release()
+        for p in self.particles:
+            if p is not None:
+                p.cleanUp(do_gc=False)
+
+    def stepToObservation(self, observation_time, write_now=False, courant_number=0.8):
+        """Advance to observation_time with model error after every
+        model_time_step, as CDKLM16.dataAssimilationStep does for each member
+        (S/CDKLM16.py:742-806), all members at once."""
+        eng = self._engine()
+        p0 = self.particles[0]
+        mts = p0.model_time_step
+        full = int(round(observation_time - p0.t) / mts)
+        leftover = observation_time - p0.t - full * mts
+        if leftover / mts < 0.1 and full > 1:
+            leftover += mts
+            full -= 1
+        if leftover / mts < 0.00001:
+            leftover = 0
+        assert full > 0, "There is less than CDKLM16.model_time_step until the observation"
+        eng.updateDt(courant_number=courant_number)
+        for i in range(full + 1):
+            if i == 0 and leftover == 0:
+                continue
+            if i == 0:
+                eng.step(leftover)
+                eng.perturb(perturbation_scale=np.sqrt(leftover / mts))
+            else:
+                eng.step(mts, apply_stochastic_term=eng._noise is not None)
+            for p in self.particles:
+                p.total_time_steps += 1
+            if p0.total_time_steps % 5 == 0:
+                eng.updateDt(courant_number=courant_number)
+        self.t = observation_time
+
+    def modelStep(self, sub_t, rank="", update_dt=True):
+        eng = self._engine()
+        eng.step(sub_t, apply_stochastic_term=eng._noise is not None, noise_cadence="step")
+        if update_dt:
+            eng.updateDt()
+        self.t = self.particles[0].t
+        return self.t
+
+    def updateDt(self):
+        self._engine().updateDt()
+
+    def observeParticles(self, drifter_positions):
+        """hu, hv at the cells of the given positions, (particles, drifters, 2)."""
+        n, nd = len(self.particles), len(drifter_positions)
+        out = np.empty((n, nd, 2))
+        ix = np.floor(np.asarray(drifter_positions)[:, 0] / self.data_args['dx']).astype(int)
+        iy = np.floor(np.asarray(drifter_positions)[:, 1] / self.data_args['dy']).astype(int)
+        for p in range(n):
+            eta, hu, hv = self.particles[p].download(interior_domain_only=True)
+            out[p, :, 0] = np.asarray(hu)[iy, ix]
+            out[p, :, 1] = np.asarray(hv)[iy, ix]
+        return out
+
+    def getNumParticles(self):
+        return self.numParticles
+
+    def syncGPU(self):
+        if self.engine is not None:
+            self.engine.synchronize()
+        for p in self.particles:
+            p.gpu_stream.synchronize()

@@ -1,0 +1,129 @@
+"""Ensemble of perturbed copies of one simulator plus a synthetic truth
+(drop-in for ``ensembles/OceanNoiseEnsemble.py:43-790``, drifter-position and
+direct-flow observations).
+
+The truth and all particles advance in one batched engine; the model error
+is applied after every RK2 step, as ``CDKLM16.step`` does.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from ..drifters.GPUDrifterCollection import GPUDrifterCollection
+from ..SWEsimulators import CDKLM16
+from .BatchedEnsemble import BatchedEnsemble
+
+
+class ObservationType:
+    DrifterPosition = 1
+    UnderlyingFlow = 2
+    DirectUnderlyingFlow = 3
+    StaticBuoys = 4
+
+
+class OceanNoiseEnsemble:
+    def __init__(self, gpu_ctx, numParticles, sim, num_drifters=1, observation_type=ObservationType.DrifterPosition,
+                 buoys_positions=None, observation_variance=None, observation_variance_factor=5.0,
+                 initialization_variance_factor_drifter_position=0.0, initialization_variance_factor_ocean_field=0.0,
+                 compensate_for_eta=True, ensemble_small_scale_perturbation=True, rng_seed=2024):
+        self.gpu_ctx = gpu_ctx
+        self.numParticles = numParticles
+        self.particles = [None] * (numParticles + 1)
+        self.particlesActive = [True] * numParticles
+        self.obs_index = numParticles
+        self.t = 0.0
+        self.observation_type = observation_type
+        self.observedDrifterPositions = []
+        eta, hu, hv = sim.download()
+        Hi = sim.downloadBathymetry()[0]
+        self.nx, self.ny, self.dx, self.dy, self.dt = sim.nx, sim.ny, sim.dx, sim.dy, sim.dt
+        self.boundaryConditions = sim.boundary_conditions
+        self.g, self.f, self.beta, self.r = sim.g, sim.f, sim.coriolis_beta, sim.r
+        self.observation_variance = (observation_variance_factor * self.dx) ** 2 if observation_variance is None \
+            else observation_variance
+        self.observation_cov = np.eye(2) * self.observation_variance
+        self.observation_cov_inverse = np.eye(2) * (1.0 / self.observation_variance)
+        self.initialization_cov_drifters = np.eye(2) * initialization_variance_factor_drifter_position * self.dx
+        self.driftersPerOceanModel = np.int32(num_drifters)
+        me = sim.model_error
+        # sim.f is already compensated for the first interior cell; pass it back uncompensated
+        f_in = float(sim.f) + float(sim.coriolis_beta) * 2 * float(sim.dy)
+        for i in range(numParticles + 1):
+            p = CDKLM16.CDKLM16(gpu_ctx, eta, hu, hv, Hi, self.nx, self.ny, self.dx, self.dy, self.dt, self.g,
+                                f_in, self.r, coriolis_beta=self.beta, boundary_conditions=self.boundaryConditions)
+            if me is not None:
+                p.setSOARModelError(small_scale_perturbation_amplitude=me.soar_q0,
+                                    small_scale_perturbation_interpolation_factor=int(me.interpolation_factor))
+            if initialization_variance_factor_ocean_field != 0.0:
+                p.perturbState(perturbation_scale=initialization_variance_factor_ocean_field)
+            d = GPUDrifterCollection(gpu_ctx, int(num_drifters), observation_variance=self.observation_variance,
+                                     boundaryConditions=self.boundaryConditions,
+                                     initialization_cov_drifters=self.initialization_cov_drifters,
+                                     domain_size_x=self.nx * self.dx, domain_size_y=self.ny * self.dy)
+            if buoys_positions is not None:
+                d.setDrifterPositions(buoys_positions)
+            else:
+                d.uniformly_distribute_drifters(initialization_cov_drifters=self.initialization_cov_drifters)
+            p.attachDrifters(d)
+            self.particles[i] = p
+        self.engine = BatchedEnsemble(self.particles)
+        if me is not None:
+            self.engine.set_noise([p.model_error for p in self.particles], rng_seed=rng_seed)
+        self._addObservation(self.observeTrueDrifters())
+
+    def cleanUp(self):
+        self.engine.release()
+        for p in self.particles:
+            if p is not None:
+                p.cleanUp(do_gc=False)
+
+    def _addObservation(self, positions):
+        self.observedDrifterPositions.append([self.t, positions])
+
+    def step(self, t, stochastic_particles=True, stochastic_truth=True):
+        """All particles and the truth advance by t (S/.../OceanNoiseEnsemble.py:517-532)."""
+        if stochastic_particles != stochastic_truth:
+            raise NotImplementedError("truth and particles share one batched step")
+        self.engine.step(t, apply_stochastic_term=stochastic_particles, noise_cadence="step")
+        self.t = self.particles[self.obs_index].t
+        return self.t
+
+    def observeDrifters(self):
+        out = np.empty((self.numParticles, self.driftersPerOceanModel, 2))
+        for p in range(self.numParticles):
+            out[p] = self.particles[p].drifters.getDrifterPositions()
+        return out
+
+    def observeTrueDrifters(self):
+        return self.particles[self.obs_index].drifters.getDrifterPositions()
+
+    def observeTrueState(self):
+        if self.observedDrifterPositions[-1][0] != self.t:
+            self._addObservation(self.observeTrueDrifters())
+        if self.observation_type == ObservationType.DrifterPosition:
+            return self.observedDrifterPositions[-1][1]
+        eta, hu, hv = self.downloadTrueOceanState()
+        pos = self.observedDrifterPositions[-1][1]
+        ix = np.floor(pos[:, 0] / self.dx).astype(int)
+        iy = np.floor(pos[:, 1] / self.dy).astype(int)
+        return np.stack([pos[:, 0], pos[:, 1], np.asarray(hu)[iy, ix], np.asarray(hv)[iy, ix]], axis=1)
+
+    def getDistances(self, obs=None):
+        obs = self.observeTrueDrifters() if obs is None else obs
+        return np.array([np.linalg.norm(self.particles[p].drifters.getDrifterPositions() - obs, axis=1).mean()
+                         for p in range(self.numParticles)])
+
+    def downloadParticleOceanState(self, particleNo):
+        return self.particles[particleNo].download(interior_domain_only=True)
+
+    def downloadTrueOceanState(self):
+        return self.particles[self.obs_index].download(interior_domain_only=True)
+
+    def getNumParticles(self):
+        return self.numParticles
+
+    def getNx(self):
+        return self.nx
+
+    def getNy(self):
+        return self.ny

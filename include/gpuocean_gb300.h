@@ -60,6 +60,10 @@ typedef struct GocCdklmParams {
     int32_t bc_north, bc_east, bc_south, bc_west;
     float land_value;               /* corner depth that marks land (1e20) */
     const float* coriolis_f; int32_t coriolis_nx, coriolis_ny;
+    /* optional: the texture evaluated at every cell centre, (ny+4) x (nx+4)
+     * with pitch coriolis_cell_pitch bytes (goc_cell_texture); NULL = look
+     * the texture up in the kernel */
+    const float* coriolis_cell; int32_t coriolis_cell_pitch;
     const float* angle;      int32_t angle_nx, angle_ny;
     const float* wind_x_cur; const float* wind_x_next; int32_t wind_x_nx, wind_x_ny;
     const float* wind_y_cur; const float* wind_y_next; int32_t wind_y_nx, wind_y_ny;
@@ -108,12 +112,14 @@ int64_t goc_kernel_launch_count(void);
  * Reads Q^n from (eta0, hu0, hv0), writes Q^{n+1} into (eta1, hu1, hv1):
  * interior cells, and for periodic boundaries also the ghost images.  The
  * two buffer sets must not overlap (the caller swaps them after the call).
- * Hi: corner depths after goc_bathymetry_init.
+ * Hi, Hm: corner depths and cell means from goc_bathymetry_init (the
+ * reference kernel takes the same pair, Hi_ptr_/Hm_ptr_).
  */
 int goc_cdklm_rk2_step(const GocCdklmParams* p, float dt,
                        const float* eta0, const float* hu0, const float* hv0,
                        float* eta1, float* hu1, float* hv1, int pitch,
-                       const float* Hi, int Hi_pitch, void* stream);
+                       const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch,
+                       void* stream);
 
 /*
  * One Runge-Kutta stage, reference semantics: cdklm_swe_2D
@@ -127,7 +133,17 @@ int goc_cdklm_stage(const GocCdklmParams* p, float dt, int rk_step,
                     const float* eta_in, const float* hu_in, const float* hv_in,
                     float* eta_out, float* hu_out, float* hv_out,
                     float* eta_alt, float* hu_alt, float* hv_alt, int pitch,
-                    const float* Hi, int Hi_pitch, void* stream);
+                    const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch,
+                    void* stream);
+
+/*
+ * Evaluate a texture at every cell centre of an (ny+4) x (nx+4) grid,
+ * s = (i+0.5)/(nx+4), t = (j+0.5)/(ny+4), with the kernels' bilinear lookup
+ * (the positions coriolisF uses, K/CDKLM16_kernel.cu:49-57).  Fills
+ * GocCdklmParams.coriolis_cell.
+ */
+int goc_cell_texture(const float* tex, int tex_nx, int tex_ny, int nx, int ny,
+                     float* out, int out_pitch, void* stream);
 
 /*
  * Periodic ghost-cell fill, north/south before east/west.
@@ -162,6 +178,171 @@ int goc_max_dt(int nx, int ny, float dx, float dy, float g,
                const float* eta, const float* hu, const float* hv, int pitch,
                const float* Hm, int Hm_pitch, float land_value,
                float* partials, int partials_capacity, float* dt_out, void* stream);
+
+/* ---------------- drifters ---------------------------------------------- */
+
+/*
+ * Advect num_drifters + 1 positions (the last is the observation) by one
+ * forward-Euler step with cell-centred bilinear velocities hu/(Hm + eta),
+ * optional wind drift and periodic wrap.  Replaces passiveDrifterKernel
+ * (K/driftKernels.cu:74-183) as launched by GPUDrifterCollection.drift
+ * (D/GPUDrifterCollection.py:210-233, prepared "iifffiiPiPiPiPiiiiPifPPPPff").
+ * Cell indices outside the grid are clamped.
+ */
+int goc_drift(int nx, int ny, float dx, float dy, float dt, int x_zero_ref, int y_zero_ref,
+              const float* eta, const float* hu, const float* hv, int pitch,
+              const float* Hm, int Hm_pitch, int periodic_north_south, int periodic_east_west,
+              int num_drifters, float* positions, int positions_pitch, float sensitivity,
+              const float* wind_x_cur, const float* wind_x_next,
+              const float* wind_y_cur, const float* wind_y_next, int wind_nx, int wind_ny,
+              float wind_t, float wind_drift_factor, void* stream);
+
+/* Periodic wrap of drifter positions; replaces enforceBoundaryConditions
+ * (K/driftKernels.cu:187-223). */
+int goc_drift_enforce_boundary(float domain_size_x, float domain_size_y, int periodic_north_south,
+                               int periodic_east_west, int num_drifters, float* positions,
+                               int positions_pitch, void* stream);
+
+/* ---------------- stochastic model error (SOAR) --------------------------- */
+
+/*
+ * One SOAR model-error configuration (S/OceanStateNoise.py:47-272): a
+ * coarse grid with interpolation_factor cells per coarse cell, a random
+ * field of (cny, cnx) normals in each periodic direction and (cny+8, cnx+8)
+ * otherwise, and the (cny+4, cnx+4) coarse buffer the SOAR field goes to.
+ * f, beta, g, north_x/y feed the geostrophic balance
+ * (K/ocean_noise.cu:361-378); with f == 0 the Coriolis texture is used.
+ */
+typedef struct GocNoiseDesc {
+    int32_t coarse_nx, coarse_ny;
+    float coarse_dx, coarse_dy;
+    float soar_q0, soar_L;
+    int32_t periodic_ns, periodic_ew;
+    int32_t interpolation_factor;
+    int32_t offset_i, offset_j;        /* coarse-grid alignment offsets */
+    const float* random; int32_t random_pitch;   /* bytes */
+    float* coarse; int32_t coarse_pitch;         /* bytes */
+    float f, beta, g;
+    float north_x, north_y;
+    const float* coriolis_f; int32_t coriolis_nx, coriolis_ny;
+} GocNoiseDesc;
+
+/* LCG draws (K/random_number_generators.cu:58-134 uniformDistribution /
+ * normalDistribution, launched by U/RandomNumbers.py:165-185): each uint64
+ * seed advances twice and gives two numbers; normal = Box-Muller. */
+int goc_lcg_fill(int seed_nx, int seed_ny, int random_nx, unsigned long long* seeds, int seed_pitch,
+                 float* random, int random_pitch, int normal, void* stream);
+
+/* curand XORWOW normals, the reference's default generator
+ * (U/RandomNumbers.py:86-97 via pycuda.curandom).  `states` holds
+ * goc_xorwow_state_bytes(nx*ny) bytes. */
+size_t goc_xorwow_state_bytes(int n);
+int goc_xorwow_init(void* states, int n, unsigned long long seed, void* stream);
+int goc_xorwow_normal(void* states, int nx, int ny, float* random, int random_pitch, void* stream);
+
+/* SOAR-correlated coarse field from the random field
+ * (K/ocean_noise.cu:141-247, S/OceanStateNoise.py:394-416). */
+int goc_soar(const GocNoiseDesc* noise, float perturbation_scale, int additive, void* stream);
+
+/* Add the coarse field (bicubic up-sampled for factors > 1) and its
+ * geostrophically balanced momentum to the interior of (eta, hu, hv);
+ * replaces geostrophicBalance / bicubicInterpolation (K/ocean_noise.cu:256-666,
+ * S/OceanStateNoise.py:418-459).  periodic_ghosts = 1 also refreshes the
+ * periodic ghost images of the perturbed cells. */
+int goc_perturb_ocean(const GocNoiseDesc* noise, int nx, int ny, float dx, float dy,
+                      float* eta, float* hu, float* hv, int pitch, const float* Hi, int Hi_pitch,
+                      float land_value, int periodic_ghosts, void* stream);
+
+/* ---------------- batched ensemble engine -------------------------------- */
+
+/*
+ * One ensemble member: parameters, bathymetry and its two state buffer
+ * sets.  Members may differ in grid size, spacing, physics and boundaries.
+ * Replaces the per-member simulator objects that the reference's ensembles
+ * step in Python loops (E/OceanNoiseEnsemble.py:517-543,
+ * E/OceanModelEnsemble.py:138-150, E/MultiLevelOceanEnsemble.py:95-141;
+ * E/ = src/gpuocean/ensembles).
+ */
+typedef struct GocMemberDesc {
+    GocCdklmParams p;
+    const float* Hi;  int32_t Hi_pitch;     /* corner depths (bytes pitch) */
+    const float* Hm;  int32_t Hm_pitch;     /* cell means (for the CFL limit) */
+    float* eta[2]; float* hu[2]; float* hv[2];  /* buffer set 0 holds the state */
+    int32_t pitch;                          /* state pitch in bytes */
+} GocMemberDesc;
+
+/*
+ * Build an ensemble handle: copies the member table to the device and
+ * builds the member/tile work queue (member-major 32x16 tiles).  Up to
+ * `max_substeps` RK2 steps can be scheduled per block.
+ */
+int goc_ensemble_create(const GocMemberDesc* members, int n_members, int max_substeps, void** ensemble);
+int goc_ensemble_destroy(void* ensemble);
+int goc_ensemble_size(void* ensemble, int* n_members, int* n_tiles);
+
+/*
+ * Per-member step schedule of one block: dt_table is n_members x
+ * max_substeps (row-major, host memory), member m takes n_substeps[m] steps.
+ * This is the dt sequence of S/CDKLM16.py:493-509 (local_dt = min(dt,
+ * t_end - t_now)) evaluated once per member on the host.
+ */
+int goc_ensemble_set_schedule(void* ensemble, const float* dt_table, const int* n_substeps, void* stream);
+
+/*
+ * Step k of the block for every member with k < n_substeps[m]: one
+ * persistent launch over the member/tile work queue; each tile runs the
+ * fused RK2 step (see goc_cdklm_rk2_step) from set (k % 2) into set
+ * ((k + 1) % 2).  Graph-capturable.
+ */
+int goc_ensemble_rk2_substep(void* ensemble, int k, void* stream);
+
+/* Close a block of `n_launched` substeps: advects the drifters of the last
+ * step of members that ran all of them, then makes buffer set 0 the current
+ * state again (swaps members whose block had an odd number of steps).
+ * Graph-capturable. */
+int goc_ensemble_end_block(void* ensemble, int n_launched, void* stream);
+
+/*
+ * Attach drifters: positions[m] is member m's device array of
+ * (num_drifters[m] + 1) x 2 floats (x, y in metres from the south-west
+ * interior corner; the last row is the observation position), NULL for a
+ * member without drifters.  Each RK2 substep then also advects the
+ * drifters with the state after the previous substep, as
+ * GPUDrifterCollection.driftFromSim does after every step
+ * (D/GPUDrifterCollection.py:198-233, K/driftKernels.cu:74-183).  Wind drift
+ * is not applied in the batched engine.
+ */
+int goc_ensemble_set_drifters(void* ensemble, float* const* positions, const int* num_drifters,
+                              float sensitivity, void* stream);
+
+/* Copy member m's current descriptor (device pointers) to the host.
+ * Synchronises `stream`. */
+int goc_ensemble_get_member(void* ensemble, int m, GocMemberDesc* out, void* stream);
+
+/*
+ * CFL limit of every member into dt_out[0..n_members) (device memory), the
+ * batched form of goc_max_dt.  Uses per-block partial minima held in
+ * scratch owned by the ensemble handle.
+ */
+int goc_ensemble_max_dt(void* ensemble, float* dt_out, void* stream);
+
+/*
+ * Model error of every member in two launches (SOAR over all coarse grids,
+ * then the balanced transfer into each member's state, with periodic ghost
+ * images).  noise[m] configures member m of `ensemble`.  Replaces the
+ * per-member OceanStateNoise.perturbSim calls of the reference's ensembles
+ * (E/OceanNoiseEnsemble.py:517-543 via S/CDKLM16.py:567-568,726-733).
+ * substep = -1 perturbs every member's current state between blocks;
+ * substep = k perturbs, right after RK2 step k of a block, the members that
+ * took step k (the cadence of step(t, apply_stochastic_term=True)).
+ * goc_noise_batch_generate draws new XORWOW normals into the members'
+ * random fields (same substep rule) after goc_noise_batch_seed.
+ */
+int goc_noise_batch_create(void* ensemble, const GocNoiseDesc* noise, void** batch);
+int goc_noise_batch_destroy(void* batch);
+int goc_noise_batch_seed(void* batch, unsigned long long seed, void* stream);
+int goc_noise_batch_generate(void* batch, void* ensemble, int substep, void* stream);
+int goc_noise_batch_perturb(void* batch, void* ensemble, float perturbation_scale, int substep, void* stream);
 
 #ifdef __cplusplus
 }

@@ -43,7 +43,7 @@ def test_argument_validation_without_gpu():
     lib = _lib.load()
     p = _lib.GocCdklmParams()
     p.nx, p.ny = 0, 4
-    rc = lib.goc_cdklm_rk2_step(ctypes.byref(p), 1.0, None, None, None, None, None, None, 64, None, 64, None)
+    rc = lib.goc_cdklm_rk2_step(ctypes.byref(p), 1.0, None, None, None, None, None, None, 64, None, 64, None, 64, None)
     assert rc == -1 and "nx, ny" in _lib.last_error()
     assert lib.goc_max_dt_partials(256, 256) == 8 * 32
     rc = lib.goc_max_dt(8, 8, 1.0, 1.0, 9.8, None, None, None, 48, None, 48, 1e20, None, 0, None, None)

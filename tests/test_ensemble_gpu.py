@@ -1,0 +1,179 @@
+"""The batched ensemble engine against member-by-member stepping."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _member(ctx, nx, ny, bc, seed, drifters=0):
+    from gpuocean_gb300.SWEsimulators import CDKLM16
+    from gpuocean_gb300.drifters import GPUDrifterCollection
+    from gpuocean_gb300.utils import BenchmarkCases, Common
+    c = BenchmarkCases.double_jet_case(nx=nx, ny=ny, dx=5000.0, dy=5000.0, seed=seed)
+    b = Common.BoundaryConditions(*bc)
+    sim = CDKLM16.CDKLM16(ctx, c["eta0"], c["hu0"], c["hv0"], c["H"], nx, ny, c["dx"], c["dy"], 0.0, c["g"],
+                          c["f"], 0.0, coriolis_beta=c["coriolis_beta"], boundary_conditions=b)
+    if drifters:
+        rng = np.random.default_rng(seed)
+        d = GPUDrifterCollection.GPUDrifterCollection(ctx, drifters, boundaryConditions=b,
+                                                      domain_size_x=nx * c["dx"], domain_size_y=ny * c["dy"],
+                                                      gpu_stream=sim.gpu_stream)
+        d.setDrifterPositions(np.stack([rng.uniform(0, nx * c["dx"], drifters),
+                                        rng.uniform(0, ny * c["dy"], drifters)], axis=1))
+        d.setObservationPosition(np.array([nx * c["dx"] / 3, ny * c["dy"] / 3]))
+        sim.attachDrifters(d)
+    return sim
+
+
+SPECS = [(64, 40, (1, 2, 1, 2), 3), (33, 17, (1, 1, 1, 1), 4), (48, 48, (2, 2, 2, 2), 5), (128, 64, (2, 1, 2, 1), 6)]
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_batched_equals_member_by_member(gpu_ctx, use_graph):
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
+    a = [_member(gpu_ctx, *s, drifters=50) for s in SPECS]
+    b = [_member(gpu_ctx, *s, drifters=50) for s in SPECS]
+    for s in a + b:
+        s.updateDt()
+    ens = BatchedEnsemble(a, use_graph=use_graph)
+    for _ in range(4):
+        ens.step(60.0)
+        for s in b:
+            s.step(60.0)
+    ens.synchronize()
+    for sa, sb in zip(a, b):
+        assert sa.t == sb.t and sa.num_iterations == sb.num_iterations
+        for x, y in zip(sa.download(), sb.download()):
+            xi, yi = np.asarray(x)[2:-2, 2:-2], np.asarray(y)[2:-2, 2:-2]
+            assert np.array_equal(xi, yi)
+        assert np.array_equal(sa.drifters.getDrifterPositions(), sb.drifters.getDrifterPositions())
+        assert np.array_equal(sa.drifters.getObservationPosition(), sb.drifters.getObservationPosition())
+
+
+def test_batched_dt_matches_single(gpu_ctx):
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
+    a = [_member(gpu_ctx, *s) for s in SPECS]
+    ens = BatchedEnsemble(a)
+    dts = ens.updateDt(courant_number=0.8)
+    for s, v in zip(a, dts):
+        assert np.float32(v) == np.float32(s.downloadMaxDt())
+
+
+def test_member_counts_and_shared_bathymetry(gpu_ctx):
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
+    a = [_member(gpu_ctx, 64, 40, (1, 2, 1, 2), 3) for _ in range(3)] + [_member(gpu_ctx, 64, 40, (1, 2, 1, 2), 9)]
+    ens = BatchedEnsemble(a)
+    assert ens._bathy_owner == [0, 0, 0, 3]
+    assert ens.n_tiles == 4 * 2 * 3
+
+
+def _with_noise(sims, factor, seed):
+    rng = np.random.default_rng(seed)
+    for s in sims:
+        s.setSOARModelError(small_scale_perturbation_amplitude=1e-3, small_scale_perturbation_interpolation_factor=factor)
+    xis = []
+    for s in sims:
+        n = s.model_error
+        xi = rng.standard_normal((n.rand_ny, n.rand_nx)).astype(np.float32)
+        n.setRandomNumbers(xi)
+        xis.append(xi)
+    return xis
+
+
+@pytest.mark.parametrize("factor", [1, 3])
+def test_batched_noise_block_cadence_equals_member_by_member(gpu_ctx, factor):
+    """dataAssimilationStep cadence: block of steps, then one perturbation."""
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
+    specs = [(48, 30, (1, 2, 1, 2), 3), (24, 42, (1, 1, 1, 1), 4), (36, 36, (2, 2, 2, 2), 5)]
+    a = [_member(gpu_ctx, *s, drifters=20) for s in specs]
+    b = [_member(gpu_ctx, *s, drifters=20) for s in specs]
+    xa, xb = _with_noise(a, factor, 1), _with_noise(b, factor, 1)
+    for s in a + b:
+        s.updateDt()
+    ens = BatchedEnsemble(a)
+    ens.set_noise([s.model_error for s in a])  # injected random fields, no device RNG
+    for _ in range(3):
+        ens.step(60.0, apply_stochastic_term=True)
+        for s in b:
+            s.step(60.0, apply_stochastic_term=False)
+            s.perturbState(update_random_field=False)
+    ens.synchronize()
+    for sa, sb in zip(a, b):
+        for x, y in zip(sa.download(), sb.download()):
+            assert np.array_equal(np.asarray(x)[2:-2, 2:-2], np.asarray(y)[2:-2, 2:-2])
+        assert np.array_equal(sa.drifters.getDrifterPositions(), sb.drifters.getDrifterPositions())
+
+
+def test_batched_noise_step_cadence_equals_member_by_member(gpu_ctx, monkeypatch):
+    """CDKLM16.step cadence: perturbation after every RK2 step, before drift."""
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
+    from gpuocean_gb300.SWEsimulators import CDKLM16
+    specs = [(48, 30, (1, 2, 1, 2), 3), (24, 42, (1, 1, 1, 1), 4)]
+    a = [_member(gpu_ctx, *s, drifters=20) for s in specs]
+    b = [_member(gpu_ctx, *s, drifters=20) for s in specs]
+    _with_noise(a, 1, 2), _with_noise(b, 1, 2)
+    for s in a + b:
+        s.updateDt()
+    orig = CDKLM16.CDKLM16.perturbState
+    monkeypatch.setattr(CDKLM16.CDKLM16, "perturbState",
+                        lambda self, **kw: orig(self, update_random_field=False))
+    ens = BatchedEnsemble(a)
+    ens.set_noise([s.model_error for s in a])
+    for _ in range(2):
+        ens.step(60.0, apply_stochastic_term=True, noise_cadence="step")
+        for s in b:
+            s.step(60.0, apply_stochastic_term=True)
+    ens.synchronize()
+    for sa, sb in zip(a, b):
+        for x, y in zip(sa.download(), sb.download()):
+            assert np.array_equal(np.asarray(x)[2:-2, 2:-2], np.asarray(y)[2:-2, 2:-2])
+        assert np.array_equal(sa.drifters.getDrifterPositions(), sb.drifters.getDrifterPositions())
+
+
+def test_device_rng_noise_statistics(gpu_ctx):
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
+    a = [_member(gpu_ctx, 48, 30, (1, 2, 1, 2), 3) for _ in range(4)]
+    _with_noise(a, 1, 3)
+    ens = BatchedEnsemble(a)
+    ens.set_noise([s.model_error for s in a], rng_seed=99)
+    before = [np.asarray(s.download()[0]) for s in a]
+    ens.perturb()
+    ens.synchronize()
+    xis = [s.model_error.getRandomNumbers() for s in a]
+    assert all(abs(x.mean()) < 0.2 and abs(x.std() - 1) < 0.2 for x in xis)
+    assert not np.array_equal(xis[0], xis[1])
+    after = [np.asarray(s.download()[0]) for s in a]
+    assert all(not np.array_equal(x, y) for x, y in zip(before, after))
+
+
+def test_ensemble_classes_run(gpu_ctx):
+    from gpuocean_gb300.ensembles.MultiLevelOceanEnsemble import MultiLevelOceanEnsemble
+    from gpuocean_gb300.ensembles.OceanModelEnsemble import OceanModelEnsemble
+    from gpuocean_gb300.utils import BenchmarkCases, Common
+    c = BenchmarkCases.double_jet_case(nx=64, ny=40)
+    sim_args = dict(dt=0.0, g=c["g"], f=c["f"], r=0.0, coriolis_beta=c["coriolis_beta"], model_time_step=60.0)
+    data_args = dict(eta0=c["eta0"], hu0=c["hu0"], hv0=c["hv0"], H=c["H"], nx=64, ny=40, dx=c["dx"], dy=c["dy"],
+                     boundary_conditions=Common.BoundaryConditions(1, 2, 1, 2))
+    ens = OceanModelEnsemble(gpu_ctx, sim_args, data_args, dict(small_scale_perturbation_amplitude=1e-4), 4)
+    ens.attachDrifters(np.array([[1e5, 1e5], [2e5, 1e5]]))
+    ens.stepToObservation(600.0)
+    assert abs(ens.particles[0].t - 600.0) < 1e-6
+    obs = ens.observeParticles(np.array([[1e5, 1e5]]))
+    assert obs.shape == (4, 1, 2) and np.all(np.isfinite(obs))
+    # two-level ensemble with grids of different size in one launch
+    lv = [BenchmarkCases.double_jet_case(nx=32, ny=20), BenchmarkCases.double_jet_case(nx=64, ny=40)]
+
+    def mk(cc):
+        from gpuocean_gb300.SWEsimulators import CDKLM16
+        s = CDKLM16.CDKLM16(gpu_ctx, cc["eta0"], cc["hu0"], cc["hv0"], cc["H"], cc["nx"], cc["ny"], cc["dx"],
+                            cc["dy"], 0.0, cc["g"], cc["f"], 0.0, coriolis_beta=cc["coriolis_beta"],
+                            boundary_conditions=Common.BoundaryConditions(1, 2, 1, 2), model_time_step=60.0)
+        return s
+    ml = MultiLevelOceanEnsemble([[mk(lv[0]) for _ in range(3)], [[mk(lv[1]) for _ in range(2)],
+                                                                  [mk(lv[0]) for _ in range(2)]]])
+    for s in ml.members:
+        s.updateDt()
+    ml.step(120.0, apply_stochastic_term=False)
+    assert all(abs(s.t - 120.0) < 1e-6 for s in ml.members)
+    est = ml.estimate(np.mean)
+    assert est.shape == (3, 40, 64) and np.all(np.isfinite(est))
