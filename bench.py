@@ -32,6 +32,10 @@ MODEL_TIME_STEP = 60.0
 NOISE_FACTOR = 8          # coarse grid every 8 cells
 NOISE_L_COARSE = 8.0      # SOAR length scale in coarse cells
 NOISE_STD = 0.003         # target std of the SOAR eta perturbation [m]
+# DRAM bytes (read + write) per member-cell-step of ensemble_rk2_kernel, from
+# one ncu capture of a 96-member C3 launch (460,593,408 B over 96 x 512 x 300
+# member-cell-steps); traffic of a bench launch is scaled by its member-cells.
+NCU_DRAM_BYTES_PER_MEMBER_CELL = 460593408 / (96 * 512 * 300)
 
 
 def soar_q0(L_cells=NOISE_L_COARSE, std=NOISE_STD):
@@ -404,7 +408,7 @@ def main():
     for e in kev:
         _lib.call("goc_event_create", ctypes.byref(e))
     ens._sched_key = None
-    durations, bytes_k = [], []
+    durations, bytes_k, cells_k = [], [], []
     for _ in range(3):
         scheds, table, n, nsub = ens._schedule(MODEL_TIME_STEP)
         _lib.call("goc_ensemble_set_schedule", ens._handle, table.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
@@ -420,6 +424,7 @@ def main():
             _lib.call("goc_event_elapsed_ms", kev[2 * k], kev[2 * k + 1], ctypes.byref(t))
             durations.append(t.value / 1000.0)
             bytes_k.append(algorithmic_bytes_per_launch(sims, n_active[k], distinct_bathy))
+            cells_k.append(sum(int(s.nx) * int(s.ny) for s in sims[:n_active[k]]))
         for m, s in enumerate(sims):
             for x in scheds[m]:
                 s.t += np.float64(x)
@@ -428,6 +433,7 @@ def main():
         ens._ptrs = ens._current_ptrs()
     ens._sched_key = None
     avg_bytes = float(np.mean(bytes_k))
+    traffic = NCU_DRAM_BYTES_PER_MEMBER_CELL * float(np.mean(cells_k))
     avg_dur = float(np.mean(durations))
     achieved = avg_bytes / avg_dur / 1e9
     peak, peak_kind = measured_peaks()
@@ -535,7 +541,9 @@ def main():
                                     "members_sampled": len(pm_sims),
                                     "batched_over_per_member": value / world / per_member_rate},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "kernel": "ensemble_rk2_kernel",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 96-member "
+                                           "launch, scaled per member-cell", "kernel": "ensemble_rk2_kernel",
                          "peak_kind": peak_kind, "avg_launch_ms": 1000.0 * avg_dur,
                          "algorithmic_bytes_per_launch": avg_bytes},
             "e2e": e2e, "gpu_launches": launches, "clocks": clk, "cpu_baseline": cpu,
