@@ -83,6 +83,9 @@ SIGNATURES = {
     "goc_max_dt_partials": (c_int, [c_int, c_int]),
     "goc_max_dt": (c_int, [c_int, c_int, c_float, c_float, c_float, c_void_p, c_void_p, c_void_p, c_int,
                            c_void_p, c_int, c_float, c_void_p, c_int, c_void_p, c_void_p]),
+    "goc_max_dt_noalloc_capacity": (c_int, []),
+    "goc_max_dt_noalloc": (c_int, [c_int, c_int, c_float, c_float, c_float, c_void_p, c_void_p, c_void_p, c_int,
+                                   c_void_p, c_int, c_float, c_void_p, c_void_p]),
     "goc_drift": (c_int, [c_int, c_int, c_float, c_float, c_float, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int,
                           c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_float,
                           c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_float, c_float, c_void_p]),

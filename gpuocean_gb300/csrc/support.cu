@@ -212,3 +212,63 @@ extern "C" int goc_max_dt(int nx, int ny, float dx, float dy, float g, const flo
     count_launch();
     return check_launch("dt_final_kernel");
 }
+
+// ---------------------------------------------------------------------------
+// CFL limit without allocation: the per-block partial minima live in a
+// file-scope device array instead of caller-provided scratch.
+// ---------------------------------------------------------------------------
+
+#include <mutex>
+
+namespace goc {
+
+// Room for the partial minima of grids up to 65536 reduction blocks of
+// 32 x 8 cells (16.7 M interior cells, e.g. 4096 x 4096).  Every GPU that
+// loads the library holds these 256 KiB until the process exits.
+constexpr int kNoAllocPartials = 65536;
+static __device__ __align__(256) float g_dt_partials[kNoAllocPartials];
+
+// Device address of g_dt_partials, looked up once per device.  In host code
+// the array's name is only a host-side stand-in, so the address must come
+// from cudaGetSymbolAddress with the device current.
+constexpr int kMaxDevices = 64;
+static float* g_dt_partials_addr[kMaxDevices] = {nullptr};
+static std::mutex g_dt_partials_mutex;
+
+static int noalloc_partials(float** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_max_dt_noalloc: cudaGetDevice: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return set_error(GOC_ERR_UNSUPPORTED, "goc_max_dt_noalloc: device %d", dev);
+    std::lock_guard<std::mutex> lock(g_dt_partials_mutex);
+    if (!g_dt_partials_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_dt_partials);
+        if (e != cudaSuccess)
+            return set_error(GOC_ERR_CUDA, "goc_max_dt_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+        g_dt_partials_addr[dev] = static_cast<float*>(p);
+    }
+    *out = g_dt_partials_addr[dev];
+    return GOC_OK;
+}
+
+}  // namespace goc
+
+extern "C" int goc_max_dt_noalloc_capacity(void) { return goc::kNoAllocPartials; }
+
+extern "C" int goc_max_dt_noalloc(int nx, int ny, float dx, float dy, float g, const float* eta, const float* hu,
+                                  const float* hv, int pitch, const float* Hm, int Hm_pitch, float land_value,
+                                  float* dt_out, void* stream) {
+    if (nx < 1 || ny < 1) return set_error(GOC_ERR_ARG, "goc_max_dt_noalloc: nx, ny must be >= 1");
+    const int need = goc_max_dt_partials(nx, ny);
+    if (need > goc::kNoAllocPartials)
+        return set_error(GOC_ERR_ARG,
+                         "goc_max_dt_noalloc: a %d x %d grid needs %d partial minima, the built-in scratch holds %d "
+                         "(at most %d reduction blocks of %d x %d cells); use goc_max_dt with caller scratch",
+                         nx, ny, need, goc::kNoAllocPartials, goc::kNoAllocPartials, goc::kDtBX, goc::kDtBY);
+    float* partials = nullptr;
+    int rc = goc::noalloc_partials(&partials);
+    if (rc) return rc;
+    return goc_max_dt(nx, ny, dx, dy, g, eta, hu, hv, pitch, Hm, Hm_pitch, land_value, partials, need, dt_out,
+                      stream);
+}

@@ -179,6 +179,31 @@ int goc_max_dt(int nx, int ny, float dx, float dy, float g,
                const float* Hm, int Hm_pitch, float land_value,
                float* partials, int partials_capacity, float* dt_out, void* stream);
 
+/*
+ * The CFL limit of goc_max_dt without any allocation by the caller or the
+ * library: the per-block partial minima go to a scratch array that is part
+ * of the library image (no counterpart in the reference, whose Python host
+ * allocates its dt buffers with PyCUDA).  For callers that cannot allocate
+ * device memory on their step path: a host model that owns all device memory
+ * through its own pool and has no allocator to lend, or a loop that must not
+ * pay the implicit device synchronisation of cudaMalloc/cudaFree.
+ *  - Limit: goc_max_dt_noalloc_capacity() partial minima (65536, i.e. grids of
+ *    up to 65536 blocks of 32 x 8 interior cells); larger grids are rejected
+ *    with GOC_ERR_ARG.  The array (256 KiB) stays resident on every GPU that
+ *    loads the library until the process exits.
+ *  - The first call on a device looks up the array's device address with
+ *    cudaGetSymbolAddress while that device is current; make that first call
+ *    before any stream capture.
+ *  - All calls share the one array: calls whose kernels overlap on the GPU
+ *    (e.g. on two streams at once) race.  Each call overwrites every partial
+ *    it reads, so nothing needs clearing between calls.
+ *  - No cudaMalloc, cudaFree or allocating library routine is called.
+ */
+int goc_max_dt_noalloc_capacity(void);
+int goc_max_dt_noalloc(int nx, int ny, float dx, float dy, float g,
+                       const float* eta, const float* hu, const float* hv, int pitch,
+                       const float* Hm, int Hm_pitch, float land_value, float* dt_out, void* stream);
+
 /* ---------------- drifters ---------------------------------------------- */
 
 /*
