@@ -20,8 +20,14 @@ LIB = os.path.join(HERE, "libgpuocean_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
           "--expt-relaxed-constexpr", "-ftz=true", "-prec-div=false", "-prec-sqrt=false"]
-# per-file extra flags
-EXTRA = {"noise.cu": ["-use_fast_math"]}
+# per-file extra flags.  The step translation units keep every multiply and
+# add separately rounded (no FMA contraction), as the reference compiles its
+# step kernel (--fmad=false): with the same operation order this makes the
+# RK2 step bit-identical to the reference's kernel.  The noise kernels use
+# fast math, as the reference's do.
+EXTRA = {"noise.cu": ["-use_fast_math"],
+         "cdklm_step.cu": ["-fmad=false"],
+         "ensemble.cu": ["-fmad=false"]}
 
 
 def nvcc_path() -> str:

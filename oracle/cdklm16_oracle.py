@@ -587,9 +587,10 @@ class OracleCDKLM16:
                         desingularization_eps, flux_slope_eps, depth_cutoff,
                         flux_balancer, rho_o, wind_stress_factor, one_dimensional).rounded()
         north0 = (math.sin(float(angle.flat[0])), math.cos(float(angle.flat[0])))
-        f32_f = np.float32(f)
         beta = np.float32(coriolis_beta)
-        f_comp = np.float32(f32_f - beta * (2 * np.float32(dx) * north0[0] + 2 * np.float32(dy) * north0[1]))
+        # S/CDKLM16.py:148-149 compensates in double precision; Simulator
+        # stores the result as float32 (S/Simulator.py:90)
+        f_comp = np.float32(float(f) - float(coriolis_beta) * (2 * float(dx) * north0[0] + 2 * float(dy) * north0[1]))
         self.f = f_comp
         self.coriolis_beta = beta
         if beta != 0.0:

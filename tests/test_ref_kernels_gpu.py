@@ -1,0 +1,298 @@
+"""Parity against the reference's own CUDA kernels (the second oracle).
+
+The reference kernels are compiled from the reference sources into
+``oracle/_ref/*.cubin`` (``oracle/build_ref.py``) and driven by
+``oracle/ref_kernels.py``, which replays the reference host's launch sequence.
+The product runs through its drop-in classes on the same inputs.
+
+The RK2 step is compared bit for bit: the product evaluates the same
+operations in the same order, compiled without FMA contraction as the
+reference's step kernel is (--fmad=false), so after 1000 steps of the
+256 x 256 Gaussian bump (CFL 0.45) and of the 512 x 300 double jet the states
+are identical (the stated bound, max|d eta| <= 1e-5 m and max|d hu,hv| <=
+1e-4 m^2/s, is met with zero difference).  The noise kernels are fast-math on
+both sides and compared within 2e-5 of the perturbation on identical injected
+normal draws; drifter positions within 1e-6 of the domain size.  Both runs
+get bit-identical inputs: the reference kernels read the Coriolis and angle
+textures that the product's host built.
+"""
+import json
+import time
+
+import numpy as np
+import pytest
+
+from oracle import ref_kernels as rk
+
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(not rk.available(), reason="reference kernels not built (no reference sources)")]
+
+
+def _bump256():
+    nx = ny = 256
+    dx = dy = 200.0
+    x = (np.arange(nx + 4) - 2 + 0.5 - nx / 2.0)
+    y = (np.arange(ny + 4) - 2 + 0.5 - ny / 2.0)
+    eta = (0.1 * np.exp(-(x[None, :] ** 2 + y[:, None] ** 2) / (2.0 * 10.0 ** 2))).astype(np.float32)
+    z = np.zeros_like(eta)
+    H = np.full((ny + 5, nx + 5), 60.0, np.float32)
+    return dict(eta0=eta, hu0=z, hv0=z.copy(), H=H, nx=nx, ny=ny, dx=dx, dy=dy, g=9.81, f=1.2e-4, r=0.0,
+                coriolis_beta=0.0, boundary=(1, 1, 1, 1))
+
+
+def _textures(c, dt):
+    from oracle.cdklm16_oracle import BC, OracleCDKLM16
+    o = OracleCDKLM16(c["eta0"], c["hu0"], c["hv0"], c["H"], c["nx"], c["ny"], c["dx"], c["dy"], dt, c["g"],
+                      c["f"], c["r"], coriolis_beta=c["coriolis_beta"], boundary_conditions=BC(*c["boundary"]))
+    return o.ftex, o.angle_tex, o.f
+
+
+def _product(ctx, c, dt):
+    from gpuocean_gb300.SWEsimulators import CDKLM16
+    from gpuocean_gb300.utils import Common
+    return CDKLM16.CDKLM16(ctx, c["eta0"], c["hu0"], c["hv0"], c["H"], c["nx"], c["ny"], c["dx"], c["dy"], dt,
+                           c["g"], c["f"], c["r"], coriolis_beta=c["coriolis_beta"],
+                           boundary_conditions=Common.BoundaryConditions(*c["boundary"]))
+
+
+def _reference(config, c, dt, sim=None):
+    """The reference kernels on the inputs of case `c`.  With `sim`, the
+    Coriolis and angle textures and the compensated f are the ones the
+    product's host computed (the same host arithmetic as S/CDKLM16.py:147-239),
+    so that both runs see bit-identical inputs."""
+    if sim is not None:
+        ftex = sim.coriolis_f_arr.download(sim.gpu_stream)
+        angle = sim.angle_arr.download(sim.gpu_stream)
+        f = sim.f
+    else:
+        ftex, angle, f = _textures(c, dt)
+    return rk.RefCDKLM16(config, c["eta0"], c["hu0"], c["hv0"], c["H"], c["nx"], c["ny"], c["dx"], c["dy"], dt,
+                         c["g"], f, c["r"], ftex, angle, bc=c["boundary"], beta=c["coriolis_beta"])
+
+
+def _interior(arrs, nx, ny):
+    return [np.asarray(a)[2:ny + 2, 2:nx + 2] for a in arrs]
+
+
+def _diffs(sim, ref, nx, ny):
+    mine = _interior(sim.download(), nx, ny)
+    theirs = _interior(ref.download(), nx, ny)
+    return [float(np.max(np.abs(a.astype(np.float64) - b))) for a, b in zip(mine, theirs)], theirs
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from gpuocean_gb300.utils import Common
+    return Common.CUDAContext()
+
+
+def test_bathymetry_matches_reference_kernels(ctx):
+    from gpuocean_gb300.utils.BenchmarkCases import double_jet_case
+    c = double_jet_case()
+    sim = _product(ctx, c, 1.0)
+    ref = _reference("cdklm_jet512", c, 1.0, sim)
+    Bi, Bm = sim.downloadBathymetry()
+    rBi, rBm = ref.bathymetry()
+    np.testing.assert_array_equal(np.asarray(Bm), rBm)
+    np.testing.assert_array_equal(np.asarray(Bi), rBi)
+    ref.free()
+    sim.cleanUp()
+
+
+def test_bump256_1000_steps_within_stated_tolerance(ctx):
+    c = _bump256()
+    sim = _product(ctx, c, 0.0)
+    sim.updateDt(courant_number=0.45)
+    dt = float(sim.dt)
+    ref = _reference("cdklm_bump256", c, dt, sim)
+    ref_dt = float(np.float32(0.45 * ref.max_dt()))
+    assert abs(ref_dt - dt) <= 1e-6 * dt, (ref_dt, dt)
+    for _ in range(1000):
+        sim.step(dt)
+        ref.step(dt)
+    (de, dhu, dhv), theirs = _diffs(sim, ref, c["nx"], c["ny"])
+    print(json.dumps({"case": "bump256 1000 steps", "dt": dt, "max_abs_diff": [de, dhu, dhv],
+                      "max_abs_ref": [float(np.max(np.abs(t))) for t in theirs]}))
+    assert de <= 1e-5 and dhu <= 1e-4 and dhv <= 1e-4, (de, dhu, dhv)
+    assert de == 0.0 and dhu == 0.0 and dhv == 0.0, "the RK2 step is expected to be bit-identical"
+    ref.free()
+    sim.cleanUp()
+
+
+@pytest.mark.parametrize("boundary", [(1, 2, 1, 2), (1, 1, 1, 1)], ids=["periodic_x", "walls"])
+def test_double_jet_1000_steps(ctx, boundary):
+    from gpuocean_gb300.utils.BenchmarkCases import double_jet_case
+    c = double_jet_case()
+    c["boundary"] = boundary
+    sim = _product(ctx, c, 0.0)
+    sim.updateDt(courant_number=0.8)
+    dt = float(sim.dt)
+    ref = _reference("cdklm_jet512", c, dt, sim)
+    for _ in range(1000):
+        sim.step(dt)
+        ref.step(dt)
+    (de, dhu, dhv), theirs = _diffs(sim, ref, c["nx"], c["ny"])
+    scale = [float(np.max(np.abs(t))) for t in theirs]
+    print(json.dumps({"case": f"double jet 512x300 1000 steps, bc {boundary}", "dt": dt, "max_abs_diff": [de, dhu, dhv],
+                      "max_abs_ref": scale}))
+    assert de == 0.0 and dhu == 0.0 and dhv == 0.0, (de, dhu, dhv)
+    ref.free()
+    sim.cleanUp()
+
+
+def test_friction_odd_grid_random_state(ctx):
+    nx, ny = 77, 45
+    rng = np.random.default_rng(11)
+    H = (40.0 + 10.0 * rng.random((ny + 5, nx + 5))).astype(np.float32)
+    eta = (0.3 * rng.standard_normal((ny + 4, nx + 4))).astype(np.float32)
+    hu = (2.0 * rng.standard_normal((ny + 4, nx + 4))).astype(np.float32)
+    hv = (2.0 * rng.standard_normal((ny + 4, nx + 4))).astype(np.float32)
+    c = dict(eta0=eta, hu0=hu, hv0=hv, H=H, nx=nx, ny=ny, dx=150.0, dy=170.0, g=9.81, f=1.0e-4, r=2.4e-3,
+             coriolis_beta=0.0, boundary=(1, 1, 1, 1))
+    sim = _product(ctx, c, 0.0)
+    sim.updateDt(courant_number=0.5)
+    dt = float(sim.dt)
+    ref = _reference("cdklm_fric77", c, dt, sim)
+    for _ in range(200):
+        sim.step(dt)
+        ref.step(dt)
+    (de, dhu, dhv), theirs = _diffs(sim, ref, nx, ny)
+    scale = [float(np.max(np.abs(t))) for t in theirs]
+    print(json.dumps({"case": "friction 77x45 random 200 steps", "max_abs_diff": [de, dhu, dhv],
+                      "max_abs_ref": scale}))
+    assert de == 0.0 and dhu == 0.0 and dhv == 0.0, (de, dhu, dhv)
+    ref.free()
+    sim.cleanUp()
+
+
+def _soar_q0(L_cells=8.0, std=0.003):
+    oy, ox = np.mgrid[-2:3, -2:3]
+    d = np.sqrt(ox ** 2 + oy ** 2) / L_cells
+    return std / np.sqrt(np.sum(((1 + d) * np.exp(-d)) ** 2))
+
+
+@pytest.mark.parametrize("factor,config,case", [(1, "noise_const", "bump"), (7, "noise_const", "bump"),
+                                                (8, "noise_jet512", "jet"), (1, "noise_jet512", "jet")])
+def test_soar_perturbation_on_injected_normals(ctx, factor, config, case):
+    from gpuocean_gb300.SWEsimulators import OceanStateNoise
+    from gpuocean_gb300.utils.BenchmarkCases import double_jet_case
+    c = _bump256() if case == "bump" else double_jet_case()
+    cdk = "cdklm_bump256" if case == "bump" else "cdklm_jet512"
+    sim = _product(ctx, c, 1.0)
+    ref = _reference(cdk, c, 1.0, sim)
+    cdx = c["dx"] * factor
+    q0, L = _soar_q0(), 8.0 * cdx
+    noise = OceanStateNoise.OceanStateNoise.fromsim(sim, soar_q0=q0, soar_L=L, interpolation_factor=factor,
+                                                    strict_odd_factor=False)
+    rnoise = rk.RefNoise(config, ref, q0, L, interpolation_factor=factor)
+    assert (int(noise.rand_ny), int(noise.rand_nx)) == (rnoise.rand_ny, rnoise.rand_nx)
+    xi = np.random.default_rng(7).standard_normal((rnoise.rand_ny, rnoise.rand_nx)).astype(np.float32)
+    before = _interior(sim.download(), c["nx"], c["ny"])
+    noise.setRandomNumbers(xi)
+    noise.perturbSim(sim, update_random_field=False)
+    rnoise.set_random(xi)
+    rnoise.perturb(ref)
+    mine = _interior(sim.download(), c["nx"], c["ny"])
+    theirs = _interior(ref.download(), c["nx"], c["ny"])
+    rel = []
+    for m, t, b in zip(mine, theirs, before):
+        dp = (t.astype(np.float64) - b)             # the reference's perturbation
+        err = np.max(np.abs(m.astype(np.float64) - t))
+        rel.append(float(err / np.max(np.abs(dp))))
+        print(json.dumps({"case": f"SOAR factor {factor} on {case}", "max_rel_diff_of_perturbation": rel[-1]}))
+        assert np.max(np.abs(dp)) > 0
+        assert err <= 2e-5 * np.max(np.abs(dp)) + 4 * np.spacing(np.float32(np.max(np.abs(t)))), \
+            (factor, err, np.max(np.abs(dp)))
+    rnoise.free()
+    ref.free()
+    sim.cleanUp()
+
+
+def test_double_jet_with_model_error_and_drifters(ctx):
+    """40 steps of the C3 member: SOAR model error after every step on the same
+    injected draws, 200 drifters advected by both."""
+    from gpuocean_gb300.SWEsimulators import OceanStateNoise
+    from gpuocean_gb300.drifters import GPUDrifterCollection
+    from gpuocean_gb300.utils import Common
+    from gpuocean_gb300.utils.BenchmarkCases import double_jet_case
+    c = double_jet_case()
+    sim = _product(ctx, c, 0.0)
+    sim.updateDt(courant_number=0.8)
+    dt = float(sim.dt)
+    ref = _reference("cdklm_jet512", c, dt, sim)
+    factor = 8
+    q0, L = _soar_q0(), 8.0 * c["dx"] * factor
+    noise = OceanStateNoise.OceanStateNoise.fromsim(sim, soar_q0=q0, soar_L=L, interpolation_factor=factor,
+                                                    strict_odd_factor=False)
+    rnoise = rk.RefNoise("noise_jet512", ref, q0, L, interpolation_factor=factor)
+    Lx, Ly = c["nx"] * c["dx"], c["ny"] * c["dy"]
+    rng = np.random.default_rng(3)
+    pos = np.stack([rng.random(201) * Lx, rng.random(201) * Ly], axis=1).astype(np.float32)
+    drifters = GPUDrifterCollection.GPUDrifterCollection(
+        ctx, 200, boundaryConditions=Common.BoundaryConditions(*c["boundary"]), domain_size_x=Lx, domain_size_y=Ly)
+    drifters.setDrifterPositions(pos[:-1])
+    drifters.setObservationPosition(pos[-1])
+    rdrift = rk.RefDrifters(pos, Lx, Ly, 0, 1)
+    draws = np.random.default_rng(99).standard_normal((40, rnoise.rand_ny, rnoise.rand_nx)).astype(np.float32)
+    for k in range(40):
+        # the order of S/CDKLM16.py:519-575: RK2 step, model error on the k-th
+        # injected draw, ghost fill, drift
+        sim.step(dt, apply_stochastic_term=False)
+        noise.setRandomNumbers(draws[k])
+        noise.perturbSim(sim, update_random_field=False)
+        sim.applyBoundaryConditions()
+        drifters.driftFromSim(sim, dt)
+        ref.step(dt)
+        rnoise.set_random(draws[k])
+        rnoise.perturb(ref)
+        ref._boundary(ref.h0)
+        rdrift.drift(ref, dt)
+    (de, dhu, dhv), theirs = _diffs(sim, ref, c["nx"], c["ny"])
+    scale = [float(np.max(np.abs(t))) for t in theirs]
+    mine_pos = np.asarray(drifters.getDrifterPositions())
+    ref_pos = rdrift.positions()[:-1]
+    dpos = float(np.max(np.abs(mine_pos - ref_pos)))
+    print(json.dumps({"case": "double jet + SOAR + drifters, 40 steps", "max_abs_diff": [de, dhu, dhv],
+                      "max_abs_ref": scale, "max_abs_drifter_diff_m": dpos}))
+    # the step is bit-identical; what remains comes from the fast-math noise
+    # transfer (within 2e-5 of each perturbation), carried by 40 steps
+    assert de <= 1e-5 and dhu <= 2e-5 * scale[1] and dhv <= 2e-5 * max(scale[1], scale[2]), (de, dhu, dhv)
+    assert dpos <= 1e-6 * max(Lx, Ly)
+    rdrift.free()
+    rnoise.free()
+    ref.free()
+    sim.cleanUp()
+
+
+def test_reference_kernel_step_rate(ctx):
+    """Throughput of the reference kernels launched per member (the way the
+    reference's ensembles step), beside the product's plain per-member step,
+    on the 512 x 300 double-jet member.  Printed as one JSON line."""
+    from gpuocean_gb300.utils.BenchmarkCases import double_jet_case
+    c = double_jet_case()
+    sim = _product(ctx, c, 0.0)
+    sim.updateDt(courant_number=0.8)
+    dt = float(sim.dt)
+    ref = _reference("cdklm_jet512", c, dt, sim)
+    n = 300
+    for _ in range(20):
+        ref.step(dt)
+        sim.step(dt)
+    ref.synchronize()
+    sim.gpu_stream.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(n):
+        ref.step(dt)
+    ref.synchronize()
+    t_ref = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for _ in range(n):
+        sim.step(dt)
+    sim.gpu_stream.synchronize()
+    t_prod = time.perf_counter() - t0
+    cells = c["nx"] * c["ny"] * n
+    print(json.dumps({"case": "per-member step rate, double jet 512x300", "steps": n,
+                      "reference_kernels_cell_steps_per_s": cells / t_ref,
+                      "product_cell_steps_per_s": cells / t_prod}))
+    ref.free()
+    sim.cleanUp()
