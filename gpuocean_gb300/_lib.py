@@ -86,6 +86,9 @@ SIGNATURES = {
     "goc_max_dt_noalloc_capacity": (c_int, []),
     "goc_max_dt_noalloc": (c_int, [c_int, c_int, c_float, c_float, c_float, c_void_p, c_void_p, c_void_p, c_int,
                                    c_void_p, c_int, c_float, c_void_p, c_void_p]),
+    "goc_cdklm_vjp_partials": (c_int, [c_int, c_int]),
+    "goc_cdklm_stage_vjp": (c_int, [ctypes.POINTER(GocCdklmParams), c_float, c_int] + [c_void_p] * 18 +
+                            [c_int, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
     "goc_drift": (c_int, [c_int, c_int, c_float, c_float, c_float, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int,
                           c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_float,
                           c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_float, c_float, c_void_p]),

@@ -1,0 +1,162 @@
+"""Adjoint of the CDKLM16 RK2 step behind ``torch.autograd.Function``.
+
+The reverse sweep is hand-written CUDA (``goc_cdklm_stage_vjp``); torch only
+holds the buffers and routes gradients.  ``CDKLM16Rollout`` runs ``n_steps``
+RK2 steps of a simulator's configuration from a given state and uniform wind
+stress, returns the interior state every ``obs_every`` steps, and in backward
+returns the gradients of any loss of those states with respect to the
+initial (eta, hu, hv) and the wind stress.  Long rollouts keep only every
+K-th state (K = ceil(sqrt(n_steps))) and recompute each segment of K steps in
+the backward sweep, so memory grows as sqrt(n_steps).
+
+Data-assimilation use (variational, 4D-Var style)::
+
+    adj = StepAdjoint(sim)                        # a CDKLM16 with rk_order 2
+    eta0 = torch.tensor(..., device="cuda", requires_grad=True)
+    states = CDKLM16Rollout.apply(adj, 400, 10, eta0, hu0, hv0, wind)
+    loss = misfit(states, observations)           # any torch expression
+    loss.backward()                               # eta0.grad, ..., wind.grad
+
+The reference has no adjoint; this covers its RK2 step (S/CDKLM16.py:519-530
+with K/CDKLM16_kernel.cu:475-1090, S/ = src/gpuocean/SWEsimulators,
+K/ = src/gpuocean/gpu_kernels) with uniform wind and no pressure field.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+class StepAdjoint:
+    """The RK2 step of ``sim`` (its parameters, bathymetry and Coriolis data)
+    with a fixed dt and a uniform wind stress held in a device tensor."""
+
+    def __init__(self, sim, dt=None):
+        if int(sim.rk_order) != 2:
+            raise ValueError("the adjoint covers the RK2 step only")
+        self.sim = sim
+        self.nx, self.ny = int(sim.nx), int(sim.ny)
+        self.dt = float(np.float32(sim.dt if dt is None else dt))
+        self.device = torch.device("cuda", torch.cuda.current_device())
+        self.pitch = 4 * (self.nx + 4)
+        self.Hi = sim.bathymetry.Bi
+        self.Hm = sim.bathymetry.Bm
+        self.wsf = float(sim.wind_stress_factor)
+        self.wind = torch.zeros(2, dtype=torch.float32, device=self.device)
+        p = _lib.GocCdklmParams.from_buffer_copy(sim._params)
+        p.wind_x_cur = p.wind_x_next = self.wind.data_ptr()
+        p.wind_y_cur = p.wind_y_next = self.wind.data_ptr() + 4
+        p.wind_x_nx = p.wind_x_ny = p.wind_y_nx = p.wind_y_ny = 1
+        p.wind_t = 0.0
+        self.params = p
+        n = _lib.load().goc_cdklm_vjp_partials(self.nx, self.ny)
+        self.partials = torch.zeros((2, n), dtype=torch.float32, device=self.device)
+        sim.gpu_stream.synchronize()
+
+    @property
+    def shape(self):
+        return (self.ny + 4, self.nx + 4)
+
+    def zeros(self):
+        return [torch.zeros(self.shape, dtype=torch.float32, device=self.device) for _ in range(3)]
+
+    def _stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    def set_wind(self, tau):
+        """Uniform wind stress (x, y) before the simulator's wind_stress_factor."""
+        self.wind.copy_(torch.as_tensor(tau, dtype=torch.float32, device=self.device))
+
+    def state(self, eta, hu, hv):
+        return [torch.as_tensor(np.asarray(a, dtype=np.float32), device=self.device).contiguous()
+                for a in (eta, hu, hv)]
+
+    def step(self, q_in, q_out):
+        _lib.call("goc_cdklm_rk2_step", ctypes.byref(self.params), ctypes.c_float(self.dt),
+                  *[_ptr(a) for a in q_in], *[_ptr(a) for a in q_out], self.pitch,
+                  self.Hi.ptr, int(self.Hi.pitch), self.Hm.ptr, int(self.Hm.pitch), self._stream())
+
+    def stage1(self, q_in, q_star):
+        _lib.call("goc_cdklm_stage", ctypes.byref(self.params), ctypes.c_float(self.dt), 0,
+                  *[_ptr(a) for a in q_in], *[_ptr(a) for a in q_star], None, None, None, self.pitch,
+                  self.Hi.ptr, int(self.Hi.pitch), self.Hm.ptr, int(self.Hm.pitch), self._stream())
+
+    def step_vjp(self, q_n, q_star, lam_next, lam_star, lam_n):
+        """lam_n = (dQ^{n+1}/dQ^n)^T lam_next on interior cells; returns the
+        gradient contribution for the wind stress (x, y) as a device tensor."""
+        s = self._stream()
+        common = (self.pitch, self.Hi.ptr, int(self.Hi.pitch), self.Hm.ptr, int(self.Hm.pitch))
+        _lib.call("goc_cdklm_stage_vjp", ctypes.byref(self.params), ctypes.c_float(self.dt), 1,
+                  *[_ptr(a) for a in q_star], *[_ptr(a) for a in q_n], *[_ptr(a) for a in lam_next],
+                  None, None, None, *[_ptr(a) for a in lam_star], *[_ptr(a) for a in lam_n],
+                  *common, _ptr(self.partials[0]), s)
+        _lib.call("goc_cdklm_stage_vjp", ctypes.byref(self.params), ctypes.c_float(self.dt), 0,
+                  *[_ptr(a) for a in q_n], None, None, None, *[_ptr(a) for a in lam_star],
+                  *[_ptr(a) for a in lam_n], *[_ptr(a) for a in lam_n], None, None, None,
+                  *common, _ptr(self.partials[1]), s)
+        return self.wsf * self.partials.view(2, -1, 2).sum(dim=(0, 1))
+
+
+class CDKLM16Rollout(torch.autograd.Function):
+    """``apply(adj, n_steps, obs_every, eta0, hu0, hv0, wind)`` ->
+    interior states (n_steps // obs_every, 3, ny, nx) after steps
+    obs_every, 2 obs_every, ...  eta0/hu0/hv0: (ny+4, nx+4) float32 CUDA
+    tensors (ghost cells are ignored); wind: (2,) stress."""
+
+    @staticmethod
+    def forward(ctx, adj, n_steps, obs_every, eta0, hu0, hv0, wind):
+        n_steps, obs_every = int(n_steps), int(obs_every)
+        if n_steps < 1 or obs_every < 1:
+            raise ValueError("n_steps and obs_every must be >= 1")
+        adj.set_wind(wind.detach())
+        K = max(1, int(math.ceil(math.sqrt(n_steps))))
+        q = [a.detach().to(torch.float32).contiguous().clone() for a in (eta0, hu0, hv0)]
+        buf = [torch.empty_like(a) for a in q]
+        ckpts = {0: [a.clone() for a in q]}
+        outs = []
+        for n in range(n_steps):
+            adj.step(q, buf)
+            q, buf = buf, q
+            if (n + 1) % K == 0 and n + 1 < n_steps:
+                ckpts[n + 1] = [a.clone() for a in q]
+            if (n + 1) % obs_every == 0:
+                outs.append(torch.stack([a[2:-2, 2:-2] for a in q]))
+        ctx.adj, ctx.K, ctx.n_steps, ctx.obs_every, ctx.ckpts = adj, K, n_steps, obs_every, ckpts
+        if not outs:
+            raise ValueError("n_steps must be at least obs_every")
+        return torch.stack(outs)
+
+    @staticmethod
+    def backward(ctx, grad):
+        adj, K, n_steps, every = ctx.adj, ctx.K, ctx.n_steps, ctx.obs_every
+        grad = grad.contiguous()
+        lam, lam_n, lam_s, q_s = adj.zeros(), adj.zeros(), adj.zeros(), adj.zeros()
+        wind_bar = torch.zeros(2, dtype=torch.float32, device=adj.device)
+        for start in sorted(ctx.ckpts, reverse=True):
+            end = min(start + K, n_steps)
+            states = [ctx.ckpts[start]]
+            for _ in range(start, end - 1):
+                nxt = [torch.empty_like(a) for a in states[-1]]
+                adj.step(states[-1], nxt)
+                states.append(nxt)
+            for n in range(end - 1, start - 1, -1):
+                if (n + 1) % every == 0:
+                    g = grad[(n + 1) // every - 1]
+                    for c in range(3):
+                        lam[c][2:-2, 2:-2] += g[c]
+                q_n = states[n - start]
+                adj.stage1(q_n, q_s)
+                wind_bar += adj.step_vjp(q_n, q_s, lam, lam_s, lam_n)
+                lam, lam_n = lam_n, lam
+            del states
+        ctx.ckpts = None
+        return None, None, None, lam[0], lam[1], lam[2], wind_bar

@@ -27,7 +27,8 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 # fast math, as the reference's do.
 EXTRA = {"noise.cu": ["-use_fast_math"],
          "cdklm_step.cu": ["-fmad=false"],
-         "ensemble.cu": ["-fmad=false"]}
+         "ensemble.cu": ["-fmad=false"],
+         "cdklm_adjoint.cu": ["-fmad=false"]}
 
 
 def nvcc_path() -> str:

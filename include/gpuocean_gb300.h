@@ -204,6 +204,40 @@ int goc_max_dt_noalloc(int nx, int ny, float dx, float dy, float g,
                        const float* eta, const float* hu, const float* hv, int pitch,
                        const float* Hm, int Hm_pitch, float land_value, float* dt_out, void* stream);
 
+/* ---------------- adjoint of the RK2 step --------------------------------- */
+
+/*
+ * Vector-Jacobian product of one RK2 stage (no counterpart in the reference,
+ * which has no adjoint).  With y the stage output on interior cells,
+ *   rk_step 0:  y = S1(x),     x = Q^n        (the first stage)
+ *   rk_step 1:  y = S2(a, x),  x = Q*, a = Q^n (the second stage)
+ * the call writes, on interior cells,
+ *   xb = base + (dS/dx)^T yb      (base may be NULL)
+ *   ab = (dS2/da)^T yb             (rk_step 1 only)
+ * and, if wind_partials is not NULL, goc_cdklm_vjp_partials(nx, ny) floats
+ * of per-tile partial sums (x, y interleaved) of (dS/dX_eff)^T yb, where
+ * X_eff = wind_stress_factor * stress is the uniform wind stress the step
+ * adds.  Ghost cells of the adjoint arrays are neither read nor written:
+ * ghost cells of the state are periodic images or wall mirrors of interior
+ * cells, and their adjoint is folded onto those cells.  Branches (limiter,
+ * dry clamps, desingularisation) follow the recomputed forward state.
+ * Requirements: rk_order 2, uniform (1x1) wind stress, no pressure field,
+ * nx >= 40 with periodic x and ny >= 24 with periodic y.  An RK2 step's VJP
+ * is the rk_step-1 call (x = Q*, a = Q^n, yb = lambda^{n+1}, xb = lambda*,
+ * ab = lambda^n) followed by the rk_step-0 call (x = Q^n, yb = lambda*,
+ * base = xb = lambda^n); Q* comes from goc_cdklm_stage with rk_step 0.
+ */
+int goc_cdklm_vjp_partials(int nx, int ny);
+int goc_cdklm_stage_vjp(const GocCdklmParams* p, float dt, int rk_step,
+                        const float* x_eta, const float* x_hu, const float* x_hv,
+                        const float* a_eta, const float* a_hu, const float* a_hv,
+                        const float* yb_eta, const float* yb_hu, const float* yb_hv,
+                        const float* base_eta, const float* base_hu, const float* base_hv,
+                        float* xb_eta, float* xb_hu, float* xb_hv,
+                        float* ab_eta, float* ab_hu, float* ab_hv, int pitch,
+                        const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch,
+                        float* wind_partials, void* stream);
+
 /* ---------------- drifters ---------------------------------------------- */
 
 /*

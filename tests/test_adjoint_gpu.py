@@ -1,0 +1,405 @@
+"""The hand-written CUDA adjoint of the RK2 step against autograd of the FP64
+torch restatement (oracle/cdklm16_torch.py), and the rollout gradient against
+central finite differences of the FP64 oracle.
+
+Tolerances: one step's vector-Jacobian product agrees with FP64 autograd to
+1e-4 of the largest gradient entry per field (the CUDA adjoint runs in FP32
+on the FP32 forward state); the wind-stress gradient to 1e-4 relative.
+"""
+import json
+
+import numpy as np
+import pytest
+import torch
+
+from oracle.cdklm16_oracle import BC, OracleCDKLM16
+from oracle.cdklm16_torch import TorchCDKLM16
+
+pytestmark = pytest.mark.gpu
+
+
+def _smooth(rng, shape, scale, width=4.0):
+    a = rng.standard_normal(shape)
+    k = np.exp(-0.5 * (np.arange(-8, 9) / width) ** 2)
+    k /= k.sum()
+    for ax in (0, 1):
+        a = np.apply_along_axis(lambda r: np.convolve(r, k, mode="same"), ax, a)
+    return (scale * a / np.max(np.abs(a))).astype(np.float32)
+
+
+CASES = {
+    "walls_f": dict(nx=64, ny=48, bc=(1, 1, 1, 1), f=1.0e-4, beta=0.0, r=0.0),
+    "periodic_x_beta_friction": dict(nx=80, ny=40, bc=(1, 2, 1, 2), f=1.0e-4, beta=2.0e-9, r=3.0e-3),
+    "periodic_xy": dict(nx=64, ny=32, bc=(2, 2, 2, 2), f=1.2e-4, beta=0.0, r=0.0),
+}
+
+
+def _case(name, seed=0):
+    c = dict(CASES[name])
+    rng = np.random.default_rng(seed)
+    nx, ny = c["nx"], c["ny"]
+    # depth constant within 5 cells of a wall: the wall-mirrored ghost cells
+    # then have exactly the interior cell's depth.  Otherwise the flux
+    # balancer's switch at a wall face (u_m > -u_p, K/CDKLM16_kernel.cu:137)
+    # compares two numbers that are equal up to rounding, and FP32 and FP64
+    # take different branches of a discontinuous flux there.
+    taper = np.ones((ny + 5, nx + 5))
+    if c["bc"][1] == 1:
+        taper[:, :7] = 0.0
+        taper[:, -7:] = 0.0
+    if c["bc"][0] == 1:
+        taper[:7, :] = 0.0
+        taper[-7:, :] = 0.0
+    c["H"] = (35.0 + taper * _smooth(rng, (ny + 5, nx + 5), 5.0)).astype(np.float32)
+    c["eta"] = _smooth(rng, (ny + 4, nx + 4), 0.3)
+    c["hu"] = _smooth(rng, (ny + 4, nx + 4), 8.0)
+    c["hv"] = _smooth(rng, (ny + 4, nx + 4), 8.0)
+    c["dx"], c["dy"], c["g"] = 200.0, 180.0, 9.81
+    c["wind"] = (1.0e-4, -6.0e-5)
+    return c
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from gpuocean_gb300.utils import Common
+    return Common.CUDAContext()
+
+
+def _sim(ctx, c, dt):
+    from gpuocean_gb300.SWEsimulators import CDKLM16
+    from gpuocean_gb300.utils import Common
+    return CDKLM16.CDKLM16(ctx, c["eta"], c["hu"], c["hv"], c["H"], c["nx"], c["ny"], c["dx"], c["dy"], dt,
+                           c["g"], c["f"], c["r"], coriolis_beta=c["beta"],
+                           boundary_conditions=Common.BoundaryConditions(*c["bc"]))
+
+
+def _torch_ref(c, dt, q0):
+    o = OracleCDKLM16(c["eta"], c["hu"], c["hv"], c["H"], c["nx"], c["ny"], c["dx"], c["dy"], dt, c["g"], c["f"],
+                      c["r"], coriolis_beta=c["beta"], boundary_conditions=BC(*c["bc"]))
+    return TorchCDKLM16(o)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_step_vjp_matches_fp64_autograd(ctx, name):
+    """One RK2 step's VJP at a random smooth state."""
+    from gpuocean_gb300.adjoint import StepAdjoint
+    c = _case(name)
+    dt = 2.0
+    sim = _sim(ctx, c, dt)
+    adj = StepAdjoint(sim)
+    adj.set_wind(c["wind"])
+    q = adj.state(*sim.download())
+    rng = np.random.default_rng(5)
+    lam_next = adj.zeros()
+    lam_host = [rng.standard_normal((c["ny"], c["nx"])) for _ in range(3)]
+    for a, b in zip(lam_next, lam_host):
+        a[2:-2, 2:-2] = torch.as_tensor(b, dtype=torch.float32)
+    q_s, lam_s, lam_n = adj.zeros(), adj.zeros(), adj.zeros()
+    adj.stage1(q, q_s)
+    wind_bar = adj.step_vjp(q, q_s, lam_next, lam_s, lam_n).cpu().numpy()
+    torch.cuda.synchronize()
+    ours = [a.cpu().numpy().astype(np.float64)[2:-2, 2:-2] for a in lam_n]
+
+    tq = _torch_ref(c, dt, q)
+    qt = [torch.tensor(a.cpu().numpy().astype(np.float64), requires_grad=True) for a in q]
+    X = torch.tensor(float(np.float32(c["wind"][0])), dtype=torch.float64, requires_grad=True)
+    Y = torch.tensor(float(np.float32(c["wind"][1])), dtype=torch.float64, requires_grad=True)
+    out = tq.rk2_step(qt, X, Y, dt)
+    loss = sum((o[2:-2, 2:-2] * torch.as_tensor(b)).sum() for o, b in zip(out, lam_host))
+    loss.backward()
+    ref = [a.grad.numpy()[2:-2, 2:-2] for a in qt]
+    errs = [float(np.max(np.abs(a - b)) / np.max(np.abs(b))) for a, b in zip(ours, ref)]
+    werr = [float(abs(wind_bar[0] - X.grad.item()) / abs(X.grad.item())),
+            float(abs(wind_bar[1] - Y.grad.item()) / abs(Y.grad.item()))]
+    print(json.dumps({"case": name, "rel_err_eta_hu_hv": errs, "rel_err_wind": werr}))
+    assert max(errs) <= 1e-4, errs
+    assert max(werr) <= 1e-4, werr
+    sim.cleanUp()
+
+
+def _stage_vjps(adj, q, q_s, lam):
+    """Both stage VJPs of the CUDA adjoint: (x-bar of stage 2 w.r.t. Q*,
+    a-bar of stage 2 w.r.t. Q^n, x-bar of stage 1 w.r.t. Q^n for y-bar = lam)."""
+    import ctypes
+    from gpuocean_gb300 import _lib
+    from gpuocean_gb300.adjoint import _ptr
+    s = adj._stream()
+    common = (adj.pitch, adj.Hi.ptr, int(adj.Hi.pitch), adj.Hm.ptr, int(adj.Hm.pitch))
+    xs, an, x0 = adj.zeros(), adj.zeros(), adj.zeros()
+    _lib.call("goc_cdklm_stage_vjp", ctypes.byref(adj.params), ctypes.c_float(adj.dt), 1, *[_ptr(a) for a in q_s],
+              *[_ptr(a) for a in q], *[_ptr(a) for a in lam], None, None, None, *[_ptr(a) for a in xs],
+              *[_ptr(a) for a in an], *common, None, s)
+    _lib.call("goc_cdklm_stage_vjp", ctypes.byref(adj.params), ctypes.c_float(adj.dt), 0, *[_ptr(a) for a in q],
+              None, None, None, *[_ptr(a) for a in lam], None, None, None, *[_ptr(a) for a in x0], None, None, None,
+              *common, None, s)
+    torch.cuda.synchronize()
+    return [[a.cpu().numpy().astype(np.float64)[2:-2, 2:-2] for a in v] for v in (xs, an, x0)]
+
+
+def test_stage_vjps_of_moving_bump_match_autograd_at_the_same_point(ctx):
+    """The Gaussian bump with a smooth current: each stage VJP against FP64
+    autograd of the same stage evaluated at the same FP32 points (Q^n and the
+    CUDA first stage Q*).
+
+    Exact comparisons need states without FP32 ties: at rest, h = 60 m + eta
+    with eta ~ 1e-5 m is quantised in FP32 (one ulp of 60 is 3.8e-6), so
+    neighbouring depths, wave speeds and limiter arguments tie exactly in
+    FP32 but not in FP64, and the two precisions take different subgradients
+    (the CUDA adjoint differentiates the FP32 computation)."""
+    from gpuocean_gb300.adjoint import StepAdjoint
+    from oracle.cdklm16_torch import periodic_ghosts
+    c = dict(_bump_case(64, moving=True), wind=(1.0e-4, -6.0e-5))
+    dt = 2.0
+    sim = _sim(ctx, c, dt)
+    adj = StepAdjoint(sim)
+    adj.set_wind(c["wind"])
+    q = adj.state(*sim.download())
+    q_s = adj.zeros()
+    adj.stage1(q, q_s)
+    rng = np.random.default_rng(4)
+    lam = adj.zeros()
+    lam_host = [rng.standard_normal((c["ny"], c["nx"])) for _ in range(3)]
+    for a, b in zip(lam, lam_host):
+        a[2:-2, 2:-2] = torch.as_tensor(b, dtype=torch.float32)
+    xs, an, x0 = _stage_vjps(adj, q, q_s, lam)
+    tq = _torch_ref(c, dt, q)
+    X = torch.tensor(float(np.float32(c["wind"][0])), dtype=torch.float64)
+    Y = torch.tensor(float(np.float32(c["wind"][1])), dtype=torch.float64)
+    f64 = lambda v: [torch.tensor(a.cpu().numpy().astype(np.float64), requires_grad=True) for a in v]
+    qn, qs = f64(q), f64(q_s)
+    out = tq.stage(periodic_ghosts(qs, c["nx"], c["ny"], tq.bc),
+                   periodic_ghosts(qn, c["nx"], c["ny"], tq.bc), X, Y, dt, 1)
+    sum((o * torch.as_tensor(b)).sum() for o, b in zip(out, lam_host)).backward()
+    ref_xs = [a.grad.numpy()[2:-2, 2:-2] for a in qs]
+    ref_an = [a.grad.numpy()[2:-2, 2:-2] for a in qn]
+    qn0 = f64(q)
+    out = tq.stage(periodic_ghosts(qn0, c["nx"], c["ny"], tq.bc), None, X, Y, dt, 0)
+    sum((o * torch.as_tensor(b)).sum() for o, b in zip(out, lam_host)).backward()
+    ref_x0 = [a.grad.numpy()[2:-2, 2:-2] for a in qn0]
+    errs = {k: [float(np.max(np.abs(a - b)) / np.max(np.abs(b))) for a, b in zip(o, r)]
+            for k, o, r in (("stage2_qstar", xs, ref_xs), ("stage2_qn", an, ref_an), ("stage1", x0, ref_x0))}
+    print(json.dumps({"case": "moving bump, stage VJPs", "rel_err": errs}))
+    assert max(max(v) for v in errs.values()) <= 1e-5, errs
+    sim.cleanUp()
+
+
+def _bump_case(n=64, amplitude=0.1, moving=False):
+    """The Gaussian-bump configuration (dx = dy = 200 m, H = 60 m, f = 1.2e-4,
+    walls) on an n x n grid, sigma = 10 cells; at rest, or with a smooth
+    random current of up to 0.1 m/s (hu, hv up to 6 m^2/s)."""
+    x = (np.arange(n + 4) - 2 + 0.5 - n / 2.0)
+    eta = (amplitude * np.exp(-(x[None, :] ** 2 + x[:, None] ** 2) / (2.0 * 10.0 ** 2))).astype(np.float32)
+    hu = np.zeros_like(eta)
+    hv = np.zeros_like(eta)
+    if moving:
+        rng = np.random.default_rng(21)
+        hu = _smooth(rng, eta.shape, 6.0)
+        hv = _smooth(rng, eta.shape, 6.0)
+    return dict(nx=n, ny=n, bc=(1, 1, 1, 1), f=1.2e-4, beta=0.0, r=0.0, dx=200.0, dy=200.0, g=9.81,
+                H=np.full((n + 5, n + 5), 60.0, np.float32), eta=eta, hu=hu, hv=hv)
+
+
+def _misfit_setup(c, n_obs_points, seed):
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(c["nx"] * c["ny"], size=n_obs_points, replace=False)
+    return idx // c["nx"], idx % c["nx"]
+
+
+def test_rollout_gradient_matches_fp64_finite_differences(ctx):
+    """400 RK2 steps of the Gaussian bump (64 x 64) with uniform wind stress
+    (1e-4, 0); loss = squared misfit of (u, v) at 64 seeded cells every 10
+    steps against a truth run from a bump of half the amplitude without wind
+    (FP64 oracle).
+    Directional derivatives of the adjoint gradient are compared with central
+    finite differences (eps = 1e-3) of the FP64 oracle rollout: along the
+    gradient itself (relative error), along two random smooth directions
+    (error relative to |grad| |direction|) and for the two wind components
+    (error relative to |wind gradient|)."""
+    from gpuocean_gb300.adjoint import CDKLM16Rollout, StepAdjoint
+    c = _bump_case(64)
+    n_steps, every = 400, 10
+    sim = _sim(ctx, c, 0.0)
+    sim.updateDt(courant_number=0.45)
+    dt = float(sim.dt)
+    adj = StepAdjoint(sim)
+    dev = adj.device
+    tau = np.array([1.0e-4, 0.0], dtype=np.float32)
+    rows, cols = _misfit_setup(c, 64, 3)
+    Hm = torch.as_tensor(np.asarray(sim.downloadBathymetry()[1], dtype=np.float32)[2:-2, 2:-2], device=dev)
+
+    def uv(states):
+        h = states[:, 0] + Hm
+        return states[:, 1, rows, cols] / h[:, rows, cols], states[:, 2, rows, cols] / h[:, rows, cols]
+
+    q0 = adj.state(*sim.download())
+    o_base = OracleCDKLM16(c["eta"], c["hu"], c["hv"], c["H"], c["nx"], c["ny"], c["dx"], c["dy"], dt, c["g"],
+                           c["f"], c["r"], boundary_conditions=BC(*c["bc"]))
+    Hm64 = np.asarray(o_base.Hm, dtype=np.float64)[2:-2, 2:-2]
+    base = [np.asarray(a.detach().cpu().numpy(), dtype=np.float64) for a in q0]
+
+    def rollout64(q, tx, ty):
+        o = OracleCDKLM16(c["eta"], c["hu"], c["hv"], c["H"], c["nx"], c["ny"], c["dx"], c["dy"], dt, c["g"],
+                          c["f"], c["r"], boundary_conditions=BC(*c["bc"]))
+        o.Q0 = [a.copy() for a in q]
+        o.Q1 = [a.copy() for a in q]
+        sh = (c["ny"] + 4, c["nx"] + 4)
+        o.wind = (np.full(sh, tx), np.full(sh, ty))
+        for k in range(n_steps // every):
+            for _ in range(every):
+                o.step(dt)
+            e, hu, hv = (a[2:-2, 2:-2] for a in o.Q0)
+            h = e[rows, cols] + Hm64[rows, cols]
+            yield hu[rows, cols] / h, hv[rows, cols] / h
+
+    # the truth (half the bump, no wind) in FP64, used by both sides
+    truth0 = [b.copy() for b in base]
+    truth0[0] = truth0[0] * 0.5
+    obs = list(rollout64(truth0, 0.0, 0.0))
+    u_obs_h = np.stack([a for a, _ in obs])
+    v_obs_h = np.stack([b for _, b in obs])
+    u_obs = torch.as_tensor(u_obs_h, dtype=torch.float32, device=dev)
+    v_obs = torch.as_tensor(v_obs_h, dtype=torch.float32, device=dev)
+
+    x = [a.clone().requires_grad_(True) for a in q0]
+    w = torch.tensor(tau, device=dev, requires_grad=True)
+    states = CDKLM16Rollout.apply(adj, n_steps, every, *x, w)
+    u, v = uv(states)
+    loss = ((u - u_obs) ** 2).sum() + ((v - v_obs) ** 2).sum()
+    loss.backward()
+    grads = [a.grad.double().cpu().numpy() for a in x]
+    gw = w.grad.double().cpu().numpy()
+
+    def loss64(q, tx, ty):
+        return sum(np.sum((a - u_obs_h[k]) ** 2) + np.sum((b - v_obs_h[k]) ** 2)
+                   for k, (a, b) in enumerate(rollout64(q, tx, ty)))
+
+    def fd_state(delta, eps=1.0e-3):
+        return (loss64([b + eps * dd for b, dd in zip(base, delta)], float(tau[0]), float(tau[1])) -
+                loss64([b - eps * dd for b, dd in zip(base, delta)], float(tau[0]), float(tau[1]))) / (2 * eps)
+
+    gnorm = np.sqrt(sum(float(np.sum(g * g)) for g in grads))
+    results = {}
+    # along the gradient (scaled to a 1e-2 m eta change at most)
+    scale = 1.0e-2 / max(float(np.max(np.abs(g))) for g in grads)
+    delta = [scale * g for g in grads]
+    ad = sum(float(np.sum(g * dd)) for g, dd in zip(grads, delta))
+    fd = fd_state(delta)
+    results["gradient_direction"] = (ad, fd, abs(ad - fd) / abs(fd))
+    rng = np.random.default_rng(9)
+    for d in range(2):
+        delta = [_smooth(rng, base[0].shape, s).astype(np.float64) for s in (0.01, 0.1, 0.1)]
+        for a in delta:
+            a[:2, :] = 0; a[-2:, :] = 0; a[:, :2] = 0; a[:, -2:] = 0
+        dnorm = np.sqrt(sum(float(np.sum(dd * dd)) for dd in delta))
+        ad = sum(float(np.sum(g * dd)) for g, dd in zip(grads, delta))
+        fd = fd_state(delta)
+        results[f"random_{d}"] = (ad, fd, abs(ad - fd) / (gnorm * dnorm))
+    wnorm = float(np.sqrt(np.sum(gw * gw)))
+    for comp in range(2):
+        h = 1.0e-3 * 1.0e-4
+        tp, tm = [float(tau[0]), float(tau[1])], [float(tau[0]), float(tau[1])]
+        tp[comp] += h
+        tm[comp] -= h
+        fd = (loss64(base, *tp) - loss64(base, *tm)) / (2 * h)
+        results[f"wind_{'xy'[comp]}"] = (float(gw[comp]), fd, abs(float(gw[comp]) - fd) / wnorm)
+    loss_fd = loss64(base, float(tau[0]), float(tau[1]))
+    print(json.dumps({"case": "rollout 400 steps 64x64 bump, FD of FP64 oracle", "results": results,
+                      "loss_fp32": float(loss.item()), "loss_fp64": loss_fd}))
+    # random directions: the adjoint of the FP32 forward against FP64 finite
+    # differences, error relative to |grad| |direction|
+    assert max(results["random_0"][2], results["random_1"][2]) <= 1e-4, results
+    # along the gradient and for the wind the comparison is limited by the
+    # FP32 forward itself: with H = 60 m and eta ~ 0.1 m an FP32 rollout of
+    # 400 steps differs from the FP64 one by ~1e-3 of eta (h = H + eta loses
+    # the low bits of eta), so the two losses have different minimisers by
+    # that much; the adjoint itself is checked exactly against the FP64 VJP
+    # chain on the FP32 trajectory (test below)
+    assert results["gradient_direction"][2] <= 2e-3, results
+    assert max(results["wind_x"][2], results["wind_y"][2]) <= 2e-3, results
+    sim.cleanUp()
+
+
+def test_rollout_adjoint_matches_fp64_vjp_chain(ctx):
+    """100 steps of the moving bump with wind: the CUDA adjoint of the whole
+    rollout (sqrt(N) checkpointing) against the chain of FP64 autograd stage
+    VJPs evaluated at the same FP32 trajectory points (Q^n and Q* of every
+    step)."""
+    from gpuocean_gb300.adjoint import CDKLM16Rollout, StepAdjoint
+    from oracle.cdklm16_torch import periodic_ghosts
+    c = _bump_case(64, moving=True)
+    n_steps, every = 100, 10
+    sim = _sim(ctx, c, 0.0)
+    sim.updateDt(courant_number=0.45)
+    dt = float(sim.dt)
+    adj = StepAdjoint(sim)
+    dev = adj.device
+    tau = np.array([1.0e-4, 2.0e-5], dtype=np.float32)
+    rows, cols = _misfit_setup(c, 64, 3)
+    Hm32 = np.asarray(sim.downloadBathymetry()[1], dtype=np.float32)[2:-2, 2:-2]
+    Hm = torch.as_tensor(Hm32, device=dev)
+    q0 = adj.state(*sim.download())
+    rng = np.random.default_rng(12)
+    n_obs = n_steps // every
+    u_obs = torch.as_tensor(0.01 * rng.standard_normal((n_obs, 64)), dtype=torch.float32, device=dev)
+    v_obs = torch.as_tensor(0.01 * rng.standard_normal((n_obs, 64)), dtype=torch.float32, device=dev)
+    x = [a.clone().requires_grad_(True) for a in q0]
+    w = torch.tensor(tau, device=dev, requires_grad=True)
+    st = CDKLM16Rollout.apply(adj, n_steps, every, *x, w)
+    h = st[:, 0] + Hm
+    loss = ((st[:, 1, rows, cols] / h[:, rows, cols] - u_obs) ** 2).sum() + \
+           ((st[:, 2, rows, cols] / h[:, rows, cols] - v_obs) ** 2).sum()
+    loss.backward()
+    ours = [a.grad.double().cpu().numpy()[2:-2, 2:-2] for a in x]
+    ours_w = w.grad.double().cpu().numpy()
+
+    # the FP32 trajectory with its first stages
+    adj.set_wind(tau)
+    traj, stars = [[a.clone() for a in q0]], []
+    for _ in range(n_steps):
+        qs = adj.zeros()
+        adj.stage1(traj[-1], qs)
+        nxt = [torch.empty_like(a) for a in q0]
+        adj.step(traj[-1], nxt)
+        stars.append(qs)
+        traj.append(nxt)
+    to64 = lambda v: [torch.tensor(a.cpu().numpy().astype(np.float64)) for a in v]
+    traj = [to64(v) for v in traj]
+    stars = [to64(v) for v in stars]
+    tq = _torch_ref(c, dt, None)
+    X = torch.tensor(float(tau[0]), dtype=torch.float64, requires_grad=True)
+    Y = torch.tensor(float(tau[1]), dtype=torch.float64, requires_grad=True)
+    Hm64 = torch.as_tensor(Hm32.astype(np.float64))
+    uo, vo = u_obs.double().cpu(), v_obs.double().cpu()
+    nx, ny = c["nx"], c["ny"]
+    lam = [torch.zeros(ny, nx, dtype=torch.float64) for _ in range(3)]
+
+    def interior_grad(q):
+        g = [a.grad[2:-2, 2:-2].clone() for a in q]
+        return g
+
+    for n in range(n_steps - 1, -1, -1):
+        if (n + 1) % every == 0:
+            k = (n + 1) // every - 1
+            s = [a.clone().requires_grad_(True) for a in traj[n + 1]]
+            e, hu, hv = (a[2:-2, 2:-2] for a in s)
+            hh = e[rows, cols] + Hm64[rows, cols]
+            (((hu[rows, cols] / hh - uo[k]) ** 2).sum() + ((hv[rows, cols] / hh - vo[k]) ** 2).sum()).backward()
+            lam = [a + b for a, b in zip(lam, interior_grad(s))]
+        qn = [a.clone().requires_grad_(True) for a in traj[n]]
+        qs = [a.clone().requires_grad_(True) for a in stars[n]]
+        out = tq.stage(periodic_ghosts(qs, nx, ny, tq.bc), periodic_ghosts(qn, nx, ny, tq.bc), X, Y, dt, 1)
+        sum((o * l).sum() for o, l in zip(out, lam)).backward()
+        lam_s = interior_grad(qs)
+        lam_direct = interior_grad(qn)
+        qn2 = [a.clone().requires_grad_(True) for a in traj[n]]
+        out = tq.stage(periodic_ghosts(qn2, nx, ny, tq.bc), None, X, Y, dt, 0)
+        sum((o * l).sum() for o, l in zip(out, lam_s)).backward()
+        lam = [a + b for a, b in zip(lam_direct, interior_grad(qn2))]
+    ref = [a.numpy() for a in lam]
+    ref_w = np.array([X.grad.item(), Y.grad.item()])
+    errs = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(ours, ref)]
+    werr = float(np.linalg.norm(ours_w - ref_w) / np.linalg.norm(ref_w))
+    print(json.dumps({"case": "rollout 100 steps, CUDA adjoint vs FP64 VJP chain", "rel_l2_err": errs,
+                      "wind_rel_err": werr}))
+    assert max(errs) <= 1e-4 and werr <= 1e-4, (errs, werr)
+    sim.cleanUp()
