@@ -333,6 +333,87 @@ def run_multilevel(ctx, args, levels=((128, 64, 512), (256, 128, 128), (512, 256
             "per_member_sample": len(sample)}
 
 
+def run_adjoint(ctx, n=256, n_steps=400, every=10, n_points=64):
+    """Adjoint of the CDKLM16 rollout: the Gaussian bump (n x n, dx = dy =
+    200 m, H = 60 m, f = 1.2e-4, walls, 0.1 m amplitude, sigma 10 cells) with
+    uniform wind stress (1e-4, 0) m^2/s^2, CFL 0.45, n_steps RK2 steps; loss =
+    squared (u, v) misfit at n_points seeded cells every `every` steps against
+    a truth run from half the bump without wind.  Times forward and backward
+    of the autograd rollout with CUDA events on torch's stream, with the whole
+    trajectory kept and with sqrt(N) checkpointing, and the kernels alone
+    (one step VJP against one fused step)."""
+    import torch
+    from gpuocean_gb300.adjoint import CDKLM16Rollout, StepAdjoint
+    from gpuocean_gb300.SWEsimulators import CDKLM16
+    x = (np.arange(n + 4) - 2 + 0.5 - n / 2.0)
+    eta = (0.1 * np.exp(-(x[None, :] ** 2 + x[:, None] ** 2) / 200.0)).astype(np.float32)
+    z = np.zeros_like(eta)
+    H = np.full((n + 5, n + 5), 60.0, np.float32)
+    sim = CDKLM16.CDKLM16(ctx, eta, z, z.copy(), H, n, n, 200.0, 200.0, 0.0, 9.81, 1.2e-4, 0.0)
+    sim.updateDt(courant_number=0.45)
+    rng = np.random.default_rng(3)
+    idx = rng.choice(n * n, size=n_points, replace=False)
+    rows, cols = idx // n, idx % n
+    out = {"config": f"bump {n}x{n}, wind (1e-4, 0), {n_steps} steps, (u, v) misfit at {n_points} cells every "
+                     f"{every} steps", "dt": float(sim.dt)}
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    for label, frac in (("stored", 0.5), ("checkpointed", 0.0)):
+        adj = StepAdjoint(sim, memory_fraction=frac)
+        dev = adj.device
+        Hm = torch.as_tensor(np.asarray(sim.downloadBathymetry()[1], np.float32)[2:-2, 2:-2], device=dev)
+        q0 = adj.state(*sim.download())
+        with torch.no_grad():
+            t0 = [a.clone() for a in q0]
+            t0[0] *= 0.5
+            ts = CDKLM16Rollout.apply(adj, n_steps, every, *t0, torch.zeros(2, device=dev))
+            hh = ts[:, 0] + Hm
+            u_obs = ts[:, 1, rows, cols] / hh[:, rows, cols]
+            v_obs = ts[:, 2, rows, cols] / hh[:, rows, cols]
+        times = []
+        for _ in range(3):
+            xs = [a.clone().requires_grad_(True) for a in q0]
+            w = torch.tensor([1.0e-4, 0.0], device=dev, requires_grad=True)
+            e0, e1, e2 = ev(), ev(), ev()
+            torch.cuda.synchronize()
+            e0.record()
+            st = CDKLM16Rollout.apply(adj, n_steps, every, *xs, w)
+            hh = st[:, 0] + Hm
+            loss = ((st[:, 1, rows, cols] / hh[:, rows, cols] - u_obs) ** 2).sum() + \
+                   ((st[:, 2, rows, cols] / hh[:, rows, cols] - v_obs) ** 2).sum()
+            e1.record()
+            loss.backward()
+            e2.record()
+            torch.cuda.synchronize()
+            times.append((e0.elapsed_time(e1), e1.elapsed_time(e2)))
+        fwd, bwd = times[-1]
+        out[label] = {"segment_steps": adj.segment_length(n_steps), "forward_ms": fwd, "backward_ms": bwd,
+                      "adjoint_over_forward": bwd / fwd}
+    # kernels alone: one step VJP (two stage-VJP launches) against one fused step
+    qa, qb, qs = adj.zeros(), adj.zeros(), adj.zeros()
+    la, ls, ln = adj.zeros(), adj.zeros(), adj.zeros()
+    for a, b in zip(qa, q0):
+        a.copy_(b)
+    adj.step_with_stage(qa, qb, qs)
+
+    def timeit(fn, reps=200):
+        for _ in range(10):
+            fn()
+        a, b = ev(), ev()
+        torch.cuda.synchronize()
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    t_step = timeit(lambda: adj.step(qa, qb))
+    t_vjp = timeit(lambda: adj.step_vjp(qa, qs, la, ls, ln))
+    out["kernels"] = {"step_ms": t_step, "step_vjp_ms": t_vjp, "vjp_over_step": t_vjp / t_step}
+    sim.cleanUp()
+    return out
+
+
 # ---------------------------------------------------------------------------
 # main arm
 # ---------------------------------------------------------------------------
@@ -348,6 +429,7 @@ def main():
     ap.add_argument("--per-member-sample", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-multilevel", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     rank, world, local = dist_env()
     spec = workload_spec(args.workload, args.members if args.workload == "c3" else 1)
@@ -515,6 +597,7 @@ def main():
     per_member_rate = pm_cells / (time.perf_counter() - t0)
 
     multilevel = None if args.no_multilevel else run_multilevel(ctx, args)
+    adjoint = None if args.no_adjoint else run_adjoint(ctx)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -547,7 +630,7 @@ def main():
                          "peak_kind": peak_kind, "avg_launch_ms": 1000.0 * avg_dur,
                          "algorithmic_bytes_per_launch": avg_bytes},
             "e2e": e2e, "gpu_launches": launches, "clocks": clk, "cpu_baseline": cpu,
-            "multilevel": multilevel,
+            "multilevel": multilevel, "adjoint": adjoint,
             "wall_s": wall,
         }
         print(json.dumps(line), flush=True)

@@ -40,10 +40,11 @@ class StepAdjoint:
     """The RK2 step of ``sim`` (its parameters, bathymetry and Coriolis data)
     with a fixed dt and a uniform wind stress held in a device tensor."""
 
-    def __init__(self, sim, dt=None):
+    def __init__(self, sim, dt=None, memory_fraction=0.5):
         if int(sim.rk_order) != 2:
             raise ValueError("the adjoint covers the RK2 step only")
         self.sim = sim
+        self.memory_fraction = float(memory_fraction)
         self.nx, self.ny = int(sim.nx), int(sim.ny)
         self.dt = float(np.float32(sim.dt if dt is None else dt))
         self.device = torch.device("cuda", torch.cuda.current_device())
@@ -85,6 +86,22 @@ class StepAdjoint:
                   *[_ptr(a) for a in q_in], *[_ptr(a) for a in q_out], self.pitch,
                   self.Hi.ptr, int(self.Hi.pitch), self.Hm.ptr, int(self.Hm.pitch), self._stream())
 
+    def step_with_stage(self, q_in, q_out, q_star):
+        """One RK2 step that also keeps the first-stage state Q*."""
+        _lib.call("goc_cdklm_rk2_step_stage", ctypes.byref(self.params), ctypes.c_float(self.dt),
+                  *[_ptr(a) for a in q_in], *[_ptr(a) for a in q_out], *[_ptr(a) for a in q_star], self.pitch,
+                  self.Hi.ptr, int(self.Hi.pitch), self.Hm.ptr, int(self.Hm.pitch), self._stream())
+
+    def segment_length(self, n_steps):
+        """Steps per checkpoint segment: all of them when the trajectory and
+        its first stages fit in ``memory_fraction`` of the free device
+        memory (no recompute), else ceil(sqrt(n_steps))."""
+        need = 2 * n_steps * 3 * 4 * (self.nx + 4) * (self.ny + 4)
+        free, _ = torch.cuda.mem_get_info(self.device)
+        if self.memory_fraction > 0 and need <= self.memory_fraction * free:
+            return n_steps
+        return max(1, int(math.ceil(math.sqrt(n_steps))))
+
     def stage1(self, q_in, q_star):
         _lib.call("goc_cdklm_stage", ctypes.byref(self.params), ctypes.c_float(self.dt), 0,
                   *[_ptr(a) for a in q_in], *[_ptr(a) for a in q_star], None, None, None, self.pitch,
@@ -110,53 +127,73 @@ class CDKLM16Rollout(torch.autograd.Function):
     """``apply(adj, n_steps, obs_every, eta0, hu0, hv0, wind)`` ->
     interior states (n_steps // obs_every, 3, ny, nx) after steps
     obs_every, 2 obs_every, ...  eta0/hu0/hv0: (ny+4, nx+4) float32 CUDA
-    tensors (ghost cells are ignored); wind: (2,) stress."""
+    tensors (ghost cells are ignored); wind: (2,) stress.
+
+    The forward keeps every K-th state (K from ``adj.segment_length``); the
+    backward sweep recomputes each segment once, keeping its states and
+    first stages, and runs the step VJPs over it in reverse.  With K =
+    n_steps (the whole trajectory fits) nothing is recomputed."""
 
     @staticmethod
     def forward(ctx, adj, n_steps, obs_every, eta0, hu0, hv0, wind):
         n_steps, obs_every = int(n_steps), int(obs_every)
         if n_steps < 1 or obs_every < 1:
             raise ValueError("n_steps and obs_every must be >= 1")
-        adj.set_wind(wind.detach())
-        K = max(1, int(math.ceil(math.sqrt(n_steps))))
-        q = [a.detach().to(torch.float32).contiguous().clone() for a in (eta0, hu0, hv0)]
-        buf = [torch.empty_like(a) for a in q]
-        ckpts = {0: [a.clone() for a in q]}
-        outs = []
-        for n in range(n_steps):
-            adj.step(q, buf)
-            q, buf = buf, q
-            if (n + 1) % K == 0 and n + 1 < n_steps:
-                ckpts[n + 1] = [a.clone() for a in q]
-            if (n + 1) % obs_every == 0:
-                outs.append(torch.stack([a[2:-2, 2:-2] for a in q]))
-        ctx.adj, ctx.K, ctx.n_steps, ctx.obs_every, ctx.ckpts = adj, K, n_steps, obs_every, ckpts
-        if not outs:
+        if n_steps < obs_every:
             raise ValueError("n_steps must be at least obs_every")
+        adj.set_wind(wind.detach())
+        K = adj.segment_length(n_steps)
+        q = [a.detach().to(torch.float32).contiguous().clone() for a in (eta0, hu0, hv0)]
+        outs = []
+        if K >= n_steps:
+            # the whole trajectory with its first stages
+            states, stars = [q], []
+            for n in range(n_steps):
+                nxt, qs = [torch.empty_like(a) for a in q], [torch.empty_like(a) for a in q]
+                adj.step_with_stage(states[-1], nxt, qs)
+                states.append(nxt)
+                stars.append(qs)
+                if (n + 1) % obs_every == 0:
+                    outs.append(torch.stack([a[2:-2, 2:-2] for a in nxt]))
+            ctx.segments = {0: (states, stars)}
+        else:
+            buf = [torch.empty_like(a) for a in q]
+            ctx.segments = {0: ([a.clone() for a in q], None)}
+            for n in range(n_steps):
+                adj.step(q, buf)
+                q, buf = buf, q
+                if (n + 1) % K == 0 and n + 1 < n_steps:
+                    ctx.segments[n + 1] = ([a.clone() for a in q], None)
+                if (n + 1) % obs_every == 0:
+                    outs.append(torch.stack([a[2:-2, 2:-2] for a in q]))
+        ctx.adj, ctx.K, ctx.n_steps, ctx.obs_every = adj, K, n_steps, obs_every
         return torch.stack(outs)
 
     @staticmethod
     def backward(ctx, grad):
         adj, K, n_steps, every = ctx.adj, ctx.K, ctx.n_steps, ctx.obs_every
         grad = grad.contiguous()
-        lam, lam_n, lam_s, q_s = adj.zeros(), adj.zeros(), adj.zeros(), adj.zeros()
+        lam, lam_n, lam_s = adj.zeros(), adj.zeros(), adj.zeros()
         wind_bar = torch.zeros(2, dtype=torch.float32, device=adj.device)
-        for start in sorted(ctx.ckpts, reverse=True):
+        for start in sorted(ctx.segments, reverse=True):
             end = min(start + K, n_steps)
-            states = [ctx.ckpts[start]]
-            for _ in range(start, end - 1):
-                nxt = [torch.empty_like(a) for a in states[-1]]
-                adj.step(states[-1], nxt)
-                states.append(nxt)
+            states, stars = ctx.segments[start]
+            if stars is None:
+                states, stars = [states], []
+                for _ in range(start, end):
+                    nxt = [torch.empty_like(a) for a in states[-1]]
+                    qs = [torch.empty_like(a) for a in states[-1]]
+                    adj.step_with_stage(states[-1], nxt, qs)
+                    states.append(nxt)
+                    stars.append(qs)
             for n in range(end - 1, start - 1, -1):
                 if (n + 1) % every == 0:
                     g = grad[(n + 1) // every - 1]
                     for c in range(3):
                         lam[c][2:-2, 2:-2] += g[c]
-                q_n = states[n - start]
-                adj.stage1(q_n, q_s)
-                wind_bar += adj.step_vjp(q_n, q_s, lam, lam_s, lam_n)
+                wind_bar += adj.step_vjp(states[n - start], stars[n - start], lam, lam_s, lam_n)
                 lam, lam_n = lam_n, lam
-            del states
-        ctx.ckpts = None
+            del states, stars
+            ctx.segments[start] = None
+        ctx.segments = None
         return None, None, None, lam[0], lam[1], lam[2], wind_bar

@@ -88,6 +88,26 @@ extern "C" int goc_cdklm_rk2_step(const GocCdklmParams* p, float dt, const float
                        Hi, Hi_pitch / 4, Hm, Hm_pitch / 4, st);
 }
 
+extern "C" int goc_cdklm_rk2_step_stage(const GocCdklmParams* p, float dt, const float* eta0, const float* hu0,
+                                        const float* hv0, float* eta1, float* hu1, float* hv1, float* eta_s,
+                                        float* hu_s, float* hv_s, int pitch, const float* Hi, int Hi_pitch,
+                                        const float* Hm, int Hm_pitch, void* stream) {
+    int rc = validate_params(p, "goc_cdklm_rk2_step_stage");
+    if (rc) return rc;
+    if ((rc = check_pitch(p, pitch, Hi_pitch, Hm_pitch, "goc_cdklm_rk2_step_stage"))) return rc;
+    if (!eta0 || !hu0 || !hv0 || !eta1 || !hu1 || !hv1 || !eta_s || !hu_s || !hv_s || !Hi || !Hm)
+        return set_error(GOC_ERR_ARG, "goc_cdklm_rk2_step_stage: null buffer");
+    if (eta0 == eta1 || eta_s == eta0 || eta_s == eta1)
+        return set_error(GOC_ERR_ARG, "goc_cdklm_rk2_step_stage: the three buffer sets must differ");
+    if (p->rk_order != 2) return set_error(GOC_ERR_ARG, "goc_cdklm_rk2_step_stage: params.rk_order must be 2");
+    StepConst k;
+    bool cf, sf;
+    cudaStream_t st = as_stream(stream);
+    if ((rc = make_const(p, &k, &cf, &sf))) return rc;
+    return dispatch<2>(p, k, cf, sf, dt, 1, eta0, hu0, hv0, eta1, hu1, hv1, eta_s, hu_s, hv_s, pitch / 4, Hi,
+                       Hi_pitch / 4, Hm, Hm_pitch / 4, st);
+}
+
 extern "C" int goc_cdklm_stage(const GocCdklmParams* p, float dt, int rk_step, const float* eta_in,
                                const float* hu_in, const float* hv_in, float* eta_out, float* hu_out,
                                float* hv_out, float* eta_alt, float* hu_alt, float* hv_alt, int pitch,

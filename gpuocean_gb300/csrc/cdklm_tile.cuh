@@ -579,6 +579,12 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
             const bool okx = !BORDER || px || (gx >= 2 && gx < nx + 2);
             const bool oky = !BORDER || py || (gy >= 2 && gy < ny + 2);
             if (!(okx && oky)) continue;
+            // the first-stage state of the tile's own cells, when asked for
+            // (the adjoint's second-stage VJP reads it)
+            if (e_alt && i >= HALO && i < HALO + TX && j >= HALO && j < HALO + TY && gx < nx + 2 && gy < ny + 2) {
+                const size_t os = (size_t)gy * pitch + gx;
+                e_alt[os] = qe[r]; hu_alt[os] = qu[r]; hv_alt[os] = qv[r];
+            }
             float oe, ou, ov;
             desingularize_cell(p, qe[r], qu[r], qv[r], S.Hmb[j][i], oe, ou, ov);
             S.D[0][j][i] = oe; S.D[1][j][i] = ou; S.D[2][j][i] = ov;

@@ -122,6 +122,19 @@ int goc_cdklm_rk2_step(const GocCdklmParams* p, float dt,
                        void* stream);
 
 /*
+ * goc_cdklm_rk2_step that also writes the first-stage state Q* of the
+ * interior cells to (eta_s, hu_s, hv_s): the same values goc_cdklm_stage
+ * with rk_step 0 gives, at no extra launch.  For the adjoint's recompute of
+ * a rollout segment (no counterpart in the reference).
+ */
+int goc_cdklm_rk2_step_stage(const GocCdklmParams* p, float dt,
+                             const float* eta0, const float* hu0, const float* hv0,
+                             float* eta1, float* hu1, float* hv1,
+                             float* eta_s, float* hu_s, float* hv_s, int pitch,
+                             const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch,
+                             void* stream);
+
+/*
  * One Runge-Kutta stage, reference semantics: cdklm_swe_2D
  * (K/CDKLM16_kernel.cu:475-1090) with rk_step = step_.  Interior cells of
  * the output set are written; for RK2 stage 1 and RK3 stages 1-2 the output

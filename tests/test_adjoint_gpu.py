@@ -403,3 +403,38 @@ def test_rollout_adjoint_matches_fp64_vjp_chain(ctx):
                       "wind_rel_err": werr}))
     assert max(errs) <= 1e-4 and werr <= 1e-4, (errs, werr)
     sim.cleanUp()
+
+
+def test_checkpointed_rollout_equals_stored_rollout(ctx):
+    """sqrt(N) checkpointing recomputes segments with the same kernels: the
+    gradient is bit-identical to the one from the fully stored trajectory,
+    and the fused step that keeps Q* matches the step and the first-stage
+    kernels bit for bit."""
+    from gpuocean_gb300.adjoint import CDKLM16Rollout, StepAdjoint
+    c = _bump_case(64, moving=True)
+    sim = _sim(ctx, c, 0.0)
+    sim.updateDt(courant_number=0.45)
+    q0 = None
+    grads = []
+    for frac in (0.5, 0.0):
+        adj = StepAdjoint(sim, memory_fraction=frac)
+        assert (adj.segment_length(37) == 37) == (frac > 0)
+        q0 = adj.state(*sim.download())
+        x = [a.clone().requires_grad_(True) for a in q0]
+        w = torch.tensor([1.0e-4, -3.0e-5], device=adj.device, requires_grad=True)
+        st = CDKLM16Rollout.apply(adj, 37, 5, *x, w)
+        (st[:, 1] ** 2).sum().backward()
+        grads.append([a.grad.clone() for a in x] + [w.grad.clone()])
+    for a, b in zip(*grads):
+        assert torch.equal(a, b)
+    # the fused step with Q* against the plain step and the first stage
+    q1, q1b, qs, qs_ref = adj.zeros(), adj.zeros(), adj.zeros(), adj.zeros()
+    adj.step_with_stage(q0, q1, qs)
+    adj.step(q0, q1b)
+    adj.stage1(q0, qs_ref)
+    torch.cuda.synchronize()
+    for a, b in zip(q1, q1b):
+        assert torch.equal(a[2:-2, 2:-2], b[2:-2, 2:-2])
+    for a, b in zip(qs, qs_ref):
+        assert torch.equal(a[2:-2, 2:-2], b[2:-2, 2:-2])
+    sim.cleanUp()
