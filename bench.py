@@ -307,6 +307,7 @@ def run_multilevel(ctx, args, levels=((128, 64, 512), (256, 128, 128), (512, 256
         cells += ens.step(MODEL_TIME_STEP, apply_stochastic_term=True)
     ens.synchronize()
     batched = cells / (time.perf_counter() - t0)
+    shape = list(ens.tile_shape)
     ens.release()
     # member by member: a sample of every level, stepped from Python
     sample = [s for lv in range(len(levels)) for s in sims[sum(l[2] for l in levels[:lv]):][:8]]
@@ -330,7 +331,7 @@ def run_multilevel(ctx, args, levels=((128, 64, 512), (256, 128, 128), (512, 256
     return {"workload": "c4", "levels": [list(l) for l in levels], "members": len(sims),
             "value": batched, "unit": "member-cell-steps/s", "blocks": blocks,
             "per_member_baseline": per_member, "batched_over_per_member": batched / per_member,
-            "per_member_sample": len(sample)}
+            "per_member_sample": len(sample), "tile_shape": shape}
 
 
 def run_adjoint(ctx, n=256, n_steps=400, every=10, n_points=64):
@@ -619,7 +620,10 @@ def main():
                                        f"L={NOISE_L_COARSE:g} coarse cells, std {NOISE_STD} m") if noise else None,
                        "substeps_per_block": int(sched[3]), "l2": "inputs larger than L2"
                        if 24 * sum(int(s.nx) * int(s.ny) for s in sims) > 129e6 else "inputs smaller than L2",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}",
+                       "tile_shape": list(ens.tile_shape),
+                       "autotune_ms_per_launch": {f"{a}x{b}": t for (a, b), t in
+                                                  getattr(ens, "autotune_timings", {}).items()}},
             "per_member_baseline": {"value": per_member_rate, "unit": "member-cell-steps/s",
                                     "members_sampled": len(pm_sims),
                                     "batched_over_per_member": value / world / per_member_rate},

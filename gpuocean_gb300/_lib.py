@@ -101,6 +101,10 @@ SIGNATURES = {
     "goc_ensemble_set_schedule": (c_int, [c_void_p, c_fp, ctypes.POINTER(c_int), c_void_p]),
     "goc_ensemble_rk2_substep": (c_int, [c_void_p, c_int, c_void_p]),
     "goc_ensemble_end_block": (c_int, [c_void_p, c_int, c_void_p]),
+    "goc_ensemble_tile_shape_count": (c_int, []),
+    "goc_ensemble_tile_shape": (c_int, [c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
+    "goc_ensemble_set_tile_shape": (c_int, [c_void_p, c_int]),
+    "goc_ensemble_get_tile_shape": (c_int, [c_void_p, ctypes.POINTER(c_int)]),
     "goc_ensemble_get_member": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "goc_ensemble_max_dt": (c_int, [c_void_p, c_void_p, c_void_p]),
     "goc_ensemble_set_drifters": (c_int, [c_void_p, c_void_p, ctypes.POINTER(c_int), c_float, c_void_p]),

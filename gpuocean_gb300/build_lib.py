@@ -28,6 +28,8 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 EXTRA = {"noise.cu": ["-use_fast_math"],
          "cdklm_step.cu": ["-fmad=false"],
          "ensemble.cu": ["-fmad=false"],
+         **{f"ensemble_shape_{tx}x{ty}.cu": ["-fmad=false"]
+            for tx, ty in ((32, 16), (32, 8), (16, 16), (64, 8), (32, 24))},
          "cdklm_adjoint.cu": ["-fmad=false"]}
 
 

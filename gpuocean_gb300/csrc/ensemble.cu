@@ -2,103 +2,15 @@
 // advances in one persistent launch per RK2 step over a member/tile work
 // queue, instead of one Python-driven launch sequence per member
 // (E/OceanNoiseEnsemble.py:517-543, E/MultiLevelOceanEnsemble.py:95-141).
-#include <algorithm>
 #include <cstdio>
-#include <vector>
 
-#include "cdklm_tile.cuh"
-#include "cfl.cuh"
-#include "drift.cuh"
+#include "ensemble.cuh"
 
 namespace goc {
-
-struct Ensemble {
-    int n_members = 0;
-    int n_tiles = 0;
-    int max_substeps = 0;
-    int n_dt_items = 0;
-    bool const_f = true, simple = true;
-    std::vector<GocMemberDesc> host;      // descriptors as created (set 0 current)
-    GocMemberDesc* d_members = nullptr;   // device copy, buffers swapped on device
-    int4* d_tiles = nullptr;              // (member, tile_x, tile_y, 0)
-    float* d_dt = nullptr;                // n_members x max_substeps
-    int* d_nsub = nullptr;                // n_substeps per member
-    int4* d_dt_items = nullptr;           // CFL work: (member, bx, by, partial index)
-    int2* d_dt_ranges = nullptr;          // per member [first partial, count)
-    float* d_partials = nullptr;          // CFL scratch
-    // drifters: one (N_m + 1) x 2 position array per member
-    float** d_drift_pos = nullptr;        // per member, null = no drifters
-    int4* d_drift_chunks = nullptr;       // (member, first drifter, count, 0)
-    int n_drift_chunks = 0;
-    float drift_sensitivity = 1.0f;
-};
-
-constexpr int kDriftChunk = 256;
-
-__device__ __forceinline__ DriftGrid member_drift_grid(const GocMemberDesc& d, int set) {
-    return DriftGrid{d.p.nx, d.p.ny, d.p.dx, d.p.dy, 2, 2, d.eta[set], d.hu[set], d.hv[set], d.pitch / 4,
-                     d.Hm, d.Hm_pitch / 4, d.p.bc_north == 2, d.p.bc_east == 2};
-}
-
-// Advect one chunk of a member's drifters with the state of buffer set `set`.
-__device__ __forceinline__ void drift_chunk(const GocMemberDesc& d, float* pos, int first, int count, int set,
-                                           float dt, float sensitivity) {
-    const DriftGrid g = member_drift_grid(d, set);
-    for (int q = threadIdx.x; q < count; q += blockDim.x) {
-        float* p = pos + 2 * (size_t)(first + q);
-        float px = p[0], py = p[1];
-        drift_one(g, nullptr, dt, sensitivity, px, py);
-        p[0] = px;
-        p[1] = py;
-    }
-}
 
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
-
-template <bool CONST_F, bool SIMPLE_FORCING>
-__global__ void __launch_bounds__(kNT, 3)
-ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __restrict__ tiles, int n_tiles,
-                    const float* __restrict__ dt_table, const int* __restrict__ nsub, int max_sub, int k,
-                    float* const* __restrict__ drift_pos, const int4* __restrict__ drift_chunks, int n_chunks,
-                    float sensitivity) {
-    extern __shared__ __align__(16) float smem_raw[];
-    __shared__ GocMemberDesc md;
-    __shared__ StepConst kc;
-    int cur = -1;
-    // Work items: the RK2 tiles of step k, then (for k >= 1) the drifter
-    // chunks of step k-1, which read the input state of step k (buffer set
-    // k % 2) that no tile of this launch writes.
-    const int n_items = n_tiles + (k >= 1 ? n_chunks : 0);
-    for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
-        if (item >= n_tiles) {
-            const int4 c = drift_chunks[item - n_tiles];
-            if (k - 1 >= __ldg(nsub + c.x)) continue;
-            drift_chunk(members[c.x], drift_pos[c.x], c.y, c.z, k & 1,
-                        __ldg(dt_table + (size_t)c.x * max_sub + (k - 1)), sensitivity);
-            continue;
-        }
-        const int4 t = tiles[item];
-        const int m = t.x;
-        if (k >= __ldg(nsub + m)) continue;  // member already at the end of its block
-        if (m != cur) {
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                md = members[m];
-                kc = make_step_const(md.p);
-            }
-            __syncthreads();
-            cur = m;
-        }
-        const int in = k & 1, out = in ^ 1;
-        const float dt = __ldg(dt_table + (size_t)m * max_sub + k);
-        cdklm_tile<kTX, kTY, 2, kNT, CONST_F, SIMPLE_FORCING>(
-            md.p, kc, dt, 1, t.y, t.z, md.eta[in], md.hu[in], md.hv[in], md.eta[out], md.hu[out], md.hv[out],
-            nullptr, nullptr, nullptr, md.pitch / 4, md.Hi, md.Hi_pitch / 4, md.Hm, md.Hm_pitch / 4, smem_raw);
-        __syncthreads();
-    }
-}
 
 // Drift of the last step of members that ran all `n_launched` steps of the block.
 __global__ void ensemble_end_drift_kernel(const GocMemberDesc* __restrict__ members, const int* __restrict__ nsub,
@@ -159,43 +71,6 @@ __global__ void __launch_bounds__(256) ensemble_dt_final_kernel(const float* __r
     }
 }
 
-// Kernel attributes and the persistent grid are set up once per variant,
-// outside any stream capture (goc_ensemble_create calls this).
-template <bool CF, bool SF>
-static int configure_ensemble_kernel(int* grid_out) {
-    constexpr size_t smem = sizeof(TileSmem<kTX + 8, kTY + 8>);
-    static int grid = 0;
-    if (grid == 0) {
-        auto kern = ensemble_rk2_kernel<CF, SF>;
-        cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(err));
-        int blocks = 0;
-        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, kNT, smem);
-        if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(err));
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        grid = std::max(1, sms) * std::max(1, blocks);
-    }
-    *grid_out = grid;
-    return GOC_OK;
-}
-
-template <bool CF, bool SF>
-static int launch_ensemble(Ensemble* e, int k, cudaStream_t st) {
-    constexpr size_t smem = sizeof(TileSmem<kTX + 8, kTY + 8>);
-    auto kern = ensemble_rk2_kernel<CF, SF>;
-    int full = 0;
-    int rc = configure_ensemble_kernel<CF, SF>(&full);
-    if (rc) return rc;
-    const int items = e->n_tiles + (k >= 1 ? e->n_drift_chunks : 0);
-    const int grid = std::min(items, full);
-    kern<<<grid, kNT, smem, st>>>(e->d_members, e->d_tiles, e->n_tiles, e->d_dt, e->d_nsub, e->max_substeps, k,
-                                  e->d_drift_pos, e->d_drift_chunks, e->n_drift_chunks, e->drift_sensitivity);
-    count_launch();
-    return check_launch("ensemble_rk2_kernel");
-}
-
 static void free_ensemble(Ensemble* e) {
     cudaFree(e->d_members);
     cudaFree(e->d_tiles);
@@ -219,6 +94,49 @@ const GocMemberDesc* ensemble_device_members(void* ensemble) { return static_cas
 
 const int* ensemble_device_nsub(void* ensemble) { return static_cast<Ensemble*>(ensemble)->d_nsub; }
 
+static int shape_configure(const Ensemble* e, int* grid) {
+    switch (e->shape) {
+        case 0: return ensemble_configure_shape<32, 16>(e, grid);
+        case 1: return ensemble_configure_shape<32, 8>(e, grid);
+        case 2: return ensemble_configure_shape<16, 16>(e, grid);
+        case 3: return ensemble_configure_shape<64, 8>(e, grid);
+        case 4: return ensemble_configure_shape<32, 24>(e, grid);
+    }
+    return set_error(GOC_ERR_ARG, "ensemble: tile shape %d out of range", e->shape);
+}
+
+static int shape_launch(Ensemble* e, int k, cudaStream_t st) {
+    switch (e->shape) {
+        case 0: return ensemble_launch_shape<32, 16>(e, k, st);
+        case 1: return ensemble_launch_shape<32, 8>(e, k, st);
+        case 2: return ensemble_launch_shape<16, 16>(e, k, st);
+        case 3: return ensemble_launch_shape<64, 8>(e, k, st);
+        case 4: return ensemble_launch_shape<32, 24>(e, k, st);
+    }
+    return set_error(GOC_ERR_ARG, "ensemble: tile shape %d out of range", e->shape);
+}
+
+// (Re)build the member/tile work queue for the ensemble's tile shape.
+static int build_tiles(Ensemble* e) {
+    const TileShape sh = kEnsembleShapes[e->shape];
+    std::vector<int4> tiles;
+    for (int m = 0; m < e->n_members; ++m) {
+        const GocCdklmParams& p = e->host[m].p;
+        const int tx = (p.nx + sh.tx - 1) / sh.tx, ty = (p.ny + sh.ty - 1) / sh.ty;
+        for (int j = 0; j < ty; ++j)
+            for (int i = 0; i < tx; ++i) tiles.push_back(make_int4(m, i, j, 0));
+    }
+    cudaFree(e->d_tiles);
+    e->d_tiles = nullptr;
+    cudaError_t err = cudaMalloc(&e->d_tiles, sizeof(int4) * tiles.size());
+    if (err == cudaSuccess)
+        err = cudaMemcpy(e->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice);
+    if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "ensemble tile queue: %s", cudaGetErrorString(err));
+    e->n_tiles = (int)tiles.size();
+    int grid = 0;
+    return shape_configure(e, &grid);
+}
+
 }  // namespace goc
 
 using namespace goc;
@@ -232,7 +150,7 @@ extern "C" int goc_ensemble_create(const GocMemberDesc* members, int n_members, 
     e->n_members = n_members;
     e->max_substeps = max_substeps;
     e->host.assign(members, members + n_members);
-    std::vector<int4> tiles, dt_items;
+    std::vector<int4> dt_items;
     std::vector<int2> ranges;
     for (int m = 0; m < n_members; ++m) {
         const GocMemberDesc& d = members[m];
@@ -254,22 +172,17 @@ extern "C" int goc_ensemble_create(const GocMemberDesc* members, int n_members, 
         e->const_f = e->const_f && d.p.coriolis_nx == 1 && d.p.coriolis_ny == 1;
         e->simple = e->simple && d.p.wind_x_nx == 1 && d.p.wind_x_ny == 1 && d.p.wind_y_nx == 1 &&
                     d.p.wind_y_ny == 1 && d.p.atm_p_nx == 1 && d.p.atm_p_ny == 1;
-        const int tx = (d.p.nx + kTX - 1) / kTX, ty = (d.p.ny + kTY - 1) / kTY;
-        for (int j = 0; j < ty; ++j)
-            for (int i = 0; i < tx; ++i) tiles.push_back(make_int4(m, i, j, 0));
         const int bx = (d.p.nx + kDtBX - 1) / kDtBX, by = (d.p.ny + kDtBY - 1) / kDtBY;
         ranges.push_back(make_int2((int)dt_items.size(), bx * by));
         for (int j = 0; j < by; ++j)
             for (int i = 0; i < bx; ++i) dt_items.push_back(make_int4(m, i, j, (int)dt_items.size()));
     }
-    e->n_tiles = (int)tiles.size();
     e->n_dt_items = (int)dt_items.size();
     cudaError_t err = cudaSuccess;
     auto alloc = [&](void** p, size_t bytes) {
         if (err == cudaSuccess) err = cudaMalloc(p, bytes);
     };
     alloc((void**)&e->d_members, sizeof(GocMemberDesc) * n_members);
-    alloc((void**)&e->d_tiles, sizeof(int4) * tiles.size());
     alloc((void**)&e->d_dt, sizeof(float) * (size_t)n_members * max_substeps);
     alloc((void**)&e->d_nsub, sizeof(int) * n_members);
     alloc((void**)&e->d_dt_items, sizeof(int4) * dt_items.size());
@@ -277,7 +190,6 @@ extern "C" int goc_ensemble_create(const GocMemberDesc* members, int n_members, 
     alloc((void**)&e->d_partials, sizeof(float) * dt_items.size());
     if (err == cudaSuccess)
         err = cudaMemcpy(e->d_members, members, sizeof(GocMemberDesc) * n_members, cudaMemcpyHostToDevice);
-    if (err == cudaSuccess) err = cudaMemcpy(e->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice);
     if (err == cudaSuccess)
         err = cudaMemcpy(e->d_dt_items, dt_items.data(), sizeof(int4) * dt_items.size(), cudaMemcpyHostToDevice);
     if (err == cudaSuccess)
@@ -288,11 +200,7 @@ extern "C" int goc_ensemble_create(const GocMemberDesc* members, int n_members, 
         free_ensemble(e);
         return set_error(GOC_ERR_CUDA, "goc_ensemble_create: %s", cudaGetErrorString(err));
     }
-    int grid = 0, rc = GOC_OK;
-    if (e->const_f && e->simple) rc = configure_ensemble_kernel<true, true>(&grid);
-    else if (e->const_f) rc = configure_ensemble_kernel<true, false>(&grid);
-    else if (e->simple) rc = configure_ensemble_kernel<false, true>(&grid);
-    else rc = configure_ensemble_kernel<false, false>(&grid);
+    int rc = build_tiles(e);
     if (rc) {
         free_ensemble(e);
         return rc;
@@ -340,11 +248,35 @@ extern "C" int goc_ensemble_rk2_substep(void* ensemble, int k, void* stream) {
     if (!ensemble) return set_error(GOC_ERR_ARG, "goc_ensemble_rk2_substep: null handle");
     Ensemble* e = static_cast<Ensemble*>(ensemble);
     if (k < 0 || k >= e->max_substeps) return set_error(GOC_ERR_ARG, "goc_ensemble_rk2_substep: k=%d out of range", k);
-    cudaStream_t st = as_stream(stream);
-    if (e->const_f && e->simple) return launch_ensemble<true, true>(e, k, st);
-    if (e->const_f) return launch_ensemble<true, false>(e, k, st);
-    if (e->simple) return launch_ensemble<false, true>(e, k, st);
-    return launch_ensemble<false, false>(e, k, st);
+    return shape_launch(e, k, as_stream(stream));
+}
+
+extern "C" int goc_ensemble_tile_shape_count(void) { return kNumEnsembleShapes; }
+
+extern "C" int goc_ensemble_tile_shape(int index, int* tx, int* ty) {
+    if (index < 0 || index >= kNumEnsembleShapes || !tx || !ty)
+        return set_error(GOC_ERR_ARG, "goc_ensemble_tile_shape: index %d out of range", index);
+    *tx = kEnsembleShapes[index].tx;
+    *ty = kEnsembleShapes[index].ty;
+    return GOC_OK;
+}
+
+extern "C" int goc_ensemble_set_tile_shape(void* ensemble, int index) {
+    if (!ensemble) return set_error(GOC_ERR_ARG, "goc_ensemble_set_tile_shape: null handle");
+    if (index < 0 || index >= kNumEnsembleShapes)
+        return set_error(GOC_ERR_ARG, "goc_ensemble_set_tile_shape: index %d out of range", index);
+    Ensemble* e = static_cast<Ensemble*>(ensemble);
+    if (e->shape == index) return GOC_OK;
+    cudaError_t err = cudaDeviceSynchronize();   // the old queue may be in use
+    if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_ensemble_set_tile_shape: %s", cudaGetErrorString(err));
+    e->shape = index;
+    return build_tiles(e);
+}
+
+extern "C" int goc_ensemble_get_tile_shape(void* ensemble, int* index) {
+    if (!ensemble || !index) return set_error(GOC_ERR_ARG, "goc_ensemble_get_tile_shape: null argument");
+    *index = static_cast<Ensemble*>(ensemble)->shape;
+    return GOC_OK;
 }
 
 extern "C" int goc_ensemble_end_block(void* ensemble, int n_launched, void* stream) {

@@ -1,0 +1,183 @@
+// Batched ensemble engine: shared declarations of the host handle, the
+// persistent member/tile kernel (templated on the tile shape) and its
+// launchers.  Each tile shape is instantiated in a translation unit of its
+// own (ensemble_shape_*.cu) so that the variants compile in parallel.
+#pragma once
+
+#include <algorithm>
+#include <vector>
+
+#include "cdklm_tile.cuh"
+#include "cfl.cuh"
+#include "drift.cuh"
+
+namespace goc {
+
+// Output tile shapes (cells) the engine can run; the autotuner picks one per
+// ensemble.  Index 0 is the default.
+struct TileShape { int tx, ty; };
+constexpr TileShape kEnsembleShapes[] = {{32, 16}, {32, 8}, {16, 16}, {64, 8}, {32, 24}};
+constexpr int kNumEnsembleShapes = sizeof(kEnsembleShapes) / sizeof(kEnsembleShapes[0]);
+
+// CTAs per SM the shared memory of a shape allows (at most 3), used as the
+// launch-bounds occupancy target of its kernel.
+template <int TX, int TY>
+constexpr int shape_min_blocks() {
+    return (int)(3 * sizeof(TileSmem<TX + 8, TY + 8>) <= 227 * 1024 ? 3
+               : 2 * sizeof(TileSmem<TX + 8, TY + 8>) <= 227 * 1024 ? 2 : 1);
+}
+
+struct Ensemble {
+    int n_members = 0;
+    int n_tiles = 0;
+    int max_substeps = 0;
+    int n_dt_items = 0;
+    bool const_f = true, simple = true;
+    std::vector<GocMemberDesc> host;      // descriptors as created (set 0 current)
+    GocMemberDesc* d_members = nullptr;   // device copy, buffers swapped on device
+    int4* d_tiles = nullptr;              // (member, tile_x, tile_y, 0)
+    float* d_dt = nullptr;                // n_members x max_substeps
+    int* d_nsub = nullptr;                // n_substeps per member
+    int4* d_dt_items = nullptr;           // CFL work: (member, bx, by, partial index)
+    int2* d_dt_ranges = nullptr;          // per member [first partial, count)
+    float* d_partials = nullptr;          // CFL scratch
+    // drifters: one (N_m + 1) x 2 position array per member
+    float** d_drift_pos = nullptr;        // per member, null = no drifters
+    int4* d_drift_chunks = nullptr;       // (member, first drifter, count, 0)
+    int n_drift_chunks = 0;
+    float drift_sensitivity = 1.0f;
+    int shape = 0;                        // index into kEnsembleShapes
+};
+
+constexpr int kDriftChunk = 256;
+
+__device__ __forceinline__ DriftGrid member_drift_grid(const GocMemberDesc& d, int set) {
+    return DriftGrid{d.p.nx, d.p.ny, d.p.dx, d.p.dy, 2, 2, d.eta[set], d.hu[set], d.hv[set], d.pitch / 4,
+                     d.Hm, d.Hm_pitch / 4, d.p.bc_north == 2, d.p.bc_east == 2};
+}
+
+// Advect one chunk of a member's drifters with the state of buffer set `set`.
+__device__ __forceinline__ void drift_chunk(const GocMemberDesc& d, float* pos, int first, int count, int set,
+                                           float dt, float sensitivity) {
+    const DriftGrid g = member_drift_grid(d, set);
+    for (int q = threadIdx.x; q < count; q += blockDim.x) {
+        float* p = pos + 2 * (size_t)(first + q);
+        float px = p[0], py = p[1];
+        drift_one(g, nullptr, dt, sensitivity, px, py);
+        p[0] = px;
+        p[1] = py;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// the persistent RK2 kernel
+// ---------------------------------------------------------------------------
+
+template <int TX, int TY, int MINB, bool CONST_F, bool SIMPLE_FORCING>
+__global__ void __launch_bounds__(kNT, MINB)
+ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __restrict__ tiles, int n_tiles,
+                    const float* __restrict__ dt_table, const int* __restrict__ nsub, int max_sub, int k,
+                    float* const* __restrict__ drift_pos, const int4* __restrict__ drift_chunks, int n_chunks,
+                    float sensitivity) {
+    extern __shared__ __align__(16) float smem_raw[];
+    __shared__ GocMemberDesc md;
+    __shared__ StepConst kc;
+    int cur = -1;
+    // Work items: the RK2 tiles of step k, then (for k >= 1) the drifter
+    // chunks of step k-1, which read the input state of step k (buffer set
+    // k % 2) that no tile of this launch writes.
+    const int n_items = n_tiles + (k >= 1 ? n_chunks : 0);
+    for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+        if (item >= n_tiles) {
+            const int4 c = drift_chunks[item - n_tiles];
+            if (k - 1 >= __ldg(nsub + c.x)) continue;
+            drift_chunk(members[c.x], drift_pos[c.x], c.y, c.z, k & 1,
+                        __ldg(dt_table + (size_t)c.x * max_sub + (k - 1)), sensitivity);
+            continue;
+        }
+        const int4 t = tiles[item];
+        const int m = t.x;
+        if (k >= __ldg(nsub + m)) continue;  // member already at the end of its block
+        if (m != cur) {
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                md = members[m];
+                kc = make_step_const(md.p);
+            }
+            __syncthreads();
+            cur = m;
+        }
+        const int in = k & 1, out = in ^ 1;
+        const float dt = __ldg(dt_table + (size_t)m * max_sub + k);
+        cdklm_tile<TX, TY, 2, kNT, CONST_F, SIMPLE_FORCING>(
+            md.p, kc, dt, 1, t.y, t.z, md.eta[in], md.hu[in], md.hv[in], md.eta[out], md.hu[out], md.hv[out],
+            nullptr, nullptr, nullptr, md.pitch / 4, md.Hi, md.Hi_pitch / 4, md.Hm, md.Hm_pitch / 4, smem_raw);
+        __syncthreads();
+    }
+}
+
+// Kernel attributes and the persistent grid are set up once per variant,
+// outside any stream capture (goc_ensemble_create calls this).
+template <int TX, int TY, bool CF, bool SF>
+int configure_ensemble_kernel(int* grid_out) {
+    constexpr size_t smem = sizeof(TileSmem<TX + 8, TY + 8>);
+    static int grid = 0;
+    if (grid == 0) {
+        auto kern = ensemble_rk2_kernel<TX, TY, shape_min_blocks<TX, TY>(), CF, SF>;
+        cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(err));
+        int blocks = 0;
+        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, kNT, smem);
+        if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(err));
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        grid = std::max(1, sms) * std::max(1, blocks);
+    }
+    *grid_out = grid;
+    return GOC_OK;
+}
+
+template <int TX, int TY, bool CF, bool SF>
+int launch_ensemble(Ensemble* e, int k, cudaStream_t st) {
+    constexpr size_t smem = sizeof(TileSmem<TX + 8, TY + 8>);
+    auto kern = ensemble_rk2_kernel<TX, TY, shape_min_blocks<TX, TY>(), CF, SF>;
+    int full = 0;
+    int rc = configure_ensemble_kernel<TX, TY, CF, SF>(&full);
+    if (rc) return rc;
+    const int items = e->n_tiles + (k >= 1 ? e->n_drift_chunks : 0);
+    const int grid = std::min(items, full);
+    kern<<<grid, kNT, smem, st>>>(e->d_members, e->d_tiles, e->n_tiles, e->d_dt, e->d_nsub, e->max_substeps, k,
+                                  e->d_drift_pos, e->d_drift_chunks, e->n_drift_chunks, e->drift_sensitivity);
+    count_launch();
+    return check_launch("ensemble_rk2_kernel");
+}
+
+// Launchers of one tile shape (explicitly instantiated per shape).
+template <int TX, int TY>
+int ensemble_configure_shape(const Ensemble* e, int* grid) {
+    if (e->const_f && e->simple) return configure_ensemble_kernel<TX, TY, true, true>(grid);
+    if (e->const_f) return configure_ensemble_kernel<TX, TY, true, false>(grid);
+    if (e->simple) return configure_ensemble_kernel<TX, TY, false, true>(grid);
+    return configure_ensemble_kernel<TX, TY, false, false>(grid);
+}
+
+template <int TX, int TY>
+int ensemble_launch_shape(Ensemble* e, int k, cudaStream_t st) {
+    if (e->const_f && e->simple) return launch_ensemble<TX, TY, true, true>(e, k, st);
+    if (e->const_f) return launch_ensemble<TX, TY, true, false>(e, k, st);
+    if (e->simple) return launch_ensemble<TX, TY, false, true>(e, k, st);
+    return launch_ensemble<TX, TY, false, false>(e, k, st);
+}
+
+#define GOC_ENSEMBLE_SHAPE_EXTERN(TX, TY)                                           \
+    extern template int ensemble_configure_shape<TX, TY>(const Ensemble*, int*);     \
+    extern template int ensemble_launch_shape<TX, TY>(Ensemble*, int, cudaStream_t);
+GOC_ENSEMBLE_SHAPE_EXTERN(32, 16)
+GOC_ENSEMBLE_SHAPE_EXTERN(32, 8)
+GOC_ENSEMBLE_SHAPE_EXTERN(16, 16)
+GOC_ENSEMBLE_SHAPE_EXTERN(64, 8)
+GOC_ENSEMBLE_SHAPE_EXTERN(32, 24)
+#undef GOC_ENSEMBLE_SHAPE_EXTERN
+
+}  // namespace goc

@@ -1,0 +1,7 @@
+// The batched ensemble kernel with 32x8 output tiles.
+#include "ensemble.cuh"
+
+namespace goc {
+template int ensemble_configure_shape<32, 8>(const Ensemble*, int*);
+template int ensemble_launch_shape<32, 8>(Ensemble*, int, cudaStream_t);
+}  // namespace goc

@@ -22,6 +22,10 @@ from .. import _lib
 from ..utils import Common
 
 
+# member grid signature -> index of the fastest tile shape (per process)
+_AUTOTUNE_CACHE = {}
+
+
 class GocMemberDesc(ctypes.Structure):
     """Mirror of ``GocMemberDesc`` in include/gpuocean_gb300.h."""
     _fields_ = [
@@ -52,7 +56,7 @@ class BatchedEnsemble:
     use_graph: replay each distinct block schedule as a CUDA graph.
     """
 
-    def __init__(self, sims, share_bathymetry=None, use_graph=True, stream=None):
+    def __init__(self, sims, share_bathymetry=None, use_graph=True, stream=None, autotune=True):
         assert len(sims) > 0
         for s in sims:
             assert int(s.rk_order) == 2, "the batched engine runs the fused RK2 step"
@@ -66,11 +70,14 @@ class BatchedEnsemble:
         self._noises = None
         self._rng_seed = None
         self._bathy_owner = list(range(len(sims)))
+        self._shape_index = 0
         if share_bathymetry is None:
             share_bathymetry = True
         if share_bathymetry:
             self._dedupe_bathymetry()
         self._build()
+        if autotune:
+            self.autotune()
 
     # ------------------------------------------------------------------
     def _dedupe_bathymetry(self):
@@ -108,6 +115,8 @@ class BatchedEnsemble:
         h = ctypes.c_void_p()
         _lib.call("goc_ensemble_create", self._descs_host, len(self.sims), int(max_substeps), ctypes.byref(h))
         self._handle = h.value
+        if self._shape_index:
+            _lib.call("goc_ensemble_set_tile_shape", self._handle, int(self._shape_index))
         self.max_substeps = int(max_substeps)
         self._ptrs = self._current_ptrs()
         self._graphs = {}
@@ -157,6 +166,79 @@ class BatchedEnsemble:
         nm, nt = ctypes.c_int(), ctypes.c_int()
         _lib.call("goc_ensemble_size", self._handle, ctypes.byref(nm), ctypes.byref(nt))
         return nt.value
+
+    # ------------------------------------------------------------------
+    @staticmethod
+    def tile_shapes():
+        """The output tile shapes (cells) the persistent kernel can run."""
+        lib = _lib.load()
+        out = []
+        for i in range(lib.goc_ensemble_tile_shape_count()):
+            tx, ty = ctypes.c_int(), ctypes.c_int()
+            _lib.call("goc_ensemble_tile_shape", i, ctypes.byref(tx), ctypes.byref(ty))
+            out.append((tx.value, ty.value))
+        return out
+
+    @property
+    def tile_shape(self):
+        return self.tile_shapes()[self._shape_index]
+
+    def set_tile_shape(self, index):
+        _lib.call("goc_ensemble_set_tile_shape", self._handle, int(index))
+        self._shape_index = int(index)
+        for g in self._graphs.values():
+            _lib.load().goc_graph_destroy(g[0])
+        self._graphs = {}
+
+    def _grid_signature(self):
+        sizes = {}
+        for s in self.sims:
+            key = (int(s.nx), int(s.ny))
+            sizes[key] = sizes.get(key, 0) + 1
+        flags = tuple(sorted({(s.coriolis_cell is None, int(s.boundary_conditions.east)) for s in self.sims}))
+        return (tuple(sorted(sizes.items())), flags)
+
+    def autotune(self, repeats=5, candidates=None):
+        """Time the persistent RK2 launch of every tile shape on this
+        ensemble and keep the fastest.  Each timed launch is RK2 step 0 of a
+        one-step schedule: it reads buffer set 0 (the current state) and
+        writes set 1, so the members' state is left as it was.  Results are
+        cached per process by member grid sizes."""
+        sig = self._grid_signature()
+        best = _AUTOTUNE_CACHE.get(sig)
+        if best is None:
+            shapes = self.tile_shapes()
+            idx = list(range(len(shapes))) if candidates is None else list(candidates)
+            n = len(self.sims)
+            table = np.zeros((n, self.max_substeps), dtype=np.float32)
+            table[:, 0] = [np.float32(s.dt) for s in self.sims]
+            nsub = np.ones(n, dtype=np.int32)
+            _lib.call("goc_ensemble_set_schedule", self._handle, table.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                      nsub.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), self.stream.handle)
+            self._sched_key = None
+            ev = [ctypes.c_void_p(), ctypes.c_void_p()]
+            for e in ev:
+                _lib.call("goc_event_create", ctypes.byref(e))
+            timings = {}
+            for i in idx:
+                _lib.call("goc_ensemble_set_tile_shape", self._handle, int(i))
+                for _ in range(2):
+                    _lib.call("goc_ensemble_rk2_substep", self._handle, 0, self.stream.handle)
+                _lib.call("goc_event_record", ev[0], self.stream.handle)
+                for _ in range(repeats):
+                    _lib.call("goc_ensemble_rk2_substep", self._handle, 0, self.stream.handle)
+                _lib.call("goc_event_record", ev[1], self.stream.handle)
+                self.stream.synchronize()
+                ms = ctypes.c_float()
+                _lib.call("goc_event_elapsed_ms", ev[0], ev[1], ctypes.byref(ms))
+                timings[shapes[i]] = ms.value / repeats
+            for e in ev:
+                _lib.load().goc_event_destroy(e)
+            best = min(idx, key=lambda i: timings[shapes[i]])
+            _AUTOTUNE_CACHE[sig] = best
+            self.autotune_timings = timings
+        self.set_tile_shape(best)
+        return self.tile_shape
 
     # ------------------------------------------------------------------
     def _schedule(self, t_end):

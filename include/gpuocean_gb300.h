@@ -368,6 +368,19 @@ int goc_ensemble_set_schedule(void* ensemble, const float* dt_table, const int* 
  */
 int goc_ensemble_rk2_substep(void* ensemble, int k, void* stream);
 
+/*
+ * Output tile shapes of the persistent kernel (no counterpart in the
+ * reference).  goc_ensemble_tile_shape gives shape `index` in cells;
+ * goc_ensemble_set_tile_shape rebuilds the member/tile work queue for it
+ * (synchronises the device; call outside stream capture, and re-capture
+ * graphs afterwards).  Every shape computes bit-identical states; the
+ * autotuner (BatchedEnsemble.autotune) times them and keeps the fastest.
+ */
+int goc_ensemble_tile_shape_count(void);
+int goc_ensemble_tile_shape(int index, int* tx, int* ty);
+int goc_ensemble_set_tile_shape(void* ensemble, int index);
+int goc_ensemble_get_tile_shape(void* ensemble, int* index);
+
 /* Close a block of `n_launched` substeps: advects the drifters of the last
  * step of members that ran all of them, then makes buffer set 0 the current
  * state again (swaps members whose block had an odd number of steps).

@@ -64,7 +64,8 @@ def test_member_counts_and_shared_bathymetry(gpu_ctx):
     a = [_member(gpu_ctx, 64, 40, (1, 2, 1, 2), 3) for _ in range(3)] + [_member(gpu_ctx, 64, 40, (1, 2, 1, 2), 9)]
     ens = BatchedEnsemble(a)
     assert ens._bathy_owner == [0, 0, 0, 3]
-    assert ens.n_tiles == 4 * 2 * 3
+    tx, ty = ens.tile_shape
+    assert ens.n_tiles == 4 * ((64 + tx - 1) // tx) * ((40 + ty - 1) // ty)
 
 
 def _with_noise(sims, factor, seed):
@@ -177,3 +178,42 @@ def test_ensemble_classes_run(gpu_ctx):
     assert all(abs(s.t - 120.0) < 1e-6 for s in ml.members)
     est = ml.estimate(np.mean)
     assert est.shape == (3, 40, 64) and np.all(np.isfinite(est))
+
+
+def test_every_tile_shape_gives_identical_states(gpu_ctx):
+    """The autotuner may pick any tile shape: each computes bit-identical
+    states (the per-cell arithmetic does not depend on the tiling)."""
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
+    shapes = BatchedEnsemble.tile_shapes()
+    assert len(shapes) >= 3 and shapes[0] == (32, 16)
+    results = []
+    for idx in range(len(shapes)):
+        a = [_member(gpu_ctx, *s, drifters=20) for s in SPECS]
+        for s in a:
+            s.updateDt()
+        ens = BatchedEnsemble(a, autotune=False)
+        ens.set_tile_shape(idx)
+        assert ens.tile_shape == shapes[idx]
+        for _ in range(2):
+            ens.step(60.0)
+        ens.synchronize()
+        results.append([[np.asarray(x)[2:-2, 2:-2] for x in s.download()] for s in a])
+        ens.release()
+    for r in results[1:]:
+        for sa, sb in zip(results[0], r):
+            for x, y in zip(sa, sb):
+                assert np.array_equal(x, y)
+
+
+def test_autotune_keeps_the_state_and_picks_a_shape(gpu_ctx):
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble, _AUTOTUNE_CACHE
+    a = [_member(gpu_ctx, *s) for s in SPECS]
+    before = [[np.asarray(x)[2:-2, 2:-2].copy() for x in s.download()] for s in a]
+    _AUTOTUNE_CACHE.clear()
+    ens = BatchedEnsemble(a, autotune=True)
+    assert ens.tile_shape in BatchedEnsemble.tile_shapes()
+    assert set(ens.autotune_timings) == set(BatchedEnsemble.tile_shapes())
+    after = [[np.asarray(x)[2:-2, 2:-2] for x in s.download()] for s in a]
+    for sa, sb in zip(before, after):
+        for x, y in zip(sa, sb):
+            assert np.array_equal(x, y)
