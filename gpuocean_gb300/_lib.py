@@ -94,6 +94,9 @@ SIGNATURES = {
     "goc_drift": (c_int, [c_int, c_int, c_float, c_float, c_float, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int,
                           c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_float,
                           c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_float, c_float, c_void_p]),
+    "goc_drift_vjp": (c_int, [c_int, c_int, c_float, c_float, c_float, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                              c_int, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_float,
+                              c_void_p, c_void_p, c_void_p, c_void_p]),
     "goc_drift_enforce_boundary": (c_int, [c_float, c_float, c_int, c_int, c_int, c_void_p, c_int, c_void_p]),
     "goc_ensemble_create": (c_int, [c_void_p, c_int, c_int, ctypes.POINTER(c_void_p)]),
     "goc_ensemble_destroy": (c_int, [c_void_p]),

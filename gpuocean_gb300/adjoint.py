@@ -107,6 +107,26 @@ class StepAdjoint:
                   *[_ptr(a) for a in q_in], *[_ptr(a) for a in q_star], None, None, None, self.pitch,
                   self.Hi.ptr, int(self.Hi.pitch), self.Hm.ptr, int(self.Hm.pitch), self._stream())
 
+    def drift(self, q, positions):
+        """Advect (N, 2) positions in place by one forward-Euler step with the
+        state q (the state after the step, as CDKLM16.drifterStep does)."""
+        n = positions.shape[0]
+        b = self.sim.boundary_conditions
+        z = ctypes.c_void_p(self.wind.data_ptr())
+        _lib.call("goc_drift", self.nx, self.ny, ctypes.c_float(self.sim.dx), ctypes.c_float(self.sim.dy),
+                  ctypes.c_float(self.dt), 2, 2, *[_ptr(a) for a in q], self.pitch, self.Hm.ptr, int(self.Hm.pitch),
+                  int(b.isPeriodicNorthSouth()), int(b.isPeriodicEastWest()), n - 1, _ptr(positions), 8,
+                  ctypes.c_float(1.0), z, z, z, z, 1, 1, ctypes.c_float(0.0), ctypes.c_float(0.0), self._stream())
+
+    def drift_vjp(self, q, positions, pos_bar, lam):
+        """pos_bar (N, 2): adjoint of the positions after the drift on entry,
+        of those before on return; the state adjoint is added to lam."""
+        b = self.sim.boundary_conditions
+        _lib.call("goc_drift_vjp", self.nx, self.ny, ctypes.c_float(self.sim.dx), ctypes.c_float(self.sim.dy),
+                  ctypes.c_float(self.dt), 2, 2, *[_ptr(a) for a in q], self.pitch, self.Hm.ptr, int(self.Hm.pitch),
+                  int(b.isPeriodicNorthSouth()), int(b.isPeriodicEastWest()), positions.shape[0], _ptr(positions), 8,
+                  _ptr(pos_bar), 8, ctypes.c_float(1.0), *[_ptr(a) for a in lam], self._stream())
+
     def step_vjp(self, q_n, q_star, lam_next, lam_star, lam_n):
         """lam_n = (dQ^{n+1}/dQ^n)^T lam_next on interior cells; returns the
         gradient contribution for the wind stress (x, y) as a device tensor."""
@@ -123,6 +143,93 @@ class StepAdjoint:
         return self.wsf * self.partials.view(2, -1, 2).sum(dim=(0, 1))
 
 
+def _rollout_forward(ctx, adj, n_steps, obs_every, init, wind, positions0):
+    n_steps, obs_every = int(n_steps), int(obs_every)
+    if n_steps < 1 or obs_every < 1:
+        raise ValueError("n_steps and obs_every must be >= 1")
+    if n_steps < obs_every:
+        raise ValueError("n_steps must be at least obs_every")
+    adj.set_wind(wind.detach())
+    K = adj.segment_length(n_steps)
+    q = [a.detach().to(torch.float32).contiguous().clone() for a in init]
+    outs, pouts = [], []
+    pos = None
+    track = []
+    if positions0 is not None:
+        pos = positions0.detach().to(torch.float32).contiguous().clone()
+        track = [pos.clone()]
+    if K >= n_steps:
+        states, stars = [q], []
+        for n in range(n_steps):
+            nxt, qs = [torch.empty_like(a) for a in q], [torch.empty_like(a) for a in q]
+            adj.step_with_stage(states[-1], nxt, qs)
+            states.append(nxt)
+            stars.append(qs)
+            if pos is not None:
+                adj.drift(nxt, pos)
+                track.append(pos.clone())
+            if (n + 1) % obs_every == 0:
+                outs.append(torch.stack([a[2:-2, 2:-2] for a in nxt]))
+                if pos is not None:
+                    pouts.append(pos.clone())
+        ctx.segments = {0: (states, stars)}
+    else:
+        buf = [torch.empty_like(a) for a in q]
+        ctx.segments = {0: ([a.clone() for a in q], None)}
+        for n in range(n_steps):
+            adj.step(q, buf)
+            q, buf = buf, q
+            if pos is not None:
+                adj.drift(q, pos)
+                track.append(pos.clone())
+            if (n + 1) % K == 0 and n + 1 < n_steps:
+                ctx.segments[n + 1] = ([a.clone() for a in q], None)
+            if (n + 1) % obs_every == 0:
+                outs.append(torch.stack([a[2:-2, 2:-2] for a in q]))
+                if pos is not None:
+                    pouts.append(pos.clone())
+    ctx.adj, ctx.K, ctx.n_steps, ctx.obs_every, ctx.track = adj, K, n_steps, obs_every, track
+    return torch.stack(outs), (torch.stack(pouts) if pos is not None else None)
+
+
+def _rollout_backward(ctx, grad, grad_pos):
+    adj, K, n_steps, every = ctx.adj, ctx.K, ctx.n_steps, ctx.obs_every
+    grad = grad.contiguous() if grad is not None else None
+    lam, lam_n, lam_s = adj.zeros(), adj.zeros(), adj.zeros()
+    wind_bar = torch.zeros(2, dtype=torch.float32, device=adj.device)
+    track = ctx.track
+    pos_bar = torch.zeros_like(track[0]) if track else None
+    for start in sorted(ctx.segments, reverse=True):
+        end = min(start + K, n_steps)
+        states, stars = ctx.segments[start]
+        if stars is None:
+            states, stars = [states], []
+            for _ in range(start, end):
+                nxt = [torch.empty_like(a) for a in states[-1]]
+                qs = [torch.empty_like(a) for a in states[-1]]
+                adj.step_with_stage(states[-1], nxt, qs)
+                states.append(nxt)
+                stars.append(qs)
+        for n in range(end - 1, start - 1, -1):
+            if (n + 1) % every == 0:
+                k = (n + 1) // every - 1
+                if grad is not None:
+                    for c in range(3):
+                        lam[c][2:-2, 2:-2] += grad[k, c]
+                if pos_bar is not None and grad_pos is not None:
+                    pos_bar += grad_pos[k]
+            if pos_bar is not None:
+                # the drift after step n read the state after it
+                adj.drift_vjp(states[n + 1 - start], track[n], pos_bar, lam)
+            wind_bar += adj.step_vjp(states[n - start], stars[n - start], lam, lam_s, lam_n)
+            lam, lam_n = lam_n, lam
+        del states, stars
+        ctx.segments[start] = None
+    ctx.segments = None
+    ctx.track = None
+    return lam, wind_bar, pos_bar
+
+
 class CDKLM16Rollout(torch.autograd.Function):
     """``apply(adj, n_steps, obs_every, eta0, hu0, hv0, wind)`` ->
     interior states (n_steps // obs_every, 3, ny, nx) after steps
@@ -136,64 +243,30 @@ class CDKLM16Rollout(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, adj, n_steps, obs_every, eta0, hu0, hv0, wind):
-        n_steps, obs_every = int(n_steps), int(obs_every)
-        if n_steps < 1 or obs_every < 1:
-            raise ValueError("n_steps and obs_every must be >= 1")
-        if n_steps < obs_every:
-            raise ValueError("n_steps must be at least obs_every")
-        adj.set_wind(wind.detach())
-        K = adj.segment_length(n_steps)
-        q = [a.detach().to(torch.float32).contiguous().clone() for a in (eta0, hu0, hv0)]
-        outs = []
-        if K >= n_steps:
-            # the whole trajectory with its first stages
-            states, stars = [q], []
-            for n in range(n_steps):
-                nxt, qs = [torch.empty_like(a) for a in q], [torch.empty_like(a) for a in q]
-                adj.step_with_stage(states[-1], nxt, qs)
-                states.append(nxt)
-                stars.append(qs)
-                if (n + 1) % obs_every == 0:
-                    outs.append(torch.stack([a[2:-2, 2:-2] for a in nxt]))
-            ctx.segments = {0: (states, stars)}
-        else:
-            buf = [torch.empty_like(a) for a in q]
-            ctx.segments = {0: ([a.clone() for a in q], None)}
-            for n in range(n_steps):
-                adj.step(q, buf)
-                q, buf = buf, q
-                if (n + 1) % K == 0 and n + 1 < n_steps:
-                    ctx.segments[n + 1] = ([a.clone() for a in q], None)
-                if (n + 1) % obs_every == 0:
-                    outs.append(torch.stack([a[2:-2, 2:-2] for a in q]))
-        ctx.adj, ctx.K, ctx.n_steps, ctx.obs_every = adj, K, n_steps, obs_every
-        return torch.stack(outs)
+        states, _ = _rollout_forward(ctx, adj, n_steps, obs_every, (eta0, hu0, hv0), wind, None)
+        return states
 
     @staticmethod
     def backward(ctx, grad):
-        adj, K, n_steps, every = ctx.adj, ctx.K, ctx.n_steps, ctx.obs_every
-        grad = grad.contiguous()
-        lam, lam_n, lam_s = adj.zeros(), adj.zeros(), adj.zeros()
-        wind_bar = torch.zeros(2, dtype=torch.float32, device=adj.device)
-        for start in sorted(ctx.segments, reverse=True):
-            end = min(start + K, n_steps)
-            states, stars = ctx.segments[start]
-            if stars is None:
-                states, stars = [states], []
-                for _ in range(start, end):
-                    nxt = [torch.empty_like(a) for a in states[-1]]
-                    qs = [torch.empty_like(a) for a in states[-1]]
-                    adj.step_with_stage(states[-1], nxt, qs)
-                    states.append(nxt)
-                    stars.append(qs)
-            for n in range(end - 1, start - 1, -1):
-                if (n + 1) % every == 0:
-                    g = grad[(n + 1) // every - 1]
-                    for c in range(3):
-                        lam[c][2:-2, 2:-2] += g[c]
-                wind_bar += adj.step_vjp(states[n - start], stars[n - start], lam, lam_s, lam_n)
-                lam, lam_n = lam_n, lam
-            del states, stars
-            ctx.segments[start] = None
-        ctx.segments = None
+        lam, wind_bar, _ = _rollout_backward(ctx, grad, None)
         return None, None, None, lam[0], lam[1], lam[2], wind_bar
+
+
+class CDKLM16DrifterRollout(torch.autograd.Function):
+    """``apply(adj, n_steps, obs_every, eta0, hu0, hv0, wind, positions0)``
+    -> (states, positions): the rollout of ``CDKLM16Rollout`` with passive
+    drifters (N, 2) advected after every step by the state after it
+    (``CDKLM16.drifterStep``, S/CDKLM16.py:575 and
+    D/GPUDrifterCollection.py:198-233, D/ = src/gpuocean/drifters); positions
+    (n_obs, N, 2) at the observation steps.  Gradients of a loss of either
+    output flow to the initial state, the wind stress and the initial
+    positions.  No wind drift."""
+
+    @staticmethod
+    def forward(ctx, adj, n_steps, obs_every, eta0, hu0, hv0, wind, positions0):
+        return _rollout_forward(ctx, adj, n_steps, obs_every, (eta0, hu0, hv0), wind, positions0)
+
+    @staticmethod
+    def backward(ctx, grad, grad_pos):
+        lam, wind_bar, pos_bar = _rollout_backward(ctx, grad, grad_pos)
+        return None, None, None, lam[0], lam[1], lam[2], wind_bar, pos_bar

@@ -269,6 +269,22 @@ int goc_drift(int nx, int ny, float dx, float dy, float dt, int x_zero_ref, int 
               const float* wind_y_cur, const float* wind_y_next, int wind_nx, int wind_ny,
               float wind_t, float wind_drift_factor, void* stream);
 
+/*
+ * Adjoint of one goc_drift step without wind drift (no counterpart in the
+ * reference).  positions: the positions before the step; positions_bar
+ * holds the adjoint of the positions after the step on entry and of those
+ * before it on return.  The adjoint of the state the step read (interior
+ * cells; periodic ghost images folded onto their cells, wall ghosts carry
+ * none) is ADDED to (eta_bar, hu_bar, hv_bar) with atomic additions, so the
+ * summation order, and the last bits of the sums, vary between runs.
+ */
+int goc_drift_vjp(int nx, int ny, float dx, float dy, float dt, int x_zero_ref, int y_zero_ref,
+                  const float* eta, const float* hu, const float* hv, int pitch,
+                  const float* Hm, int Hm_pitch, int periodic_north_south, int periodic_east_west,
+                  int num_positions, const float* positions, int positions_pitch,
+                  float* positions_bar, int positions_bar_pitch, float sensitivity,
+                  float* eta_bar, float* hu_bar, float* hv_bar, void* stream);
+
 /* Periodic wrap of drifter positions; replaces enforceBoundaryConditions
  * (K/driftKernels.cu:187-223). */
 int goc_drift_enforce_boundary(float domain_size_x, float domain_size_y, int periodic_north_south,

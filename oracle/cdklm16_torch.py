@@ -347,3 +347,37 @@ class TorchCDKLM16:
         Q = periodic_ghosts(Q, self.nx, self.ny, self.bc)
         Qs = self._assemble(Q, self.stage(Q, None, X, Y, dt, 0))
         return self._assemble(Q, self.stage(Qs, Q, X, Y, dt, 1))
+
+
+def drift(positions, eta, hu, hv, Hm, nx, ny, dx, dy, dt, periodic_ns, periodic_ew, x0ref=2, y0ref=2):
+    """One forward-Euler drifter step on torch tensors: the restatement of
+    ``oracle.noise_oracle.drift`` (K/driftKernels.cu:74-183) for autograd.
+    positions (N, 2); eta, hu, hv, Hm full (ny+4, nx+4) arrays."""
+    u_f = hu / (Hm + eta)
+    v_f = hv / (Hm + eta)
+    x, y = positions[:, 0], positions[:, 1]
+    fx, fy = torch.floor(x / dx), torch.floor(y / dy)
+    cx = (fx + x0ref).long()
+    cy = (fy + y0ref).long()
+    frx, fry = x / dx - fx, y / dy - fy
+    x0 = torch.where(frx < 0.5, cx - 1, cx)
+    xf = torch.where(frx < 0.5, frx + 0.5, frx - 0.5)
+    y0 = torch.where(fry < 0.5, cy - 1, cy)
+    yf = torch.where(fry < 0.5, fry + 0.5, fry - 0.5)
+    x0c, x1c = x0.clamp(0, nx + 3), (x0 + 1).clamp(0, nx + 3)
+    y0c, y1c = y0.clamp(0, ny + 3), (y0 + 1).clamp(0, ny + 3)
+
+    def interp(fld):
+        a = (1 - xf) * fld[y0c, x0c] + xf * fld[y0c, x1c]
+        b = (1 - xf) * fld[y1c, x0c] + xf * fld[y1c, x1c]
+        return (1 - yf) * a + yf * b
+    x = x + interp(u_f) * dt
+    y = y + interp(v_f) * dt
+    Lx, Ly = nx * dx, ny * dy
+    if periodic_ew:
+        x = torch.where(x < 0, x + Lx, x)
+        x = torch.where(x > Lx, x - Lx, x)
+    if periodic_ns:
+        y = torch.where(y < 0, y + Ly, y)
+        y = torch.where(y > Ly, y - Ly, y)
+    return torch.stack([x, y], dim=1)

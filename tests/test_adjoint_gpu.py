@@ -438,3 +438,180 @@ def test_checkpointed_rollout_equals_stored_rollout(ctx):
     for a, b in zip(qs, qs_ref):
         assert torch.equal(a[2:-2, 2:-2], b[2:-2, 2:-2])
     sim.cleanUp()
+
+
+@pytest.mark.parametrize("name", ["walls_f", "periodic_xy"])
+def test_drift_vjp_matches_fp64_autograd(ctx, name):
+    """One drift step's VJP (position and state adjoints) against FP64
+    autograd of the torch restatement of the drift."""
+    from gpuocean_gb300.adjoint import StepAdjoint
+    from oracle.cdklm16_torch import drift as drift64, periodic_ghosts
+    c = _case(name)
+    sim = _sim(ctx, c, 5.0)
+    adj = StepAdjoint(sim)
+    q = adj.state(*sim.download())
+    # ghost cells as the step leaves them: periodic images (walls: untouched)
+    q1 = adj.zeros()
+    adj.step(q, q1)
+    rng = np.random.default_rng(8)
+    Lx, Ly = c["nx"] * c["dx"], c["ny"] * c["dy"]
+    n = 300
+    pos = torch.as_tensor(np.stack([rng.uniform(0, Lx, n), rng.uniform(0, Ly, n)], axis=1), dtype=torch.float32,
+                          device=adj.device)
+    pbar_after = rng.standard_normal((n, 2))
+    pbar = torch.as_tensor(pbar_after, dtype=torch.float32, device=adj.device).contiguous()
+    lam = adj.zeros()
+    adj.drift_vjp(q1, pos.clone(), pbar, lam)
+    torch.cuda.synchronize()
+    ours_p = pbar.double().cpu().numpy()
+    ours_l = [a.double().cpu().numpy()[2:-2, 2:-2] for a in lam]
+    Hm = torch.as_tensor(np.asarray(sim.downloadBathymetry()[1], dtype=np.float64))
+    interior = [torch.tensor(a.cpu().numpy().astype(np.float64)[2:-2, 2:-2], requires_grad=True) for a in q1]
+    full = [torch.as_tensor(a.cpu().numpy().astype(np.float64)) for a in q1]
+    full = [torch.cat([a[:2], torch.cat([a[2:-2, :2], b, a[2:-2, -2:]], dim=1), a[-2:]], dim=0)
+            for a, b in zip(full, interior)]
+    bc = BC(*c["bc"])
+    if bc.periodic_ew() or bc.periodic_ns():
+        full = periodic_ghosts(full, c["nx"], c["ny"], bc)
+    p0 = torch.tensor(pos.cpu().numpy().astype(np.float64), requires_grad=True)
+    p1 = drift64(p0, *full, Hm, c["nx"], c["ny"], c["dx"], c["dy"], adj.dt, bc.periodic_ns(), bc.periodic_ew())
+    (p1 * torch.as_tensor(pbar_after)).sum().backward()
+    ref_p = p0.grad.numpy()
+    ref_l = [a.grad.numpy() for a in interior]
+    ep = float(np.max(np.abs(ours_p - ref_p)) / np.max(np.abs(ref_p)))
+    el = [float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-30)) for a, b in zip(ours_l, ref_l)]
+    print(json.dumps({"case": f"drift VJP {name}", "rel_err_positions": ep, "rel_err_state": el}))
+    assert ep <= 1e-5 and max(el) <= 1e-5, (ep, el)
+    sim.cleanUp()
+
+
+def test_drifter_rollout_matches_fp64_chain_and_fd(ctx):
+    """100 steps of the moving bump with 64 drifters; loss = squared distance
+    of the drifters to target positions every 10 steps plus a (u, v) misfit.
+    The CUDA gradient against (a) the chain of FP64 autograd VJPs (stages and
+    drift) on the same FP32 trajectory and (b) central finite differences of
+    the FP64 oracle along a random initial-state direction."""
+    from gpuocean_gb300.adjoint import CDKLM16DrifterRollout, StepAdjoint
+    from oracle.cdklm16_torch import drift as drift64, periodic_ghosts
+    from oracle.noise_oracle import drift as drift_np
+    c = _bump_case(64, moving=True)
+    n_steps, every = 100, 10
+    sim = _sim(ctx, c, 0.0)
+    sim.updateDt(courant_number=0.45)
+    dt = float(sim.dt)
+    adj = StepAdjoint(sim)
+    dev = adj.device
+    tau = np.array([1.0e-4, 0.0], dtype=np.float32)
+    rng = np.random.default_rng(31)
+    L = c["nx"] * c["dx"]
+    nd = 64
+    p0 = np.stack([rng.uniform(0.2 * L, 0.8 * L, nd), rng.uniform(0.2 * L, 0.8 * L, nd)], axis=1).astype(np.float32)
+    target = torch.as_tensor(p0 + rng.normal(0.0, 50.0, p0.shape).astype(np.float32), device=dev)
+    q0 = adj.state(*sim.download())
+    x = [a.clone().requires_grad_(True) for a in q0]
+    w = torch.tensor(tau, device=dev, requires_grad=True)
+    pt = torch.as_tensor(p0, device=dev).requires_grad_(True)
+    st, ps = CDKLM16DrifterRollout.apply(adj, n_steps, every, *x, w, pt)
+    loss = ((ps - target) ** 2).sum() * 1.0e-4 + (st[:, 1, 10:20, 10:20] ** 2).sum()
+    loss.backward()
+    ours = [a.grad.double().cpu().numpy()[2:-2, 2:-2] for a in x]
+    ours_p = pt.grad.double().cpu().numpy()
+    ours_w = w.grad.double().cpu().numpy()
+
+    # (a) FP64 VJP chain on the FP32 trajectory
+    adj.set_wind(tau)
+    traj, stars, track = [[a.clone() for a in q0]], [], [torch.as_tensor(p0, device=dev)]
+    pos = track[0].clone()
+    for _ in range(n_steps):
+        qs, nxt = adj.zeros(), [torch.empty_like(a) for a in q0]
+        adj.step_with_stage(traj[-1], nxt, qs)
+        adj.drift(nxt, pos)
+        traj.append(nxt)
+        stars.append(qs)
+        track.append(pos.clone())
+    to64 = lambda v: [torch.tensor(a.cpu().numpy().astype(np.float64)) for a in v]
+    traj, stars = [to64(v) for v in traj], [to64(v) for v in stars]
+    track = [torch.tensor(a.cpu().numpy().astype(np.float64)) for a in track]
+    tq = _torch_ref(c, dt, None)
+    X = torch.tensor(float(tau[0]), dtype=torch.float64, requires_grad=True)
+    Y = torch.tensor(float(tau[1]), dtype=torch.float64, requires_grad=True)
+    Hm64 = torch.as_tensor(np.asarray(sim.downloadBathymetry()[1], dtype=np.float64))
+    tg = target.double().cpu()
+    nx, ny = c["nx"], c["ny"]
+    bc = tq.bc
+    lam = [torch.zeros(ny, nx, dtype=torch.float64) for _ in range(3)]
+    pbar = torch.zeros(nd, 2, dtype=torch.float64)
+
+    def with_interior(v):
+        inner = [a[2:-2, 2:-2].clone().requires_grad_(True) for a in v]
+        full = [torch.cat([a[:2], torch.cat([a[2:-2, :2], b, a[2:-2, -2:]], dim=1), a[-2:]], dim=0)
+                for a, b in zip(v, inner)]
+        return inner, full
+
+    for n in range(n_steps - 1, -1, -1):
+        if (n + 1) % every == 0:
+            k = (n + 1) // every - 1
+            pbar = pbar + 2.0e-4 * (track[n + 1] - tg)
+            s = traj[n + 1]
+            lam[1] = lam[1] + torch.zeros(ny, nx, dtype=torch.float64).index_put_(
+                (torch.arange(10, 20)[:, None], torch.arange(10, 20)[None, :]), 2.0 * s[1][12:22, 12:22])
+        # drift after step n (reads the state after it)
+        inner, full = with_interior(traj[n + 1])
+        pp = track[n].clone().requires_grad_(True)
+        p1 = drift64(pp, *full, Hm64, nx, ny, c["dx"], c["dy"], dt, bc.periodic_ns(), bc.periodic_ew())
+        (p1 * pbar).sum().backward()
+        pbar = pp.grad.clone()
+        lam = [a + b.grad for a, b in zip(lam, inner)]
+        # the step
+        qn = [a.clone().requires_grad_(True) for a in traj[n]]
+        qs = [a.clone().requires_grad_(True) for a in stars[n]]
+        out = tq.stage(periodic_ghosts(qs, nx, ny, bc), periodic_ghosts(qn, nx, ny, bc), X, Y, dt, 1)
+        sum((o * l).sum() for o, l in zip(out, lam)).backward()
+        lam_s = [a.grad[2:-2, 2:-2].clone() for a in qs]
+        lam_d = [a.grad[2:-2, 2:-2].clone() for a in qn]
+        qn2 = [a.clone().requires_grad_(True) for a in traj[n]]
+        out = tq.stage(periodic_ghosts(qn2, nx, ny, bc), None, X, Y, dt, 0)
+        sum((o * l).sum() for o, l in zip(out, lam_s)).backward()
+        lam = [a + b.grad[2:-2, 2:-2] for a, b in zip(lam_d, qn2)]
+    ref = [a.numpy() for a in lam]
+    errs = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(ours, ref)]
+    perr = float(np.linalg.norm(ours_p - pbar.numpy()) / np.linalg.norm(pbar.numpy()))
+    ref_w = np.array([X.grad.item(), Y.grad.item()])
+    werr = float(np.linalg.norm(ours_w - ref_w) / np.linalg.norm(ref_w))
+
+    # (b) FD of the FP64 oracle with drifters along a random state direction
+    o0 = OracleCDKLM16(c["eta"], c["hu"], c["hv"], c["H"], nx, ny, c["dx"], c["dy"], dt, c["g"], c["f"], c["r"],
+                       boundary_conditions=BC(*c["bc"]))
+    Hm_np = np.asarray(o0.Hm, dtype=np.float64)
+    base = [np.asarray(a.cpu().numpy(), dtype=np.float64) for a in q0]
+    tgt = target.double().cpu().numpy()
+
+    def loss64(q):
+        o = OracleCDKLM16(c["eta"], c["hu"], c["hv"], c["H"], nx, ny, c["dx"], c["dy"], dt, c["g"], c["f"], c["r"],
+                          boundary_conditions=BC(*c["bc"]))
+        o.Q0 = [a.copy() for a in q]
+        o.Q1 = [a.copy() for a in q]
+        sh = (ny + 4, nx + 4)
+        o.wind = (np.full(sh, float(tau[0])), np.full(sh, float(tau[1])))
+        p = p0.astype(np.float64)
+        total = 0.0
+        for k in range(n_steps):
+            o.step(dt)
+            p = drift_np(p, *o.Q0, Hm_np, nx, ny, c["dx"], c["dy"], dt, False, False)
+            if (k + 1) % every == 0:
+                total += 1.0e-4 * np.sum((p - tgt) ** 2) + np.sum(o.Q0[1][12:22, 12:22] ** 2)
+        return total
+    delta = [_smooth(rng, base[0].shape, s).astype(np.float64) for s in (0.01, 0.1, 0.1)]
+    for a in delta:
+        a[:2, :] = 0; a[-2:, :] = 0; a[:, :2] = 0; a[:, -2:] = 0
+    eps = 1.0e-3
+    fd = (loss64([b + eps * d for b, d in zip(base, delta)]) - loss64([b - eps * d for b, d in zip(base, delta)])) / (2 * eps)
+    ad = sum(float(np.sum(g * d[2:-2, 2:-2])) for g, d in zip(ours, delta))
+    gnorm = np.sqrt(sum(float(np.sum(g * g)) for g in ours))
+    dnorm = np.sqrt(sum(float(np.sum(d * d)) for d in delta))
+    fd_err = abs(ad - fd) / (gnorm * dnorm)
+    print(json.dumps({"case": "drifter rollout 100 steps", "chain_rel_l2": errs, "positions_rel": perr,
+                      "wind_rel": werr, "fd": [ad, fd, fd_err]}))
+    assert max(errs) <= 1e-4 and perr <= 1e-4 and werr <= 1e-4, (errs, perr, werr)
+    assert fd_err <= 1e-4, (ad, fd, fd_err)
+    sim.cleanUp()
