@@ -395,6 +395,8 @@ def run_adjoint(ctx, n=256, n_steps=400, every=10, n_points=64):
     for a, b in zip(qa, q0):
         a.copy_(b)
     adj.step_with_stage(qa, qb, qs)
+    for a in la:            # a dense adjoint: every reverse pass does its full work
+        a.normal_()
 
     def timeit(fn, reps=200):
         for _ in range(10):
@@ -412,7 +414,67 @@ def run_adjoint(ctx, n=256, n_steps=400, every=10, n_points=64):
     t_vjp = timeit(lambda: adj.step_vjp(qa, qs, la, ls, ln))
     out["kernels"] = {"step_ms": t_step, "step_vjp_ms": t_vjp, "vjp_over_step": t_vjp / t_step}
     sim.cleanUp()
+    out["batched"] = run_adjoint_batched(ctx, ev, timeit)
     return out
+
+
+def run_adjoint_batched(ctx, ev, timeit, n=128, members=128, n_steps=400, every=10, n_points=64):
+    """The adjoint over `members` members of the n x n bump at once (states
+    perturbed per member, one uniform wind each): one launch per forward step
+    and two per step VJP for all members."""
+    import torch
+    from gpuocean_gb300.adjoint import CDKLM16EnsembleRollout, EnsembleStepAdjoint
+    from gpuocean_gb300.SWEsimulators import CDKLM16
+    x = (np.arange(n + 4) - 2 + 0.5 - n / 2.0)
+    eta = (0.1 * np.exp(-(x[None, :] ** 2 + x[:, None] ** 2) / 200.0)).astype(np.float32)
+    z = np.zeros_like(eta)
+    sim = CDKLM16.CDKLM16(ctx, eta, z, z.copy(), np.full((n + 5, n + 5), 60.0, np.float32), n, n, 200.0, 200.0, 0.0,
+                          9.81, 1.2e-4, 0.0)
+    sim.updateDt(courant_number=0.45)
+    adj = EnsembleStepAdjoint(sim, members)
+    dev = adj.device
+    rng = np.random.default_rng(5)
+    base = torch.as_tensor(np.stack([np.asarray(a, np.float32) for a in sim.download()]), device=dev)
+    scale = torch.as_tensor(rng.uniform(0.8, 1.2, members), dtype=torch.float32, device=dev)
+    q0 = base.unsqueeze(0).repeat(members, 1, 1, 1)
+    q0[:, 0] *= scale[:, None, None]
+    winds = torch.as_tensor(rng.normal(0.0, 1.0e-4, (members, 2)), dtype=torch.float32, device=dev)
+    idx = rng.choice(n * n, size=n_points, replace=False)
+    rows, cols = idx // n, idx % n
+    with torch.no_grad():
+        t0 = q0.clone()
+        t0[:, 0] *= 0.5
+        ts = CDKLM16EnsembleRollout.apply(adj, n_steps, every, t0, torch.zeros_like(winds))
+    times = []
+    for _ in range(2):
+        q = q0.clone().requires_grad_(True)
+        w = winds.clone().requires_grad_(True)
+        e0, e1, e2 = ev(), ev(), ev()
+        torch.cuda.synchronize()
+        e0.record()
+        st = CDKLM16EnsembleRollout.apply(adj, n_steps, every, q, w)
+        loss = ((st[..., 1:, rows, cols] - ts[..., 1:, rows, cols]) ** 2).sum()
+        e1.record()
+        loss.backward()
+        e2.record()
+        torch.cuda.synchronize()
+        times.append((e0.elapsed_time(e1), e1.elapsed_time(e2)))
+    fwd, bwd = times[-1]
+    qa, qb, qs = adj.zeros(), adj.zeros(), adj.zeros()
+    qa.copy_(q0)
+    adj.step(qa, qb, qs)
+    la, ls, ln = adj.zeros(), adj.zeros(), adj.zeros()
+    la.normal_()
+    t_step = timeit(lambda: adj.step(qa, qb))
+    t_vjp = timeit(lambda: adj.step_vjp(qa, qs, la, ls, ln))
+    sim.cleanUp()
+    cells = members * n * n
+    return {"config": f"{members} members x {n}x{n} bump, per-member wind, {n_steps} steps, (hu, hv) misfit at "
+                      f"{n_points} cells every {every} steps", "segment_steps": adj.segment_length(n_steps),
+            "forward_ms": fwd, "backward_ms": bwd, "adjoint_over_forward": bwd / fwd,
+            "kernels": {"step_ms": t_step, "step_vjp_ms": t_vjp, "vjp_over_step": t_vjp / t_step,
+                        "forward_member_cell_steps_per_s": cells / (t_step * 1e-3),
+                        "adjoint_member_cell_steps_per_s": cells / (t_vjp * 1e-3)}}
 
 
 # ---------------------------------------------------------------------------

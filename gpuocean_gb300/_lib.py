@@ -89,6 +89,11 @@ SIGNATURES = {
     "goc_max_dt_noalloc": (c_int, [c_int, c_int, c_float, c_float, c_float, c_void_p, c_void_p, c_void_p, c_int,
                                    c_void_p, c_int, c_float, c_void_p, c_void_p]),
     "goc_cdklm_vjp_partials": (c_int, [c_int, c_int]),
+    "goc_cdklm_rk2_step_members": (c_int, [ctypes.POINTER(GocCdklmParams), c_float] + [c_void_p] * 9 +
+                                   [c_int, ctypes.c_longlong, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_void_p]),
+    "goc_cdklm_stage_vjp_members": (c_int, [ctypes.POINTER(GocCdklmParams), c_float, c_int] + [c_void_p] * 18 +
+                                    [c_int, ctypes.c_longlong, c_int, c_int, c_void_p, c_int, c_void_p, c_int,
+                                     c_void_p, c_void_p]),
     "goc_cdklm_stage_vjp": (c_int, [ctypes.POINTER(GocCdklmParams), c_float, c_int] + [c_void_p] * 18 +
                             [c_int, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
     "goc_drift": (c_int, [c_int, c_int, c_float, c_float, c_float, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int,

@@ -128,8 +128,8 @@ class StepAdjoint:
                   _ptr(pos_bar), 8, ctypes.c_float(1.0), *[_ptr(a) for a in lam], self._stream())
 
     def step_vjp(self, q_n, q_star, lam_next, lam_star, lam_n):
-        """lam_n = (dQ^{n+1}/dQ^n)^T lam_next on interior cells; returns the
-        gradient contribution for the wind stress (x, y) as a device tensor."""
+        """lam_n = (dQ^{n+1}/dQ^n)^T lam_next on interior cells; the wind-stress
+        gradient accumulates on the device (``wind_grad``)."""
         s = self._stream()
         common = (self.pitch, self.Hi.ptr, int(self.Hi.pitch), self.Hm.ptr, int(self.Hm.pitch))
         _lib.call("goc_cdklm_stage_vjp", ctypes.byref(self.params), ctypes.c_float(self.dt), 1,
@@ -140,6 +140,13 @@ class StepAdjoint:
                   *[_ptr(a) for a in q_n], None, None, None, *[_ptr(a) for a in lam_star],
                   *[_ptr(a) for a in lam_n], *[_ptr(a) for a in lam_n], None, None, None,
                   *common, _ptr(self.partials[1]), s)
+        return None
+
+    def reset_wind_grad(self):
+        self.partials.zero_()
+
+    def wind_grad(self):
+        """Wind-stress gradient accumulated by step_vjp since the last reset."""
         return self.wsf * self.partials.view(2, -1, 2).sum(dim=(0, 1))
 
 
@@ -196,7 +203,7 @@ def _rollout_backward(ctx, grad, grad_pos):
     adj, K, n_steps, every = ctx.adj, ctx.K, ctx.n_steps, ctx.obs_every
     grad = grad.contiguous() if grad is not None else None
     lam, lam_n, lam_s = adj.zeros(), adj.zeros(), adj.zeros()
-    wind_bar = torch.zeros(2, dtype=torch.float32, device=adj.device)
+    adj.reset_wind_grad()
     track = ctx.track
     pos_bar = torch.zeros_like(track[0]) if track else None
     for start in sorted(ctx.segments, reverse=True):
@@ -221,13 +228,13 @@ def _rollout_backward(ctx, grad, grad_pos):
             if pos_bar is not None:
                 # the drift after step n read the state after it
                 adj.drift_vjp(states[n + 1 - start], track[n], pos_bar, lam)
-            wind_bar += adj.step_vjp(states[n - start], stars[n - start], lam, lam_s, lam_n)
+            adj.step_vjp(states[n - start], stars[n - start], lam, lam_s, lam_n)
             lam, lam_n = lam_n, lam
         del states, stars
         ctx.segments[start] = None
     ctx.segments = None
     ctx.track = None
-    return lam, wind_bar, pos_bar
+    return lam, adj.wind_grad(), pos_bar
 
 
 class CDKLM16Rollout(torch.autograd.Function):
@@ -270,3 +277,137 @@ class CDKLM16DrifterRollout(torch.autograd.Function):
     def backward(ctx, grad, grad_pos):
         lam, wind_bar, pos_bar = _rollout_backward(ctx, grad, grad_pos)
         return None, None, None, lam[0], lam[1], lam[2], wind_bar, pos_bar
+
+
+class EnsembleStepAdjoint:
+    """The RK2 step and its adjoint for ``n_members`` members that share the
+    configuration of ``sim`` (parameters, bathymetry, Coriolis data) but not
+    their state or their uniform wind stress.  States are stacked tensors
+    (n_members, 3, ny+4, nx+4); one launch covers all members."""
+
+    def __init__(self, sim, n_members, dt=None, memory_fraction=0.5):
+        self.one = StepAdjoint(sim, dt=dt, memory_fraction=memory_fraction)
+        self.n = int(n_members)
+        self.nx, self.ny, self.dt, self.device = self.one.nx, self.one.ny, self.one.dt, self.one.device
+        self.plane = (self.ny + 4) * (self.nx + 4)
+        self.wind = torch.zeros((self.n, 2), dtype=torch.float32, device=self.device)
+        p = _lib.GocCdklmParams.from_buffer_copy(self.one.params)
+        p.wind_x_cur = p.wind_x_next = self.wind.data_ptr()
+        p.wind_y_cur = p.wind_y_next = self.wind.data_ptr() + 4
+        self.params = p
+        per = _lib.load().goc_cdklm_vjp_partials(self.nx, self.ny)
+        self.partials = torch.zeros((2, self.n, per), dtype=torch.float32, device=self.device)
+        self.memory_fraction = float(memory_fraction)
+
+    def zeros(self):
+        return torch.zeros((self.n, 3, self.ny + 4, self.nx + 4), dtype=torch.float32, device=self.device)
+
+    def set_wind(self, tau):
+        """(n_members, 2) or (2,) uniform stress before wind_stress_factor."""
+        tau = torch.as_tensor(tau, dtype=torch.float32, device=self.device)
+        self.wind.copy_(tau.expand(self.n, 2))
+
+    def _p3(self, q):
+        if q is None:
+            return (None, None, None)
+        assert q.is_contiguous() and q.shape == (self.n, 3, self.ny + 4, self.nx + 4)
+        b = q.data_ptr()
+        return tuple(ctypes.c_void_p(b + 4 * c * self.plane) for c in range(3))
+
+    def segment_length(self, n_steps):
+        need = 2 * n_steps * self.n * 3 * 4 * self.plane
+        free, _ = torch.cuda.mem_get_info(self.device)
+        if self.memory_fraction > 0 and need <= self.memory_fraction * free:
+            return n_steps
+        return max(1, int(math.ceil(math.sqrt(n_steps))))
+
+    def step(self, q_in, q_out, q_star=None):
+        o = self.one
+        _lib.call("goc_cdklm_rk2_step_members", ctypes.byref(self.params), ctypes.c_float(self.dt),
+                  *self._p3(q_in), *self._p3(q_out), *self._p3(q_star), o.pitch, 3 * self.plane, self.n, 2,
+                  o.Hi.ptr, int(o.Hi.pitch), o.Hm.ptr, int(o.Hm.pitch), o._stream())
+
+    def step_vjp(self, q_n, q_star, lam_next, lam_star, lam_n):
+        """lam_n = VJP of every member's step; the (n_members, 2) wind-stress
+        gradient accumulates on the device (``wind_grad``)."""
+        o = self.one
+        s = o._stream()
+        common = (o.pitch, 3 * self.plane, self.n, 2, o.Hi.ptr, int(o.Hi.pitch), o.Hm.ptr, int(o.Hm.pitch))
+        _lib.call("goc_cdklm_stage_vjp_members", ctypes.byref(self.params), ctypes.c_float(self.dt), 1,
+                  *self._p3(q_star), *self._p3(q_n), *self._p3(lam_next), None, None, None, *self._p3(lam_star),
+                  *self._p3(lam_n), *common, ctypes.c_void_p(self.partials[0].data_ptr()), s)
+        _lib.call("goc_cdklm_stage_vjp_members", ctypes.byref(self.params), ctypes.c_float(self.dt), 0,
+                  *self._p3(q_n), None, None, None, *self._p3(lam_star), *self._p3(lam_n), *self._p3(lam_n),
+                  None, None, None, *common, ctypes.c_void_p(self.partials[1].data_ptr()), s)
+        return None
+
+    def reset_wind_grad(self):
+        self.partials.zero_()
+
+    def wind_grad(self):
+        return self.one.wsf * self.partials.view(2, self.n, -1, 2).sum(dim=(0, 2))
+
+
+class CDKLM16EnsembleRollout(torch.autograd.Function):
+    """``apply(adj, n_steps, obs_every, q0, wind)`` with an
+    ``EnsembleStepAdjoint``: q0 (n_members, 3, ny+4, nx+4), wind
+    (n_members, 2) -> interior states (n_obs, n_members, 3, ny, nx).  The
+    batched form of ``CDKLM16Rollout`` (same storage and checkpointing)."""
+
+    @staticmethod
+    def forward(ctx, adj, n_steps, obs_every, q0, wind):
+        n_steps, obs_every = int(n_steps), int(obs_every)
+        if n_steps < obs_every or obs_every < 1:
+            raise ValueError("need n_steps >= obs_every >= 1")
+        adj.set_wind(wind.detach())
+        K = adj.segment_length(n_steps)
+        q = q0.detach().to(torch.float32).contiguous().clone()
+        outs = []
+        if K >= n_steps:
+            states, stars = [q], []
+            for n in range(n_steps):
+                nxt, qs = torch.empty_like(q), torch.empty_like(q)
+                adj.step(states[-1], nxt, qs)
+                states.append(nxt)
+                stars.append(qs)
+                if (n + 1) % obs_every == 0:
+                    outs.append(nxt[:, :, 2:-2, 2:-2].clone())
+            ctx.segments = {0: (states, stars)}
+        else:
+            buf = torch.empty_like(q)
+            ctx.segments = {0: (q.clone(), None)}
+            for n in range(n_steps):
+                adj.step(q, buf)
+                q, buf = buf, q
+                if (n + 1) % K == 0 and n + 1 < n_steps:
+                    ctx.segments[n + 1] = (q.clone(), None)
+                if (n + 1) % obs_every == 0:
+                    outs.append(q[:, :, 2:-2, 2:-2].clone())
+        ctx.adj, ctx.K, ctx.n_steps, ctx.obs_every = adj, K, n_steps, obs_every
+        return torch.stack(outs)
+
+    @staticmethod
+    def backward(ctx, grad):
+        adj, K, n_steps, every = ctx.adj, ctx.K, ctx.n_steps, ctx.obs_every
+        grad = grad.contiguous()
+        lam, lam_n, lam_s = adj.zeros(), adj.zeros(), adj.zeros()
+        adj.reset_wind_grad()
+        for start in sorted(ctx.segments, reverse=True):
+            end = min(start + K, n_steps)
+            states, stars = ctx.segments[start]
+            if stars is None:
+                states, stars = [states], []
+                for _ in range(start, end):
+                    nxt, qs = torch.empty_like(states[-1]), torch.empty_like(states[-1])
+                    adj.step(states[-1], nxt, qs)
+                    states.append(nxt)
+                    stars.append(qs)
+            for n in range(end - 1, start - 1, -1):
+                if (n + 1) % every == 0:
+                    lam[:, :, 2:-2, 2:-2] += grad[(n + 1) // every - 1]
+                adj.step_vjp(states[n - start], stars[n - start], lam, lam_s, lam_n)
+                lam, lam_n = lam_n, lam
+            del states, stars
+            ctx.segments[start] = None
+        ctx.segments = None
+        return None, None, None, lam, adj.wind_grad()

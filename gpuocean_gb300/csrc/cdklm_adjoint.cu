@@ -329,9 +329,10 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
         if (threadIdx.x == 0) {
             float sx = 0.f, sy = 0.f;
             for (int w = 0; w < NT / 32; ++w) { sx += red[0][w]; sy += red[1][w]; }
+            // each tile owns its two slots: accumulate across calls
             const int t = tile_y * gridDim.x + tile_x;
-            wind_partials[2 * t] = sx;
-            wind_partials[2 * t + 1] = sy;
+            wind_partials[2 * t] += sx;
+            wind_partials[2 * t + 1] += sy;
         }
     }
 }
@@ -355,6 +356,42 @@ stage_vjp_kernel(const GocCdklmParams p, const StepConst k, float dt, int rk_ste
         stage_vjp_body<kAX, kAY, kANT, CONST_F, false>(p, k, dt, rk_step, tx, ty, xe, xu, xv, ae, au, av, ybe, ybu,
                                                        ybv, bbe, bbu, bbv, xbe, xbu, xbv, abe, abu, abv, pitch, Hi_g,
                                                        hi_pitch, Hm_g, hm_pitch, wind_partials, smem_raw);
+}
+
+// Members sharing parameters and bathymetry: member blockIdx.z works at
+// offset z * member_stride (states and adjoints), z * wind_stride (wind) and
+// z * partials_stride (wind partials).
+template <bool CONST_F>
+__global__ void __launch_bounds__(kANT, 2)
+stage_vjp_members_kernel(const GocCdklmParams p, const StepConst k, float dt, int rk_step, const float* xe,
+                         const float* xu, const float* xv, const float* ae, const float* au, const float* av,
+                         const float* ybe, const float* ybu, const float* ybv, const float* bbe, const float* bbu,
+                         const float* bbv, float* xbe, float* xbu, float* xbv, float* abe, float* abu, float* abv,
+                         int pitch, long long member_stride, int wind_stride, const float* Hi_g, int hi_pitch,
+                         const float* Hm_g, int hm_pitch, float* wind_partials, int partials_stride) {
+    extern __shared__ __align__(16) float smem_raw[];
+    const size_t o = (size_t)blockIdx.z * (size_t)member_stride;
+    GocCdklmParams pm = p;
+    if (wind_stride) {
+        const size_t wo = (size_t)blockIdx.z * wind_stride;
+        pm.wind_x_cur += wo; pm.wind_x_next += wo; pm.wind_y_cur += wo; pm.wind_y_next += wo;
+    }
+    auto sh = [&](const float* q) { return q ? q + o : q; };
+    auto shw = [&](float* q) { return q ? q + o : q; };
+    float* wp = wind_partials ? wind_partials + (size_t)blockIdx.z * partials_stride : nullptr;
+    const int tx = blockIdx.x, ty = blockIdx.y;
+    const int x0 = 2 + tx * kAX - kAHalo, y0 = 2 + ty * kAY - kAHalo;
+    const bool border = x0 < 2 || y0 < 2 || x0 + kAX + 2 * kAHalo > p.nx + 2 || y0 + kAY + 2 * kAHalo > p.ny + 2;
+    if (border)
+        stage_vjp_body<kAX, kAY, kANT, CONST_F, true>(pm, k, dt, rk_step, tx, ty, sh(xe), sh(xu), sh(xv), sh(ae),
+                                                      sh(au), sh(av), sh(ybe), sh(ybu), sh(ybv), sh(bbe), sh(bbu),
+                                                      sh(bbv), shw(xbe), shw(xbu), shw(xbv), shw(abe), shw(abu),
+                                                      shw(abv), pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, wp, smem_raw);
+    else
+        stage_vjp_body<kAX, kAY, kANT, CONST_F, false>(pm, k, dt, rk_step, tx, ty, sh(xe), sh(xu), sh(xv), sh(ae),
+                                                       sh(au), sh(av), sh(ybe), sh(ybu), sh(ybv), sh(bbe), sh(bbu),
+                                                       sh(bbv), shw(xbe), shw(xbu), shw(xbv), shw(abe), shw(abu),
+                                                       shw(abv), pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, wp, smem_raw);
 }
 
 static int vjp_check(const GocCdklmParams* p, int pitch, int Hi_pitch, int Hm_pitch, const char* who) {
@@ -437,4 +474,58 @@ extern "C" int goc_cdklm_stage_vjp(const GocCdklmParams* p, float dt, int rk_ste
     return launch_vjp<false>(p, k, dt, rk_step, x_eta, x_hu, x_hv, a_eta, a_hu, a_hv, yb_eta, yb_hu, yb_hv,
                              base_eta, base_hu, base_hv, xb_eta, xb_hu, xb_hv, ab_eta, ab_hu, ab_hv, pf, Hi, hip, Hm,
                              hmp, wind_partials, st);
+}
+
+extern "C" int goc_cdklm_stage_vjp_members(const GocCdklmParams* p, float dt, int rk_step, const float* x_eta,
+                                           const float* x_hu, const float* x_hv, const float* a_eta,
+                                           const float* a_hu, const float* a_hv, const float* yb_eta,
+                                           const float* yb_hu, const float* yb_hv, const float* base_eta,
+                                           const float* base_hu, const float* base_hv, float* xb_eta, float* xb_hu,
+                                           float* xb_hv, float* ab_eta, float* ab_hu, float* ab_hv, int pitch,
+                                           long long member_stride, int n_members, int wind_stride,
+                                           const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch,
+                                           float* wind_partials, void* stream) {
+    int rc = vjp_check(p, pitch, Hi_pitch, Hm_pitch, "goc_cdklm_stage_vjp_members");
+    if (rc) return rc;
+    if (rk_step != 0 && rk_step != 1)
+        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp_members: rk_step must be 0 or 1");
+    if (!x_eta || !x_hu || !x_hv || !yb_eta || !yb_hu || !yb_hv || !xb_eta || !xb_hu || !xb_hv || !Hi || !Hm)
+        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp_members: null buffer");
+    if (rk_step == 1 && (!a_eta || !a_hu || !a_hv || !ab_eta || !ab_hu || !ab_hv))
+        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp_members: the second stage needs Q^n and its adjoint");
+    if ((base_eta || base_hu || base_hv) && !(base_eta && base_hu && base_hv))
+        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp_members: base must be all three arrays or none");
+    if (xb_eta == yb_eta || xb_eta == x_eta)
+        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp_members: x-bar must not alias x or y-bar");
+    if (n_members < 1 || n_members > 65535 || member_stride < (long long)(p->ny + 4) * (pitch / 4) || wind_stride < 0)
+        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp_members: bad member count or stride");
+    const StepConst k = make_step_const(*p);
+    const bool cf = (p->coriolis_nx == 1 && p->coriolis_ny == 1);
+    cudaStream_t st = as_stream(stream);
+    constexpr int W = kAX + 2 * kAHalo, H = kAY + 2 * kAHalo;
+    constexpr size_t smem = sizeof(AdjSmem<W, H>);
+    const int partials = goc_cdklm_vjp_partials(p->nx, p->ny);
+    dim3 grid((p->nx + kAX - 1) / kAX, (p->ny + kAY - 1) / kAY, n_members);
+    static bool configured[2] = {false, false};
+    if (!configured[cf]) {
+        cudaError_t e = cf ? cudaFuncSetAttribute(stage_vjp_members_kernel<true>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                           : cudaFuncSetAttribute(stage_vjp_members_kernel<false>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return set_error(GOC_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+        configured[cf] = true;
+    }
+    const int pf = pitch / 4, hip = Hi_pitch / 4, hmp = Hm_pitch / 4;
+    if (cf)
+        stage_vjp_members_kernel<true><<<grid, kANT, smem, st>>>(
+            *p, k, dt, rk_step, x_eta, x_hu, x_hv, a_eta, a_hu, a_hv, yb_eta, yb_hu, yb_hv, base_eta, base_hu,
+            base_hv, xb_eta, xb_hu, xb_hv, ab_eta, ab_hu, ab_hv, pf, member_stride, wind_stride, Hi, hip, Hm, hmp,
+            wind_partials, partials);
+    else
+        stage_vjp_members_kernel<false><<<grid, kANT, smem, st>>>(
+            *p, k, dt, rk_step, x_eta, x_hu, x_hv, a_eta, a_hu, a_hv, yb_eta, yb_hu, yb_hv, base_eta, base_hu,
+            base_hv, xb_eta, xb_hu, xb_hv, ab_eta, ab_hu, ab_hv, pf, member_stride, wind_stride, Hi, hip, Hm, hmp,
+            wind_partials, partials);
+    count_launch();
+    return check_launch("stage_vjp_members_kernel");
 }

@@ -18,6 +18,51 @@ static int make_const(const GocCdklmParams* p, StepConst* k, bool* const_f, bool
     return GOC_OK;
 }
 
+// Members that share parameters and bathymetry but not their state: member
+// z of the launch (blockIdx.z) reads and writes its buffers at offset
+// z * member_stride floats, and its uniform wind stress at z * wind_stride.
+template <int TX, int TY, int NT, bool CONST_F, bool SIMPLE_FORCING>
+__global__ void __launch_bounds__(NT, 3)
+cdklm_members_kernel(const GocCdklmParams p, const StepConst k, float dt, const float* __restrict__ e_in,
+                     const float* __restrict__ hu_in, const float* __restrict__ hv_in, float* e_out, float* hu_out,
+                     float* hv_out, float* e_st, float* hu_st, float* hv_st, int pitch, long long member_stride,
+                     int wind_stride, const float* __restrict__ Hi_g, int hi_pitch, const float* __restrict__ Hm_g,
+                     int hm_pitch) {
+    extern __shared__ __align__(16) float smem_raw[];
+    const size_t off = (size_t)blockIdx.z * (size_t)member_stride;
+    GocCdklmParams pm = p;
+    if (wind_stride) {
+        const size_t wo = (size_t)blockIdx.z * wind_stride;
+        pm.wind_x_cur += wo; pm.wind_x_next += wo; pm.wind_y_cur += wo; pm.wind_y_next += wo;
+    }
+    cdklm_tile<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING>(pm, k, dt, 1, blockIdx.x, blockIdx.y, e_in + off, hu_in + off,
+                                                       hv_in + off, e_out + off, hu_out + off, hv_out + off,
+                                                       e_st ? e_st + off : nullptr, e_st ? hu_st + off : nullptr,
+                                                       e_st ? hv_st + off : nullptr, pitch, Hi_g, hi_pitch, Hm_g,
+                                                       hm_pitch, smem_raw);
+}
+
+template <bool CF, bool SF>
+static int launch_members(const GocCdklmParams* p, const StepConst& k, float dt, const float* e0, const float* hu0,
+                          const float* hv0, float* e1, float* hu1, float* hv1, float* es, float* hus, float* hvs,
+                          int pitch_f, long long stride, int n, int wind_stride, const float* Hi, int hip,
+                          const float* Hm, int hmp, cudaStream_t st) {
+    constexpr int W = kTX + 8, H = kTY + 8;
+    constexpr size_t smem = sizeof(TileSmem<W, H>);
+    auto kern = cdklm_members_kernel<kTX, kTY, kNT, CF, SF>;
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return set_error(GOC_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+        configured = true;
+    }
+    dim3 grid((p->nx + kTX - 1) / kTX, (p->ny + kTY - 1) / kTY, n);
+    kern<<<grid, kNT, smem, st>>>(*p, k, dt, e0, hu0, hv0, e1, hu1, hv1, es, hus, hvs, pitch_f, stride, wind_stride,
+                                  Hi, hip, Hm, hmp);
+    count_launch();
+    return check_launch("cdklm_members_kernel");
+}
+
 template <int NSTAGE, bool CF, bool SF>
 static int launch_tile(const GocCdklmParams* p, const StepConst& k, float dt, int rk_step,
                        const float* e0, const float* hu0, const float* hv0, float* e1, float* hu1, float* hv1,
@@ -106,6 +151,33 @@ extern "C" int goc_cdklm_rk2_step_stage(const GocCdklmParams* p, float dt, const
     if ((rc = make_const(p, &k, &cf, &sf))) return rc;
     return dispatch<2>(p, k, cf, sf, dt, 1, eta0, hu0, hv0, eta1, hu1, hv1, eta_s, hu_s, hv_s, pitch / 4, Hi,
                        Hi_pitch / 4, Hm, Hm_pitch / 4, st);
+}
+
+extern "C" int goc_cdklm_rk2_step_members(const GocCdklmParams* p, float dt, const float* eta0, const float* hu0,
+                                          const float* hv0, float* eta1, float* hu1, float* hv1, float* eta_s,
+                                          float* hu_s, float* hv_s, int pitch, long long member_stride,
+                                          int n_members, int wind_stride, const float* Hi, int Hi_pitch,
+                                          const float* Hm, int Hm_pitch, void* stream) {
+    int rc = validate_params(p, "goc_cdklm_rk2_step_members");
+    if (rc) return rc;
+    if ((rc = check_pitch(p, pitch, Hi_pitch, Hm_pitch, "goc_cdklm_rk2_step_members"))) return rc;
+    if (!eta0 || !hu0 || !hv0 || !eta1 || !hu1 || !hv1 || !Hi || !Hm)
+        return set_error(GOC_ERR_ARG, "goc_cdklm_rk2_step_members: null buffer");
+    if ((eta_s || hu_s || hv_s) && !(eta_s && hu_s && hv_s))
+        return set_error(GOC_ERR_ARG, "goc_cdklm_rk2_step_members: the first-stage set must be all or none");
+    if (n_members < 1 || n_members > 65535 || member_stride < (long long)(p->ny + 4) * (pitch / 4) || wind_stride < 0)
+        return set_error(GOC_ERR_ARG, "goc_cdklm_rk2_step_members: bad member count or stride");
+    if (p->rk_order != 2) return set_error(GOC_ERR_ARG, "goc_cdklm_rk2_step_members: params.rk_order must be 2");
+    StepConst k;
+    bool cf, sf;
+    cudaStream_t st = as_stream(stream);
+    if ((rc = make_const(p, &k, &cf, &sf))) return rc;
+    if (!sf) return set_error(GOC_ERR_UNSUPPORTED, "goc_cdklm_rk2_step_members: needs uniform forcing textures");
+    if (cf)
+        return launch_members<true, true>(p, k, dt, eta0, hu0, hv0, eta1, hu1, hv1, eta_s, hu_s, hv_s, pitch / 4,
+                                          member_stride, n_members, wind_stride, Hi, Hi_pitch / 4, Hm, Hm_pitch / 4, st);
+    return launch_members<false, true>(p, k, dt, eta0, hu0, hv0, eta1, hu1, hv1, eta_s, hu_s, hv_s, pitch / 4,
+                                       member_stride, n_members, wind_stride, Hi, Hi_pitch / 4, Hm, Hm_pitch / 4, st);
 }
 
 extern "C" int goc_cdklm_stage(const GocCdklmParams* p, float dt, int rk_step, const float* eta_in,

@@ -227,8 +227,9 @@ int goc_max_dt_noalloc(int nx, int ny, float dx, float dy, float g,
  * the call writes, on interior cells,
  *   xb = base + (dS/dx)^T yb      (base may be NULL)
  *   ab = (dS2/da)^T yb             (rk_step 1 only)
- * and, if wind_partials is not NULL, goc_cdklm_vjp_partials(nx, ny) floats
- * of per-tile partial sums (x, y interleaved) of (dS/dX_eff)^T yb, where
+ * and, if wind_partials is not NULL, ADDS to its goc_cdklm_vjp_partials(nx, ny)
+ * floats the per-tile partial sums (x, y interleaved) of (dS/dX_eff)^T yb
+ * (the caller zeroes them; calls on one stream may share them), where
  * X_eff = wind_stress_factor * stress is the uniform wind stress the step
  * adds.  Ghost cells of the adjoint arrays are neither read nor written:
  * ghost cells of the state are periodic images or wall mirrors of interior
@@ -241,6 +242,35 @@ int goc_max_dt_noalloc(int nx, int ny, float dx, float dy, float g,
  * base = xb = lambda^n); Q* comes from goc_cdklm_stage with rk_step 0.
  */
 int goc_cdklm_vjp_partials(int nx, int ny);
+
+/*
+ * Member-batched forms for ensembles that share parameters and bathymetry
+ * but not their state (no counterpart in the reference): member z of one
+ * launch works on the buffers at offset z * member_stride floats from the
+ * given pointers, and reads its uniform wind stress at offset
+ * z * wind_stride floats from the parameters' wind pointers (0 = shared).
+ * goc_cdklm_rk2_step_members is goc_cdklm_rk2_step_stage for n_members
+ * members (eta_s, hu_s, hv_s may be NULL); goc_cdklm_stage_vjp_members is
+ * goc_cdklm_stage_vjp for n_members members, member z writing its
+ * goc_cdklm_vjp_partials(nx, ny) wind partials at z times that count.
+ */
+int goc_cdklm_rk2_step_members(const GocCdklmParams* p, float dt,
+                               const float* eta0, const float* hu0, const float* hv0,
+                               float* eta1, float* hu1, float* hv1,
+                               float* eta_s, float* hu_s, float* hv_s, int pitch,
+                               long long member_stride, int n_members, int wind_stride,
+                               const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch,
+                               void* stream);
+int goc_cdklm_stage_vjp_members(const GocCdklmParams* p, float dt, int rk_step,
+                                const float* x_eta, const float* x_hu, const float* x_hv,
+                                const float* a_eta, const float* a_hu, const float* a_hv,
+                                const float* yb_eta, const float* yb_hu, const float* yb_hv,
+                                const float* base_eta, const float* base_hu, const float* base_hv,
+                                float* xb_eta, float* xb_hu, float* xb_hv,
+                                float* ab_eta, float* ab_hu, float* ab_hv, int pitch,
+                                long long member_stride, int n_members, int wind_stride,
+                                const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch,
+                                float* wind_partials, void* stream);
 int goc_cdklm_stage_vjp(const GocCdklmParams* p, float dt, int rk_step,
                         const float* x_eta, const float* x_hu, const float* x_hv,
                         const float* a_eta, const float* a_hu, const float* a_hv,

@@ -96,7 +96,9 @@ def test_step_vjp_matches_fp64_autograd(ctx, name):
         a[2:-2, 2:-2] = torch.as_tensor(b, dtype=torch.float32)
     q_s, lam_s, lam_n = adj.zeros(), adj.zeros(), adj.zeros()
     adj.stage1(q, q_s)
-    wind_bar = adj.step_vjp(q, q_s, lam_next, lam_s, lam_n).cpu().numpy()
+    adj.reset_wind_grad()
+    adj.step_vjp(q, q_s, lam_next, lam_s, lam_n)
+    wind_bar = adj.wind_grad().cpu().numpy()
     torch.cuda.synchronize()
     ours = [a.cpu().numpy().astype(np.float64)[2:-2, 2:-2] for a in lam_n]
 
@@ -614,4 +616,39 @@ def test_drifter_rollout_matches_fp64_chain_and_fd(ctx):
                       "wind_rel": werr, "fd": [ad, fd, fd_err]}))
     assert max(errs) <= 1e-4 and perr <= 1e-4 and werr <= 1e-4, (errs, perr, werr)
     assert fd_err <= 1e-4, (ad, fd, fd_err)
+    sim.cleanUp()
+
+
+def test_member_batched_rollout_equals_single_rollouts(ctx):
+    """Config-5 style batching: members sharing the configuration run in one
+    launch per step (forward) and two per step VJP; each member's gradient is
+    bit-identical to its own single rollout, the wind gradients agree to
+    1e-6 (a different summation order of the per-tile partials)."""
+    from gpuocean_gb300.adjoint import (CDKLM16EnsembleRollout, CDKLM16Rollout, EnsembleStepAdjoint,
+                                        StepAdjoint)
+    c = _case("walls_f")
+    sim = _sim(ctx, c, 2.0)
+    n_members, n_steps, every = 4, 30, 5
+    rng = np.random.default_rng(17)
+    base = np.stack([np.asarray(a, dtype=np.float32) for a in sim.download()])
+    q0 = np.stack([base + np.stack([_smooth(rng, base[0].shape, s) for s in (0.05, 1.0, 1.0)])
+                   for _ in range(n_members)]).astype(np.float32)
+    winds = rng.normal(0.0, 1.0e-4, (n_members, 2)).astype(np.float32)
+    for frac in (0.5, 0.0):
+        eadj = EnsembleStepAdjoint(sim, n_members, memory_fraction=frac)
+        q = torch.as_tensor(q0, device=eadj.device).requires_grad_(True)
+        w = torch.as_tensor(winds, device=eadj.device).requires_grad_(True)
+        st = CDKLM16EnsembleRollout.apply(eadj, n_steps, every, q, w)
+        (st[:, :, 1] ** 2 + 0.1 * st[:, :, 0]).sum().backward()
+        gq, gw = q.grad.cpu().numpy(), w.grad.cpu().numpy()
+        adj = StepAdjoint(sim, memory_fraction=frac)
+        for m in range(n_members):
+            x = [torch.as_tensor(q0[m, k], device=adj.device).requires_grad_(True) for k in range(3)]
+            wm = torch.as_tensor(winds[m], device=adj.device).requires_grad_(True)
+            sm = CDKLM16Rollout.apply(adj, n_steps, every, *x, wm)
+            assert torch.equal(sm, st[:, m])
+            (sm[:, 1] ** 2 + 0.1 * sm[:, 0]).sum().backward()
+            for k in range(3):
+                assert np.array_equal(x[k].grad.cpu().numpy()[2:-2, 2:-2], gq[m, k, 2:-2, 2:-2])
+            np.testing.assert_allclose(wm.grad.cpu().numpy(), gw[m], rtol=1e-6)
     sim.cleanUp()
