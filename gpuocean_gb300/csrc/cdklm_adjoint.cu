@@ -22,9 +22,10 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
                                const float* __restrict__ Hi_g, int hi_pitch, const float* __restrict__ Hm_g,
                                int hm_pitch, float* wind_partials, float* smem_raw) {
     constexpr int W = TX + 2 * kAHalo, H = TY + 2 * kAHalo;
-    AdjSmem<W, H>& A = *reinterpret_cast<AdjSmem<W, H>*>(smem_raw);
-    TileSmem<W, H>& S = A.T;
-    Tile<W, H, NT, BORDER> T{S, p, k, 2 + tile_x * TX - kAHalo, 2 + tile_y * TY - kAHalo, 0.f, 1.f, 0.f, 0.f, 0.f};
+    using SM = AdjSmem<W, H, !CONST_F>;
+    SM& A = *reinterpret_cast<SM*>(smem_raw);
+    SM& S = A;
+    Tile<W, H, NT, BORDER, SM> T{S, p, k, 2 + tile_x * TX - kAHalo, 2 + tile_y * TY - kAHalo, 0.f, 1.f, 0.f, 0.f, 0.f};
     {
         const float a = __ldg(p.angle);
         T.nX = sinf(a);
@@ -34,7 +35,7 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
         T.wind_X = p.wind_stress_factor * (wt * __ldg(p.wind_x_next) + (1.0f - wt) * __ldg(p.wind_x_cur));
         T.wind_Y = p.wind_stress_factor * (wt * __ldg(p.wind_y_next) + (1.0f - wt) * __ldg(p.wind_y_cur));
     }
-    AdjTile<W, H, NT, BORDER> R{A, T, p, k};
+    AdjTile<W, H, NT, BORDER, !CONST_F> R{A, T, p, k};
     const int nx = p.nx, ny = p.ny;
     const bool px = k.periodic_x, py = k.periodic_y;
 
@@ -84,7 +85,6 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
         const float hu = su * __ldg(xu + o);
         const float hv = sv * __ldg(xv + o);
         const float hmb = __ldg(Hm_g + (size_t)hy * hm_pitch + hx);
-        S.Hmb[j][i] = hmb;
         float oe, ou, ov;
         desingularize_cell(p, e, hu, hv, hmb, oe, ou, ov);
         S.D[0][j][i] = oe; S.D[1][j][i] = ou; S.D[2][j][i] = ov;
@@ -99,7 +99,7 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
             }
         }
 #pragma unroll
-        for (int c = 0; c < 3; ++c) { A.Db[c][j][i] = 0.0f; A.FDb[c][j][i] = 0.0f; }
+        for (int c = 0; c < 3; ++c) A.Db[c][j][i] = 0.0f;
     }
     __syncthreads();
 
@@ -109,9 +109,19 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
     T.template faces<2, W - 2, 2, H - 2, CONST_F>();
     __syncthreads();
 
-    // 4. cell pass: RK combination, friction and source terms in reverse
+    // 4. cell pass: RK combination, friction and source terms in reverse.
+    //    The flux-divergence adjoints stay in registers until every cell has
+    //    read the fluxes, then replace them in the Gy planes.
     float wXb = 0.0f, wYb = 0.0f;
-    for (int idx = threadIdx.x; idx < (W - 4) * (H - 4); idx += NT) {
+    constexpr int NCELL = (W - 4) * (H - 4);
+    constexpr int PER = (NCELL + NT - 1) / NT;
+    float fdb[PER][3];
+#pragma unroll
+    for (int r = 0; r < PER; ++r) { fdb[r][0] = 0.f; fdb[r][1] = 0.f; fdb[r][2] = 0.f; }
+#pragma unroll
+    for (int r = 0; r < PER; ++r) {
+        const int idx = threadIdx.x + r * NT;
+        if (idx >= NCELL) continue;
         const int i = 2 + idx % (W - 4), j = 2 + idx / (W - 4);
         const int gx = T.x0 + i, gy = T.y0 + j;
         const int gxs = (BORDER && px) ? wrap_interior(gx, nx) : gx;
@@ -169,9 +179,9 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
         }
         float hsb = 0.0f;
         friction_vjp(p, dt, hsum, hu, hv, Cb, hsb, hub, hvb);
-        A.FDb[0][j][i] = -L1b;
-        A.FDb[1][j][i] = -L2b;
-        A.FDb[2][j][i] = -L3b;
+        fdb[r][0] = -L1b;
+        fdb[r][1] = -L2b;
+        fdb[r][2] = -L3b;
         const float uc = S.D[1][j][i], vc = S.D[2][j][i];
         if (hsum >= p.depth_cutoff && ec != kDryFlag) {
             const float st1b = L2b, st2b = L3b;
@@ -205,49 +215,45 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
         }
     }
     __syncthreads();
-    // slope-bar accumulators replace the fluxes
+    // the fluxes are dead: Gy takes the flux-divergence adjoints (zero outside
+    // the cells of the pass), Fx the slope adjoints
     for (int idx = threadIdx.x; idx < H * W; idx += NT) {
         const int i = idx % W, j = idx / W;
 #pragma unroll
         for (int c = 0; c < 3; ++c) { S.Fx[c][j][i] = 0.0f; S.Gy[c][j][i] = 0.0f; }
     }
     __syncthreads();
+#pragma unroll
+    for (int r = 0; r < PER; ++r) {
+        const int idx = threadIdx.x + r * NT;
+        if (idx >= NCELL) continue;
+        const int i = 2 + idx % (W - 4), j = 2 + idx / (W - 4);
+        S.Gy[0][j][i] = fdb[r][0]; S.Gy[1][j][i] = fdb[r][1]; S.Gy[2][j][i] = fdb[r][2];
+    }
+    __syncthreads();
+    auto FDb = [&](int c) -> float (&)[H][W] { return S.Gy[c]; };
 
-    // 5. faces in reverse, two colours each
+    // 5. faces in reverse, two colours each.  x faces are coloured as a
+    //    checkerboard ((i + j) even / odd): faces of one row never share a
+    //    cell, and a warp that spans two rows touches even banks in one and
+    //    odd banks in the other, so the stride-2 accesses do not conflict.
     constexpr int NXF = W - 3, NYF = H - 4;     // east faces of cells [1, W-2) on rows [2, H-2)
 #pragma unroll 1
     for (int colour = 0; colour < 2; ++colour) {
         for (int idx = threadIdx.x; idx < ((NXF + 1) / 2) * NYF; idx += NT) {
-            const int i = 1 + colour + 2 * (idx % ((NXF + 1) / 2));
             const int j = 2 + idx / ((NXF + 1) / 2);
+            const int i = 1 + 2 * (idx % ((NXF + 1) / 2)) + ((j + colour) & 1);
             if (i >= W - 2) continue;
-            const float F0b = (A.FDb[0][j][i] - A.FDb[0][j][i + 1]) * k.inv_dx;
-            const float F1b = (A.FDb[1][j][i] - A.FDb[1][j][i + 1]) * k.inv_dx;
-            const float F2b = (A.FDb[2][j][i] - A.FDb[2][j][i + 1]) * k.inv_dx;
+            const float F0b = (FDb(0)[j][i] - FDb(0)[j][i + 1]) * k.inv_dx;
+            const float F1b = (FDb(1)[j][i] - FDb(1)[j][i + 1]) * k.inv_dx;
+            const float F2b = (FDb(2)[j][i] - FDb(2)[j][i + 1]) * k.inv_dx;
             if (F0b == 0.0f && F1b == 0.0f && F2b == 0.0f) continue;
             R.template face_x_vjp<CONST_F>(i, j, F0b, F1b, F2b);
         }
         __syncthreads();
     }
-    if (!p.one_dimensional) {
-        constexpr int NXG = W - 4, NYG = H - 3;   // north faces of cells [2, W-2) on rows [1, H-2)
-#pragma unroll 1
-        for (int colour = 0; colour < 2; ++colour) {
-            for (int idx = threadIdx.x; idx < NXG * ((NYG + 1) / 2); idx += NT) {
-                const int i = 2 + idx % NXG;
-                const int j = 1 + colour + 2 * (idx / NXG);
-                if (j >= H - 2) continue;
-                const float G0b = (A.FDb[0][j][i] - A.FDb[0][j + 1][i]) * k.inv_dy;
-                const float G1b = (A.FDb[1][j][i] - A.FDb[1][j + 1][i]) * k.inv_dy;
-                const float G2b = (A.FDb[2][j][i] - A.FDb[2][j + 1][i]) * k.inv_dy;
-                if (G0b == 0.0f && G1b == 0.0f && G2b == 0.0f) continue;
-                R.template face_y_vjp<CONST_F>(i, j, G0b, G1b, G2b);
-            }
-            __syncthreads();
-        }
-    }
-
-    // 6. slopes in reverse, three colours each
+    // 6. x slopes in reverse (three colours); their adjoints are complete
+    //    once the x faces are done
     constexpr int NXS = W - 2, NYS = H - 4;     // x slopes of cells [1, W-1) on rows [2, H-2)
 #pragma unroll 1
     for (int colour = 0; colour < 3; ++colour) {
@@ -260,6 +266,32 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
         }
         __syncthreads();
     }
+    // Fx is cleared again for the y-slope adjoints
+    for (int idx = threadIdx.x; idx < H * W; idx += NT) {
+        const int i = idx % W, j = idx / W;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) S.Fx[c][j][i] = 0.0f;
+    }
+    __syncthreads();
+    // 7. y faces and y slopes in reverse
+    if (!p.one_dimensional) {
+        constexpr int NXG = W - 4, NYG = H - 3;   // north faces of cells [2, W-2) on rows [1, H-2)
+#pragma unroll 1
+        for (int colour = 0; colour < 2; ++colour) {
+            for (int idx = threadIdx.x; idx < NXG * ((NYG + 1) / 2); idx += NT) {
+                const int i = 2 + idx % NXG;
+                const int j = 1 + colour + 2 * (idx / NXG);
+                if (j >= H - 2) continue;
+                const float G0b = (FDb(0)[j][i] - FDb(0)[j + 1][i]) * k.inv_dy;
+                const float G1b = (FDb(1)[j][i] - FDb(1)[j + 1][i]) * k.inv_dy;
+                const float G2b = (FDb(2)[j][i] - FDb(2)[j + 1][i]) * k.inv_dy;
+                if (G0b == 0.0f && G1b == 0.0f && G2b == 0.0f) continue;
+                R.template face_y_vjp<CONST_F>(i, j, G0b, G1b, G2b);
+            }
+            __syncthreads();
+        }
+    }
+
     constexpr int NXY = W - 4, NYY = H - 2;     // y slopes of cells [2, W-2) on rows [1, H-1)
 #pragma unroll 1
     for (int colour = 0; colour < 3; ++colour) {
@@ -273,8 +305,9 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
         __syncthreads();
     }
 
-    // 7. desingularisation in reverse at every staged position, as the
-    //    adjoint of the memory cell it read (signs of the wall mirrors)
+    // 8. desingularisation in reverse at every staged position, as the
+    //    adjoint of the memory cell it read (signs of the wall mirrors); the
+    //    result per position goes to the Gy planes
     for (int idx = threadIdx.x; idx < H * W; idx += NT) {
         const int i = idx % W, j = idx / W;
         const float d0 = A.Db[0][j][i], d1 = A.Db[1][j][i], d2 = A.Db[2][j][i];
@@ -287,37 +320,38 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
             const float e = __ldg(xe + o);
             const float hu = su * __ldg(xu + o);
             const float hv = sv * __ldg(xv + o);
-            desingularize_cell_vjp(p, e, hu, hv, S.Hmb[j][i], d0, d1, d2, eb, hub, hvb);
+            const float hmb = __ldg(Hm_g + (size_t)hy * hm_pitch + hx);
+            desingularize_cell_vjp(p, e, hu, hv, hmb, d0, d1, d2, eb, hub, hvb);
             hub *= su;
             hvb *= sv;
         }
-        A.FDb[0][j][i] = eb; A.FDb[1][j][i] = hub; A.FDb[2][j][i] = hvb;
+        S.Gy[0][j][i] = eb; S.Gy[1][j][i] = hub; S.Gy[2][j][i] = hvb;
     }
     __syncthreads();
 
-    // 8. x-bar of the tile's interior cells: own position plus the wall
+    // 9. x-bar of the tile's interior cells: own position plus the wall
     //    mirror positions that read it
     for (int idx = threadIdx.x; idx < TX * TY; idx += NT) {
         const int i = kAHalo + idx % TX, j = kAHalo + idx / TX;
         const int gx = T.x0 + i, gy = T.y0 + j;
         if (gx >= nx + 2 || gy >= ny + 2) continue;
-        float s0 = A.FDb[0][j][i], s1 = A.FDb[1][j][i], s2 = A.FDb[2][j][i];
+        float s0 = S.Gy[0][j][i], s1 = S.Gy[1][j][i], s2 = S.Gy[2][j][i];
         if (BORDER) {
             int mi = -1;
             if (p.bc_west == 1 && (gx == 2 || gx == 3)) mi = i - (2 * gx - 3);
             if (p.bc_east == 1 && (gx == nx || gx == nx + 1)) mi = i + (2 * nx + 3 - 2 * gx);
-            if (mi >= 0 && mi < W) { s0 += A.FDb[0][j][mi]; s1 += A.FDb[1][j][mi]; s2 += A.FDb[2][j][mi]; }
+            if (mi >= 0 && mi < W) { s0 += S.Gy[0][j][mi]; s1 += S.Gy[1][j][mi]; s2 += S.Gy[2][j][mi]; }
             int mj = -1;
             if (p.bc_south == 1 && (gy == 2 || gy == 3)) mj = j - (2 * gy - 3);
             if (p.bc_north == 1 && (gy == ny || gy == ny + 1)) mj = j + (2 * ny + 3 - 2 * gy);
-            if (mj >= 0 && mj < H) { s0 += A.FDb[0][mj][i]; s1 += A.FDb[1][mj][i]; s2 += A.FDb[2][mj][i]; }
+            if (mj >= 0 && mj < H) { s0 += S.Gy[0][mj][i]; s1 += S.Gy[1][mj][i]; s2 += S.Gy[2][mj][i]; }
         }
         const size_t o = (size_t)gy * pitch + gx;
         if (bbe) { s0 += __ldg(bbe + o); s1 += __ldg(bbu + o); s2 += __ldg(bbv + o); }
         xbe[o] = s0; xbu[o] = s1; xbv[o] = s2;
     }
 
-    // 9. wind-stress adjoint of the tile's cells
+    // 10. wind-stress adjoint of the tile's cells
     if (wind_partials) {
         __shared__ float red[2][NT / 32];
         for (int off = 16; off > 0; off >>= 1) {
@@ -338,7 +372,7 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
 }
 
 template <bool CONST_F>
-__global__ void __launch_bounds__(kANT, 2)
+__global__ void __launch_bounds__(kANT, CONST_F ? 3 : 2)
 stage_vjp_kernel(const GocCdklmParams p, const StepConst k, float dt, int rk_step, const float* xe, const float* xu,
                  const float* xv, const float* ae, const float* au, const float* av, const float* ybe,
                  const float* ybu, const float* ybv, const float* bbe, const float* bbu, const float* bbv,
@@ -362,7 +396,7 @@ stage_vjp_kernel(const GocCdklmParams p, const StepConst k, float dt, int rk_ste
 // offset z * member_stride (states and adjoints), z * wind_stride (wind) and
 // z * partials_stride (wind partials).
 template <bool CONST_F>
-__global__ void __launch_bounds__(kANT, 2)
+__global__ void __launch_bounds__(kANT, CONST_F ? 3 : 2)
 stage_vjp_members_kernel(const GocCdklmParams p, const StepConst k, float dt, int rk_step, const float* xe,
                          const float* xu, const float* xv, const float* ae, const float* au, const float* av,
                          const float* ybe, const float* ybu, const float* ybv, const float* bbe, const float* bbu,
@@ -421,7 +455,7 @@ static int launch_vjp(const GocCdklmParams* p, const StepConst& k, float dt, int
                       int pitch_f, const float* Hi, int hip_f, const float* Hm, int hmp_f, float* wind,
                       cudaStream_t st) {
     constexpr int W = kAX + 2 * kAHalo, H = kAY + 2 * kAHalo;
-    constexpr size_t smem = sizeof(AdjSmem<W, H>);
+    constexpr size_t smem = sizeof(AdjSmem<W, H, !CF>);
     auto kern = stage_vjp_kernel<CF>;
     static bool configured = false;
     if (!configured) {
@@ -503,7 +537,7 @@ extern "C" int goc_cdklm_stage_vjp_members(const GocCdklmParams* p, float dt, in
     const bool cf = (p->coriolis_nx == 1 && p->coriolis_ny == 1);
     cudaStream_t st = as_stream(stream);
     constexpr int W = kAX + 2 * kAHalo, H = kAY + 2 * kAHalo;
-    constexpr size_t smem = sizeof(AdjSmem<W, H>);
+    const size_t smem = cf ? sizeof(AdjSmem<W, H, false>) : sizeof(AdjSmem<W, H, true>);
     const int partials = goc_cdklm_vjp_partials(p->nx, p->ny);
     dim3 grid((p->nx + kAX - 1) / kAX, (p->ny + kAY - 1) / kAY, n_members);
     static bool configured[2] = {false, false};

@@ -24,11 +24,21 @@
 
 namespace goc {
 
-template <int W, int H>
+// Shared memory of the VJP tile.  The forward recompute uses D, Sx, Sy, Fx,
+// Gy, Hi (and Fc with a Coriolis texture); after the cell pass the flux
+// planes are reused: Fx holds the slope adjoints (x slopes, then y slopes)
+// and Gy the flux-divergence adjoint of each cell, later the x-bar of each
+// staged position.  18 planes with a constant f: three CTAs per SM.
+template <int W, int H, bool HAS_FC>
 struct AdjSmem {
-    TileSmem<W, H> T;       // forward recompute; Fx/Gy hold slope-bar after the cell pass
+    float D[3][H][W];
+    float Sx[3][H][W];
+    float Sy[3][H][W];
+    float Fx[3][H][W];
+    float Gy[3][H][W];
     float Db[3][H][W];      // adjoint of the desingularised (eta, u, v)
-    float FDb[3][H][W];     // adjoint of the flux divergence of each cell; later x-bar per position
+    float Hi[H + 1][W + 1];
+    float Fc[HAS_FC ? H : 1][HAS_FC ? W : 1];
 };
 
 // ---------------------------------------------------------------------------
@@ -224,22 +234,23 @@ __device__ __forceinline__ void friction_vjp(const GocCdklmParams& p, float dt, 
 // the tile
 // ---------------------------------------------------------------------------
 
-template <int W, int H, int NT, bool BORDER>
+template <int W, int H, int NT, bool BORDER, bool HAS_FC>
 struct AdjTile {
-    AdjSmem<W, H>& A;
-    Tile<W, H, NT, BORDER>& T;
+    using SM = AdjSmem<W, H, HAS_FC>;
+    SM& A;
+    Tile<W, H, NT, BORDER, SM>& T;
     const GocCdklmParams& p;
     const StepConst& k;
 
-    // slope-bar planes live in the (then unused) flux planes
-    __device__ float (&Sxb(int c))[H][W] { return A.T.Fx[c]; }
-    __device__ float (&Syb(int c))[H][W] { return A.T.Gy[c]; }
+    // the slope adjoints of one direction at a time live in the flux planes Fx
+    __device__ float (&Sxb(int c))[H][W] { return A.Fx[c]; }
+    __device__ float (&Syb(int c))[H][W] { return A.Fx[c]; }
 
     // Reverse of one x face (east face of local cell (i, j)), adding to the
     // D-bar and x-slope-bar of cells i and i+1.
     template <bool CONST_F>
     __device__ void face_x_vjp(int i, int j, float F0b, float F1b, float F2b) {
-        TileSmem<W, H>& S = A.T;
+        SM& S = A;
         const float ebm = S.D[0][j][i], ebp = S.D[0][j][i + 1];
         const bool dm = (ebm == kDryFlag), dp = (ebp == kDryFlag);
         if (dm && dp) return;
@@ -299,7 +310,7 @@ struct AdjTile {
     // Reverse of one y face (north face of local cell (i, j)).
     template <bool CONST_F>
     __device__ void face_y_vjp(int i, int j, float G0b, float G1b, float G2b) {
-        TileSmem<W, H>& S = A.T;
+        SM& S = A;
         const float ebm = S.D[0][j][i], ebp = S.D[0][j + 1][i];
         const bool dm = (ebm == kDryFlag), dp = (ebp == kDryFlag);
         if (dm && dp) return;
@@ -358,7 +369,7 @@ struct AdjTile {
     // Reverse of the x slopes of local cell (i, j): adds to D-bar of i-1, i, i+1.
     template <bool CONST_F>
     __device__ void slope_x_vjp(int i, int j) {
-        TileSmem<W, H>& S = A.T;
+        SM& S = A;
         const float g0 = Sxb(0)[j][i], g1 = Sxb(1)[j][i], g2 = Sxb(2)[j][i];
         if (g0 == 0.0f && g1 == 0.0f && g2 == 0.0f) return;
         const float th = p.theta;
@@ -414,7 +425,7 @@ struct AdjTile {
     // Reverse of the y slopes of local cell (i, j): adds to D-bar of j-1, j, j+1.
     template <bool CONST_F>
     __device__ void slope_y_vjp(int i, int j) {
-        TileSmem<W, H>& S = A.T;
+        SM& S = A;
         const float g0 = Syb(0)[j][i], g1 = Syb(1)[j][i], g2 = Syb(2)[j][i];
         if (g0 == 0.0f && g1 == 0.0f && g2 == 0.0f) return;
         const float th = p.theta;

@@ -124,9 +124,11 @@ __device__ __forceinline__ void cdklm_flux(const GocCdklmParams& p, const StepCo
     F2 = f2;
 }
 
-template <int W, int H, int NT, bool BORDER>
+// SM: the shared-memory layout; any struct with the members of TileSmem that
+// the stage code reads (D, Sx, Sy, Fx, Gy, Hi and, with a Coriolis texture, Fc).
+template <int W, int H, int NT, bool BORDER, class SM = TileSmem<W, H>>
 struct Tile {
-    TileSmem<W, H>& S;
+    SM& S;
     const GocCdklmParams& p;
     const StepConst& k;
     int x0, y0;               // global cell of local (0,0)
