@@ -100,6 +100,13 @@ REF_CONFIGS = {
     "init_bm": ("initHm_kernel.cu", {"block_width": 16, "block_height": 16}, []),
     "noise_const": ("ocean_noise.cu", noise_defines(), NOISE_FLAGS),
     "noise_jet512": ("ocean_noise.cu", noise_defines(coriolis_shape=jet_texture_shape(512, 300)), NOISE_FLAGS),
+    # the three levels of the multi-level ensemble (2560 km x 1500 km, double jet)
+    **{f"cdklm_ml{nx}x{ny}": ("CDKLM16_kernel.cu",
+                              cdklm_defines(nx, ny, 2560e3 / nx, 1500e3 / ny, coriolis_shape=jet_texture_shape(nx, ny)),
+                              CDKLM_FLAGS)
+       for nx, ny in ((128, 64), (256, 128), (512, 256))},
+    **{f"noise_ml{nx}x{ny}": ("ocean_noise.cu", noise_defines(coriolis_shape=jet_texture_shape(nx, ny)), NOISE_FLAGS)
+       for nx, ny in ((128, 64), (256, 128), (512, 256))},
     # GPUDrifterCollection with the default 1x1 wind (D/GPUDrifterCollection.py:70-76)
     "drift": ("driftKernels.cu", {"block_width": 64, "block_height": 1, "WIND_X_NX": 1, "WIND_X_NY": 1,
                                   "WIND_Y_NX": 1, "WIND_Y_NY": 1}, []),

@@ -296,3 +296,75 @@ def test_reference_kernel_step_rate(ctx):
                       "product_cell_steps_per_s": cells / t_prod}))
     ref.free()
     sim.cleanUp()
+
+
+def _ref_block_rate(ctx, c, cdk, noise_cfg, n_drifters, members, blocks=3, block_s=60.0, factor=8):
+    """Member-cell-steps/s of the reference kernels stepping `members`
+    copies of case `c` one after the other, each block being
+    step(block_s) + drifters after every step + one SOAR perturbation
+    (injected normals), the member-by-member cadence of the reference's
+    ensembles."""
+    sim = _product(ctx, c, 0.0)
+    sim.updateDt(courant_number=0.8)
+    dt = float(sim.dt)
+    refs = []
+    rng = np.random.default_rng(1)
+    for _ in range(members):
+        ref = _reference(cdk, c, dt, sim)
+        q0, L = _soar_q0(), 8.0 * c["dx"] * factor
+        rn = rk.RefNoise(noise_cfg, ref, q0, L, interpolation_factor=factor)
+        rn.set_random(rng.standard_normal((rn.rand_ny, rn.rand_nx)).astype(np.float32))
+        rd = None
+        if n_drifters:
+            Lx, Ly = c["nx"] * c["dx"], c["ny"] * c["dy"]
+            pos = np.stack([rng.random(n_drifters + 1) * Lx, rng.random(n_drifters + 1) * Ly], axis=1)
+            rd = rk.RefDrifters(pos.astype(np.float32), Lx, Ly, 0, 1)
+        refs.append((ref, rn, rd))
+
+    def block(ref, rn, rd):
+        ref.step(block_s, drifters=rd)
+        rn.perturb(ref)
+        ref._boundary(ref.h0)
+
+    for r in refs:
+        block(*r)
+    refs[0][0].synchronize()
+    steps0 = sum(r[0].num_iterations for r in refs)
+    t0 = time.perf_counter()
+    for _ in range(blocks):
+        for r in refs:
+            block(*r)
+    refs[0][0].synchronize()
+    wall = time.perf_counter() - t0
+    steps = sum(r[0].num_iterations for r in refs) - steps0
+    for ref, rn, rd in refs:
+        rn.free()
+        ref.free()
+        if rd is not None:
+            rd.free()
+    sim.cleanUp()
+    return steps * c["nx"] * c["ny"] / wall, wall / (blocks * members)
+
+
+def test_reference_kernel_member_rates_c3_c4(ctx):
+    """The reference's kernels stepped member by member (its ensembles'
+    pattern) on the benchmark workloads: C3 (512 x 300 double jet, 1000
+    drifters, SOAR every 60 s, coarse factor 8) and C4 (levels 128 x 64,
+    256 x 128, 512 x 256 of one 2560 km x 1500 km domain, 512 / 128 / 32
+    members, SOAR every 60 s).  Normals are injected, so the reference's
+    random-number generation is not timed.  Printed as one JSON line."""
+    from gpuocean_gb300.utils.BenchmarkCases import double_jet_case
+    c3, _ = _ref_block_rate(ctx, double_jet_case(), "cdklm_jet512", "noise_jet512", 1000, members=4)
+    levels = ((128, 64, 512), (256, 128, 128), (512, 256, 32))
+    total_cells, total_time = 0.0, 0.0
+    per_level = {}
+    for nx, ny, n in levels:
+        c = double_jet_case(nx=nx, ny=ny, dx=2560e3 / nx, dy=1500e3 / ny)
+        rate, t_block = _ref_block_rate(ctx, c, f"cdklm_ml{nx}x{ny}", f"noise_ml{nx}x{ny}", 0, members=4)
+        per_level[f"{nx}x{ny}"] = rate
+        total_time += n * t_block
+        total_cells += n * t_block * rate
+    c4 = total_cells / total_time
+    print(json.dumps({"case": "reference kernels member by member", "c3_member_cell_steps_per_s": c3,
+                      "c4_member_cell_steps_per_s": c4, "c4_levels": per_level}))
+    assert c3 > 0 and c4 > 0
