@@ -411,3 +411,54 @@ class CDKLM16EnsembleRollout(torch.autograd.Function):
             ctx.segments[start] = None
         ctx.segments = None
         return None, None, None, lam, adj.wind_grad()
+
+
+def _main(argv=None):
+    """``python -m gpuocean_gb300.adjoint [--members M] [--n N] [--calls C]``:
+    C step VJPs of M members of the N x N Gaussian bump (H = 60 m, walls)
+    with a dense random adjoint, after 20 forward steps; prints the mean
+    time of one step VJP and of one forward step.  A small, self-contained
+    workload for timing and profiling the adjoint kernels."""
+    import argparse
+    import json
+    from .SWEsimulators import CDKLM16
+    from .utils import Common
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--members", type=int, default=32)
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--calls", type=int, default=4)
+    a = ap.parse_args(argv)
+    ctx = Common.CUDAContext()
+    n = a.n
+    x = (np.arange(n + 4) - 2 + 0.5 - n / 2.0)
+    eta = (0.1 * np.exp(-(x[None, :] ** 2 + x[:, None] ** 2) / 200.0)).astype(np.float32)
+    z = np.zeros_like(eta)
+    sim = CDKLM16.CDKLM16(ctx, eta, z, z.copy(), np.full((n + 5, n + 5), 60.0, np.float32), n, n, 200.0, 200.0,
+                          0.0, 9.81, 1.2e-4, 0.0)
+    sim.updateDt(courant_number=0.45)
+    adj = EnsembleStepAdjoint(sim, a.members)
+    base = torch.as_tensor(np.stack([np.asarray(v, np.float32) for v in sim.download()]), device=adj.device)
+    q0 = base.unsqueeze(0).repeat(a.members, 1, 1, 1).contiguous()
+    q1, qs = adj.zeros(), adj.zeros()
+    for _ in range(20):
+        adj.step(q0, q1, qs)
+        q0, q1 = q1, q0
+    lam, ls, ln = adj.zeros(), adj.zeros(), adj.zeros()
+    lam.normal_()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    torch.cuda.synchronize()
+    ev[0].record()
+    for _ in range(a.calls):
+        adj.step_vjp(q0, qs, lam, ls, ln)
+    ev[1].record()
+    for _ in range(a.calls):
+        adj.step(q0, q1, qs)
+    ev[2].record()
+    torch.cuda.synchronize()
+    vjp, step = ev[0].elapsed_time(ev[1]) / a.calls, ev[1].elapsed_time(ev[2]) / a.calls
+    print(json.dumps({"members": a.members, "n": n, "step_vjp_ms": vjp, "step_ms": step, "ratio": vjp / step}))
+    sim.cleanUp()
+
+
+if __name__ == "__main__":
+    _main()
