@@ -149,16 +149,28 @@ __device__ __forceinline__ float coarse_at(const GocNoiseDesc& d, int j, int i) 
     return d.coarse[(size_t)j * (d.coarse_pitch / 4) + i];
 }
 
-// Bicubic value of the coarse field at fine cell (ti, tj) (K/ocean_noise.cu:497-586)
-__device__ float bicubic_value(const GocNoiseDesc& d, const OceanRef& o, int ti, int tj) {
+// Bicubic up-sampling of the coarse field (K/ocean_noise.cu:497-586), split in
+// three parts so that a tile computes the coefficient matrix of each coarse
+// cell once and evaluates it at every fine cell inside: the coarse cell (ci, cj)
+// of fine cell (ti, tj) with the fractional position (rx, ry) in it, the 4x4
+// coefficients A of coarse cell (ci, cj), and the polynomial.
+__device__ __forceinline__ int bicubic_ci(const GocNoiseDesc& d, const OceanRef& o, int ti, float* rx) {
     const float x = (ti - 2 + 0.5f + d.offset_i) * o.dx;
-    const float y = (tj - 2 + 0.5f + d.offset_j) * o.dy;
     int ci = (int)floorf(x / d.coarse_dx + 2 - 0.5f);
-    int cj = (int)floorf(y / d.coarse_dy + 2 - 0.5f);
     if (ci > d.coarse_nx + 1) ci -= 1;
+    *rx = (x - (ci - 2 + 0.5f) * d.coarse_dx) / d.coarse_dx;
+    return ci;
+}
+
+__device__ __forceinline__ int bicubic_cj(const GocNoiseDesc& d, const OceanRef& o, int tj, float* ry) {
+    const float y = (tj - 2 + 0.5f + d.offset_j) * o.dy;
+    int cj = (int)floorf(y / d.coarse_dy + 2 - 0.5f);
     if (cj > d.coarse_ny + 1) cj -= 1;
-    const float rx = (x - (ci - 2 + 0.5f) * d.coarse_dx) / d.coarse_dx;
-    const float ry = (y - (cj - 2 + 0.5f) * d.coarse_dy) / d.coarse_dy;
+    *ry = (y - (cj - 2 + 0.5f) * d.coarse_dy) / d.coarse_dy;
+    return cj;
+}
+
+__device__ __forceinline__ void bicubic_coeffs(const GocNoiseDesc& d, int ci, int cj, float* A /* [16], row-major */) {
     float c[4][4];  // c[row][col] = coarse[cj-1+row][ci-1+col]
 #pragma unroll
     for (int r = 0; r < 4; ++r)
@@ -176,7 +188,7 @@ __device__ float bicubic_value(const GocNoiseDesc& d, const OceanRef& o, int ti,
     F[2][2] = (F[1][2] - fy_10) / 2.0f; F[2][3] = (F[1][3] - fy_11) / 2.0f;
     F[3][2] = (fy20 - F[0][2]) / 2.0f; F[3][3] = (fy21 - F[0][3]) / 2.0f;
     const float B[4][4] = {{1, 0, 0, 0}, {0, 0, 1, 0}, {-3, 3, -2, -1}, {2, -2, 1, 1}};
-    float FB[4][4], A[4][4];   // FB = F B^T, A = B FB
+    float FB[4][4];   // FB = F B^T, A = B FB
 #pragma unroll
     for (int r = 0; r < 4; ++r)
 #pragma unroll
@@ -186,14 +198,25 @@ __device__ float bicubic_value(const GocNoiseDesc& d, const OceanRef& o, int ti,
     for (int r = 0; r < 4; ++r)
 #pragma unroll
         for (int q = 0; q < 4; ++q)
-            A[r][q] = B[r][0] * FB[0][q] + B[r][1] * FB[1][q] + B[r][2] * FB[2][q] + B[r][3] * FB[3][q];
+            A[4 * r + q] = B[r][0] * FB[0][q] + B[r][1] * FB[1][q] + B[r][2] * FB[2][q] + B[r][3] * FB[3][q];
+}
+
+__device__ __forceinline__ float bicubic_eval(const float* A, float rx, float ry) {
     const float xv[4] = {1.0f, rx, rx * rx, rx * rx * rx};
     const float yv[4] = {1.0f, ry, ry * ry, ry * ry * ry};
     float v = 0.0f;
 #pragma unroll
     for (int r = 0; r < 4; ++r)
-        v += xv[r] * (A[r][0] * yv[0] + A[r][1] * yv[1] + A[r][2] * yv[2] + A[r][3] * yv[3]);
+        v += xv[r] * (A[4 * r] * yv[0] + A[4 * r + 1] * yv[1] + A[4 * r + 2] * yv[2] + A[4 * r + 3] * yv[3]);
     return v;
+}
+
+// Bicubic value of the coarse field at fine cell (ti, tj).
+__device__ float bicubic_value(const GocNoiseDesc& d, const OceanRef& o, int ti, int tj) {
+    float rx, ry, A[16];
+    const int ci = bicubic_ci(d, o, ti, &rx), cj = bicubic_cj(d, o, tj, &ry);
+    bicubic_coeffs(d, ci, cj, A);
+    return bicubic_eval(A, rx, ry);
 }
 
 // Perturbation of interior cell (ti, tj).  `factor1`: the coarse grid is the
@@ -231,18 +254,40 @@ __device__ __forceinline__ void perturb_cell(const GocNoiseDesc& d, const OceanR
 }
 
 constexpr int kNB = 16;  // noise tile edge
+constexpr int kNC = 10;  // coarse cells per tile edge held in shared memory (enough for factor >= 2)
 
 // One 16x16 tile of interior cells (tile origin bx, by in interior cells).
 __device__ void perturb_tile(const GocNoiseDesc& d, const OceanRef& o, int bx, int by) {
     __shared__ float s_de[kNB + 2][kNB + 2];
-    const int tx = threadIdx.x, ty = threadIdx.y;
+    __shared__ float s_A[kNC * kNC][17];
+    const int tx = threadIdx.x, ty = threadIdx.y, t = ty * kNB + tx;
     const bool factor1 = d.interpolation_factor <= 1;
     // d_eta on the tile + 1 ring (interior origin at ghost offset 2)
-    for (int j = ty; j < kNB + 2; j += kNB)
-        for (int i = tx; i < kNB + 2; i += kNB) {
-            const int gi = 2 + bx + i - 1, gj = 2 + by + j - 1;
-            s_de[j][i] = factor1 ? coarse_at(d, gj, gi) : bicubic_value(d, o, gi, gj);
+    const int gi0 = 2 + bx - 1, gj0 = 2 + by - 1;
+    if (factor1) {
+        for (int j = ty; j < kNB + 2; j += kNB)
+            for (int i = tx; i < kNB + 2; i += kNB) s_de[j][i] = coarse_at(d, gj0 + j, gi0 + i);
+    } else {
+        // the coarse cells under the tile: the index is monotone in the fine index
+        float r;
+        const int ci0 = bicubic_ci(d, o, gi0, &r), ci1 = bicubic_ci(d, o, gi0 + kNB + 1, &r);
+        const int cj0 = bicubic_cj(d, o, gj0, &r), cj1 = bicubic_cj(d, o, gj0 + kNB + 1, &r);
+        const int ncx = ci1 - ci0 + 1, ncy = cj1 - cj0 + 1;
+        if (ncx <= kNC && ncy <= kNC) {
+            for (int c = t; c < ncx * ncy; c += kNB * kNB) bicubic_coeffs(d, ci0 + c % ncx, cj0 + c / ncx, s_A[c]);
+            __syncthreads();
+            for (int j = ty; j < kNB + 2; j += kNB)
+                for (int i = tx; i < kNB + 2; i += kNB) {
+                    float rx, ry;
+                    const int ci = bicubic_ci(d, o, gi0 + i, &rx), cj = bicubic_cj(d, o, gj0 + j, &ry);
+                    const int a = clampi(cj - cj0, 0, ncy - 1) * ncx + clampi(ci - ci0, 0, ncx - 1);
+                    s_de[j][i] = bicubic_eval(s_A[a], rx, ry);
+                }
+        } else {
+            for (int j = ty; j < kNB + 2; j += kNB)
+                for (int i = tx; i < kNB + 2; i += kNB) s_de[j][i] = bicubic_value(d, o, gi0 + i, gj0 + j);
         }
+    }
     __syncthreads();
     const int ti = 2 + bx + tx, tj = 2 + by + ty;
     if (ti < o.nx + 2 && tj < o.ny + 2)
