@@ -334,6 +334,72 @@ def run_multilevel(ctx, args, levels=((128, 64, 512), (256, 128, 128), (512, 256
             "per_member_sample": len(sample), "tile_shape": shape}
 
 
+def run_statistics(ens, sims, peak, peak_kind, n_positions=1000, repeats=10):
+    """Observation operator and ensemble statistics on the C3 ensemble
+    (every member at 512 x 300): one launch observing every member at
+    n_positions shared positions, and mean + variance of (eta, hu, hv) and of
+    the desingularised (u, v) over all members (E/BaseOceanStateEnsemble.py:
+    79-176).  The member states (12 B per member-cell) exceed L2.  Algorithmic
+    bytes: the member fields read once plus the two output fields.  The
+    reference's path - download every member, reduce with NumPy - is timed
+    once on the same members."""
+    from gpuocean_gb300 import _lib
+    n = len(sims)
+    nx, ny = int(sims[0].nx), int(sims[0].ny)
+    cells = nx * ny
+    stream = ens.stream.handle
+    ev = [ctypes.c_void_p(), ctypes.c_void_p()]
+    for e in ev:
+        _lib.call("goc_event_create", ctypes.byref(e))
+
+    def timed(fn):
+        fn()
+        ens.synchronize()
+        _lib.call("goc_event_record", ev[0], stream)
+        for _ in range(repeats):
+            fn()
+        _lib.call("goc_event_record", ev[1], stream)
+        ens.synchronize()
+        ms = ctypes.c_float()
+        _lib.call("goc_event_elapsed_ms", ev[0], ev[1], ctypes.byref(ms))
+        return ms.value / repeats
+
+    out = {"members": n, "nx": nx, "ny": ny}
+    m, v = ens.moments(download=False)
+    mu, vu = ens.moments(quantity="velocity", desingularise=1e-5, download=False)
+    ens._ensure_table()
+    for key, q, planes, eps, bm, bv in (("state", 0, 3, 0.0, m, v), ("velocity", 1, 2, 1e-5, mu, vu)):
+        ms = timed(lambda: _lib.call("goc_ensemble_moments", ens._handle, 0, n, q, ctypes.c_float(eps), 0, bm.ptr,
+                                     bv.ptr, stream))
+        alg = n * cells * (12 if q == 0 else 16) + 2 * planes * cells * 4
+        out[f"moments_{key}_ms"] = ms
+        out[f"moments_{key}_gbs"] = alg / (ms * 1e-3) / 1e9
+        out[f"moments_{key}_frac"] = out[f"moments_{key}_gbs"] / peak
+    for b in (m, v, mu, vu):
+        b.free()
+    out["peak_gbs"], out["peak_kind"] = peak, peak_kind
+    out["bytes_per_member_cell"] = {"state": 12, "velocity": "16 (eta, hu, hv, Hm)"}
+    rng = np.random.default_rng(3)
+    pos = np.stack([rng.uniform(0, nx * float(sims[0].dx), n_positions),
+                    rng.uniform(0, ny * float(sims[0].dy), n_positions)], axis=1).astype(np.float32)
+    ens.observe(pos)
+    out_buf = ens._obs_out
+    pbuf = ens._obs_pos
+    out["observe_ms"] = timed(lambda: _lib.call("goc_ensemble_observe", ens._handle, 0, n, pbuf.ptr, 8,
+                                                ctypes.c_longlong(0), n_positions, out_buf.ptr, stream))
+    out["observe_positions"] = n_positions
+    for e in ev:
+        _lib.load().goc_event_destroy(e)
+    # the reference's path: download every member's interior, reduce with NumPy
+    t0 = time.perf_counter()
+    st = np.moveaxis(np.array([np.array(s.download(interior_domain_only=True)) for s in sims]), 0, -1)
+    np.mean(st, axis=-1)
+    np.var(st, axis=-1)
+    out["host_download_numpy_ms"] = 1000.0 * (time.perf_counter() - t0)
+    out["device_over_host"] = out["host_download_numpy_ms"] / (out["moments_state_ms"])
+    return out
+
+
 def run_adjoint(ctx, n=256, n_steps=400, every=10, n_points=64):
     """Adjoint of the CDKLM16 rollout: the Gaussian bump (n x n, dx = dy =
     200 m, H = 60 m, f = 1.2e-4, walls, 0.1 m amplitude, sigma 10 cells) with
@@ -493,6 +559,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-multilevel", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-statistics", action="store_true")
     args = ap.parse_args()
     rank, world, local = dist_env()
     spec = workload_spec(args.workload, args.members if args.workload == "c3" else 1)
@@ -659,6 +726,7 @@ def main():
         s.gpu_stream.synchronize()
     per_member_rate = pm_cells / (time.perf_counter() - t0)
 
+    ens_stats = None if args.no_statistics else run_statistics(ens, sims, *measured_peaks())
     multilevel = None if args.no_multilevel else run_multilevel(ctx, args)
     adjoint = None if args.no_adjoint else run_adjoint(ctx)
 
@@ -696,7 +764,7 @@ def main():
                          "peak_kind": peak_kind, "avg_launch_ms": 1000.0 * avg_dur,
                          "algorithmic_bytes_per_launch": avg_bytes},
             "e2e": e2e, "gpu_launches": launches, "clocks": clk, "cpu_baseline": cpu,
-            "multilevel": multilevel, "adjoint": adjoint,
+            "multilevel": multilevel, "adjoint": adjoint, "statistics": ens_stats,
             "wall_s": wall,
         }
         print(json.dumps(line), flush=True)

@@ -64,6 +64,8 @@ SIGNATURES = {
     "goc_event_create": (c_int, [ctypes.POINTER(c_void_p)]),
     "goc_event_destroy": (c_int, [c_void_p]),
     "goc_event_record": (c_int, [c_void_p, c_void_p]),
+    "goc_stream_fan_out": (c_int, [c_void_p, c_void_p, c_int]),
+    "goc_stream_fan_in": (c_int, [c_void_p, c_void_p, c_int]),
     "goc_event_elapsed_ms": (c_int, [c_void_p, c_void_p, ctypes.POINTER(c_float)]),
     "goc_graph_begin_capture": (c_int, [c_void_p]),
     "goc_graph_end_capture": (c_int, [c_void_p, ctypes.POINTER(c_void_p)]),
@@ -103,6 +105,13 @@ SIGNATURES = {
                               c_int, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_float,
                               c_void_p, c_void_p, c_void_p, c_void_p]),
     "goc_drift_enforce_boundary": (c_int, [c_float, c_float, c_int, c_int, c_int, c_void_p, c_int, c_void_p]),
+    "goc_observe_underlying_flow": (c_int, [c_int, c_int, c_float, c_float, c_int, c_int, c_void_p, c_int, c_void_p,
+                                            c_int, c_void_p, c_int, c_float, c_int, c_void_p, c_int, c_void_p, c_int,
+                                            c_void_p]),
+    "goc_ensemble_observe": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, ctypes.c_longlong, c_int, c_void_p,
+                                     c_void_p]),
+    "goc_ensemble_moments": (c_int, [c_void_p, c_int, c_int, c_int, c_float, c_int, c_void_p, c_void_p, c_void_p]),
+    "goc_ml_combine": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p]),
     "goc_ensemble_create": (c_int, [c_void_p, c_int, c_int, ctypes.POINTER(c_void_p)]),
     "goc_ensemble_destroy": (c_int, [c_void_p]),
     "goc_ensemble_size": (c_int, [c_void_p, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),

@@ -126,6 +126,42 @@ int goc_stream_synchronize(void* stream) {
     return cuda_result(cudaStreamSynchronize(as_stream(stream)), "cudaStreamSynchronize");
 }
 
+// Device-side ordering between one stream and many (no host wait).  Each
+// signalling stream gets a timing-free event recorded on it; the event is
+// released right after the waits are queued (the waits keep the recorded
+// state).
+static int wait_on(cudaStream_t waiter, cudaStream_t signaller) {
+    if (waiter == signaller) return GOC_OK;
+    cudaEvent_t e = nullptr;
+    cudaError_t err = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if (err == cudaSuccess) err = cudaEventRecord(e, signaller);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(waiter, e, 0);
+    if (e) cudaEventDestroy(e);
+    return cuda_result(err, "stream ordering");
+}
+
+int goc_stream_fan_out(void* signaller, void* const* waiters, int n_waiters) {
+    if (n_waiters < 0 || (n_waiters > 0 && !waiters)) return set_error(GOC_ERR_ARG, "goc_stream_fan_out: bad list");
+    if (n_waiters == 0) return GOC_OK;
+    cudaEvent_t e = nullptr;
+    cudaError_t err = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if (err == cudaSuccess) err = cudaEventRecord(e, as_stream(signaller));
+    for (int i = 0; err == cudaSuccess && i < n_waiters; ++i)
+        if (waiters[i] != signaller) err = cudaStreamWaitEvent(as_stream(waiters[i]), e, 0);
+    if (e) cudaEventDestroy(e);
+    return cuda_result(err, "goc_stream_fan_out");
+}
+
+int goc_stream_fan_in(void* waiter, void* const* signallers, int n_signallers) {
+    if (n_signallers < 0 || (n_signallers > 0 && !signallers))
+        return set_error(GOC_ERR_ARG, "goc_stream_fan_in: bad list");
+    for (int i = 0; i < n_signallers; ++i) {
+        int rc = wait_on(as_stream(waiter), as_stream(signallers[i]));
+        if (rc) return rc;
+    }
+    return GOC_OK;
+}
+
 int goc_event_create(void** event) {
     if (!event) return set_error(GOC_ERR_ARG, "goc_event_create: null out pointer");
     cudaEvent_t e = nullptr;

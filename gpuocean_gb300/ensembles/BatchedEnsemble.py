@@ -123,8 +123,37 @@ class BatchedEnsemble:
         self._sched_key = None
         self._dt_dev = Common.DevicePtr(4 * len(self.sims))
         self._attach_drifters()
+        self._collect_streams()
         if getattr(self, "_noises", None) is not None:
             self.set_noise(self._noises, getattr(self, "_random_pool", None))
+
+    def _collect_streams(self):
+        """The members' own streams (simulator, drifters, model error): the
+        engine's stream is ordered after them before it reads the members
+        and they after it once it has written them, on the device, so a
+        member's own calls (download, upload, perturbState, ...) always see
+        the engine's results and the engine theirs."""
+        handles = {}
+        for s in self.sims:
+            objs = [s.gpu_stream]
+            if s.hasDrifters:
+                objs.append(getattr(s.drifters, "gpu_stream", None))
+            if getattr(s, "model_error", None) is not None:
+                objs.append(getattr(s.model_error, "gpu_stream", None))
+            for o in objs:
+                h = Common._stream_handle(o)
+                if h is not None and h != self.stream.handle:
+                    handles[h] = None
+        self._member_streams = (ctypes.c_void_p * max(1, len(handles)))(*handles.keys())
+        self._n_member_streams = len(handles)
+
+    def _after_members(self):
+        """Engine stream waits for the work queued on the members' streams."""
+        _lib.call("goc_stream_fan_in", self.stream.handle, self._member_streams, self._n_member_streams)
+
+    def _before_members(self):
+        """Members' streams wait for the work queued on the engine stream."""
+        _lib.call("goc_stream_fan_out", self.stream.handle, self._member_streams, self._n_member_streams)
 
     def _attach_drifters(self):
         """Drifter collections attached to the members are advected inside
@@ -148,6 +177,11 @@ class BatchedEnsemble:
 
     def release(self):
         self.release_noise()
+        for name in ("_obs_pos", "_obs_out"):
+            buf = getattr(self, name, None)
+            if buf is not None:
+                buf.free()
+                setattr(self, name, None)
         for g in getattr(self, "_graphs", {}).values():
             _lib.load().goc_graph_destroy(g[0])
         self._graphs = {}
@@ -207,6 +241,7 @@ class BatchedEnsemble:
         sig = self._grid_signature()
         best = _AUTOTUNE_CACHE.get(sig)
         if best is None:
+            self._after_members()
             shapes = self.tile_shapes()
             idx = list(range(len(shapes))) if candidates is None else list(candidates)
             n = len(self.sims)
@@ -284,6 +319,7 @@ class BatchedEnsemble:
         self._noise = h.value
         self._noise_descs = descs
         self._noises = noises
+        self._collect_streams()
         self._rng_seed = rng_seed
         if rng_seed is not None:
             _lib.call("goc_noise_batch_seed", self._noise, ctypes.c_ulonglong(int(rng_seed)), self.stream.handle)
@@ -305,7 +341,9 @@ class BatchedEnsemble:
     def perturb(self, perturbation_scale=1.0, update_random_field=True):
         """Add the SOAR model error to every member's current state."""
         before = _lib.load().goc_kernel_launch_count()
+        self._after_members()
         self._noise_launch(-1, perturbation_scale, update_random_field)
+        self._before_members()
         self.kernels_launched += _lib.load().goc_kernel_launch_count() - before
 
     def _launch_block(self, nsub, noise=None):
@@ -333,11 +371,8 @@ class BatchedEnsemble:
         for s in self.sims:
             if s.t == 0:
                 s.bc_kernel.boundaryCondition(s.gpu_stream, s.gpu_data.h0, s.gpu_data.hu0, s.gpu_data.hv0)
-                s.gpu_stream.synchronize()
-        for s in self.sims:
-            if s.hasDrifters:
-                s.drifters.gpu_stream.synchronize()
         scheds, table, n, nsub = self._schedule(t_end)
+        self._after_members()
         key = (n.tobytes(), table.tobytes())
         if key != getattr(self, "_sched_key", None):
             _lib.call("goc_ensemble_set_schedule", self._handle, table.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
@@ -355,6 +390,7 @@ class BatchedEnsemble:
             self.kernels_launched += entry[1]
         else:
             self.kernels_launched += self._launch_block(nsub, with_noise)
+        self._before_members()
         cells = 0
         for m, s in enumerate(self.sims):
             for local_dt in scheds[m]:
@@ -371,8 +407,99 @@ class BatchedEnsemble:
     def synchronize(self):
         self.stream.synchronize()
 
+    # ------------------------------------------------------------------
+    # observation operator and ensemble statistics
+    # ------------------------------------------------------------------
+    def _ensure_table(self):
+        """The device member table must point at the current buffers."""
+        if self._current_ptrs() != self._ptrs:
+            self._build(max_substeps=self.max_substeps)
+
+    def _scratch(self, name, nbytes):
+        buf = getattr(self, name, None)
+        if buf is None or buf.nbytes < nbytes:
+            if buf is not None:
+                buf.free()
+            buf = Common.DevicePtr(max(int(nbytes), 256))
+            setattr(self, name, buf)
+        return buf
+
+    def _download(self, buf, shape, dtype=np.float32):
+        out = np.empty(shape, dtype=dtype)
+        if out.nbytes:
+            _lib.call("goc_memcpy_d2h_async", out.ctypes.data, buf.ptr, ctypes.c_size_t(out.nbytes), self.stream.handle)
+        self.stream.synchronize()
+        return out
+
+    def observe(self, positions=None, first=0, count=None, drifters=None):
+        """(eta, hu, hv) of members [first, first + count) at the cells
+        holding the given positions, in one launch: an array (count,
+        positions, 3).  positions: (D, 2) metres from the south-west
+        interior corner (host), or ``drifters``: a GPUDrifterCollection whose
+        device positions every member observes (its last row, the
+        observation position, is left out), as the reference's GPU path of
+        observeParticles does (E/BaseOceanStateEnsemble.py:113-130)."""
+        count = len(self.sims) - first if count is None else int(count)
+        self._ensure_table()
+        self._after_members()
+        if drifters is not None:
+            _lib.call("goc_stream_fan_in", self.stream.handle,
+                      (ctypes.c_void_p * 1)(Common._stream_handle(drifters.gpu_stream)), 1)
+            D = int(drifters.getNumDrifters())
+            pos_ptr, pitch = drifters.driftersDevice.ptr, int(drifters.driftersDevice.pitch)
+        else:
+            pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 2)
+            D = pos.shape[0]
+            buf = self._scratch("_obs_pos", pos.nbytes)
+            if pos.nbytes:
+                _lib.call("goc_memcpy_h2d_async", buf.ptr, pos.ctypes.data, ctypes.c_size_t(pos.nbytes),
+                          self.stream.handle)
+            pos_ptr, pitch = buf.ptr, 8
+        out = self._scratch("_obs_out", 12 * count * D)
+        before = _lib.load().goc_kernel_launch_count()
+        _lib.call("goc_ensemble_observe", self._handle, int(first), count, pos_ptr, pitch, ctypes.c_longlong(0), D,
+                  out.ptr, self.stream.handle)
+        self.kernels_launched += _lib.load().goc_kernel_launch_count() - before
+        return self._download(out, (count, D, 3))
+
+    def moments(self, first=0, count=None, quantity="state", desingularise=None, ddof=0, mean=True, var=True,
+                download=True):
+        """Mean and variance over members [first, first + count) (one grid)
+        per interior cell, in one pass over HBM.  quantity "state": planes
+        (eta, hu, hv); "velocity": (u, v) = (hu, hv) / (eta + Hm),
+        desingularised with eps = ``desingularise`` when given
+        (U/OceanographicUtilities.py:413-414).  Returns (mean, var) arrays of
+        shape (planes, ny, nx) (None for the one not asked for); with
+        ``download=False`` the device buffers instead."""
+        count = len(self.sims) - first if count is None else int(count)
+        assert quantity in ("state", "velocity")
+        self._ensure_table()
+        self._after_members()
+        s0 = self.sims[first]
+        planes = 3 if quantity == "state" else 2
+        nbytes = 4 * planes * int(s0.nx) * int(s0.ny)
+        bm = Common.DevicePtr(nbytes) if mean else None
+        bv = Common.DevicePtr(nbytes) if var else None
+        eps = 0.0 if desingularise is None else float(desingularise)
+        before = _lib.load().goc_kernel_launch_count()
+        _lib.call("goc_ensemble_moments", self._handle, int(first), count, 0 if quantity == "state" else 1,
+                  ctypes.c_float(eps), int(ddof), bm.ptr if bm else None, bv.ptr if bv else None, self.stream.handle)
+        self.kernels_launched += _lib.load().goc_kernel_launch_count() - before
+        if not download:
+            return bm, bv
+        shape = (planes, int(s0.ny), int(s0.nx))
+        out = []
+        for b in (bm, bv):
+            if b is None:
+                out.append(None)
+            else:
+                out.append(self._download(b, shape))
+                b.free()
+        return tuple(out)
+
     def updateDt(self, courant_number=None):
         """Batched CFL limit of every member (one reduction launch pair)."""
+        self._after_members()
         _lib.call("goc_ensemble_max_dt", self._handle, self._dt_dev.ptr, self.stream.handle)
         out = np.zeros(len(self.sims), dtype=np.float32)
         _lib.call("goc_memcpy_d2h_async", out.ctypes.data, self._dt_dev.ptr, ctypes.c_size_t(out.nbytes),

@@ -7,9 +7,23 @@ the member/tile work queue.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 
+from .. import _lib
+from ..utils import Common
 from .BatchedEnsemble import BatchedEnsemble
+
+
+def _device_statistic(func, kwargs):
+    """("mean" | "var", ddof) when func is a statistic the device computes
+    (np.mean, or np.var with at most a ddof keyword), else None."""
+    if func is np.mean and not kwargs:
+        return "mean", 0
+    if func is np.var and set(kwargs) <= {"ddof"}:
+        return "var", int(kwargs.get("ddof", 0))
+    return None
 
 
 class MultiLevelOceanEnsemble:
@@ -58,30 +72,119 @@ class MultiLevelOceanEnsemble:
                 self.engine.updateDt(courant_number=courant_number)
         self.t = s0.t
 
+    # ------------------------------------------------------------------
+    # state transfer (E/MultiLevelOceanEnsemble.py:143-239)
+    # ------------------------------------------------------------------
+    def _groups(self):
+        """Member ranges of the flat engine order: level 0, then per higher
+        level the fine partners followed by the coarse partners."""
+        out = [(0, int(self.Nes[0]))]
+        a = int(self.Nes[0])
+        for l_idx in range(1, self.numLevels):
+            n = int(self.Nes[l_idx])
+            out.append(((a, n), (a + n, n)))
+            a += 2 * n
+        return out
+
     def download(self, interior_domain_only=True):
-        """State per level: level 0 (Ne, 3, ny, nx); higher levels a pair."""
+        """State per level, (3, ny, nx, Ne); higher levels a [fine, coarse]
+        pair (E/MultiLevelOceanEnsemble.py:143-170)."""
         def states(sims):
-            return np.array([np.array(s.download(interior_domain_only=interior_domain_only)) for s in sims])
+            return np.moveaxis(np.array([np.array(s.download(interior_domain_only=interior_domain_only))
+                                         for s in sims]), 0, -1)
         out = [states(self.ML_ensemble[0])]
         for l_idx in range(1, self.numLevels):
             out.append([states(self.ML_ensemble[l_idx][0]), states(self.ML_ensemble[l_idx][1])])
         return out
 
-    def estimate(self, func, **kwargs):
-        """Multi-level estimator: func over level 0 plus the fine-coarse
-        differences of the higher levels, on the finest grid."""
-        state = self.download()
-        est = func(state[0], axis=0, **kwargs)
+    def downloadVelocities(self, interior_domain_only=True):
+        """(u, v) = (hu, hv) / (eta + Hm) per level, (2, ny, nx, Ne)
+        (E/MultiLevelOceanEnsemble.py:187-224)."""
+        def vel(sims):
+            _, Hm = sims[0].downloadBathymetry(interior_domain_only=interior_domain_only)
+            out = []
+            for s in sims:
+                eta, hu, hv = s.download(interior_domain_only=interior_domain_only)
+                out.append(np.array([hu / (eta + Hm), hv / (eta + Hm)]))
+            return np.moveaxis(np.array(out), 0, -1)
+        out = [vel(self.ML_ensemble[0])]
         for l_idx in range(1, self.numLevels):
-            fine = func(state[l_idx][0], axis=0, **kwargs)
-            coarse = func(state[l_idx][1], axis=0, **kwargs)
-            ry = fine.shape[-2] // est.shape[-2]
-            rx = fine.shape[-1] // est.shape[-1]
-            est = np.repeat(np.repeat(est, ry, axis=-2), rx, axis=-1)
-            ry = fine.shape[-2] // coarse.shape[-2]
-            rx = fine.shape[-1] // coarse.shape[-1]
-            est = est + fine - np.repeat(np.repeat(coarse, ry, axis=-2), rx, axis=-1)
+            out.append([vel(self.ML_ensemble[l_idx][0]), vel(self.ML_ensemble[l_idx][1])])
+        return out
+
+    def upload(self, ML_state):
+        """Interior states back into every member (E/MultiLevelOceanEnsemble.py:227-239)."""
+        def put(sims, st):
+            for e, s in enumerate(sims):
+                s.upload(*np.pad(st[:, :, :, e], ((0, 0), (2, 2), (2, 2))))
+        put(self.ML_ensemble[0], ML_state[0])
+        for l_idx in range(1, self.numLevels):
+            put(self.ML_ensemble[l_idx][0], ML_state[l_idx][0])
+            put(self.ML_ensemble[l_idx][1], ML_state[l_idx][1])
+
+    # ------------------------------------------------------------------
+    # estimators (E/MultiLevelOceanEnsemble.py:242-267)
+    # ------------------------------------------------------------------
+    def estimate(self, func, **kwargs):
+        """ML estimator of a statistic of (eta, hu, hv).  np.mean and np.var
+        (with ddof) run on the device: one pass over each level group's
+        members plus one launch assembling the estimate on the finest grid;
+        any other func runs on the downloaded states."""
+        stat = _device_statistic(func, kwargs)
+        if stat is not None:
+            return self._device_estimate("state", *stat)
+        return self._estimate_pure(self.download(), func, **kwargs)
+
+    def estimateVelocity(self, func, **kwargs):
+        """ML estimator of a statistic of (u, v) = (hu, hv) / (eta + Hm)."""
+        stat = _device_statistic(func, kwargs)
+        if stat is not None:
+            return self._device_estimate("velocity", *stat)
+        return self._estimate_pure(self.downloadVelocities(), func, **kwargs)
+
+    def _estimate_pure(self, ML_state, func, **kwargs):
+        """The estimator on downloaded states (E/MultiLevelOceanEnsemble.py:258-267):
+        level-0 statistic plus the fine-coarse differences, on the finest grid."""
+        L = self.numLevels
+        est = np.zeros(ML_state[-1][0].shape[:-1])
+        est += func(ML_state[0], axis=-1, **kwargs).repeat(2 ** (L - 1), 1).repeat(2 ** (L - 1), 2)
+        for l_idx in range(1, L):
+            d = func(ML_state[l_idx][0], axis=-1, **kwargs) - \
+                func(ML_state[l_idx][1], axis=-1, **kwargs).repeat(2, 1).repeat(2, 2)
+            est += d.repeat(2 ** (L - l_idx - 1), 1).repeat(2 ** (L - l_idx - 1), 2)
         return est
+
+    def _device_estimate(self, quantity, which, ddof):
+        eng = self.engine
+        groups = self._groups()
+        bufs = []
+        try:
+            def stat(first, n):
+                m, v = eng.moments(first, n, quantity=quantity, ddof=ddof, mean=which == "mean",
+                                   var=which == "var", download=False)
+                b = m if which == "mean" else v
+                bufs.append(b)
+                return b.ptr
+            L = self.numLevels
+            fine = (ctypes.c_void_p * L)()
+            coarse = (ctypes.c_void_p * L)()
+            fine[0] = stat(*groups[0])
+            for l_idx in range(1, L):
+                fine[l_idx] = stat(*groups[l_idx][0])
+                coarse[l_idx] = stat(*groups[l_idx][1])
+            nx = np.ascontiguousarray(self.nxs, dtype=np.int32)
+            ny = np.ascontiguousarray(self.nys, dtype=np.int32)
+            planes = 3 if quantity == "state" else 2
+            out_shape = (planes, int(ny[-1]), int(nx[-1]))
+            out = Common.DevicePtr(8 * int(np.prod(out_shape)))
+            bufs.append(out)
+            _lib.call("goc_ml_combine", L, fine, coarse, nx.ctypes.data, ny.ctypes.data, planes, out.ptr,
+                      eng.stream.handle)
+            eng.kernels_launched += 1
+            return eng._download(out, out_shape, np.float64)
+        finally:
+            for b in bufs:
+                b.free()
 
     def cleanUp(self):
         self.engine.release()

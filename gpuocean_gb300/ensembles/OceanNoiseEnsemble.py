@@ -12,6 +12,12 @@ import numpy as np
 from ..drifters.GPUDrifterCollection import GPUDrifterCollection
 from ..SWEsimulators import CDKLM16
 from .BatchedEnsemble import BatchedEnsemble
+from .MultiLevelOceanEnsemble import _device_statistic
+
+
+def _desingularise(h, hu, eps):
+    """U/OceanographicUtilities.py:413-414."""
+    return hu / np.maximum(np.minimum(h * h / (2.0 * eps) + 0.5 * eps, eps), np.abs(h))
 
 
 class ObservationType:
@@ -45,6 +51,12 @@ class OceanNoiseEnsemble:
         self.observation_cov_inverse = np.eye(2) * (1.0 / self.observation_variance)
         self.initialization_cov_drifters = np.eye(2) * initialization_variance_factor_drifter_position * self.dx
         self.driftersPerOceanModel = np.int32(num_drifters)
+        self.compensate_for_eta = compensate_for_eta
+        self.base_H = np.asarray(Hi)
+        # mean cell-centre depth (E/OceanNoiseEnsemble.py:152-155)
+        Hm = sim.downloadBathymetry()[1][2:-2, 2:-2]
+        self.mean_depth = np.mean(Hm)
+        self.constant_depth = np.max(Hm) == np.min(Hm)
         me = sim.model_error
         # sim.f is already compensated for the first interior cell; pass it back uncompensated
         f_in = float(sim.f) + float(sim.coriolis_beta) * 2 * float(sim.dy)
@@ -107,6 +119,78 @@ class OceanNoiseEnsemble:
         ix = np.floor(pos[:, 0] / self.dx).astype(int)
         iy = np.floor(pos[:, 1] / self.dy).astype(int)
         return np.stack([pos[:, 0], pos[:, 1], np.asarray(hu)[iy, ix], np.asarray(hv)[iy, ix]], axis=1)
+
+    # ------------------------------------------------------------------
+    # observation operator and statistics (E/BaseOceanStateEnsemble.py:79-176)
+    # ------------------------------------------------------------------
+    def getNumDrifters(self):
+        return int(self.driftersPerOceanModel)
+
+    def observeParticles(self, gpu=False, innovation=False, observations=None):
+        """(hu, hv) of every particle at the observed cells, (particles,
+        drifters, 2), or the innovation against the truth's observation
+        (E/BaseOceanStateEnsemble.py:79-145).  All particles are observed in
+        one launch.  gpu=True observes at the truth's drifters in device
+        memory (the reference's GPU path); otherwise at the cells of
+        observations[:, :2], found in float64 as the reference's CPU path
+        does.  Innovation: obs * (mean_depth + eta) / mean_depth - particle
+        when compensate_for_eta, else obs - particle."""
+        if self.observation_type == ObservationType.DrifterPosition:
+            raise ValueError('Observation type DataAssimilationUtils.ObservationType.DrifterPosition is not supported')
+        n = self.getNumParticles()
+        if gpu:
+            assert not innovation, 'Innovation is not supported when the observations are made on the GPU'
+            obs = self.engine.observe(first=0, count=n, drifters=self.particles[self.obs_index].drifters)
+            out = obs[:, :, 1:].astype(np.float64)
+        else:
+            if observations is None:
+                observations = self.observeTrueState()
+            observations = np.asarray(observations)
+            ix = np.floor(observations[:, 0] / self.dx).astype(np.int64)
+            iy = np.floor(observations[:, 1] / self.dy).astype(np.int64)
+            # the cell centres select exactly the cells found above
+            centres = np.stack([(ix + 0.5) * self.dx, (iy + 0.5) * self.dy], axis=1)
+            obs = self.engine.observe(centres, first=0, count=n)
+            if innovation:
+                md = np.float32(self.mean_depth)
+                comp = ((md + obs[:, :, 0]) / md).astype(np.float64) if self.compensate_for_eta else 1.0
+                out = np.stack([observations[:, 2] * comp - obs[:, :, 1].astype(np.float64),
+                                observations[:, 3] * comp - obs[:, :, 2].astype(np.float64)], axis=2)
+            else:
+                out = obs[:, :, 1:].astype(np.float64)
+        for p in range(n):
+            if not self.particlesActive[p]:
+                out[p] = np.nan
+        return out
+
+    def estimate(self, func, **kwargs):
+        """func over the particles of (eta, hu, hv), shape (3, ny, nx)
+        (E/BaseOceanStateEnsemble.py:147-158).  np.mean and np.var (with
+        ddof) run on the device in one pass; other funcs on the downloads."""
+        stat = _device_statistic(func, kwargs)
+        if stat is not None:
+            m, v = self.engine.moments(0, self.getNumParticles(), "state", ddof=stat[1], mean=stat[0] == "mean",
+                                       var=stat[0] == "var")
+            return m if stat[0] == "mean" else v
+        st = np.moveaxis(np.array([np.array(self.downloadParticleOceanState(e))
+                                   for e in range(self.getNumParticles())]), 0, -1)
+        return func(st, axis=-1, **kwargs)
+
+    def estimateVelocity(self, func, desingularise=0.00001, **kwargs):
+        """func over the particles of the desingularised velocities (u, v),
+        shape (2, ny, nx) (E/BaseOceanStateEnsemble.py:160-176)."""
+        stat = _device_statistic(func, kwargs)
+        if stat is not None:
+            m, v = self.engine.moments(0, self.getNumParticles(), "velocity", desingularise=desingularise,
+                                       ddof=stat[1], mean=stat[0] == "mean", var=stat[0] == "var")
+            return m if stat[0] == "mean" else v
+        _, Hm = self.particles[0].downloadBathymetry(interior_domain_only=True)
+        vel = []
+        for e in range(self.getNumParticles()):
+            eta, hu, hv = self.downloadParticleOceanState(e)
+            h = eta + Hm
+            vel.append(np.array([_desingularise(h, hu, desingularise), _desingularise(h, hv, desingularise)]))
+        return func(np.moveaxis(np.array(vel), 0, -1), axis=-1, **kwargs)
 
     def getDistances(self, obs=None):
         obs = self.observeTrueDrifters() if obs is None else obs

@@ -93,6 +93,12 @@ int goc_stream_synchronize(void* stream);
 int goc_event_create(void** event);
 int goc_event_destroy(void* event);
 int goc_event_record(void* event, void* stream);
+/* Device-side ordering (no host wait): every stream of `waiters` waits for
+ * the work queued so far on `signaller` (fan_out), or `waiter` waits for the
+ * work queued so far on every stream of `signallers` (fan_in).  A batched
+ * ensemble uses them to order its own stream with its members' streams. */
+int goc_stream_fan_out(void* signaller, void* const* waiters, int n_waiters);
+int goc_stream_fan_in(void* waiter, void* const* signallers, int n_signallers);
 int goc_event_elapsed_ms(void* start, void* stop, float* ms);
 int goc_graph_begin_capture(void* stream);
 int goc_graph_end_capture(void* stream, void** graph_exec);
@@ -474,6 +480,75 @@ int goc_noise_batch_destroy(void* batch);
 int goc_noise_batch_seed(void* batch, unsigned long long seed, void* stream);
 int goc_noise_batch_generate(void* batch, void* ensemble, int substep, void* stream);
 int goc_noise_batch_perturb(void* batch, void* ensemble, float perturbation_scale, int substep, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Observation operator and ensemble statistics
+ * ------------------------------------------------------------------------ */
+
+/*
+ * Drop-in for the observeUnderlyingFlow kernel (K/observationKernels.cu:29-83,
+ * launched from E/BaseOceanStateEnsemble.py:117-130 with the prepared format
+ * "iiffiiPiPiPifiPiPi" of E/OceanNoiseEnsemble.py:333-339): for drifter d
+ * at positions + d * positions_pitch (x, y in metres), observations + d *
+ * observation_pitch receives (hu, hv) of the cell
+ * (floor(x / dx) + x_zero_ref, floor(y / dy) + y_zero_ref).  Pitches in
+ * bytes.  eta and H are accepted for signature parity and not read (the
+ * reference reads neither).  Cell indices are clamped to the array (the
+ * reference reads outside it for positions outside the domain).
+ */
+int goc_observe_underlying_flow(int nx, int ny, float dx, float dy, int x_zero_ref, int y_zero_ref,
+                                const float* eta, int eta_pitch, const float* hu, int hu_pitch,
+                                const float* hv, int hv_pitch, float H, int num_drifters,
+                                const float* positions, int positions_pitch, float* observations,
+                                int observation_pitch, void* stream);
+
+/*
+ * The observation operator over members [first_member, first_member +
+ * n_members) of an ensemble in one launch (replaces the per-particle loop
+ * of BaseOceanStateEnsemble.observeParticles, E/BaseOceanStateEnsemble.py:
+ * 79-145).  For member i of the range and position d: out[(i *
+ * num_positions + d) * 3 + {0, 1, 2}] = (eta, hu, hv) of the member's current
+ * state at the cell holding the position (zero reference cell 2, as the
+ * reference's ensembles pass).  Positions are (x, y) rows with a pitch in
+ * bytes; member i reads them at positions + i * positions_member_stride
+ * bytes (0: every member observes the same positions).  Device memory.
+ */
+int goc_ensemble_observe(void* ensemble, int first_member, int n_members, const float* positions,
+                         int positions_pitch, long long positions_member_stride, int num_positions,
+                         float* out, void* stream);
+
+/*
+ * Mean and variance over members [first_member, first_member + n_members)
+ * of an ensemble, per interior cell, in one pass over the members' current
+ * states (replaces the download-and-NumPy loops of estimate /
+ * estimateVelocity, E/BaseOceanStateEnsemble.py:147-176 and
+ * E/MultiLevelOceanEnsemble.py:143-250 with func = np.mean / np.var).
+ * The members must share one grid.  quantity 0: planes (eta, hu, hv);
+ * quantity 1: planes (u, v) = (hu, hv) / h with h = eta + Hm, desingularised
+ * as U/OceanographicUtilities.py:413-414 does when desing_eps > 0 (plain
+ * division otherwise).  mean / var: device arrays of planes x ny x nx
+ * float32 (either may be NULL); var divides by n_members - ddof.  The sums
+ * are shifted by the first member's value.  Large member groups on small
+ * grids are split over slices whose sums go to scratch owned by the library
+ * (grown on demand, which synchronises the stream; not graph-capturable).
+ */
+int goc_ensemble_moments(void* ensemble, int first_member, int n_members, int quantity, float desing_eps,
+                         int ddof, float* mean, float* var, void* stream);
+
+/*
+ * The multi-level estimator of MultiLevelOceanEnsemble._estimate_pure
+ * (E/MultiLevelOceanEnsemble.py:258-267) on the device.  Level l has a
+ * statistic fine[l] on an ny[l] x nx[l] grid (planes x ny x nx float32) and,
+ * for l > 0, the coarse partners' statistic coarse[l] on the grid of level
+ * l - 1; every level is the finest grid coarsened by 2^(top - l).  out
+ * (planes x ny[top] x nx[top] float64) = fine[0] + sum over l > 0 of
+ * (fine[l] - coarse[l]), each held constant over the finest cells it covers;
+ * the differences are formed in float32 and accumulated in float64 in level
+ * order.  fine / coarse / nx / ny are host arrays of n_levels entries
+ * (device pointers); at most 8 levels.
+ */
+int goc_ml_combine(int n_levels, const float* const* fine, const float* const* coarse, const int* nx,
+                   const int* ny, int n_planes, double* out, void* stream);
 
 #ifdef __cplusplus
 }

@@ -110,6 +110,8 @@ REF_CONFIGS = {
     # GPUDrifterCollection with the default 1x1 wind (D/GPUDrifterCollection.py:70-76)
     "drift": ("driftKernels.cu", {"block_width": 64, "block_height": 1, "WIND_X_NX": 1, "WIND_X_NY": 1,
                                   "WIND_Y_NX": 1, "WIND_Y_NY": 1}, []),
+    # OceanNoiseEnsemble's observation kernels, no defines and default options (E/OceanNoiseEnsemble.py:333-339)
+    "observation": ("observationKernels.cu", {}, []),
 }
 
 
@@ -476,6 +478,30 @@ class RefNoise:
 # ---------------------------------------------------------------------------
 # drifters through the reference kernels
 # ---------------------------------------------------------------------------
+
+def ref_observe_underlying_flow(nx, ny, dx, dy, hu, hv, positions, H=60.0):
+    """observeUnderlyingFlow (K/observationKernels.cu:29-83) on (ny+4, nx+4)
+    host arrays, launched as BaseOceanStateEnsemble.observeParticles does
+    (E/BaseOceanStateEnsemble.py:117-130: zero reference cells 2, one block of
+    num_drifters threads, tight (D, 2) float32 output).  Returns (D, 2)."""
+    drv = Driver.get()
+    pos = np.ascontiguousarray(positions, dtype=np.float32)
+    D = pos.shape[0]
+    eta_a = Array2D(drv, np.zeros_like(np.asarray(hu, np.float32)))
+    hu_a, hv_a = Array2D(drv, hu), Array2D(drv, hv)
+    pos_a = Array2D(drv, pos)
+    obs_a = Array2D(drv, np.zeros((D, 2), np.float32))
+    try:
+        k = drv.function("observation", "observeUnderlyingFlow")
+        drv.launch(k, "iiffiiPiPiPifiPiPi", (1, 1), (D, 1, 1), int(nx), int(ny), np.float32(dx), np.float32(dy), 2, 2,
+                   eta_a.ptr, eta_a.pitch, hu_a.ptr, hu_a.pitch, hv_a.ptr, hv_a.pitch, np.float32(H), D,
+                   pos_a.ptr, pos_a.pitch, obs_a.ptr, obs_a.pitch)
+        drv.synchronize()
+        return obs_a.download()
+    finally:
+        for a in (eta_a, hu_a, hv_a, pos_a, obs_a):
+            a.free()
+
 
 class RefDrifters:
     """GPUDrifterCollection (D/GPUDrifterCollection.py:34-253), 1x1 zero wind."""

@@ -19,6 +19,7 @@ import numpy as np
 
 
 def import_reference(root):
+    sys.dont_write_bytecode = True   # the checkout is read-only: no __pycache__ inside it
     for name in ["pycuda", "pycuda.driver", "pycuda.gpuarray", "pycuda.compiler", "pycuda.curandom",
                  "pycuda.autoinit", "matplotlib", "matplotlib.pyplot", "matplotlib.gridspec",
                  "matplotlib.animation", "matplotlib.colors", "netCDF4", "mpi4py"]:
