@@ -33,9 +33,10 @@ NOISE_FACTOR = 8          # coarse grid every 8 cells
 NOISE_L_COARSE = 8.0      # SOAR length scale in coarse cells
 NOISE_STD = 0.003         # target std of the SOAR eta perturbation [m]
 # DRAM bytes (read + write) per member-cell-step of ensemble_rk2_kernel, from
-# one ncu capture of a 96-member C3 launch (460,593,408 B over 96 x 512 x 300
-# member-cell-steps); traffic of a bench launch is scaled by its member-cells.
-NCU_DRAM_BYTES_PER_MEMBER_CELL = 460593408 / (96 * 512 * 300)
+# one ncu capture of a 96-member C3 launch (242.6 MB read + 141.3 MB written
+# over 96 x 512 x 300 member-cell-steps, step built without FMA contraction);
+# traffic of a bench launch is scaled by its member-cells.
+NCU_DRAM_BYTES_PER_MEMBER_CELL = 383.9e6 / (96 * 512 * 300)
 
 
 def soar_q0(L_cells=NOISE_L_COARSE, std=NOISE_STD):
