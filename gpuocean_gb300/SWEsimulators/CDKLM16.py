@@ -293,6 +293,27 @@ class CDKLM16(Simulator):
             use_lcg=use_lcg, xorwow_seed=xorwow_seed,
             block_width=block_width_model_error, block_height=block_height_model_error)
 
+    def setKLModelError(self, kl_decay=1.2, kl_scaling=1.0, include_cos=True, include_sin=True,
+                        basis_x_start=1, basis_y_start=1, basis_x_end=10, basis_y_end=10,
+                        use_lcg=False, xorwow_seed=None, np_seed=None, block_width=16, block_height=16):
+        """Karhunen-Loeve model error (S/CDKLM16.py:639-651)."""
+        from . import ModelErrorKL
+        self.model_error = ModelErrorKL.ModelErrorKL.fromsim(
+            self, kl_decay=kl_decay, kl_scaling=kl_scaling, include_cos=include_cos, include_sin=include_sin,
+            basis_x_start=basis_x_start, basis_y_start=basis_y_start, basis_x_end=basis_x_end,
+            basis_y_end=basis_y_end, use_lcg=use_lcg, xorwow_seed=xorwow_seed, np_seed=np_seed,
+            block_width=block_width, block_height=block_height)
+
+    def setKLModelErrorSimilarAs(self, otherSim):
+        """The KL model error of another simulator's parameters (S/CDKLM16.py:653-660)."""
+        from . import ModelErrorKL
+        me = otherSim.model_error
+        self.model_error = ModelErrorKL.ModelErrorKL.fromsim(
+            self, kl_decay=me.kl_decay, kl_scaling=me.kl_scaling, include_cos=me.include_cos,
+            include_sin=me.include_sin, basis_x_start=me.basis_x_start, basis_y_start=me.basis_y_start,
+            basis_x_end=me.basis_x_end, basis_y_end=me.basis_y_end, use_lcg=me.use_lcg,
+            block_width=me.local_size[0], block_height=me.local_size[1])
+
     def perturbState(self, perturbation_scale=1.0, update_random_field=True, q0_scale=1):
         if q0_scale != 1:
             perturbation_scale = q0_scale

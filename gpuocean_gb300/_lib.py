@@ -105,6 +105,16 @@ SIGNATURES = {
                               c_int, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_float,
                               c_void_p, c_void_p, c_void_p, c_void_p]),
     "goc_drift_enforce_boundary": (c_int, [c_float, c_float, c_int, c_int, c_int, c_void_p, c_int, c_void_p]),
+    "goc_kl_table_floats": (ctypes.c_longlong, [c_int, c_int, c_void_p]),
+    "goc_kl_perturb": (c_int, [c_void_p, c_int, c_int, c_float, c_float, c_float, c_int, c_void_p, c_void_p, c_void_p,
+                               c_int, c_void_p, c_int, c_int, c_int, c_void_p]),
+    "goc_kl_batch_create": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    "goc_kl_batch_destroy": (c_int, [c_void_p]),
+    "goc_kl_batch_seed": (c_int, [c_void_p, ctypes.c_ulonglong, c_void_p]),
+    "goc_kl_batch_generate": (c_int, [c_void_p, c_void_p, c_int, c_void_p]),
+    "goc_kl_batch_set_rollers": (c_int, [c_void_p, c_void_p, c_int, c_void_p]),
+    "goc_kl_batch_set_random": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
+    "goc_kl_batch_perturb": (c_int, [c_void_p, c_void_p, c_float, c_int, c_void_p]),
     "goc_observe_underlying_flow": (c_int, [c_int, c_int, c_float, c_float, c_int, c_int, c_void_p, c_int, c_void_p,
                                             c_int, c_void_p, c_int, c_float, c_int, c_void_p, c_int, c_void_p, c_int,
                                             c_void_p]),

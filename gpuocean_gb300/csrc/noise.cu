@@ -134,7 +134,8 @@ __device__ __forceinline__ void store_cell(const OceanRef& o, int ti, int tj, fl
     }
 }
 
-__device__ __forceinline__ float noise_coriolis(const GocNoiseDesc& d, const OceanRef& o, int ti, int tj) {
+template <class D>
+__device__ __forceinline__ float noise_coriolis(const D& d, const OceanRef& o, int ti, int tj) {
     float c = d.f + d.beta * ((ti + 0.5f) * o.dx * d.north_x + (tj + 0.5f) * o.dy * d.north_y);
     if (d.f == 0.0f && d.coriolis_f) {
         const float s = (ti + 0.5f) / (o.nx + 4.0f), t = (tj + 0.5f) / (o.ny + 4.0f);
@@ -359,6 +360,165 @@ __global__ void xorwow_batched_init_kernel(curandStateXORWOW_t* states, int n, u
     if (i < n) curand_init(seed, (unsigned long long)i, 0ULL, states + i);
 }
 
+// ---------------------------------------------------------------------------
+// Karhunen-Loeve model error (K/ocean_noise.cu:666-954)
+// ---------------------------------------------------------------------------
+//
+// The reference sums 2 Nx Ny terms per cell, each with two powers and two
+// sines or cosines.  The sum separates: with a_n = n^-decay,
+//   d_eta(x, y) = sum_j a_m(j) [ sin(2 pi m y_s) Bs_j(x) + cos(2 pi m y_c) Bc_j(x) ],
+//   Bs_j(x) = sum_i r_sin[j][i] a_n(i) sin(2 pi n x_s)   (Bc likewise),
+// so one launch tabulates Bs, Bc per column and the y factors per row, and
+// the perturbation costs 2 Ny multiply-adds per cell.  Table layout (floats):
+// Bs, Bc: [Ny][nx + 2]; As, Ac: [Ny][ny + 2]; column / row t stands for the
+// full-array cell t + 1 (the interior plus one ghost cell on each side).
+
+struct KLRoll {
+    float xs, ys, xc, yc;
+};
+
+__host__ __device__ __forceinline__ int kl_count_x(const GocKLDesc& d) { return d.basis_x_end - d.basis_x_start + 1; }
+__host__ __device__ __forceinline__ int kl_count_y(const GocKLDesc& d) { return d.basis_y_end - d.basis_y_start + 1; }
+
+__device__ void kl_table_entry(const GocKLDesc& d, KLRoll r, int nx, int ny, int part, int t) {
+    const int NX = kl_count_x(d), NY = kl_count_y(d);
+    const int CX = nx + 2, RY = ny + 2;
+    float* Bs = d.table;
+    float* Bc = Bs + (size_t)NY * CX;
+    float* As = Bc + (size_t)NY * CX;
+    float* Ac = As + (size_t)NY * RY;
+    const float* rns = d.random;
+    const int rp = d.random_pitch / 4;
+    if (part == 0) {
+        if (t >= CX) return;
+        // unit-square coordinate of full-array column t + 1, evaluated in
+        // double as (ti + 0.5 - 2) / nx is in K/ocean_noise.cu:826
+        const float x = (float)((t + 1 + 0.5 - 2) / nx);
+        const float xs = x + r.xs, xc = x + r.xc;
+        for (int j = 0; j < NY; ++j) {
+            float bs = 0.0f, bc = 0.0f;
+            for (int i = 0; i < NX; ++i) {
+                const int n = d.basis_x_start + i;
+                const float an = powf((float)n, -d.kl_decay);
+                bs += rns[(size_t)j * rp + i] * an * sinpif(2 * n * xs);
+                bc += rns[(size_t)(NY + j) * rp + i] * an * cospif(2 * n * xc);
+            }
+            Bs[(size_t)j * CX + t] = d.include_sin ? bs : 0.0f;
+            Bc[(size_t)j * CX + t] = d.include_cos ? bc : 0.0f;
+        }
+    } else {
+        if (t >= RY) return;
+        const float y = (float)((t + 1 + 0.5 - 2) / ny);
+        const float ys = y + r.ys, yc = y + r.yc;
+        for (int j = 0; j < NY; ++j) {
+            const int m = d.basis_y_start + j;
+            const float am = powf((float)m, -d.kl_decay);
+            As[(size_t)j * RY + t] = am * sinpif(2 * m * ys);
+            Ac[(size_t)j * RY + t] = am * cospif(2 * m * yc);
+        }
+    }
+}
+
+constexpr int kKX = 32, kKY = 8;  // KL perturbation tile (interior cells)
+
+// kl_sample_eta / kl_sample_ocean_state on one tile with interior origin
+// (bx, by): d_eta on the tile + 1 ring from the tables, then (unless
+// eta_only) the geostrophically balanced hu, hv of K/ocean_noise.cu:901-947.
+// The reference computes a dry-cell flag there and does not use it: land
+// cells are perturbed as well.
+__device__ void kl_perturb_tile(const GocKLDesc& d, const OceanRef& o, float scale, int eta_only, int bx, int by) {
+    __shared__ float s_d[kKY + 2][kKX + 2];
+    const int NY = kl_count_y(d), CX = o.nx + 2, RY = o.ny + 2;
+    const float* Bs = d.table;
+    const float* Bc = Bs + (size_t)NY * CX;
+    const float* As = Bc + (size_t)NY * CX;
+    const float* Ac = As + (size_t)NY * RY;
+    const float amp = scale * d.kl_scaling;
+    for (int k = threadIdx.y * kKX + threadIdx.x; k < (kKY + 2) * (kKX + 2); k += kKX * kKY) {
+        const int i = k % (kKX + 2), j = k / (kKX + 2);
+        const int cx = bx + i, ry = by + j;   // table column / row of full-array cell (1 + bx + i, 1 + by + j)
+        float v = 0.0f;
+        if (cx < CX && ry < RY) {
+            for (int q = 0; q < NY; ++q)
+                v += As[(size_t)q * RY + ry] * Bs[(size_t)q * CX + cx] + Ac[(size_t)q * RY + ry] * Bc[(size_t)q * CX + cx];
+            v *= amp;
+        }
+        s_d[j][i] = v;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int ti = 2 + bx + tx, tj = 2 + by + ty;
+    if (ti < o.nx + 2 && tj < o.ny + 2) {
+        const float de = s_d[ty + 1][tx + 1];
+        const size_t k = (size_t)tj * o.pitch + ti;
+        if (eta_only) {
+            o.eta[k] += de;
+        } else {
+            const float* h0 = o.Hi + (size_t)tj * o.hi_pitch + ti;
+            const float* h1 = h0 + o.hi_pitch;
+            const float H_mid = 0.25f * (h0[0] + h0[1] + h1[0] + h1[1]);
+            const float cor = noise_coriolis(d, o, ti, tj);
+            const float ex = (s_d[ty + 1][tx + 2] - s_d[ty + 1][tx]) / (2.0f * o.dx);
+            const float ey = (s_d[ty + 2][tx + 1] - s_d[ty][tx + 1]) / (2.0f * o.dy);
+            const float dhu = -(d.g / cor) * (H_mid + de) * ey;
+            const float dhv = (d.g / cor) * (H_mid + de) * ex;
+            store_cell(o, ti, tj, o.eta[k] + de, o.hu[k] + dhu, o.hv[k] + dhv);
+        }
+    }
+    __syncthreads();
+}
+
+__global__ void kl_table_kernel(GocKLDesc d, int nx, int ny) {
+    kl_table_entry(d, KLRoll{d.roll_x_sin, d.roll_y_sin, d.roll_x_cos, d.roll_y_cos}, nx, ny, blockIdx.y,
+                   blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void kl_perturb_kernel(GocKLDesc d, OceanRef o, float scale, int eta_only) {
+    kl_perturb_tile(d, o, scale, eta_only, blockIdx.x * kKX, blockIdx.y * kKY);
+}
+
+// batched: member m uses the normals and rollers of member src[m]
+__global__ void kl_table_batched_kernel(const GocKLDesc* __restrict__ kl, const int* __restrict__ src,
+                                        const float4* __restrict__ rollers, int n, int roll_set,
+                                        const GocMemberDesc* __restrict__ mem, const int4* __restrict__ items,
+                                        const int* __restrict__ nsub, int substep) {
+    const int4 it = items[blockIdx.x];   // (member, part, first entry, 0)
+    int set;
+    if (!member_set(nsub, it.x, substep, &set)) return;
+    const float4 r = rollers[(size_t)roll_set * n + src[it.x]];
+    kl_table_entry(kl[it.x], KLRoll{r.x, r.y, r.z, r.w}, mem[it.x].p.nx, mem[it.x].p.ny, it.y, it.z + threadIdx.x);
+}
+
+__global__ void kl_perturb_batched_kernel(const GocKLDesc* __restrict__ kl, const GocMemberDesc* __restrict__ mem,
+                                          const int4* __restrict__ items, const int* __restrict__ nsub, int substep,
+                                          float scale) {
+    const int4 it = items[blockIdx.x];   // (member, tile x, tile y, 0)
+    int set;
+    if (!member_set(nsub, it.x, substep, &set)) return;
+    const GocMemberDesc& m = mem[it.x];
+    const OceanRef o{m.p.nx, m.p.ny, m.p.dx, m.p.dy, m.eta[set], m.hu[set], m.hv[set], m.pitch / 4, m.Hi,
+                     m.Hi_pitch / 4, m.p.land_value, m.p.bc_north == 2, m.p.bc_east == 2};
+    kl_perturb_tile(kl[it.x], o, scale, 0, it.y * kKX, it.z * kKY);
+}
+
+// XORWOW normals into the source members' fields; chunk = (member, first
+// element, count, first state)
+__global__ void kl_xorwow_batched_kernel(const GocKLDesc* __restrict__ kl, const int4* __restrict__ chunks,
+                                         curandStateXORWOW_t* states, const int* __restrict__ nsub, int substep) {
+    const int4 c = chunks[blockIdx.x];
+    int set;
+    if (!member_set(nsub, c.x, substep, &set)) return;
+    const GocKLDesc& d = kl[c.x];
+    const int NX = kl_count_x(d);
+    float* rnd = const_cast<float*>(d.random);
+    for (int q = threadIdx.x; q < c.z; q += blockDim.x) {
+        const int e = c.y + q;
+        curandStateXORWOW_t st = states[c.w + q];
+        rnd[(size_t)(e / NX) * (d.random_pitch / 4) + e % NX] = curand_normal(&st);
+        states[c.w + q] = st;
+    }
+}
+
 }  // namespace goc
 
 using namespace goc;
@@ -559,4 +719,230 @@ extern "C" int goc_noise_batch_perturb(void* batch, void* ensemble, float pertur
                                                                   b->d_pert_items, nsub, substep);
     count_launch();
     return check_launch("perturb_batched_kernel");
+}
+
+// ---------------------------------------------------------------------------
+// Karhunen-Loeve model error: entry points
+// ---------------------------------------------------------------------------
+
+static int cuda_rc(cudaError_t e, const char* what) {
+    return e == cudaSuccess ? GOC_OK : set_error(GOC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+static int check_kl(const GocKLDesc* d, int nx, int ny, const char* who) {
+    if (!d) return set_error(GOC_ERR_ARG, "%s: null descriptor", who);
+    if (nx < 1 || ny < 1) return set_error(GOC_ERR_ARG, "%s: bad grid", who);
+    if (d->basis_x_start < 0 || d->basis_y_start < 0 || kl_count_x(*d) < 1 || kl_count_y(*d) < 1)
+        return set_error(GOC_ERR_ARG, "%s: bad basis ranges", who);
+    if (kl_count_x(*d) * kl_count_y(*d) > 1 << 20) return set_error(GOC_ERR_ARG, "%s: too many basis functions", who);
+    return GOC_OK;
+}
+
+extern "C" long long goc_kl_table_floats(int nx, int ny, const GocKLDesc* kl) {
+    if (check_kl(kl, nx, ny, "goc_kl_table_floats")) return GOC_ERR_ARG;
+    return 2LL * kl_count_y(*kl) * ((long long)(nx + 2) + (ny + 2));
+}
+
+extern "C" int goc_kl_perturb(const GocKLDesc* kl, int nx, int ny, float dx, float dy, float perturbation_scale,
+                              int eta_only, float* eta, float* hu, float* hv, int pitch, const float* Hi, int Hi_pitch,
+                              int periodic_ns, int periodic_ew, void* stream) {
+    int rc = check_kl(kl, nx, ny, "goc_kl_perturb");
+    if (rc) return rc;
+    if (!kl->table || !kl->random || kl->random_pitch < 4 * kl_count_x(*kl) || kl->random_pitch % 4)
+        return set_error(GOC_ERR_ARG, "goc_kl_perturb: table or random field missing");
+    if (!eta_only && !kl->coriolis_f && kl->f == 0.0f)
+        return set_error(GOC_ERR_ARG, "goc_kl_perturb: f = 0 needs the Coriolis texture");
+    OceanRef o;
+    if (eta_only) {
+        if (!eta || pitch < (nx + 4) * 4 || pitch % 4) return set_error(GOC_ERR_ARG, "goc_kl_perturb: bad eta");
+        o = OceanRef{nx, ny, dx, dy, eta, nullptr, nullptr, pitch / 4, nullptr, 0, 0.0f, 0, 0};
+    } else if ((rc = make_ocean(nx, ny, dx, dy, eta, hu, hv, pitch, Hi, Hi_pitch, 0.0f, periodic_ns, periodic_ew, &o,
+                                "goc_kl_perturb"))) {
+        return rc;
+    }
+    cudaStream_t st = as_stream(stream);
+    const int ntab = std::max(nx, ny) + 2;
+    kl_table_kernel<<<dim3((ntab + 127) / 128, 2), 128, 0, st>>>(*kl, nx, ny);
+    count_launch();
+    if ((rc = check_launch("kl_table_kernel"))) return rc;
+    dim3 grd((nx + kKX - 1) / kKX, (ny + kKY - 1) / kKY);
+    kl_perturb_kernel<<<grd, dim3(kKX, kKY), 0, st>>>(*kl, o, perturbation_scale, eta_only);
+    count_launch();
+    return check_launch("kl_perturb_kernel");
+}
+
+struct KLBatch {
+    int n = 0, max_sets = 0;
+    GocKLDesc* d_kl = nullptr;
+    int* d_src = nullptr;
+    float4* d_rollers = nullptr;
+    float* d_arena = nullptr;                   // tables and random fields
+    int4* d_tab_items = nullptr;
+    int4* d_tile_items = nullptr;
+    int4* d_rng_chunks = nullptr;
+    curandStateXORWOW_t* d_states = nullptr;
+    int n_tab = 0, n_tile = 0, n_rng = 0, n_states = 0;
+    std::vector<GocKLDesc> host;
+    std::vector<int> src;
+};
+
+static void kl_batch_free(KLBatch* b) {
+    cudaFree(b->d_kl); cudaFree(b->d_src); cudaFree(b->d_rollers); cudaFree(b->d_arena);
+    cudaFree(b->d_tab_items); cudaFree(b->d_tile_items); cudaFree(b->d_rng_chunks); cudaFree(b->d_states);
+    delete b;
+}
+
+extern "C" int goc_kl_batch_create(void* ensemble, const GocKLDesc* kl, const int* source, int max_sets, void** out) {
+    if (!out || !kl || !source || !ensemble || max_sets < 1)
+        return set_error(GOC_ERR_ARG, "goc_kl_batch_create: bad arguments");
+    *out = nullptr;
+    int n = 0;
+    const GocMemberDesc* members = ensemble_host_members(ensemble, &n);
+    for (int m = 0; m < n; ++m) {
+        const GocKLDesc& d = kl[m];
+        int rc = check_kl(&d, members[m].p.nx, members[m].p.ny, "goc_kl_batch_create");
+        if (rc) return rc;
+        const int s = source[m];
+        if (s < 0 || s >= n || source[s] != s)
+            return set_error(GOC_ERR_ARG, "goc_kl_batch_create: member %d: source %d is not its own source", m, s);
+        if (kl_count_x(kl[s]) != kl_count_x(d) || kl_count_y(kl[s]) != kl_count_y(d))
+            return set_error(GOC_ERR_ARG, "goc_kl_batch_create: member %d and its source differ in basis size", m);
+        if (d.f == 0.0f && !d.coriolis_f)
+            return set_error(GOC_ERR_ARG, "goc_kl_batch_create: member %d: f = 0 needs the Coriolis texture", m);
+    }
+    KLBatch* b = new KLBatch();
+    b->n = n;
+    b->max_sets = max_sets;
+    b->host.assign(kl, kl + n);
+    b->src.assign(source, source + n);
+    // arena: every member's tables, then the source members' random fields
+    std::vector<size_t> tab_off(n), rnd_off(n, 0);
+    size_t off = 0;
+    for (int m = 0; m < n; ++m) {
+        tab_off[m] = off;
+        off += (size_t)goc_kl_table_floats(members[m].p.nx, members[m].p.ny, &kl[m]);
+        off = (off + 31) & ~(size_t)31;
+    }
+    std::vector<int4> tab, tile, rng;
+    int states = 0;
+    for (int m = 0; m < n; ++m) {
+        if (source[m] == m) {
+            rnd_off[m] = off;
+            const int cnt = 2 * kl_count_y(kl[m]) * kl_count_x(kl[m]);
+            off += ((size_t)cnt + 31) & ~(size_t)31;
+            for (int f = 0; f < cnt; f += 256) {
+                const int c = std::min(256, cnt - f);
+                rng.push_back(make_int4(m, f, c, states));
+                states += c;
+            }
+        }
+        const int nx = members[m].p.nx, ny = members[m].p.ny;
+        for (int t = 0; t < nx + 2; t += 128) tab.push_back(make_int4(m, 0, t, 0));
+        for (int t = 0; t < ny + 2; t += 128) tab.push_back(make_int4(m, 1, t, 0));
+        for (int j = 0; j < (ny + kKY - 1) / kKY; ++j)
+            for (int i = 0; i < (nx + kKX - 1) / kKX; ++i) tile.push_back(make_int4(m, i, j, 0));
+    }
+    b->n_tab = (int)tab.size();
+    b->n_tile = (int)tile.size();
+    b->n_rng = (int)rng.size();
+    b->n_states = states;
+    cudaError_t e = cudaMalloc(&b->d_arena, off * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(b->d_arena, 0, off * sizeof(float));
+    for (int m = 0; m < n; ++m) {
+        b->host[m].table = b->d_arena + tab_off[m];
+        b->host[m].random = b->d_arena + rnd_off[source[m]];
+        b->host[m].random_pitch = 4 * kl_count_x(kl[m]);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_kl, sizeof(GocKLDesc) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_src, sizeof(int) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_rollers, sizeof(float4) * (size_t)n * max_sets);
+    if (e == cudaSuccess) e = cudaMemset(b->d_rollers, 0, sizeof(float4) * (size_t)n * max_sets);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_tab_items, sizeof(int4) * tab.size());
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_tile_items, sizeof(int4) * tile.size());
+    if (e == cudaSuccess && !rng.empty()) e = cudaMalloc(&b->d_rng_chunks, sizeof(int4) * rng.size());
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_kl, b->host.data(), sizeof(GocKLDesc) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_src, source, sizeof(int) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_tab_items, tab.data(), sizeof(int4) * tab.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_tile_items, tile.data(), sizeof(int4) * tile.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !rng.empty())
+        e = cudaMemcpy(b->d_rng_chunks, rng.data(), sizeof(int4) * rng.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        kl_batch_free(b);
+        return set_error(GOC_ERR_CUDA, "goc_kl_batch_create: %s", cudaGetErrorString(e));
+    }
+    *out = b;
+    return GOC_OK;
+}
+
+extern "C" int goc_kl_batch_destroy(void* batch) {
+    if (batch) kl_batch_free(static_cast<KLBatch*>(batch));
+    return GOC_OK;
+}
+
+extern "C" int goc_kl_batch_seed(void* batch, unsigned long long seed, void* stream) {
+    if (!batch) return set_error(GOC_ERR_ARG, "goc_kl_batch_seed: null handle");
+    KLBatch* b = static_cast<KLBatch*>(batch);
+    if (b->n_states == 0) return GOC_OK;
+    if (!b->d_states) {
+        cudaError_t e = cudaMalloc(&b->d_states, sizeof(curandStateXORWOW_t) * (size_t)b->n_states);
+        if (e != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_kl_batch_seed: %s", cudaGetErrorString(e));
+    }
+    xorwow_batched_init_kernel<<<(b->n_states + 127) / 128, 128, 0, as_stream(stream)>>>(b->d_states, b->n_states, seed);
+    count_launch();
+    return check_launch("xorwow_batched_init_kernel");
+}
+
+extern "C" int goc_kl_batch_generate(void* batch, void* ensemble, int substep, void* stream) {
+    if (!batch || !ensemble) return set_error(GOC_ERR_ARG, "goc_kl_batch_generate: null handle");
+    KLBatch* b = static_cast<KLBatch*>(batch);
+    if (!b->d_states) return set_error(GOC_ERR_ARG, "goc_kl_batch_generate: call goc_kl_batch_seed first");
+    if (b->n_rng == 0) return GOC_OK;
+    kl_xorwow_batched_kernel<<<b->n_rng, 256, 0, as_stream(stream)>>>(b->d_kl, b->d_rng_chunks, b->d_states,
+                                                                     ensemble_device_nsub(ensemble), substep);
+    count_launch();
+    return check_launch("kl_xorwow_batched_kernel");
+}
+
+extern "C" int goc_kl_batch_set_rollers(void* batch, const float* rollers, int n_sets, void* stream) {
+    if (!batch || !rollers) return set_error(GOC_ERR_ARG, "goc_kl_batch_set_rollers: null argument");
+    KLBatch* b = static_cast<KLBatch*>(batch);
+    if (n_sets < 1 || n_sets > b->max_sets)
+        return set_error(GOC_ERR_ARG, "goc_kl_batch_set_rollers: %d sets, room for %d", n_sets, b->max_sets);
+    return cuda_rc(cudaMemcpyAsync(b->d_rollers, rollers, sizeof(float4) * (size_t)b->n * n_sets,
+                                   cudaMemcpyHostToDevice, as_stream(stream)),
+                   "goc_kl_batch_set_rollers");
+}
+
+extern "C" int goc_kl_batch_set_random(void* batch, int member, const float* host_normals, void* stream) {
+    if (!batch || !host_normals) return set_error(GOC_ERR_ARG, "goc_kl_batch_set_random: null argument");
+    KLBatch* b = static_cast<KLBatch*>(batch);
+    if (member < 0 || member >= b->n) return set_error(GOC_ERR_ARG, "goc_kl_batch_set_random: bad member");
+    const GocKLDesc& d = b->host[b->src[member]];
+    const size_t bytes = sizeof(float) * 2 * kl_count_y(d) * kl_count_x(d);
+    return cuda_rc(cudaMemcpyAsync(const_cast<float*>(d.random), host_normals, bytes, cudaMemcpyHostToDevice,
+                                   as_stream(stream)),
+                   "goc_kl_batch_set_random");
+}
+
+extern "C" int goc_kl_batch_perturb(void* batch, void* ensemble, float perturbation_scale, int substep, void* stream) {
+    if (!batch || !ensemble) return set_error(GOC_ERR_ARG, "goc_kl_batch_perturb: null handle");
+    KLBatch* b = static_cast<KLBatch*>(batch);
+    int n = 0;
+    ensemble_host_members(ensemble, &n);
+    if (n != b->n) return set_error(GOC_ERR_ARG, "goc_kl_batch_perturb: ensemble has %d members, batch %d", n, b->n);
+    if (substep + 1 < 0 || substep + 1 >= b->max_sets)
+        return set_error(GOC_ERR_ARG, "goc_kl_batch_perturb: substep %d outside the roller sets", substep);
+    cudaStream_t st = as_stream(stream);
+    const int* nsub = ensemble_device_nsub(ensemble);
+    const GocMemberDesc* dm = ensemble_device_members(ensemble);
+    kl_table_batched_kernel<<<b->n_tab, 128, 0, st>>>(b->d_kl, b->d_src, b->d_rollers, b->n, substep + 1, dm,
+                                                      b->d_tab_items, nsub, substep);
+    count_launch();
+    int rc = check_launch("kl_table_batched_kernel");
+    if (rc) return rc;
+    kl_perturb_batched_kernel<<<b->n_tile, dim3(kKX, kKY), 0, st>>>(b->d_kl, dm, b->d_tile_items, nsub, substep,
+                                                                    perturbation_scale);
+    count_launch();
+    return check_launch("kl_perturb_batched_kernel");
 }

@@ -67,7 +67,9 @@ class BatchedEnsemble:
         self._graphs = {}
         self._handle = None
         self._noise = None
+        self._noise_kind = None
         self._noises = None
+        self._noise_sources = None
         self._rng_seed = None
         self._bathy_owner = list(range(len(sims)))
         self._shape_index = 0
@@ -125,7 +127,11 @@ class BatchedEnsemble:
         self._attach_drifters()
         self._collect_streams()
         if getattr(self, "_noises", None) is not None:
-            self.set_noise(self._noises, getattr(self, "_random_pool", None))
+            # a rebuilt handle gets new generator states: continue from a new seed
+            self._reseeds = getattr(self, "_reseeds", 0) + 1
+            seed = None if self._rng_seed is None else self._rng_seed + 7919 * self._reseeds
+            self.set_noise(self._noises, getattr(self, "_random_pool", None), rng_seed=seed,
+                           sources=self._noise_sources)
 
     def _collect_streams(self):
         """The members' own streams (simulator, drifters, model error): the
@@ -290,49 +296,107 @@ class BatchedEnsemble:
         return scheds, table, n, nsub
 
     # ------------------------------------------------------------------
-    def set_noise(self, noises, random_pool=None, rng_seed=None):
+    def set_noise(self, noises, random_pool=None, rng_seed=None, sources=None):
         """Model error of every member in two launches per perturbation.
 
-        noises: one OceanStateNoise per member.  random_pool: optional device
-        array holding every member's random field back to back (one upload
-        refreshes them all); by default each member's own buffer is used.
-        rng_seed: draw fresh XORWOW normals on the device before every
-        perturbation (otherwise the random fields are used as they are, e.g.
-        injected from the host).
+        noises: one OceanStateNoise (SOAR) or one ModelErrorKL per member.
+        random_pool (SOAR): optional device array holding every member's
+        random field back to back (one upload refreshes them all); by default
+        each member's own buffer is used.  rng_seed: draw fresh XORWOW normals
+        on the device before every perturbation (otherwise the random fields
+        are used as they are, e.g. injected from the host).  sources (KL):
+        sources[m] is the member whose normals and rollers member m uses -
+        the coarse partner of a multi-level pair perturbed "similar as" its
+        fine partner (S/CDKLM16.py:782-790); by default every member its own.
         """
-        from ..SWEsimulators.OceanStateNoise import GocNoiseDesc
+        from ..SWEsimulators.ModelErrorKL import GocKLDesc, ModelErrorKL
         assert len(noises) == len(self.sims)
-        descs = (GocNoiseDesc * len(self.sims))()
-        off = 0
-        for m, (n, s) in enumerate(zip(noises, self.sims)):
-            d = n.descriptor(s.f, s.coriolis_beta, s.g)
-            if random_pool is not None:
-                d.random = random_pool.ptr + off
-                off += int(n.rand_ny) * int(n.random_numbers.pitch)
-            descs[m] = d
-        if random_pool is not None:
-            assert off <= random_pool.nbytes, "random pool too small"
-        self._random_pool = random_pool
         self.release_noise()
-        h = ctypes.c_void_p()
-        _lib.call("goc_noise_batch_create", self._handle, descs, ctypes.byref(h))
-        self._noise = h.value
-        self._noise_descs = descs
+        if all(isinstance(n, ModelErrorKL) for n in noises):
+            src = np.arange(len(self.sims), dtype=np.int32) if sources is None else \
+                np.ascontiguousarray(sources, dtype=np.int32)
+            descs = (GocKLDesc * len(self.sims))(*[n.batch_descriptor(s) for n, s in zip(noises, self.sims)])
+            h = ctypes.c_void_p()
+            _lib.call("goc_kl_batch_create", self._handle, descs, src.ctypes.data, int(self.max_substeps) + 1,
+                      ctypes.byref(h))
+            self._noise, self._noise_kind = h.value, "kl"
+            self._noise_sources = src
+            self._kl_rollers = np.zeros((int(self.max_substeps) + 1, len(self.sims), 4), dtype=np.float32)
+            if rng_seed is not None:
+                _lib.call("goc_kl_batch_seed", self._noise, ctypes.c_ulonglong(int(rng_seed)), self.stream.handle)
+            else:
+                # the members' own current normals
+                for m, n in enumerate(noises):
+                    if src[m] == m:
+                        rn = np.ascontiguousarray(n.getRandomNumbers(), dtype=np.float32)
+                        _lib.call("goc_kl_batch_set_random", self._noise, m, rn.ctypes.data, self.stream.handle)
+                self.stream.synchronize()
+        else:
+            from ..SWEsimulators.OceanStateNoise import GocNoiseDesc
+            descs = (GocNoiseDesc * len(self.sims))()
+            off = 0
+            for m, (n, s) in enumerate(zip(noises, self.sims)):
+                d = n.descriptor(s.f, s.coriolis_beta, s.g)
+                if random_pool is not None:
+                    d.random = random_pool.ptr + off
+                    off += int(n.rand_ny) * int(n.random_numbers.pitch)
+                descs[m] = d
+            if random_pool is not None:
+                assert off <= random_pool.nbytes, "random pool too small"
+            self._random_pool = random_pool
+            h = ctypes.c_void_p()
+            _lib.call("goc_noise_batch_create", self._handle, descs, ctypes.byref(h))
+            self._noise, self._noise_kind = h.value, "soar"
+            self._noise_descs = descs
+            if rng_seed is not None:
+                _lib.call("goc_noise_batch_seed", self._noise, ctypes.c_ulonglong(int(rng_seed)), self.stream.handle)
         self._noises = noises
-        self._collect_streams()
         self._rng_seed = rng_seed
-        if rng_seed is not None:
-            _lib.call("goc_noise_batch_seed", self._noise, ctypes.c_ulonglong(int(rng_seed)), self.stream.handle)
+        self._collect_streams()
         for g in self._graphs.values():
             _lib.load().goc_graph_destroy(g[0])
         self._graphs = {}
 
+    def set_kl_random(self, member, normals):
+        """Inject the (2 Ny, Nx) normals that member `member` (and every
+        member whose source it is) uses at the next perturbations."""
+        assert self._noise_kind == "kl"
+        rn = np.ascontiguousarray(normals, dtype=np.float32)
+        _lib.call("goc_kl_batch_set_random", self._noise, int(member), rn.ctypes.data, self.stream.handle)
+        self.stream.synchronize()
+
+    def _kl_draw_rollers(self, sets):
+        """Rollers of the coming perturbations: for every roller set k and
+        every source member that perturbs there, four uniforms from its
+        model error's generator in the order x_sin, y_sin, x_cos, y_cos, as
+        each perturbSim call of the reference draws them
+        (S/ModelErrorKL.py:277-300).  sets: list of (set index, members)."""
+        r = self._kl_rollers
+        for k, members in sets:
+            for m in members:
+                if self._noise_sources[m] != m:
+                    continue
+                me = self._noises[m]
+                me._setRollers(None, None, None, None)
+                r[k, m] = (me.roll_x_sin, me.roll_y_sin, me.roll_x_cos, me.roll_y_cos)
+        n_sets = max(k for k, _ in sets) + 1
+        _lib.call("goc_kl_batch_set_rollers", self._noise, r.ctypes.data, int(n_sets), self.stream.handle)
+
     def release_noise(self):
         if getattr(self, "_noise", None):
-            _lib.load().goc_noise_batch_destroy(self._noise)
+            if self._noise_kind == "kl":
+                _lib.load().goc_kl_batch_destroy(self._noise)
+            else:
+                _lib.load().goc_noise_batch_destroy(self._noise)
             self._noise = None
 
     def _noise_launch(self, substep, scale=1.0, update_random_field=True):
+        if self._noise_kind == "kl":
+            if update_random_field and self._rng_seed is not None:
+                _lib.call("goc_kl_batch_generate", self._noise, self._handle, int(substep), self.stream.handle)
+            _lib.call("goc_kl_batch_perturb", self._noise, self._handle, ctypes.c_float(scale), int(substep),
+                      self.stream.handle)
+            return
         if update_random_field and self._rng_seed is not None:
             _lib.call("goc_noise_batch_generate", self._noise, self._handle, int(substep), self.stream.handle)
         _lib.call("goc_noise_batch_perturb", self._noise, self._handle, ctypes.c_float(scale), int(substep),
@@ -342,6 +406,8 @@ class BatchedEnsemble:
         """Add the SOAR model error to every member's current state."""
         before = _lib.load().goc_kernel_launch_count()
         self._after_members()
+        if self._noise_kind == "kl":
+            self._kl_draw_rollers([(0, range(len(self.sims)))])
         self._noise_launch(-1, perturbation_scale, update_random_field)
         self._before_members()
         self.kernels_launched += _lib.load().goc_kernel_launch_count() - before
@@ -373,6 +439,12 @@ class BatchedEnsemble:
                 s.bc_kernel.boundaryCondition(s.gpu_stream, s.gpu_data.h0, s.gpu_data.hu0, s.gpu_data.hv0)
         scheds, table, n, nsub = self._schedule(t_end)
         self._after_members()
+        if with_noise is not None and self._noise_kind == "kl":
+            if with_noise == "block":
+                self._kl_draw_rollers([(0, range(len(self.sims)))])
+            else:
+                self._kl_draw_rollers([(k + 1, [m for m in range(len(self.sims)) if n[m] > k])
+                                       for k in range(nsub)])
         key = (n.tobytes(), table.tobytes())
         if key != getattr(self, "_sched_key", None):
             _lib.call("goc_ensemble_set_schedule", self._handle, table.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),

@@ -47,7 +47,17 @@ class MultiLevelOceanEnsemble:
         self.members = self._flat()
         self.engine = BatchedEnsemble(self.members)
         if all(s.model_error is not None for s in self.members):
-            self.engine.set_noise([s.model_error for s in self.members], rng_seed=rng_seed)
+            from ..SWEsimulators.ModelErrorKL import ModelErrorKL
+            sources = None
+            if all(isinstance(s.model_error, ModelErrorKL) for s in self.members):
+                # a coarse partner is perturbed with its fine partner's normals
+                # and rollers (perturbSimilarAs in dataAssimilationStep,
+                # S/CDKLM16.py:782-790): the KL basis lives on the unit square,
+                # so both see the same field at their own resolution
+                sources = np.arange(len(self.members), dtype=np.int32)
+                for l_idx, ((fa, n), (ca, _)) in enumerate(self._groups()[1:], start=1):
+                    sources[ca:ca + n] = np.arange(fa, fa + n)
+            self.engine.set_noise([s.model_error for s in self.members], rng_seed=rng_seed, sources=sources)
 
     def _flat(self):
         out = list(self.ML_ensemble[0])

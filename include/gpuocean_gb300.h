@@ -482,6 +482,71 @@ int goc_noise_batch_generate(void* batch, void* ensemble, int substep, void* str
 int goc_noise_batch_perturb(void* batch, void* ensemble, float perturbation_scale, int substep, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Karhunen-Loeve model error (S/ModelErrorKL.py:38-463, K/ocean_noise.cu:666-954)
+ * ------------------------------------------------------------------------ */
+
+/*
+ * One KL model error: d_eta(x, y) = scale * kl_scaling * sum over basis rows
+ * j (m = basis_y_start + j) and columns i (n = basis_x_start + i) of
+ * m^-kl_decay n^-kl_decay (r_sin[j][i] sin(2 pi m y_s) sin(2 pi n x_s) +
+ * r_cos[j][i] cos(2 pi m y_c) cos(2 pi n x_c)) on the unit square, with
+ * x_s = x + roll_x_sin etc.; random holds the (2 Ny) x Nx normals (sine rows
+ * first), pitch in bytes.  The sum is separable: per column a table of the
+ * x sums, per row the y factors, so a cell costs 2 Ny multiply-adds instead
+ * of 4 Nx Ny transcendental terms.  table: device scratch of
+ * goc_kl_table_floats(nx, ny, kl) floats.  f, beta, g, north and the
+ * Coriolis texture as for the SOAR noise.
+ */
+typedef struct GocKLDesc {
+    int32_t basis_x_start, basis_x_end, basis_y_start, basis_y_end;
+    int32_t include_cos, include_sin;
+    float kl_decay, kl_scaling;
+    float roll_x_sin, roll_y_sin, roll_x_cos, roll_y_cos;
+    const float* random; int32_t random_pitch;
+    float f, beta, g;
+    float north_x, north_y;
+    const float* coriolis_f; int32_t coriolis_nx, coriolis_ny;
+    float* table;
+} GocKLDesc;
+
+/* Scratch size (floats) of the basis tables for an nx x ny grid; < 0 on bad
+ * arguments. */
+long long goc_kl_table_floats(int nx, int ny, const GocKLDesc* kl);
+
+/*
+ * kl_sample_eta (eta_only = 1) or kl_sample_ocean_state (eta_only = 0,
+ * with the geostrophically balanced hu, hv of K/ocean_noise.cu:901-947):
+ * adds the KL perturbation times perturbation_scale to the interior of the
+ * (ny+4) x (nx+4) state.  With periodic_ns / periodic_ew the periodic ghost
+ * images of the perturbed cells are written as well (the boundary fill the
+ * reference runs after perturbState in CDKLM16.step).  Two launches: the
+ * basis tables, then the perturbation.
+ */
+int goc_kl_perturb(const GocKLDesc* kl, int nx, int ny, float dx, float dy, float perturbation_scale,
+                   int eta_only, float* eta, float* hu, float* hv, int pitch, const float* Hi, int Hi_pitch,
+                   int periodic_ns, int periodic_ew, void* stream);
+
+/*
+ * KL model error of every member of an ensemble.  kl[m] configures member m
+ * (its table and random pointers are ignored: the batch owns both);
+ * source[m] is the member whose normals and rollers member m uses (m itself,
+ * or the fine partner of a multi-level pair, the coupling of
+ * perturbSimilarAs, S/CDKLM16.py:782-790).  goc_kl_batch_seed seeds XORWOW
+ * states for every source member's normals; goc_kl_batch_generate draws new
+ * normals (substep rule of goc_noise_batch_perturb);
+ * goc_kl_batch_set_rollers uploads n_sets x n_members x 4 rollers (host;
+ * set 0 is used with substep -1, set k + 1 with substep k);
+ * goc_kl_batch_set_random copies host normals for member m's source.
+ */
+int goc_kl_batch_create(void* ensemble, const GocKLDesc* kl, const int* source, int max_sets, void** batch);
+int goc_kl_batch_destroy(void* batch);
+int goc_kl_batch_seed(void* batch, unsigned long long seed, void* stream);
+int goc_kl_batch_generate(void* batch, void* ensemble, int substep, void* stream);
+int goc_kl_batch_set_rollers(void* batch, const float* rollers, int n_sets, void* stream);
+int goc_kl_batch_set_random(void* batch, int member, const float* host_normals, void* stream);
+int goc_kl_batch_perturb(void* batch, void* ensemble, float perturbation_scale, int substep, void* stream);
+
+/* ------------------------------------------------------------------------
  * Observation operator and ensemble statistics
  * ------------------------------------------------------------------------ */
 

@@ -68,9 +68,10 @@ def cdklm_defines(nx, ny, dx, dy, g=9.81, r=0.0, theta=1.8, rk_order=2, coriolis
             "USE_DIRECT_LOOKUP": "False"}
 
 
-def noise_defines(coriolis_shape=(1, 1), angle_shape=(1, 1), block=(16, 16)):
-    """S/OceanStateNoise.py:206-213."""
-    return {"block_width": block[0], "block_height": block[1], "kl_rand_nx": 1, "kl_rand_ny": 1,
+def noise_defines(coriolis_shape=(1, 1), angle_shape=(1, 1), block=(16, 16), kl_rand=(1, 1)):
+    """S/OceanStateNoise.py:206-213; for the KL model error kl_rand = (rand_nx,
+    rand_ny) = (Nx, 2 Ny) as S/ModelErrorKL.py:179-187 passes them."""
+    return {"block_width": block[0], "block_height": block[1], "kl_rand_nx": kl_rand[0], "kl_rand_ny": kl_rand[1],
             "CORIOLIS_F_NX": int(coriolis_shape[1]), "CORIOLIS_F_NY": int(coriolis_shape[0]),
             "ANGLE_NX": int(angle_shape[1]), "ANGLE_NY": int(angle_shape[0])}
 
@@ -110,6 +111,9 @@ REF_CONFIGS = {
     # GPUDrifterCollection with the default 1x1 wind (D/GPUDrifterCollection.py:70-76)
     "drift": ("driftKernels.cu", {"block_width": 64, "block_height": 1, "WIND_X_NX": 1, "WIND_X_NY": 1,
                                   "WIND_Y_NX": 1, "WIND_Y_NY": 1}, []),
+    # ModelErrorKL with the default basis (1..10 x 1..10) and with the double-jet case's (2..8 x 1..7)
+    "noise_kl10": ("ocean_noise.cu", noise_defines(kl_rand=(10, 20)), NOISE_FLAGS),
+    "noise_kl7": ("ocean_noise.cu", noise_defines(kl_rand=(7, 14)), NOISE_FLAGS),
     # OceanNoiseEnsemble's observation kernels, no defines and default options (E/OceanNoiseEnsemble.py:333-339)
     "observation": ("observationKernels.cu", {}, []),
 }
@@ -478,6 +482,41 @@ class RefNoise:
 # ---------------------------------------------------------------------------
 # drifters through the reference kernels
 # ---------------------------------------------------------------------------
+
+def ref_kl_perturb(config, nx, ny, dx, dy, eta, hu, hv, Hi, rns, basis=(1, 10, 1, 10), include_cos=True,
+                   include_sin=True, kl_decay=1.2, kl_scaling=1.0, rollers=(0.0, 0.0, 0.0, 0.0), f=1.2e-4,
+                   beta=0.0, g=9.81, perturbation_scale=1.0, eta_only=False, land_value=1e20):
+    """ModelErrorKL.perturbOceanState / perturbEta through the reference's
+    kernels (S/ModelErrorKL.py:313-449): kl_sample_ocean_state on a grid of
+    ceil(n / 14) blocks of 16 x 16 (one ghost ring per block), or
+    kl_sample_eta on ceil(n / 16) blocks.  1x1 Coriolis (0) and angle (0)
+    textures.  Host arrays in, (eta, hu, hv) out."""
+    drv = Driver.get()
+    arrs = [Array2D(drv, a) for a in (eta, hu, hv)]
+    Hi_a = Array2D(drv, Hi)
+    r_a = Array2D(drv, rns)
+    zero = Array2D(drv, np.zeros((1, 1), np.float32))
+    try:
+        scale = np.float32(perturbation_scale * np.float32(kl_scaling))
+        common = [int(basis[0]), int(basis[1]), int(basis[2]), int(basis[3]), int(include_cos), int(include_sin),
+                  np.float32(kl_decay), scale, *[np.float32(r) for r in rollers], r_a.ptr, r_a.pitch]
+        if eta_only:
+            k = drv.function(config, "kl_sample_eta")
+            drv.launch(k, "iiiiiiiiffffffPiPi", (_ceil(nx, 16), _ceil(ny, 16)), (16, 16, 1), int(nx), int(ny),
+                       *common, arrs[0].ptr, arrs[0].pitch)
+        else:
+            k = drv.function(config, "kl_sample_ocean_state")
+            drv.launch(k, "iifffffPPiiiiiiffffffPiPiPiPiPif", (_ceil(nx, 14), _ceil(ny, 14)), (16, 16, 1),
+                       int(nx), int(ny), np.float32(dx), np.float32(dy), np.float32(g), np.float32(f),
+                       np.float32(beta), zero.ptr, zero.ptr, *common, arrs[0].ptr, arrs[0].pitch,
+                       arrs[1].ptr, arrs[1].pitch, arrs[2].ptr, arrs[2].pitch, Hi_a.ptr, Hi_a.pitch,
+                       np.float32(land_value))
+        drv.synchronize()
+        return tuple(a.download() for a in arrs)
+    finally:
+        for a in arrs + [Hi_a, r_a, zero]:
+            a.free()
+
 
 def ref_observe_underlying_flow(nx, ny, dx, dy, hu, hv, positions, H=60.0):
     """observeUnderlyingFlow (K/observationKernels.cu:29-83) on (ny+4, nx+4)

@@ -1,0 +1,151 @@
+"""Karhunen-Loeve model error on the device: against the reference's own
+kl_sample_ocean_state / kl_sample_eta kernels (compiled from the reference
+sources) and the FP64 oracle (pinned to the reference's CPU twin by
+tests/test_kl_oracle.py), and the batched ensemble path against the
+single-simulator path.
+
+The device evaluates the separable basis sum from tables (a different
+summation order from the reference's 2 Nx Ny terms per cell), so parity is
+a tolerance: eta within 2e-5 of the perturbation's largest magnitude; the
+balanced hu, hv (centred differences of eta, which cancel) within 4e-4 of
+theirs; each no further from the FP64 oracle than twice the reference
+kernel's own distance plus 2e-6.  Batched and single paths run the same
+device code: bit-identical."""
+import json
+
+import numpy as np
+import pytest
+
+from oracle import kl_oracle as ko
+from oracle import ref_kernels as rk
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.abs(np.asarray(a, np.float64) - b).max() / max(np.abs(b).max(), 1e-30))
+
+
+CASES = [
+    # config, basis (x0, x1, y0, y1), include (cos, sin), eta_only, nx, ny
+    ("noise_kl10", (1, 10, 1, 10), (True, True), False, 77, 45),
+    ("noise_kl10", (1, 10, 1, 10), (False, True), False, 64, 64),
+    ("noise_kl10", (1, 10, 1, 10), (True, True), True, 77, 45),
+    ("noise_kl7", (2, 8, 1, 7), (True, True), False, 128, 96),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}-{c[4]}x{c[5]}-cos{int(c[2][0])}-eta{int(c[3])}")
+def test_kl_matches_reference_kernels(gpu_ctx, case):
+    if not rk.available():
+        pytest.skip("reference kernels not built (no reference sources)")
+    from gpuocean_gb300.SWEsimulators.ModelErrorKL import ModelErrorKL
+    from gpuocean_gb300.utils import Common
+    config, basis, (inc_cos, inc_sin), eta_only, nx, ny = case
+    dx, dy, f, beta, g = 2000.0, 2500.0, 1.2e-4, 2e-11, 9.81
+    rng = np.random.default_rng(nx * 7 + ny)
+    NX, NY = basis[1] - basis[0] + 1, basis[3] - basis[2] + 1
+    rns = rng.standard_normal((2 * NY, NX)).astype(np.float32)
+    rollers = tuple(float(r) for r in rng.uniform(size=4))
+    eta = (0.05 * rng.standard_normal((ny + 4, nx + 4))).astype(np.float32)
+    hu = rng.standard_normal((ny + 4, nx + 4)).astype(np.float32)
+    hv = rng.standard_normal((ny + 4, nx + 4)).astype(np.float32)
+    Hi = (100.0 + 10.0 * rng.standard_normal((ny + 5, nx + 5))).astype(np.float32)
+    kw = dict(basis=basis, include_cos=inc_cos, include_sin=inc_sin, kl_decay=1.25, kl_scaling=0.025,
+              rollers=rollers, f=f, beta=beta, g=g, perturbation_scale=0.7, eta_only=eta_only)
+    ref = rk.ref_kl_perturb(config, nx, ny, dx, dy, eta, hu, hv, Hi, rns, **kw)
+
+    stream = Common.Stream()
+    me = ModelErrorKL(gpu_ctx, stream, nx, ny, dx, dy, Common.BoundaryConditions(), kl_decay=1.25,
+                      kl_scaling=0.025, include_cos=inc_cos, include_sin=inc_sin, basis_x_start=basis[0],
+                      basis_x_end=basis[1], basis_y_start=basis[2], basis_y_end=basis[3])
+    arrs = [Common.CUDAArray2D(stream, nx, ny, 2, 2, a) for a in (eta, hu, hv)]
+    Hi_a = Common.CUDAArray2D(stream, nx + 1, ny + 1, 2, 2, Hi)
+    roll = dict(roll_x_sin=rollers[0], roll_y_sin=rollers[1], roll_x_cos=rollers[2], roll_y_cos=rollers[3])
+    if eta_only:
+        me.perturbEta(arrs[0], random_numbers=rns, perturbation_scale=0.7, **roll)
+    else:
+        me.perturbOceanState(arrs[0], arrs[1], arrs[2], Hi_a, dx, dy, f, beta=beta, g=g, random_numbers=rns,
+                             perturbation_scale=0.7, **roll)
+    got = [a.download(stream) for a in arrs]
+    for a in arrs + [Hi_a]:
+        a.release()
+    me.cleanUp()
+
+    d = ko.kl_d_eta(nx, ny, rns, basis[0], basis[1], basis[2], basis[3], inc_cos, inc_sin, np.float32(1.25),
+                    np.float32(0.025), 0.7, rollers)
+    if eta_only:
+        ora = [eta.astype(np.float64), hu, hv]
+        ora[0][2:-2, 2:-2] += d[1:-1, 1:-1]
+    else:
+        ora = ko.kl_perturb_state(eta, hu, hv, Hi, d, dx, dy, f, beta, g)
+    out = {"case": f"{config} {nx}x{ny}"}
+    for q, name in enumerate(("eta", "hu", "hv")):
+        pert_ref = np.asarray(ref[q], np.float64) - (eta, hu, hv)[q]
+        pert_got = np.asarray(got[q], np.float64) - (eta, hu, hv)[q]
+        pert_ora = np.asarray(ora[q], np.float64) - (eta, hu, hv)[q]
+        if np.abs(pert_ref).max() == 0:
+            assert np.abs(pert_got).max() == 0, name
+            continue
+        e_gr = _rel(pert_got, pert_ref)
+        e_go, e_ro = _rel(pert_got, pert_ora), _rel(pert_ref, pert_ora)
+        out[name] = {"vs_reference": e_gr, "vs_oracle": e_go, "reference_vs_oracle": e_ro}
+        assert e_gr <= (2e-5 if name == "eta" else 4e-4), (name, e_gr)
+        assert e_go <= 2.0 * e_ro + 2e-6, (name, e_go, e_ro)
+    print(json.dumps(out))
+
+
+def _kl_members(ctx, n, nx, ny, seed0):
+    from test_ensemble_gpu import _member
+    sims = []
+    for k in range(n):
+        s = _member(ctx, nx, ny, (1, 2, 1, 2), 3)
+        s.updateDt()
+        s.setKLModelError(kl_decay=1.25, kl_scaling=0.025, basis_x_start=2, basis_x_end=8, basis_y_start=1,
+                          basis_y_end=7, np_seed=seed0 + k)
+        sims.append(s)
+    return sims
+
+
+def test_kl_batched_equals_single(gpu_ctx):
+    """One batched perturbation of every member equals perturbSim member by
+    member with the same normals and rollers (rollers drawn from twin
+    generators with the same seeds)."""
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
+    a = _kl_members(gpu_ctx, 4, 64, 40, 100)
+    b = _kl_members(gpu_ctx, 4, 64, 40, 100)
+    rng = np.random.default_rng(4)
+    normals = [rng.standard_normal((14, 7)).astype(np.float32) for _ in a]
+    for s, r in zip(a, normals):
+        s.model_error.setRandomNumbers(r)
+    ens = BatchedEnsemble(a, autotune=False)
+    ens.set_noise([s.model_error for s in a])
+    ens.perturb(perturbation_scale=0.5, update_random_field=False)
+    ens.synchronize()
+    for s, r in zip(b, normals):
+        s.model_error.perturbSim(s, perturbation_scale=0.5, random_numbers=r)
+    for sa, sb in zip(a, b):
+        for x, y in zip(sa.download(), sb.download()):
+            assert np.array_equal(np.asarray(x), np.asarray(y))
+    ens.release()
+
+
+def test_kl_multilevel_partner_coupling(gpu_ctx):
+    """With sources, the coarse partner is perturbed with its fine partner's
+    normals and rollers - what perturbSimSimilarAs does in
+    dataAssimilationStep."""
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
+    fine, coarse = _kl_members(gpu_ctx, 1, 64, 32, 7)[0], _kl_members(gpu_ctx, 1, 32, 16, 8)[0]
+    fine2, coarse2 = _kl_members(gpu_ctx, 1, 64, 32, 7)[0], _kl_members(gpu_ctx, 1, 32, 16, 8)[0]
+    r = np.random.default_rng(9).standard_normal((14, 7)).astype(np.float32)
+    fine.model_error.setRandomNumbers(r)
+    ens = BatchedEnsemble([fine, coarse], autotune=False)
+    ens.set_noise([fine.model_error, coarse.model_error], sources=[0, 0])
+    ens.perturb(update_random_field=False)
+    ens.synchronize()
+    fine2.model_error.perturbSim(fine2, random_numbers=r)
+    coarse2.model_error.perturbSimSimilarAs(coarse2, modelError=fine2.model_error)
+    for sa, sb in ((fine, fine2), (coarse, coarse2)):
+        for x, y in zip(sa.download(), sb.download()):
+            assert np.array_equal(np.asarray(x), np.asarray(y))
+    ens.release()
