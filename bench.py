@@ -401,6 +401,49 @@ def run_statistics(ens, sims, peak, peak_kind, n_positions=1000, repeats=10):
     return out
 
 
+def run_kl(ens, sims, peak, peak_kind, repeats=10):
+    """Karhunen-Loeve model error on the C3 ensemble (every member at
+    512 x 300) with the double-jet case's KL parameters (basis 2..8 x 1..7,
+    decay 1.25, scaling 0.025; S/ModelErrorKL.py, the reference's
+    DoubleJetCase model_error=2): one batched perturbation of all members -
+    the basis tables, then the balanced update of every member-cell - timed
+    with CUDA events, normals drawn on the device.  Algorithmic bytes of the
+    update: read and write eta, hu, hv (24 B per member-cell) plus the shared
+    corner depths once."""
+    from gpuocean_gb300 import _lib
+    from gpuocean_gb300.SWEsimulators.ModelErrorKL import ModelErrorKL
+    kls = [ModelErrorKL.fromsim(s, kl_decay=1.25, kl_scaling=0.025, basis_x_start=2, basis_x_end=8,
+                                basis_y_start=1, basis_y_end=7, np_seed=9000 + m) for m, s in enumerate(sims)]
+    ens.set_noise(kls, rng_seed=31)
+    for _ in range(3):
+        ens.perturb(perturbation_scale=1e-3)
+    ens.synchronize()
+    stream = ens.stream.handle
+    ev = [ctypes.c_void_p(), ctypes.c_void_p()]
+    for e in ev:
+        _lib.call("goc_event_create", ctypes.byref(e))
+    _lib.call("goc_event_record", ev[0], stream)
+    for _ in range(repeats):
+        ens.perturb(perturbation_scale=1e-3)
+    _lib.call("goc_event_record", ev[1], stream)
+    ens.synchronize()
+    ms = ctypes.c_float()
+    _lib.call("goc_event_elapsed_ms", ev[0], ev[1], ctypes.byref(ms))
+    for e in ev:
+        _lib.load().goc_event_destroy(e)
+    per = ms.value / repeats
+    nx, ny = int(sims[0].nx), int(sims[0].ny)
+    cells = len(sims) * nx * ny
+    alg = 24 * cells + 4 * (nx + 5) * (ny + 5)
+    ens.release_noise()
+    for k in kls:
+        k.cleanUp()
+    return {"members": len(sims), "nx": nx, "ny": ny, "perturbation_ms": per,
+            "member_cells_per_s": cells / (per * 1e-3), "gbs": alg / (per * 1e-3) / 1e9,
+            "frac": alg / (per * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
+            "launches": "RNG + tables + update (3)"}
+
+
 def run_adjoint(ctx, n=256, n_steps=400, every=10, n_points=64):
     """Adjoint of the CDKLM16 rollout: the Gaussian bump (n x n, dx = dy =
     200 m, H = 60 m, f = 1.2e-4, walls, 0.1 m amplitude, sigma 10 cells) with
@@ -728,6 +771,7 @@ def main():
     per_member_rate = pm_cells / (time.perf_counter() - t0)
 
     ens_stats = None if args.no_statistics else run_statistics(ens, sims, *measured_peaks())
+    kl = None if args.no_statistics else run_kl(ens, sims, *measured_peaks())
     multilevel = None if args.no_multilevel else run_multilevel(ctx, args)
     adjoint = None if args.no_adjoint else run_adjoint(ctx)
 
@@ -765,7 +809,7 @@ def main():
                          "peak_kind": peak_kind, "avg_launch_ms": 1000.0 * avg_dur,
                          "algorithmic_bytes_per_launch": avg_bytes},
             "e2e": e2e, "gpu_launches": launches, "clocks": clk, "cpu_baseline": cpu,
-            "multilevel": multilevel, "adjoint": adjoint, "statistics": ens_stats,
+            "multilevel": multilevel, "adjoint": adjoint, "statistics": ens_stats, "kl_model_error": kl,
             "wall_s": wall,
         }
         print(json.dumps(line), flush=True)

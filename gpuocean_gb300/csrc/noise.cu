@@ -419,50 +419,90 @@ __device__ void kl_table_entry(const GocKLDesc& d, KLRoll r, int nx, int ny, int
     }
 }
 
-constexpr int kKX = 32, kKY = 8;  // KL perturbation tile (interior cells)
+constexpr int kKX = 32, kKY = 32;  // KL perturbation tile (interior cells)
+constexpr int kKT = 8;             // thread rows: each thread owns kKY / kKT cells of a column
+constexpr int kKR = kKY / kKT;
+constexpr int kKLMaxRows = 32;     // basis rows staged in shared memory (more: read from the tables directly)
 
 // kl_sample_eta / kl_sample_ocean_state on one tile with interior origin
 // (bx, by): d_eta on the tile + 1 ring from the tables, then (unless
 // eta_only) the geostrophically balanced hu, hv of K/ocean_noise.cu:901-947.
 // The reference computes a dry-cell flag there and does not use it: land
-// cells are perturbed as well.
+// cells are perturbed as well.  Every thread loads the state and corner
+// depths of its kKR cells first and the tile's slices of the tables are
+// staged in shared memory, so the DRAM and L2 round trips overlap.
 __device__ void kl_perturb_tile(const GocKLDesc& d, const OceanRef& o, float scale, int eta_only, int bx, int by) {
     __shared__ float s_d[kKY + 2][kKX + 2];
+    __shared__ float s_bx[2][kKLMaxRows][kKX + 2];
+    __shared__ float s_ay[2][kKLMaxRows][kKY + 2];
     const int NY = kl_count_y(d), CX = o.nx + 2, RY = o.ny + 2;
     const float* Bs = d.table;
     const float* Bc = Bs + (size_t)NY * CX;
     const float* As = Bc + (size_t)NY * CX;
     const float* Ac = As + (size_t)NY * RY;
     const float amp = scale * d.kl_scaling;
-    for (int k = threadIdx.y * kKX + threadIdx.x; k < (kKY + 2) * (kKX + 2); k += kKX * kKY) {
-        const int i = k % (kKX + 2), j = k / (kKX + 2);
+    const int tx = threadIdx.x, t = threadIdx.y * kKX + tx;
+    const int ti = 2 + bx + tx;
+    float e0[kKR], u0[kKR], v0[kKR], H_mid[kKR];
+#pragma unroll
+    for (int r = 0; r < kKR; ++r) {
+        const int ty = threadIdx.y + r * kKT, tj = 2 + by + ty;
+        e0[r] = u0[r] = v0[r] = H_mid[r] = 0.0f;
+        if (ti < o.nx + 2 && tj < o.ny + 2) {
+            const size_t k = (size_t)tj * o.pitch + ti;
+            e0[r] = o.eta[k];
+            if (!eta_only) {
+                u0[r] = o.hu[k];
+                v0[r] = o.hv[k];
+                const float* h0 = o.Hi + (size_t)tj * o.hi_pitch + ti;
+                const float* h1 = h0 + o.hi_pitch;
+                H_mid[r] = 0.25f * (h0[0] + h0[1] + h1[0] + h1[1]);
+            }
+        }
+    }
+    const bool staged = NY <= kKLMaxRows;
+    if (staged) {
+        // rows (sine block, then cosine block) over the thread rows, columns over the lanes
+        for (int wr = threadIdx.y; wr < 2 * NY; wr += kKT) {
+            const int w = wr >= NY, r = wr - w * NY;
+            const float* B = (w ? Bc : Bs) + (size_t)r * CX;
+            const float* A = (w ? Ac : As) + (size_t)r * RY;
+            for (int c = tx; c < kKX + 2; c += kKX) s_bx[w][r][c] = bx + c < CX ? B[bx + c] : 0.0f;
+            for (int c = tx; c < kKY + 2; c += kKX) s_ay[w][r][c] = by + c < RY ? A[by + c] : 0.0f;
+        }
+        __syncthreads();
+    }
+    for (int q = t; q < (kKY + 2) * (kKX + 2); q += kKX * kKT) {
+        const int i = q % (kKX + 2), j = q / (kKX + 2);
         const int cx = bx + i, ry = by + j;   // table column / row of full-array cell (1 + bx + i, 1 + by + j)
         float v = 0.0f;
         if (cx < CX && ry < RY) {
-            for (int q = 0; q < NY; ++q)
-                v += As[(size_t)q * RY + ry] * Bs[(size_t)q * CX + cx] + Ac[(size_t)q * RY + ry] * Bc[(size_t)q * CX + cx];
+            if (staged) {
+#pragma unroll 4
+                for (int r = 0; r < NY; ++r) v += s_ay[0][r][j] * s_bx[0][r][i] + s_ay[1][r][j] * s_bx[1][r][i];
+            } else {
+                for (int r = 0; r < NY; ++r)
+                    v += As[(size_t)r * RY + ry] * Bs[(size_t)r * CX + cx] + Ac[(size_t)r * RY + ry] * Bc[(size_t)r * CX + cx];
+            }
             v *= amp;
         }
         s_d[j][i] = v;
     }
     __syncthreads();
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int ti = 2 + bx + tx, tj = 2 + by + ty;
-    if (ti < o.nx + 2 && tj < o.ny + 2) {
+#pragma unroll
+    for (int r = 0; r < kKR; ++r) {
+        const int ty = threadIdx.y + r * kKT, tj = 2 + by + ty;
+        if (ti >= o.nx + 2 || tj >= o.ny + 2) continue;
         const float de = s_d[ty + 1][tx + 1];
-        const size_t k = (size_t)tj * o.pitch + ti;
         if (eta_only) {
-            o.eta[k] += de;
+            o.eta[(size_t)tj * o.pitch + ti] = e0[r] + de;
         } else {
-            const float* h0 = o.Hi + (size_t)tj * o.hi_pitch + ti;
-            const float* h1 = h0 + o.hi_pitch;
-            const float H_mid = 0.25f * (h0[0] + h0[1] + h1[0] + h1[1]);
             const float cor = noise_coriolis(d, o, ti, tj);
             const float ex = (s_d[ty + 1][tx + 2] - s_d[ty + 1][tx]) / (2.0f * o.dx);
             const float ey = (s_d[ty + 2][tx + 1] - s_d[ty][tx + 1]) / (2.0f * o.dy);
-            const float dhu = -(d.g / cor) * (H_mid + de) * ey;
-            const float dhv = (d.g / cor) * (H_mid + de) * ex;
-            store_cell(o, ti, tj, o.eta[k] + de, o.hu[k] + dhu, o.hv[k] + dhv);
+            const float dhu = -(d.g / cor) * (H_mid[r] + de) * ey;
+            const float dhv = (d.g / cor) * (H_mid[r] + de) * ex;
+            store_cell(o, ti, tj, e0[r] + de, u0[r] + dhu, v0[r] + dhv);
         }
     }
     __syncthreads();
@@ -473,7 +513,7 @@ __global__ void kl_table_kernel(GocKLDesc d, int nx, int ny) {
                    blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-__global__ void kl_perturb_kernel(GocKLDesc d, OceanRef o, float scale, int eta_only) {
+__global__ void __launch_bounds__(kKX * kKT, 4) kl_perturb_kernel(GocKLDesc d, OceanRef o, float scale, int eta_only) {
     kl_perturb_tile(d, o, scale, eta_only, blockIdx.x * kKX, blockIdx.y * kKY);
 }
 
@@ -489,7 +529,8 @@ __global__ void kl_table_batched_kernel(const GocKLDesc* __restrict__ kl, const 
     kl_table_entry(kl[it.x], KLRoll{r.x, r.y, r.z, r.w}, mem[it.x].p.nx, mem[it.x].p.ny, it.y, it.z + threadIdx.x);
 }
 
-__global__ void kl_perturb_batched_kernel(const GocKLDesc* __restrict__ kl, const GocMemberDesc* __restrict__ mem,
+__global__ void __launch_bounds__(kKX * kKT, 4)
+kl_perturb_batched_kernel(const GocKLDesc* __restrict__ kl, const GocMemberDesc* __restrict__ mem,
                                           const int4* __restrict__ items, const int* __restrict__ nsub, int substep,
                                           float scale) {
     const int4 it = items[blockIdx.x];   // (member, tile x, tile y, 0)
@@ -517,6 +558,19 @@ __global__ void kl_xorwow_batched_kernel(const GocKLDesc* __restrict__ kl, const
         rnd[(size_t)(e / NX) * (d.random_pitch / 4) + e % NX] = curand_normal(&st);
         states[c.w + q] = st;
     }
+}
+
+// Rollers of the source members that perturb at `substep`, drawn on the
+// device (one XORWOW state per member): set substep + 1.
+__global__ void kl_roll_batched_kernel(const int* __restrict__ src, curandStateXORWOW_t* states, float4* rollers,
+                                       int n, const int* __restrict__ nsub, int substep) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    int set;
+    if (m >= n || src[m] != m || !member_set(nsub, m, substep, &set)) return;
+    curandStateXORWOW_t st = states[m];
+    const float a = curand_uniform(&st), b = curand_uniform(&st), c = curand_uniform(&st), d = curand_uniform(&st);
+    rollers[(size_t)(substep + 1) * n + m] = make_float4(a, b, c, d);
+    states[m] = st;
 }
 
 }  // namespace goc
@@ -766,7 +820,7 @@ extern "C" int goc_kl_perturb(const GocKLDesc* kl, int nx, int ny, float dx, flo
     count_launch();
     if ((rc = check_launch("kl_table_kernel"))) return rc;
     dim3 grd((nx + kKX - 1) / kKX, (ny + kKY - 1) / kKY);
-    kl_perturb_kernel<<<grd, dim3(kKX, kKY), 0, st>>>(*kl, o, perturbation_scale, eta_only);
+    kl_perturb_kernel<<<grd, dim3(kKX, kKT), 0, st>>>(*kl, o, perturbation_scale, eta_only);
     count_launch();
     return check_launch("kl_perturb_kernel");
 }
@@ -780,7 +834,7 @@ struct KLBatch {
     int4* d_tab_items = nullptr;
     int4* d_tile_items = nullptr;
     int4* d_rng_chunks = nullptr;
-    curandStateXORWOW_t* d_states = nullptr;
+    curandStateXORWOW_t* d_states = nullptr;       // normals, then one roller state per member
     int n_tab = 0, n_tile = 0, n_rng = 0, n_states = 0;
     std::vector<GocKLDesc> host;
     std::vector<int> src;
@@ -883,12 +937,12 @@ extern "C" int goc_kl_batch_destroy(void* batch) {
 extern "C" int goc_kl_batch_seed(void* batch, unsigned long long seed, void* stream) {
     if (!batch) return set_error(GOC_ERR_ARG, "goc_kl_batch_seed: null handle");
     KLBatch* b = static_cast<KLBatch*>(batch);
-    if (b->n_states == 0) return GOC_OK;
+    const int total = b->n_states + b->n;
     if (!b->d_states) {
-        cudaError_t e = cudaMalloc(&b->d_states, sizeof(curandStateXORWOW_t) * (size_t)b->n_states);
+        cudaError_t e = cudaMalloc(&b->d_states, sizeof(curandStateXORWOW_t) * (size_t)total);
         if (e != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_kl_batch_seed: %s", cudaGetErrorString(e));
     }
-    xorwow_batched_init_kernel<<<(b->n_states + 127) / 128, 128, 0, as_stream(stream)>>>(b->d_states, b->n_states, seed);
+    xorwow_batched_init_kernel<<<(total + 127) / 128, 128, 0, as_stream(stream)>>>(b->d_states, total, seed);
     count_launch();
     return check_launch("xorwow_batched_init_kernel");
 }
@@ -897,11 +951,20 @@ extern "C" int goc_kl_batch_generate(void* batch, void* ensemble, int substep, v
     if (!batch || !ensemble) return set_error(GOC_ERR_ARG, "goc_kl_batch_generate: null handle");
     KLBatch* b = static_cast<KLBatch*>(batch);
     if (!b->d_states) return set_error(GOC_ERR_ARG, "goc_kl_batch_generate: call goc_kl_batch_seed first");
-    if (b->n_rng == 0) return GOC_OK;
-    kl_xorwow_batched_kernel<<<b->n_rng, 256, 0, as_stream(stream)>>>(b->d_kl, b->d_rng_chunks, b->d_states,
-                                                                     ensemble_device_nsub(ensemble), substep);
+    if (substep + 1 < 0 || substep + 1 >= b->max_sets)
+        return set_error(GOC_ERR_ARG, "goc_kl_batch_generate: substep %d outside the roller sets", substep);
+    cudaStream_t st = as_stream(stream);
+    const int* nsub = ensemble_device_nsub(ensemble);
+    if (b->n_rng > 0) {
+        kl_xorwow_batched_kernel<<<b->n_rng, 256, 0, st>>>(b->d_kl, b->d_rng_chunks, b->d_states, nsub, substep);
+        count_launch();
+        int rc = check_launch("kl_xorwow_batched_kernel");
+        if (rc) return rc;
+    }
+    kl_roll_batched_kernel<<<(b->n + 127) / 128, 128, 0, st>>>(b->d_src, b->d_states + b->n_states, b->d_rollers,
+                                                               b->n, nsub, substep);
     count_launch();
-    return check_launch("kl_xorwow_batched_kernel");
+    return check_launch("kl_roll_batched_kernel");
 }
 
 extern "C" int goc_kl_batch_set_rollers(void* batch, const float* rollers, int n_sets, void* stream) {
@@ -941,7 +1004,7 @@ extern "C" int goc_kl_batch_perturb(void* batch, void* ensemble, float perturbat
     count_launch();
     int rc = check_launch("kl_table_batched_kernel");
     if (rc) return rc;
-    kl_perturb_batched_kernel<<<b->n_tile, dim3(kKX, kKY), 0, st>>>(b->d_kl, dm, b->d_tile_items, nsub, substep,
+    kl_perturb_batched_kernel<<<b->n_tile, dim3(kKX, kKT), 0, st>>>(b->d_kl, dm, b->d_tile_items, nsub, substep,
                                                                     perturbation_scale);
     count_launch();
     return check_launch("kl_perturb_batched_kernel");

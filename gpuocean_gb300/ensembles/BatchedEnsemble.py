@@ -77,6 +77,8 @@ class BatchedEnsemble:
             share_bathymetry = True
         if share_bathymetry:
             self._dedupe_bathymetry()
+        self._orig_streams = []
+        self._adopt_streams(self.sims)
         self._build()
         if autotune:
             self.autotune()
@@ -112,7 +114,7 @@ class BatchedEnsemble:
         return tuple(s.gpu_data.h0.ptr for s in self.sims)
 
     def _build(self, max_substeps=8):
-        self.release()
+        self._release_handles()
         self._descs_host = self._descs()
         h = ctypes.c_void_p()
         _lib.call("goc_ensemble_create", self._descs_host, len(self.sims), int(max_substeps), ctypes.byref(h))
@@ -132,6 +134,31 @@ class BatchedEnsemble:
             seed = None if self._rng_seed is None else self._rng_seed + 7919 * self._reseeds
             self.set_noise(self._noises, getattr(self, "_random_pool", None), rng_seed=seed,
                            sources=self._noise_sources)
+
+    def _adopt_streams(self, objs):
+        """Members (and their drifters and model errors) issue their own
+        work on the engine's stream while they belong to the engine, so a
+        member's calls (download, upload, perturbState, ...) and the
+        engine's launches are ordered without any synchronisation.  The
+        original streams come back with release()."""
+        for s in objs:
+            s.gpu_stream.synchronize()
+            for o in (s, getattr(s, "drifters", None) if getattr(s, "hasDrifters", False) else None,
+                      getattr(s, "model_error", None)):
+                if o is None or getattr(o, "gpu_stream", None) is self.stream:
+                    continue
+                self._orig_streams.append((o, o.gpu_stream))
+                o.gpu_stream = self.stream
+                rng = getattr(o, "rng", None)
+                if rng is not None and hasattr(rng, "gpu_stream"):
+                    self._orig_streams.append((rng, rng.gpu_stream))
+                    rng.gpu_stream = self.stream
+
+    def _restore_streams(self):
+        self.stream.synchronize()
+        for o, st in reversed(getattr(self, "_orig_streams", [])):
+            o.gpu_stream = st
+        self._orig_streams = []
 
     def _collect_streams(self):
         """The members' own streams (simulator, drifters, model error): the
@@ -154,12 +181,15 @@ class BatchedEnsemble:
         self._n_member_streams = len(handles)
 
     def _after_members(self):
-        """Engine stream waits for the work queued on the members' streams."""
-        _lib.call("goc_stream_fan_in", self.stream.handle, self._member_streams, self._n_member_streams)
+        """Engine stream waits for the work queued on the members' streams
+        (those not adopted: none unless a member's objects were replaced)."""
+        if self._n_member_streams:
+            _lib.call("goc_stream_fan_in", self.stream.handle, self._member_streams, self._n_member_streams)
 
     def _before_members(self):
         """Members' streams wait for the work queued on the engine stream."""
-        _lib.call("goc_stream_fan_out", self.stream.handle, self._member_streams, self._n_member_streams)
+        if self._n_member_streams:
+            _lib.call("goc_stream_fan_out", self.stream.handle, self._member_streams, self._n_member_streams)
 
     def _attach_drifters(self):
         """Drifter collections attached to the members are advected inside
@@ -182,6 +212,11 @@ class BatchedEnsemble:
                       ctypes.c_float(sens), self.stream.handle)
 
     def release(self):
+        """Free the device handles and give the members their own streams back."""
+        self._release_handles()
+        self._restore_streams()
+
+    def _release_handles(self):
         self.release_noise()
         for name in ("_obs_pos", "_obs_out"):
             buf = getattr(self, name, None)
@@ -306,12 +341,23 @@ class BatchedEnsemble:
         on the device before every perturbation (otherwise the random fields
         are used as they are, e.g. injected from the host).  sources (KL):
         sources[m] is the member whose normals and rollers member m uses -
+        drawn on the device with the normals when rng_seed is given, else
+        from each member's own generator on the host, as perturbSim does -
         the coarse partner of a multi-level pair perturbed "similar as" its
         fine partner (S/CDKLM16.py:782-790); by default every member its own.
         """
         from ..SWEsimulators.ModelErrorKL import GocKLDesc, ModelErrorKL
         assert len(noises) == len(self.sims)
         self.release_noise()
+        for n in noises:
+            if getattr(n, "gpu_stream", None) is not self.stream:
+                n.gpu_stream.synchronize()
+                self._orig_streams.append((n, n.gpu_stream))
+                n.gpu_stream = self.stream
+                rng = getattr(n, "rng", None)
+                if rng is not None and hasattr(rng, "gpu_stream"):
+                    self._orig_streams.append((rng, rng.gpu_stream))
+                    rng.gpu_stream = self.stream
         if all(isinstance(n, ModelErrorKL) for n in noises):
             src = np.arange(len(self.sims), dtype=np.int32) if sources is None else \
                 np.ascontiguousarray(sources, dtype=np.int32)
@@ -406,7 +452,9 @@ class BatchedEnsemble:
         """Add the SOAR model error to every member's current state."""
         before = _lib.load().goc_kernel_launch_count()
         self._after_members()
-        if self._noise_kind == "kl":
+        if self._noise_kind == "kl" and not (update_random_field and self._rng_seed is not None):
+            # injected normals: rollers from the members' own generators, as
+            # perturbSim draws them; with device draws they come with the normals
             self._kl_draw_rollers([(0, range(len(self.sims)))])
         self._noise_launch(-1, perturbation_scale, update_random_field)
         self._before_members()
@@ -439,7 +487,7 @@ class BatchedEnsemble:
                 s.bc_kernel.boundaryCondition(s.gpu_stream, s.gpu_data.h0, s.gpu_data.hu0, s.gpu_data.hv0)
         scheds, table, n, nsub = self._schedule(t_end)
         self._after_members()
-        if with_noise is not None and self._noise_kind == "kl":
+        if with_noise is not None and self._noise_kind == "kl" and self._rng_seed is None:
             if with_noise == "block":
                 self._kl_draw_rollers([(0, range(len(self.sims)))])
             else:

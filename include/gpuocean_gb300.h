@@ -532,8 +532,9 @@ int goc_kl_perturb(const GocKLDesc* kl, int nx, int ny, float dx, float dy, floa
  * source[m] is the member whose normals and rollers member m uses (m itself,
  * or the fine partner of a multi-level pair, the coupling of
  * perturbSimilarAs, S/CDKLM16.py:782-790).  goc_kl_batch_seed seeds XORWOW
- * states for every source member's normals; goc_kl_batch_generate draws new
- * normals (substep rule of goc_noise_batch_perturb);
+ * states for every source member's normals and rollers; goc_kl_batch_generate draws new
+ * normals and rollers on the device (substep rule of
+ * goc_noise_batch_perturb; the rollers go to set substep + 1);
  * goc_kl_batch_set_rollers uploads n_sets x n_members x 4 rollers (host;
  * set 0 is used with substep -1, set k + 1 with substep k);
  * goc_kl_batch_set_random copies host normals for member m's source.

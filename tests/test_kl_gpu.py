@@ -6,11 +6,12 @@ single-simulator path.
 
 The device evaluates the separable basis sum from tables (a different
 summation order from the reference's 2 Nx Ny terms per cell), so parity is
-a tolerance: eta within 2e-5 of the perturbation's largest magnitude; the
-balanced hu, hv (centred differences of eta, which cancel) within 4e-4 of
-theirs; each no further from the FP64 oracle than twice the reference
-kernel's own distance plus 2e-6.  Batched and single paths run the same
-device code: bit-identical."""
+a tolerance: eta within 5e-6 of the perturbation's largest magnitude; the
+balanced hu, hv (centred differences of eta, which cancel) within 2e-5 of
+theirs (measured: <= 1e-6 and <= 2.8e-6); each no further from the FP64
+oracle than twice the reference kernel's own distance plus 2e-6 (measured:
+the device is 1.5-3x closer to the oracle than the reference kernel).
+Batched and single paths run the same device code: bit-identical."""
 import json
 
 import numpy as np
@@ -90,7 +91,7 @@ def test_kl_matches_reference_kernels(gpu_ctx, case):
         e_gr = _rel(pert_got, pert_ref)
         e_go, e_ro = _rel(pert_got, pert_ora), _rel(pert_ref, pert_ora)
         out[name] = {"vs_reference": e_gr, "vs_oracle": e_go, "reference_vs_oracle": e_ro}
-        assert e_gr <= (2e-5 if name == "eta" else 4e-4), (name, e_gr)
+        assert e_gr <= (5e-6 if name == "eta" else 2e-5), (name, e_gr)
         assert e_go <= 2.0 * e_ro + 2e-6, (name, e_go, e_ro)
     print(json.dumps(out))
 
@@ -149,3 +150,62 @@ def test_kl_multilevel_partner_coupling(gpu_ctx):
         for x, y in zip(sa.download(), sb.download()):
             assert np.array_equal(np.asarray(x), np.asarray(y))
     ens.release()
+
+
+def test_kl_rates_reference_per_member_vs_batched(gpu_ctx):
+    """KL model error of 64 members of the 512 x 300 double jet (the
+    double-jet case's KL parameters: basis 2..8 x 1..7, decay 1.25, scaling
+    0.025): the reference's kl_sample_ocean_state launched member by member
+    (its ensembles' pattern; normals injected, so its random-number draws
+    are not timed) against one batched perturbation of all members (two
+    launches).  Printed as one JSON line."""
+    if not rk.available():
+        pytest.skip("reference kernels not built (no reference sources)")
+    import time
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
+    from gpuocean_gb300.utils import Common
+    n, nx, ny = 64, 512, 300
+    sims = _kl_members(gpu_ctx, n, nx, ny, 300)
+    ens = BatchedEnsemble(sims, autotune=False)
+    ens.set_noise([s.model_error for s in sims])
+    for _ in range(3):
+        ens.perturb(update_random_field=False)
+    ens.synchronize()
+    reps = 10
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ens.perturb(update_random_field=False)
+    ens.synchronize()
+    batched = (time.perf_counter() - t0) / reps
+
+    drv = rk.Driver.get()
+    rng = np.random.default_rng(1)
+    z = np.zeros((ny + 4, nx + 4), np.float32)
+    Hi = np.full((ny + 5, nx + 5), 230.0, np.float32)
+    arrs = [rk.Array2D(drv, z) for _ in range(3)]
+    Hi_a, r_a = rk.Array2D(drv, Hi), rk.Array2D(drv, rng.standard_normal((14, 7)).astype(np.float32))
+    zero = rk.Array2D(drv, np.zeros((1, 1), np.float32))
+    k = drv.function("noise_kl7", "kl_sample_ocean_state")
+
+    def launch():
+        drv.launch(k, "iifffffPPiiiiiiffffffPiPiPiPiPif", (-(-nx // 14), -(-ny // 14)), (16, 16, 1), nx, ny,
+                   5000.0, 5000.0, 9.81, 1.2e-4, 2e-11, zero.ptr, zero.ptr, 2, 8, 1, 7, 1, 1, 1.25, 0.025,
+                   0.1, 0.2, 0.3, 0.4, r_a.ptr, r_a.pitch, arrs[0].ptr, arrs[0].pitch, arrs[1].ptr, arrs[1].pitch,
+                   arrs[2].ptr, arrs[2].pitch, Hi_a.ptr, Hi_a.pitch, 1e20)
+    for _ in range(3):
+        launch()
+    drv.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps * n):
+        launch()
+    drv.synchronize()
+    ref_member = (time.perf_counter() - t0) / (reps * n)
+    for a in arrs + [Hi_a, r_a, zero]:
+        a.free()
+    ens.release()
+    cells = n * nx * ny
+    print(json.dumps({"case": "KL model error, 64 x 512x300", "reference_per_member_ms": 1e3 * ref_member,
+                      "reference_member_cells_per_s": nx * ny / ref_member,
+                      "batched_all_members_ms": 1e3 * batched, "batched_member_cells_per_s": cells / batched,
+                      "speedup": n * ref_member / batched}))
+    assert batched < n * ref_member
