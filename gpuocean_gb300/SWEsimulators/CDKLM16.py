@@ -75,8 +75,6 @@ class CDKLM16(Simulator):
         wind = WindStress.WindStress() if wind is None else wind
         atmospheric_pressure = AtmosphericPressure.AtmosphericPressure() if atmospheric_pressure is None else atmospheric_pressure
         boundary_conditions = Common.BoundaryConditions() if boundary_conditions is None else boundary_conditions
-        if boundary_conditions.isSponge():
-            raise NotImplementedError("sponge boundary conditions (3, 4) are not supported")
         angle = np.asarray(angle)
         ghost_cells_x = ghost_cells_y = 2
         self.boundary_conditions = boundary_conditions
@@ -211,6 +209,7 @@ class CDKLM16(Simulator):
         if self.gpu_data_extra is not None:
             self.gpu_data_extra.release()
         self.bathymetry.release()
+        self.bc_kernel.release()
         self.device_dt.free()
         self.max_dt_buffer.free()
         if self.coriolis_cell is not None:
@@ -236,7 +235,13 @@ class CDKLM16(Simulator):
 
     def _rk_step(self, local_dt):
         d = self.gpu_data
-        if self.rk_order == 2:
+        if self.rk_order == 2 and self.boundary_conditions.isSponge():
+            # sponge boundaries act between the stages (S/CDKLM16.py:519-530):
+            # stage by stage, with the boundary kernels on the stage buffer
+            self._stage((d.h0, d.hu0, d.hv0), (d.h1, d.hu1, d.hv1), local_dt, 0)
+            self.bc_kernel.boundaryCondition(self.gpu_stream, d.h1, d.hu1, d.hv1)
+            self._stage((d.h1, d.hu1, d.hv1), (d.h0, d.hu0, d.hv0), local_dt, 1)
+        elif self.rk_order == 2:
             _lib.call("goc_cdklm_rk2_step", ctypes.byref(self._params), ctypes.c_float(local_dt),
                       d.h0.ptr, d.hu0.ptr, d.hv0.ptr, d.h1.ptr, d.hu1.ptr, d.hv1.ptr, int(d.h0.pitch),
                       self.bathymetry.Bi.ptr, int(self.bathymetry.Bi.pitch),
@@ -272,9 +277,12 @@ class CDKLM16(Simulator):
             local_dt = np.float32(min(self.dt, np.float32(t_end - t_now)))
             self._params.wind_t = float(np.float32(self.update_wind_stress()))
             self._params.atm_p_t = float(np.float32(self.update_atmospheric_pressure()))
+            self.bc_kernel.update_bc_values(self.gpu_stream, self.t)
             self._rk_step(local_dt)
-            if self.model_error is not None and apply_stochastic_term:
+            perturbed = self.model_error is not None and apply_stochastic_term
+            if perturbed:
                 self.perturbState()
+            if perturbed or self.boundary_conditions.isSponge():
                 self.bc_kernel.boundaryCondition(self.gpu_stream, self.gpu_data.h0, self.gpu_data.hu0,
                                                  self.gpu_data.hv0)
             self.drifterStep(local_dt)

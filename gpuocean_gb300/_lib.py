@@ -105,6 +105,9 @@ SIGNATURES = {
                               c_int, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_float,
                               c_void_p, c_void_p, c_void_p, c_void_p]),
     "goc_drift_enforce_boundary": (c_int, [c_float, c_float, c_int, c_int, c_int, c_void_p, c_int, c_void_p]),
+    "goc_sponge_boundary": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                    c_void_p, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_int, c_float,
+                                    c_void_p]),
     "goc_kl_table_floats": (ctypes.c_longlong, [c_int, c_int, c_void_p]),
     "goc_kl_perturb": (c_int, [c_void_p, c_int, c_int, c_float, c_float, c_float, c_int, c_void_p, c_void_p, c_void_p,
                                c_int, c_void_p, c_int, c_int, c_int, c_void_p]),

@@ -18,8 +18,13 @@ OBJ = os.path.join(HERE, "_obj")
 LIB = os.path.join(HERE, "libgpuocean_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-          "--expt-relaxed-constexpr", "-ftz=true", "-prec-div=false", "-prec-sqrt=false"]
+BASE = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "--expt-relaxed-constexpr"]
+# the reference builds its step kernel with flush-to-zero and approximate
+# division and square root (S/CDKLM16.py:277-281); most of this library does
+# the same.  Files in DEFAULT_MATH keep CUDA's default (IEEE) arithmetic, as
+# the reference's boundary kernels are built (U/Common.py:1140-1151).
+COMMON = BASE + ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]
+DEFAULT_MATH = {"sponge.cu"}
 # per-file extra flags.  The step translation units keep every multiply and
 # add separately rounded (no FMA contraction), as the reference compiles its
 # step kernel (--fmad=false): with the same operation order this makes the
@@ -61,7 +66,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
         s = os.path.join(CSRC, src)
         o = os.path.join(OBJ, src[:-3] + ".o")
         if force or _needs(o, [s] + headers):
-            cmd = [nvcc, *ARCH, *COMMON, *EXTRA.get(src, []), "-c", s, "-o", o]
+            flags = BASE if src in DEFAULT_MATH else COMMON
+            cmd = [nvcc, *ARCH, *flags, *EXTRA.get(src, []), "-c", s, "-o", o]
             jobs.append((src, cmd))
     failed = []
 

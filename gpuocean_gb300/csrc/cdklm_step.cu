@@ -184,7 +184,7 @@ extern "C" int goc_cdklm_stage(const GocCdklmParams* p, float dt, int rk_step, c
                                const float* hu_in, const float* hv_in, float* eta_out, float* hu_out,
                                float* hv_out, float* eta_alt, float* hu_alt, float* hv_alt, int pitch,
                                const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch, void* stream) {
-    int rc = validate_params(p, "goc_cdklm_stage");
+    int rc = validate_params(p, "goc_cdklm_stage", true);
     if (rc) return rc;
     if ((rc = check_pitch(p, pitch, Hi_pitch, Hm_pitch, "goc_cdklm_stage"))) return rc;
     if (!eta_in || !hu_in || !hv_in || !eta_out || !hu_out || !hv_out || !Hi || !Hm)

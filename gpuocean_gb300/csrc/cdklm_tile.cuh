@@ -734,7 +734,10 @@ cdklm_tile_kernel(const GocCdklmParams p, const StepConst k, float dt, int rk_st
 constexpr int kTX = 32, kTY = 16, kNT = 256;
 
 // Host-side validation of a parameter set (shared by all entry points).
-inline int validate_params(const GocCdklmParams* p, const char* who) {
+// allow_open: open (sponge) boundaries, flags 3 and 4, whose ghost cells the
+// stage reads as stored - only the single-stage entry takes them, since the
+// sponge kernels act between the stages.
+inline int validate_params(const GocCdklmParams* p, const char* who, bool allow_open = false) {
     if (!p) return set_error(GOC_ERR_ARG, "%s: null params", who);
     if (p->nx < 1 || p->ny < 1) return set_error(GOC_ERR_ARG, "%s: nx, ny must be >= 1 (got %d, %d)", who, p->nx, p->ny);
     if (!(p->dx > 0.0f) || !(p->dy > 0.0f) || !(p->g > 0.0f))
@@ -744,8 +747,9 @@ inline int validate_params(const GocCdklmParams* p, const char* who) {
         return set_error(GOC_ERR_ARG, "%s: 3rd order Runge Kutta supported only without friction", who);
     const int b[4] = {p->bc_north, p->bc_east, p->bc_south, p->bc_west};
     for (int i = 0; i < 4; ++i)
-        if (b[i] != 1 && b[i] != 2)
-            return set_error(GOC_ERR_UNSUPPORTED, "%s: boundary flag %d not supported (1 = wall, 2 = periodic)", who, b[i]);
+        if (b[i] != 1 && b[i] != 2 && !(allow_open && (b[i] == 3 || b[i] == 4)))
+            return set_error(GOC_ERR_UNSUPPORTED, "%s: boundary flag %d not supported here (1 = wall, 2 = periodic%s)",
+                             who, b[i], allow_open ? ", 3, 4 = sponge" : "; sponges need the single-stage entry");
     if ((p->bc_north == 2) != (p->bc_south == 2) || (p->bc_east == 2) != (p->bc_west == 2))
         return set_error(GOC_ERR_ARG, "%s: periodic boundaries must come in opposite pairs", who);
     if (!p->coriolis_f || p->coriolis_nx < 1 || p->coriolis_ny < 1)

@@ -60,6 +60,8 @@ class BatchedEnsemble:
         assert len(sims) > 0
         for s in sims:
             assert int(s.rk_order) == 2, "the batched engine runs the fused RK2 step"
+            if s.boundary_conditions.isSponge():
+                raise NotImplementedError("sponge boundaries act between the RK stages; step such members on their own")
         self.sims = list(sims)
         self.stream = stream if stream is not None else Common.Stream()
         self.use_graph = use_graph

@@ -6,8 +6,8 @@ Replaces the PyCUDA-based classes of the reference (U/ = src/gpuocean/utils):
 * ``CUDAArray2D``                U/Common.py:516-644 (tight pitch float32 device arrays)
 * ``SWEDataArakawaA``            U/Common.py:774-831 (double-buffered state)
 * ``BoundaryConditions``         U/Common.py:920-1046
-* ``BoundaryConditionsData``     U/Common.py:1051-1117 (accepted; sponge data is not used)
-* ``BoundaryConditionsArakawaA`` U/Common.py:1121-1404 (periodic ghost fill)
+* ``BoundaryConditionsData``     U/Common.py:1051-1117 (exterior data of the sponges)
+* ``BoundaryConditionsArakawaA`` U/Common.py:1121-1404 (periodic ghosts, flow relaxation, linear interpolation)
 * ``Bathymetry``                 U/Common.py:1408-1561
 
 Device memory, streams and copies go through the library's C ABI.
@@ -232,8 +232,8 @@ class SWEDataArakawaA:
 class BoundaryConditions:
     """Boundary flags: 1 wall, 2 periodic, 3 flow relaxation, 4 linear interpolation.
 
-    Flags 3 and 4 (sponge boundaries) are accepted by this class, but the
-    simulators of this package support walls and periodic boundaries only.
+    Flags 3 and 4 are sponge boundaries: spongeCells gives, per side, the
+    rows or columns of the array (ghost cells included) that the sponge spans.
     """
 
     def __init__(self, north=1, east=1, south=1, west=1,
@@ -284,45 +284,129 @@ class BoundaryConditions:
 
 
 class SingleBoundaryConditionData:
+    """Exterior solution along one side over time (U/Common.py:1040-1078):
+    lists of 1D float32 arrays h, hu, hv, one per time stamp."""
+
     def __init__(self, h=None, hu=None, hv=None):
         self.h = [np.zeros(2, dtype=np.float32)] if h is None else h
         self.hu = [np.zeros(2, dtype=np.float32)] if hu is None else hu
         self.hv = [np.zeros(2, dtype=np.float32)] if hv is None else hv
         self.numSteps = len(self.h)
         self.shape = self.h[0].shape
+        for i in range(self.numSteps):
+            for a in (self.h[i], self.hu[i], self.hv[i]):
+                assert a.shape == self.shape, str(self.shape) + " vs " + str(a.shape)
+                assert a.dtype == np.float32, "boundary data needs to be of type np.float32"
+
+    def __str__(self):
+        return str(self.numSteps) + " steps, each " + str(self.shape)
 
 
 class BoundaryConditionsData:
-    """External boundary data for sponge boundaries (kept for API parity)."""
+    """Exterior solution for the sponge boundaries over time (U/Common.py:1081-1117)."""
 
     def __init__(self, t=None, north=None, south=None, east=None, west=None):
-        self.t = [0] if t is None else t
-        self.numSteps = len(self.t)
+        self.t = [0]
+        self.numSteps = 1
         self.north = north or SingleBoundaryConditionData()
         self.south = south or SingleBoundaryConditionData()
         self.east = east or SingleBoundaryConditionData()
         self.west = west or SingleBoundaryConditionData()
+        if t is not None:
+            self.t = t
+            self.numSteps = len(t)
+        for data in (self.north, self.south, self.east, self.west):
+            assert data.numSteps == self.numSteps, "Wrong timesteps " + str(data.numSteps) + " vs " + str(self.numSteps)
+        assert self.north.h[0].shape == self.south.h[0].shape, "Wrong shape of north vs south"
+        assert self.east.h[0].shape == self.west.h[0].shape, "Wrong shape of east vs west"
+
+    def __str__(self):
+        return ("Steps=" + str(self.numSteps) + ", [north=" + str(self.north) + "], [south=" + str(self.south)
+                + "], [east=" + str(self.east) + "], [west=" + str(self.west) + "]")
 
 
 class BoundaryConditionsArakawaA:
-    """Periodic ghost fill of an (eta, hu, hv) triple (U/Common.py:1310-1330)."""
+    """Ghost and sponge cells of an (eta, hu, hv) triple (U/Common.py:1120-1400):
+    periodic images (flag 2), flow relaxation towards exterior data (flag 3)
+    and linear interpolation (flag 4), north-south first, then east-west."""
 
     def __init__(self, gpu_ctx, gpu_stream, nx, ny, halo_x, halo_y, boundary_conditions,
                  bc_data=None, block_width=16, block_height=16):
         self.boundary_conditions = boundary_conditions
         self.nx, self.ny = np.int32(nx), np.int32(ny)
         self.halo_x, self.halo_y = np.int32(halo_x), np.int32(halo_y)
-        if boundary_conditions.isSponge():
-            raise NotImplementedError("sponge boundary conditions (3, 4) are not supported")
+        self.bc_data = BoundaryConditionsData() if bc_data is None else bc_data
+        bc = boundary_conditions
+        sp = bc.spongeCells
+        self.sponge_cells = np.array([sp.get('north', 0), sp.get('east', 0), sp.get('south', 0), sp.get('west', 0)],
+                                     dtype=np.int32)
+        self.bc_timestamps = [None, None]
+        self.bc_t = np.float32(0.0)
+        self.ns_nx = int(self.bc_data.north.h[0].shape[0])
+        self.ew_ny = int(self.bc_data.east.h[0].shape[0])
+        self.frs = 3 in (int(bc.north), int(bc.south), int(bc.east), int(bc.west))
+        self.bc_ns = [None, None]
+        self.bc_ew = [None, None]
+        if bc.isSponge():
+            z_ns = np.zeros((2, self.ns_nx, 3), np.float32)
+            z_ew = np.zeros((self.ew_ny, 2, 3), np.float32)
+            self.bc_ns = [CUDAArray2D(gpu_stream, 3 * self.ns_nx, 2, 0, 0, z_ns.reshape(2, -1)) for _ in range(2)]
+            self.bc_ew = [CUDAArray2D(gpu_stream, 6, self.ew_ny, 0, 0, z_ew.reshape(self.ew_ny, -1)) for _ in range(2)]
 
     def update_bc_values(self, gpu_stream, t):
-        return None
+        """Time interpolation of the exterior data for the flow relaxation
+        scheme (U/Common.py:1193-1308)."""
+        if not self.frs:
+            return
+        data = self.bc_data
+        t_max_index = len(data.t) - 1
+        t0_index = max(0, np.searchsorted(data.t, t) - 1)
+        t1_index = min(t_max_index, np.searchsorted(data.t, t))
+        new_t0, new_t1 = data.t[t0_index], data.t[t1_index]
+        old_t0, old_t1 = self.bc_timestamps
+        self.bc_timestamps = [new_t0, new_t1]
+
+        def pack_ns(d, i):
+            return np.transpose(np.vstack((np.squeeze(d.h[i]), np.squeeze(d.hu[i]), np.squeeze(d.hv[i]))))
+
+        def pack_ew(d, i):
+            return np.transpose(np.vstack((np.squeeze(d.h[i]), np.squeeze(d.hu[i]), np.squeeze(d.hv[i]))))
+
+        for slot, (old, new, idx) in enumerate(((old_t0, new_t0, t0_index), (old_t1, new_t1, t1_index))):
+            if new != old:
+                ns = np.stack([pack_ns(data.south, idx), pack_ns(data.north, idx)]).astype(np.float32)
+                ew = np.stack([pack_ew(data.west, idx), pack_ew(data.east, idx)], axis=1).astype(np.float32)
+                self.bc_ns[slot].upload(gpu_stream, np.ascontiguousarray(ns.reshape(2, -1)))
+                self.bc_ew[slot].upload(gpu_stream, np.ascontiguousarray(ew.reshape(self.ew_ny, -1)))
+        elapsed = t - new_t0
+        interval = max(1.0e-10, (new_t1 - new_t0))
+        self.bc_t = np.float32(max(0.0, min(1.0, elapsed / interval)))
+
+    def _sponge(self, gpu_stream, h, u, v, north, east, south, west):
+        ns0, ns1 = (a.ptr if a is not None else None for a in self.bc_ns)
+        ew0, ew1 = (a.ptr if a is not None else None for a in self.bc_ew)
+        _lib.call("goc_sponge_boundary", int(self.nx), int(self.ny), int(north), int(east), int(south), int(west),
+                  self.sponge_cells.ctypes.data, h.ptr, u.ptr, v.ptr, int(h.pitch), ns0, ns1, self.ns_nx,
+                  ew0, ew1, self.ew_ny, ctypes.c_float(self.bc_t), _stream_handle(gpu_stream))
 
     def boundaryCondition(self, gpu_stream, h, u, v):
         bc = self.boundary_conditions
-        if bc.north == 2 or bc.east == 2:
-            _lib.call("goc_periodic_ghosts", int(self.nx), int(self.ny), int(bc.north), int(bc.east),
-                      h.ptr, u.ptr, v.ptr, int(h.pitch), _stream_handle(gpu_stream))
+        n, e, s, w = int(bc.north), int(bc.east), int(bc.south), int(bc.west)
+        if n == 2:
+            _lib.call("goc_periodic_ghosts", int(self.nx), int(self.ny), 2, 1, h.ptr, u.ptr, v.ptr, int(h.pitch),
+                      _stream_handle(gpu_stream))
+        elif n in (3, 4) or s in (3, 4):
+            self._sponge(gpu_stream, h, u, v, n, 1, s, 1)
+        if e == 2:
+            _lib.call("goc_periodic_ghosts", int(self.nx), int(self.ny), 1, 2, h.ptr, u.ptr, v.ptr, int(h.pitch),
+                      _stream_handle(gpu_stream))
+        elif e in (3, 4) or w in (3, 4):
+            self._sponge(gpu_stream, h, u, v, 1, e, 1, w)
+
+    def release(self):
+        for a in self.bc_ns + self.bc_ew:
+            if a is not None:
+                a.release()
 
 
 class Bathymetry:

@@ -174,6 +174,23 @@ int goc_periodic_ghosts(int nx, int ny, int bc_north, int bc_east,
                         float* eta, float* hu, float* hv, int pitch, void* stream);
 
 /*
+ * Open (sponge) boundaries, BoundaryConditionsArakawaA.boundaryCondition for
+ * flags 3 (flow relaxation scheme) and 4 (linear interpolation)
+ * (U/Common.py:1310-1350, K/boundary_kernels.cu:250-541): north-south first,
+ * then east-west; a periodic pair (flag 2) is skipped here (goc_periodic_ghosts
+ * fills it).  sponge_cells = {north, east, south, west}: rows / columns of the
+ * (ny+4) x (nx+4) array, ghost cells included, that each sponge spans.  The
+ * flow relaxation reads the exterior solution from (2 x ns_nx x 3) float
+ * arrays (row 0 south, row 1 north; channels eta, hu, hv) and
+ * (ew_ny x 2 x 3) arrays (column 0 west, column 1 east), blended as
+ * bc_t * next + (1 - bc_t) * current.  Device memory, pitch in bytes.
+ */
+int goc_sponge_boundary(int nx, int ny, int bc_north, int bc_east, int bc_south, int bc_west,
+                        const int* sponge_cells, float* eta, float* hu, float* hv, int pitch,
+                        const float* ns_current, const float* ns_next, int ns_nx,
+                        const float* ew_current, const float* ew_next, int ew_ny, float bc_t, void* stream);
+
+/*
  * Bathymetry set-up: makes the corner depths periodic or mirrored and
  * computes the cell means.  Replaces U/Common.py:1438-1491,1538-1561:
  * periodic/closed_boundary_intersections_NS/EW (K/boundary_kernels.cu:122-247)

@@ -53,8 +53,9 @@ def _f(x):
 
 def cdklm_defines(nx, ny, dx, dy, g=9.81, r=0.0, theta=1.8, rk_order=2, coriolis_shape=(1, 1),
                   angle_shape=(1, 1), desing_eps=0.1, flux_slope_eps=0.1, depth_cutoff=1e-5,
-                  rho_o=1025.0, wind_stress_factor=1.0, flux_balancer=0.8, block=(12, 32)):
-    """S/CDKLM16.py:242-269 (one_dimensional False, 1x1 wind/pressure)."""
+                  rho_o=1025.0, wind_stress_factor=1.0, flux_balancer=0.8, block=(12, 32),
+                  wind_shape=(1, 1), pressure_shape=(1, 1)):
+    """S/CDKLM16.py:242-269 (one_dimensional False); texture shapes are (ny, nx)."""
     return {"block_width": block[0], "block_height": block[1],
             "KPSIMULATOR_DESING_EPS": _f(desing_eps), "KPSIMULATOR_FLUX_SLOPE_EPS": _f(flux_slope_eps),
             "KPSIMULATOR_DEPTH_CUTOFF": _f(depth_cutoff), "THETA": _f(theta), "RK_ORDER": int(rk_order),
@@ -63,8 +64,9 @@ def cdklm_defines(nx, ny, dx, dy, g=9.81, r=0.0, theta=1.8, rk_order=2, coriolis
             "FLUX_BALANCER": _f(flux_balancer),
             "CORIOLIS_F_NX": int(coriolis_shape[1]), "CORIOLIS_F_NY": int(coriolis_shape[0]),
             "ANGLE_NX": int(angle_shape[1]), "ANGLE_NY": int(angle_shape[0]),
-            "ATMOS_PRES_NX": 1, "ATMOS_PRES_NY": 1,
-            "WIND_STRESS_X_NX": 1, "WIND_STRESS_X_NY": 1, "WIND_STRESS_Y_NX": 1, "WIND_STRESS_Y_NY": 1,
+            "ATMOS_PRES_NX": int(pressure_shape[1]), "ATMOS_PRES_NY": int(pressure_shape[0]),
+            "WIND_STRESS_X_NX": int(wind_shape[1]), "WIND_STRESS_X_NY": int(wind_shape[0]),
+            "WIND_STRESS_Y_NX": int(wind_shape[1]), "WIND_STRESS_Y_NY": int(wind_shape[0]),
             "USE_DIRECT_LOOKUP": "False"}
 
 
@@ -111,6 +113,14 @@ REF_CONFIGS = {
     # GPUDrifterCollection with the default 1x1 wind (D/GPUDrifterCollection.py:70-76)
     "drift": ("driftKernels.cu", {"block_width": 64, "block_height": 1, "WIND_X_NX": 1, "WIND_X_NY": 1,
                                   "WIND_Y_NX": 1, "WIND_Y_NY": 1}, []),
+    # open boundaries: the reference's sponge test grid (T/schemes/CombinedCDKLM16_test.py:43-56) and
+    # boundary kernels for per-cell exterior data along 50 x 70 and 64 x 48 grids
+    "cdklm_sponge50x70": ("CDKLM16_kernel.cu", cdklm_defines(50, 70, 200.0, 200.0), CDKLM_FLAGS),
+    "boundary_data54x74": ("boundary_kernels.cu", {"block_width": 16, "block_height": 16, "BC_NS_NX": 54,
+                                                   "BC_NS_NY": 2, "BC_EW_NX": 2, "BC_EW_NY": 74}, []),
+    # time-varying textured wind stress and atmospheric pressure on a 77 x 45 grid
+    "cdklm_forcing77": ("CDKLM16_kernel.cu", cdklm_defines(77, 45, 150.0, 170.0, wind_shape=(5, 7),
+                                                           pressure_shape=(6, 8)), CDKLM_FLAGS),
     # ModelErrorKL with the default basis (1..10 x 1..10) and with the double-jet case's (2..8 x 1..7)
     "noise_kl10": ("ocean_noise.cu", noise_defines(kl_rand=(10, 20)), NOISE_FLAGS),
     "noise_kl7": ("ocean_noise.cu", noise_defines(kl_rand=(7, 14)), NOISE_FLAGS),
@@ -269,7 +279,8 @@ class RefCDKLM16:
     """
 
     def __init__(self, config, eta0, hu0, hv0, H, nx, ny, dx, dy, dt, g, f, r, ftex, angle_tex,
-                 bc=(1, 1, 1, 1), beta=0.0, courant_number=0.8, block=(12, 32)):
+                 bc=(1, 1, 1, 1), beta=0.0, courant_number=0.8, block=(12, 32), sponge_cells=(0, 0, 0, 0),
+                 bc_data=None, bc_config="boundary", wind=None, pressure=None):
         drv = self.drv = Driver.get()
         self.config = config
         self.nx, self.ny = int(nx), int(ny)
@@ -282,6 +293,18 @@ class RefCDKLM16:
         self.k_step = drv.function(config, "cdklm_swe_2D")
         self.k_bc_ns = drv.function("boundary", "periodicBoundary_NS")
         self.k_bc_ew = drv.function("boundary", "periodicBoundary_EW")
+        # open boundaries (U/Common.py:1121-1400): sponge widths (north, east,
+        # south, west), exterior data {"t": [...], side: [(h, hu, hv), ...]}
+        self.sponge_cells = tuple(int(c) for c in sponge_cells)
+        self.bc_config = bc_config
+        self.bc_data = bc_data
+        self.bc_timestamps = [None, None]
+        self.bc_t = np.float32(0.0)
+        self.bc_arrays = None
+        # time-varying forcing (S/Simulator.py:183-288): (t, [u], [v]) and (t, [P])
+        self.wind, self.pressure = wind, pressure
+        self.wind_stamps, self.pressure_stamps = [None, None], [None, None]
+        self.wind_arrays = self.pressure_arrays = None
         self.k_dt_block = drv.function("max_dt", "per_block_max_dt")
         self.k_dt_reduce = drv.function("max_dt", "max_dt_reduction")
         self.mask_value = np.float32(1.0e20)
@@ -296,6 +319,16 @@ class RefCDKLM16:
         self.h0 = [Array2D(drv, a) for a in (eta0, hu0, hv0)]
         self.h1 = [Array2D(drv, a) for a in (eta0, hu0, hv0)]
         self.ftex = Array2D(drv, np.asarray(ftex, np.float32))
+        if wind is not None:
+            z = np.zeros_like(np.asarray(wind[1][0], np.float32))
+            self.wind_arrays = [Array2D(drv, z) for _ in range(4)]      # x cur, x next, y cur, y next
+        if pressure is not None:
+            z = np.zeros_like(np.asarray(pressure[1][0], np.float32))
+            self.pressure_arrays = [Array2D(drv, z) for _ in range(2)]
+        if bc_data is not None:
+            ns_n, ew_n = len(bc_data["north"][0][0]), len(bc_data["east"][0][0])
+            self.bc_arrays = [Array2D(drv, np.zeros((2, 3 * ns_n), np.float32)) for _ in range(2)] + \
+                [Array2D(drv, np.zeros((ew_n, 6), np.float32)) for _ in range(2)]
         self.angle = Array2D(drv, np.asarray(angle_tex, np.float32))
         self.zero = Array2D(drv, np.zeros((1, 1), np.float32))
         nblocks = self.global_size[0] * self.global_size[1]
@@ -327,43 +360,122 @@ class RefCDKLM16:
                    self.Hi.ptr, self.Hi.pitch, self.mask_value, self.Hm.ptr, self.Hm.pitch)
         drv.synchronize()
 
-    # U/Common.py:1310-1350
+    # U/Common.py:1193-1308
+    def _update_bc_values(self, t):
+        n, e, s, w = self.bc
+        if 3 not in (n, e, s, w):
+            return
+        d = self.bc_data
+        tl = d["t"]
+        i0 = max(0, np.searchsorted(tl, t) - 1)
+        i1 = min(len(tl) - 1, np.searchsorted(tl, t))
+        new = [tl[i0], tl[i1]]
+        old, self.bc_timestamps = self.bc_timestamps, new
+
+        def row(side, i):
+            h, hu, hv = d[side][i]
+            return np.transpose(np.vstack((np.squeeze(h), np.squeeze(hu), np.squeeze(hv))))
+
+        for slot, idx in ((0, i0), (1, i1)):
+            if new[slot] != old[slot]:
+                ns = np.stack([row("south", idx), row("north", idx)]).astype(np.float32)
+                ew = np.stack([row("west", idx), row("east", idx)], axis=1).astype(np.float32)
+                self.bc_arrays[slot].upload(ns.reshape(2, -1))
+                self.bc_arrays[2 + slot].upload(ew.reshape(ew.shape[0], -1))
+        self.bc_t = np.float32(max(0.0, min(1.0, (t - new[0]) / max(1.0e-10, new[1] - new[0]))))
+
+    # U/Common.py:1310-1400
     def _boundary(self, Q):
         drv = self.drv
         bs = (16, 16)
         gs = (_ceil(self.nx + 4 + 1, 16), _ceil(self.ny + 4 + 1, 16))
         h, u, v = Q
-        if self.bc[0] == 2:
-            drv.launch(self.k_bc_ns, "iiiiPiPiPi", gs, bs, self.nx, self.ny, 2, 2,
-                       h.ptr, h.pitch, u.ptr, u.pitch, v.ptr, v.pitch)
-        if self.bc[1] == 2:
+        n, e, s, w = self.bc
+        spn, spe, sps, spw = self.sponge_cells
+        st = (h.ptr, h.pitch, u.ptr, u.pitch, v.ptr, v.pitch)
+        cfg = self.bc_config
+        if n == 2:
+            drv.launch(self.k_bc_ns, "iiiiPiPiPi", gs, bs, self.nx, self.ny, 2, 2, *st)
+        else:
+            if n == 3 or s == 3:
+                drv.launch(drv.function(cfg, "flowRelaxationScheme_NS"), "iiiiiiiiPiPiPiPPf", gs, bs, n, s,
+                           self.nx, self.ny, 2, 2, spn, sps, *st, self.bc_arrays[0].ptr, self.bc_arrays[1].ptr,
+                           self.bc_t)
+            if n == 4 or s == 4:
+                drv.launch(drv.function(cfg, "linearInterpolation_NS"), "iiiiiiiiPiPiPi", gs, bs, n, s,
+                           self.nx, self.ny, 2, 2, spn, sps, *st)
+        if e == 2:
             # periodic_boundary_EW(stream, h, v, u) is called with (h, u, v)
             drv.launch(self.k_bc_ew, "iiiiPiPiPi", gs, bs, self.nx, self.ny, 2, 2,
                        h.ptr, h.pitch, v.ptr, v.pitch, u.ptr, u.pitch)
+        else:
+            if e == 3 or w == 3:
+                drv.launch(drv.function(cfg, "flowRelaxationScheme_EW"), "iiiiiiiiPiPiPiPPf", gs, bs, e, w,
+                           self.nx, self.ny, 2, 2, spe, spw, *st, self.bc_arrays[2].ptr, self.bc_arrays[3].ptr,
+                           self.bc_t)
+            if e == 4 or w == 4:
+                drv.launch(drv.function(cfg, "linearInterpolation_EW"), "iiiiiiiiPiPiPi", gs, bs, e, w,
+                           self.nx, self.ny, 2, 2, spe, spw, *st)
+
+    # S/Simulator.py:183-288
+    @staticmethod
+    def _forcing_t(tl, t, stamps, upload):
+        i0 = max(0, np.searchsorted(tl, t) - 1)
+        i1 = min(len(tl) - 1, np.searchsorted(tl, t))
+        new = [tl[i0], tl[i1]]
+        if new[0] != stamps[0]:
+            upload(i0, 0)
+        if new[1] != stamps[1]:
+            upload(i1, 1)
+        stamps[:] = new
+        return np.float32(max(0.0, min(1.0, (t - new[0]) / max(1.0e-10, new[1] - new[0]))))
+
+    def _forcing(self):
+        wt = pt = np.float32(0.0)
+        if self.wind is not None:
+            tl, us, vs = self.wind
+
+            def up(i, slot):
+                self.wind_arrays[slot].upload(np.asarray(us[i], np.float32))
+                self.wind_arrays[2 + slot].upload(np.asarray(vs[i], np.float32))
+            wt = self._forcing_t(tl, self.t, self.wind_stamps, up)
+        if self.pressure is not None:
+            tl, ps = self.pressure
+
+            def up(i, slot):
+                self.pressure_arrays[slot].upload(np.asarray(ps[i], np.float32))
+            pt = self._forcing_t(tl, self.t, self.pressure_stamps, up)
+        return wt, pt
 
     # S/CDKLM16.py:688-723
-    def _call(self, Qin, Qout, local_dt, rk_step):
+    def _call(self, Qin, Qout, local_dt, rk_step, wind_t=0.0, pressure_t=0.0):
         n, e, s, w = self.bc
         bcs = (n << 24) | (s << 16) | (e << 8) | w
         (hi, ui, vi), (ho, uo, vo) = Qin, Qout
         z = self.zero.ptr
+        pa = [a.ptr for a in self.pressure_arrays] if self.pressure_arrays else [z, z]
+        wa = [a.ptr for a in self.wind_arrays] if self.wind_arrays else [z, z, z, z]
         self.drv.launch(self.k_step, "fiPiPiPiPiPiPiPiPifPPPPfPPPPfi", self.global_size, self.local_size,
                         np.float32(local_dt), rk_step,
                         hi.ptr, hi.pitch, ui.ptr, ui.pitch, vi.ptr, vi.pitch,
                         ho.ptr, ho.pitch, uo.ptr, uo.pitch, vo.ptr, vo.pitch,
                         self.Hi.ptr, self.Hi.pitch, self.Hm.ptr, self.Hm.pitch, self.mask_value,
-                        self.ftex.ptr, self.angle.ptr, z, z, 0.0, z, z, z, z, 0.0, bcs)
+                        self.ftex.ptr, self.angle.ptr, pa[0], pa[1], np.float32(pressure_t),
+                        wa[0], wa[1], wa[2], wa[3], np.float32(wind_t), bcs)
 
     # S/CDKLM16.py:477-584 (RK2, constant forcing)
     def step(self, t_end, noise=None, drifters=None):
         if self.t == 0:
+            self._update_bc_values(self.t)
             self._boundary(self.h0)
         t_now = 0.0
         while t_now < t_end:
             local_dt = np.float32(min(self.dt, np.float32(t_end - t_now)))
-            self._call(self.h0, self.h1, local_dt, 0)
+            wt, pt = self._forcing()
+            self._update_bc_values(self.t)
+            self._call(self.h0, self.h1, local_dt, 0, wt, pt)
             self._boundary(self.h1)
-            self._call(self.h1, self.h0, local_dt, 1)
+            self._call(self.h1, self.h0, local_dt, 1, wt, pt)
             if noise is not None:
                 noise.perturb(self)
             self._boundary(self.h0)
@@ -400,6 +512,8 @@ class RefCDKLM16:
         return self.Hi.download(), self.Hm.download()
 
     def free(self):
+        for a in (self.wind_arrays or []) + (self.pressure_arrays or []) + (self.bc_arrays or []):
+            a.free()
         for a in self.h0 + self.h1 + [self.Hi, self.Hm, self.ftex, self.angle, self.zero, self.dt_blocks,
                                       self.dt_buf]:
             a.free()
