@@ -631,3 +631,63 @@ class BatchedEnsemble:
             cn = s.courant_number if courant_number is None else courant_number
             s.dt = cn * v
         return out
+
+
+def _main(argv=None):
+    """``python -m gpuocean_gb300.ensembles.BatchedEnsemble [--members M]
+    [--nx NX] [--ny NY] [--repeats R]``: M members of the double-jet case on
+    an NX x NY grid stepped one 60 s block, then R launches each of the
+    member moments of (eta, hu, hv) and of one observation of every member
+    at 1000 positions; prints their mean times.  A small, self-contained
+    workload for timing and profiling the statistics kernels."""
+    import argparse
+    import json
+    from ..SWEsimulators import CDKLM16
+    from ..utils import BenchmarkCases
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--members", type=int, default=128)
+    ap.add_argument("--nx", type=int, default=512)
+    ap.add_argument("--ny", type=int, default=300)
+    ap.add_argument("--repeats", type=int, default=5)
+    a = ap.parse_args(argv)
+    ctx = Common.CUDAContext()
+    c = BenchmarkCases.double_jet_case(nx=a.nx, ny=a.ny, dx=5000.0, dy=5000.0, seed=2)
+    b = Common.BoundaryConditions(1, 2, 1, 2)
+    sims = [CDKLM16.CDKLM16(ctx, c["eta0"], c["hu0"], c["hv0"], c["H"], a.nx, a.ny, c["dx"], c["dy"], 0.0, c["g"],
+                            c["f"], 0.0, coriolis_beta=c["coriolis_beta"], boundary_conditions=b)
+            for _ in range(a.members)]
+    ens = BatchedEnsemble(sims, autotune=False)
+    ens.step(60.0)
+    m, v = ens.moments(download=False)
+    rng = np.random.default_rng(0)
+    pos = np.stack([rng.uniform(0, a.nx * c["dx"], 1000), rng.uniform(0, a.ny * c["dy"], 1000)], axis=1)
+    ens.observe(pos)
+    ev = [ctypes.c_void_p() for _ in range(3)]
+    for e in ev:
+        _lib.call("goc_event_create", ctypes.byref(e))
+    st = ens.stream.handle
+    _lib.call("goc_event_record", ev[0], st)
+    for _ in range(a.repeats):
+        _lib.call("goc_ensemble_moments", ens._handle, 0, a.members, 0, ctypes.c_float(0.0), 0, m.ptr, v.ptr, st)
+    _lib.call("goc_event_record", ev[1], st)
+    for _ in range(a.repeats):
+        _lib.call("goc_ensemble_observe", ens._handle, 0, a.members, ens._obs_pos.ptr, 8, ctypes.c_longlong(0), 1000,
+                  ens._obs_out.ptr, st)
+    _lib.call("goc_event_record", ev[2], st)
+    ens.synchronize()
+    t = [ctypes.c_float(), ctypes.c_float()]
+    _lib.call("goc_event_elapsed_ms", ev[0], ev[1], ctypes.byref(t[0]))
+    _lib.call("goc_event_elapsed_ms", ev[1], ev[2], ctypes.byref(t[1]))
+    cells = a.members * a.nx * a.ny
+    print(json.dumps({"members": a.members, "nx": a.nx, "ny": a.ny, "moments_ms": t[0].value / a.repeats,
+                      "moments_gbs": (12 * cells + 24 * a.nx * a.ny) / (t[0].value / a.repeats * 1e-3) / 1e9,
+                      "observe_ms": t[1].value / a.repeats}))
+    for e in ev:
+        _lib.load().goc_event_destroy(e)
+    m.free()
+    v.free()
+    ens.release()
+
+
+if __name__ == "__main__":
+    _main()
