@@ -58,36 +58,6 @@ def dist_env():
     return rank, world, local
 
 
-class Dist:
-    """Barrier and max-reduction across torchrun ranks (no-op for one rank)."""
-
-    def __init__(self, world, backend):
-        self.world = world
-        self.pg = None
-        if world > 1:
-            import torch.distributed as td
-            td.init_process_group(backend=backend)
-            self.td = td
-
-    def barrier(self):
-        if self.world > 1:
-            self.td.barrier()
-
-    def max(self, v):
-        if self.world == 1:
-            return v
-        import torch
-        t = torch.tensor([float(v)], dtype=torch.float64)
-        if self.td.get_backend() == "nccl":
-            t = t.cuda()
-        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
-        return float(t.item())
-
-    def close(self):
-        if self.world > 1:
-            self.td.destroy_process_group()
-
-
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons during the timed region."""
 
@@ -614,7 +584,8 @@ def main():
     from gpuocean_gb300 import _lib
     from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
     from gpuocean_gb300.utils import Common
-    dist = Dist(world, "nccl" if world > 1 else "gloo")
+    from gpuocean_gb300.utils.replicas import ReplicaGroup
+    dist = ReplicaGroup(world, "nccl" if world > 1 else "gloo", rank=rank)
     ctx = Common.CUDAContext(device=local)
     case = make_case(spec)
     sims = build_members(ctx, spec, case)
@@ -654,7 +625,8 @@ def main():
     _lib.call("goc_event_elapsed_ms", ev[0], ev[1], ctypes.byref(ms))
     elapsed = dist.max(ms.value / 1000.0)
     launches = ens.kernels_launched - launches0
-    value = cells * world / elapsed
+    # replicas: every rank runs the whole workload on its own GPU
+    value = dist.throughput(cells, ms.value / 1000.0)
 
     # dominant kernel: per-launch CUDA-event times of the RK2 ensemble kernel
     # on the launching stream, over a few eager blocks
@@ -740,7 +712,7 @@ def main():
                           8 * (n_d + 1), stream)
         ens.synchronize()
         e2e_wall = time.perf_counter() - t0
-        e2e = {"value": e2e_cells * world / dist.max(e2e_wall), "unit": "member-cell-steps/s",
+        e2e = {"value": dist.throughput(e2e_cells, e2e_wall), "unit": "member-cell-steps/s",
                "h2d_bytes_per_step": in_obs + in_rand, "d2h_bytes_per_step": out_bytes}
         _lib.call("goc_host_free", host_in)
         _lib.call("goc_host_free", host_out)
