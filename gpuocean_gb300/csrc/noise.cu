@@ -220,23 +220,21 @@ __device__ float bicubic_value(const GocNoiseDesc& d, const OceanRef& o, int ti,
     return bicubic_eval(A, rx, ry);
 }
 
-// Perturbation of interior cell (ti, tj).  `factor1`: the coarse grid is the
-// computational grid (geostrophicBalance, the state's own depth in h and land
-// cells zeroed); otherwise bicubic up-sampling (bicubicInterpolation, land
-// cells unperturbed).  `de(jj, ii)` gives the perturbation of eta.
+// Perturbation of interior cell (ti, tj) from its state (e, u, v) and corner
+// depths hc = (Hi[tj][ti], Hi[tj][ti+1], Hi[tj+1][ti], Hi[tj+1][ti+1]).
+// `factor1`: the coarse grid is the computational grid (geostrophicBalance,
+// the state's own depth in h and land cells zeroed); otherwise bicubic
+// up-sampling (bicubicInterpolation, land cells unperturbed).  `de(jj, ii)`
+// gives the perturbation of eta.
 template <typename DE>
 __device__ __forceinline__ void perturb_cell(const GocNoiseDesc& d, const OceanRef& o, int ti, int tj, bool factor1,
-                                             DE de) {
-    const float* h0 = o.Hi + (size_t)tj * o.hi_pitch + ti;
-    const float* h1 = h0 + o.hi_pitch;
-    const bool dry = (h0[0] == o.land) || (h0[1] == o.land) || (h1[0] == o.land) || (h1[1] == o.land);
-    const float H_mid = 0.25f * (h0[0] + h0[1] + h1[0] + h1[1]);
+                                             DE de, float e, float u, float v, const float* hc) {
+    const bool dry = (hc[0] == o.land) || (hc[1] == o.land) || (hc[2] == o.land) || (hc[3] == o.land);
+    const float H_mid = 0.25f * (hc[0] + hc[1] + hc[2] + hc[3]);
     const float cor = noise_coriolis(d, o, ti, tj);
     const float dc = de(tj, ti);
     const float ex = (de(tj, ti + 1) - de(tj, ti - 1)) / (2.0f * o.dx);
     const float ey = (de(tj + 1, ti) - de(tj - 1, ti)) / (2.0f * o.dy);
-    const size_t k = (size_t)tj * o.pitch + ti;
-    float e = o.eta[k], u = o.hu[k], v = o.hv[k];
     if (factor1) {
         const float h_mid = dc + H_mid + e;
         const float dhu = -(d.g / cor) * h_mid * ey;
@@ -254,51 +252,80 @@ __device__ __forceinline__ void perturb_cell(const GocNoiseDesc& d, const OceanR
     store_cell(o, ti, tj, e, u, v);
 }
 
-constexpr int kNB = 16;  // noise tile edge
-constexpr int kNC = 10;  // coarse cells per tile edge held in shared memory (enough for factor >= 2)
+constexpr int kNB = 16;                            // SOAR tile edge (coarse cells)
+constexpr int kPX = 32, kPY = 32, kPT = 8;          // transfer tile (fine cells) and thread rows
+constexpr int kPR = kPY / kPT;                      // cells per thread
+constexpr int kNC = 12;  // coarse cells per tile edge held in shared memory (factor >= 4 for 34 fine cells)
 
-// One 16x16 tile of interior cells (tile origin bx, by in interior cells).
+// One kPX x kPY tile of interior cells (tile origin bx, by in interior
+// cells).  Each thread owns kPR cells of one column; their state and corner
+// depths are loaded first so that the loads overlap the perturbation field.
 __device__ void perturb_tile(const GocNoiseDesc& d, const OceanRef& o, int bx, int by) {
-    __shared__ float s_de[kNB + 2][kNB + 2];
+    __shared__ float s_de[kPY + 2][kPX + 2];
     __shared__ float s_A[kNC * kNC][17];
-    const int tx = threadIdx.x, ty = threadIdx.y, t = ty * kNB + tx;
+    const int tx = threadIdx.x, t = threadIdx.y * kPX + tx;
+    constexpr int NT = kPX * kPT;
     const bool factor1 = d.interpolation_factor <= 1;
+    const int ti = 2 + bx + tx;
+    float q[kPR][3], hc[kPR][4];
+#pragma unroll
+    for (int r = 0; r < kPR; ++r) {
+        const int tj = 2 + by + threadIdx.y + r * kPT;
+        q[r][0] = q[r][1] = q[r][2] = 0.0f;
+        hc[r][0] = hc[r][1] = hc[r][2] = hc[r][3] = 0.0f;
+        if (ti < o.nx + 2 && tj < o.ny + 2) {
+            const size_t k = (size_t)tj * o.pitch + ti;
+            q[r][0] = o.eta[k];
+            q[r][1] = o.hu[k];
+            q[r][2] = o.hv[k];
+            const float* h0 = o.Hi + (size_t)tj * o.hi_pitch + ti;
+            hc[r][0] = h0[0];
+            hc[r][1] = h0[1];
+            hc[r][2] = h0[o.hi_pitch];
+            hc[r][3] = h0[o.hi_pitch + 1];
+        }
+    }
     // d_eta on the tile + 1 ring (interior origin at ghost offset 2)
     const int gi0 = 2 + bx - 1, gj0 = 2 + by - 1;
+    constexpr int NR = (kPY + 2) * (kPX + 2);
     if (factor1) {
-        for (int j = ty; j < kNB + 2; j += kNB)
-            for (int i = tx; i < kNB + 2; i += kNB) s_de[j][i] = coarse_at(d, gj0 + j, gi0 + i);
+        for (int c = t; c < NR; c += NT) s_de[c / (kPX + 2)][c % (kPX + 2)] = coarse_at(d, gj0 + c / (kPX + 2),
+                                                                                          gi0 + c % (kPX + 2));
     } else {
         // the coarse cells under the tile: the index is monotone in the fine index
         float r;
-        const int ci0 = bicubic_ci(d, o, gi0, &r), ci1 = bicubic_ci(d, o, gi0 + kNB + 1, &r);
-        const int cj0 = bicubic_cj(d, o, gj0, &r), cj1 = bicubic_cj(d, o, gj0 + kNB + 1, &r);
+        const int ci0 = bicubic_ci(d, o, gi0, &r), ci1 = bicubic_ci(d, o, gi0 + kPX + 1, &r);
+        const int cj0 = bicubic_cj(d, o, gj0, &r), cj1 = bicubic_cj(d, o, gj0 + kPY + 1, &r);
         const int ncx = ci1 - ci0 + 1, ncy = cj1 - cj0 + 1;
         if (ncx <= kNC && ncy <= kNC) {
-            for (int c = t; c < ncx * ncy; c += kNB * kNB) bicubic_coeffs(d, ci0 + c % ncx, cj0 + c / ncx, s_A[c]);
+            for (int c = t; c < ncx * ncy; c += NT) bicubic_coeffs(d, ci0 + c % ncx, cj0 + c / ncx, s_A[c]);
             __syncthreads();
-            for (int j = ty; j < kNB + 2; j += kNB)
-                for (int i = tx; i < kNB + 2; i += kNB) {
-                    float rx, ry;
-                    const int ci = bicubic_ci(d, o, gi0 + i, &rx), cj = bicubic_cj(d, o, gj0 + j, &ry);
-                    const int a = clampi(cj - cj0, 0, ncy - 1) * ncx + clampi(ci - ci0, 0, ncx - 1);
-                    s_de[j][i] = bicubic_eval(s_A[a], rx, ry);
-                }
+            for (int c = t; c < NR; c += NT) {
+                const int j = c / (kPX + 2), i = c % (kPX + 2);
+                float rx, ry;
+                const int ci = bicubic_ci(d, o, gi0 + i, &rx), cj = bicubic_cj(d, o, gj0 + j, &ry);
+                const int a = clampi(cj - cj0, 0, ncy - 1) * ncx + clampi(ci - ci0, 0, ncx - 1);
+                s_de[j][i] = bicubic_eval(s_A[a], rx, ry);
+            }
         } else {
-            for (int j = ty; j < kNB + 2; j += kNB)
-                for (int i = tx; i < kNB + 2; i += kNB) s_de[j][i] = bicubic_value(d, o, gi0 + i, gj0 + j);
+            for (int c = t; c < NR; c += NT)
+                s_de[c / (kPX + 2)][c % (kPX + 2)] = bicubic_value(d, o, gi0 + c % (kPX + 2), gj0 + c / (kPX + 2));
         }
     }
     __syncthreads();
-    const int ti = 2 + bx + tx, tj = 2 + by + ty;
-    if (ti < o.nx + 2 && tj < o.ny + 2)
-        perturb_cell(d, o, ti, tj, factor1,
-                     [&](int jj, int ii) { return s_de[jj - (2 + by) + 1][ii - (2 + bx) + 1]; });
+#pragma unroll
+    for (int r = 0; r < kPR; ++r) {
+        const int tj = 2 + by + threadIdx.y + r * kPT;
+        if (ti < o.nx + 2 && tj < o.ny + 2)
+            perturb_cell(d, o, ti, tj, factor1,
+                         [&](int jj, int ii) { return s_de[jj - (2 + by) + 1][ii - (2 + bx) + 1]; },
+                         q[r][0], q[r][1], q[r][2], hc[r]);
+    }
     __syncthreads();
 }
 
-__global__ void perturb_kernel(GocNoiseDesc d, OceanRef o) {
-    perturb_tile(d, o, blockIdx.x * kNB, blockIdx.y * kNB);
+__global__ void __launch_bounds__(kPX * kPT, 3) perturb_kernel(GocNoiseDesc d, OceanRef o) {
+    perturb_tile(d, o, blockIdx.x * kPX, blockIdx.y * kPY);
 }
 
 // ---------------------------------------------------------------------------
@@ -327,7 +354,7 @@ __global__ void soar_batched_active_kernel(const GocNoiseDesc* __restrict__ nd, 
     soar_cell(d, scale, 0, it.y * kNB + threadIdx.x, it.z * kNB + threadIdx.y, d.random, d.coarse);
 }
 
-__global__ void perturb_batched_kernel(const GocNoiseDesc* __restrict__ nd, const GocMemberDesc* __restrict__ mem,
+__global__ void __launch_bounds__(kPX * kPT, 3) perturb_batched_kernel(const GocNoiseDesc* __restrict__ nd, const GocMemberDesc* __restrict__ mem,
                                        const int4* __restrict__ items, const int* __restrict__ nsub, int substep) {
     const int4 it = items[blockIdx.x];
     int set;
@@ -335,7 +362,7 @@ __global__ void perturb_batched_kernel(const GocNoiseDesc* __restrict__ nd, cons
     const GocMemberDesc& m = mem[it.x];
     const OceanRef o{m.p.nx, m.p.ny, m.p.dx, m.p.dy, m.eta[set], m.hu[set], m.hv[set], m.pitch / 4, m.Hi,
                      m.Hi_pitch / 4, m.p.land_value, m.p.bc_north == 2, m.p.bc_east == 2};
-    perturb_tile(nd[it.x], o, it.y * kNB, it.z * kNB);
+    perturb_tile(nd[it.x], o, it.y * kPX, it.z * kPY);
 }
 
 // XORWOW normals for every member's random field; one state per element.
@@ -649,7 +676,7 @@ extern "C" int goc_perturb_ocean(const GocNoiseDesc* d, int nx, int ny, float dx
     if ((rc = make_ocean(nx, ny, dx, dy, eta, hu, hv, pitch, Hi, Hi_pitch, land_value,
                          periodic_ghosts && d->periodic_ns, periodic_ghosts && d->periodic_ew, &o, "goc_perturb_ocean")))
         return rc;
-    dim3 blk(kNB, kNB), grd((nx + kNB - 1) / kNB, (ny + kNB - 1) / kNB);
+    dim3 blk(kPX, kPT), grd((nx + kPX - 1) / kPX, (ny + kPY - 1) / kPY);
     perturb_kernel<<<grd, blk, 0, as_stream(stream)>>>(*d, o);
     count_launch();
     return check_launch("perturb_kernel");
@@ -690,8 +717,8 @@ extern "C" int goc_noise_batch_create(void* ensemble, const GocNoiseDesc* noise,
         }
         for (int j = 0; j < (noise[m].coarse_ny + 4 + kNB - 1) / kNB; ++j)
             for (int i = 0; i < (noise[m].coarse_nx + 4 + kNB - 1) / kNB; ++i) soar.push_back(make_int4(m, i, j, 0));
-        for (int j = 0; j < (md.p.ny + kNB - 1) / kNB; ++j)
-            for (int i = 0; i < (md.p.nx + kNB - 1) / kNB; ++i) pert.push_back(make_int4(m, i, j, 0));
+        for (int j = 0; j < (md.p.ny + kPY - 1) / kPY; ++j)
+            for (int i = 0; i < (md.p.nx + kPX - 1) / kPX; ++i) pert.push_back(make_int4(m, i, j, 0));
         const int rnx = noise[m].periodic_ew ? noise[m].coarse_nx : noise[m].coarse_nx + 8;
         const int rny = noise[m].periodic_ns ? noise[m].coarse_ny : noise[m].coarse_ny + 8;
         for (int f = 0; f < rnx * rny; f += 256) {
@@ -769,7 +796,7 @@ extern "C" int goc_noise_batch_perturb(void* batch, void* ensemble, float pertur
     count_launch();
     int rc = check_launch("soar_batched_active_kernel");
     if (rc) return rc;
-    perturb_batched_kernel<<<b->n_pert, dim3(kNB, kNB), 0, st>>>(b->d_noise, ensemble_device_members(ensemble),
+    perturb_batched_kernel<<<b->n_pert, dim3(kPX, kPT), 0, st>>>(b->d_noise, ensemble_device_members(ensemble),
                                                                   b->d_pert_items, nsub, substep);
     count_launch();
     return check_launch("perturb_batched_kernel");
