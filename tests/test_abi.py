@@ -48,3 +48,46 @@ def test_argument_validation_without_gpu():
     assert lib.goc_max_dt_partials(256, 256) == 8 * 32
     rc = lib.goc_max_dt(8, 8, 1.0, 1.0, 9.8, None, None, None, 48, None, 48, 1e20, None, 0, None, None)
     assert rc == -1
+
+
+def test_new_entry_points_validate_without_gpu():
+    """Observation, statistics, KL and sponge entries reject bad arguments
+    before any CUDA call."""
+    import numpy as np
+    lib = _lib.load()
+    # observation operator: empty grid, bad pitch; zero drifters is a no-op
+    assert lib.goc_observe_underlying_flow(0, 4, 1.0, 1.0, 2, 2, None, 0, None, 0, None, 0, 1.0, 3, None, 8, None, 8,
+                                           None) == -1
+    assert lib.goc_observe_underlying_flow(4, 4, 1.0, 1.0, 2, 2, None, 0, 1, 4, 1, 4, 1.0, 3, 1, 8, 1, 8, None) == -1
+    assert "pitch" in _lib.last_error()
+    assert lib.goc_observe_underlying_flow(4, 4, 1.0, 1.0, 2, 2, None, 0, None, 0, None, 0, 1.0, 0, None, 8, None, 8,
+                                           None) == 0
+    # ensemble statistics need a handle; the multi-level assembly checks its levels
+    assert lib.goc_ensemble_observe(None, 0, 1, 1, 8, 0, 1, 1, None) == -1
+    assert lib.goc_ensemble_moments(None, 0, 1, 0, 0.0, 0, 1, 1, None) == -1
+    fine = (ctypes.c_void_p * 2)(1, 1)
+    coarse = (ctypes.c_void_p * 2)(None, 1)
+    nx = np.array([6, 13], np.int32)   # 13 is not twice 6
+    ny = np.array([4, 8], np.int32)
+    assert lib.goc_ml_combine(2, fine, coarse, nx.ctypes.data, ny.ctypes.data, 3, 1, None) == -1
+    assert "coarsened" in _lib.last_error()
+    assert lib.goc_ml_combine(9, fine, coarse, nx.ctypes.data, ny.ctypes.data, 3, 1, None) == -1
+    # KL: table size from the basis; empty basis ranges are rejected
+    from gpuocean_gb300.SWEsimulators.ModelErrorKL import GocKLDesc
+    d = GocKLDesc()
+    d.basis_x_start, d.basis_x_end, d.basis_y_start, d.basis_y_end = 2, 8, 1, 7
+    assert lib.goc_kl_table_floats(512, 300, ctypes.byref(d)) == 2 * 7 * (514 + 302)
+    d.basis_y_end = 0
+    assert lib.goc_kl_table_floats(512, 300, ctypes.byref(d)) < 0
+    assert lib.goc_kl_perturb(ctypes.byref(d), 8, 8, 1.0, 1.0, 1.0, 1, 1, None, None, 48, None, 0, 0, 0, None) == -1
+    # sponges: flow relaxation needs exterior data, linear interpolation sponge cells
+    cells = np.array([4, 0, 4, 0], np.int32)
+    assert lib.goc_sponge_boundary(8, 8, 3, 1, 3, 1, cells.ctypes.data, 1, 1, 1, 48, None, None, 2, None, None, 2,
+                                   0.0, None) == -1
+    assert "exterior" in _lib.last_error()
+    cells0 = np.zeros(4, np.int32)
+    assert lib.goc_sponge_boundary(8, 8, 4, 1, 4, 1, cells0.ctypes.data, 1, 1, 1, 48, None, None, 2, None, None, 2,
+                                   0.0, None) == -1
+    big = np.array([99, 0, 0, 0], np.int32)
+    assert lib.goc_sponge_boundary(8, 8, 4, 1, 1, 1, big.ctypes.data, 1, 1, 1, 48, None, None, 2, None, None, 2,
+                                   0.0, None) == -1
