@@ -371,6 +371,36 @@ def run_statistics(ens, sims, peak, peak_kind, n_positions=1000, repeats=10):
     return out
 
 
+def run_c2(ctx, days=10.0):
+    """The double jet of one simulator for `days` of simulated time (512 x 300,
+    dx = dy = 5 km, periodic x, walls y, beta plane, 230 m + 10 m random
+    bathymetry): dt from updateDt at Courant 0.8, kept fixed; the model is
+    stepped through the public API (CDKLM16.step, one fused RK2 launch per
+    step), one hour per call; wall time on the host around the whole run."""
+    from gpuocean_gb300.SWEsimulators import CDKLM16
+    from gpuocean_gb300.utils import BenchmarkCases, Common
+    c = BenchmarkCases.double_jet_case(nx=512, ny=300)
+    sim = CDKLM16.CDKLM16(ctx, c["eta0"], c["hu0"], c["hv0"], c["H"], 512, 300, c["dx"], c["dy"], 0.0, c["g"], c["f"],
+                          c["r"], coriolis_beta=c["coriolis_beta"],
+                          boundary_conditions=Common.BoundaryConditions(*c["boundary"]))
+    sim.updateDt(courant_number=0.8)
+    sim.step(3600.0)
+    sim.gpu_stream.synchronize()
+    t_end = days * 86400.0
+    t0 = time.perf_counter()
+    steps0 = sim.num_iterations
+    while sim.t < t_end - 1e-6:
+        sim.step(min(3600.0, t_end - sim.t))
+    sim.gpu_stream.synchronize()
+    wall = time.perf_counter() - t0
+    steps = sim.num_iterations - steps0
+    eta = np.asarray(sim.download(interior_domain_only=True)[0])
+    out = {"config": f"double jet 512x300, {days:g} days, dt {float(sim.dt):.3f} s fixed", "steps": int(steps),
+           "wall_s": wall, "cell_steps_per_s": steps * 512 * 300 / wall, "finite": bool(np.isfinite(eta).all())}
+    sim.cleanUp()
+    return out
+
+
 def run_kl(ens, sims, peak, peak_kind, repeats=10):
     """Karhunen-Loeve model error on the C3 ensemble (every member at
     512 x 300) with the double-jet case's KL parameters (basis 2..8 x 1..7,
@@ -574,6 +604,7 @@ def main():
     ap.add_argument("--no-multilevel", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-statistics", action="store_true")
+    ap.add_argument("--no-c2", action="store_true")
     args = ap.parse_args()
     rank, world, local = dist_env()
     spec = workload_spec(args.workload, args.members if args.workload == "c3" else 1)
@@ -701,15 +732,13 @@ def main():
         e2e_cells = 0
         t0 = time.perf_counter()
         for b in range(e2e_steps):
-            for m, s in enumerate(sims):
-                _lib.call("goc_memcpy_h2d_async", s.drifters.driftersDevice.ptr + 8 * n_d, host_in.value + 8 * m,
-                          8, stream)
+            # one copy of all observation positions, scattered on the device
+            ens.upload_observation_positions(host_in.value)
             if noise:
                 _lib.call("goc_memcpy_h2d_async", pool.ptr, host_in.value + in_obs + b * in_rand, in_rand, stream)
             e2e_cells += ens.step(MODEL_TIME_STEP, apply_stochastic_term=noise)
-            for m, s in enumerate(sims):
-                _lib.call("goc_memcpy_d2h_async", host_out.value + 8 * (n_d + 1) * m, s.drifters.driftersDevice.ptr,
-                          8 * (n_d + 1), stream)
+            # every member's drifters gathered on the device, one copy back
+            ens.download_drifters(host_out.value)
         ens.synchronize()
         e2e_wall = time.perf_counter() - t0
         e2e = {"value": dist.throughput(e2e_cells, e2e_wall), "unit": "member-cell-steps/s",
@@ -744,6 +773,7 @@ def main():
 
     ens_stats = None if args.no_statistics else run_statistics(ens, sims, *measured_peaks())
     kl = None if args.no_statistics else run_kl(ens, sims, *measured_peaks())
+    c2 = None if args.no_c2 else run_c2(ctx)
     multilevel = None if args.no_multilevel else run_multilevel(ctx, args)
     adjoint = None if args.no_adjoint else run_adjoint(ctx)
 
@@ -781,7 +811,7 @@ def main():
                          "peak_kind": peak_kind, "avg_launch_ms": 1000.0 * avg_dur,
                          "algorithmic_bytes_per_launch": avg_bytes},
             "e2e": e2e, "gpu_launches": launches, "clocks": clk, "cpu_baseline": cpu,
-            "multilevel": multilevel, "adjoint": adjoint, "statistics": ens_stats, "kl_model_error": kl,
+            "multilevel": multilevel, "adjoint": adjoint, "statistics": ens_stats, "kl_model_error": kl, "c2_ten_days": c2,
             "wall_s": wall,
         }
         print(json.dumps(line), flush=True)

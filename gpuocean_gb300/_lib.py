@@ -118,6 +118,9 @@ SIGNATURES = {
     "goc_kl_batch_set_rollers": (c_int, [c_void_p, c_void_p, c_int, c_void_p]),
     "goc_kl_batch_set_random": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "goc_kl_batch_perturb": (c_int, [c_void_p, c_void_p, c_float, c_int, c_void_p]),
+    "goc_ensemble_drifter_rows": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "goc_ensemble_gather_drifters": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "goc_ensemble_scatter_observations": (c_int, [c_void_p, c_void_p, c_void_p]),
     "goc_observe_underlying_flow": (c_int, [c_int, c_int, c_float, c_float, c_int, c_int, c_void_p, c_int, c_void_p,
                                             c_int, c_void_p, c_int, c_float, c_int, c_void_p, c_int, c_void_p, c_int,
                                             c_void_p]),

@@ -2,6 +2,7 @@
 // advances in one persistent launch per RK2 step over a member/tile work
 // queue, instead of one Python-driven launch sequence per member
 // (E/OceanNoiseEnsemble.py:517-543, E/MultiLevelOceanEnsemble.py:95-141).
+#include <climits>
 #include <cstdio>
 
 #include "ensemble.cuh"
@@ -81,6 +82,7 @@ static void free_ensemble(Ensemble* e) {
     cudaFree(e->d_partials);
     cudaFree(e->d_drift_pos);
     cudaFree(e->d_drift_chunks);
+    cudaFree(e->d_drift_n);
     delete e;
 }
 
@@ -328,21 +330,32 @@ extern "C" int goc_ensemble_set_drifters(void* ensemble, float* const* positions
     if (!ensemble || !positions || !num_drifters) return set_error(GOC_ERR_ARG, "goc_ensemble_set_drifters: null argument");
     Ensemble* e = static_cast<Ensemble*>(ensemble);
     std::vector<int4> chunks;
+    std::vector<int> nd(e->n_members, 0);
+    long long packed = 0;
     for (int m = 0; m < e->n_members; ++m) {
         if (!positions[m]) continue;
         if (num_drifters[m] < 0) return set_error(GOC_ERR_ARG, "goc_ensemble_set_drifters: negative count");
+        nd[m] = num_drifters[m];
         const int n = num_drifters[m] + 1;  // with the observation row
-        for (int f = 0; f < n; f += kDriftChunk) chunks.push_back(make_int4(m, f, std::min(kDriftChunk, n - f), 0));
+        if (packed + n > INT_MAX) return set_error(GOC_ERR_ARG, "goc_ensemble_set_drifters: too many drifters");
+        for (int f = 0; f < n; f += kDriftChunk)
+            chunks.push_back(make_int4(m, f, std::min(kDriftChunk, n - f), (int)(packed + f)));
+        packed += n;
     }
     cudaStream_t st = as_stream(stream);
     cudaError_t err = cudaStreamSynchronize(st);
     cudaFree(e->d_drift_pos);
     cudaFree(e->d_drift_chunks);
+    cudaFree(e->d_drift_n);
     e->d_drift_pos = nullptr;
     e->d_drift_chunks = nullptr;
+    e->d_drift_n = nullptr;
     e->n_drift_chunks = 0;
+    e->drift_rows = 0;
     if (err == cudaSuccess) err = cudaMalloc(&e->d_drift_pos, sizeof(float*) * e->n_members);
     if (err == cudaSuccess) err = cudaMemcpy(e->d_drift_pos, positions, sizeof(float*) * e->n_members, cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMalloc(&e->d_drift_n, sizeof(int) * e->n_members);
+    if (err == cudaSuccess) err = cudaMemcpy(e->d_drift_n, nd.data(), sizeof(int) * e->n_members, cudaMemcpyHostToDevice);
     if (err == cudaSuccess && !chunks.empty()) {
         err = cudaMalloc(&e->d_drift_chunks, sizeof(int4) * chunks.size());
         if (err == cudaSuccess)
@@ -350,6 +363,56 @@ extern "C" int goc_ensemble_set_drifters(void* ensemble, float* const* positions
     }
     if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_ensemble_set_drifters: %s", cudaGetErrorString(err));
     e->n_drift_chunks = (int)chunks.size();
+    e->drift_rows = packed;
     e->drift_sensitivity = sensitivity;
     return GOC_OK;
+}
+
+namespace goc {
+// every member's drifter rows (positions and observation row) into one
+// packed array, in member order
+__global__ void ensemble_gather_drifters_kernel(float* const* __restrict__ pos, const int4* __restrict__ chunks,
+                                                float* __restrict__ dst) {
+    const int4 c = chunks[blockIdx.x];
+    const float* src = pos[c.x];
+    for (int q = threadIdx.x; q < 2 * c.z; q += blockDim.x) dst[2 * (size_t)c.w + q] = src[2 * (size_t)c.y + q];
+}
+
+// observation row of every member with drifters from an (n_members x 2) array
+__global__ void ensemble_scatter_observations_kernel(float* const* __restrict__ pos, const int* __restrict__ nd,
+                                                     int n, const float* __restrict__ src) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n || !pos[m]) return;
+    float* row = pos[m] + 2 * (size_t)nd[m];
+    row[0] = src[2 * m];
+    row[1] = src[2 * m + 1];
+}
+}  // namespace goc
+
+extern "C" int goc_ensemble_drifter_rows(void* ensemble, long long* rows) {
+    if (!ensemble || !rows) return set_error(GOC_ERR_ARG, "goc_ensemble_drifter_rows: null argument");
+    *rows = static_cast<Ensemble*>(ensemble)->drift_rows;
+    return GOC_OK;
+}
+
+extern "C" int goc_ensemble_gather_drifters(void* ensemble, float* dst, void* stream) {
+    if (!ensemble) return set_error(GOC_ERR_ARG, "goc_ensemble_gather_drifters: null ensemble");
+    Ensemble* e = static_cast<Ensemble*>(ensemble);
+    if (e->n_drift_chunks == 0) return GOC_OK;
+    if (!dst) return set_error(GOC_ERR_ARG, "goc_ensemble_gather_drifters: null destination");
+    ensemble_gather_drifters_kernel<<<e->n_drift_chunks, 256, 0, as_stream(stream)>>>(e->d_drift_pos,
+                                                                                     e->d_drift_chunks, dst);
+    count_launch();
+    return check_launch("ensemble_gather_drifters_kernel");
+}
+
+extern "C" int goc_ensemble_scatter_observations(void* ensemble, const float* src, void* stream) {
+    if (!ensemble) return set_error(GOC_ERR_ARG, "goc_ensemble_scatter_observations: null ensemble");
+    Ensemble* e = static_cast<Ensemble*>(ensemble);
+    if (!e->d_drift_pos) return GOC_OK;
+    if (!src) return set_error(GOC_ERR_ARG, "goc_ensemble_scatter_observations: null source");
+    ensemble_scatter_observations_kernel<<<(e->n_members + 127) / 128, 128, 0, as_stream(stream)>>>(
+        e->d_drift_pos, e->d_drift_n, e->n_members, src);
+    count_launch();
+    return check_launch("ensemble_scatter_observations_kernel");
 }

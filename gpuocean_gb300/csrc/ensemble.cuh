@@ -43,8 +43,10 @@ struct Ensemble {
     float* d_partials = nullptr;          // CFL scratch
     // drifters: one (N_m + 1) x 2 position array per member
     float** d_drift_pos = nullptr;        // per member, null = no drifters
-    int4* d_drift_chunks = nullptr;       // (member, first drifter, count, 0)
+    int4* d_drift_chunks = nullptr;       // (member, first row, count, packed row of the first row)
     int n_drift_chunks = 0;
+    int* d_drift_n = nullptr;             // drifters per member (the observation row is row n)
+    long long drift_rows = 0;             // rows of all members' position arrays, packed
     float drift_sensitivity = 1.0f;
     int shape = 0;                        // index into kEnsembleShapes
 };

@@ -220,7 +220,7 @@ class BatchedEnsemble:
 
     def _release_handles(self):
         self.release_noise()
-        for name in ("_obs_pos", "_obs_out"):
+        for name in ("_obs_pos", "_obs_out", "_drift_gather", "_obs_scatter"):
             buf = getattr(self, name, None)
             if buf is not None:
                 buf.free()
@@ -583,6 +583,47 @@ class BatchedEnsemble:
                   out.ptr, self.stream.handle)
         self.kernels_launched += _lib.load().goc_kernel_launch_count() - before
         return self._download(out, (count, D, 3))
+
+    def drifter_rows(self):
+        """Rows of all members' drifter arrays (N_m positions and the
+        observation row each), the size of download_drifters' result."""
+        rows = ctypes.c_longlong()
+        _lib.call("goc_ensemble_drifter_rows", self._handle, ctypes.byref(rows))
+        return rows.value
+
+    def download_drifters(self, out=None):
+        """Every member's drifter rows, member by member, as one (rows, 2)
+        float32 array: one gather launch and one copy instead of a download
+        per collection.  out: a host array to fill (pinned memory makes the
+        copy asynchronous to the host) or its address as an int."""
+        self._ensure_table()
+        rows = self.drifter_rows()
+        buf = self._scratch("_drift_gather", 8 * rows)
+        _lib.call("goc_ensemble_gather_drifters", self._handle, buf.ptr, self.stream.handle)
+        self.kernels_launched += 1
+        if isinstance(out, int):
+            _lib.call("goc_memcpy_d2h_async", out, buf.ptr, ctypes.c_size_t(8 * rows), self.stream.handle)
+            return None
+        if out is None:
+            out = np.empty((rows, 2), dtype=np.float32)
+        _lib.call("goc_memcpy_d2h_async", out.ctypes.data, buf.ptr, ctypes.c_size_t(8 * rows), self.stream.handle)
+        self.stream.synchronize()
+        return out
+
+    def upload_observation_positions(self, positions):
+        """The observation row of every member with drifters from an
+        (n_members, 2) array (or the address of one in host memory): one
+        copy and one scatter launch."""
+        n = len(self.sims)
+        buf = self._scratch("_obs_scatter", 8 * n)
+        if isinstance(positions, int):
+            _lib.call("goc_memcpy_h2d_async", buf.ptr, positions, ctypes.c_size_t(8 * n), self.stream.handle)
+        else:
+            pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(n, 2)
+            _lib.call("goc_memcpy_h2d_async", buf.ptr, pos.ctypes.data, ctypes.c_size_t(8 * n), self.stream.handle)
+            self.stream.synchronize()
+        _lib.call("goc_ensemble_scatter_observations", self._handle, buf.ptr, self.stream.handle)
+        self.kernels_launched += 1
 
     def moments(self, first=0, count=None, quantity="state", desingularise=None, ddof=0, mean=True, var=True,
                 download=True):

@@ -469,6 +469,18 @@ int goc_ensemble_end_block(void* ensemble, int n_launched, void* stream);
 int goc_ensemble_set_drifters(void* ensemble, float* const* positions, const int* num_drifters,
                               float sensitivity, void* stream);
 
+/*
+ * Every member's drifter rows (N_m positions and the observation row) in one
+ * packed (rows x 2) float array, member by member, and the observation rows of
+ * every member with drifters from an (n_members x 2) array: one launch each
+ * instead of a copy per member (the reference reads and writes each
+ * collection on its own, D/GPUDrifterCollection.py:179-200).  Device memory;
+ * goc_ensemble_drifter_rows gives the packed row count.
+ */
+int goc_ensemble_drifter_rows(void* ensemble, long long* rows);
+int goc_ensemble_gather_drifters(void* ensemble, float* dst, void* stream);
+int goc_ensemble_scatter_observations(void* ensemble, const float* src, void* stream);
+
 /* Copy member m's current descriptor (device pointers) to the host.
  * Synchronises `stream`. */
 int goc_ensemble_get_member(void* ensemble, int m, GocMemberDesc* out, void* stream);

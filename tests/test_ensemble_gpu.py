@@ -217,3 +217,29 @@ def test_autotune_keeps_the_state_and_picks_a_shape(gpu_ctx):
     for sa, sb in zip(before, after):
         for x, y in zip(sa, sb):
             assert np.array_equal(x, y)
+
+
+def test_packed_drifter_transfers(gpu_ctx):
+    """download_drifters / upload_observation_positions move every member's
+    drifter rows in one launch and one copy, equal to the per-collection
+    accessors."""
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
+    sims = [_member(gpu_ctx, *s, drifters=30 + 7 * i) for i, s in enumerate(SPECS)]
+    for s in sims:
+        s.updateDt()
+    ens = BatchedEnsemble(sims, autotune=False)
+    ens.step(120.0)
+    rows = ens.download_drifters()
+    assert rows.shape == (ens.drifter_rows(), 2) == (sum(31 + 7 * i for i in range(len(SPECS))), 2)
+    off = 0
+    for s in sims:
+        n = s.drifters.getNumDrifters()
+        assert np.array_equal(rows[off:off + n], s.drifters.getDrifterPositions())
+        assert np.array_equal(rows[off + n], s.drifters.getObservationPosition())
+        off += n + 1
+    obs = np.random.default_rng(3).uniform(0, 1e5, (len(sims), 2)).astype(np.float32)
+    ens.upload_observation_positions(obs)
+    ens.synchronize()
+    for s, o in zip(sims, obs):
+        assert np.array_equal(s.drifters.getObservationPosition(), o)
+    ens.release()
