@@ -37,6 +37,11 @@ NOISE_STD = 0.003         # target std of the SOAR eta perturbation [m]
 # over 96 x 512 x 300 member-cell-steps, step built without FMA contraction);
 # traffic of a bench launch is scaled by its member-cells.
 NCU_DRAM_BYTES_PER_MEMBER_CELL = 383.9e6 / (96 * 512 * 300)
+# Warp instructions per member-cell-step of the same capture
+# (smsp__inst_executed.sum = 1.115e9): the step is bound by instruction issue,
+# whose ceiling is 4 warp instructions per cycle per SM.
+NCU_WARP_INST_PER_MEMBER_CELL = 1.115e9 / (96 * 512 * 300)
+SM_COUNT = 152
 
 
 def soar_q0(L_cells=NOISE_L_COARSE, std=NOISE_STD):
@@ -369,6 +374,18 @@ def run_statistics(ens, sims, peak, peak_kind, n_positions=1000, repeats=10):
     out["host_download_numpy_ms"] = 1000.0 * (time.perf_counter() - t0)
     out["device_over_host"] = out["host_download_numpy_ms"] / (out["moments_state_ms"])
     return out
+
+
+def issue_roofline(member_cells, seconds, clk):
+    """The fused step against its actual bound, instruction issue: warp
+    instructions per launch (ncu count per member-cell-step x member-cells)
+    per second, against 4 per cycle on each of the 152 SMs at the SM clock
+    sampled during the timed region."""
+    mhz = (clk or {}).get("sm_mhz") or 2070.0
+    achieved = NCU_WARP_INST_PER_MEMBER_CELL * member_cells / seconds / 1e9
+    peak = 4 * SM_COUNT * mhz * 1e6 / 1e9
+    return {"achieved": achieved, "peak": peak, "unit": "G warp-instructions/s", "frac": achieved / peak,
+            "source": "ncu smsp__inst_executed.sum of a 96-member launch, scaled per member-cell"}
 
 
 def run_c2(ctx, days=10.0):
@@ -809,7 +826,8 @@ def main():
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 96-member "
                                            "launch, scaled per member-cell", "kernel": "ensemble_rk2_kernel",
                          "peak_kind": peak_kind, "avg_launch_ms": 1000.0 * avg_dur,
-                         "algorithmic_bytes_per_launch": avg_bytes},
+                         "algorithmic_bytes_per_launch": avg_bytes,
+                         "issue": issue_roofline(float(np.mean(cells_k)), avg_dur, clk)},
             "e2e": e2e, "gpu_launches": launches, "clocks": clk, "cpu_baseline": cpu,
             "multilevel": multilevel, "adjoint": adjoint, "statistics": ens_stats, "kl_model_error": kl, "c2_ten_days": c2,
             "wall_s": wall,
