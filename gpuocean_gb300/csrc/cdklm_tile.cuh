@@ -452,14 +452,25 @@ __host__ __device__ inline StepConst make_step_const(const GocCdklmParams& p) {
 // fused RK2 step (NSTAGE = 2).  Called by the single-simulator kernel and by
 // the persistent ensemble kernel; the caller synchronises the block before
 // the shared memory is reused.
-template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING, bool BORDER>
+// Rows of stage-1 results a tile of a column strip hands to the next tile of
+// the strip (TY rows further north): the tile's local rows [H - 6, H - 2) are
+// the next tile's rows [2, 6).
+constexpr int kHandRows = 4;
+
+// S1: first local row of the stage-1 region the body computes (2: all of it;
+// 6: the rows [2, 6) come from `side_in`, the previous tile of the strip).
+// side_out (if not null) receives the stage-1 rows the next tile of the strip
+// reuses.  Only the RK2 fused path (NSTAGE = 2) streams.
+template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING, bool BORDER, int S1 = 2>
 __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const StepConst& k, float dt, int rk_step,
                                                 int tile_x, int tile_y,
                                                 const float* __restrict__ e_in, const float* __restrict__ hu_in,
                                                 const float* __restrict__ hv_in, float* e_out, float* hu_out,
                                                 float* hv_out, float* e_alt, float* hu_alt, float* hv_alt, int pitch,
                                                 const float* __restrict__ Hi_g, int hi_pitch,
-                                                const float* __restrict__ Hm_g, int hm_pitch, float* smem_raw) {
+                                                const float* __restrict__ Hm_g, int hm_pitch, float* smem_raw,
+                                                const float* side_in = nullptr, float* side_out = nullptr) {
+    static_assert(S1 == 2 || (NSTAGE == 2 && S1 == 2 + kHandRows), "stage-1 rows start at 2 or after the hand-over");
     constexpr int HALO = 2 * NSTAGE;
     constexpr int W = TX + 2 * HALO, H = TY + 2 * HALO;
     TileSmem<W, H>& S = *reinterpret_cast<TileSmem<W, H>*>(smem_raw);
@@ -543,12 +554,12 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
     __syncthreads();
 
     if (NSTAGE == 2) {
-        // ---- stage 1 on the tile + 2 cells ----
-        T.template slopes<2, W - 2, 2, H - 2, CONST_F>();
+        // ---- stage 1 on the tile + 2 cells (rows from S1) ----
+        T.template slopes<2, W - 2, S1, H - 2, CONST_F>();
         __syncthreads();
-        T.template faces<2, W - 2, 2, H - 2, CONST_F>();
+        T.template faces<2, W - 2, S1, H - 2, CONST_F>();
         __syncthreads();
-        constexpr int NU = (W - 4) * (H - 4);
+        constexpr int NU = (W - 4) * (H - 2 - S1);
         // Results are kept in registers until every thread has read its
         // cell of D^n, then written as D* (each thread owns its cells).
         constexpr int PER = (NU + NT - 1) / NT;
@@ -558,7 +569,7 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
             const int idx = threadIdx.x + r * NT;
             qe[r] = 0.f; qu[r] = 0.f; qv[r] = 0.f;
             if (idx >= NU) continue;
-            const int i = 2 + idx % (W - 4), j = 2 + idx / (W - 4);
+            const int i = 2 + idx % (W - 4), j = S1 + idx / (W - 4);
             int gx = T.x0 + i, gy = T.y0 + j;
             const int gxs = (BORDER && px) ? wrap_interior(gx, nx) : gx;
             const int gys = (BORDER && py) ? wrap_interior(gy, ny) : gy;
@@ -578,7 +589,7 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
         for (int r = 0; r < PER; ++r) {
             const int idx = threadIdx.x + r * NT;
             if (idx >= NU) continue;
-            const int i = 2 + idx % (W - 4), j = 2 + idx / (W - 4);
+            const int i = 2 + idx % (W - 4), j = S1 + idx / (W - 4);
             const int gx = T.x0 + i, gy = T.y0 + j;
             const bool okx = !BORDER || px || (gx >= 2 && gx < nx + 2);
             const bool oky = !BORDER || py || (gy >= 2 && gy < ny + 2);
@@ -621,6 +632,20 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
             }
         }
         __syncthreads();
+        if (S1 != 2 || side_out) {
+            // stage-1 rows handed over along the strip: take the previous
+            // tile's rows [2, 6), keep this tile's rows [H - 6, H - 2)
+            constexpr int NH = kHandRows * W;
+            for (int q = threadIdx.x; q < NH; q += NT) {
+                const int j = q / W, i = q % W;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    if (S1 != 2) S.D[c][2 + j][i] = side_in[c * NH + q];
+                    if (side_out) side_out[c * NH + q] = S.D[c][H - 2 - kHandRows + j][i];
+                }
+            }
+            if (S1 != 2) __syncthreads();
+        }
         // ---- stage 2 on the tile ----
         // Q^n of the thread's own output cells, loaded now so that the
         // loads overlap the stage-2 slopes and faces
@@ -736,6 +761,43 @@ __device__ __forceinline__ void cdklm_tile(const GocCdklmParams& p, const StepCo
         cdklm_tile_body<TX, TY, NSTAGE, NT, CONST_F, SIMPLE_FORCING, false>(
             p, k, dt, rk_step, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, e_alt, hu_alt, hv_alt,
             pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw);
+}
+
+// Tile `tile_y` of the column strip `tile_x` in a run of consecutive tiles
+// of one strip (fused RK2): reuse = the previous tile of the run handed over
+// its last stage-1 rows through side_in; side_out (or null for the run's last
+// tile) receives this tile's.  A tile whose staged rows reach outside the
+// interior rows computes all of its stage-1 rows: the north/south wall
+// mirrors of its first rows land in rows it does not take over.  East/west
+// borders keep the hand-over (their mirrors stay within a row).
+template <int TX, int TY, int NT, bool CONST_F, bool SIMPLE_FORCING>
+__device__ __forceinline__ void cdklm_strip_tile(const GocCdklmParams& p, const StepConst& k, float dt, int tile_x,
+                                                 int tile_y, bool reuse, const float* __restrict__ e_in,
+                                                 const float* __restrict__ hu_in, const float* __restrict__ hv_in,
+                                                 float* e_out, float* hu_out, float* hv_out, int pitch,
+                                                 const float* __restrict__ Hi_g, int hi_pitch,
+                                                 const float* __restrict__ Hm_g, int hm_pitch, float* smem_raw,
+                                                 const float* side_in, float* side_out) {
+    constexpr int S1 = 2 + kHandRows;
+    const bool border = tile_on_border<TX, TY, 2>(p, tile_x, tile_y);
+    const int y0 = 2 + tile_y * TY - 4;
+    reuse = reuse && y0 >= 2 && y0 + TY + 8 <= p.ny + 2;
+    if (border && reuse)
+        cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, true, S1>(
+            p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
+            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, side_in, side_out);
+    else if (border)
+        cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, true, 2>(
+            p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
+            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, nullptr, side_out);
+    else if (reuse)
+        cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, false, S1>(
+            p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
+            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, side_in, side_out);
+    else
+        cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, false, 2>(
+            p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
+            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, nullptr, side_out);
 }
 
 template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING>

@@ -119,22 +119,37 @@ static int shape_launch(Ensemble* e, int k, cudaStream_t st) {
 }
 
 // (Re)build the member/tile work queue for the ensemble's tile shape.
+// Work queue: every member's column strips cut into runs of at most kRunTiles
+// consecutive tiles; a CTA steps a run from south to north, handing the
+// overlapping stage-1 rows from one tile to the next.  Runs of a strip are
+// balanced in length, and the longest runs go first.
+constexpr int kRunTiles = 8;
+
 static int build_tiles(Ensemble* e) {
     const TileShape sh = kEnsembleShapes[e->shape];
     std::vector<int4> tiles;
+    int n_tiles = 0;
     for (int m = 0; m < e->n_members; ++m) {
         const GocCdklmParams& p = e->host[m].p;
         const int tx = (p.nx + sh.tx - 1) / sh.tx, ty = (p.ny + sh.ty - 1) / sh.ty;
-        for (int j = 0; j < ty; ++j)
-            for (int i = 0; i < tx; ++i) tiles.push_back(make_int4(m, i, j, 0));
+        const int runs = (ty + kRunTiles - 1) / kRunTiles;
+        for (int i = 0; i < tx; ++i)
+            for (int r = 0, j = 0; r < runs; ++r) {
+                const int len = ty / runs + (r < ty % runs ? 1 : 0);
+                tiles.push_back(make_int4(m, i, j, len));
+                j += len;
+            }
+        n_tiles += tx * ty;
     }
+    std::stable_sort(tiles.begin(), tiles.end(), [](const int4& a, const int4& b) { return a.w > b.w; });
     cudaFree(e->d_tiles);
     e->d_tiles = nullptr;
     cudaError_t err = cudaMalloc(&e->d_tiles, sizeof(int4) * tiles.size());
     if (err == cudaSuccess)
         err = cudaMemcpy(e->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice);
     if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "ensemble tile queue: %s", cudaGetErrorString(err));
-    e->n_tiles = (int)tiles.size();
+    e->n_tiles = n_tiles;
+    e->n_runs = (int)tiles.size();
     int grid = 0;
     return shape_configure(e, &grid);
 }

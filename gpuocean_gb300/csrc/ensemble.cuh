@@ -23,19 +23,20 @@ constexpr int kNumEnsembleShapes = sizeof(kEnsembleShapes) / sizeof(kEnsembleSha
 // launch-bounds occupancy target of its kernel.
 template <int TX, int TY>
 constexpr int shape_min_blocks() {
-    return (int)(3 * sizeof(TileSmem<TX + 8, TY + 8>) <= 227 * 1024 ? 3
-               : 2 * sizeof(TileSmem<TX + 8, TY + 8>) <= 227 * 1024 ? 2 : 1);
+    constexpr size_t b = sizeof(TileSmem<TX + 8, TY + 8>) + 2 * 3 * kHandRows * (TX + 8) * sizeof(float) + 1024;
+    return (int)(3 * b <= 228 * 1024 ? 3 : 2 * b <= 228 * 1024 ? 2 : 1);
 }
 
 struct Ensemble {
     int n_members = 0;
-    int n_tiles = 0;
+    int n_tiles = 0;                      // output tiles of all members
+    int n_runs = 0;                       // work items: runs of consecutive tiles of a column strip
     int max_substeps = 0;
     int n_dt_items = 0;
     bool const_f = true, simple = true;
     std::vector<GocMemberDesc> host;      // descriptors as created (set 0 current)
     GocMemberDesc* d_members = nullptr;   // device copy, buffers swapped on device
-    int4* d_tiles = nullptr;              // (member, tile_x, tile_y, 0)
+    int4* d_tiles = nullptr;              // runs (member, tile_x, first tile_y, tiles)
     float* d_dt = nullptr;                // n_members x max_substeps
     int* d_nsub = nullptr;                // n_substeps per member
     int4* d_dt_items = nullptr;           // CFL work: (member, bx, by, partial index)
@@ -97,6 +98,7 @@ ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __res
                         __ldg(dt_table + (size_t)c.x * max_sub + (k - 1)), sensitivity);
             continue;
         }
+        // a run of t.w consecutive tiles of the column strip t.y, from tile row t.z
         const int4 t = tiles[item];
         const int m = t.x;
         if (k >= __ldg(nsub + m)) continue;  // member already at the end of its block
@@ -111,18 +113,33 @@ ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __res
         }
         const int in = k & 1, out = in ^ 1;
         const float dt = __ldg(dt_table + (size_t)m * max_sub + k);
-        cdklm_tile<TX, TY, 2, kNT, CONST_F, SIMPLE_FORCING>(
-            md.p, kc, dt, 1, t.y, t.z, md.eta[in], md.hu[in], md.hv[in], md.eta[out], md.hu[out], md.hv[out],
-            nullptr, nullptr, nullptr, md.pitch / 4, md.Hi, md.Hi_pitch / 4, md.Hm, md.Hm_pitch / 4, smem_raw);
-        __syncthreads();
+        float* side = smem_raw + sizeof(TileSmem<TX + 8, TY + 8>) / sizeof(float);
+        constexpr int NSIDE = 3 * kHandRows * (TX + 8);
+        for (int r = 0; r < t.w; ++r) {
+            // stage-1 rows handed along the run through two alternating buffers
+            const float* side_in = side + ((r + 1) & 1) * NSIDE;
+            float* side_out = r + 1 < t.w ? side + (r & 1) * NSIDE : nullptr;
+            cdklm_strip_tile<TX, TY, kNT, CONST_F, SIMPLE_FORCING>(
+                md.p, kc, dt, t.y, t.z + r, r > 0, md.eta[in], md.hu[in], md.hv[in], md.eta[out], md.hu[out],
+                md.hv[out], md.pitch / 4, md.Hi, md.Hi_pitch / 4, md.Hm, md.Hm_pitch / 4, smem_raw, side_in,
+                side_out);
+            __syncthreads();
+        }
     }
+}
+
+// Dynamic shared memory of the persistent kernel: the tile planes plus two
+// hand-over buffers of stage-1 rows.
+template <int TX, int TY>
+constexpr size_t ensemble_smem() {
+    return sizeof(TileSmem<TX + 8, TY + 8>) + 2 * 3 * kHandRows * (TX + 8) * sizeof(float);
 }
 
 // Kernel attributes and the persistent grid are set up once per variant,
 // outside any stream capture (goc_ensemble_create calls this).
 template <int TX, int TY, bool CF, bool SF>
 int configure_ensemble_kernel(int* grid_out) {
-    constexpr size_t smem = sizeof(TileSmem<TX + 8, TY + 8>);
+    constexpr size_t smem = ensemble_smem<TX, TY>();
     static int grid = 0;
     if (grid == 0) {
         auto kern = ensemble_rk2_kernel<TX, TY, shape_min_blocks<TX, TY>(), CF, SF>;
@@ -142,14 +159,14 @@ int configure_ensemble_kernel(int* grid_out) {
 
 template <int TX, int TY, bool CF, bool SF>
 int launch_ensemble(Ensemble* e, int k, cudaStream_t st) {
-    constexpr size_t smem = sizeof(TileSmem<TX + 8, TY + 8>);
+    constexpr size_t smem = ensemble_smem<TX, TY>();
     auto kern = ensemble_rk2_kernel<TX, TY, shape_min_blocks<TX, TY>(), CF, SF>;
     int full = 0;
     int rc = configure_ensemble_kernel<TX, TY, CF, SF>(&full);
     if (rc) return rc;
-    const int items = e->n_tiles + (k >= 1 ? e->n_drift_chunks : 0);
+    const int items = e->n_runs + (k >= 1 ? e->n_drift_chunks : 0);
     const int grid = std::min(items, full);
-    kern<<<grid, kNT, smem, st>>>(e->d_members, e->d_tiles, e->n_tiles, e->d_dt, e->d_nsub, e->max_substeps, k,
+    kern<<<grid, kNT, smem, st>>>(e->d_members, e->d_tiles, e->n_runs, e->d_dt, e->d_nsub, e->max_substeps, k,
                                   e->d_drift_pos, e->d_drift_chunks, e->n_drift_chunks, e->drift_sensitivity);
     count_launch();
     return check_launch("ensemble_rk2_kernel");
