@@ -139,12 +139,12 @@ struct Tile {
     __device__ float F(int j, int i, bool const_f) const { return const_f ? f0 : S.Fc[j][i]; }
 
     // x slopes on [ux0-1, ux1+1) x [uy0, uy1) and y slopes on
-    // [ux0, ux1) x [uy0-1, uy1+1)
+    // [ux0, ux1) x [uy0-1, uy1+1); `skip` leading rows are left out
     template <int UX0, int UX1, int UY0, int UY1, bool CONST_F>
-    __device__ void slopes() {
+    __device__ void slopes(int skip = 0) {
         constexpr int NXS = UX1 - UX0 + 2, NYS = UY1 - UY0;
         const float th = p.theta;
-        for (int idx = threadIdx.x; idx < NXS * NYS; idx += NT) {
+        for (int idx = threadIdx.x + skip * NXS; idx < NXS * NYS; idx += NT) {
             const int i = UX0 - 1 + idx % NXS;
             const int j = UY0 + idx / NXS;
             const int gx = x0 + i;
@@ -183,7 +183,7 @@ struct Tile {
         }
         constexpr int NXY = UX1 - UX0, NYY = UY1 - UY0 + 2;
         const float eX = nY, eY = -nX;  // east vector
-        for (int idx = threadIdx.x; idx < NXY * NYY; idx += NT) {
+        for (int idx = threadIdx.x + skip * NXY; idx < NXY * NYY; idx += NT) {
             const int i = UX0 + idx % NXY;
             const int j = UY0 - 1 + idx / NXY;
             const int gy = y0 + j;
@@ -223,11 +223,11 @@ struct Tile {
     }
 
     // east faces of cells [ux0-1, ux1) x [uy0, uy1); north faces of cells
-    // [ux0, ux1) x [uy0-1, uy1)
+    // [ux0, ux1) x [uy0-1, uy1); `skip` leading rows are left out
     template <int UX0, int UX1, int UY0, int UY1, bool CONST_F>
-    __device__ void faces() {
+    __device__ void faces(int skip = 0) {
         constexpr int NXF = UX1 - UX0 + 1, NYF = UY1 - UY0;
-        for (int idx = threadIdx.x; idx < NXF * NYF; idx += NT) {
+        for (int idx = threadIdx.x + skip * NXF; idx < NXF * NYF; idx += NT) {
             const int i = UX0 - 1 + idx % NXF;
             const int j = UY0 + idx / NXF;
             const int gxp = x0 + i + 1;  // global column of the plus cell
@@ -262,7 +262,7 @@ struct Tile {
         }
         constexpr int NXG = UX1 - UX0, NYG = UY1 - UY0 + 1;
         const float eX = nY, eY = -nX;
-        for (int idx = threadIdx.x; idx < NXG * NYG; idx += NT) {
+        for (int idx = threadIdx.x + skip * NXG; idx < NXG * NYG; idx += NT) {
             const int i = UX0 + idx % NXG;
             const int j = UY0 - 1 + idx / NXG;
             const int gyp = y0 + j + 1;
@@ -457,11 +457,13 @@ __host__ __device__ inline StepConst make_step_const(const GocCdklmParams& p) {
 // the next tile's rows [2, 6).
 constexpr int kHandRows = 4;
 
-// S1: first local row of the stage-1 region the body computes (2: all of it;
+// s1: first local row of the stage-1 region the body computes (2: all of it;
 // 6: the rows [2, 6) come from `side_in`, the previous tile of the strip).
 // side_out (if not null) receives the stage-1 rows the next tile of the strip
-// reuses.  Only the RK2 fused path (NSTAGE = 2) streams.
-template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING, bool BORDER, int S1 = 2>
+// reuses.  Only the RK2 fused path (NSTAGE = 2) streams.  s1 is a run-time
+// value so that one instantiation serves both kinds of tile (the kernel's
+// code stays within the instruction cache).
+template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING, bool BORDER>
 __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const StepConst& k, float dt, int rk_step,
                                                 int tile_x, int tile_y,
                                                 const float* __restrict__ e_in, const float* __restrict__ hu_in,
@@ -469,8 +471,8 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
                                                 float* hv_out, float* e_alt, float* hu_alt, float* hv_alt, int pitch,
                                                 const float* __restrict__ Hi_g, int hi_pitch,
                                                 const float* __restrict__ Hm_g, int hm_pitch, float* smem_raw,
-                                                const float* side_in = nullptr, float* side_out = nullptr) {
-    static_assert(S1 == 2 || (NSTAGE == 2 && S1 == 2 + kHandRows), "stage-1 rows start at 2 or after the hand-over");
+                                                int s1 = 2, const float* side_in = nullptr,
+                                                float* side_out = nullptr) {
     constexpr int HALO = 2 * NSTAGE;
     constexpr int W = TX + 2 * HALO, H = TY + 2 * HALO;
     TileSmem<W, H>& S = *reinterpret_cast<TileSmem<W, H>*>(smem_raw);
@@ -554,12 +556,13 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
     __syncthreads();
 
     if (NSTAGE == 2) {
-        // ---- stage 1 on the tile + 2 cells (rows from S1) ----
-        T.template slopes<2, W - 2, S1, H - 2, CONST_F>();
+        // ---- stage 1 on the tile + 2 cells (rows from s1) ----
+        T.template slopes<2, W - 2, 2, H - 2, CONST_F>(s1 - 2);
         __syncthreads();
-        T.template faces<2, W - 2, S1, H - 2, CONST_F>();
+        T.template faces<2, W - 2, 2, H - 2, CONST_F>(s1 - 2);
         __syncthreads();
-        constexpr int NU = (W - 4) * (H - 2 - S1);
+        constexpr int NU = (W - 4) * (H - 4);
+        const int nu = (W - 4) * (H - 2 - s1);
         // Results are kept in registers until every thread has read its
         // cell of D^n, then written as D* (each thread owns its cells).
         constexpr int PER = (NU + NT - 1) / NT;
@@ -568,8 +571,8 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
         for (int r = 0; r < PER; ++r) {
             const int idx = threadIdx.x + r * NT;
             qe[r] = 0.f; qu[r] = 0.f; qv[r] = 0.f;
-            if (idx >= NU) continue;
-            const int i = 2 + idx % (W - 4), j = S1 + idx / (W - 4);
+            if (idx >= nu) continue;
+            const int i = 2 + idx % (W - 4), j = s1 + idx / (W - 4);
             int gx = T.x0 + i, gy = T.y0 + j;
             const int gxs = (BORDER && px) ? wrap_interior(gx, nx) : gx;
             const int gys = (BORDER && py) ? wrap_interior(gy, ny) : gy;
@@ -588,8 +591,8 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
 #pragma unroll
         for (int r = 0; r < PER; ++r) {
             const int idx = threadIdx.x + r * NT;
-            if (idx >= NU) continue;
-            const int i = 2 + idx % (W - 4), j = S1 + idx / (W - 4);
+            if (idx >= nu) continue;
+            const int i = 2 + idx % (W - 4), j = s1 + idx / (W - 4);
             const int gx = T.x0 + i, gy = T.y0 + j;
             const bool okx = !BORDER || px || (gx >= 2 && gx < nx + 2);
             const bool oky = !BORDER || py || (gy >= 2 && gy < ny + 2);
@@ -632,7 +635,7 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
             }
         }
         __syncthreads();
-        if (S1 != 2 || side_out) {
+        if (s1 != 2 || side_out) {
             // stage-1 rows handed over along the strip: take the previous
             // tile's rows [2, 6), keep this tile's rows [H - 6, H - 2)
             constexpr int NH = kHandRows * W;
@@ -640,11 +643,11 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
                 const int j = q / W, i = q % W;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    if (S1 != 2) S.D[c][2 + j][i] = side_in[c * NH + q];
+                    if (s1 != 2) S.D[c][2 + j][i] = side_in[c * NH + q];
                     if (side_out) side_out[c * NH + q] = S.D[c][H - 2 - kHandRows + j][i];
                 }
             }
-            if (S1 != 2) __syncthreads();
+            if (s1 != 2) __syncthreads();
         }
         // ---- stage 2 on the tile ----
         // Q^n of the thread's own output cells, loaded now so that the
@@ -778,26 +781,17 @@ __device__ __forceinline__ void cdklm_strip_tile(const GocCdklmParams& p, const 
                                                  const float* __restrict__ Hi_g, int hi_pitch,
                                                  const float* __restrict__ Hm_g, int hm_pitch, float* smem_raw,
                                                  const float* side_in, float* side_out) {
-    constexpr int S1 = 2 + kHandRows;
     const bool border = tile_on_border<TX, TY, 2>(p, tile_x, tile_y);
     const int y0 = 2 + tile_y * TY - 4;
-    reuse = reuse && y0 >= 2 && y0 + TY + 8 <= p.ny + 2;
-    if (border && reuse)
-        cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, true, S1>(
+    const int s1 = (reuse && y0 >= 2 && y0 + TY + 8 <= p.ny + 2) ? 2 + kHandRows : 2;
+    if (border)
+        cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, true>(
             p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
-            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, side_in, side_out);
-    else if (border)
-        cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, true, 2>(
-            p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
-            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, nullptr, side_out);
-    else if (reuse)
-        cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, false, S1>(
-            p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
-            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, side_in, side_out);
+            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, s1, side_in, side_out);
     else
-        cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, false, 2>(
+        cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, false>(
             p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
-            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, nullptr, side_out);
+            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, s1, side_in, side_out);
 }
 
 template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING>
