@@ -138,6 +138,17 @@ struct Tile {
 
     __device__ float F(int j, int i, bool const_f) const { return const_f ? f0 : S.Fc[j][i]; }
 
+    // Start thread of the second loop of a phase whose first loop has n_first
+    // items: the warps that take one item more in the first loop (from thread
+    // 0) start the second loop at its end, so no warp takes the extra item of
+    // both loops (the phase ends at a barrier, so its slowest warp sets its
+    // length).  Whole warps are rotated, so each warp still reads one run of
+    // consecutive cells.
+    __device__ static int second_loop_thread(int n_first) {
+        const int tail = ((n_first % NT) + 31) & ~31;
+        return (int)((threadIdx.x + NT - tail) % NT);
+    }
+
     // x slopes on [ux0-1, ux1+1) x [uy0, uy1) and y slopes on
     // [ux0, ux1) x [uy0-1, uy1+1); `skip` leading rows are left out
     template <int UX0, int UX1, int UY0, int UY1, bool CONST_F>
@@ -183,7 +194,7 @@ struct Tile {
         }
         constexpr int NXY = UX1 - UX0, NYY = UY1 - UY0 + 2;
         const float eX = nY, eY = -nX;  // east vector
-        for (int idx = threadIdx.x + skip * NXY; idx < NXY * NYY; idx += NT) {
+        for (int idx = second_loop_thread(NXS * (NYS - skip)) + skip * NXY; idx < NXY * NYY; idx += NT) {
             const int i = UX0 + idx % NXY;
             const int j = UY0 - 1 + idx / NXY;
             const int gy = y0 + j;
@@ -262,7 +273,7 @@ struct Tile {
         }
         constexpr int NXG = UX1 - UX0, NYG = UY1 - UY0 + 1;
         const float eX = nY, eY = -nX;
-        for (int idx = threadIdx.x + skip * NXG; idx < NXG * NYG; idx += NT) {
+        for (int idx = second_loop_thread(NXF * (NYF - skip)) + skip * NXG; idx < NXG * NYG; idx += NT) {
             const int i = UX0 + idx % NXG;
             const int j = UY0 - 1 + idx / NXG;
             const int gyp = y0 + j + 1;
