@@ -124,6 +124,24 @@ __device__ __forceinline__ void cdklm_flux(const GocCdklmParams& p, const StepCo
     F2 = f2;
 }
 
+// Cell (i, j) of item `idx` of a loop over an NX x ny block of cells.  The
+// tile planes are 8 floats wider than most loops, so a warp that ran on
+// across the end of a row would meet its own banks again at the next row
+// (two shared-memory wavefronts instead of one).  The block is therefore
+// walked as its first M = 32 * floor(NX / 32) columns row by row (each warp
+// one run of 32 consecutive cells), then its last NX - M columns packed row
+// after row.  Loops narrower than 32 cells walk the block row by row.
+template <int NX>
+__device__ __forceinline__ void block_cell(int idx, int ny, int& i, int& j) {
+    constexpr int M = NX < 32 ? NX : 32 * (NX / 32), R = NX - M;
+    if (R == 0 || idx < M * ny) {
+        i = idx % M; j = idx / M;
+    } else {
+        const int q = idx - M * ny;
+        i = M + q % (R > 0 ? R : 1); j = q / (R > 0 ? R : 1);
+    }
+}
+
 // SM: the shared-memory layout; any struct with the members of TileSmem that
 // the stage code reads (D, Sx, Sy, Fx, Gy, Hi and, with a Coriolis texture, Fc).
 template <int W, int H, int NT, bool BORDER, class SM = TileSmem<W, H>>
@@ -155,9 +173,10 @@ struct Tile {
     __device__ void slopes(int skip = 0) {
         constexpr int NXS = UX1 - UX0 + 2, NYS = UY1 - UY0;
         const float th = p.theta;
-        for (int idx = threadIdx.x + skip * NXS; idx < NXS * NYS; idx += NT) {
-            const int i = UX0 - 1 + idx % NXS;
-            const int j = UY0 + idx / NXS;
+        for (int idx = threadIdx.x; idx < NXS * (NYS - skip); idx += NT) {
+            int i, j;
+            block_cell<NXS>(idx, NYS - skip, i, j);
+            i += UX0 - 1; j += UY0 + skip;
             const int gx = x0 + i;
             const float eL = S.D[0][j][i - 1], eC = S.D[0][j][i], eR = S.D[0][j][i + 1];
             const float uL = S.D[1][j][i - 1], uC = S.D[1][j][i], uR = S.D[1][j][i + 1];
@@ -194,9 +213,10 @@ struct Tile {
         }
         constexpr int NXY = UX1 - UX0, NYY = UY1 - UY0 + 2;
         const float eX = nY, eY = -nX;  // east vector
-        for (int idx = second_loop_thread(NXS * (NYS - skip)) + skip * NXY; idx < NXY * NYY; idx += NT) {
-            const int i = UX0 + idx % NXY;
-            const int j = UY0 - 1 + idx / NXY;
+        for (int idx = second_loop_thread(NXS * (NYS - skip)); idx < NXY * (NYY - skip); idx += NT) {
+            int i, j;
+            block_cell<NXY>(idx, NYY - skip, i, j);
+            i += UX0; j += UY0 - 1 + skip;
             const int gy = y0 + j;
             const float eL = S.D[0][j - 1][i], eC = S.D[0][j][i], eU = S.D[0][j + 1][i];
             const float uL = S.D[1][j - 1][i], uC = S.D[1][j][i], uU = S.D[1][j + 1][i];
@@ -238,9 +258,10 @@ struct Tile {
     template <int UX0, int UX1, int UY0, int UY1, bool CONST_F>
     __device__ void faces(int skip = 0) {
         constexpr int NXF = UX1 - UX0 + 1, NYF = UY1 - UY0;
-        for (int idx = threadIdx.x + skip * NXF; idx < NXF * NYF; idx += NT) {
-            const int i = UX0 - 1 + idx % NXF;
-            const int j = UY0 + idx / NXF;
+        for (int idx = threadIdx.x; idx < NXF * (NYF - skip); idx += NT) {
+            int i, j;
+            block_cell<NXF>(idx, NYF - skip, i, j);
+            i += UX0 - 1; j += UY0 + skip;
             const int gxp = x0 + i + 1;  // global column of the plus cell
             const float ebm = S.D[0][j][i], ebp = S.D[0][j][i + 1];
             float F0 = 0.f, F1 = 0.f, F2 = 0.f;
@@ -273,9 +294,10 @@ struct Tile {
         }
         constexpr int NXG = UX1 - UX0, NYG = UY1 - UY0 + 1;
         const float eX = nY, eY = -nX;
-        for (int idx = second_loop_thread(NXF * (NYF - skip)) + skip * NXG; idx < NXG * NYG; idx += NT) {
-            const int i = UX0 + idx % NXG;
-            const int j = UY0 - 1 + idx / NXG;
+        for (int idx = second_loop_thread(NXF * (NYF - skip)); idx < NXG * (NYG - skip); idx += NT) {
+            int i, j;
+            block_cell<NXG>(idx, NYG - skip, i, j);
+            i += UX0; j += UY0 - 1 + skip;
             const int gyp = y0 + j + 1;
             const float ebm = S.D[0][j][i], ebp = S.D[0][j + 1][i];
             float G0 = 0.f, G1 = 0.f, G2 = 0.f;
@@ -583,7 +605,9 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
             const int idx = threadIdx.x + r * NT;
             qe[r] = 0.f; qu[r] = 0.f; qv[r] = 0.f;
             if (idx >= nu) continue;
-            const int i = 2 + idx % (W - 4), j = s1 + idx / (W - 4);
+            int i, j;
+            block_cell<W - 4>(idx, H - 2 - s1, i, j);
+            i += 2; j += s1;
             int gx = T.x0 + i, gy = T.y0 + j;
             const int gxs = (BORDER && px) ? wrap_interior(gx, nx) : gx;
             const int gys = (BORDER && py) ? wrap_interior(gy, ny) : gy;
@@ -603,7 +627,9 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
         for (int r = 0; r < PER; ++r) {
             const int idx = threadIdx.x + r * NT;
             if (idx >= nu) continue;
-            const int i = 2 + idx % (W - 4), j = s1 + idx / (W - 4);
+            int i, j;
+            block_cell<W - 4>(idx, H - 2 - s1, i, j);
+            i += 2; j += s1;
             const int gx = T.x0 + i, gy = T.y0 + j;
             const bool okx = !BORDER || px || (gx >= 2 && gx < nx + 2);
             const bool oky = !BORDER || py || (gy >= 2 && gy < ny + 2);
