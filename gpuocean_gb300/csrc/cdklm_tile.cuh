@@ -25,6 +25,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "tma.cuh"
 
 namespace goc {
 
@@ -122,6 +123,18 @@ __device__ __forceinline__ void cdklm_flux(const GocCdklmParams& p, const StepCo
     float f2 = (um_ > -up_) ? fb * Fm2 : fb * Fp2;
     f2 += (1.0f - fb) * (((ap * Fm2 - am * Fp2) + apam * (hp * vp_ - hm * vm_)) * inv);
     F2 = f2;
+}
+
+// Issue the TMA copies of the (eta, hu, hv) box at (x, y) (x a multiple of
+// 4) into the staging planes Sx[0], Sx[1], Sy[0].  The caller is one thread,
+// after a barrier that ended every generic access of those planes.
+template <int W, int H>
+__device__ __forceinline__ void tma_stage_tile(TileTma& t, TileSmem<W, H>& S, int x, int y) {
+    fence_proxy_async_shared();
+    mbar_arrive_expect_tx(t.bar, 3u * W * H * sizeof(float));
+    tma_load_2d(&S.Sx[0][0][0], t.in_maps + 0, x, y, t.bar);
+    tma_load_2d(&S.Sx[1][0][0], t.in_maps + 1, x, y, t.bar);
+    tma_load_2d(&S.Sy[0][0][0], t.in_maps + 2, x, y, t.bar);
 }
 
 // Cell (i, j) of item `idx` of a loop over an NX x ny block of cells.  The
@@ -505,7 +518,7 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
                                                 const float* __restrict__ Hi_g, int hi_pitch,
                                                 const float* __restrict__ Hm_g, int hm_pitch, float* smem_raw,
                                                 int s1 = 2, const float* side_in = nullptr,
-                                                float* side_out = nullptr) {
+                                                float* side_out = nullptr, TileTma* tma = nullptr) {
     constexpr int HALO = 2 * NSTAGE;
     constexpr int W = TX + 2 * HALO, H = TY + 2 * HALO;
     TileSmem<W, H>& S = *reinterpret_cast<TileSmem<W, H>*>(smem_raw);
@@ -540,6 +553,19 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
     // phases' global loads are in flight together (the barrier after them
     // covers both)
 
+    // Q^n of an interior tile may have been staged by TMA into the planes
+    // Sx[0], Sx[1], Sy[0] (box from column x0 - 2: TMA boxes start on 16-byte
+    // boundaries): wait for it.  A wait that runs out falls back to loads.
+    bool staged = false;
+    if (!BORDER && tma && tma->staged) {
+        staged = mbar_wait_bounded(tma->bar, tma->phase, kTmaWaitLimit);
+        tma->phase ^= 1u;
+        if (!staged) {
+            *tma->off = 1;
+            atomicExch(tma->err, 1);
+        }
+    }
+
     // 2. Q^n with wall mirrors and periodic images, desingularised with the
     //    cell-mean depth of the (unmirrored) cell (K/CDKLM16_kernel.cu:614-656)
     for (int idx = threadIdx.x; idx < H * W; idx += NT) {
@@ -566,10 +592,17 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
             gx = clampi(gx, 0, nx + 3);
             gy = clampi(gy, 0, ny + 3);
         }
-        const size_t o = (size_t)my * pitch + mx;
-        const float e = __ldg(e_in + o);
-        const float hu = su * __ldg(hu_in + o);
-        const float hv = sv * __ldg(hv_in + o);
+        float e, hu, hv;
+        if (!BORDER && staged && i < W - 2) {
+            e = S.Sx[0][j][i + 2];
+            hu = S.Sx[1][j][i + 2];
+            hv = S.Sy[0][j][i + 2];
+        } else {
+            const size_t o = (size_t)my * pitch + mx;
+            e = __ldg(e_in + o);
+            hu = su * __ldg(hu_in + o);
+            hv = sv * __ldg(hv_in + o);
+        }
         const float hmb = __ldg(Hm_g + (size_t)gy * hm_pitch + gx);
         S.Hmb[j][i] = hmb;
         float oe, ou, ov;
@@ -707,6 +740,10 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
         __syncthreads();
         T.template faces<4, W - 4, 4, H - 4, CONST_F>();
         __syncthreads();
+        // the last phase reads neither Sx[0..1] nor Sy[0..1]: stage the next
+        // tile of the strip there meanwhile
+        if (tma && tma->next_tile_y >= 0 && threadIdx.x == 0)
+            tma_stage_tile<W, H>(*tma, S, T.x0 - 2, 2 + tma->next_tile_y * TY - HALO);
 #pragma unroll
         for (int r = 0; r < PER2; ++r) {
             const int idx = threadIdx.x + r * NT;
@@ -817,18 +854,18 @@ __device__ __forceinline__ void cdklm_strip_tile(const GocCdklmParams& p, const 
                                                  float* e_out, float* hu_out, float* hv_out, int pitch,
                                                  const float* __restrict__ Hi_g, int hi_pitch,
                                                  const float* __restrict__ Hm_g, int hm_pitch, float* smem_raw,
-                                                 const float* side_in, float* side_out) {
+                                                 const float* side_in, float* side_out, TileTma* tma) {
     const bool border = tile_on_border<TX, TY, 2>(p, tile_x, tile_y);
     const int y0 = 2 + tile_y * TY - 4;
     const int s1 = (reuse && y0 >= 2 && y0 + TY + 8 <= p.ny + 2) ? 2 + kHandRows : 2;
     if (border)
         cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, true>(
             p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
-            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, s1, side_in, side_out);
+            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, s1, side_in, side_out, tma);
     else
         cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, false>(
             p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
-            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, s1, side_in, side_out);
+            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, s1, side_in, side_out, tma);
 }
 
 template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING>

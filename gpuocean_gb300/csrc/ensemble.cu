@@ -2,7 +2,10 @@
 // advances in one persistent launch per RK2 step over a member/tile work
 // queue, instead of one Python-driven launch sequence per member
 // (E/OceanNoiseEnsemble.py:517-543, E/MultiLevelOceanEnsemble.py:95-141).
+#include <cudaTypedefs.h>
+
 #include <climits>
+#include <cstdint>
 #include <cstdio>
 
 #include "ensemble.cuh"
@@ -83,7 +86,78 @@ static void free_ensemble(Ensemble* e) {
     cudaFree(e->d_drift_pos);
     cudaFree(e->d_drift_chunks);
     cudaFree(e->d_drift_n);
+    cudaFree(e->d_tmaps);
+    cudaFree(e->d_tma_base);
+    cudaFree(e->d_tma_err);
+    cudaFree(e->d_tma_tiles);
     delete e;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (null if
+// the driver does not provide it).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// TMA maps of every member's (eta, hu, hv) in both buffer sets, one box per
+// tile shape (the shape's tile + 4 cells on each side).  A member is staged
+// by TMA when every buffer starts on a 16-byte boundary, its row pitch is a
+// multiple of 16 bytes and every map encodes; otherwise its tiles load Q^n
+// with ordinary loads.
+static int build_tma_maps(Ensemble* e) {
+    const int n = e->n_members;
+    std::vector<CUtensorMap> maps((size_t)kNumEnsembleShapes * n * 6);
+    std::vector<const float*> base(n, nullptr);
+    const PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    e->n_tma_members = 0;
+    for (int m = 0; m < n; ++m) {
+        const GocMemberDesc& d = e->host[m];
+        float* const buf[2][3] = {{d.eta[0], d.hu[0], d.hv[0]}, {d.eta[1], d.hu[1], d.hv[1]}};
+        bool ok = encode != nullptr && d.pitch % 16 == 0;
+        for (int set = 0; set < 2; ++set)
+            for (int c = 0; c < 3; ++c) ok = ok && reinterpret_cast<uintptr_t>(buf[set][c]) % 16 == 0;
+        for (int sh = 0; ok && sh < kNumEnsembleShapes; ++sh) {
+            const cuuint64_t dims[2] = {(cuuint64_t)d.p.nx + 4, (cuuint64_t)d.p.ny + 4};
+            const cuuint64_t strides[1] = {(cuuint64_t)d.pitch};
+            const cuuint32_t box[2] = {(cuuint32_t)kEnsembleShapes[sh].tx + 8, (cuuint32_t)kEnsembleShapes[sh].ty + 8};
+            const cuuint32_t unit[2] = {1, 1};
+            for (int set = 0; ok && set < 2; ++set)
+                for (int c = 0; ok && c < 3; ++c)
+                    ok = encode(&maps[(((size_t)sh * n + m) * 2 + set) * 3 + c], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                                buf[set][c], dims, strides, box, unit, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+        }
+        if (ok) {
+            base[m] = d.eta[0];
+            ++e->n_tma_members;
+        }
+    }
+    cudaError_t err = cudaMalloc(&e->d_tmaps, sizeof(CUtensorMap) * maps.size());
+    if (err == cudaSuccess) err = cudaMalloc(&e->d_tma_base, sizeof(const float*) * n);
+    if (err == cudaSuccess) err = cudaMalloc(&e->d_tma_err, sizeof(int));
+    if (err == cudaSuccess) err = cudaMalloc(&e->d_tma_tiles, sizeof(unsigned long long));
+    if (err == cudaSuccess)
+        err = cudaMemcpy(e->d_tmaps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess)
+        err = cudaMemcpy(e->d_tma_base, base.data(), sizeof(const float*) * n, cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMemset(e->d_tma_err, 0, sizeof(int));
+    if (err == cudaSuccess) err = cudaMemset(e->d_tma_tiles, 0, sizeof(unsigned long long));
+    if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "ensemble TMA maps: %s", cudaGetErrorString(err));
+    return GOC_OK;
 }
 
 const GocMemberDesc* ensemble_host_members(void* ensemble, int* n_members) {
@@ -121,27 +195,46 @@ static int shape_launch(Ensemble* e, int k, cudaStream_t st) {
 // (Re)build the member/tile work queue for the ensemble's tile shape.
 // Work queue: every member's column strips cut into runs of at most kRunTiles
 // consecutive tiles; a CTA steps a run from south to north, handing the
-// overlapping stage-1 rows from one tile to the next.  Runs of a strip are
-// balanced in length, and the longest runs go first.
+// overlapping stage-1 rows from one tile to the next.  A run holds either
+// interior tiles only or border tiles only (the two are different code), and
+// all interior runs come before all border runs, longest first within each
+// group: while the interior runs last, every CTA of an SM executes the same
+// code, which keeps the instruction cache warm; the short border runs then
+// even out the end of the launch.
 constexpr int kRunTiles = 8;
+
+static bool host_tile_on_border(const GocCdklmParams& p, int tx, int ty, int i, int j) {
+    const int x0 = 2 + i * tx - 4, y0 = 2 + j * ty - 4;
+    return x0 < 2 || y0 < 2 || x0 + tx + 8 > p.nx + 2 || y0 + ty + 8 > p.ny + 2;
+}
 
 static int build_tiles(Ensemble* e) {
     const TileShape sh = kEnsembleShapes[e->shape];
-    std::vector<int4> tiles;
+    std::vector<int4> inner, border;
     int n_tiles = 0;
     for (int m = 0; m < e->n_members; ++m) {
         const GocCdklmParams& p = e->host[m].p;
         const int tx = (p.nx + sh.tx - 1) / sh.tx, ty = (p.ny + sh.ty - 1) / sh.ty;
-        const int runs = (ty + kRunTiles - 1) / kRunTiles;
         for (int i = 0; i < tx; ++i)
-            for (int r = 0, j = 0; r < runs; ++r) {
-                const int len = ty / runs + (r < ty % runs ? 1 : 0);
-                tiles.push_back(make_int4(m, i, j, len));
-                j += len;
+            for (int j = 0; j < ty;) {
+                // a maximal stretch of tiles of one kind, cut into balanced runs
+                const bool b = host_tile_on_border(p, sh.tx, sh.ty, i, j);
+                int end = j + 1;
+                while (end < ty && host_tile_on_border(p, sh.tx, sh.ty, i, end) == b) ++end;
+                const int len = end - j, runs = (len + kRunTiles - 1) / kRunTiles;
+                for (int r = 0; r < runs; ++r) {
+                    const int n = len / runs + (r < len % runs ? 1 : 0);
+                    (b ? border : inner).push_back(make_int4(m, i, j, n));
+                    j += n;
+                }
             }
         n_tiles += tx * ty;
     }
-    std::stable_sort(tiles.begin(), tiles.end(), [](const int4& a, const int4& b) { return a.w > b.w; });
+    auto longest_first = [](const int4& a, const int4& b) { return a.w > b.w; };
+    std::stable_sort(inner.begin(), inner.end(), longest_first);
+    std::stable_sort(border.begin(), border.end(), longest_first);
+    std::vector<int4> tiles(inner);
+    tiles.insert(tiles.end(), border.begin(), border.end());
     cudaFree(e->d_tiles);
     e->d_tiles = nullptr;
     cudaError_t err = cudaMalloc(&e->d_tiles, sizeof(int4) * tiles.size());
@@ -217,7 +310,8 @@ extern "C" int goc_ensemble_create(const GocMemberDesc* members, int n_members, 
         free_ensemble(e);
         return set_error(GOC_ERR_CUDA, "goc_ensemble_create: %s", cudaGetErrorString(err));
     }
-    int rc = build_tiles(e);
+    int rc = build_tma_maps(e);
+    if (!rc) rc = build_tiles(e);
     if (rc) {
         free_ensemble(e);
         return rc;
@@ -229,6 +323,26 @@ extern "C" int goc_ensemble_create(const GocMemberDesc* members, int n_members, 
 extern "C" int goc_ensemble_destroy(void* ensemble) {
     if (!ensemble) return GOC_OK;
     free_ensemble(static_cast<Ensemble*>(ensemble));
+    return GOC_OK;
+}
+
+extern "C" int goc_ensemble_tma_status(void* ensemble, int* staged_members, long long* staged_tiles,
+                                       int* wait_errors) {
+    if (!ensemble) return set_error(GOC_ERR_ARG, "goc_ensemble_tma_status: null handle");
+    Ensemble* e = static_cast<Ensemble*>(ensemble);
+    if (staged_members) *staged_members = e->n_tma_members;
+    if (staged_tiles) {
+        unsigned long long v = 0;
+        const cudaError_t err = cudaMemcpy(&v, e->d_tma_tiles, sizeof(v), cudaMemcpyDeviceToHost);
+        if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_ensemble_tma_status: %s", cudaGetErrorString(err));
+        *staged_tiles = (long long)v;
+    }
+    if (wait_errors) {
+        int v = 0;
+        const cudaError_t err = cudaMemcpy(&v, e->d_tma_err, sizeof(int), cudaMemcpyDeviceToHost);
+        if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_ensemble_tma_status: %s", cudaGetErrorString(err));
+        *wait_errors = v;
+    }
     return GOC_OK;
 }
 

@@ -37,6 +37,11 @@ struct Ensemble {
     std::vector<GocMemberDesc> host;      // descriptors as created (set 0 current)
     GocMemberDesc* d_members = nullptr;   // device copy, buffers swapped on device
     int4* d_tiles = nullptr;              // runs (member, tile_x, first tile_y, tiles)
+    CUtensorMap* d_tmaps = nullptr;       // [shape][member][buffer set][eta, hu, hv] TMA maps of the state
+    const float** d_tma_base = nullptr;   // per member: set-0 eta buffer (null: member not staged by TMA)
+    int* d_tma_err = nullptr;             // set when a staging wait ran out
+    unsigned long long* d_tma_tiles = nullptr;  // tiles staged by TMA so far
+    int n_tma_members = 0;
     float* d_dt = nullptr;                // n_members x max_substeps
     int* d_nsub = nullptr;                // n_substeps per member
     int4* d_dt_items = nullptr;           // CFL work: (member, bx, by, partial index)
@@ -81,10 +86,25 @@ __global__ void __launch_bounds__(kNT, MINB)
 ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __restrict__ tiles, int n_tiles,
                     const float* __restrict__ dt_table, const int* __restrict__ nsub, int max_sub, int k,
                     float* const* __restrict__ drift_pos, const int4* __restrict__ drift_chunks, int n_chunks,
-                    float sensitivity) {
-    extern __shared__ __align__(16) float smem_raw[];
+                    float sensitivity, const CUtensorMap* __restrict__ tmaps,
+                    const float* const* __restrict__ tma_base, int* tma_err,
+                    unsigned long long* tma_tiles) {
+    extern __shared__ __align__(128) float smem_raw[];
+    // TMA writes the staging planes on 128-byte boundaries: stage only if the
+    // dynamic shared memory starts on one (the pointer itself stays the
+    // shared array, so every access keeps shared-memory addressing)
+    const bool smem_aligned = (smem_u32(smem_raw) & 127u) == 0;
     __shared__ GocMemberDesc md;
     __shared__ StepConst kc;
+    __shared__ __align__(8) uint64_t tma_bar;
+    __shared__ int tma_off;
+    if (threadIdx.x == 0) {
+        mbar_init(&tma_bar, 1);
+        tma_off = 0;
+    }
+    __syncthreads();
+    TileTma tma{nullptr, &tma_bar, 0u, false, -1, &tma_off, tma_err};
+    unsigned staged_tiles = 0;  // counted by thread 0
     int cur = -1;
     // Work items: the RK2 tiles of step k, then (for k >= 1) the drifter
     // chunks of step k-1, which read the input state of step k (buffer set
@@ -115,17 +135,33 @@ ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __res
         const float dt = __ldg(dt_table + (size_t)m * max_sub + k);
         float* side = smem_raw + sizeof(TileSmem<TX + 8, TY + 8>) / sizeof(float);
         constexpr int NSIDE = 3 * kHandRows * (TX + 8);
+        // TMA staging of the member's input set (interior tiles only); tma_off
+        // is read after a barrier, so the choice is the same in every thread
+        const float* base = tma_base[m];
+        const bool use_tma = base != nullptr && tma_off == 0 && smem_aligned;
+        tma.in_maps = use_tma ? tmaps + ((size_t)m * 2 + (md.eta[in] == base ? 0 : 1)) * 3 : nullptr;
+        bool pending = false;  // the previous tile of the run staged this one
         for (int r = 0; r < t.w; ++r) {
+            const int ty = t.z + r;
+            tma.staged = use_tma && !tile_on_border<TX, TY, 2>(md.p, t.y, ty);
+            staged_tiles += tma.staged ? 1u : 0u;
+            if (tma.staged && !pending && threadIdx.x == 0)
+                tma_stage_tile<TX + 8, TY + 8>(tma, *reinterpret_cast<TileSmem<TX + 8, TY + 8>*>(smem_raw),
+                                               t.y * TX - 4, 2 + ty * TY - 4);
+            tma.next_tile_y =
+                (use_tma && r + 1 < t.w && !tile_on_border<TX, TY, 2>(md.p, t.y, ty + 1)) ? ty + 1 : -1;
             // stage-1 rows handed along the run through two alternating buffers
             const float* side_in = side + ((r + 1) & 1) * NSIDE;
             float* side_out = r + 1 < t.w ? side + (r & 1) * NSIDE : nullptr;
             cdklm_strip_tile<TX, TY, kNT, CONST_F, SIMPLE_FORCING>(
-                md.p, kc, dt, t.y, t.z + r, r > 0, md.eta[in], md.hu[in], md.hv[in], md.eta[out], md.hu[out],
+                md.p, kc, dt, t.y, ty, r > 0, md.eta[in], md.hu[in], md.hv[in], md.eta[out], md.hu[out],
                 md.hv[out], md.pitch / 4, md.Hi, md.Hi_pitch / 4, md.Hm, md.Hm_pitch / 4, smem_raw, side_in,
-                side_out);
+                side_out, &tma);
+            pending = tma.next_tile_y >= 0;
             __syncthreads();
         }
     }
+    if (threadIdx.x == 0 && staged_tiles) atomicAdd(tma_tiles, (unsigned long long)staged_tiles);
 }
 
 // Dynamic shared memory of the persistent kernel: the tile planes plus two
@@ -167,7 +203,9 @@ int launch_ensemble(Ensemble* e, int k, cudaStream_t st) {
     const int items = e->n_runs + (k >= 1 ? e->n_drift_chunks : 0);
     const int grid = std::min(items, full);
     kern<<<grid, kNT, smem, st>>>(e->d_members, e->d_tiles, e->n_runs, e->d_dt, e->d_nsub, e->max_substeps, k,
-                                  e->d_drift_pos, e->d_drift_chunks, e->n_drift_chunks, e->drift_sensitivity);
+                                  e->d_drift_pos, e->d_drift_chunks, e->n_drift_chunks, e->drift_sensitivity,
+                                  e->d_tmaps + (size_t)e->shape * e->n_members * 6, e->d_tma_base, e->d_tma_err,
+                                  e->d_tma_tiles);
     count_launch();
     return check_launch("ensemble_rk2_kernel");
 }

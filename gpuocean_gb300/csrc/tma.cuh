@@ -1,0 +1,80 @@
+// Tensor-memory-accelerator (TMA) staging of state tiles: 2-D tiled bulk
+// copies global -> shared that complete on an mbarrier (sm_90+ PTX, used
+// here for sm_103a).  Only the types of <cuda.h> are used; the tensor maps
+// are encoded through the driver entry point the runtime hands out, so the
+// library does not link libcuda.
+#pragma once
+
+#include <cuda.h>
+#include <stdint.h>
+
+namespace goc {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    // make the initialised barrier visible to the async proxy
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// The calling thread arrives on the barrier and announces `bytes` of copies.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Wait for the phase of parity `parity` to complete, at most `limit` polls
+// (each poll may suspend the thread for a hardware-defined interval).
+// Returns false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int limit) {
+    for (int it = 0; it < limit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// Order this thread's earlier generic-proxy accesses of shared memory (made
+// visible to it by a preceding barrier) before later async-proxy writes.
+__device__ __forceinline__ void fence_proxy_async_shared() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Tiled 2-D copy of the box at (x, y) (elements; x * 4 bytes must be a
+// multiple of 16) of `map` into shared memory at `dst`, completing on `bar`.
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Polls before a staging wait gives up (far longer than any copy takes).
+constexpr int kTmaWaitLimit = 1 << 22;
+
+// Per-CTA state of the staging of one tile's (eta, hu, hv) (Q^n) by TMA.
+struct TileTma {
+    const CUtensorMap* in_maps;  // eta, hu, hv maps of the input buffer set (null: no staging)
+    uint64_t* bar;               // completes when a staged tile has landed
+    uint32_t phase;              // parity of the barrier phase to wait for next
+    bool staged;                 // this tile's Q^n is (being) staged
+    int next_tile_y;             // tile row to stage during this tile's last phase (-1: none)
+    int* off;                    // shared flag: a wait ran out, the CTA stops staging
+    int* err;                    // global flag the host reads
+};
+
+}  // namespace goc

@@ -244,6 +244,15 @@ class BatchedEnsemble:
         _lib.call("goc_ensemble_size", self._handle, ctypes.byref(nm), ctypes.byref(nt))
         return nt.value
 
+    def tma_status(self):
+        """(members whose interior tiles stage their input state by TMA,
+        tiles staged so far, staging waits that ran out - 0 in normal
+        operation).  Synchronises."""
+        staged, tiles, errors = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_int()
+        _lib.call("goc_ensemble_tma_status", self._handle, ctypes.byref(staged), ctypes.byref(tiles),
+                  ctypes.byref(errors))
+        return staged.value, tiles.value, errors.value
+
     # ------------------------------------------------------------------
     @staticmethod
     def tile_shapes():

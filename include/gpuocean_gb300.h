@@ -420,6 +420,15 @@ typedef struct GocMemberDesc {
 int goc_ensemble_create(const GocMemberDesc* members, int n_members, int max_substeps, void** ensemble);
 int goc_ensemble_destroy(void* ensemble);
 int goc_ensemble_size(void* ensemble, int* n_members, int* n_tiles);
+/*
+ * TMA staging of the step's input state: number of members whose interior
+ * tiles load (eta, hu, hv) by tensor-map bulk copies (every buffer on a
+ * 16-byte boundary and a row pitch that is a multiple of 16 bytes), the
+ * number of tiles staged so far, and the device flag set when a staging wait
+ * ran out (0 in normal operation; the CTA then loads with ordinary loads).
+ * Reading the device counters synchronises.  Any output may be NULL.
+ */
+int goc_ensemble_tma_status(void* ensemble, int* staged_members, long long* staged_tiles, int* wait_errors);
 
 /*
  * Per-member step schedule of one block: dt_table is n_members x

@@ -50,6 +50,27 @@ def test_batched_equals_member_by_member(gpu_ctx, use_graph):
         assert np.array_equal(sa.drifters.getObservationPosition(), sb.drifters.getObservationPosition())
 
 
+def test_tma_staging_status(gpu_ctx):
+    """Members whose buffers and row pitch sit on 16-byte boundaries stage
+    their interior tiles by TMA (33x17 has a 148-byte pitch: ordinary loads);
+    no staging wait runs out.  Results are covered by the bit-identity test
+    above, whose 128x64 member has interior tiles in runs of two."""
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
+    a = [_member(gpu_ctx, *s) for s in SPECS]
+    ens = BatchedEnsemble(a, autotune=False)
+    ens.set_tile_shape(0)  # 32x16
+    assert ens.tile_shape == (32, 16)
+    for _ in range(2):
+        ens.step(60.0)
+    ens.synchronize()
+    staged, tiles, errors = ens.tma_status()
+    assert staged == 3
+    # interior 32x16 tiles: 2 x 2 of the 128x64 member per RK2 step (none
+    # on the smaller grids), at least one step per 60 s block
+    assert tiles >= 2 * 4
+    assert errors == 0
+
+
 def test_batched_dt_matches_single(gpu_ctx):
     from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
     a = [_member(gpu_ctx, *s) for s in SPECS]
