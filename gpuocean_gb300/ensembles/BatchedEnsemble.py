@@ -51,7 +51,8 @@ def step_schedule(dt, t_end):
 class BatchedEnsemble:
     """Steps a list of RK2 ``CDKLM16`` simulators together on one GPU stream.
 
-    share_bathymetry: point members with identical corner depths at one copy
+    share_bathymetry: point members with identical corner depths (and members
+    with identical per-cell Coriolis tables) at one copy
     (None = detect by comparing the device arrays once).
     use_graph: replay each distinct block schedule as a CUDA graph.
     """
@@ -74,11 +75,13 @@ class BatchedEnsemble:
         self._noise_sources = None
         self._rng_seed = None
         self._bathy_owner = list(range(len(sims)))
+        self._coriolis_owner = list(range(len(sims)))
         self._shape_index = 0
         if share_bathymetry is None:
             share_bathymetry = True
         if share_bathymetry:
             self._dedupe_bathymetry()
+            self._dedupe_coriolis()
         self._orig_streams = []
         self._adopt_streams(self.sims)
         self._build()
@@ -96,6 +99,20 @@ class BatchedEnsemble:
             else:
                 seen[key] = (m, Bi)
 
+    def _dedupe_coriolis(self):
+        # members with identical per-cell Coriolis tables (beta planes) read
+        # one copy, which then stays in L2 instead of one copy per member
+        seen = {}
+        for m, s in enumerate(self.sims):
+            if s.coriolis_cell is None:
+                continue
+            F = np.ascontiguousarray(np.ma.getdata(s.coriolis_cell.download(s.gpu_stream)))
+            key = (F.shape, F.tobytes().__hash__())
+            if key in seen and np.array_equal(seen[key][1], F):
+                self._coriolis_owner[m] = seen[key][0]
+            else:
+                seen[key] = (m, F)
+
     def _descs(self):
         descs = (GocMemberDesc * len(self.sims))()
         for m, s in enumerate(self.sims):
@@ -105,6 +122,9 @@ class BatchedEnsemble:
             b = self.sims[self._bathy_owner[m]].bathymetry
             d.Hi, d.Hi_pitch = b.Bi.ptr, int(b.Bi.pitch)
             d.Hm, d.Hm_pitch = b.Bm.ptr, int(b.Bm.pitch)
+            c = self.sims[self._coriolis_owner[m]].coriolis_cell
+            if c is not None:
+                d.p.coriolis_cell, d.p.coriolis_cell_pitch = c.ptr, int(c.pitch)
             g = s.gpu_data
             d.eta[0], d.eta[1] = g.h0.ptr, g.h1.ptr
             d.hu[0], d.hu[1] = g.hu0.ptr, g.hu1.ptr

@@ -81,12 +81,27 @@ def test_batched_dt_matches_single(gpu_ctx):
 
 
 def test_member_counts_and_shared_bathymetry(gpu_ctx):
+    """Identical corner depths and identical beta-plane Coriolis tables are
+    read from one copy; the shared tables give the members' own results."""
     from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
-    a = [_member(gpu_ctx, 64, 40, (1, 2, 1, 2), 3) for _ in range(3)] + [_member(gpu_ctx, 64, 40, (1, 2, 1, 2), 9)]
+    spec = [(128, 64, (1, 2, 1, 2), 3)] * 3 + [(128, 64, (1, 2, 1, 2), 9)]
+    a = [_member(gpu_ctx, *s) for s in spec]
+    b = [_member(gpu_ctx, *s) for s in spec]
     ens = BatchedEnsemble(a)
     assert ens._bathy_owner == [0, 0, 0, 3]
+    assert ens._coriolis_owner == [0, 0, 0, 0]
     tx, ty = ens.tile_shape
-    assert ens.n_tiles == 4 * ((64 + tx - 1) // tx) * ((40 + ty - 1) // ty)
+    assert ens.n_tiles == 4 * ((128 + tx - 1) // tx) * ((64 + ty - 1) // ty)
+    for s in a + b:
+        s.updateDt()
+    for _ in range(2):
+        ens.step(60.0)
+        for s in b:
+            s.step(60.0)
+    ens.synchronize()
+    for sa, sb in zip(a, b):
+        for x, y in zip(sa.download(), sb.download()):
+            assert np.array_equal(np.asarray(x)[2:-2, 2:-2], np.asarray(y)[2:-2, 2:-2])
 
 
 def _with_noise(sims, factor, seed):
