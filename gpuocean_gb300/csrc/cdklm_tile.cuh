@@ -627,17 +627,13 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
         __syncthreads();
         T.template faces<2, W - 2, 2, H - 2, CONST_F>(s1 - 2);
         __syncthreads();
-        constexpr int NU = (W - 4) * (H - 4);
         const int nu = (W - 4) * (H - 2 - s1);
-        // Results are kept in registers until every thread has read its
-        // cell of D^n, then written as D* (each thread owns its cells).
-        constexpr int PER = (NU + NT - 1) / NT;
-        float qe[PER], qu[PER], qv[PER];
-#pragma unroll
-        for (int r = 0; r < PER; ++r) {
-            const int idx = threadIdx.x + r * NT;
-            qe[r] = 0.f; qu[r] = 0.f; qv[r] = 0.f;
-            if (idx >= nu) continue;
+        // Results go to the planes Sx[0], Sx[1], Sy[0] (dead after the faces:
+        // the cell update reads only Sx[2] and Sy[2]) and become D* once
+        // every thread has read its cell of D^n.  A rolled loop keeps one copy
+        // of the cell update in the kernel (the step is sensitive to the
+        // instruction cache).
+        for (int idx = threadIdx.x; idx < nu; idx += NT) {
             int i, j;
             block_cell<W - 4>(idx, H - 2 - s1, i, j);
             i += 2; j += s1;
@@ -653,13 +649,10 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
             float nhu = (hu + dt * L2) / (1.0f + C);
             float nhv = (hv + dt * L3) / (1.0f + C);
             finish_cell(p, Hm, ne, nhu, nhv);
-            qe[r] = ne; qu[r] = nhu; qv[r] = nhv;
+            S.Sx[0][j][i] = ne; S.Sx[1][j][i] = nhu; S.Sy[0][j][i] = nhv;
         }
         __syncthreads();
-#pragma unroll
-        for (int r = 0; r < PER; ++r) {
-            const int idx = threadIdx.x + r * NT;
-            if (idx >= nu) continue;
+        for (int idx = threadIdx.x; idx < nu; idx += NT) {
             int i, j;
             block_cell<W - 4>(idx, H - 2 - s1, i, j);
             i += 2; j += s1;
@@ -667,14 +660,15 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
             const bool okx = !BORDER || px || (gx >= 2 && gx < nx + 2);
             const bool oky = !BORDER || py || (gy >= 2 && gy < ny + 2);
             if (!(okx && oky)) continue;
+            const float qe = S.Sx[0][j][i], qu = S.Sx[1][j][i], qv = S.Sy[0][j][i];
             // the first-stage state of the tile's own cells, when asked for
             // (the adjoint's second-stage VJP reads it)
             if (e_alt && i >= HALO && i < HALO + TX && j >= HALO && j < HALO + TY && gx < nx + 2 && gy < ny + 2) {
                 const size_t os = (size_t)gy * pitch + gx;
-                e_alt[os] = qe[r]; hu_alt[os] = qu[r]; hv_alt[os] = qv[r];
+                e_alt[os] = qe; hu_alt[os] = qu; hv_alt[os] = qv;
             }
             float oe, ou, ov;
-            desingularize_cell(p, qe[r], qu[r], qv[r], S.Hmb[j][i], oe, ou, ov);
+            desingularize_cell(p, qe, qu, qv, S.Hmb[j][i], oe, ou, ov);
             S.D[0][j][i] = oe; S.D[1][j][i] = ou; S.D[2][j][i] = ov;
             if (BORDER) {
                 // wall ghosts of the stage result (K/CDKLM16_kernel.cu:420-470)
@@ -687,20 +681,20 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
                 const int gxs = px ? wrap_interior(gx, nx) : gx;
                 const int gys = py ? wrap_interior(gy, ny) : gy;
                 if (p.bc_north == 1) {
-                    if (gys == ny + 1) mirror(i, j + 1, qe[r], qu[r], -qv[r]);
-                    if (gys == ny) mirror(i, j + 3, qe[r], qu[r], -qv[r]);
+                    if (gys == ny + 1) mirror(i, j + 1, qe, qu, -qv);
+                    if (gys == ny) mirror(i, j + 3, qe, qu, -qv);
                 }
                 if (p.bc_south == 1) {
-                    if (gys == 2) mirror(i, j - 1, qe[r], qu[r], -qv[r]);
-                    if (gys == 3) mirror(i, j - 3, qe[r], qu[r], -qv[r]);
+                    if (gys == 2) mirror(i, j - 1, qe, qu, -qv);
+                    if (gys == 3) mirror(i, j - 3, qe, qu, -qv);
                 }
                 if (p.bc_east == 1) {
-                    if (gxs == nx + 1) mirror(i + 1, j, qe[r], -qu[r], qv[r]);
-                    if (gxs == nx) mirror(i + 3, j, qe[r], -qu[r], qv[r]);
+                    if (gxs == nx + 1) mirror(i + 1, j, qe, -qu, qv);
+                    if (gxs == nx) mirror(i + 3, j, qe, -qu, qv);
                 }
                 if (p.bc_west == 1) {
-                    if (gxs == 2) mirror(i - 1, j, qe[r], -qu[r], qv[r]);
-                    if (gxs == 3) mirror(i - 3, j, qe[r], -qu[r], qv[r]);
+                    if (gxs == 2) mirror(i - 1, j, qe, -qu, qv);
+                    if (gxs == 3) mirror(i - 3, j, qe, -qu, qv);
                 }
             }
         }
