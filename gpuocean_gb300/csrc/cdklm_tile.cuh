@@ -714,22 +714,6 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
             if (s1 != 2) __syncthreads();
         }
         // ---- stage 2 on the tile ----
-        // Q^n of the thread's own output cells, loaded now so that the
-        // loads overlap the stage-2 slopes and faces
-        constexpr int PER2 = (TX * TY + NT - 1) / NT;
-        float qa[PER2][3];
-#pragma unroll
-        for (int r = 0; r < PER2; ++r) {
-            const int idx = threadIdx.x + r * NT;
-            qa[r][0] = qa[r][1] = qa[r][2] = 0.0f;
-            if (idx >= TX * TY) continue;
-            const int gx = T.x0 + 4 + idx % TX, gy = T.y0 + 4 + idx / TX;
-            if (BORDER && (gx >= nx + 2 || gy >= ny + 2)) continue;
-            const size_t o = (size_t)gy * pitch + gx;
-            qa[r][0] = __ldg(e_in + o);
-            qa[r][1] = __ldg(hu_in + o);
-            qa[r][2] = __ldg(hv_in + o);
-        }
         T.template slopes<4, W - 4, 4, H - 4, CONST_F>();
         __syncthreads();
         T.template faces<4, W - 4, 4, H - 4, CONST_F>();
@@ -738,18 +722,17 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
         // tile of the strip there meanwhile
         if (tma && tma->next_tile_y >= 0 && threadIdx.x == 0)
             tma_stage_tile<W, H>(*tma, S, T.x0 - 2, 2 + tma->next_tile_y * TY - HALO);
-#pragma unroll
-        for (int r = 0; r < PER2; ++r) {
-            const int idx = threadIdx.x + r * NT;
-            if (idx >= TX * TY) continue;
+        // A rolled loop keeps one copy of the cell update; Q^n of the cell is
+        // loaded first, so its latency overlaps the update.
+        for (int idx = threadIdx.x; idx < TX * TY; idx += NT) {
             const int i = 4 + idx % TX, j = 4 + idx / TX;
             const int gx = T.x0 + i, gy = T.y0 + j;
             if (BORDER && (gx >= nx + 2 || gy >= ny + 2)) continue;
+            const size_t o = (size_t)gy * pitch + gx;
+            const float ea = __ldg(e_in + o), hua = __ldg(hu_in + o), hva = __ldg(hv_in + o);
             float L1, L2, L3, ec, hu, hv, Hm, hsum;
             T.template rhs<CONST_F, SIMPLE_FORCING>(i, j, gx, gy, L1, L2, L3, ec, hu, hv, Hm, hsum);
             const float C = T.friction(dt, hsum, hu, hv);
-            const size_t o = (size_t)gy * pitch + gx;
-            const float ea = qa[r][0], hua = qa[r][1], hva = qa[r][2];
             float ne = 0.5f * (ea + (ec + dt * L1));
             float nhu = 0.5f * (hua + (hu + dt * L2)) / (1.0f + 0.5f * C);
             float nhv = 0.5f * (hva + (hv + dt * L3)) / (1.0f + 0.5f * C);
