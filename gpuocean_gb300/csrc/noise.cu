@@ -258,31 +258,30 @@ constexpr int kPR = kPY / kPT;                      // cells per thread
 constexpr int kNC = 12;  // coarse cells per tile edge held in shared memory (factor >= 4 for 34 fine cells)
 
 // One kPX x kPY tile of interior cells (tile origin bx, by in interior
-// cells).  Each thread owns kPR cells of one column; their state and corner
-// depths are loaded first so that the loads overlap the perturbation field.
+// cells).  Each thread owns kPR cells of one column; their state is loaded
+// first so that the loads overlap the perturbation field (the corner depths,
+// shared by the members and L2-resident, are read when used).
 __device__ void perturb_tile(const GocNoiseDesc& d, const OceanRef& o, int bx, int by) {
     __shared__ float s_de[kPY + 2][kPX + 2];
     __shared__ float s_A[kNC * kNC][17];
+    // coarse column / row of every fine column / row of the tile + 1 ring and
+    // the fractional position in it (the bicubic index is separable)
+    __shared__ int s_ci[kPX + 2], s_cj[kPY + 2];
+    __shared__ float s_rx[kPX + 2], s_ry[kPY + 2];
     const int tx = threadIdx.x, t = threadIdx.y * kPX + tx;
     constexpr int NT = kPX * kPT;
     const bool factor1 = d.interpolation_factor <= 1;
     const int ti = 2 + bx + tx;
-    float q[kPR][3], hc[kPR][4];
+    float q[kPR][3];
 #pragma unroll
     for (int r = 0; r < kPR; ++r) {
         const int tj = 2 + by + threadIdx.y + r * kPT;
         q[r][0] = q[r][1] = q[r][2] = 0.0f;
-        hc[r][0] = hc[r][1] = hc[r][2] = hc[r][3] = 0.0f;
         if (ti < o.nx + 2 && tj < o.ny + 2) {
             const size_t k = (size_t)tj * o.pitch + ti;
             q[r][0] = o.eta[k];
             q[r][1] = o.hu[k];
             q[r][2] = o.hv[k];
-            const float* h0 = o.Hi + (size_t)tj * o.hi_pitch + ti;
-            hc[r][0] = h0[0];
-            hc[r][1] = h0[1];
-            hc[r][2] = h0[o.hi_pitch];
-            hc[r][3] = h0[o.hi_pitch + 1];
         }
     }
     // d_eta on the tile + 1 ring (interior origin at ghost offset 2)
@@ -299,13 +298,16 @@ __device__ void perturb_tile(const GocNoiseDesc& d, const OceanRef& o, int bx, i
         const int ncx = ci1 - ci0 + 1, ncy = cj1 - cj0 + 1;
         if (ncx <= kNC && ncy <= kNC) {
             for (int c = t; c < ncx * ncy; c += NT) bicubic_coeffs(d, ci0 + c % ncx, cj0 + c / ncx, s_A[c]);
+            if (t < kPX + 2) {
+                s_ci[t] = clampi(bicubic_ci(d, o, gi0 + t, &s_rx[t]) - ci0, 0, ncx - 1);
+            } else if (t >= 64 && t < 64 + kPY + 2) {
+                const int j = t - 64;
+                s_cj[j] = clampi(bicubic_cj(d, o, gj0 + j, &s_ry[j]) - cj0, 0, ncy - 1);
+            }
             __syncthreads();
             for (int c = t; c < NR; c += NT) {
                 const int j = c / (kPX + 2), i = c % (kPX + 2);
-                float rx, ry;
-                const int ci = bicubic_ci(d, o, gi0 + i, &rx), cj = bicubic_cj(d, o, gj0 + j, &ry);
-                const int a = clampi(cj - cj0, 0, ncy - 1) * ncx + clampi(ci - ci0, 0, ncx - 1);
-                s_de[j][i] = bicubic_eval(s_A[a], rx, ry);
+                s_de[j][i] = bicubic_eval(s_A[s_cj[j] * ncx + s_ci[i]], s_rx[i], s_ry[j]);
             }
         } else {
             for (int c = t; c < NR; c += NT)
@@ -316,10 +318,13 @@ __device__ void perturb_tile(const GocNoiseDesc& d, const OceanRef& o, int bx, i
 #pragma unroll
     for (int r = 0; r < kPR; ++r) {
         const int tj = 2 + by + threadIdx.y + r * kPT;
-        if (ti < o.nx + 2 && tj < o.ny + 2)
+        if (ti < o.nx + 2 && tj < o.ny + 2) {
+            const float* h0 = o.Hi + (size_t)tj * o.hi_pitch + ti;
+            const float hc[4] = {__ldg(h0), __ldg(h0 + 1), __ldg(h0 + o.hi_pitch), __ldg(h0 + o.hi_pitch + 1)};
             perturb_cell(d, o, ti, tj, factor1,
                          [&](int jj, int ii) { return s_de[jj - (2 + by) + 1][ii - (2 + bx) + 1]; },
-                         q[r][0], q[r][1], q[r][2], hc[r]);
+                         q[r][0], q[r][1], q[r][2], hc);
+        }
     }
     __syncthreads();
 }
