@@ -133,6 +133,7 @@ SIGNATURES = {
     "goc_ensemble_size": (c_int, [c_void_p, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
     "goc_ensemble_tma_status": (c_int, [c_void_p, ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_longlong),
                                         ctypes.POINTER(c_int)]),
+    "goc_selftest_wait_timeout": (c_int, [ctypes.c_double, ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_double)]),
     "goc_ensemble_set_schedule": (c_int, [c_void_p, c_fp, ctypes.POINTER(c_int), c_void_p]),
     "goc_ensemble_rk2_substep": (c_int, [c_void_p, c_int, c_void_p]),
     "goc_ensemble_end_block": (c_int, [c_void_p, c_int, c_void_p]),

@@ -558,7 +558,7 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
     // boundaries): wait for it.  A wait that runs out falls back to loads.
     bool staged = false;
     if (!BORDER && tma && tma->staged) {
-        staged = mbar_wait_bounded(tma->bar, tma->phase, kTmaWaitLimit);
+        staged = mbar_wait_bounded(tma->bar, tma->phase, kTmaWaitLimitNs);
         tma->phase ^= 1u;
         if (!staged) {
             *tma->off = 1;

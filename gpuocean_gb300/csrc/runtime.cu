@@ -7,6 +7,7 @@
 #include <string>
 
 #include "common.cuh"
+#include "tma.cuh"
 
 namespace goc {
 
@@ -220,3 +221,48 @@ int goc_graph_destroy(void* graph_exec) {
 int64_t goc_kernel_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// self-test of the bounded mbarrier wait that guards TMA staging
+// ---------------------------------------------------------------------------
+
+namespace goc {
+// Waits on a barrier phase that nothing completes; the wait must give up
+// after limit_ns and report it.
+__global__ void wait_timeout_selftest_kernel(int* timed_out, unsigned long long* waited_ns, uint64_t limit_ns) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    const uint64_t t0 = global_ns();
+    const bool done = mbar_wait_bounded(&bar, 0, limit_ns);
+    const uint64_t t1 = global_ns();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *timed_out = done ? 0 : 1;
+        *waited_ns = t1 - t0;
+    }
+}
+}  // namespace goc
+
+extern "C" int goc_selftest_wait_timeout(double limit_ms, int* timed_out, double* waited_ms) {
+    if (!timed_out || !waited_ms || !(limit_ms > 0.0) || limit_ms > 1000.0)
+        return goc::set_error(GOC_ERR_ARG, "goc_selftest_wait_timeout: limit in (0, 1000] ms and outputs required");
+    int* d_flag = nullptr;
+    unsigned long long* d_ns = nullptr;
+    cudaError_t err = cudaMalloc(&d_flag, sizeof(int));
+    if (err == cudaSuccess) err = cudaMalloc(&d_ns, sizeof(unsigned long long));
+    if (err == cudaSuccess) {
+        goc::wait_timeout_selftest_kernel<<<1, 64>>>(d_flag, d_ns, (uint64_t)(limit_ms * 1e6));
+        err = cudaGetLastError();
+    }
+    int flag = 0;
+    unsigned long long ns = 0;
+    if (err == cudaSuccess) err = cudaMemcpy(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost);
+    if (err == cudaSuccess) err = cudaMemcpy(&ns, d_ns, sizeof(ns), cudaMemcpyDeviceToHost);
+    cudaFree(d_flag);
+    cudaFree(d_ns);
+    if (err != cudaSuccess) return goc::set_error(GOC_ERR_CUDA, "goc_selftest_wait_timeout: %s", cudaGetErrorString(err));
+    *timed_out = flag;
+    *waited_ms = ns / 1e6;
+    return GOC_OK;
+}

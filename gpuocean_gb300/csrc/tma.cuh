@@ -38,11 +38,19 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return done != 0;
 }
 
-// Wait for the phase of parity `parity` to complete, at most `limit` polls
-// (each poll may suspend the thread for a hardware-defined interval).
-// Returns false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int limit) {
-    for (int it = 0; it < limit; ++it)
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait for the phase of parity `parity` to complete, for at most `limit_ns`
+// nanoseconds of the global timer (and at most 2^26 polls, whatever the
+// timer does).  Returns false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (uint32_t it = 0; it < (1u << 26) && global_ns() - t0 < limit_ns; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -63,8 +71,8 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
         : "memory");
 }
 
-// Polls before a staging wait gives up (far longer than any copy takes).
-constexpr int kTmaWaitLimit = 1 << 22;
+// Time after which a staging wait gives up (far longer than any copy takes).
+constexpr uint64_t kTmaWaitLimitNs = 200000000ull;  // 0.2 s
 
 // Per-CTA state of the staging of one tile's (eta, hu, hv) (Q^n) by TMA.
 struct TileTma {

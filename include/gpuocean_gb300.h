@@ -429,6 +429,14 @@ int goc_ensemble_size(void* ensemble, int* n_members, int* n_tiles);
  * Reading the device counters synchronises.  Any output may be NULL.
  */
 int goc_ensemble_tma_status(void* ensemble, int* staged_members, long long* staged_tiles, int* wait_errors);
+/*
+ * Self-test of the bounded wait that guards TMA staging: one CTA waits on an
+ * mbarrier phase that nothing completes, for limit_ms (0 < limit_ms <= 1000)
+ * of the GPU's global timer.  timed_out = 1 when the wait gave up as it
+ * should; waited_ms = the time it waited.  Nothing faults and nothing hangs:
+ * the kernel returns and the context stays usable.
+ */
+int goc_selftest_wait_timeout(double limit_ms, int* timed_out, double* waited_ms);
 
 /*
  * Per-member step schedule of one block: dt_table is n_members x

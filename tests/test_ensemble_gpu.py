@@ -71,6 +71,21 @@ def test_tma_staging_status(gpu_ctx):
     assert errors == 0
 
 
+def test_staging_wait_gives_up(gpu_ctx):
+    """The wait that guards TMA staging is bounded by the GPU's clock: on a
+    barrier phase that nothing completes it gives up after its limit and says
+    so, and the context stays usable (a step runs afterwards)."""
+    import ctypes
+    from gpuocean_gb300 import _lib
+    timed_out, waited = ctypes.c_int(), ctypes.c_double()
+    _lib.call("goc_selftest_wait_timeout", ctypes.c_double(5.0), ctypes.byref(timed_out), ctypes.byref(waited))
+    assert timed_out.value == 1
+    assert 5.0 <= waited.value < 1000.0
+    sim = _member(gpu_ctx, 64, 40, (1, 2, 1, 2), 3)
+    sim.step(60.0)
+    assert np.isfinite(np.asarray(sim.download()[0])).all()
+
+
 def test_batched_dt_matches_single(gpu_ctx):
     from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
     a = [_member(gpu_ctx, *s) for s in SPECS]
