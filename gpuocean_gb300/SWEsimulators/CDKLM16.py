@@ -270,6 +270,12 @@ class CDKLM16(Simulator):
         if self.t == 0:
             self.bc_kernel.update_bc_values(self.gpu_stream, self.t)
             self.bc_kernel.boundaryCondition(self.gpu_stream, self.gpu_data.h0, self.gpu_data.hu0, self.gpu_data.hv0)
+        # nothing between the RK2 steps: the run of steps goes to the library
+        # in one call once both forcing weights are 1 (time-independent forcing)
+        plain = (not update_dt and self.rk_order == 2 and not self.boundary_conditions.isSponge()
+                 and not (self.model_error is not None and apply_stochastic_term)
+                 and not self.hasDrifters and not self.hasCrossProductDrifter
+                 and len(self.wind_stress.t) == 1 and len(self.atmospheric_pressure.t) == 1)
         t_now = 0.0
         while t_now < t_end:
             if update_dt:
@@ -277,6 +283,8 @@ class CDKLM16(Simulator):
             local_dt = np.float32(min(self.dt, np.float32(t_end - t_now)))
             self._params.wind_t = float(np.float32(self.update_wind_stress()))
             self._params.atm_p_t = float(np.float32(self.update_atmospheric_pressure()))
+            if plain and self._params.wind_t == 1.0 and self._params.atm_p_t == 1.0:
+                return self._plain_steps(t_now, t_end)
             self.bc_kernel.update_bc_values(self.gpu_stream, self.t)
             self._rk_step(local_dt)
             perturbed = self.model_error is not None and apply_stochastic_term
@@ -289,6 +297,27 @@ class CDKLM16(Simulator):
             self.t += np.float64(local_dt)
             t_now += np.float64(local_dt)
             self.num_iterations += 1
+        return self.t
+
+    def _plain_steps(self, t_now, t_end):
+        """The remaining steps of step(t_end) as one goc_cdklm_rk2_steps call:
+        the same dt sequence, time and iteration bookkeeping as the loop."""
+        dts = []
+        while t_now < t_end:
+            local_dt = np.float32(min(self.dt, np.float32(t_end - t_now)))
+            dts.append(local_dt)
+            t_now += np.float64(local_dt)
+        arr = np.asarray(dts, dtype=np.float32)
+        d = self.gpu_data
+        _lib.call("goc_cdklm_rk2_steps", ctypes.byref(self._params), arr.ctypes.data, len(arr),
+                  d.h0.ptr, d.hu0.ptr, d.hv0.ptr, d.h1.ptr, d.hu1.ptr, d.hv1.ptr, int(d.h0.pitch),
+                  self.bathymetry.Bi.ptr, int(self.bathymetry.Bi.pitch),
+                  self.bathymetry.Bm.ptr, int(self.bathymetry.Bm.pitch), self.stream_handle)
+        if len(arr) % 2:
+            d.swap()
+        for x in arr:
+            self.t += np.float64(x)
+        self.num_iterations += len(arr)
         return self.t
 
     # ------------------------------------------------------------------

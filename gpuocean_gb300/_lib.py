@@ -75,6 +75,8 @@ SIGNATURES = {
     "goc_cdklm_rk2_step": (c_int, [ctypes.POINTER(GocCdklmParams), c_float,
                                    c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
                                    c_void_p, c_int, c_void_p, c_int, c_void_p]),
+    "goc_cdklm_rk2_steps": (c_int, [ctypes.POINTER(GocCdklmParams), c_void_p, c_int] + [c_void_p] * 6 +
+                            [c_int, c_void_p, c_int, c_void_p, c_int, c_void_p]),
     "goc_cdklm_rk2_step_stage": (c_int, [ctypes.POINTER(GocCdklmParams), c_float] + [c_void_p] * 9 +
                                  [c_int, c_void_p, c_int, c_void_p, c_int, c_void_p]),
     "goc_cdklm_stage": (c_int, [ctypes.POINTER(GocCdklmParams), c_float, c_int,

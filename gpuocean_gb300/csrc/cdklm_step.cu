@@ -133,6 +133,40 @@ extern "C" int goc_cdklm_rk2_step(const GocCdklmParams* p, float dt, const float
                        Hi, Hi_pitch / 4, Hm, Hm_pitch / 4, st);
 }
 
+// n_steps fused RK2 steps with the time steps dts[0..n_steps) (host
+// memory), alternating between buffer set 0 and set 1 from set 0: the state
+// ends in set n_steps % 2.  One launch per step, issued from this loop, so a
+// long run of steps is not bound by the caller's per-step overhead.
+extern "C" int goc_cdklm_rk2_steps(const GocCdklmParams* p, const float* dts, int n_steps, float* eta0, float* hu0,
+                                   float* hv0, float* eta1, float* hu1, float* hv1, int pitch, const float* Hi,
+                                   int Hi_pitch, const float* Hm, int Hm_pitch, void* stream) {
+    int rc = validate_params(p, "goc_cdklm_rk2_steps");
+    if (rc) return rc;
+    if ((rc = check_pitch(p, pitch, Hi_pitch, Hm_pitch, "goc_cdklm_rk2_steps"))) return rc;
+    if (n_steps < 0 || (n_steps > 0 && !dts)) return set_error(GOC_ERR_ARG, "goc_cdklm_rk2_steps: bad step list");
+    if (!eta0 || !hu0 || !hv0 || !eta1 || !hu1 || !hv1 || !Hi || !Hm)
+        return set_error(GOC_ERR_ARG, "goc_cdklm_rk2_steps: null buffer");
+    if (eta0 == eta1 || hu0 == hu1 || hv0 == hv1)
+        return set_error(GOC_ERR_ARG, "goc_cdklm_rk2_steps: the two buffer sets must differ");
+    if (p->rk_order != 2) return set_error(GOC_ERR_ARG, "goc_cdklm_rk2_steps: params.rk_order must be 2");
+    for (int s = 0; s < n_steps; ++s)
+        if (!(dts[s] >= 0.0f)) return set_error(GOC_ERR_ARG, "goc_cdklm_rk2_steps: dt %d must be >= 0", s);
+    StepConst k;
+    bool cf, sf;
+    cudaStream_t st = as_stream(stream);
+    if ((rc = make_const(p, &k, &cf, &sf))) return rc;
+    float* e[2] = {eta0, eta1};
+    float* u[2] = {hu0, hu1};
+    float* v[2] = {hv0, hv1};
+    for (int s = 0; s < n_steps; ++s) {
+        const int a = s & 1, b = a ^ 1;
+        if ((rc = dispatch<2>(p, k, cf, sf, dts[s], 1, e[a], u[a], v[a], e[b], u[b], v[b], nullptr, nullptr, nullptr,
+                              pitch / 4, Hi, Hi_pitch / 4, Hm, Hm_pitch / 4, st)))
+            return rc;
+    }
+    return GOC_OK;
+}
+
 extern "C" int goc_cdklm_rk2_step_stage(const GocCdklmParams* p, float dt, const float* eta0, const float* hu0,
                                         const float* hv0, float* eta1, float* hu1, float* hv1, float* eta_s,
                                         float* hu_s, float* hv_s, int pitch, const float* Hi, int Hi_pitch,

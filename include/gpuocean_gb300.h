@@ -128,6 +128,17 @@ int goc_cdklm_rk2_step(const GocCdklmParams* p, float dt,
                        void* stream);
 
 /*
+ * n_steps fused RK2 steps (dts in host memory), from buffer set 0
+ * (eta0, hu0, hv0) alternating with set 1; the state ends in set
+ * n_steps % 2.  The loop of CDKLM16.step (S/CDKLM16.py:493-509) for a run of
+ * steps with nothing between them (no model error, drifters, sponge or
+ * time-varying forcing), issued from the library.
+ */
+int goc_cdklm_rk2_steps(const GocCdklmParams* p, const float* dts, int n_steps, float* eta0, float* hu0,
+                        float* hv0, float* eta1, float* hu1, float* hv1, int pitch, const float* Hi, int Hi_pitch,
+                        const float* Hm, int Hm_pitch, void* stream);
+
+/*
  * goc_cdklm_rk2_step that also writes the first-stage state Q* of the
  * interior cells to (eta_s, hu_s, hv_s): the same values goc_cdklm_stage
  * with rk_step 0 gives, at no extra launch.  For the adjoint's recompute of

@@ -126,3 +126,32 @@ def test_friction_wind_and_dry_land(gpu_ctx):
         assert np.all(np.isfinite(a))
         assert np.max(np.abs(a - b)) / np.max(np.abs(b)) < 1e-4
     sim.cleanUp()
+
+
+def test_step_run_equals_step_by_step(gpu_ctx):
+    """One long step() call (after its first step, the run of steps is a
+    single library call) leaves the state, time and iteration count of the
+    same dt sequence taken one step() call at a time."""
+    from gpuocean_gb300.SWEsimulators import CDKLM16
+    from gpuocean_gb300.utils import BenchmarkCases, Common
+    sims = []
+    for _ in range(2):
+        c = BenchmarkCases.double_jet_case(nx=96, ny=64, dx=5000.0, dy=5000.0, seed=7)
+        s = CDKLM16.CDKLM16(gpu_ctx, c["eta0"], c["hu0"], c["hv0"], c["H"], 96, 64, c["dx"], c["dy"], 0.0, c["g"],
+                            c["f"], c["r"], coriolis_beta=c["coriolis_beta"],
+                            boundary_conditions=Common.BoundaryConditions(*c["boundary"]))
+        s.updateDt(courant_number=0.8)
+        sims.append(s)
+    a, b = sims
+    t_end = 25.5 * float(a.dt)
+    a.step(t_end)
+    dts, t_now = [], 0.0
+    while t_now < t_end:
+        dts.append(np.float32(min(b.dt, np.float32(t_end - t_now))))
+        t_now += np.float64(dts[-1])
+    for dt in dts:
+        b.step(float(dt))
+    assert a.num_iterations == b.num_iterations == 26
+    assert a.t == b.t
+    for x, y in zip(a.download(), b.download()):
+        assert np.array_equal(np.asarray(x), np.asarray(y))
