@@ -91,3 +91,42 @@ def test_new_entry_points_validate_without_gpu():
     big = np.array([99, 0, 0, 0], np.int32)
     assert lib.goc_sponge_boundary(8, 8, 4, 1, 1, 1, big.ctypes.data, 1, 1, 1, 48, None, None, 2, None, None, 2,
                                    0.0, None) == -1
+
+
+def test_step_run_and_tma_entries_validate_without_gpu():
+    """The multi-step entry, the TMA status query and the wait self-test
+    reject bad arguments before any CUDA call."""
+    import numpy as np
+    lib = _lib.load()
+    p = _lib.GocCdklmParams()
+    p.nx, p.ny, p.dx, p.dy, p.g, p.rk_order = 8, 8, 1.0, 1.0, 9.81, 2
+    p.theta, p.desing_eps, p.flux_slope_eps, p.depth_cutoff, p.flux_balancer = 1.3, 0.1, 0.1, 1e-5, 0.8
+    p.bc_north = p.bc_east = p.bc_south = p.bc_west = 1
+    p.land_value = 1e20
+    # one-value textures (validation checks the pointers and sizes, it does not read them)
+    for name in ("coriolis_f", "angle", "wind_x_cur", "wind_x_next", "wind_y_cur", "wind_y_next", "atm_p_cur",
+                 "atm_p_next"):
+        setattr(p, name, 16)
+    for name in ("coriolis", "angle", "wind_x", "wind_y", "atm_p"):
+        setattr(p, name + "_nx", 1)
+        setattr(p, name + "_ny", 1)
+    dts = np.full(3, 1.0, np.float32)
+    # null buffers
+    rc = lib.goc_cdklm_rk2_steps(ctypes.byref(p), dts.ctypes.data, 3, None, None, None, None, None, None, 48,
+                                 None, 52, None, 48, None)
+    assert rc == -1 and "null buffer" in _lib.last_error()
+    # negative step count / missing dt list / negative dt
+    rc = lib.goc_cdklm_rk2_steps(ctypes.byref(p), None, 2, 1, 1, 1, 2, 2, 2, 48, 1, 52, 1, 48, None)
+    assert rc == -1 and "step list" in _lib.last_error()
+    rc = lib.goc_cdklm_rk2_steps(ctypes.byref(p), dts.ctypes.data, -1, 1, 1, 1, 2, 2, 2, 48, 1, 52, 1, 48, None)
+    assert rc == -1 and "step list" in _lib.last_error()
+    bad = np.array([1.0, -1.0], np.float32)
+    rc = lib.goc_cdklm_rk2_steps(ctypes.byref(p), bad.ctypes.data, 2, 1, 1, 1, 2, 2, 2, 48, 1, 52, 1, 48, None)
+    assert rc == -1 and "dt 1" in _lib.last_error()
+    # the two buffer sets must differ
+    rc = lib.goc_cdklm_rk2_steps(ctypes.byref(p), dts.ctypes.data, 3, 1, 1, 1, 1, 1, 1, 48, 1, 52, 1, 48, None)
+    assert rc == -1 and "differ" in _lib.last_error()
+    assert lib.goc_ensemble_tma_status(None, None, None, None) == -1
+    timed_out, waited = ctypes.c_int(), ctypes.c_double()
+    assert lib.goc_selftest_wait_timeout(0.0, ctypes.byref(timed_out), ctypes.byref(waited)) == -1
+    assert lib.goc_selftest_wait_timeout(5000.0, ctypes.byref(timed_out), ctypes.byref(waited)) == -1
