@@ -225,18 +225,20 @@ def run_reference(args, spec, rank, world):
         return
     cores = os.cpu_count() or 1
     n_members = max(cores, 1)
-    rate, wall = cpu_reference_rate(spec, n_members, 1, cores)
-    rates = [rate]
-    for _ in range(max(0, args.steps - 1)):
-        if wall > 60:
-            break
-        r, _w = cpu_reference_rate(spec, n_members, 1, cores)
+    for _ in range(args.warmup):
+        cpu_reference_rate(spec, n_members, 1, cores)
+    # timed steps: at most K, and no more once 90 s of them have run
+    rates, walls = [], []
+    while len(rates) < max(1, args.steps) and sum(walls) < 90.0:
+        r, w = cpu_reference_rate(spec, n_members, 1, cores)
         rates.append(r)
+        walls.append(w)
     value = statistics.median(rates)
+    wall = statistics.median(walls)
     sample = (f"{n_members} members x 1 block of {MODEL_TIME_STEP:.0f} s of the {spec['name']} workload per step, "
               f"FP64 NumPy restatement (the reference has no CPU step), one member per process")
     line = {"metric": "member-cell-steps/s", "value": value, "unit": "member-cell-steps/s", "n_gpus": world,
-            "steps": len(rates), "warmup": 0, "ms_per_step": 1000.0 * wall, "higher_is_better": True,
+            "steps": len(rates), "warmup": args.warmup, "ms_per_step": 1000.0 * wall, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": spec["name"], "members": n_members, "nx": spec["nx"], "ny": spec["ny"]},
             "impl": "reference",
