@@ -115,10 +115,12 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
     float wXb = 0.0f, wYb = 0.0f;
     constexpr int NCELL = (W - 4) * (H - 4);
     constexpr int PER = (NCELL + NT - 1) / NT;
+    // A rolled loop keeps one copy of the cell pass in the kernel (it is
+    // sensitive to the instruction cache); fdb then lives in local memory.
     float fdb[PER][3];
 #pragma unroll
     for (int r = 0; r < PER; ++r) { fdb[r][0] = 0.f; fdb[r][1] = 0.f; fdb[r][2] = 0.f; }
-#pragma unroll
+#pragma unroll 1
     for (int r = 0; r < PER; ++r) {
         const int idx = threadIdx.x + r * NT;
         if (idx >= NCELL) continue;
