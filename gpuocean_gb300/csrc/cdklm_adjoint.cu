@@ -366,7 +366,7 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
             float sx = 0.f, sy = 0.f;
             for (int w = 0; w < NT / 32; ++w) { sx += red[0][w]; sy += red[1][w]; }
             // each tile owns its two slots: accumulate across calls
-            const int t = tile_y * gridDim.x + tile_x;
+            const int t = tile_y * ((p.nx + TX - 1) / TX) + tile_x;
             wind_partials[2 * t] += sx;
             wind_partials[2 * t + 1] += sy;
         }
@@ -394,9 +394,44 @@ stage_vjp_kernel(const GocCdklmParams p, const StepConst k, float dt, int rk_ste
                                                        hi_pitch, Hm_g, hm_pitch, wind_partials, smem_raw);
 }
 
-// Members sharing parameters and bathymetry: member blockIdx.z works at
-// offset z * member_stride (states and adjoints), z * wind_stride (wind) and
-// z * partials_stride (wind partials).
+// Tile of position q when the ntx x nty tiles are taken interior tiles first
+// (the rectangle [ix0, ix1) x [iy0, iy1), row by row), then the border frame
+// (the rows below and above the rectangle, then the columns beside it).
+__device__ __forceinline__ void interior_first_tile(int q, int ntx, int nty, int ix0, int ix1, int iy0, int iy1,
+                                                    int& tx, int& ty) {
+    const int iw = ix1 - ix0, ih = iy1 - iy0;
+    if (iw <= 0 || ih <= 0) {
+        tx = q % ntx; ty = q / ntx;
+        return;
+    }
+    if (q < iw * ih) {
+        tx = ix0 + q % iw; ty = iy0 + q / iw;
+        return;
+    }
+    q -= iw * ih;
+    if (q < iy0 * ntx) {
+        tx = q % ntx; ty = q / ntx;
+        return;
+    }
+    q -= iy0 * ntx;
+    const int nb = (nty - iy1) * ntx;
+    if (q < nb) {
+        tx = q % ntx; ty = iy1 + q / ntx;
+        return;
+    }
+    q -= nb;
+    const int side = ntx - iw > 0 ? ntx - iw : 1;
+    const int c = q % side;
+    ty = iy0 + q / side;
+    tx = c < ix0 ? c : ix1 + (c - ix0);
+}
+
+// Members sharing parameters and bathymetry.  Block b works on member
+// m = b % n_members at offset m * member_stride (states and adjoints),
+// m * wind_stride (wind) and m * partials_stride (wind partials), on tile
+// position b / n_members of the interior-first order: while the interior
+// tiles of all members last, every CTA runs the interior code (the kernel is
+// sensitive to the instruction cache).
 template <bool CONST_F>
 __global__ void __launch_bounds__(kANT, CONST_F ? 3 : 2)
 stage_vjp_members_kernel(const GocCdklmParams p, const StepConst k, float dt, int rk_step, const float* xe,
@@ -404,18 +439,22 @@ stage_vjp_members_kernel(const GocCdklmParams p, const StepConst k, float dt, in
                          const float* ybe, const float* ybu, const float* ybv, const float* bbe, const float* bbu,
                          const float* bbv, float* xbe, float* xbu, float* xbv, float* abe, float* abu, float* abv,
                          int pitch, long long member_stride, int wind_stride, const float* Hi_g, int hi_pitch,
-                         const float* Hm_g, int hm_pitch, float* wind_partials, int partials_stride) {
+                         const float* Hm_g, int hm_pitch, float* wind_partials, int partials_stride,
+                         int n_members, int4 inner) {
     extern __shared__ __align__(16) float smem_raw[];
-    const size_t o = (size_t)blockIdx.z * (size_t)member_stride;
+    const int member = (int)(blockIdx.x % (unsigned)n_members);
+    int tx, ty;
+    interior_first_tile((int)(blockIdx.x / (unsigned)n_members), (p.nx + kAX - 1) / kAX, (p.ny + kAY - 1) / kAY,
+                        inner.x, inner.y, inner.z, inner.w, tx, ty);
+    const size_t o = (size_t)member * (size_t)member_stride;
     GocCdklmParams pm = p;
     if (wind_stride) {
-        const size_t wo = (size_t)blockIdx.z * wind_stride;
+        const size_t wo = (size_t)member * wind_stride;
         pm.wind_x_cur += wo; pm.wind_x_next += wo; pm.wind_y_cur += wo; pm.wind_y_next += wo;
     }
     auto sh = [&](const float* q) { return q ? q + o : q; };
     auto shw = [&](float* q) { return q ? q + o : q; };
-    float* wp = wind_partials ? wind_partials + (size_t)blockIdx.z * partials_stride : nullptr;
-    const int tx = blockIdx.x, ty = blockIdx.y;
+    float* wp = wind_partials ? wind_partials + (size_t)member * partials_stride : nullptr;
     const int x0 = 2 + tx * kAX - kAHalo, y0 = 2 + ty * kAY - kAHalo;
     const bool border = x0 < 2 || y0 < 2 || x0 + kAX + 2 * kAHalo > p.nx + 2 || y0 + kAY + 2 * kAHalo > p.ny + 2;
     if (border)
@@ -541,7 +580,24 @@ extern "C" int goc_cdklm_stage_vjp_members(const GocCdklmParams* p, float dt, in
     constexpr int W = kAX + 2 * kAHalo, H = kAY + 2 * kAHalo;
     const size_t smem = cf ? sizeof(AdjSmem<W, H, false>) : sizeof(AdjSmem<W, H, true>);
     const int partials = goc_cdklm_vjp_partials(p->nx, p->ny);
-    dim3 grid((p->nx + kAX - 1) / kAX, (p->ny + kAY - 1) / kAY, n_members);
+    // interior tile rectangle (contiguous in x and in y)
+    const int ntx = (p->nx + kAX - 1) / kAX, nty = (p->ny + kAY - 1) / kAY;
+    int4 inner = make_int4(0, 0, 0, 0);
+    for (int t = 0, first = -1; t < ntx; ++t) {
+        const int x0 = 2 + t * kAX - kAHalo;
+        if (x0 >= 2 && x0 + kAX + 2 * kAHalo <= p->nx + 2) {
+            if (first < 0) first = inner.x = t;
+            inner.y = t + 1;
+        }
+    }
+    for (int t = 0, first = -1; t < nty; ++t) {
+        const int y0 = 2 + t * kAY - kAHalo;
+        if (y0 >= 2 && y0 + kAY + 2 * kAHalo <= p->ny + 2) {
+            if (first < 0) first = inner.z = t;
+            inner.w = t + 1;
+        }
+    }
+    const dim3 grid((unsigned)(ntx * nty) * (unsigned)n_members);
     static bool configured[2] = {false, false};
     if (!configured[cf]) {
         cudaError_t e = cf ? cudaFuncSetAttribute(stage_vjp_members_kernel<true>,
@@ -556,12 +612,12 @@ extern "C" int goc_cdklm_stage_vjp_members(const GocCdklmParams* p, float dt, in
         stage_vjp_members_kernel<true><<<grid, kANT, smem, st>>>(
             *p, k, dt, rk_step, x_eta, x_hu, x_hv, a_eta, a_hu, a_hv, yb_eta, yb_hu, yb_hv, base_eta, base_hu,
             base_hv, xb_eta, xb_hu, xb_hv, ab_eta, ab_hu, ab_hv, pf, member_stride, wind_stride, Hi, hip, Hm, hmp,
-            wind_partials, partials);
+            wind_partials, partials, n_members, inner);
     else
         stage_vjp_members_kernel<false><<<grid, kANT, smem, st>>>(
             *p, k, dt, rk_step, x_eta, x_hu, x_hv, a_eta, a_hu, a_hv, yb_eta, yb_hu, yb_hv, base_eta, base_hu,
             base_hv, xb_eta, xb_hu, xb_hv, ab_eta, ab_hu, ab_hv, pf, member_stride, wind_stride, Hi, hip, Hm, hmp,
-            wind_partials, partials);
+            wind_partials, partials, n_members, inner);
     count_launch();
     return check_launch("stage_vjp_members_kernel");
 }
