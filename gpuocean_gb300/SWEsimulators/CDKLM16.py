@@ -49,6 +49,34 @@ def calcCoriolisParams(lat):
     return [2.0 * omega * np.sin(lat), 2.0 * omega * np.cos(lat) / a]
 
 
+def _reference_cell_f(f, coriolis_beta, dx, dy, angle, gx=2, gy=2):
+    """f moved from the grid origin to the first interior cell
+    (S/CDKLM16.py:147-149)."""
+    north = np.array([np.sin(angle.flat[0]), np.cos(angle.flat[0])])
+    return f - coriolis_beta * (gx * dx * north[0] + gy * dy * north[1])
+
+
+def _unshifted_f(f_stored, beta, dx, dy, gx, gy):
+    """The f that the constructor's move to the first interior cell (default
+    angle) turns into f_stored, bit for bit (same arithmetic as the
+    constructor)."""
+    angle = np.array([[0]], dtype=np.float32)
+    target = np.float32(f_stored)
+    moved = lambda c: np.float32(_reference_cell_f(c, beta, dx, dy, angle, gx, gy))
+    cand = float(target) + float(target) - float(moved(float(target)))
+    for _ in range(8):
+        got = moved(cand)
+        if got == target:
+            return cand
+        cand += float(target) - float(got)
+    for _ in range(64):
+        got = moved(cand)
+        if got == target:
+            return cand
+        cand = float(np.nextafter(np.float32(cand), np.float32(np.inf if got < target else -np.inf)))
+    return cand
+
+
 class CDKLM16(Simulator):
     """Chertock, Dudzinski, Kurganov & Lukacova-Medvidova (2016) well-balanced
     central-upwind scheme for the rotating shallow-water equations."""
@@ -68,8 +96,6 @@ class CDKLM16(Simulator):
         assert rk_order in (1, 2, 3), "Only 1st, 2nd and 3rd order Runge Kutta supported"
         if rk_order == 3:
             assert r == 0.0, "3rd order Runge Kutta supported only without friction"
-        if write_netcdf:
-            raise NotImplementedError("NetCDF output is not part of this package")
         if use_direct_lookup:
             raise NotImplementedError("use_direct_lookup is not supported; pressure is always interpolated")
         wind = WindStress.WindStress() if wind is None else wind
@@ -79,8 +105,7 @@ class CDKLM16(Simulator):
         ghost_cells_x = ghost_cells_y = 2
         self.boundary_conditions = boundary_conditions
         # compensate f for the reference cell (S/CDKLM16.py:147-149)
-        north = np.array([np.sin(angle.flat[0]), np.cos(angle.flat[0])])
-        f = f - coriolis_beta * (ghost_cells_x * dx * north[0] + ghost_cells_y * dy * north[1])
+        f = _reference_cell_f(f, coriolis_beta, dx, dy, angle, ghost_cells_x, ghost_cells_y)
         self.max_wind_direction_perturbation = max_wind_direction_perturbation
         super().__init__(gpu_ctx, nx, ny, ghost_cells_x, ghost_cells_y, dx, dy, dt, g, f, r, None, t,
                          theta, rk_order, coriolis_beta, 0, wind, atmospheric_pressure, write_netcdf,
@@ -164,6 +189,12 @@ class CDKLM16(Simulator):
         self._params = self._make_params()
         if self.dt <= 0:
             self.updateDt()
+        if self.write_netcdf:
+            from ..utils import SimWriter
+            self.sim_writer = SimWriter.SimNetCDFWriter(self, super_dir_name=super_dir_name,
+                                                        filename=netcdf_filename,
+                                                        ignore_ghostcells=self.ignore_ghostcells,
+                                                        offset_x=self.offset_x, offset_y=self.offset_y)
 
     # ------------------------------------------------------------------
     def _make_params(self):
@@ -201,6 +232,7 @@ class CDKLM16(Simulator):
         return self.gpu_stream.handle
 
     def cleanUp(self, do_gc=True):
+        self.closeNetCDF()
         if getattr(self, "gpu_data", None) is None:
             return
         if self.model_error is not None:
@@ -284,7 +316,8 @@ class CDKLM16(Simulator):
             self._params.wind_t = float(np.float32(self.update_wind_stress()))
             self._params.atm_p_t = float(np.float32(self.update_atmospheric_pressure()))
             if plain and self._params.wind_t == 1.0 and self._params.atm_p_t == 1.0:
-                return self._plain_steps(t_now, t_end)
+                self._plain_steps(t_now, t_end)
+                break
             self.bc_kernel.update_bc_values(self.gpu_stream, self.t)
             self._rk_step(local_dt)
             perturbed = self.model_error is not None and apply_stochastic_term
@@ -297,6 +330,8 @@ class CDKLM16(Simulator):
             self.t += np.float64(local_dt)
             t_now += np.float64(local_dt)
             self.num_iterations += 1
+        if self.write_netcdf and write_now:
+            self.writeState()
         return self.t
 
     def _plain_steps(self, t_now, t_end):
@@ -329,6 +364,8 @@ class CDKLM16(Simulator):
             interpolation_factor=small_scale_perturbation_interpolation_factor,
             use_lcg=use_lcg, xorwow_seed=xorwow_seed,
             block_width=block_width_model_error, block_height=block_height_model_error)
+        if self.write_netcdf:
+            self.sim_writer.writeModelError(self)
 
     def setKLModelError(self, kl_decay=1.2, kl_scaling=1.0, include_cos=True, include_sin=True,
                         basis_x_start=1, basis_y_start=1, basis_x_end=10, basis_y_end=10,
@@ -340,6 +377,8 @@ class CDKLM16(Simulator):
             basis_x_start=basis_x_start, basis_y_start=basis_y_start, basis_x_end=basis_x_end,
             basis_y_end=basis_y_end, use_lcg=use_lcg, xorwow_seed=xorwow_seed, np_seed=np_seed,
             block_width=block_width, block_height=block_height)
+        if self.write_netcdf:
+            self.sim_writer.writeModelError(self)
 
     def setKLModelErrorSimilarAs(self, otherSim):
         """The KL model error of another simulator's parameters (S/CDKLM16.py:653-660)."""
@@ -417,12 +456,92 @@ class CDKLM16(Simulator):
             self.total_time_steps += 1
             if self.total_time_steps % 5 == 0:
                 self.updateDt(courant_number=courant_number)
+        if self.write_netcdf and write_now:
+            self.sim_writer.writeTimestep(self)
         assert round(observation_time) == round(self.t), \
             'The simulation time is not the same as observation time after dataAssimilationStep! \n' + \
             '(self.t, observation_time, diff): ' + str((self.t, observation_time, self.t - observation_time))
 
     def writeState(self):
-        return None
+        if self.write_netcdf:
+            self.sim_writer.writeTimestep(self)
+
+    @classmethod
+    def fromfilename(cls, gpu_ctx, filename, cont_write_netcdf=True, new_netcdf_filename=None, time0=None):
+        """A simulator hot-started from a file of SimNetCDFWriter: its
+        parameters and the last written state (or the state at time0)
+        (S/CDKLM16.py:403-473).  cont_write_netcdf: write the continued run
+        to new_netcdf_filename (generated when None)."""
+        from ..utils import SimReader
+        reader = SimReader.SimNetCDFReader(filename, ignore_ghostcells=False)
+        try:
+            name = str(reader.get("simulator_short"))
+            assert name == cls.__name__, ("Trying to initialize a " + cls.__name__ +
+                                          " simulator with netCDF file based on " + name + " results.")
+            H = reader.getH()
+            if time0 is None:
+                eta0, hu0, hv0, time0 = reader.getLastTimeStep()
+            else:
+                eta0, hu0, hv0, time0 = reader.getStateAtTime(time0)
+            if H.ndim == 3:
+                H = H[0]
+            dx, dy, beta = reader.get("dx"), reader.get("dy"), reader.get("coriolis_beta")
+            # The file holds the simulator's f, already moved to the first
+            # interior cell by the constructor (S/CDKLM16.py:147-149), which
+            # moves a given f again: hand it the f that moves to the stored one
+            # (the reference passes the stored f on and shifts it twice).
+            gx, gy = int(reader.get("ghost_cells_west")), int(reader.get("ghost_cells_south"))
+            f = _unshifted_f(reader.get("coriolis_force"), beta, dx, dy, gx, gy)
+            params = dict(gpu_ctx=gpu_ctx, eta0=eta0, hu0=hu0, hv0=hv0, H=H,
+                          nx=int(reader.get("nx")), ny=int(reader.get("ny")),
+                          dx=dx, dy=dy, dt=reader.get("dt"), g=reader.get("g"),
+                          f=f, r=reader.get("bottom_friction_r"), t=float(time0),
+                          theta=reader.get("minmod_theta"), rk_order=int(reader.get("time_integrator")),
+                          coriolis_beta=reader.get("coriolis_beta"), write_netcdf=cont_write_netcdf,
+                          netcdf_filename=new_netcdf_filename, wind=WindStress.WindStress(),
+                          boundary_conditions=reader.getBC())
+            if reader.has("model_time_step"):
+                params["model_time_step"] = reader.get("model_time_step")
+        finally:
+            reader.close()
+        return cls(**params)
+
+    def setModelErrorFromFile(self, filename, use_lcg=False, xorwow_seed=None):
+        """The model error described by the attributes of a simulator file
+        (S/CDKLM16.py:600-637)."""
+        from ..utils import SimReader
+        reader = SimReader.SimNetCDFReader(filename, ignore_ghostcells=False)
+        try:
+            name = str(reader.get("simulator_short"))
+            assert name == self.__class__.__name__, ("Trying to initialize a " + self.__class__.__name__ +
+                                                     " simulator with netCDF file based on " + name + " results.")
+            if reader.has("small_scale_perturbation"):
+                # files of an older writer
+                if reader.get("small_scale_perturbation") == "True":
+                    self.setSOARModelError(
+                        small_scale_perturbation_amplitude=reader.get("small_scale_perturbation_amplitude"),
+                        small_scale_perturbation_interpolation_factor=int(
+                            reader.get("small_scale_perturbation_interpolation_factor")),
+                        use_lcg=use_lcg, xorwow_seed=xorwow_seed)
+            elif reader.has("has_model_error") and reader.get("has_model_error") == "True":
+                kind = reader.get("model_error_name")
+                if kind == "OceanStateNoise":
+                    self.setSOARModelError(
+                        small_scale_perturbation_amplitude=reader.get("small_scale_perturbation_amplitude"),
+                        small_scale_perturbation_interpolation_factor=int(
+                            reader.get("small_scale_perturbation_interpolation_factor")),
+                        use_lcg=use_lcg, xorwow_seed=xorwow_seed)
+                elif kind == "ModelErrorKL":
+                    self.setKLModelError(kl_decay=reader.get("kl_decay"), kl_scaling=reader.get("kl_scaling"),
+                                         include_cos=reader.get("include_cos") == "True",
+                                         include_sin=reader.get("include_sin") == "True",
+                                         basis_x_start=int(reader.get("basis_x_start")),
+                                         basis_y_start=int(reader.get("basis_y_start")),
+                                         basis_x_end=int(reader.get("basis_x_end")),
+                                         basis_y_end=int(reader.get("basis_y_end")),
+                                         use_lcg=use_lcg, xorwow_seed=xorwow_seed)
+        finally:
+            reader.close()
 
     # ------------------------------------------------------------------
     def downloadMaxDt(self):

@@ -280,7 +280,25 @@ class BoundaryConditions:
     def __str__(self):
         return ("north: " + self._toString(self.north) + ", east: " + self._toString(self.east)
                 + ", south: " + self._toString(self.south) + ", west: " + self._toString(self.west)
-                + ", spongeCells: " + str(self.spongeCells))
+                + ", spongeCells: " + str({k: int(v) for k, v in self.spongeCells.items()}))
+
+    @classmethod
+    def fromstring(cls, bc_string):
+        """The boundary conditions of their text form (as __str__ writes it and
+        as simulator files store it, U/Common.py:1010-1045)."""
+        import re
+        flags = {"Wall": 1, "Periodic": 2, "Flow_Relaxation_Scheme": 3, "Open_Linear_Interpolation": 4}
+        side = {}
+        for name in ("north", "east", "south", "west"):
+            m = re.search(name + r"\s*:\s*([A-Za-z_:|]+)", bc_string)
+            side[name] = flags.get(m.group(1).rstrip(",") if m else "", -1)
+        sponge = {"north": 0, "south": 0, "east": 0, "west": 0}
+        m = re.search(r"spongeCells\s*:\s*\{([^}]*)\}", bc_string)
+        if m:
+            for key, val in re.findall(r"'?(north|south|east|west)'?\s*:\s*(?:np\.int\d+\()?(-?\d+)", m.group(1)):
+                sponge[key] = int(val)
+        return cls(north=side["north"], east=side["east"], south=side["south"], west=side["west"],
+                   spongeCells=sponge)
 
 
 class SingleBoundaryConditionData:
