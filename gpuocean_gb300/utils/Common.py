@@ -193,7 +193,9 @@ class CUDAArray2D:
 
     @staticmethod
     def convert_to_float32(data):
-        if not np.issubdtype(data.dtype, np.float32) or np.isfortran(data) or not data.flags.c_contiguous:
+        # native float32 in C order (the device copy takes the raw bytes, so a
+        # big-endian array, as NetCDF files hold, is converted too)
+        if data.dtype != np.dtype(np.float32) or np.isfortran(data) or not data.flags.c_contiguous:
             return np.ascontiguousarray(data, dtype=np.float32)
         return data
 
