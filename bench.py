@@ -21,6 +21,7 @@ import statistics
 import subprocess
 import sys
 import threading
+import tempfile
 import time
 
 import numpy as np
@@ -420,6 +421,43 @@ def run_c2(ctx, days=10.0):
     return out
 
 
+def run_netcdf(ctx, timesteps=10):
+    """NetCDF output and hot start of the 512 x 300 double jet: host wall time
+    per written time step (download of eta, hu, hv + the file write, the file
+    closed at the end) and for CDKLM16.fromfilename of the last one.  The file
+    lives in a temporary directory under the repository."""
+    from gpuocean_gb300.SWEsimulators import CDKLM16
+    from gpuocean_gb300.utils import BenchmarkCases, Common
+    c = BenchmarkCases.double_jet_case(nx=512, ny=300)
+    with tempfile.TemporaryDirectory(dir=ROOT) as d:
+        fn = os.path.join(d, "double_jet")
+        sim = CDKLM16.CDKLM16(ctx, c["eta0"], c["hu0"], c["hv0"], c["H"], 512, 300, c["dx"], c["dy"], 0.0, c["g"],
+                              c["f"], c["r"], coriolis_beta=c["coriolis_beta"],
+                              boundary_conditions=Common.BoundaryConditions(*c["boundary"]),
+                              write_netcdf=True, netcdf_filename=fn)
+        sim.updateDt(courant_number=0.8)
+        sim.step(600.0, write_now=False)
+        sim.gpu_stream.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(timesteps):
+            sim.writeState()
+        sim.closeNetCDF()
+        write_s = time.perf_counter() - t0
+        size = os.path.getsize(fn + ".nc")
+        t0 = time.perf_counter()
+        hot = CDKLM16.CDKLM16.fromfilename(ctx, fn + ".nc", cont_write_netcdf=False)
+        hot.gpu_stream.synchronize()
+        hot_s = time.perf_counter() - t0
+        same = all(np.array_equal(np.asarray(a), np.asarray(b)) for a, b in zip(sim.download(), hot.download()))
+        hot.cleanUp()
+        sim.cleanUp()
+    mb = 3 * 516 * 304 * 4 / 1e6
+    return {"config": "double jet 512x300, classic NetCDF (64-bit offset)", "timesteps": timesteps + 1,
+            "write_ms_per_timestep": 1000.0 * write_s / timesteps, "mb_per_timestep": mb,
+            "write_mb_per_s": mb * timesteps / write_s, "file_mb": size / 1e6,
+            "hot_start_ms": 1000.0 * hot_s, "hot_start_state_identical": bool(same)}
+
+
 def run_kl(ens, sims, peak, peak_kind, repeats=10):
     """Karhunen-Loeve model error on the C3 ensemble (every member at
     512 x 300) with the double-jet case's KL parameters (basis 2..8 x 1..7,
@@ -793,6 +831,7 @@ def main():
     ens_stats = None if args.no_statistics else run_statistics(ens, sims, *measured_peaks())
     kl = None if args.no_statistics else run_kl(ens, sims, *measured_peaks())
     c2 = None if args.no_c2 else run_c2(ctx)
+    netcdf = None if args.no_c2 else run_netcdf(ctx)
     multilevel = None if args.no_multilevel else run_multilevel(ctx, args)
     adjoint = None if args.no_adjoint else run_adjoint(ctx)
 
@@ -831,7 +870,7 @@ def main():
                          "algorithmic_bytes_per_launch": avg_bytes,
                          "issue": issue_roofline(float(np.mean(cells_k)), avg_dur, clk)},
             "e2e": e2e, "gpu_launches": launches, "clocks": clk, "cpu_baseline": cpu,
-            "multilevel": multilevel, "adjoint": adjoint, "statistics": ens_stats, "kl_model_error": kl, "c2_ten_days": c2,
+            "multilevel": multilevel, "adjoint": adjoint, "statistics": ens_stats, "kl_model_error": kl, "c2_ten_days": c2, "netcdf": netcdf,
             "wall_s": wall,
         }
         print(json.dumps(line), flush=True)
