@@ -124,7 +124,9 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
     for (int r = 0; r < PER; ++r) {
         const int idx = threadIdx.x + r * NT;
         if (idx >= NCELL) continue;
-        const int i = 2 + idx % (W - 4), j = 2 + idx / (W - 4);
+        int i, j;
+        block_cell<W - 4>(idx, H - 4, i, j);
+        i += 2; j += 2;
         const int gx = T.x0 + i, gy = T.y0 + j;
         const int gxs = (BORDER && px) ? wrap_interior(gx, nx) : gx;
         const int gys = (BORDER && py) ? wrap_interior(gy, ny) : gy;
@@ -229,7 +231,9 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
     for (int r = 0; r < PER; ++r) {
         const int idx = threadIdx.x + r * NT;
         if (idx >= NCELL) continue;
-        const int i = 2 + idx % (W - 4), j = 2 + idx / (W - 4);
+        int i, j;
+        block_cell<W - 4>(idx, H - 4, i, j);
+        i += 2; j += 2;
         S.Gy[0][j][i] = fdb[r][0]; S.Gy[1][j][i] = fdb[r][1]; S.Gy[2][j][i] = fdb[r][2];
     }
     __syncthreads();
