@@ -421,6 +421,50 @@ def run_c2(ctx, days=10.0):
     return out
 
 
+def run_open_boundaries(ctx, hours=1.0):
+    """Open boundaries and time-varying forcing on one 512 x 300 simulator:
+    flow relaxation on every side (10 cells) toward exterior data at two time
+    stamps, and a 9 x 7 wind-stress texture at three time stamps; a Gaussian
+    bump on 200 m depth, beta plane.  Host wall time around `hours` of model
+    time through CDKLM16.step (each RK2 step: two stage launches with the
+    sponge between them and the time interpolation of both)."""
+    from gpuocean_gb300.SWEsimulators import CDKLM16
+    from gpuocean_gb300.utils import Common, WindStress
+    nx, ny, dx, dy = 512, 300, 5000.0, 5000.0
+    rng = np.random.default_rng(17)
+    yy, xx = np.mgrid[0:ny + 4, 0:nx + 4].astype(np.float64)
+    eta0 = (0.5 * np.exp(-((xx - nx / 2) ** 2 + (yy - ny / 2) ** 2) / 40.0 ** 2)).astype(np.float32)
+    z = np.zeros_like(eta0)
+    H = np.full((ny + 5, nx + 5), 200.0, np.float32)
+    t = [0.0, 7200.0]
+    sides = {}
+    for side, n in (("north", nx + 4), ("south", nx + 4), ("east", ny + 4), ("west", ny + 4)):
+        sides[side] = Common.SingleBoundaryConditionData(
+            h=[rng.uniform(-0.05, 0.05, n).astype(np.float32) for _ in t],
+            hu=[np.zeros(n, np.float32) for _ in t], hv=[np.zeros(n, np.float32) for _ in t])
+    data = Common.BoundaryConditionsData(t=t, **sides)
+    bc = Common.BoundaryConditions(3, 3, 3, 3, spongeCells={"north": 10, "south": 10, "east": 10, "west": 10})
+    wt = [0.0, 3600.0, 7200.0]
+    wind = WindStress.WindStress(t=wt, stress_u=[rng.uniform(-1e-4, 1e-4, (7, 9)).astype(np.float32) for _ in wt],
+                                 stress_v=[rng.uniform(-1e-4, 1e-4, (7, 9)).astype(np.float32) for _ in wt])
+    sim = CDKLM16.CDKLM16(ctx, eta0, z, z.copy(), H, nx, ny, dx, dy, 0.0, 9.81, 1.2e-4, 0.0, coriolis_beta=2e-11,
+                          boundary_conditions=bc, boundary_conditions_data=data, wind=wind)
+    sim.updateDt(courant_number=0.8)
+    sim.step(600.0)
+    sim.gpu_stream.synchronize()
+    steps0 = sim.num_iterations
+    t0 = time.perf_counter()
+    sim.step(hours * 3600.0)
+    sim.gpu_stream.synchronize()
+    wall = time.perf_counter() - t0
+    steps = sim.num_iterations - steps0
+    eta = np.asarray(sim.download(interior_domain_only=True)[0])
+    sim.cleanUp()
+    return {"config": "512x300, flow relaxation on all sides (10 cells, data at 2 times), 9x7 wind at 3 times",
+            "steps": int(steps), "wall_s": wall, "cell_steps_per_s": steps * nx * ny / wall,
+            "finite": bool(np.isfinite(eta).all())}
+
+
 def run_netcdf(ctx, timesteps=10):
     """NetCDF output and hot start of the 512 x 300 double jet: host wall time
     per written time step (download of eta, hu, hv + the file write, the file
@@ -832,6 +876,7 @@ def main():
     kl = None if args.no_statistics else run_kl(ens, sims, *measured_peaks())
     c2 = None if args.no_c2 else run_c2(ctx)
     netcdf = None if args.no_c2 else run_netcdf(ctx)
+    open_bc = None if args.no_c2 else run_open_boundaries(ctx)
     multilevel = None if args.no_multilevel else run_multilevel(ctx, args)
     adjoint = None if args.no_adjoint else run_adjoint(ctx)
 
@@ -870,7 +915,7 @@ def main():
                          "algorithmic_bytes_per_launch": avg_bytes,
                          "issue": issue_roofline(float(np.mean(cells_k)), avg_dur, clk)},
             "e2e": e2e, "gpu_launches": launches, "clocks": clk, "cpu_baseline": cpu,
-            "multilevel": multilevel, "adjoint": adjoint, "statistics": ens_stats, "kl_model_error": kl, "c2_ten_days": c2, "netcdf": netcdf,
+            "multilevel": multilevel, "adjoint": adjoint, "statistics": ens_stats, "kl_model_error": kl, "c2_ten_days": c2, "netcdf": netcdf, "open_boundaries": open_bc,
             "wall_s": wall,
         }
         print(json.dumps(line), flush=True)
