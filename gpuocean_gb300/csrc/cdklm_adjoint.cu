@@ -241,14 +241,34 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
 
     // 5. faces in reverse, two colours each.  x faces are coloured as a
     //    checkerboard ((i + j) even / odd): faces of one row never share a
-    //    cell, and a warp that spans two rows touches even banks in one and
-    //    odd banks in the other, so the stride-2 accesses do not conflict.
+    //    cell.  A warp takes 16 faces of a row and 16 of the next: the
+    //    stride-2 accesses of one half-warp cover 32 consecutive floats, and
+    //    the checkerboard puts the two rows on even and odd banks, so they do
+    //    not conflict; the remaining faces of each row come afterwards.
     constexpr int NXF = W - 3, NYF = H - 4;     // east faces of cells [1, W-2) on rows [2, H-2)
+    constexpr int FPR = (NXF + 1) / 2;          // faces of one colour per row
+    constexpr int FM = FPR < 16 ? FPR : 16, FR = FPR - FM;
+    constexpr int NITEM = FM == 16 ? ((NYF + 1) / 2) * 32 + FR * NYF : FPR * NYF;
 #pragma unroll 1
     for (int colour = 0; colour < 2; ++colour) {
-        for (int idx = threadIdx.x; idx < ((NXF + 1) / 2) * NYF; idx += NT) {
-            const int j = 2 + idx / ((NXF + 1) / 2);
-            const int i = 1 + 2 * (idx % ((NXF + 1) / 2)) + ((j + colour) & 1);
+        for (int idx = threadIdx.x; idx < NITEM; idx += NT) {
+            int row, kf;
+            if (idx < ((NYF + 1) / 2) * 32 && FM == 16) {
+                const int lane = idx & 31;
+                row = 2 * (idx >> 5) + (lane >> 4);
+                kf = lane & 15;
+                if (row >= NYF) continue;
+            } else {
+                const int q = idx - (FM == 16 ? ((NYF + 1) / 2) * 32 : 0);
+                if (FM != 16) {
+                    row = idx / FPR; kf = idx % FPR;
+                } else {
+                    if (q >= FR * NYF) continue;
+                    row = q / (FR > 0 ? FR : 1); kf = FM + q % (FR > 0 ? FR : 1);
+                }
+            }
+            const int j = 2 + row;
+            const int i = 1 + 2 * kf + ((j + colour) & 1);
             if (i >= W - 2) continue;
             const float F0b = (FDb(0)[j][i] - FDb(0)[j][i + 1]) * k.inv_dx;
             const float F1b = (FDb(1)[j][i] - FDb(1)[j][i + 1]) * k.inv_dx;
