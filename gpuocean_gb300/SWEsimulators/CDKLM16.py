@@ -171,6 +171,8 @@ class CDKLM16(Simulator):
         # CFL reduction buffers
         self.num_threads_dt = num_threads_dt
         n_part = _lib.load().goc_max_dt_partials(int(nx), int(ny))
+        if n_part < 0:
+            raise ValueError("a %d x %d grid is too large for the CFL reduction" % (nx, ny))
         self.device_dt = Common.DevicePtr(4 * n_part)
         self.num_blocks_dt = np.int32(n_part)
         self.max_dt_buffer = Common.DevicePtr(4)
@@ -423,44 +425,31 @@ class CDKLM16(Simulator):
 
     def dataAssimilationStep(self, observation_time, otherSim=None, model_error_final_step=True, write_now=True,
                              courant_number=0.8):
-        """Run to ``observation_time`` with model error every ``model_time_step``
-        (S/CDKLM16.py:742-806)."""
-        full_model_time_steps = int(round(observation_time - self.t) / self.model_time_step)
-        leftover_step_size = observation_time - self.t - full_model_time_steps * self.model_time_step
-        if leftover_step_size / self.model_time_step < 0.1 and full_model_time_steps > 1:
-            leftover_step_size += self.model_time_step
-            full_model_time_steps -= 1
-        if leftover_step_size / self.model_time_step < 0.00001:
-            leftover_step_size = 0
-        assert full_model_time_steps > 0, "There is less than CDKLM16.model_time_step until the observation"
-        self.updateDt(courant_number=courant_number)
-        if otherSim is not None:
-            otherSim.updateDt(courant_number=courant_number)
-        for i in range(full_model_time_steps + 1):
-            if i == 0 and leftover_step_size == 0:
-                continue
-            elif i == 0:
-                self.step(leftover_step_size, apply_stochastic_term=False, write_now=False)
-                self.perturbState(perturbation_scale=np.sqrt(leftover_step_size / self.model_time_step))
-                if otherSim is not None:
-                    otherSim.step(leftover_step_size, apply_stochastic_term=False, write_now=False)
-                    otherSim.perturbSimilarAs(self, perturbation_scale=np.sqrt(leftover_step_size / self.model_time_step))
-            else:
-                self.step(self.model_time_step, apply_stochastic_term=False, write_now=False)
-                if (i < full_model_time_steps) or model_error_final_step:
-                    self.perturbState()
-                if otherSim is not None:
-                    otherSim.step(self.model_time_step, apply_stochastic_term=False, write_now=False)
-                    if (i < full_model_time_steps) or model_error_final_step:
-                        otherSim.perturbSimilarAs(self)
+        """Run to ``observation_time`` in blocks of ``model_time_step`` with
+        the model error after each block (S/CDKLM16.py:742-806; the plan of
+        blocks comes from ``ObservationSchedule.blocks_to_observation``).
+        ``otherSim`` (a coarse partner) takes the same blocks and is perturbed
+        with this simulator's random field after each of them."""
+        from .ObservationSchedule import blocks_to_observation, check_arrival, refresh_dt_after
+        plan = blocks_to_observation(observation_time - self.t, self.model_time_step, model_error_final_step)
+        sims = (self,) if otherSim is None else (self, otherSim)
+        for s in sims:
+            s.updateDt(courant_number=courant_number)
+        for blk in plan:
+            for s in sims:
+                s.step(blk.length, apply_stochastic_term=False, write_now=False)
+                if blk.perturbation is None:
+                    continue
+                if s is self:
+                    self.perturbState(perturbation_scale=blk.perturbation)
+                else:
+                    s.perturbSimilarAs(self, perturbation_scale=blk.perturbation)
             self.total_time_steps += 1
-            if self.total_time_steps % 5 == 0:
+            if refresh_dt_after(self.total_time_steps):
                 self.updateDt(courant_number=courant_number)
         if self.write_netcdf and write_now:
             self.sim_writer.writeTimestep(self)
-        assert round(observation_time) == round(self.t), \
-            'The simulation time is not the same as observation time after dataAssimilationStep! \n' + \
-            '(self.t, observation_time, diff): ' + str((self.t, observation_time, self.t - observation_time))
+        check_arrival(observation_time, self.t)
 
     def writeState(self):
         if self.write_netcdf:

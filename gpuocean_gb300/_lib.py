@@ -133,6 +133,7 @@ SIGNATURES = {
     "goc_ensemble_create": (c_int, [c_void_p, c_int, c_int, ctypes.POINTER(c_void_p)]),
     "goc_ensemble_destroy": (c_int, [c_void_p]),
     "goc_ensemble_size": (c_int, [c_void_p, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
+    "goc_ensemble_staging_errors": (c_int, [c_void_p, ctypes.POINTER(c_int)]),
     "goc_ensemble_tma_status": (c_int, [c_void_p, ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_longlong),
                                         ctypes.POINTER(c_int)]),
     "goc_selftest_wait_timeout": (c_int, [ctypes.c_double, ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_double)]),

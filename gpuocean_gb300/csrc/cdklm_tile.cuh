@@ -510,7 +510,7 @@ constexpr int kHandRows = 4;
 // value so that one instantiation serves both kinds of tile (the kernel's
 // code stays within the instruction cache).
 template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING, bool BORDER>
-__device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const StepConst& k, float dt, int rk_step,
+__device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const StepConst& k, float dt, int rk_step,
                                                 int tile_x, int tile_y,
                                                 const float* __restrict__ e_in, const float* __restrict__ hu_in,
                                                 const float* __restrict__ hv_in, float* e_out, float* hu_out,
@@ -555,15 +555,23 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
 
     // Q^n of an interior tile may have been staged by TMA into the planes
     // Sx[0], Sx[1], Sy[0] (box from column x0 - 2: TMA boxes start on 16-byte
-    // boundaries): wait for it.  A wait that runs out falls back to loads.
+    // boundaries): wait for it.  Every thread waits (each thus sees the
+    // copy's writes) and the CTA uses the staged tile only if all of them saw
+    // it land.  A wait that runs out sets the error flag the host reads and
+    // stops the CTA's staging; the tile then loads Q^n itself, once the late
+    // copy has landed (a second bounded wait) so that it cannot overwrite the
+    // planes afterwards.  If it never lands the CTA gives up (returns false).
     bool staged = false;
     if (!BORDER && tma && tma->staged) {
-        staged = mbar_wait_bounded(tma->bar, tma->phase, kTmaWaitLimitNs);
-        tma->phase ^= 1u;
+        staged = __syncthreads_and(mbar_wait_bounded(tma->bar, tma->phase, kTmaWaitLimitNs)) != 0;
         if (!staged) {
-            *tma->off = 1;
-            atomicExch(tma->err, 1);
+            if (threadIdx.x == 0) {
+                *tma->off = 1;
+                atomicExch(tma->err, 1);
+            }
+            if (!__syncthreads_and(mbar_wait_bounded(tma->bar, tma->phase, kTmaWaitLimitNs))) return false;
         }
+        tma->phase ^= 1u;
     }
 
     // 2. Q^n with wall mirrors and periodic images, desingularised with the
@@ -720,7 +728,7 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
         __syncthreads();
         // the last phase reads neither Sx[0..1] nor Sy[0..1]: stage the next
         // tile of the strip there meanwhile
-        if (tma && tma->next_tile_y >= 0 && threadIdx.x == 0)
+        if (tma && tma->next_tile_y >= 0 && threadIdx.x == 0 && *tma->off == 0)
             tma_stage_tile<W, H>(*tma, S, T.x0 - 2, 2 + tma->next_tile_y * TY - HALO);
         // A rolled loop keeps one copy of the cell update; Q^n of the cell is
         // loaded first, so its latency overlaps the update.
@@ -787,6 +795,7 @@ __device__ __forceinline__ void cdklm_tile_body(const GocCdklmParams& p, const S
             de[o] = ne; du[o] = nhu; dv[o] = nhv;
         }
     }
+    return true;
 }
 
 // A tile needs the boundary logic (periodic wrap, wall mirrors, clamping,
@@ -820,12 +829,13 @@ __device__ __forceinline__ void cdklm_tile(const GocCdklmParams& p, const StepCo
 // Tile `tile_y` of the column strip `tile_x` in a run of consecutive tiles
 // of one strip (fused RK2): reuse = the previous tile of the run handed over
 // its last stage-1 rows through side_in; side_out (or null for the run's last
-// tile) receives this tile's.  A tile whose staged rows reach outside the
+// tile) receives this tile's.  Returns false when the CTA has to give up (a
+// TMA copy of its input that never landed).  A tile whose staged rows reach outside the
 // interior rows computes all of its stage-1 rows: the north/south wall
 // mirrors of its first rows land in rows it does not take over.  East/west
 // borders keep the hand-over (their mirrors stay within a row).
 template <int TX, int TY, int NT, bool CONST_F, bool SIMPLE_FORCING>
-__device__ __forceinline__ void cdklm_strip_tile(const GocCdklmParams& p, const StepConst& k, float dt, int tile_x,
+__device__ __forceinline__ bool cdklm_strip_tile(const GocCdklmParams& p, const StepConst& k, float dt, int tile_x,
                                                  int tile_y, bool reuse, const float* __restrict__ e_in,
                                                  const float* __restrict__ hu_in, const float* __restrict__ hv_in,
                                                  float* e_out, float* hu_out, float* hv_out, int pitch,
@@ -836,13 +846,12 @@ __device__ __forceinline__ void cdklm_strip_tile(const GocCdklmParams& p, const 
     const int y0 = 2 + tile_y * TY - 4;
     const int s1 = (reuse && y0 >= 2 && y0 + TY + 8 <= p.ny + 2) ? 2 + kHandRows : 2;
     if (border)
-        cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, true>(
+        return cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, true>(
             p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
             pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, s1, side_in, side_out, tma);
-    else
-        cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, false>(
-            p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
-            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, s1, side_in, side_out, tma);
+    return cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, false>(
+        p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
+        pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, s1, side_in, side_out, tma);
 }
 
 template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING>

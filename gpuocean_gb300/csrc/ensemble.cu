@@ -89,6 +89,7 @@ static void free_ensemble(Ensemble* e) {
     cudaFree(e->d_tmaps);
     cudaFree(e->d_tma_base);
     cudaFree(e->d_tma_err);
+    if (e->h_tma_err) cudaFreeHost(const_cast<int*>(e->h_tma_err));
     cudaFree(e->d_tma_tiles);
     delete e;
 }
@@ -155,6 +156,14 @@ static int build_tma_maps(Ensemble* e) {
     if (err == cudaSuccess)
         err = cudaMemcpy(e->d_tma_base, base.data(), sizeof(const float*) * n, cudaMemcpyHostToDevice);
     if (err == cudaSuccess) err = cudaMemset(e->d_tma_err, 0, sizeof(int));
+    if (err == cudaSuccess) {
+        int* h = nullptr;
+        err = cudaHostAlloc(&h, sizeof(int), cudaHostAllocDefault);
+        if (err == cudaSuccess) {
+            *h = 0;
+            e->h_tma_err = h;
+        }
+    }
     if (err == cudaSuccess) err = cudaMemset(e->d_tma_tiles, 0, sizeof(unsigned long long));
     if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "ensemble TMA maps: %s", cudaGetErrorString(err));
     return GOC_OK;
@@ -426,7 +435,19 @@ extern "C" int goc_ensemble_end_block(void* ensemble, int n_launched, void* stre
     ensemble_end_block_kernel<<<(e->n_members + 127) / 128, 128, 0, as_stream(stream)>>>(e->d_members, e->d_nsub,
                                                                                       e->n_members);
     count_launch();
-    return check_launch("ensemble_end_block_kernel");
+    int rc = check_launch("ensemble_end_block_kernel");
+    if (rc) return rc;
+    // the staging error flag, for goc_ensemble_staging_errors
+    const cudaError_t err = cudaMemcpyAsync(const_cast<int*>(e->h_tma_err), e->d_tma_err, sizeof(int),
+                                            cudaMemcpyDeviceToHost, as_stream(stream));
+    if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_ensemble_end_block: %s", cudaGetErrorString(err));
+    return GOC_OK;
+}
+
+extern "C" int goc_ensemble_staging_errors(void* ensemble, int* errors) {
+    if (!ensemble || !errors) return set_error(GOC_ERR_ARG, "goc_ensemble_staging_errors: null argument");
+    *errors = *static_cast<Ensemble*>(ensemble)->h_tma_err;
+    return GOC_OK;
 }
 
 extern "C" int goc_ensemble_get_member(void* ensemble, int m, GocMemberDesc* out, void* stream) {

@@ -40,6 +40,7 @@ struct Ensemble {
     CUtensorMap* d_tmaps = nullptr;       // [shape][member][buffer set][eta, hu, hv] TMA maps of the state
     const float** d_tma_base = nullptr;   // per member: set-0 eta buffer (null: member not staged by TMA)
     int* d_tma_err = nullptr;             // set when a staging wait ran out
+    volatile int* h_tma_err = nullptr;    // pinned host copy, refreshed at the end of every block
     unsigned long long* d_tma_tiles = nullptr;  // tiles staged by TMA so far
     int n_tma_members = 0;
     float* d_dt = nullptr;                // n_members x max_substeps
@@ -143,7 +144,10 @@ ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __res
         bool pending = false;  // the previous tile of the run staged this one
         for (int r = 0; r < t.w; ++r) {
             const int ty = t.z + r;
-            tma.staged = use_tma && !tile_on_border<TX, TY, 2>(md.p, t.y, ty);
+            // tma_off is set by thread 0 only before the previous tile's
+            // staging point and read here after a barrier: a copy of this
+            // tile was issued exactly when `pending` and tma_off is still 0
+            tma.staged = use_tma && tma_off == 0 && !tile_on_border<TX, TY, 2>(md.p, t.y, ty);
             staged_tiles += tma.staged ? 1u : 0u;
             if (tma.staged && !pending && threadIdx.x == 0)
                 tma_stage_tile<TX + 8, TY + 8>(tma, *reinterpret_cast<TileSmem<TX + 8, TY + 8>*>(smem_raw),
@@ -153,14 +157,19 @@ ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __res
             // stage-1 rows handed along the run through two alternating buffers
             const float* side_in = side + ((r + 1) & 1) * NSIDE;
             float* side_out = r + 1 < t.w ? side + (r & 1) * NSIDE : nullptr;
-            cdklm_strip_tile<TX, TY, kNT, CONST_F, SIMPLE_FORCING>(
-                md.p, kc, dt, t.y, ty, r > 0, md.eta[in], md.hu[in], md.hv[in], md.eta[out], md.hu[out],
-                md.hv[out], md.pitch / 4, md.Hi, md.Hi_pitch / 4, md.Hm, md.Hm_pitch / 4, smem_raw, side_in,
-                side_out, &tma);
-            pending = tma.next_tile_y >= 0;
+            // every thread gets the same answer (it comes from a barrier
+            // vote): a CTA whose staged input never landed stops here, with
+            // the error flag set for the host
+            if (!cdklm_strip_tile<TX, TY, kNT, CONST_F, SIMPLE_FORCING>(
+                    md.p, kc, dt, t.y, ty, r > 0, md.eta[in], md.hu[in], md.hv[in], md.eta[out], md.hu[out],
+                    md.hv[out], md.pitch / 4, md.Hi, md.Hi_pitch / 4, md.Hm, md.Hm_pitch / 4, smem_raw, side_in,
+                    side_out, &tma))
+                goto done;
+            pending = tma.next_tile_y >= 0 && tma_off == 0;
             __syncthreads();
         }
     }
+done:
     if (threadIdx.x == 0 && staged_tiles) atomicAdd(tma_tiles, (unsigned long long)staged_tiles);
 }
 

@@ -186,9 +186,14 @@ extern "C" int goc_periodic_ghosts(int nx, int ny, int bc_north, int bc_east, fl
     return GOC_OK;
 }
 
+// Reduction blocks of the CFL kernels for an nx x ny grid; -1 when the grid
+// is too large for one launch (block rows beyond the grid's y limit, or a
+// count beyond INT_MAX).  The counts are formed in 64 bits.
 extern "C" int goc_max_dt_partials(int nx, int ny) {
     if (nx < 1 || ny < 1) return 0;
-    return ((nx + kDtBX - 1) / kDtBX) * ((ny + kDtBY - 1) / kDtBY);
+    const long long bx = ((long long)nx + kDtBX - 1) / kDtBX, by = ((long long)ny + kDtBY - 1) / kDtBY;
+    if (by > 65535 || bx * by > INT_MAX) return -1;
+    return (int)(bx * by);
 }
 
 extern "C" int goc_max_dt(int nx, int ny, float dx, float dy, float g, const float* eta, const float* hu,
@@ -199,6 +204,7 @@ extern "C" int goc_max_dt(int nx, int ny, float dx, float dy, float g, const flo
     if (pitch < (nx + 4) * 4 || pitch % 4 || Hm_pitch < (nx + 4) * 4 || Hm_pitch % 4)
         return set_error(GOC_ERR_ARG, "goc_max_dt: pitch too small");
     const int need = goc_max_dt_partials(nx, ny);
+    if (need < 0) return set_error(GOC_ERR_ARG, "goc_max_dt: a %d x %d grid is too large for one launch", nx, ny);
     if (partials_capacity < need)
         return set_error(GOC_ERR_ARG, "goc_max_dt: partials holds %d floats, %d needed", partials_capacity, need);
     cudaStream_t st = as_stream(stream);
@@ -218,6 +224,9 @@ extern "C" int goc_max_dt(int nx, int ny, float dx, float dy, float g, const flo
 // file-scope device array instead of caller-provided scratch.
 // ---------------------------------------------------------------------------
 
+#include <cuda.h>
+
+#include <climits>
 #include <mutex>
 
 namespace goc {
@@ -228,27 +237,68 @@ namespace goc {
 constexpr int kNoAllocPartials = 65536;
 static __device__ __align__(256) float g_dt_partials[kNoAllocPartials];
 
-// Device address of g_dt_partials, looked up once per device.  In host code
-// the array's name is only a host-side stand-in, so the address must come
-// from cudaGetSymbolAddress with the device current.
+// Device address of g_dt_partials, looked up once per device and context.
+// In host code the array's name is only a host-side stand-in, so the address
+// must come from cudaGetSymbolAddress with the device current.  The address
+// belongs to the device's current context: when that context is replaced
+// (cudaDeviceReset and a new primary context, or another context made
+// current) the module is loaded anew and the address is looked up again.
+// Contexts are told apart by their driver-assigned ID, which is never reused
+// within a process.
 constexpr int kMaxDevices = 64;
-static float* g_dt_partials_addr[kMaxDevices] = {nullptr};
+struct NoAllocSlot {
+    float* addr = nullptr;
+    unsigned long long ctx_id = 0;
+};
+static NoAllocSlot g_dt_partials_slot[kMaxDevices];
 static std::mutex g_dt_partials_mutex;
+
+// ID of the calling thread's current context (cuCtxGetCurrent + cuCtxGetId
+// through the runtime's driver entry points, so the library need not link
+// libcuda); false if the driver does not provide them.
+static bool current_context_id(unsigned long long* id) {
+    typedef CUresult (*GetCurrentFn)(CUcontext*);
+    typedef CUresult (*GetIdFn)(CUcontext, unsigned long long*);
+    static GetCurrentFn get_current = nullptr;
+    static GetIdFn get_id = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrentFn>(p);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetIdFn>(p);
+        cudaGetLastError();
+    }
+    CUcontext ctx = nullptr;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+    return get_id(ctx, id) == CUDA_SUCCESS;
+}
 
 static int noalloc_partials(float** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_max_dt_noalloc: cudaGetDevice: %s", cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return set_error(GOC_ERR_UNSUPPORTED, "goc_max_dt_noalloc: device %d", dev);
+    unsigned long long id = 0;
+    bool have_id = current_context_id(&id);
     std::lock_guard<std::mutex> lock(g_dt_partials_mutex);
-    if (!g_dt_partials_addr[dev]) {
+    NoAllocSlot& slot = g_dt_partials_slot[dev];
+    if (!slot.addr || !have_id || slot.ctx_id != id) {
+        // (also makes the device's primary context current if none is)
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_dt_partials);
         if (e != cudaSuccess)
             return set_error(GOC_ERR_CUDA, "goc_max_dt_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-        g_dt_partials_addr[dev] = static_cast<float*>(p);
+        slot.addr = static_cast<float*>(p);
+        have_id = current_context_id(&id);
+        slot.ctx_id = have_id ? id : 0;
     }
-    *out = g_dt_partials_addr[dev];
+    *out = slot.addr;
     return GOC_OK;
 }
 
@@ -261,7 +311,7 @@ extern "C" int goc_max_dt_noalloc(int nx, int ny, float dx, float dy, float g, c
                                   float* dt_out, void* stream) {
     if (nx < 1 || ny < 1) return set_error(GOC_ERR_ARG, "goc_max_dt_noalloc: nx, ny must be >= 1");
     const int need = goc_max_dt_partials(nx, ny);
-    if (need > goc::kNoAllocPartials)
+    if (need < 0 || need > goc::kNoAllocPartials)
         return set_error(GOC_ERR_ARG,
                          "goc_max_dt_noalloc: a %d x %d grid needs %d partial minima, the built-in scratch holds %d "
                          "(at most %d reduction blocks of %d x %d cells); use goc_max_dt with caller scratch",

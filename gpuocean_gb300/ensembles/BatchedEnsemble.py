@@ -264,6 +264,15 @@ class BatchedEnsemble:
         _lib.call("goc_ensemble_size", self._handle, ctypes.byref(nm), ctypes.byref(nt))
         return nt.value
 
+    def _check_staging(self):
+        """Raise if a block that has completed on the device lost a CTA to a
+        TMA copy of its input that never landed (the device flag, copied to
+        host memory at the end of every block; no synchronisation)."""
+        errors = ctypes.c_int()
+        _lib.call("goc_ensemble_staging_errors", self._handle, ctypes.byref(errors))
+        if errors.value:
+            raise RuntimeError("batched step: a TMA staging wait ran out; the ensemble state is not valid")
+
     def tma_status(self):
         """(members whose interior tiles stage their input state by TMA,
         tiles staged so far, staging waits that ran out - 0 in normal
@@ -542,6 +551,7 @@ class BatchedEnsemble:
         else:
             self.kernels_launched += self._launch_block(nsub, with_noise)
         self._before_members()
+        self._check_staging()
         cells = 0
         for m, s in enumerate(self.sims):
             for local_dt in scheds[m]:
@@ -557,6 +567,7 @@ class BatchedEnsemble:
 
     def synchronize(self):
         self.stream.synchronize()
+        self._check_staging()
 
     # ------------------------------------------------------------------
     # observation operator and ensemble statistics
@@ -689,17 +700,20 @@ class BatchedEnsemble:
                 b.free()
         return tuple(out)
 
-    def updateDt(self, courant_number=None):
-        """Batched CFL limit of every member (one reduction launch pair)."""
+    def updateDt(self, courant_number=None, members=None):
+        """Batched CFL limit of every member (one reduction launch pair);
+        ``members``: indices of the members whose dt is set (default all)."""
         self._after_members()
         _lib.call("goc_ensemble_max_dt", self._handle, self._dt_dev.ptr, self.stream.handle)
         out = np.zeros(len(self.sims), dtype=np.float32)
         _lib.call("goc_memcpy_d2h_async", out.ctypes.data, self._dt_dev.ptr, ctypes.c_size_t(out.nbytes),
                   self.stream.handle)
         self.stream.synchronize()
-        for s, v in zip(self.sims, out):
+        chosen = range(len(self.sims)) if members is None else members
+        for m in chosen:
+            s = self.sims[m]
             cn = s.courant_number if courant_number is None else courant_number
-            s.dt = cn * v
+            s.dt = cn * out[m]
         return out
 
 

@@ -70,16 +70,54 @@ class MultiLevelOceanEnsemble:
         self.engine.step(t, apply_stochastic_term=apply_stochastic_term, noise_cadence="step")
         self.t = self.ML_ensemble[0][0].t
 
-    def stepToObservation(self, obs_time, courant_number=0.8):
-        """Advance to obs_time with model error every model_time_step."""
+    def _leaders(self):
+        """Engine indices of the simulators whose own dataAssimilationStep
+        the reference calls (level 0 and the fine partners); the coarse
+        partners ride along as ``otherSim``."""
+        groups = self._groups()
+        first, n0 = groups[0]
+        out = list(range(first, first + n0))
+        for (fa, n), _ in groups[1:]:
+            out += list(range(fa, fa + n))
+        return out
+
+    def _run_to(self, end_time, courant_number):
+        """Every member to end_time in the blocks of
+        CDKLM16.dataAssimilationStep (S/CDKLM16.py:742-806), the coarse
+        partners perturbed like their fine partners after each block.  dt:
+        all members at the start, the leaders again after every fifth block
+        they have taken."""
+        from ..SWEsimulators.ObservationSchedule import blocks_to_observation, refresh_dt_after
+        eng = self.engine
         s0 = self.ML_ensemble[0][0]
-        mts = s0.model_time_step
-        self.engine.updateDt(courant_number=courant_number)
-        n_blocks = int(round((obs_time - s0.t) / mts))
-        for b in range(n_blocks):
-            self.engine.step(mts, apply_stochastic_term=self.engine._noise is not None)
-            if (b + 1) % 5 == 0:
-                self.engine.updateDt(courant_number=courant_number)
+        plan = blocks_to_observation(end_time - s0.t, s0.model_time_step)
+        leaders = self._leaders()
+        eng.updateDt(courant_number=courant_number)
+        noisy = eng._noise is not None
+        for blk in plan:
+            eng.step(blk.length, apply_stochastic_term=noisy and blk.perturbation == 1.0)
+            if noisy and blk.perturbation is not None and blk.perturbation != 1.0:
+                eng.perturb(perturbation_scale=blk.perturbation)
+            for m in leaders:
+                self.members[m].total_time_steps += 1
+            if refresh_dt_after(s0.total_time_steps):
+                eng.updateDt(courant_number=courant_number, members=leaders)
+
+    def stepToObservation(self, obs_time, courant_number=0.8):
+        """Advance to obs_time as the reference does
+        (E/MultiLevelOceanEnsemble.py:110-141): with drifters attached, in
+        stretches of at most drift_dt, the drifters moving after each."""
+        s0 = self.ML_ensemble[0][0]
+        t = s0.t
+        while t < obs_time:
+            end = obs_time
+            if getattr(self, "drifters", None) is not None:
+                step = min(obs_time - t, self.drift_dt)
+                end = t + step
+            self._run_to(end, courant_number)
+            if getattr(self, "drifters", None) is not None:
+                self.drift(step)
+            t = end
         self.t = s0.t
 
     # ------------------------------------------------------------------

@@ -77,32 +77,26 @@ class OceanModelEnsemble:
                 p.cleanUp(do_gc=False)
 
     def stepToObservation(self, observation_time, write_now=False, courant_number=0.8):
-        """Advance to observation_time with model error after every
-        model_time_step, as CDKLM16.dataAssimilationStep does for each member
-        (S/CDKLM16.py:742-806), all members at once."""
+        """Advance to observation_time in the blocks that
+        CDKLM16.dataAssimilationStep takes for each member (S/CDKLM16.py:
+        742-806; plan from ``ObservationSchedule.blocks_to_observation``),
+        all members at once.  Full blocks with model error run as one graph
+        with the model error inside; a shorter first block is stepped and
+        then perturbed with its own scale."""
+        from ..SWEsimulators.ObservationSchedule import blocks_to_observation, refresh_dt_after
         eng = self._engine()
         p0 = self.particles[0]
-        mts = p0.model_time_step
-        full = int(round(observation_time - p0.t) / mts)
-        leftover = observation_time - p0.t - full * mts
-        if leftover / mts < 0.1 and full > 1:
-            leftover += mts
-            full -= 1
-        if leftover / mts < 0.00001:
-            leftover = 0
-        assert full > 0, "There is less than CDKLM16.model_time_step until the observation"
+        plan = blocks_to_observation(observation_time - p0.t, p0.model_time_step)
         eng.updateDt(courant_number=courant_number)
-        for i in range(full + 1):
-            if i == 0 and leftover == 0:
-                continue
-            if i == 0:
-                eng.step(leftover)
-                eng.perturb(perturbation_scale=np.sqrt(leftover / mts))
-            else:
-                eng.step(mts, apply_stochastic_term=eng._noise is not None)
+        noisy = eng._noise is not None
+        for blk in plan:
+            scaled = noisy and blk.perturbation is not None and blk.perturbation != 1.0
+            eng.step(blk.length, apply_stochastic_term=noisy and blk.perturbation == 1.0)
+            if scaled:
+                eng.perturb(perturbation_scale=blk.perturbation)
             for p in self.particles:
                 p.total_time_steps += 1
-            if p0.total_time_steps % 5 == 0:
+            if refresh_dt_after(p0.total_time_steps):
                 eng.updateDt(courant_number=courant_number)
         self.t = observation_time
 

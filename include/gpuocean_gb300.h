@@ -218,7 +218,8 @@ int goc_bathymetry_init(int nx, int ny, int bc_north, int bc_east, int bc_south,
  * land cells) to dt_out[0], before the Courant factor.
  * Replaces per_block_max_dt + max_dt_reduction (K/max_dt.cu:42-195,
  * S/CDKLM16.py:814-841).  `partials` is caller-provided scratch of at least
- * goc_max_dt_partials(nx, ny) floats.
+ * goc_max_dt_partials(nx, ny) floats (-1: the grid is too large for one
+ * launch, and goc_max_dt rejects it with GOC_ERR_ARG).
  */
 int goc_max_dt_partials(int nx, int ny);
 int goc_max_dt(int nx, int ny, float dx, float dy, float g,
@@ -240,7 +241,10 @@ int goc_max_dt(int nx, int ny, float dx, float dy, float g,
  *    loads the library until the process exits.
  *  - The first call on a device looks up the array's device address with
  *    cudaGetSymbolAddress while that device is current; make that first call
- *    before any stream capture.
+ *    before any stream capture.  The address belongs to the device's current
+ *    context: after that context is replaced (cudaDeviceReset and a new
+ *    primary context, or another context made current) the next call looks
+ *    the address up again, and that call too must come before any capture.
  *  - All calls share the one array: calls whose kernels overlap on the GPU
  *    (e.g. on two streams at once) race.  Each call overwrites every partial
  *    it reads, so nothing needs clearing between calls.
@@ -440,6 +444,15 @@ int goc_ensemble_size(void* ensemble, int* n_members, int* n_tiles);
  * Reading the device counters synchronises.  Any output may be NULL.
  */
 int goc_ensemble_tma_status(void* ensemble, int* staged_members, long long* staged_tiles, int* wait_errors);
+/*
+ * The staging error flag as of the last block that completed on the device,
+ * without synchronising: goc_ensemble_end_block copies the device flag into
+ * pinned host memory at the end of every block.  Nonzero means a CTA's
+ * staged input never landed and that CTA stopped stepping: the states of
+ * that block are not valid.  (Batched engine; no counterpart in the
+ * reference.)
+ */
+int goc_ensemble_staging_errors(void* ensemble, int* errors);
 /*
  * Self-test of the bounded wait that guards TMA staging: one CTA waits on an
  * mbarrier phase that nothing completes, for limit_ms (0 < limit_ms <= 1000)

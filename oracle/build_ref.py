@@ -27,12 +27,15 @@ sys.path.insert(0, os.path.dirname(HERE))
 
 from oracle.ref_kernels import REF_CONFIGS, REF_DIR, cubin_path  # noqa: E402
 
-DEFAULT_REFERENCE = "/root/reference"
 KERNEL_SUBDIR = os.path.join("src", "gpuocean", "gpu_kernels")
 
 
 def kernel_dir(reference=None):
-    reference = reference or os.environ.get("GPUOCEAN_REFERENCE", DEFAULT_REFERENCE)
+    """The reference's kernel directory: ``reference`` or, if None,
+    ``$GPUOCEAN_REFERENCE``; None when neither names a checkout."""
+    reference = reference or os.environ.get("GPUOCEAN_REFERENCE")
+    if not reference:
+        return None
     d = os.path.join(reference, KERNEL_SUBDIR)
     return d if os.path.isdir(d) else None
 

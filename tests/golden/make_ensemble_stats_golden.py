@@ -16,7 +16,7 @@ stubs; only NumPy code of the reference runs.  ``observeParticles`` calls
 ``np.int``, which NumPy 2 removed; it is aliased to ``int`` while the script
 runs.  Writes ``ensemble_stats_reference.npz`` next to this file.
 
-Usage:  python tests/golden/make_ensemble_stats_golden.py [reference_root]
+Usage:  python tests/golden/make_ensemble_stats_golden.py REFERENCE_ROOT (or $GPUOCEAN_REFERENCE)
 """
 import os
 import sys
@@ -142,7 +142,9 @@ def ml_case(ML):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GPUOCEAN_REFERENCE")
+    if not root:
+        sys.exit("usage: %s REFERENCE_ROOT (or set GPUOCEAN_REFERENCE)" % sys.argv[0])
     Base, ML, dautils = import_reference(root)
     out = {}
     out.update(base_case(Base, dautils))

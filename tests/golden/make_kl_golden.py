@@ -9,7 +9,7 @@ zero on a 40 x 30 grid (default basis 1..10 in both directions), for wall
 and periodic boundaries, with and without the cosine basis.  Writes
 ``kl_reference.npz`` next to this file.
 
-Usage:  python tests/golden/make_kl_golden.py [reference_root]
+Usage:  python tests/golden/make_kl_golden.py REFERENCE_ROOT (or $GPUOCEAN_REFERENCE)
 """
 import os
 import sys
@@ -71,7 +71,9 @@ def make(cls, nx, ny, dx, dy, bc, include_cos, kl_decay=1.2, kl_scaling=0.05):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GPUOCEAN_REFERENCE")
+    if not root:
+        sys.exit("usage: %s REFERENCE_ROOT (or set GPUOCEAN_REFERENCE)" % sys.argv[0])
     cls = import_reference(root)
     nx, ny, dx, dy = 40, 30, 500.0, 400.0
     rng = np.random.default_rng(21)

@@ -9,7 +9,7 @@ This script imports them from a reference checkout (PyCUDA and matplotlib are
 absent here and are replaced by inert stubs; only CPU functions are called)
 and writes ``noise_drift_reference.npz`` next to this file.
 
-Usage:  python tests/golden/make_reference_vectors.py [reference_root]
+Usage:  python tests/golden/make_reference_vectors.py REFERENCE_ROOT (or $GPUOCEAN_REFERENCE)
 """
 import os
 import sys
@@ -64,7 +64,9 @@ def make_noise(cls, nx, ny, dx, dy, pns, pew, factor=1, q0=None, L=None):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GPUOCEAN_REFERENCE")
+    if not root:
+        sys.exit("usage: %s REFERENCE_ROOT (or set GPUOCEAN_REFERENCE)" % sys.argv[0])
     Noise, CPUDrifters, Common = import_reference(root)
     out = {}
     rng = np.random.default_rng(20240601)

@@ -1,12 +1,12 @@
 """Convert the reference's CDKLM16 regression vectors into a compact fixture.
 
 Reads ``test/timestep50/CDKLM16_*_{eta,u,v}.dat`` from a checkout of the
-reference (default ``/root/reference``) and writes the interior (70 x 50) of
+reference (the first argument, or ``$GPUOCEAN_REFERENCE``) and writes the interior (70 x 50) of
 each field as float32 into ``cdklm16_timestep50.npz`` next to this script.
 The ``.dat`` files hold float32 GPU results printed as float64 text, so the
 float32 round trip is exact.  The ``u``/``v`` files hold hu/hv.
 
-Usage:  python tests/golden/make_timestep50.py [reference_root]
+Usage:  python tests/golden/make_timestep50.py REFERENCE_ROOT
 """
 import os
 import sys
@@ -21,7 +21,9 @@ CASES = ["wallBC_central", "wallBC_corner", "wallBC_upperCorner",
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GPUOCEAN_REFERENCE")
+    if not root:
+        sys.exit("usage: %s REFERENCE_ROOT (or set GPUOCEAN_REFERENCE)" % sys.argv[0])
     src = os.path.join(root, "test", "timestep50")
     out = {}
     for case in CASES:
