@@ -17,6 +17,12 @@ c_fp = ctypes.POINTER(ctypes.c_float)
 c_i64 = ctypes.c_int64
 
 
+class GocDriftWindDesc(ctypes.Structure):
+    """Mirror of ``GocDriftWindDesc`` in include/gpuocean_gb300.h."""
+    _fields_ = [("x_current", c_void_p), ("x_next", c_void_p), ("y_current", c_void_p), ("y_next", c_void_p),
+                ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("wind_drift_factor", c_float)]
+
+
 class GocCdklmParams(ctypes.Structure):
     """Mirror of ``GocCdklmParams`` in include/gpuocean_gb300.h."""
     _fields_ = [
@@ -147,6 +153,8 @@ SIGNATURES = {
     "goc_ensemble_get_member": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "goc_ensemble_max_dt": (c_int, [c_void_p, c_void_p, c_void_p]),
     "goc_ensemble_set_drifters": (c_int, [c_void_p, c_void_p, ctypes.POINTER(c_int), c_float, c_void_p]),
+    "goc_ensemble_set_drift_wind": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "goc_ensemble_set_wind_times": (c_int, [c_void_p, c_void_p, c_void_p]),
     "goc_lcg_fill": (c_int, [c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_int, c_void_p]),
     "goc_xorwow_state_bytes": (c_size_t, [c_int]),
     "goc_xorwow_init": (c_int, [c_void_p, c_int, ctypes.c_ulonglong, c_void_p]),
@@ -157,6 +165,9 @@ SIGNATURES = {
     "goc_noise_batch_create": (c_int, [c_void_p, c_void_p, ctypes.POINTER(c_void_p)]),
     "goc_noise_batch_destroy": (c_int, [c_void_p]),
     "goc_noise_batch_perturb": (c_int, [c_void_p, c_void_p, c_float, c_int, c_void_p]),
+    "goc_noise_batch_field": (c_int, [c_void_p, c_void_p, c_float, c_int, c_void_p]),
+    "goc_ensemble_set_block_noise": (c_int, [c_void_p, c_void_p, c_int]),
+    "goc_ensemble_set_noise_mask": (c_int, [c_void_p, c_void_p, c_void_p]),
     "goc_noise_batch_seed": (c_int, [c_void_p, ctypes.c_ulonglong, c_void_p]),
     "goc_noise_batch_generate": (c_int, [c_void_p, c_void_p, c_int, c_void_p]),
 }

@@ -28,9 +28,15 @@ DEFAULT_MATH = {"sponge.cu"}
 # per-file extra flags.  The step translation units keep every multiply and
 # add separately rounded (no FMA contraction), as the reference compiles its
 # step kernel (--fmad=false): with the same operation order this makes the
-# RK2 step bit-identical to the reference's kernel.  The noise kernels use
-# fast math, as the reference's do.
+# RK2 step bit-identical to the reference's kernel.  The random numbers, the
+# SOAR field and the KL model error use fast math, as the reference's noise
+# kernels do; the transfer of the SOAR field to the state is built like the
+# ensemble step, whose fused epilogue runs the same code (noise_transfer.cuh)
+# and must round identically; so must the single-collection drifter kernels
+# and the drifter work of the ensemble step.
 EXTRA = {"noise.cu": ["-use_fast_math"],
+         "noise_transfer.cu": ["-fmad=false"],
+         "drift.cu": ["-fmad=false"],
          "cdklm_step.cu": ["-fmad=false"],
          "ensemble.cu": ["-fmad=false"],
          **{f"ensemble_shape_{tx}x{ty}.cu": ["-fmad=false"]

@@ -25,6 +25,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "noise_transfer.cuh"
 #include "tma.cuh"
 
 namespace goc {
@@ -465,6 +466,19 @@ __device__ __forceinline__ void store_with_images(const GocCdklmParams& p, const
     }
 }
 
+// Model error fused into the step (ensemble launches that perturb): the
+// SOAR coarse field of the member (already computed for this block) is
+// up-sampled on the tile and its balanced perturbation is added to
+// Q^{n+1} before the write, the work of the stand-alone transfer kernel
+// (noise_transfer.cu) without its read-modify-write pass.  With `spare`,
+// the unperturbed Q^{n+1} is also written there (interior cells and
+// periodic images), for the drifters of the block's last step, which move
+// with the state before the model error.
+struct TileNoise {
+    const GocNoiseDesc* d;          // the member's descriptor (shared memory)
+    float* spare_e; float* spare_u; float* spare_v;   // unperturbed copy, or null
+};
+
 // Launch constants of a parameter set.
 // IEEE division on host and device alike, so that launch constants do not
 // depend on where they were derived (device code is built with
@@ -509,7 +523,7 @@ constexpr int kHandRows = 4;
 // reuses.  Only the RK2 fused path (NSTAGE = 2) streams.  s1 is a run-time
 // value so that one instantiation serves both kinds of tile (the kernel's
 // code stays within the instruction cache).
-template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING, bool BORDER>
+template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING, bool BORDER, bool NOISE = false>
 __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const StepConst& k, float dt, int rk_step,
                                                 int tile_x, int tile_y,
                                                 const float* __restrict__ e_in, const float* __restrict__ hu_in,
@@ -518,7 +532,8 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const S
                                                 const float* __restrict__ Hi_g, int hi_pitch,
                                                 const float* __restrict__ Hm_g, int hm_pitch, float* smem_raw,
                                                 int s1 = 2, const float* side_in = nullptr,
-                                                float* side_out = nullptr, TileTma* tma = nullptr) {
+                                                float* side_out = nullptr, TileTma* tma = nullptr,
+                                                const TileNoise* nz = nullptr) {
     constexpr int HALO = 2 * NSTAGE;
     constexpr int W = TX + 2 * HALO, H = TY + 2 * HALO;
     TileSmem<W, H>& S = *reinterpret_cast<TileSmem<W, H>*>(smem_raw);
@@ -730,6 +745,18 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const S
         // tile of the strip there meanwhile
         if (tma && tma->next_tile_y >= 0 && threadIdx.x == 0 && *tma->off == 0)
             tma_stage_tile<W, H>(*tma, S, T.x0 - 2, 2 + tma->next_tile_y * TY - HALO);
+        // model error: the eta perturbation on the tile + 1 ring, into Sy[1]
+        // (dead after the faces; the staging above does not touch it), with
+        // the cell-mean depths' plane (dead since stage 1) as scratch
+        constexpr int DW = TX + 2, DH = TY + 2;
+        float* de = &S.Sy[1][0][0];
+        if constexpr (NOISE) {
+            if (nz) {
+                noise_tile_field<DW, DH, NT>(*nz->d, p.dx, p.dy, T.x0 + HALO - 1, T.y0 + HALO - 1, de,
+                                             &S.Hmb[0][0], W * H, threadIdx.x);
+                __syncthreads();
+            }
+        }
         // A rolled loop keeps one copy of the cell update; Q^n of the cell is
         // loaded first, so its latency overlaps the update.
         for (int idx = threadIdx.x; idx < TX * TY; idx += NT) {
@@ -745,6 +772,23 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const S
             float nhu = 0.5f * (hua + (hu + dt * L2)) / (1.0f + 0.5f * C);
             float nhv = 0.5f * (hva + (hv + dt * L3)) / (1.0f + 0.5f * C);
             finish_cell(p, Hm, ne, nhu, nhv);
+            if constexpr (NOISE) {
+                if (nz) {
+                    if (nz->spare_e) {
+                        if (BORDER) {
+                            store_with_images(p, k, nz->spare_e, nz->spare_u, nz->spare_v, pitch, gx, gy, ne, nhu,
+                                              nhv);
+                        } else {
+                            nz->spare_e[o] = ne; nz->spare_u[o] = nhu; nz->spare_v[o] = nhv;
+                        }
+                    }
+                    const float* h0 = Hi_g + (size_t)gy * hi_pitch + gx;
+                    const float hc[4] = {__ldg(h0), __ldg(h0 + 1), __ldg(h0 + hi_pitch), __ldg(h0 + hi_pitch + 1)};
+                    const int ox = T.x0 + HALO - 1, oy = T.y0 + HALO - 1;
+                    perturbed_state(*nz->d, nx, ny, p.dx, p.dy, p.land_value, gx, gy, nz->d->interpolation_factor <= 1,
+                                    [&](int jj, int ii) { return de[(jj - oy) * DW + (ii - ox)]; }, ne, nhu, nhv, hc);
+                }
+            }
             if (BORDER) {
                 store_with_images(p, k, e_out, hu_out, hv_out, pitch, gx, gy, ne, nhu, nhv);
             } else {
@@ -834,24 +878,25 @@ __device__ __forceinline__ void cdklm_tile(const GocCdklmParams& p, const StepCo
 // interior rows computes all of its stage-1 rows: the north/south wall
 // mirrors of its first rows land in rows it does not take over.  East/west
 // borders keep the hand-over (their mirrors stay within a row).
-template <int TX, int TY, int NT, bool CONST_F, bool SIMPLE_FORCING>
+template <int TX, int TY, int NT, bool CONST_F, bool SIMPLE_FORCING, bool NOISE = false>
 __device__ __forceinline__ bool cdklm_strip_tile(const GocCdklmParams& p, const StepConst& k, float dt, int tile_x,
                                                  int tile_y, bool reuse, const float* __restrict__ e_in,
                                                  const float* __restrict__ hu_in, const float* __restrict__ hv_in,
                                                  float* e_out, float* hu_out, float* hv_out, int pitch,
                                                  const float* __restrict__ Hi_g, int hi_pitch,
                                                  const float* __restrict__ Hm_g, int hm_pitch, float* smem_raw,
-                                                 const float* side_in, float* side_out, TileTma* tma) {
+                                                 const float* side_in, float* side_out, TileTma* tma,
+                                                 const TileNoise* nz = nullptr) {
     const bool border = tile_on_border<TX, TY, 2>(p, tile_x, tile_y);
     const int y0 = 2 + tile_y * TY - 4;
     const int s1 = (reuse && y0 >= 2 && y0 + TY + 8 <= p.ny + 2) ? 2 + kHandRows : 2;
     if (border)
-        return cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, true>(
+        return cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, true, NOISE>(
             p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
-            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, s1, side_in, side_out, tma);
-    return cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, false>(
+            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, s1, side_in, side_out, tma, nz);
+    return cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, false, NOISE>(
         p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
-        pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, s1, side_in, side_out, tma);
+        pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, s1, side_in, side_out, tma, nz);
 }
 
 template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING>

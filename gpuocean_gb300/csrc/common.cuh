@@ -25,6 +25,12 @@ void count_launch(int n = 1);
 const GocMemberDesc* ensemble_host_members(void* ensemble, int* n_members);
 const GocMemberDesc* ensemble_device_members(void* ensemble);
 const int* ensemble_device_nsub(void* ensemble);
+// per member the block's step count if the member takes model error, else 0
+const int* ensemble_device_noise_steps(void* ensemble);
+
+// Device table of the members' SOAR descriptors of a noise batch handle
+// (noise.cu); n_members receives the batch's member count.
+const GocNoiseDesc* noise_batch_device_desc(void* batch, int* n_members);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 

@@ -17,14 +17,46 @@ namespace goc {
 // ---------------------------------------------------------------------------
 
 // Drift of the last step of members that ran all `n_launched` steps of the block.
-__global__ void ensemble_end_drift_kernel(const GocMemberDesc* __restrict__ members, const int* __restrict__ nsub,
-                                          const float* __restrict__ dt_table, int max_sub, int n_launched,
-                                          float* const* __restrict__ drift_pos, const int4* __restrict__ chunks,
-                                          float sensitivity) {
+// Drift of step s (state in buffer set (s + 1) % 2) outside the persistent
+// step: members with nsub == s + 1 (last_only: their block ended with step
+// s) or with s < nsub (every member that took step s).
+// spare: the members' unperturbed copies of the last step's state (3 per
+// member, null entries or a null table: drift with the state itself);
+// copy_only: only the members that drift with such a copy.  wind: per member
+// wind drift (factor 0: none), its time weight for step s in wind_t.
+__global__ void ensemble_drift_kernel(const GocMemberDesc* __restrict__ members, const int* __restrict__ nsub,
+                                      const float* __restrict__ dt_table, int max_sub, int s, int last_only,
+                                      float* const* __restrict__ drift_pos, const int4* __restrict__ chunks,
+                                      float sensitivity, float* const* __restrict__ spare,
+                                      const int* __restrict__ noise_steps, int copy_only,
+                                      const DriftWind* __restrict__ wind, const float* __restrict__ wind_t) {
     const int4 c = chunks[blockIdx.x];
-    if (nsub[c.x] != n_launched || n_launched == 0) return;
-    drift_chunk(members[c.x], drift_pos[c.x], c.y, c.z, n_launched & 1,
-                dt_table[(size_t)c.x * max_sub + (n_launched - 1)], sensitivity);
+    const int m = c.x, ns = nsub[m];
+    if (s < 0 || (last_only ? ns != s + 1 : s >= ns)) return;
+    // the copy holds the last step's state only if that step took model error
+    float* const* copy = (spare && spare[3 * m] && ns == s + 1 && noise_steps[m] == s + 1) ? spare + 3 * m : nullptr;
+    if (copy_only && !copy) return;
+    DriftWind w;
+    const bool windy = wind && wind[m].factor != 0.0f;
+    if (windy) {
+        w = wind[m];
+        w.t = wind_t[(size_t)m * max_sub + s];
+    }
+    const GocMemberDesc& d = members[m];
+    const DriftGrid g = member_drift_grid(d, (s + 1) & 1);
+    const float dt = dt_table[(size_t)m * max_sub + s];
+    float* pos = drift_pos[m];
+    for (int q = threadIdx.x; q < c.z; q += blockDim.x) {
+        float* p = pos + 2 * (size_t)(c.y + q);
+        float px = p[0], py = p[1];
+        if (copy)
+            drift_one_with(g, CopyVelocity{g, copy[0], copy[1], copy[2]}, windy ? &w : nullptr, dt, sensitivity, px,
+                           py);
+        else
+            drift_one(g, windy ? &w : nullptr, dt, sensitivity, px, py);
+        p[0] = px;
+        p[1] = py;
+    }
 }
 
 __global__ void ensemble_end_block_kernel(GocMemberDesc* members, const int* nsub, int n) {
@@ -83,6 +115,10 @@ static void free_ensemble(Ensemble* e) {
     cudaFree(e->d_dt_items);
     cudaFree(e->d_dt_ranges);
     cudaFree(e->d_partials);
+    if (e->d_step_chunks != e->d_drift_chunks) cudaFree(e->d_step_chunks);
+    cudaFree(e->d_wind_chunks);
+    cudaFree(e->d_wind);
+    cudaFree(e->d_wind_t);
     cudaFree(e->d_drift_pos);
     cudaFree(e->d_drift_chunks);
     cudaFree(e->d_drift_n);
@@ -91,6 +127,9 @@ static void free_ensemble(Ensemble* e) {
     cudaFree(e->d_tma_err);
     if (e->h_tma_err) cudaFreeHost(const_cast<int*>(e->h_tma_err));
     cudaFree(e->d_tma_tiles);
+    cudaFree(e->d_spare_pool);
+    cudaFree(e->d_spare);
+    cudaFree(e->d_nsub_noise);
     delete e;
 }
 
@@ -179,6 +218,8 @@ const GocMemberDesc* ensemble_device_members(void* ensemble) { return static_cas
 
 const int* ensemble_device_nsub(void* ensemble) { return static_cast<Ensemble*>(ensemble)->d_nsub; }
 
+const int* ensemble_device_noise_steps(void* ensemble) { return static_cast<Ensemble*>(ensemble)->d_nsub_noise; }
+
 static int shape_configure(const Ensemble* e, int* grid) {
     switch (e->shape) {
         case 0: return ensemble_configure_shape<32, 16>(e, grid);
@@ -190,13 +231,13 @@ static int shape_configure(const Ensemble* e, int* grid) {
     return set_error(GOC_ERR_ARG, "ensemble: tile shape %d out of range", e->shape);
 }
 
-static int shape_launch(Ensemble* e, int k, cudaStream_t st) {
+static int shape_launch(Ensemble* e, int k, cudaStream_t st, const FusedNoise* fn) {
     switch (e->shape) {
-        case 0: return ensemble_launch_shape<32, 16>(e, k, st);
-        case 1: return ensemble_launch_shape<32, 8>(e, k, st);
-        case 2: return ensemble_launch_shape<16, 16>(e, k, st);
-        case 3: return ensemble_launch_shape<64, 8>(e, k, st);
-        case 4: return ensemble_launch_shape<32, 24>(e, k, st);
+        case 0: return ensemble_launch_shape<32, 16>(e, k, st, fn);
+        case 1: return ensemble_launch_shape<32, 8>(e, k, st, fn);
+        case 2: return ensemble_launch_shape<16, 16>(e, k, st, fn);
+        case 3: return ensemble_launch_shape<64, 8>(e, k, st, fn);
+        case 4: return ensemble_launch_shape<32, 24>(e, k, st, fn);
     }
     return set_error(GOC_ERR_ARG, "ensemble: tile shape %d out of range", e->shape);
 }
@@ -304,6 +345,7 @@ extern "C" int goc_ensemble_create(const GocMemberDesc* members, int n_members, 
     alloc((void**)&e->d_members, sizeof(GocMemberDesc) * n_members);
     alloc((void**)&e->d_dt, sizeof(float) * (size_t)n_members * max_substeps);
     alloc((void**)&e->d_nsub, sizeof(int) * n_members);
+    alloc((void**)&e->d_nsub_noise, sizeof(int) * n_members);
     alloc((void**)&e->d_dt_items, sizeof(int4) * dt_items.size());
     alloc((void**)&e->d_dt_ranges, sizeof(int2) * ranges.size());
     alloc((void**)&e->d_partials, sizeof(float) * dt_items.size());
@@ -314,6 +356,7 @@ extern "C" int goc_ensemble_create(const GocMemberDesc* members, int n_members, 
     if (err == cudaSuccess)
         err = cudaMemcpy(e->d_dt_ranges, ranges.data(), sizeof(int2) * ranges.size(), cudaMemcpyHostToDevice);
     if (err == cudaSuccess) err = cudaMemset(e->d_nsub, 0, sizeof(int) * n_members);
+    if (err == cudaSuccess) err = cudaMemset(e->d_nsub_noise, 0, sizeof(int) * n_members);
     if (err == cudaSuccess) err = cudaMemset(e->d_dt, 0, sizeof(float) * (size_t)n_members * max_substeps);
     if (err != cudaSuccess) {
         free_ensemble(e);
@@ -363,6 +406,19 @@ extern "C" int goc_ensemble_size(void* ensemble, int* n_members, int* n_tiles) {
     return GOC_OK;
 }
 
+// Per member the steps of the block if it takes model error, else 0 (host
+// copy and device table); synchronises the stream (the host copy is reused).
+static int upload_noise_steps(Ensemble* e, cudaStream_t st) {
+    e->nsub_noise_host.assign(e->n_members, 0);
+    for (int m = 0; m < e->n_members && m < (int)e->nsub_host.size(); ++m)
+        e->nsub_noise_host[m] = (e->noise_mask.empty() || e->noise_mask[m]) ? e->nsub_host[m] : 0;
+    cudaError_t err = cudaMemcpyAsync(e->d_nsub_noise, e->nsub_noise_host.data(), sizeof(int) * e->n_members,
+                                      cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "ensemble noise steps: %s", cudaGetErrorString(err));
+    return GOC_OK;
+}
+
 extern "C" int goc_ensemble_set_schedule(void* ensemble, const float* dt_table, const int* n_substeps, void* stream) {
     if (!ensemble || !dt_table || !n_substeps) return set_error(GOC_ERR_ARG, "goc_ensemble_set_schedule: null argument");
     Ensemble* e = static_cast<Ensemble*>(ensemble);
@@ -381,14 +437,129 @@ extern "C" int goc_ensemble_set_schedule(void* ensemble, const float* dt_table, 
         err = cudaMemcpyAsync(e->d_nsub, n_substeps, sizeof(int) * e->n_members, cudaMemcpyHostToDevice, st);
     if (err == cudaSuccess) err = cudaStreamSynchronize(st);  // host arrays may be reused on return
     if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_ensemble_set_schedule: %s", cudaGetErrorString(err));
+    e->nsub_host.assign(n_substeps, n_substeps + e->n_members);
+    return upload_noise_steps(e, st);
+}
+
+extern "C" int goc_ensemble_set_noise_mask(void* ensemble, const int* mask, void* stream) {
+    if (!ensemble) return set_error(GOC_ERR_ARG, "goc_ensemble_set_noise_mask: null handle");
+    Ensemble* e = static_cast<Ensemble*>(ensemble);
+    if (mask) e->noise_mask.assign(mask, mask + e->n_members);
+    else e->noise_mask.clear();
+    return upload_noise_steps(e, as_stream(stream));
+}
+
+// The unperturbed copies of the members with drifters (one buffer set each,
+// with the member's pitch), allocated once.
+static int ensure_spares(Ensemble* e) {
+    if (e->d_spare) return GOC_OK;
+    std::vector<size_t> offset(e->n_members, 0);
+    size_t total = 0;
+    for (int m = 0; m < e->n_members; ++m) {
+        if (m >= (int)e->has_drifters.size() || !e->has_drifters[m]) continue;
+        const GocMemberDesc& d = e->host[m];
+        offset[m] = total;
+        total += 3 * (size_t)d.pitch * (d.p.ny + 4);
+    }
+    std::vector<float*> table(3 * (size_t)e->n_members, nullptr);
+    cudaError_t err = cudaSuccess;
+    if (total) {
+        err = cudaMalloc(&e->d_spare_pool, total);
+        // wall ghost cells are read from the state itself; the rest is written
+        // before it is read, but keep the copy defined from the start
+        if (err == cudaSuccess) err = cudaMemset(e->d_spare_pool, 0, total);
+    }
+    for (int m = 0; err == cudaSuccess && total && m < e->n_members; ++m) {
+        if (m >= (int)e->has_drifters.size() || !e->has_drifters[m]) continue;
+        const GocMemberDesc& d = e->host[m];
+        char* base = reinterpret_cast<char*>(e->d_spare_pool) + offset[m];
+        const size_t plane = (size_t)d.pitch * (d.p.ny + 4);
+        for (int c = 0; c < 3; ++c) table[3 * (size_t)m + c] = reinterpret_cast<float*>(base + c * plane);
+    }
+    if (err == cudaSuccess) err = cudaMalloc(&e->d_spare, sizeof(float*) * table.size());
+    if (err == cudaSuccess)
+        err = cudaMemcpy(e->d_spare, table.data(), sizeof(float*) * table.size(), cudaMemcpyHostToDevice);
+    if (err != cudaSuccess) {
+        cudaFree(e->d_spare_pool);
+        cudaFree(e->d_spare);
+        e->d_spare_pool = nullptr;
+        e->d_spare = nullptr;
+        return set_error(GOC_ERR_CUDA, "goc_ensemble_set_block_noise: %s", cudaGetErrorString(err));
+    }
     return GOC_OK;
+}
+
+extern "C" int goc_ensemble_set_block_noise(void* ensemble, void* noise_batch, int mode) {
+    if (!ensemble) return set_error(GOC_ERR_ARG, "goc_ensemble_set_block_noise: null handle");
+    Ensemble* e = static_cast<Ensemble*>(ensemble);
+    if (mode < 0) {
+        e->block_noise = -1;
+        e->noise_batch = nullptr;
+        return GOC_OK;
+    }
+    if (mode != kNoiseLastStep && mode != kNoiseEveryStep)
+        return set_error(GOC_ERR_ARG, "goc_ensemble_set_block_noise: mode %d (0 = last step, 1 = every step)", mode);
+    int n = 0;
+    if (!noise_batch || !noise_batch_device_desc(noise_batch, &n) || n != e->n_members)
+        return set_error(GOC_ERR_ARG, "goc_ensemble_set_block_noise: the noise batch must have one member per member");
+    if (mode == kNoiseLastStep) {
+        const int rc = ensure_spares(e);
+        if (rc) return rc;
+    }
+    e->block_noise = mode;
+    e->noise_batch = noise_batch;
+    return GOC_OK;
+}
+
+// One launch of ensemble_drift_kernel over `chunks` (see there).
+static int launch_drift(Ensemble* e, int s, int last_only, int copy_only, const int4* chunks, int n_chunks,
+                        float* const* spare, void* stream) {
+    if (n_chunks <= 0) return GOC_OK;
+    ensemble_drift_kernel<<<n_chunks, kDriftChunk, 0, as_stream(stream)>>>(
+        e->d_members, e->d_nsub, e->d_dt, e->max_substeps, s, last_only, e->d_drift_pos, chunks,
+        e->drift_sensitivity, spare, e->d_nsub_noise, copy_only, e->d_wind, e->d_wind_t);
+    count_launch();
+    return check_launch("ensemble_drift_kernel");
 }
 
 extern "C" int goc_ensemble_rk2_substep(void* ensemble, int k, void* stream) {
     if (!ensemble) return set_error(GOC_ERR_ARG, "goc_ensemble_rk2_substep: null handle");
     Ensemble* e = static_cast<Ensemble*>(ensemble);
     if (k < 0 || k >= e->max_substeps) return set_error(GOC_ERR_ARG, "goc_ensemble_rk2_substep: k=%d out of range", k);
-    return shape_launch(e, k, as_stream(stream));
+    if (k >= 1 && e->n_wind_chunks > 0) {
+        // drifters with wind drift: the drift of step k - 1 in a launch of
+        // its own (it reads set k % 2, which this step does not write)
+        const int rc = launch_drift(e, k - 1, 0, 0, e->d_wind_chunks, e->n_wind_chunks,
+                                    e->block_noise == kNoiseLastStep ? e->d_spare : nullptr, stream);
+        if (rc) return rc;
+    }
+    if (e->block_noise < 0) return shape_launch(e, k, as_stream(stream), nullptr);
+    // model error fused into this step for the members that take it here
+    bool any = false;
+    for (int m = 0; m < e->n_members && !any; ++m) {
+        const int ns = m < (int)e->nsub_noise_host.size() ? e->nsub_noise_host[m] : 0;
+        any = e->block_noise == kNoiseEveryStep ? k < ns : k == ns - 1;
+    }
+    const FusedNoise fn{noise_batch_device_desc(e->noise_batch, nullptr),
+                        e->block_noise == kNoiseLastStep ? e->d_spare : nullptr, e->block_noise};
+    if (fn.spare && k >= 1 && e->n_step_chunks > 0) {
+        // members whose block ended with step k - 1: their drifters move with
+        // the unperturbed copy of that step's state (the persistent launch
+        // leaves them out)
+        bool ended = false;
+        for (int m = 0; m < e->n_members && !ended; ++m)
+            ended = m < (int)e->has_drifters.size() && e->has_drifters[m] && e->nsub_host[m] == k &&
+                    e->nsub_noise_host[m] == k;
+        if (ended) {
+            const int rc = launch_drift(e, k - 1, 1, 1, e->d_step_chunks, e->n_step_chunks, fn.spare, stream);
+            if (rc) return rc;
+        }
+    }
+    if (any) return shape_launch(e, k, as_stream(stream), &fn);
+    // no member perturbs here, but drifters of members whose block ended
+    // with a perturbed step read that step's unperturbed copy
+    const FusedNoise plain{nullptr, fn.spare, fn.mode};
+    return fn.spare ? shape_launch(e, k, as_stream(stream), &plain) : shape_launch(e, k, as_stream(stream), nullptr);
 }
 
 extern "C" int goc_ensemble_tile_shape_count(void) { return kNumEnsembleShapes; }
@@ -425,11 +596,8 @@ extern "C" int goc_ensemble_end_block(void* ensemble, int n_launched, void* stre
     if (n_launched < 0 || n_launched > e->max_substeps)
         return set_error(GOC_ERR_ARG, "goc_ensemble_end_block: %d steps launched, max %d", n_launched, e->max_substeps);
     if (e->n_drift_chunks > 0 && n_launched > 0) {
-        ensemble_end_drift_kernel<<<e->n_drift_chunks, kDriftChunk, 0, as_stream(stream)>>>(
-            e->d_members, e->d_nsub, e->d_dt, e->max_substeps, n_launched, e->d_drift_pos, e->d_drift_chunks,
-            e->drift_sensitivity);
-        count_launch();
-        int rc = check_launch("ensemble_end_drift_kernel");
+        const int rc = launch_drift(e, n_launched - 1, 1, 0, e->d_drift_chunks, e->n_drift_chunks,
+                                    e->block_noise == kNoiseLastStep ? e->d_spare : nullptr, stream);
         if (rc) return rc;
     }
     ensemble_end_block_kernel<<<(e->n_members + 127) / 128, 128, 0, as_stream(stream)>>>(e->d_members, e->d_nsub,
@@ -475,6 +643,8 @@ extern "C" int goc_ensemble_max_dt(void* ensemble, float* dt_out, void* stream) 
     return check_launch("ensemble_dt_final_kernel");
 }
 
+static int split_chunks(Ensemble* e);
+
 extern "C" int goc_ensemble_set_drifters(void* ensemble, float* const* positions, const int* num_drifters,
                                          float sensitivity, void* stream) {
     if (!ensemble || !positions || !num_drifters) return set_error(GOC_ERR_ARG, "goc_ensemble_set_drifters: null argument");
@@ -482,8 +652,10 @@ extern "C" int goc_ensemble_set_drifters(void* ensemble, float* const* positions
     std::vector<int4> chunks;
     std::vector<int> nd(e->n_members, 0);
     long long packed = 0;
+    e->has_drifters.assign(e->n_members, 0);
     for (int m = 0; m < e->n_members; ++m) {
         if (!positions[m]) continue;
+        e->has_drifters[m] = 1;
         if (num_drifters[m] < 0) return set_error(GOC_ERR_ARG, "goc_ensemble_set_drifters: negative count");
         nd[m] = num_drifters[m];
         const int n = num_drifters[m] + 1;  // with the observation row
@@ -494,6 +666,20 @@ extern "C" int goc_ensemble_set_drifters(void* ensemble, float* const* positions
     }
     cudaStream_t st = as_stream(stream);
     cudaError_t err = cudaStreamSynchronize(st);
+    // the unperturbed copies follow the members with drifters: made anew
+    cudaFree(e->d_spare_pool);
+    cudaFree(e->d_spare);
+    e->d_spare_pool = nullptr;
+    e->d_spare = nullptr;
+    if (e->block_noise == kNoiseLastStep && err == cudaSuccess) {
+        const int rc = ensure_spares(e);
+        if (rc) return rc;
+    }
+    if (e->d_step_chunks != e->d_drift_chunks) cudaFree(e->d_step_chunks);
+    cudaFree(e->d_wind_chunks);
+    e->d_step_chunks = nullptr;
+    e->d_wind_chunks = nullptr;
+    e->n_step_chunks = e->n_wind_chunks = 0;
     cudaFree(e->d_drift_pos);
     cudaFree(e->d_drift_chunks);
     cudaFree(e->d_drift_n);
@@ -513,8 +699,76 @@ extern "C" int goc_ensemble_set_drifters(void* ensemble, float* const* positions
     }
     if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_ensemble_set_drifters: %s", cudaGetErrorString(err));
     e->n_drift_chunks = (int)chunks.size();
+    e->host_chunks = chunks;
     e->drift_rows = packed;
     e->drift_sensitivity = sensitivity;
+    return split_chunks(e);
+}
+
+// The persistent step advects the drifters of members without wind drift;
+// those with wind drift move in launches of their own (ensemble_drift_kernel).
+static int split_chunks(Ensemble* e) {
+    if (e->d_step_chunks != e->d_drift_chunks) cudaFree(e->d_step_chunks);
+    cudaFree(e->d_wind_chunks);
+    e->d_step_chunks = e->d_drift_chunks;
+    e->n_step_chunks = e->n_drift_chunks;
+    e->d_wind_chunks = nullptr;
+    e->n_wind_chunks = 0;
+    std::vector<int4> plain, windy;
+    for (const int4& c : e->host_chunks)
+        (c.x < (int)e->has_wind.size() && e->has_wind[c.x] ? windy : plain).push_back(c);
+    if (windy.empty()) return GOC_OK;
+    cudaError_t err = cudaMalloc(&e->d_wind_chunks, sizeof(int4) * windy.size());
+    if (err == cudaSuccess)
+        err = cudaMemcpy(e->d_wind_chunks, windy.data(), sizeof(int4) * windy.size(), cudaMemcpyHostToDevice);
+    e->d_step_chunks = nullptr;
+    if (err == cudaSuccess && !plain.empty()) {
+        err = cudaMalloc(&e->d_step_chunks, sizeof(int4) * plain.size());
+        if (err == cudaSuccess)
+            err = cudaMemcpy(e->d_step_chunks, plain.data(), sizeof(int4) * plain.size(), cudaMemcpyHostToDevice);
+    }
+    if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "ensemble drifter chunks: %s", cudaGetErrorString(err));
+    e->n_wind_chunks = (int)windy.size();
+    e->n_step_chunks = (int)plain.size();
+    return GOC_OK;
+}
+
+extern "C" int goc_ensemble_set_drift_wind(void* ensemble, const GocDriftWindDesc* wind, void* stream) {
+    if (!ensemble) return set_error(GOC_ERR_ARG, "goc_ensemble_set_drift_wind: null handle");
+    Ensemble* e = static_cast<Ensemble*>(ensemble);
+    std::vector<DriftWind> table(e->n_members);
+    e->has_wind.assign(e->n_members, 0);
+    for (int m = 0; wind && m < e->n_members; ++m) {
+        const GocDriftWindDesc& w = wind[m];
+        if (w.wind_drift_factor == 0.0f) {
+            table[m] = DriftWind{nullptr, nullptr, nullptr, nullptr, 1, 1, 0.0f, 0.0f};
+            continue;
+        }
+        if (!w.x_current || !w.x_next || !w.y_current || !w.y_next || w.nx < 1 || w.ny < 1)
+            return set_error(GOC_ERR_ARG, "goc_ensemble_set_drift_wind: member %d: wind textures missing", m);
+        table[m] = DriftWind{w.x_current, w.x_next, w.y_current, w.y_next, w.nx, w.ny, 0.0f, w.wind_drift_factor};
+        e->has_wind[m] = 1;
+    }
+    cudaError_t err = cudaStreamSynchronize(as_stream(stream));
+    if (err == cudaSuccess && !e->d_wind) err = cudaMalloc(&e->d_wind, sizeof(DriftWind) * e->n_members);
+    if (err == cudaSuccess && !e->d_wind_t)
+        err = cudaMalloc(&e->d_wind_t, sizeof(float) * (size_t)e->n_members * e->max_substeps);
+    if (err == cudaSuccess) err = cudaMemset(e->d_wind_t, 0, sizeof(float) * (size_t)e->n_members * e->max_substeps);
+    if (err == cudaSuccess)
+        err = cudaMemcpy(e->d_wind, table.data(), sizeof(DriftWind) * e->n_members, cudaMemcpyHostToDevice);
+    if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_ensemble_set_drift_wind: %s", cudaGetErrorString(err));
+    return split_chunks(e);
+}
+
+extern "C" int goc_ensemble_set_wind_times(void* ensemble, const float* wind_t, void* stream) {
+    if (!ensemble || !wind_t) return set_error(GOC_ERR_ARG, "goc_ensemble_set_wind_times: null argument");
+    Ensemble* e = static_cast<Ensemble*>(ensemble);
+    if (!e->d_wind_t) return set_error(GOC_ERR_ARG, "goc_ensemble_set_wind_times: call goc_ensemble_set_drift_wind first");
+    cudaStream_t st = as_stream(stream);
+    cudaError_t err = cudaMemcpyAsync(e->d_wind_t, wind_t, sizeof(float) * (size_t)e->n_members * e->max_substeps,
+                                      cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);  // the host table may be reused on return
+    if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "goc_ensemble_set_wind_times: %s", cudaGetErrorString(err));
     return GOC_OK;
 }
 

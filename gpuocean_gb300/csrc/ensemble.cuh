@@ -50,11 +50,36 @@ struct Ensemble {
     float* d_partials = nullptr;          // CFL scratch
     // drifters: one (N_m + 1) x 2 position array per member
     float** d_drift_pos = nullptr;        // per member, null = no drifters
-    int4* d_drift_chunks = nullptr;       // (member, first row, count, packed row of the first row)
+    int4* d_drift_chunks = nullptr;       // (member, first row, count, packed row of the first row), all members
     int n_drift_chunks = 0;
+    std::vector<int4> host_chunks;
+    // chunks the persistent step advects (members without wind drift) and
+    // those a launch of their own advects (members with wind drift)
+    int4* d_step_chunks = nullptr;        // == d_drift_chunks when no member has wind drift
+    int n_step_chunks = 0;
+    int4* d_wind_chunks = nullptr;
+    int n_wind_chunks = 0;
+    std::vector<char> has_wind;           // per member
+    DriftWind* d_wind = nullptr;          // per member (factor 0: none); t comes from d_wind_t
+    float* d_wind_t = nullptr;            // n_members x max_substeps: wind time weight of each step's drift
     int* d_drift_n = nullptr;             // drifters per member (the observation row is row n)
     long long drift_rows = 0;             // rows of all members' position arrays, packed
     float drift_sensitivity = 1.0f;
+    std::vector<char> has_drifters;       // per member
+    // unperturbed copies of the block's last state, for members with
+    // drifters (fused model error at the dataAssimilationStep cadence)
+    float* d_spare_pool = nullptr;
+    float** d_spare = nullptr;            // 3 per member (eta, hu, hv), null without drifters
+    // model error fused into the block's launches (goc_ensemble_set_block_noise)
+    int block_noise = -1;                 // NoiseMode, or -1: none
+    void* noise_batch = nullptr;
+    std::vector<int> nsub_host;           // steps per member of the current schedule
+    // members that take model error in the current block: their step count,
+    // 0 for members masked out (goc_ensemble_set_noise_mask); the batched
+    // noise kernels gate on this instead of the step count
+    std::vector<int> noise_mask;          // empty: every member
+    std::vector<int> nsub_noise_host;
+    int* d_nsub_noise = nullptr;
     int shape = 0;                        // index into kEnsembleShapes
 };
 
@@ -65,14 +90,19 @@ __device__ __forceinline__ DriftGrid member_drift_grid(const GocMemberDesc& d, i
                      d.Hm, d.Hm_pitch / 4, d.p.bc_north == 2, d.p.bc_east == 2};
 }
 
-// Advect one chunk of a member's drifters with the state of buffer set `set`.
+// Advect one chunk of a member's drifters with the state of buffer set `set`
+// (or, with `copy`, the unperturbed copy of that state: the drift of the
+// last step of a block whose model error was fused into that step).
 __device__ __forceinline__ void drift_chunk(const GocMemberDesc& d, float* pos, int first, int count, int set,
-                                           float dt, float sensitivity) {
+                                           float dt, float sensitivity, float* const* copy = nullptr) {
     const DriftGrid g = member_drift_grid(d, set);
     for (int q = threadIdx.x; q < count; q += blockDim.x) {
         float* p = pos + 2 * (size_t)(first + q);
         float px = p[0], py = p[1];
-        drift_one(g, nullptr, dt, sensitivity, px, py);
+        if (copy)
+            drift_one_with(g, CopyVelocity{g, copy[0], copy[1], copy[2]}, nullptr, dt, sensitivity, px, py);
+        else
+            drift_one(g, nullptr, dt, sensitivity, px, py);
         p[0] = px;
         p[1] = py;
     }
@@ -82,14 +112,26 @@ __device__ __forceinline__ void drift_chunk(const GocMemberDesc& d, float* pos, 
 // the persistent RK2 kernel
 // ---------------------------------------------------------------------------
 
-template <int TX, int TY, int MINB, bool CONST_F, bool SIMPLE_FORCING>
+// Which members a launch with fused model error perturbs.
+enum NoiseMode : int {
+    kNoiseLastStep = 0,   // members taking the last step of their block (dataAssimilationStep cadence)
+    kNoiseEveryStep = 1,  // every member taking a step (CDKLM16.step cadence)
+};
+
+// NOISE: the variant that adds the members' SOAR model error to Q^{n+1}
+// (noise: one descriptor per member, coarse fields already computed;
+// spare: per member three buffers (eta, hu, hv) for the unperturbed state,
+// or null entries / a null table; noise_steps: per member the step count of
+// the block if the member takes model error, else 0).
+template <int TX, int TY, int MINB, bool CONST_F, bool SIMPLE_FORCING, bool NOISE>
 __global__ void __launch_bounds__(kNT, MINB)
 ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __restrict__ tiles, int n_tiles,
                     const float* __restrict__ dt_table, const int* __restrict__ nsub, int max_sub, int k,
                     float* const* __restrict__ drift_pos, const int4* __restrict__ drift_chunks, int n_chunks,
                     float sensitivity, const CUtensorMap* __restrict__ tmaps,
                     const float* const* __restrict__ tma_base, int* tma_err,
-                    unsigned long long* tma_tiles) {
+                    unsigned long long* tma_tiles, const GocNoiseDesc* __restrict__ noise,
+                    float* const* __restrict__ spare, int noise_mode, const int* __restrict__ noise_steps) {
     extern __shared__ __align__(128) float smem_raw[];
     // TMA writes the staging planes on 128-byte boundaries: stage only if the
     // dynamic shared memory starts on one (the pointer itself stays the
@@ -97,6 +139,7 @@ ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __res
     const bool smem_aligned = (smem_u32(smem_raw) & 127u) == 0;
     __shared__ GocMemberDesc md;
     __shared__ StepConst kc;
+    __shared__ GocNoiseDesc nd;   // NOISE only
     __shared__ __align__(8) uint64_t tma_bar;
     __shared__ int tma_off;
     if (threadIdx.x == 0) {
@@ -107,6 +150,8 @@ ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __res
     TileTma tma{nullptr, &tma_bar, 0u, false, -1, &tma_off, tma_err};
     unsigned staged_tiles = 0;  // counted by thread 0
     int cur = -1;
+    TileNoise tn{&nd, nullptr, nullptr, nullptr};
+    bool perturb = false;   // the current member takes its model error in this launch
     // Work items: the RK2 tiles of step k, then (for k >= 1) the drifter
     // chunks of step k-1, which read the input state of step k (buffer set
     // k % 2) that no tile of this launch writes.
@@ -114,7 +159,12 @@ ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __res
     for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
         if (item >= n_tiles) {
             const int4 c = drift_chunks[item - n_tiles];
-            if (k - 1 >= __ldg(nsub + c.x)) continue;
+            const int ns = __ldg(nsub + c.x);
+            if (k - 1 >= ns) continue;
+            // a member whose last step (k - 1 = ns - 1) wrote an unperturbed
+            // copy of its state drifts with that copy, in a launch of its own
+            // (ensemble_end_drift_kernel) that keeps this kernel's code small
+            if (spare && k == ns && k == __ldg(noise_steps + c.x) && spare[3 * c.x]) continue;
             drift_chunk(members[c.x], drift_pos[c.x], c.y, c.z, k & 1,
                         __ldg(dt_table + (size_t)c.x * max_sub + (k - 1)), sensitivity);
             continue;
@@ -128,9 +178,20 @@ ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __res
             if (threadIdx.x == 0) {
                 md = members[m];
                 kc = make_step_const(md.p);
+                if constexpr (NOISE) {
+                    if (noise) nd = noise[m];
+                }
             }
             __syncthreads();
             cur = m;
+            if constexpr (NOISE) {
+                const int nn = __ldg(noise_steps + m);
+                perturb = noise != nullptr && (noise_mode == kNoiseEveryStep ? k < nn : k == nn - 1);
+                const bool keep = perturb && noise_mode == kNoiseLastStep && spare != nullptr;
+                tn.spare_e = keep ? spare[3 * m] : nullptr;
+                tn.spare_u = keep ? spare[3 * m + 1] : nullptr;
+                tn.spare_v = keep ? spare[3 * m + 2] : nullptr;
+            }
         }
         const int in = k & 1, out = in ^ 1;
         const float dt = __ldg(dt_table + (size_t)m * max_sub + k);
@@ -160,10 +221,10 @@ ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __res
             // every thread gets the same answer (it comes from a barrier
             // vote): a CTA whose staged input never landed stops here, with
             // the error flag set for the host
-            if (!cdklm_strip_tile<TX, TY, kNT, CONST_F, SIMPLE_FORCING>(
+            if (!cdklm_strip_tile<TX, TY, kNT, CONST_F, SIMPLE_FORCING, NOISE>(
                     md.p, kc, dt, t.y, ty, r > 0, md.eta[in], md.hu[in], md.hv[in], md.eta[out], md.hu[out],
                     md.hv[out], md.pitch / 4, md.Hi, md.Hi_pitch / 4, md.Hm, md.Hm_pitch / 4, smem_raw, side_in,
-                    side_out, &tma))
+                    side_out, &tma, perturb ? &tn : nullptr))
                 goto done;
             pending = tma.next_tile_y >= 0 && tma_off == 0;
             __syncthreads();
@@ -182,12 +243,12 @@ constexpr size_t ensemble_smem() {
 
 // Kernel attributes and the persistent grid are set up once per variant,
 // outside any stream capture (goc_ensemble_create calls this).
-template <int TX, int TY, bool CF, bool SF>
+template <int TX, int TY, bool CF, bool SF, bool NOISE>
 int configure_ensemble_kernel(int* grid_out) {
     constexpr size_t smem = ensemble_smem<TX, TY>();
     static int grid = 0;
     if (grid == 0) {
-        auto kern = ensemble_rk2_kernel<TX, TY, shape_min_blocks<TX, TY>(), CF, SF>;
+        auto kern = ensemble_rk2_kernel<TX, TY, shape_min_blocks<TX, TY>(), CF, SF, NOISE>;
         cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(err));
         int blocks = 0;
@@ -202,43 +263,72 @@ int configure_ensemble_kernel(int* grid_out) {
     return GOC_OK;
 }
 
-template <int TX, int TY, bool CF, bool SF>
-int launch_ensemble(Ensemble* e, int k, cudaStream_t st) {
+// Model error fused into one launch: the members' descriptors (device), the
+// spare-buffer table (or null) and the NoiseMode.
+struct FusedNoise {
+    const GocNoiseDesc* noise;
+    float* const* spare;
+    int mode;
+};
+
+template <int TX, int TY, bool CF, bool SF, bool NOISE>
+int launch_ensemble(Ensemble* e, int k, cudaStream_t st, const FusedNoise* fn) {
     constexpr size_t smem = ensemble_smem<TX, TY>();
-    auto kern = ensemble_rk2_kernel<TX, TY, shape_min_blocks<TX, TY>(), CF, SF>;
+    auto kern = ensemble_rk2_kernel<TX, TY, shape_min_blocks<TX, TY>(), CF, SF, NOISE>;
     int full = 0;
-    int rc = configure_ensemble_kernel<TX, TY, CF, SF>(&full);
+    int rc = configure_ensemble_kernel<TX, TY, CF, SF, NOISE>(&full);
     if (rc) return rc;
-    const int items = e->n_runs + (k >= 1 ? e->n_drift_chunks : 0);
+    const int items = e->n_runs + (k >= 1 ? e->n_step_chunks : 0);
     const int grid = std::min(items, full);
     kern<<<grid, kNT, smem, st>>>(e->d_members, e->d_tiles, e->n_runs, e->d_dt, e->d_nsub, e->max_substeps, k,
-                                  e->d_drift_pos, e->d_drift_chunks, e->n_drift_chunks, e->drift_sensitivity,
+                                  e->d_drift_pos, e->d_step_chunks, e->n_step_chunks, e->drift_sensitivity,
                                   e->d_tmaps + (size_t)e->shape * e->n_members * 6, e->d_tma_base, e->d_tma_err,
-                                  e->d_tma_tiles);
+                                  e->d_tma_tiles, fn ? fn->noise : nullptr, fn ? fn->spare : nullptr,
+                                  fn ? fn->mode : 0, e->d_nsub_noise);
     count_launch();
-    return check_launch("ensemble_rk2_kernel");
+    return check_launch(NOISE ? "ensemble_rk2_kernel (model error)" : "ensemble_rk2_kernel");
 }
 
 // Launchers of one tile shape (explicitly instantiated per shape).
 template <int TX, int TY>
 int ensemble_configure_shape(const Ensemble* e, int* grid) {
-    if (e->const_f && e->simple) return configure_ensemble_kernel<TX, TY, true, true>(grid);
-    if (e->const_f) return configure_ensemble_kernel<TX, TY, true, false>(grid);
-    if (e->simple) return configure_ensemble_kernel<TX, TY, false, true>(grid);
-    return configure_ensemble_kernel<TX, TY, false, false>(grid);
+    int g2 = 0, rc;
+    if (e->const_f && e->simple) {
+        rc = configure_ensemble_kernel<TX, TY, true, true, false>(grid);
+        return rc ? rc : configure_ensemble_kernel<TX, TY, true, true, true>(&g2);
+    }
+    if (e->const_f) {
+        rc = configure_ensemble_kernel<TX, TY, true, false, false>(grid);
+        return rc ? rc : configure_ensemble_kernel<TX, TY, true, false, true>(&g2);
+    }
+    if (e->simple) {
+        rc = configure_ensemble_kernel<TX, TY, false, true, false>(grid);
+        return rc ? rc : configure_ensemble_kernel<TX, TY, false, true, true>(&g2);
+    }
+    rc = configure_ensemble_kernel<TX, TY, false, false, false>(grid);
+    return rc ? rc : configure_ensemble_kernel<TX, TY, false, false, true>(&g2);
 }
 
+// fn: the model error of this launch (null: none); fn->noise null means no
+// member perturbs here but fn->spare still tells the drifter work which
+// members drift with an unperturbed copy (the plain variant runs then).
 template <int TX, int TY>
-int ensemble_launch_shape(Ensemble* e, int k, cudaStream_t st) {
-    if (e->const_f && e->simple) return launch_ensemble<TX, TY, true, true>(e, k, st);
-    if (e->const_f) return launch_ensemble<TX, TY, true, false>(e, k, st);
-    if (e->simple) return launch_ensemble<TX, TY, false, true>(e, k, st);
-    return launch_ensemble<TX, TY, false, false>(e, k, st);
+int ensemble_launch_shape(Ensemble* e, int k, cudaStream_t st, const FusedNoise* fn) {
+    if (fn && fn->noise) {
+        if (e->const_f && e->simple) return launch_ensemble<TX, TY, true, true, true>(e, k, st, fn);
+        if (e->const_f) return launch_ensemble<TX, TY, true, false, true>(e, k, st, fn);
+        if (e->simple) return launch_ensemble<TX, TY, false, true, true>(e, k, st, fn);
+        return launch_ensemble<TX, TY, false, false, true>(e, k, st, fn);
+    }
+    if (e->const_f && e->simple) return launch_ensemble<TX, TY, true, true, false>(e, k, st, fn);
+    if (e->const_f) return launch_ensemble<TX, TY, true, false, false>(e, k, st, fn);
+    if (e->simple) return launch_ensemble<TX, TY, false, true, false>(e, k, st, fn);
+    return launch_ensemble<TX, TY, false, false, false>(e, k, st, fn);
 }
 
 #define GOC_ENSEMBLE_SHAPE_EXTERN(TX, TY)                                           \
     extern template int ensemble_configure_shape<TX, TY>(const Ensemble*, int*);     \
-    extern template int ensemble_launch_shape<TX, TY>(Ensemble*, int, cudaStream_t);
+    extern template int ensemble_launch_shape<TX, TY>(Ensemble*, int, cudaStream_t, const FusedNoise*);
 GOC_ENSEMBLE_SHAPE_EXTERN(32, 16)
 GOC_ENSEMBLE_SHAPE_EXTERN(32, 8)
 GOC_ENSEMBLE_SHAPE_EXTERN(16, 16)

@@ -3,5 +3,5 @@
 
 namespace goc {
 template int ensemble_configure_shape<64, 8>(const Ensemble*, int*);
-template int ensemble_launch_shape<64, 8>(Ensemble*, int, cudaStream_t);
+template int ensemble_launch_shape<64, 8>(Ensemble*, int, cudaStream_t, const FusedNoise*);
 }  // namespace goc

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "noise_transfer.cuh"
 
 namespace goc {
 
@@ -100,255 +101,11 @@ __global__ void soar_kernel(GocNoiseDesc d, float scale, int additive) {
 }
 
 // ---------------------------------------------------------------------------
-// transfer to the ocean state
+// batched: the SOAR fields of all members in one launch (the transfer to the
+// state is in noise_transfer.cu, or fused into the ensemble step)
 // ---------------------------------------------------------------------------
-
-struct OceanRef {
-    int nx, ny;
-    float dx, dy;
-    float* eta; float* hu; float* hv; int pitch;    // floats
-    const float* Hi; int hi_pitch;                  // floats
-    float land;
-    int images_ns, images_ew;                       // write periodic ghost images
-};
-
-__device__ __forceinline__ OceanRef ocean_of(const GocMemberDesc& m, int images) {
-    return OceanRef{m.p.nx, m.p.ny, m.p.dx, m.p.dy, m.eta[0], m.hu[0], m.hv[0], m.pitch / 4, m.Hi, m.Hi_pitch / 4,
-                    m.p.land_value, images && m.p.bc_north == 2, images && m.p.bc_east == 2};
-}
-
-// Write a perturbed interior cell and, for periodic boundaries, its ghost
-// images (the boundary fill the reference runs after perturbState,
-// S/CDKLM16.py:571-572).
-__device__ __forceinline__ void store_cell(const OceanRef& o, int ti, int tj, float e, float u, float v) {
-    int xs[2] = {ti, -1}, ys[2] = {tj, -1};
-    if (o.images_ew) xs[1] = (ti < 4) ? ti + o.nx : (ti >= o.nx ? ti - o.nx : -1);
-    if (o.images_ns) ys[1] = (tj < 4) ? tj + o.ny : (tj >= o.ny ? tj - o.ny : -1);
-    for (int a = 0; a < 2; ++a) {
-        if (ys[a] < 0) continue;
-        for (int b = 0; b < 2; ++b) {
-            if (xs[b] < 0) continue;
-            const size_t k = (size_t)ys[a] * o.pitch + xs[b];
-            o.eta[k] = e; o.hu[k] = u; o.hv[k] = v;
-        }
-    }
-}
-
-template <class D>
-__device__ __forceinline__ float noise_coriolis(const D& d, const OceanRef& o, int ti, int tj) {
-    float c = d.f + d.beta * ((ti + 0.5f) * o.dx * d.north_x + (tj + 0.5f) * o.dy * d.north_y);
-    if (d.f == 0.0f && d.coriolis_f) {
-        const float s = (ti + 0.5f) / (o.nx + 4.0f), t = (tj + 0.5f) / (o.ny + 4.0f);
-        c = tex_bilinear(d.coriolis_f, d.coriolis_nx, d.coriolis_ny, s, t);
-    }
-    return c;
-}
-
-__device__ __forceinline__ float coarse_at(const GocNoiseDesc& d, int j, int i) {
-    j = clampi(j, 0, d.coarse_ny + 3);
-    i = clampi(i, 0, d.coarse_nx + 3);
-    return d.coarse[(size_t)j * (d.coarse_pitch / 4) + i];
-}
-
-// Bicubic up-sampling of the coarse field (K/ocean_noise.cu:497-586), split in
-// three parts so that a tile computes the coefficient matrix of each coarse
-// cell once and evaluates it at every fine cell inside: the coarse cell (ci, cj)
-// of fine cell (ti, tj) with the fractional position (rx, ry) in it, the 4x4
-// coefficients A of coarse cell (ci, cj), and the polynomial.
-__device__ __forceinline__ int bicubic_ci(const GocNoiseDesc& d, const OceanRef& o, int ti, float* rx) {
-    const float x = (ti - 2 + 0.5f + d.offset_i) * o.dx;
-    int ci = (int)floorf(x / d.coarse_dx + 2 - 0.5f);
-    if (ci > d.coarse_nx + 1) ci -= 1;
-    *rx = (x - (ci - 2 + 0.5f) * d.coarse_dx) / d.coarse_dx;
-    return ci;
-}
-
-__device__ __forceinline__ int bicubic_cj(const GocNoiseDesc& d, const OceanRef& o, int tj, float* ry) {
-    const float y = (tj - 2 + 0.5f + d.offset_j) * o.dy;
-    int cj = (int)floorf(y / d.coarse_dy + 2 - 0.5f);
-    if (cj > d.coarse_ny + 1) cj -= 1;
-    *ry = (y - (cj - 2 + 0.5f) * d.coarse_dy) / d.coarse_dy;
-    return cj;
-}
-
-__device__ __forceinline__ void bicubic_coeffs(const GocNoiseDesc& d, int ci, int cj, float* A /* [16], row-major */) {
-    float c[4][4];  // c[row][col] = coarse[cj-1+row][ci-1+col]
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) c[r][q] = coarse_at(d, cj - 1 + r, ci - 1 + q);
-    // values, x/y derivatives and cross derivatives at the 4 corners
-    float F[4][4];
-    F[0][0] = c[1][1]; F[0][1] = c[2][1]; F[1][0] = c[1][2]; F[1][1] = c[2][2];
-    F[2][0] = (c[1][2] - c[1][0]) / 2.0f; F[2][1] = (c[2][2] - c[2][0]) / 2.0f;
-    F[3][0] = (c[1][3] - c[1][1]) / 2.0f; F[3][1] = (c[2][3] - c[2][1]) / 2.0f;
-    F[0][2] = (c[2][1] - c[0][1]) / 2.0f; F[0][3] = (c[3][1] - c[1][1]) / 2.0f;
-    F[1][2] = (c[2][2] - c[0][2]) / 2.0f; F[1][3] = (c[3][2] - c[1][2]) / 2.0f;
-    const float fy_10 = (c[2][0] - c[0][0]) / 2.0f, fy_11 = (c[3][0] - c[1][0]) / 2.0f;
-    const float fy20 = (c[2][3] - c[0][3]) / 2.0f, fy21 = (c[3][3] - c[1][3]) / 2.0f;
-    F[2][2] = (F[1][2] - fy_10) / 2.0f; F[2][3] = (F[1][3] - fy_11) / 2.0f;
-    F[3][2] = (fy20 - F[0][2]) / 2.0f; F[3][3] = (fy21 - F[0][3]) / 2.0f;
-    const float B[4][4] = {{1, 0, 0, 0}, {0, 0, 1, 0}, {-3, 3, -2, -1}, {2, -2, 1, 1}};
-    float FB[4][4];   // FB = F B^T, A = B FB
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            FB[r][q] = F[r][0] * B[q][0] + F[r][1] * B[q][1] + F[r][2] * B[q][2] + F[r][3] * B[q][3];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            A[4 * r + q] = B[r][0] * FB[0][q] + B[r][1] * FB[1][q] + B[r][2] * FB[2][q] + B[r][3] * FB[3][q];
-}
-
-__device__ __forceinline__ float bicubic_eval(const float* A, float rx, float ry) {
-    const float xv[4] = {1.0f, rx, rx * rx, rx * rx * rx};
-    const float yv[4] = {1.0f, ry, ry * ry, ry * ry * ry};
-    float v = 0.0f;
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-        v += xv[r] * (A[4 * r] * yv[0] + A[4 * r + 1] * yv[1] + A[4 * r + 2] * yv[2] + A[4 * r + 3] * yv[3]);
-    return v;
-}
-
-// Bicubic value of the coarse field at fine cell (ti, tj).
-__device__ float bicubic_value(const GocNoiseDesc& d, const OceanRef& o, int ti, int tj) {
-    float rx, ry, A[16];
-    const int ci = bicubic_ci(d, o, ti, &rx), cj = bicubic_cj(d, o, tj, &ry);
-    bicubic_coeffs(d, ci, cj, A);
-    return bicubic_eval(A, rx, ry);
-}
-
-// Perturbation of interior cell (ti, tj) from its state (e, u, v) and corner
-// depths hc = (Hi[tj][ti], Hi[tj][ti+1], Hi[tj+1][ti], Hi[tj+1][ti+1]).
-// `factor1`: the coarse grid is the computational grid (geostrophicBalance,
-// the state's own depth in h and land cells zeroed); otherwise bicubic
-// up-sampling (bicubicInterpolation, land cells unperturbed).  `de(jj, ii)`
-// gives the perturbation of eta.
-template <typename DE>
-__device__ __forceinline__ void perturb_cell(const GocNoiseDesc& d, const OceanRef& o, int ti, int tj, bool factor1,
-                                             DE de, float e, float u, float v, const float* hc) {
-    const bool dry = (hc[0] == o.land) || (hc[1] == o.land) || (hc[2] == o.land) || (hc[3] == o.land);
-    const float H_mid = 0.25f * (hc[0] + hc[1] + hc[2] + hc[3]);
-    const float cor = noise_coriolis(d, o, ti, tj);
-    const float dc = de(tj, ti);
-    const float ex = (de(tj, ti + 1) - de(tj, ti - 1)) / (2.0f * o.dx);
-    const float ey = (de(tj + 1, ti) - de(tj - 1, ti)) / (2.0f * o.dy);
-    if (factor1) {
-        const float h_mid = dc + H_mid + e;
-        const float dhu = -(d.g / cor) * h_mid * ey;
-        const float dhv = (d.g / cor) * h_mid * ex;
-        if (dry) {
-            e = 0.0f; u = 0.0f; v = 0.0f;
-        } else {
-            e += dc; u += dhu; v += dhv;
-        }
-    } else if (!dry) {
-        e += dc;
-        u += -(d.g / cor) * (H_mid + dc) * ey;
-        v += (d.g / cor) * (H_mid + dc) * ex;
-    }
-    store_cell(o, ti, tj, e, u, v);
-}
 
 constexpr int kNB = 16;                            // SOAR tile edge (coarse cells)
-constexpr int kPX = 32, kPY = 32, kPT = 8;          // transfer tile (fine cells) and thread rows
-constexpr int kPR = kPY / kPT;                      // cells per thread
-constexpr int kNC = 12;  // coarse cells per tile edge held in shared memory (factor >= 4 for 34 fine cells)
-
-// One kPX x kPY tile of interior cells (tile origin bx, by in interior
-// cells).  Each thread owns kPR cells of one column; their state is loaded
-// first so that the loads overlap the perturbation field (the corner depths,
-// shared by the members and L2-resident, are read when used).
-__device__ void perturb_tile(const GocNoiseDesc& d, const OceanRef& o, int bx, int by) {
-    __shared__ float s_de[kPY + 2][kPX + 2];
-    __shared__ float s_A[kNC * kNC][17];
-    // coarse column / row of every fine column / row of the tile + 1 ring and
-    // the fractional position in it (the bicubic index is separable)
-    __shared__ int s_ci[kPX + 2], s_cj[kPY + 2];
-    __shared__ float s_rx[kPX + 2], s_ry[kPY + 2];
-    const int tx = threadIdx.x, t = threadIdx.y * kPX + tx;
-    constexpr int NT = kPX * kPT;
-    const bool factor1 = d.interpolation_factor <= 1;
-    const int ti = 2 + bx + tx;
-    float q[kPR][3];
-#pragma unroll
-    for (int r = 0; r < kPR; ++r) {
-        const int tj = 2 + by + threadIdx.y + r * kPT;
-        q[r][0] = q[r][1] = q[r][2] = 0.0f;
-        if (ti < o.nx + 2 && tj < o.ny + 2) {
-            const size_t k = (size_t)tj * o.pitch + ti;
-            q[r][0] = o.eta[k];
-            q[r][1] = o.hu[k];
-            q[r][2] = o.hv[k];
-        }
-    }
-    // d_eta on the tile + 1 ring (interior origin at ghost offset 2)
-    const int gi0 = 2 + bx - 1, gj0 = 2 + by - 1;
-    constexpr int NR = (kPY + 2) * (kPX + 2);
-    if (factor1) {
-        for (int c = t; c < NR; c += NT) s_de[c / (kPX + 2)][c % (kPX + 2)] = coarse_at(d, gj0 + c / (kPX + 2),
-                                                                                          gi0 + c % (kPX + 2));
-    } else {
-        // the coarse cells under the tile: the index is monotone in the fine index
-        float r;
-        const int ci0 = bicubic_ci(d, o, gi0, &r), ci1 = bicubic_ci(d, o, gi0 + kPX + 1, &r);
-        const int cj0 = bicubic_cj(d, o, gj0, &r), cj1 = bicubic_cj(d, o, gj0 + kPY + 1, &r);
-        const int ncx = ci1 - ci0 + 1, ncy = cj1 - cj0 + 1;
-        if (ncx <= kNC && ncy <= kNC) {
-            for (int c = t; c < ncx * ncy; c += NT) bicubic_coeffs(d, ci0 + c % ncx, cj0 + c / ncx, s_A[c]);
-            if (t < kPX + 2) {
-                s_ci[t] = clampi(bicubic_ci(d, o, gi0 + t, &s_rx[t]) - ci0, 0, ncx - 1);
-            } else if (t >= 64 && t < 64 + kPY + 2) {
-                const int j = t - 64;
-                s_cj[j] = clampi(bicubic_cj(d, o, gj0 + j, &s_ry[j]) - cj0, 0, ncy - 1);
-            }
-            __syncthreads();
-            for (int c = t; c < NR; c += NT) {
-                const int j = c / (kPX + 2), i = c % (kPX + 2);
-                s_de[j][i] = bicubic_eval(s_A[s_cj[j] * ncx + s_ci[i]], s_rx[i], s_ry[j]);
-            }
-        } else {
-            for (int c = t; c < NR; c += NT)
-                s_de[c / (kPX + 2)][c % (kPX + 2)] = bicubic_value(d, o, gi0 + c % (kPX + 2), gj0 + c / (kPX + 2));
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < kPR; ++r) {
-        const int tj = 2 + by + threadIdx.y + r * kPT;
-        if (ti < o.nx + 2 && tj < o.ny + 2) {
-            const float* h0 = o.Hi + (size_t)tj * o.hi_pitch + ti;
-            const float hc[4] = {__ldg(h0), __ldg(h0 + 1), __ldg(h0 + o.hi_pitch), __ldg(h0 + o.hi_pitch + 1)};
-            perturb_cell(d, o, ti, tj, factor1,
-                         [&](int jj, int ii) { return s_de[jj - (2 + by) + 1][ii - (2 + bx) + 1]; },
-                         q[r][0], q[r][1], q[r][2], hc);
-        }
-    }
-    __syncthreads();
-}
-
-__global__ void __launch_bounds__(kPX * kPT, 3) perturb_kernel(GocNoiseDesc d, OceanRef o) {
-    perturb_tile(d, o, blockIdx.x * kPX, blockIdx.y * kPY);
-}
-
-// ---------------------------------------------------------------------------
-// batched: all members of an ensemble in two launches
-// ---------------------------------------------------------------------------
-
-// substep < 0: between blocks, the state of member m is buffer set 0 of the
-// ensemble's device member table.  substep = k: right after RK2 step k of a
-// block, members that took step k hold their state in set (k + 1) % 2.
-__device__ __forceinline__ bool member_set(const int* nsub, int m, int substep, int* set) {
-    if (substep < 0) {
-        *set = 0;
-        return true;
-    }
-    if (substep >= nsub[m]) return false;
-    *set = (substep + 1) & 1;
-    return true;
-}
 
 __global__ void soar_batched_active_kernel(const GocNoiseDesc* __restrict__ nd, const int4* __restrict__ items,
                                            const int* __restrict__ nsub, int substep, float scale) {
@@ -357,17 +114,6 @@ __global__ void soar_batched_active_kernel(const GocNoiseDesc* __restrict__ nd, 
     if (!member_set(nsub, it.x, substep, &set)) return;
     const GocNoiseDesc& d = nd[it.x];
     soar_cell(d, scale, 0, it.y * kNB + threadIdx.x, it.z * kNB + threadIdx.y, d.random, d.coarse);
-}
-
-__global__ void __launch_bounds__(kPX * kPT, 3) perturb_batched_kernel(const GocNoiseDesc* __restrict__ nd, const GocMemberDesc* __restrict__ mem,
-                                       const int4* __restrict__ items, const int* __restrict__ nsub, int substep) {
-    const int4 it = items[blockIdx.x];
-    int set;
-    if (!member_set(nsub, it.x, substep, &set)) return;
-    const GocMemberDesc& m = mem[it.x];
-    const OceanRef o{m.p.nx, m.p.ny, m.p.dx, m.p.dy, m.eta[set], m.hu[set], m.hv[set], m.pitch / 4, m.Hi,
-                     m.Hi_pitch / 4, m.p.land_value, m.p.bc_north == 2, m.p.bc_east == 2};
-    perturb_tile(nd[it.x], o, it.y * kPX, it.z * kPY);
 }
 
 // XORWOW normals for every member's random field; one state per element.
@@ -660,33 +406,6 @@ extern "C" int goc_soar(const GocNoiseDesc* d, float perturbation_scale, int add
     return check_launch("soar_kernel");
 }
 
-static int make_ocean(int nx, int ny, float dx, float dy, float* eta, float* hu, float* hv, int pitch,
-                      const float* Hi, int Hi_pitch, float land, int images_ns, int images_ew, OceanRef* o,
-                      const char* who) {
-    if (nx < 1 || ny < 1 || !eta || !hu || !hv || !Hi) return set_error(GOC_ERR_ARG, "%s: bad ocean arguments", who);
-    if (pitch < (nx + 4) * 4 || Hi_pitch < (nx + 5) * 4 || pitch % 4 || Hi_pitch % 4)
-        return set_error(GOC_ERR_ARG, "%s: pitch too small", who);
-    if ((images_ns && ny < 4) || (images_ew && nx < 4))
-        return set_error(GOC_ERR_ARG, "%s: periodic directions need at least 4 cells", who);
-    *o = OceanRef{nx, ny, dx, dy, eta, hu, hv, pitch / 4, Hi, Hi_pitch / 4, land, images_ns, images_ew};
-    return GOC_OK;
-}
-
-extern "C" int goc_perturb_ocean(const GocNoiseDesc* d, int nx, int ny, float dx, float dy, float* eta, float* hu,
-                                 float* hv, int pitch, const float* Hi, int Hi_pitch, float land_value,
-                                 int periodic_ghosts, void* stream) {
-    int rc = check_noise(d, "goc_perturb_ocean");
-    if (rc) return rc;
-    OceanRef o;
-    if ((rc = make_ocean(nx, ny, dx, dy, eta, hu, hv, pitch, Hi, Hi_pitch, land_value,
-                         periodic_ghosts && d->periodic_ns, periodic_ghosts && d->periodic_ew, &o, "goc_perturb_ocean")))
-        return rc;
-    dim3 blk(kPX, kPT), grd((nx + kPX - 1) / kPX, (ny + kPY - 1) / kPY);
-    perturb_kernel<<<grd, blk, 0, as_stream(stream)>>>(*d, o);
-    count_launch();
-    return check_launch("perturb_kernel");
-}
-
 // ---------------------------------------------------------------------------
 // batched handle
 // ---------------------------------------------------------------------------
@@ -753,6 +472,14 @@ extern "C" int goc_noise_batch_create(void* ensemble, const GocNoiseDesc* noise,
     return GOC_OK;
 }
 
+namespace goc {
+const GocNoiseDesc* noise_batch_device_desc(void* batch, int* n_members) {
+    NoiseBatch* b = static_cast<NoiseBatch*>(batch);
+    if (n_members) *n_members = b->n;
+    return b->d_noise;
+}
+}  // namespace goc
+
 extern "C" int goc_noise_batch_destroy(void* batch) {
     if (!batch) return GOC_OK;
     NoiseBatch* b = static_cast<NoiseBatch*>(batch);
@@ -782,9 +509,22 @@ extern "C" int goc_noise_batch_generate(void* batch, void* ensemble, int substep
     NoiseBatch* b = static_cast<NoiseBatch*>(batch);
     if (!b->d_states) return set_error(GOC_ERR_ARG, "goc_noise_batch_generate: call goc_noise_batch_seed first");
     xorwow_batched_kernel<<<b->n_rng, 256, 0, as_stream(stream)>>>(b->d_noise, b->d_rng_chunks, b->d_states,
-                                                                 ensemble_device_nsub(ensemble), substep);
+                                                                 ensemble_device_noise_steps(ensemble), substep);
     count_launch();
     return check_launch("xorwow_batched_kernel");
+}
+
+extern "C" int goc_noise_batch_field(void* batch, void* ensemble, float perturbation_scale, int substep,
+                                     void* stream) {
+    if (!batch || !ensemble) return set_error(GOC_ERR_ARG, "goc_noise_batch_field: null handle");
+    NoiseBatch* b = static_cast<NoiseBatch*>(batch);
+    int n = 0;
+    ensemble_host_members(ensemble, &n);
+    if (n != b->n) return set_error(GOC_ERR_ARG, "goc_noise_batch_field: ensemble has %d members, batch %d", n, b->n);
+    soar_batched_active_kernel<<<b->n_soar, dim3(kNB, kNB), 0, as_stream(stream)>>>(
+        b->d_noise, b->d_soar_items, ensemble_device_noise_steps(ensemble), substep, perturbation_scale);
+    count_launch();
+    return check_launch("soar_batched_active_kernel");
 }
 
 extern "C" int goc_noise_batch_perturb(void* batch, void* ensemble, float perturbation_scale, int substep,
@@ -795,16 +535,14 @@ extern "C" int goc_noise_batch_perturb(void* batch, void* ensemble, float pertur
     ensemble_host_members(ensemble, &n);
     if (n != b->n) return set_error(GOC_ERR_ARG, "goc_noise_batch_perturb: ensemble has %d members, batch %d", n, b->n);
     cudaStream_t st = as_stream(stream);
-    const int* nsub = ensemble_device_nsub(ensemble);
+    const int* nsub = ensemble_device_noise_steps(ensemble);
     soar_batched_active_kernel<<<b->n_soar, dim3(kNB, kNB), 0, st>>>(b->d_noise, b->d_soar_items, nsub, substep,
                                                                      perturbation_scale);
     count_launch();
     int rc = check_launch("soar_batched_active_kernel");
     if (rc) return rc;
-    perturb_batched_kernel<<<b->n_pert, dim3(kPX, kPT), 0, st>>>(b->d_noise, ensemble_device_members(ensemble),
-                                                                  b->d_pert_items, nsub, substep);
-    count_launch();
-    return check_launch("perturb_batched_kernel");
+    return launch_perturb_batched(b->d_noise, ensemble_device_members(ensemble), b->d_pert_items, b->n_pert, nsub,
+                                  substep, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -986,7 +724,7 @@ extern "C" int goc_kl_batch_generate(void* batch, void* ensemble, int substep, v
     if (substep + 1 < 0 || substep + 1 >= b->max_sets)
         return set_error(GOC_ERR_ARG, "goc_kl_batch_generate: substep %d outside the roller sets", substep);
     cudaStream_t st = as_stream(stream);
-    const int* nsub = ensemble_device_nsub(ensemble);
+    const int* nsub = ensemble_device_noise_steps(ensemble);
     if (b->n_rng > 0) {
         kl_xorwow_batched_kernel<<<b->n_rng, 256, 0, st>>>(b->d_kl, b->d_rng_chunks, b->d_states, nsub, substep);
         count_launch();
@@ -1029,7 +767,7 @@ extern "C" int goc_kl_batch_perturb(void* batch, void* ensemble, float perturbat
     if (substep + 1 < 0 || substep + 1 >= b->max_sets)
         return set_error(GOC_ERR_ARG, "goc_kl_batch_perturb: substep %d outside the roller sets", substep);
     cudaStream_t st = as_stream(stream);
-    const int* nsub = ensemble_device_nsub(ensemble);
+    const int* nsub = ensemble_device_noise_steps(ensemble);
     const GocMemberDesc* dm = ensemble_device_members(ensemble);
     kl_table_batched_kernel<<<b->n_tab, 128, 0, st>>>(b->d_kl, b->d_src, b->d_rollers, b->n, substep + 1, dm,
                                                       b->d_tab_items, nsub, substep);

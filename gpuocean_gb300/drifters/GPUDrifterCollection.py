@@ -26,6 +26,12 @@ class GPUDrifterCollection(BaseDrifterCollection):
         self.block_height = 1
         self.wind = wind if wind is not None else WindStress.WindStress()
         self.wind_drift_factor = np.float32(wind_drift_factor)
+        # the drift kernel reads both wind components with the x texture's
+        # size (as the reference's does, K/driftKernels.cu:155-156): textures
+        # of different sizes would be read out of bounds
+        if self.wind_drift_factor and any(np.shape(u) != np.shape(v)
+                                          for u, v in zip(self.wind.wind_u, self.wind.wind_v)):
+            raise ValueError("wind drift needs wind_u and wind_v textures of the same shape")
         self.gpu_stream = gpu_stream if gpu_stream is not None else Common.Stream()
         self.sensitivity = 1.0
         self.driftersHost = np.zeros((self.getNumDrifters() + 1, 2), dtype=np.float32)

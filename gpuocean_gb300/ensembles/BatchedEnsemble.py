@@ -147,6 +147,7 @@ class BatchedEnsemble:
         self._ptrs = self._current_ptrs()
         self._graphs = {}
         self._sched_key = None
+        self._mask_key = None
         self._dt_dev = Common.DevicePtr(4 * len(self.sims))
         self._attach_drifters()
         self._collect_streams()
@@ -215,23 +216,60 @@ class BatchedEnsemble:
 
     def _attach_drifters(self):
         """Drifter collections attached to the members are advected inside
-        the batched step (wind drift is not applied there)."""
+        the batched step; those with wind drift in launches of their own,
+        with the collection's wind textures."""
         ptrs = (ctypes.c_void_p * len(self.sims))()
         counts = np.zeros(len(self.sims), dtype=np.int32)
+        winds = (_lib.GocDriftWindDesc * len(self.sims))()
         sens = 1.0
         self.has_drifters = False
+        self._wind_members = []
         for m, s in enumerate(self.sims):
             d = s.drifters if s.hasDrifters else None
             if d is not None and hasattr(d, "driftersDevice"):
-                if d.wind_drift_factor:
-                    raise NotImplementedError("wind drift of drifters is not applied by the batched engine")
                 ptrs[m] = d.driftersDevice.ptr
                 counts[m] = d.getNumDrifters()
                 sens = d.sensitivity
                 self.has_drifters = True
+                if d.wind_drift_factor:
+                    w = winds[m]
+                    w.x_current, w.x_next = d.wind_x_current_arr.ptr, d.wind_x_next_arr.ptr
+                    w.y_current, w.y_next = d.wind_y_current_arr.ptr, d.wind_y_next_arr.ptr
+                    w.nx, w.ny = int(d.wind_x_current_arr.nx_halo), int(d.wind_x_current_arr.ny_halo)
+                    w.wind_drift_factor = float(d.wind_drift_factor)
+                    self._wind_members.append(m)
         if self.has_drifters:
             _lib.call("goc_ensemble_set_drifters", self._handle, ptrs, counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
                       ctypes.c_float(sens), self.stream.handle)
+        if self._wind_members:
+            _lib.call("goc_ensemble_set_drift_wind", self._handle, winds, self.stream.handle)
+
+    def _wind_times(self, scheds):
+        """Time weights of the wind textures for every drift of the block
+        (the drift after step k reads the wind at the member's time before
+        step k's increment, D/GPUDrifterCollection.py:138-174), after
+        bringing each collection's current/next textures to the block's wind
+        interval.  A block may not cross a wind time stamp."""
+        table = np.zeros((len(self.sims), self.max_substeps), dtype=np.float32)
+        for m in self._wind_members:
+            s = self.sims[m]
+            d = s.drifters
+            tw = np.asarray(d.wind.t, dtype=np.float64)
+            t = float(s.t)
+            times = []
+            for local_dt in scheds[m]:
+                times.append(t)
+                t += float(np.float64(local_dt))
+            if not times:
+                continue
+            last = len(tw) - 1
+            spans = {(max(0, int(np.searchsorted(tw, x)) - 1), min(last, int(np.searchsorted(tw, x)))) for x in times}
+            if len(spans) > 1:
+                raise NotImplementedError("a batched block crosses a wind time stamp of member %d's drifters: "
+                                          "step to the time stamp first" % m)
+            for k, x in enumerate(times):
+                table[m, k] = np.float32(d.update_wind(x))
+        _lib.call("goc_ensemble_set_wind_times", self._handle, table.ctypes.data, self.stream.handle)
 
     def release(self):
         """Free the device handles and give the members their own streams back."""
@@ -357,8 +395,11 @@ class BatchedEnsemble:
         return self.tile_shape
 
     # ------------------------------------------------------------------
-    def _schedule(self, t_end):
-        scheds = [step_schedule(s.dt, t_end) for s in self.sims]
+    def _schedule(self, t_end, members=None):
+        """Per member the dt sequence of step(t_end); members not in
+        `members` (if given) take no step."""
+        chosen = set(range(len(self.sims))) if members is None else {int(m) for m in members}
+        scheds = [step_schedule(s.dt, t_end) if m in chosen else [] for m, s in enumerate(self.sims)]
         nsub = max(len(x) for x in scheds)
         if nsub > self.max_substeps or self._current_ptrs() != self._ptrs:
             # members stepped on their own, or a longer block: rebuild the table
@@ -434,6 +475,10 @@ class BatchedEnsemble:
             _lib.call("goc_noise_batch_create", self._handle, descs, ctypes.byref(h))
             self._noise, self._noise_kind = h.value, "soar"
             self._noise_descs = descs
+            # the unperturbed copies that fused model error at the block
+            # cadence needs are allocated here, outside any graph capture
+            _lib.call("goc_ensemble_set_block_noise", self._handle, self._noise, 0)
+            _lib.call("goc_ensemble_set_block_noise", self._handle, None, -1)
             if rng_seed is not None:
                 _lib.call("goc_noise_batch_seed", self._noise, ctypes.c_ulonglong(int(rng_seed)), self.stream.handle)
         self._noises = noises
@@ -500,56 +545,102 @@ class BatchedEnsemble:
         self._before_members()
         self.kernels_launched += _lib.load().goc_kernel_launch_count() - before
 
-    def _launch_block(self, nsub, noise=None):
+    def _noise_field(self, substep):
+        """New normals (device generator) and the SOAR coarse fields of the
+        members that perturb at `substep` (-1: all), ahead of the fused
+        step that adds them."""
+        if self._rng_seed is not None:
+            _lib.call("goc_noise_batch_generate", self._noise, self._handle, int(substep), self.stream.handle)
+        _lib.call("goc_noise_batch_field", self._noise, self._handle, ctypes.c_float(1.0), int(substep),
+                  self.stream.handle)
+
+    def _launch_block(self, nsub, noise=None, n=None):
         """noise: None, "block" (once after the block) or "step" (after every
-        RK2 step of each member, before its drifters move)."""
+        RK2 step of each member, before its drifters move).  SOAR model error
+        is fused into the step launches: the coarse fields are computed
+        before the first step that perturbs, and each member's perturbation
+        is added to the state the step writes.  KL model error runs as its
+        own launches after the steps.  n: the members' step counts."""
         before = _lib.load().goc_kernel_launch_count()
-        for k in range(nsub):
-            _lib.call("goc_ensemble_rk2_substep", self._handle, k, self.stream.handle)
-            if noise == "step":
-                self._noise_launch(k)
-        _lib.call("goc_ensemble_end_block", self._handle, int(nsub), self.stream.handle)
-        if noise == "block":
-            self._noise_launch(-1)
+        fused = noise is not None and self._noise_kind == "soar"
+        first = -1
+        if fused:
+            _lib.call("goc_ensemble_set_block_noise", self._handle, self._noise, 0 if noise == "block" else 1)
+            first = min((int(x) for x in n if x > 0), default=0) - 1 if noise == "block" else -1
+        try:
+            for k in range(nsub):
+                if fused and (noise == "step" or k == first):
+                    self._noise_field(k if noise == "step" else -1)
+                _lib.call("goc_ensemble_rk2_substep", self._handle, k, self.stream.handle)
+                if noise == "step" and not fused:
+                    self._noise_launch(k)
+            _lib.call("goc_ensemble_end_block", self._handle, int(nsub), self.stream.handle)
+        finally:
+            if fused:
+                _lib.call("goc_ensemble_set_block_noise", self._handle, None, -1)
+        if noise == "block" and not fused:
+            self._noise_launch(-2)   # the members that take model error in this block
         return _lib.load().goc_kernel_launch_count() - before
 
-    def step(self, t_end, apply_stochastic_term=False, noise_cadence="block"):
-        """Advance every member by ``t_end`` seconds (one block).  With
+    def step(self, t_end, apply_stochastic_term=False, noise_cadence="block", members=None):
+        """Advance the members by ``t_end`` seconds (one block).  With
         ``apply_stochastic_term`` the model error is added either once after
         the block (``noise_cadence="block"``, the ``dataAssimilationStep``
         cadence, S/CDKLM16.py:786-790) or after every RK2 step
         (``"step"``, the cadence of ``CDKLM16.step``, S/CDKLM16.py:567-568).
-        Returns the number of member-cell-steps taken."""
+        ``apply_stochastic_term`` may be one flag per member (a truth and
+        particles with different flags, E/OceanNoiseEnsemble.py:517-532).
+        ``members``: indices of the members to advance (default all); the
+        others keep their state and time.  Returns the number of
+        member-cell-steps taken."""
         assert noise_cadence in ("block", "step")
-        with_noise = noise_cadence if (apply_stochastic_term and getattr(self, "_noise", None) is not None) else None
-        for s in self.sims:
+        flags = np.broadcast_to(np.asarray(apply_stochastic_term, dtype=bool), (len(self.sims),))
+        with_noise = noise_cadence if (flags.any() and getattr(self, "_noise", None) is not None) else None
+        chosen = range(len(self.sims)) if members is None else [int(m) for m in members]
+        for m in chosen:
+            s = self.sims[m]
             if s.t == 0:
                 s.bc_kernel.boundaryCondition(s.gpu_stream, s.gpu_data.h0, s.gpu_data.hu0, s.gpu_data.hv0)
-        scheds, table, n, nsub = self._schedule(t_end)
+        scheds, table, n, nsub = self._schedule(t_end, members)
         self._after_members()
+        mask = flags.astype(np.int32)
+        if with_noise is not None and mask.tobytes() != getattr(self, "_mask_key", None):
+            _lib.call("goc_ensemble_set_noise_mask", self._handle, mask.ctypes.data, self.stream.handle)
+            self._mask_key = mask.tobytes()
         if with_noise is not None and self._noise_kind == "kl" and self._rng_seed is None:
             if with_noise == "block":
-                self._kl_draw_rollers([(0, range(len(self.sims)))])
+                self._kl_draw_rollers([(0, [m for m in range(len(self.sims)) if mask[m]])])
             else:
-                self._kl_draw_rollers([(k + 1, [m for m in range(len(self.sims)) if n[m] > k])
+                self._kl_draw_rollers([(k + 1, [m for m in range(len(self.sims)) if n[m] > k and mask[m]])
                                        for k in range(nsub)])
+        if getattr(self, "_wind_members", None):
+            self._wind_times(scheds)
         key = (n.tobytes(), table.tobytes())
         if key != getattr(self, "_sched_key", None):
             _lib.call("goc_ensemble_set_schedule", self._handle, table.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
                       n.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), self.stream.handle)
             self._sched_key = key
         if self.use_graph:
-            entry = self._graphs.get((nsub, with_noise))
+            # a fused model error depends on which step ends each member's
+            # block: such graphs are kept per step-count pattern
+            fused = with_noise is not None and self._noise_kind == "soar"
+            gkey = (nsub, with_noise, (n.tobytes(), mask.tobytes()) if fused else None)
+            entry = self._graphs.get(gkey)
             if entry is None:
+                if len(self._graphs) >= 16:
+                    old = next(iter(self._graphs))
+                    _lib.load().goc_graph_destroy(self._graphs.pop(old)[0])
                 _lib.call("goc_graph_begin_capture", self.stream.handle)
-                nodes = self._launch_block(nsub, with_noise)
-                gh = ctypes.c_void_p()
-                _lib.call("goc_graph_end_capture", self.stream.handle, ctypes.byref(gh))
-                entry = self._graphs[(nsub, with_noise)] = (gh.value, nodes)
+                try:
+                    nodes = self._launch_block(nsub, with_noise, n)
+                finally:
+                    gh = ctypes.c_void_p()
+                    _lib.call("goc_graph_end_capture", self.stream.handle, ctypes.byref(gh))
+                entry = self._graphs[gkey] = (gh.value, nodes)
             _lib.call("goc_graph_launch", entry[0], self.stream.handle)
             self.kernels_launched += entry[1]
         else:
-            self.kernels_launched += self._launch_block(nsub, with_noise)
+            self.kernels_launched += self._launch_block(nsub, with_noise, n)
         self._before_members()
         self._check_staging()
         cells = 0
@@ -699,6 +790,19 @@ class BatchedEnsemble:
                 out.append(self._download(b, shape))
                 b.free()
         return tuple(out)
+
+    def max_dt(self):
+        """Per member the CFL limit 0.25 min(dx / |u +- c|, dy / |v +- c|)
+        over its interior cells, before the Courant factor (one reduction
+        launch pair; synchronises)."""
+        self._ensure_table()
+        self._after_members()
+        _lib.call("goc_ensemble_max_dt", self._handle, self._dt_dev.ptr, self.stream.handle)
+        out = np.zeros(len(self.sims), dtype=np.float32)
+        _lib.call("goc_memcpy_d2h_async", out.ctypes.data, self._dt_dev.ptr, ctypes.c_size_t(out.nbytes),
+                  self.stream.handle)
+        self.stream.synchronize()
+        return out
 
     def updateDt(self, courant_number=None, members=None):
         """Batched CFL limit of every member (one reduction launch pair);

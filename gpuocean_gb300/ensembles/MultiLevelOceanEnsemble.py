@@ -45,6 +45,10 @@ class MultiLevelOceanEnsemble:
         self.boundary_conditions = ML_ensemble[0][0].boundary_conditions
         self.t = ML_ensemble[0][0].t
         self.members = self._flat()
+        self.drifters = None
+        self.drift_dt = None
+        self.driftTrajectory = None
+        self.drift_sensitivity = None
         self.engine = BatchedEnsemble(self.members)
         if all(s.model_error is not None for s in self.members):
             from ..SWEsimulators.ModelErrorKL import ModelErrorKL
@@ -233,6 +237,61 @@ class MultiLevelOceanEnsemble:
         finally:
             for b in bufs:
                 b.free()
+
+    # ------------------------------------------------------------------
+    # drifters (E/MultiLevelOceanEnsemble.py:450-489)
+    # ------------------------------------------------------------------
+    def attachDrifters(self, drifterEnsembleSize, numDrifters=None, drifterPositions=None, drift_dt=60,
+                       drift_sensitivity=1.0):
+        """Drifters that move with the multi-level estimates of the mean and
+        variance of the velocity (MLDrifterCollection): `numDrifters` unique
+        drifters (or one per row of drifterPositions), each with
+        drifterEnsembleSize realisations, moved every drift_dt seconds of
+        stepToObservation; their positions are recorded now."""
+        from ..drifters.MLDrifterCollection import DriftTrajectory, MLDrifterCollection
+        assert numDrifters is not None or drifterPositions is not None, \
+            "Please provide either numDrifters or drifterPositions"
+        assert numDrifters is None or drifterPositions is None, \
+            "Both numDrifters and drifterPositions are given, please provide only one of them"
+        if numDrifters is None:
+            numDrifters = np.asarray(drifterPositions).shape[0]
+        self.drifters = MLDrifterCollection(numDrifters, drifterEnsembleSize,
+                                            boundaryConditions=self.ML_ensemble[0][0].boundary_conditions,
+                                            domain_size_x=self.nxs[0] * self.dxs[0],
+                                            domain_size_y=self.nys[0] * self.dys[0])
+        if drifterPositions is not None:
+            self.drifters.setDrifterPositions(np.asarray(drifterPositions))
+        mts = self.ML_ensemble[0][0].model_time_step
+        assert drift_dt >= mts, "We require that the drift_dt (" + str(drift_dt) + \
+            ") is larger than the model time step (" + str(mts) + ")"
+        self.drift_dt = drift_dt
+        self.drift_sensitivity = drift_sensitivity
+        self.drifterEnsembeSize = drifterEnsembleSize
+        self.driftTrajectory = [DriftTrajectory() for _ in range(drifterEnsembleSize)]
+        self.registerDrifterPositions()
+
+    def drift(self, dt):
+        """Move the drifters by dt with the multi-level mean velocity, the
+        variance (ddof 1) scaling their random walk (both estimated on the
+        device on the finest grid)."""
+        assert self.drifters is not None, "No drifters found. Can't call drift() before attachDrifters(...)"
+        mean = self.estimateVelocity(np.mean)
+        var = self.estimateVelocity(np.var, ddof=1)
+        self.drifters.drift(mean[0], mean[1], self.dxs[-1], self.dys[-1], dt=dt, sensitivity=self.drift_sensitivity,
+                            u_var=var[0], v_var=var[1])
+
+    def registerDrifterPositions(self):
+        """Record the current positions of every realisation."""
+        assert self.drifters is not None, "There are no drifters in this ensemble"
+        assert self.driftTrajectory is not None, \
+            "Something went wrong. The ensemble has drifters but no observation objects..."
+        for e in range(self.drifterEnsembeSize):
+            self.driftTrajectory[e].add_observation_from_mldrifters(self.t, self.drifters, e)
+
+    def saveDriftTrajectoriesToFile(self, path, filename_prefix):
+        import os
+        for e in range(self.drifterEnsembeSize):
+            self.driftTrajectory[e].to_pickle(os.path.join(path, filename_prefix + str(e).zfill(4) + ".pickle"))
 
     def cleanUp(self):
         self.engine.release()

@@ -7,10 +7,15 @@ is applied after every RK2 step, as ``CDKLM16.step`` does.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 
+from .. import _lib
 from ..drifters.GPUDrifterCollection import GPUDrifterCollection
 from ..SWEsimulators import CDKLM16
+from ..utils import Common
+from .BaseOceanStateEnsemble import BaseOceanStateEnsemble
 from .BatchedEnsemble import BatchedEnsemble
 from .MultiLevelOceanEnsemble import _device_statistic
 
@@ -27,7 +32,7 @@ class ObservationType:
     StaticBuoys = 4
 
 
-class OceanNoiseEnsemble:
+class OceanNoiseEnsemble(BaseOceanStateEnsemble):
     def __init__(self, gpu_ctx, numParticles, sim, num_drifters=1, observation_type=ObservationType.DrifterPosition,
                  buoys_positions=None, observation_variance=None, observation_variance_factor=5.0,
                  initialization_variance_factor_drifter_position=0.0, initialization_variance_factor_ocean_field=0.0,
@@ -40,6 +45,17 @@ class OceanNoiseEnsemble:
         self.t = 0.0
         self.observation_type = observation_type
         self.observedDrifterPositions = []
+        if observation_type == ObservationType.StaticBuoys and buoys_positions is not None:
+            assert len(buoys_positions) == num_drifters, \
+                "number of given buoys positions does not match the specified num_drifters"
+        self.buoys_positions = buoys_positions
+        # statistics under the first drifter, one entry per
+        # getEnsembleVarAndRMSEUnderDrifter call
+        for q in ("eta", "hu", "hv"):
+            for name in ("varianceUnderDrifter_", "rmseUnderDrifter_", "rmseMeanUnderDrifter_",
+                         "rmseWeightedUnderDrifter_", "rUnderDrifter_"):
+                setattr(self, name + q, [])
+        self.tArray = []
         eta, hu, hv = sim.download()
         Hi = sim.downloadBathymetry()[0]
         self.nx, self.ny, self.dx, self.dy, self.dt = sim.nx, sim.ny, sim.dx, sim.dy, sim.dt
@@ -78,6 +94,12 @@ class OceanNoiseEnsemble:
                 d.uniformly_distribute_drifters(initialization_cov_drifters=self.initialization_cov_drifters)
             p.attachDrifters(d)
             self.particles[i] = p
+        if observation_type == ObservationType.StaticBuoys:
+            if self.buoys_positions is None:
+                self.buoys_positions = self.particles[-1].drifters.getDrifterPositions()
+            bp = np.asarray(self.buoys_positions, dtype=np.float64)
+            self.buoys_ids = np.stack([np.floor(bp[:, 0] / self.dx), np.floor(bp[:, 1] / self.dy)],
+                                      axis=1).astype(int)
         self.engine = BatchedEnsemble(self.particles)
         if me is not None:
             self.engine.set_noise([p.model_error for p in self.particles], rng_seed=rng_seed)
@@ -93,12 +115,68 @@ class OceanNoiseEnsemble:
         self.observedDrifterPositions.append([self.t, positions])
 
     def step(self, t, stochastic_particles=True, stochastic_truth=True):
-        """All particles and the truth advance by t (S/.../OceanNoiseEnsemble.py:517-532)."""
-        if stochastic_particles != stochastic_truth:
-            raise NotImplementedError("truth and particles share one batched step")
-        self.engine.step(t, apply_stochastic_term=stochastic_particles, noise_cadence="step")
+        """All particles and the truth advance by t in one batched block, the
+        model error after every step of the particles and of the truth as
+        their flags say (E/OceanNoiseEnsemble.py:517-532)."""
+        flags = [bool(stochastic_particles)] * self.numParticles + [bool(stochastic_truth)]
+        self.engine.step(t, apply_stochastic_term=flags, noise_cadence="step")
         self.t = self.particles[self.obs_index].t
         return self.t
+
+    def step_truth(self, t, stochastic=True):
+        """Only the truth advances by t (E/OceanNoiseEnsemble.py:535-537)."""
+        self.engine.step(t, apply_stochastic_term=bool(stochastic), noise_cadence="step", members=[self.obs_index])
+        self.t = self.particles[self.obs_index].t
+        return self.t
+
+    def step_particles(self, t, stochastic=True):
+        """Only the particles advance by t; returns the ensemble's time, which
+        follows the truth (E/OceanNoiseEnsemble.py:539-543)."""
+        self.engine.step(t, apply_stochastic_term=bool(stochastic), noise_cadence="step",
+                         members=range(self.numParticles))
+        return self.t
+
+    def resample(self, newSampleIndices, reinitialization_variance):
+        """Particle i becomes an exact copy of particle newSampleIndices[i]:
+        state and previous state by device copies (every source read before
+        any destination is written), drifters at the truth's positions for
+        flow observations and at the source particle's positions otherwise
+        (E/OceanNoiseEnsemble.py:364-406).  reinitialization_variance is
+        ignored, as in the reference."""
+        if self.observation_type == ObservationType.DrifterPosition:
+            raise ValueError('Observation type DataAssimilationUtils.ObservationType.DrifterPosition is not supported')
+        idx = [int(i) for i in newSampleIndices]
+        assert len(idx) == self.numParticles
+        flow = self.observation_type in (ObservationType.UnderlyingFlow, ObservationType.DirectUnderlyingFlow)
+        true_pos = self.observeTrueDrifters() if flow else None
+        new_pos = [true_pos if flow else self.particles[src].drifters.getDrifterPositions() for src in idx]
+        eng = self.engine
+        eng._after_members()
+        st = eng.stream.handle
+        planes = lambda p: (p.gpu_data.h0, p.gpu_data.hu0, p.gpu_data.hv0,
+                            p.gpu_data.h1, p.gpu_data.hu1, p.gpu_data.hv1)
+        sources = sorted({src for i, src in enumerate(idx) if src != i})
+        stash = {}
+        for src in sources:
+            bufs = []
+            for a in planes(self.particles[src]):
+                nbytes = int(a.pitch) * (int(self.ny) + 4)
+                b = Common.DevicePtr(nbytes)
+                _lib.call("goc_memcpy_d2d_async", b.ptr, a.ptr, ctypes.c_size_t(nbytes), st)
+                bufs.append(b)
+            stash[src] = bufs
+        for i, src in enumerate(idx):
+            if src == i:
+                continue
+            for a, b in zip(planes(self.particles[i]), stash[src]):
+                _lib.call("goc_memcpy_d2d_async", a.ptr, b.ptr, ctypes.c_size_t(int(a.pitch) * (int(self.ny) + 4)), st)
+        eng._before_members()
+        eng.synchronize()
+        for bufs in stash.values():
+            for b in bufs:
+                b.free()
+        for i in range(self.numParticles):
+            self.particles[i].drifters.setDrifterPositions(np.asarray(new_pos[i]))
 
     def observeDrifters(self):
         out = np.empty((self.numParticles, self.driftersPerOceanModel, 2))
@@ -109,16 +187,127 @@ class OceanNoiseEnsemble:
     def observeTrueDrifters(self):
         return self.particles[self.obs_index].drifters.getDrifterPositions()
 
-    def observeTrueState(self):
+    def observeTrueState(self, apply_observation_error=True):
+        """The truth observed at its drifters, [[x, y, hu, hv], ...] (or the
+        positions for drifter-position observations), following
+        E/OceanNoiseEnsemble.py:436-515: flow observations read hu, hv of the
+        truth's cell (UnderlyingFlow: the drifter's displacement since the
+        previous observation over the elapsed time, times the depth the
+        reference reads there - at the cell index of the array that includes
+        the ghost cells, a reference quirk kept for identical results;
+        StaticBuoys: at the buoys' cells).  With apply_observation_error each
+        hu, hv gets N(0, observation_variance) noise from numpy's global
+        generator, drawn in the reference's order."""
         if self.observedDrifterPositions[-1][0] != self.t:
             self._addObservation(self.observeTrueDrifters())
         if self.observation_type == ObservationType.DrifterPosition:
             return self.observedDrifterPositions[-1][1]
-        eta, hu, hv = self.downloadTrueOceanState()
-        pos = self.observedDrifterPositions[-1][1]
-        ix = np.floor(pos[:, 0] / self.dx).astype(int)
-        iy = np.floor(pos[:, 1] / self.dy).astype(int)
-        return np.stack([pos[:, 0], pos[:, 1], np.asarray(hu)[iy, ix], np.asarray(hv)[iy, ix]], axis=1)
+        D = int(self.driftersPerOceanModel)
+        out = np.empty((D, 4))
+        sd = np.sqrt(self.observation_variance)
+        if self.observation_type == ObservationType.UnderlyingFlow:
+            (t1, p1), (t0, p0) = self.observedDrifterPositions[-1], self.observedDrifterPositions[-2]
+            Hm = self.particles[self.obs_index].downloadBathymetry()[1]
+            for d in range(D):
+                x, y = p1[d, 0], p1[d, 1]
+                depth = Hm[int(np.floor(y / self.dy)), int(np.floor(x / self.dx))]
+                hu = (x - p0[d, 0]) / (t1 - t0) * depth
+                hv = (y - p0[d, 1]) / (t1 - t0) * depth
+                if apply_observation_error:
+                    hu += np.random.normal(scale=sd)
+                    hv += np.random.normal(scale=sd)
+                out[d] = (x, y, hu, hv)
+            return out
+        eta, hu_f, hv_f = self.downloadTrueOceanState()
+        hu_f, hv_f = np.asarray(hu_f), np.asarray(hv_f)
+        for d in range(D):
+            if self.observation_type == ObservationType.StaticBuoys:
+                ix, iy = self.buoys_ids[d]
+                x, y = self.buoys_positions[d][0], self.buoys_positions[d][1]
+            else:
+                x, y = self.observedDrifterPositions[-1][1][d]
+                ix, iy = int(np.floor(x / self.dx)), int(np.floor(y / self.dy))
+            hu, hv = hu_f[iy, ix], hv_f[iy, ix]
+            if apply_observation_error:
+                hu += np.random.normal(scale=sd)
+                hv += np.random.normal(scale=sd)
+            out[d] = (x, y, hu, hv)
+        return out
+
+    def setTrueDrifterPositions(self, newPositions):
+        """Move the truth's drifters (E/OceanNoiseEnsemble.py:588-593)."""
+        self.particles[self.obs_index].drifters.setDrifterPositions(newPositions)
+
+    def getCauchyWeight(self, distances=None, normalize=True):
+        """Particle weights from a Cauchy distribution of the drifter
+        distances to the truth, scale sqrt(observation variance)
+        (E/OceanNoiseEnsemble.py:571-586)."""
+        if distances is None:
+            distances = self.getDistances()
+        var = self.getObservationVariance()
+        w = 1.0 / (np.pi * np.sqrt(var) * (1 + (np.asarray(distances) ** 2 / var)))
+        return w / np.sum(w) if normalize else w
+
+    def findLargestPossibleTimeStep(self):
+        """Largest stable dt over every particle and the truth:
+        0.25 min(dx / max|u +- sqrt(g h)|, dy / max|v +- sqrt(g h)|), from
+        the batched CFL reduction on the device (E/OceanNoiseEnsemble.py:
+        595-619 downloads every state; it also scans the ghost cells, whose
+        values behind walls are stale)."""
+        return float(np.min(self.engine.max_dt()))
+
+    def printMaxOceanStates(self):
+        for no, sim in enumerate(self.particles):
+            eta, hu, hv = sim.download()
+            print("------- simNo: " + ("True state" if no == self.obs_index else str(no)) + " -------")
+            print("t = " + str(sim.t))
+            print("Max eta: ", np.max(eta))
+            print("Max hu:  ", np.max(hu))
+            print("Max hv:  ", np.max(hv))
+
+    def downloadEnsembleStatisticalFields(self):
+        """Ensemble mean of (eta, hu, hv), its distance from the truth
+        |truth - mean| and the ratio of the spread
+        sqrt(sum (x - mean)^2 / (N + 1)) to that distance, per interior cell
+        (E/OceanNoiseEnsemble.py:723-775): one device pass over the particles
+        for the mean and variance."""
+        n = int(self.numParticles)
+        mean, var = self.engine.moments(0, n, "state", ddof=0)
+        truth = np.array(self.downloadTrueOceanState(), dtype=np.float64)
+        mean = mean.astype(np.float64)
+        rmse = np.sqrt((truth - mean) ** 2)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            r = np.sqrt(var.astype(np.float64) * n / (1.0 + n)) / rmse
+        m32, e32, r32 = (x.astype(np.float32) for x in (mean, rmse, r))
+        return m32[0], m32[1], m32[2], e32[0], e32[1], e32[2], r32[0], r32[1], r32[2]
+
+    def getEnsembleVarAndRMSEUnderDrifter(self, t, allDrifters=False):
+        """Statistics of (eta, hu, hv) in the cell under the truth's first
+        drifter, appended to the *UnderDrifter_* lists: the unbiased spread,
+        the RMS distance of the particles from the truth, the distance of
+        the mean from the truth, the RMS distance relative to |truth| and the
+        ratio spread / RMS distance (E/OceanNoiseEnsemble.py:621-721).  All
+        particles are read in one observation launch."""
+        pos = self.observeTrueState()[0][0:2]
+        ix, iy = int(np.floor(pos[0] / self.dx)), int(np.floor(pos[1] / self.dy))
+        centre = np.array([[(ix + 0.5) * self.dx, (iy + 0.5) * self.dy]])
+        vals = self.engine.observe(centre, first=0, count=self.numParticles + 1)[:, 0, :].astype(np.float64)
+        truth, parts = vals[self.obs_index], vals[:self.numParticles]
+        parts = parts[~np.isnan(parts[:, 0])]
+        k = len(parts)
+        mean = parts.mean(axis=0)
+        rmse = np.sqrt(np.sum((truth - parts) ** 2, axis=0) / k)
+        rmse_mean = np.sqrt((truth - mean) ** 2)
+        rmse_w = rmse / np.abs(truth)
+        sigma = np.sqrt(np.sum((parts - mean) ** 2, axis=0) / (k - 1.0))
+        r = sigma / rmse
+        for c, q in enumerate(("eta", "hu", "hv")):
+            getattr(self, "varianceUnderDrifter_" + q).append(sigma[c])
+            getattr(self, "rmseUnderDrifter_" + q).append(rmse[c])
+            getattr(self, "rmseMeanUnderDrifter_" + q).append(rmse_mean[c])
+            getattr(self, "rmseWeightedUnderDrifter_" + q).append(rmse_w[c])
+            getattr(self, "rUnderDrifter_" + q).append(r[c])
+        self.tArray.append(t)
 
     # ------------------------------------------------------------------
     # observation operator and statistics (E/BaseOceanStateEnsemble.py:79-176)
@@ -193,9 +382,10 @@ class OceanNoiseEnsemble:
         return func(np.moveaxis(np.array(vel), 0, -1), axis=-1, **kwargs)
 
     def getDistances(self, obs=None):
-        obs = self.observeTrueDrifters() if obs is None else obs
-        return np.array([np.linalg.norm(self.particles[p].drifters.getDrifterPositions() - obs, axis=1).mean()
-                         for p in range(self.numParticles)])
+        """(particles, drifters): distance of every particle's drifters from
+        the truth's (E/OceanNoiseEnsemble.py:545-554; obs is not used there
+        either)."""
+        return np.linalg.norm(self.observeTrueDrifters() - self.observeDrifters(), axis=2)
 
     def downloadParticleOceanState(self, particleNo):
         return self.particles[particleNo].download(interior_domain_only=True)

@@ -504,11 +504,32 @@ int goc_ensemble_end_block(void* ensemble, int n_launched, void* stream);
  * member without drifters.  Each RK2 substep then also advects the
  * drifters with the state after the previous substep, as
  * GPUDrifterCollection.driftFromSim does after every step
- * (D/GPUDrifterCollection.py:198-233, K/driftKernels.cu:74-183).  Wind drift
- * is not applied in the batched engine.
+ * (D/GPUDrifterCollection.py:198-233, K/driftKernels.cu:74-183); wind drift
+ * with goc_ensemble_set_drift_wind.
  */
 int goc_ensemble_set_drifters(void* ensemble, float* const* positions, const int* num_drifters,
                               float sensitivity, void* stream);
+
+/*
+ * Wind drift of ensemble drifters (the wind branch of passiveDrifterKernel,
+ * K/driftKernels.cu:151-157, as GPUDrifterCollection(wind=...,
+ * wind_drift_factor=...) applies it): wind[m] gives member m's current and
+ * next wind textures (device, nx x ny, both components read with that size
+ * as the reference does) and factor (0: no wind drift).  Those members'
+ * drifters then move in a launch of their own before each persistent step
+ * (and at the end of the block), with the time weight of each step's drift
+ * from goc_ensemble_set_wind_times: an n_members x max_substeps host table,
+ * entry (m, k) for the drift after step k.  Call goc_ensemble_set_drift_wind
+ * again after goc_ensemble_set_drifters.  Synchronise `stream`.
+ */
+typedef struct GocDriftWindDesc {
+    const float* x_current; const float* x_next;
+    const float* y_current; const float* y_next;
+    int32_t nx, ny;
+    float wind_drift_factor;
+} GocDriftWindDesc;
+int goc_ensemble_set_drift_wind(void* ensemble, const GocDriftWindDesc* wind, void* stream);
+int goc_ensemble_set_wind_times(void* ensemble, const float* wind_t, void* stream);
 
 /*
  * Every member's drifter rows (N_m positions and the observation row) in one
@@ -540,6 +561,8 @@ int goc_ensemble_max_dt(void* ensemble, float* dt_out, void* stream);
  * per-member OceanStateNoise.perturbSim calls of the reference's ensembles
  * (E/OceanNoiseEnsemble.py:517-543 via S/CDKLM16.py:567-568,726-733).
  * substep = -1 perturbs every member's current state between blocks;
+ * substep = -2 only the members that took model error in the block just
+ * ended (see goc_ensemble_set_noise_mask);
  * substep = k perturbs, right after RK2 step k of a block, the members that
  * took step k (the cadence of step(t, apply_stochastic_term=True)).
  * goc_noise_batch_generate draws new XORWOW normals into the members'
@@ -550,6 +573,41 @@ int goc_noise_batch_destroy(void* batch);
 int goc_noise_batch_seed(void* batch, unsigned long long seed, void* stream);
 int goc_noise_batch_generate(void* batch, void* ensemble, int substep, void* stream);
 int goc_noise_batch_perturb(void* batch, void* ensemble, float perturbation_scale, int substep, void* stream);
+
+/*
+ * Model error fused into the ensemble step (the batched engine's form of
+ * perturbState after a step, S/CDKLM16.py:567-568 and 786-790; no
+ * counterpart kernel in the reference).  goc_noise_batch_field computes only
+ * the SOAR coarse fields (same substep rule as goc_noise_batch_perturb).
+ * goc_ensemble_set_block_noise(ensemble, batch, mode) then makes the
+ * following goc_ensemble_rk2_substep launches add each member's up-sampled,
+ * geostrophically balanced perturbation to Q^{n+1} inside the step, before
+ * the write, instead of a separate read-modify-write pass:
+ *   mode 0: members perturb after the last step of their block (the
+ *           dataAssimilationStep cadence); the drifters of that last step
+ *           move with the state before the perturbation, read from an
+ *           unperturbed copy the step writes (allocated here, one buffer
+ *           set per member with drifters);
+ *   mode 1: members perturb after every step (the CDKLM16.step cadence),
+ *           before their drifters move;
+ *   mode -1: no fused model error.
+ * The mode stays in force, also for goc_ensemble_end_block, until changed.
+ * The coarse fields must be computed before the first perturbing launch and
+ * stay unchanged until the last.  Results are bit-identical to stepping and
+ * then calling goc_noise_batch_perturb.  Call outside stream capture.
+ */
+int goc_noise_batch_field(void* batch, void* ensemble, float perturbation_scale, int substep, void* stream);
+int goc_ensemble_set_block_noise(void* ensemble, void* noise_batch, int mode);
+
+/*
+ * Which members take model error inside a block (mask[m] != 0), for a truth
+ * and particles stepped with different stochastic flags
+ * (E/OceanNoiseEnsemble.py:517-543; the reference calls step with
+ * apply_stochastic_term per member).  NULL: every member.  Applies to every
+ * later block (fused or not, SOAR or KL) until changed; perturbations
+ * between blocks (substep -1) ignore it.  Synchronises `stream`.
+ */
+int goc_ensemble_set_noise_mask(void* ensemble, const int* mask, void* stream);
 
 /* ------------------------------------------------------------------------
  * Karhunen-Loeve model error (S/ModelErrorKL.py:38-463, K/ocean_noise.cu:666-954)

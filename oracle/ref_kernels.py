@@ -113,6 +113,9 @@ REF_CONFIGS = {
     # GPUDrifterCollection with the default 1x1 wind (D/GPUDrifterCollection.py:70-76)
     "drift": ("driftKernels.cu", {"block_width": 64, "block_height": 1, "WIND_X_NX": 1, "WIND_X_NY": 1,
                                   "WIND_Y_NX": 1, "WIND_Y_NY": 1}, []),
+    # ... and with a 3 x 4 (nx x ny) wind texture for both components
+    "drift_wind3x4": ("driftKernels.cu", {"block_width": 64, "block_height": 1, "WIND_X_NX": 3, "WIND_X_NY": 4,
+                                          "WIND_Y_NX": 3, "WIND_Y_NY": 4}, []),
     # open boundaries: the reference's sponge test grid (T/schemes/CombinedCDKLM16_test.py:43-56) and
     # boundary kernels for per-cell exterior data along 50 x 70 and 64 x 48 grids
     "cdklm_sponge50x70": ("CDKLM16_kernel.cu", cdklm_defines(50, 70, 200.0, 200.0), CDKLM_FLAGS),
@@ -657,28 +660,33 @@ def ref_observe_underlying_flow(nx, ny, dx, dy, hu, hv, positions, H=60.0):
 
 
 class RefDrifters:
-    """GPUDrifterCollection (D/GPUDrifterCollection.py:34-253), 1x1 zero wind."""
+    """GPUDrifterCollection (D/GPUDrifterCollection.py:34-253): 1x1 zero wind,
+    or (config "drift_wind3x4") wind drift with 3 x 4 wind textures:
+    wind = (x_current, x_next, y_current, y_next) arrays of shape (4, 3)."""
 
-    def __init__(self, positions, domain_size_x, domain_size_y, periodic_ns, periodic_ew):
+    def __init__(self, positions, domain_size_x, domain_size_y, periodic_ns, periodic_ew, config="drift",
+                 wind=None, wind_drift_factor=0.0):
         drv = self.drv = Driver.get()
         pos = np.ascontiguousarray(positions, dtype=np.float32)
         self.n = pos.shape[0] - 1
         self.pos = Array2D(drv, pos)
         self.zero = Array2D(drv, np.zeros((1, 1), np.float32))
+        self.wind = [Array2D(drv, w) for w in wind] if wind is not None else None
+        self.factor = np.float32(wind_drift_factor)
         self.size = (np.float32(domain_size_x), np.float32(domain_size_y))
         self.periodic = (int(periodic_ns), int(periodic_ew))
-        self.k_drift = drv.function("drift", "passiveDrifterKernel")
-        self.k_bc = drv.function("drift", "enforceBoundaryConditions")
+        self.k_drift = drv.function(config, "passiveDrifterKernel")
+        self.k_bc = drv.function(config, "enforceBoundaryConditions")
         self.gs = (_ceil(self.n + 2, 64), 1)       # D/GPUDrifterCollection.py:107-110
 
-    def drift(self, sim: RefCDKLM16, dt):
+    def drift(self, sim: RefCDKLM16, dt, wind_t=0.0):
         h, u, v = sim.h0
-        z = self.zero.ptr
+        w = [a.ptr for a in self.wind] if self.wind is not None else [self.zero.ptr] * 4
         self.drv.launch(self.k_drift, "iifffiiPiPiPiPiiiiPifPPPPff", self.gs, (64, 1, 1),
                         sim.nx, sim.ny, sim.dx, sim.dy, np.float32(dt), 2, 2,
                         h.ptr, h.pitch, u.ptr, u.pitch, v.ptr, v.pitch, sim.Hm.ptr, sim.Hm.pitch,
                         self.periodic[0], self.periodic[1], self.n, self.pos.ptr, self.pos.pitch,
-                        1.0, z, z, z, z, 0.0, 0.0)
+                        1.0, w[0], w[1], w[2], w[3], np.float32(wind_t), self.factor)
 
     def enforce_boundary(self):
         self.drv.launch(self.k_bc, "ffiiiPi", self.gs, (64, 1, 1), self.size[0], self.size[1],
@@ -691,3 +699,5 @@ class RefDrifters:
     def free(self):
         self.pos.free()
         self.zero.free()
+        for a in self.wind or []:
+            a.free()
