@@ -96,10 +96,12 @@ class CDKLM16(Simulator):
         assert rk_order in (1, 2, 3), "Only 1st, 2nd and 3rd order Runge Kutta supported"
         if rk_order == 3:
             assert r == 0.0, "3rd order Runge Kutta supported only without friction"
-        if use_direct_lookup:
-            raise NotImplementedError("use_direct_lookup is not supported; pressure is always interpolated")
         wind = WindStress.WindStress() if wind is None else wind
         atmospheric_pressure = AtmosphericPressure.AtmosphericPressure() if atmospheric_pressure is None else atmospheric_pressure
+        if use_direct_lookup:
+            assert atmospheric_pressure.P[0].shape[0] == ny + 4 and atmospheric_pressure.P[0].shape[1] == nx + 4, \
+                "Direct lookup is only supported for same sized grids"
+        self.use_direct_lookup = bool(use_direct_lookup)
         boundary_conditions = Common.BoundaryConditions() if boundary_conditions is None else boundary_conditions
         angle = np.asarray(angle)
         ghost_cells_x = ghost_cells_y = 2
@@ -141,8 +143,10 @@ class CDKLM16(Simulator):
         if subsample_angle and angle.size >= eta0.size:
             angle = subsample_texture(angle, subsample_angle)
         angle = np.atleast_2d(np.asarray(angle, dtype=np.float32))
-        if angle.size != 1:
-            raise NotImplementedError("only a constant north angle is supported by the GB300 step kernel")
+        # a north-angle texture: every cell uses its own north vector, so the
+        # RK stages run one launch each (goc_cdklm_stage) with the ghost fill
+        # between them, as the reference steps
+        self.angle_varies = angle.size != 1
         self.angle_arr = Common.CUDAArray2D(self.gpu_stream, angle.shape[1], angle.shape[0], 0, 0, angle)
         # a spatially varying texture is evaluated once per cell centre
         self.coriolis_cell = None
@@ -227,6 +231,7 @@ class CDKLM16(Simulator):
         p.wind_y_nx, p.wind_y_ny = self.wind_stress_y_current_arr.nx_halo, self.wind_stress_y_current_arr.ny_halo
         p.atm_p_cur, p.atm_p_next = self.atmospheric_pressure_current_arr.ptr, self.atmospheric_pressure_next_arr.ptr
         p.atm_p_nx, p.atm_p_ny = self.atmospheric_pressure_current_arr.nx_halo, self.atmospheric_pressure_current_arr.ny_halo
+        p.atm_p_direct = int(self.use_direct_lookup)
         return p
 
     @property
@@ -267,9 +272,14 @@ class CDKLM16(Simulator):
                   int(d.h0.pitch), self.bathymetry.Bi.ptr, int(self.bathymetry.Bi.pitch),
                   self.bathymetry.Bm.ptr, int(self.bathymetry.Bm.pitch), self.stream_handle)
 
+    def _stagewise(self):
+        """Whether RK2 runs stage by stage: sponge boundaries act between the
+        stages, and a north-angle texture needs the single-stage kernel."""
+        return self.boundary_conditions.isSponge() or self.angle_varies
+
     def _rk_step(self, local_dt):
         d = self.gpu_data
-        if self.rk_order == 2 and self.boundary_conditions.isSponge():
+        if self.rk_order == 2 and self._stagewise():
             # sponge boundaries act between the stages (S/CDKLM16.py:519-530):
             # stage by stage, with the boundary kernels on the stage buffer
             self._stage((d.h0, d.hu0, d.hv0), (d.h1, d.hu1, d.hv1), local_dt, 0)
@@ -306,7 +316,7 @@ class CDKLM16(Simulator):
             self.bc_kernel.boundaryCondition(self.gpu_stream, self.gpu_data.h0, self.gpu_data.hu0, self.gpu_data.hv0)
         # nothing between the RK2 steps: the run of steps goes to the library
         # in one call once both forcing weights are 1 (time-independent forcing)
-        plain = (not update_dt and self.rk_order == 2 and not self.boundary_conditions.isSponge()
+        plain = (not update_dt and self.rk_order == 2 and not self._stagewise()
                  and not (self.model_error is not None and apply_stochastic_term)
                  and not self.hasDrifters and not self.hasCrossProductDrifter
                  and len(self.wind_stress.t) == 1 and len(self.atmospheric_pressure.t) == 1)
@@ -325,7 +335,7 @@ class CDKLM16(Simulator):
             perturbed = self.model_error is not None and apply_stochastic_term
             if perturbed:
                 self.perturbState()
-            if perturbed or self.boundary_conditions.isSponge():
+            if perturbed or (self.rk_order == 2 and self._stagewise()):
                 self.bc_kernel.boundaryCondition(self.gpu_stream, self.gpu_data.h0, self.gpu_data.hu0,
                                                  self.gpu_data.hv0)
             self.drifterStep(local_dt)

@@ -46,6 +46,7 @@ class GocCdklmParams(ctypes.Structure):
         ("atm_p_cur", c_void_p), ("atm_p_next", c_void_p),
         ("atm_p_nx", ctypes.c_int32), ("atm_p_ny", ctypes.c_int32),
         ("atm_p_t", c_float),
+        ("atm_p_direct", ctypes.c_int32),
     ]
 
 

@@ -63,15 +63,15 @@ static int launch_members(const GocCdklmParams* p, const StepConst& k, float dt,
     return check_launch("cdklm_members_kernel");
 }
 
-template <int NSTAGE, bool CF, bool SF>
+template <int NSTAGE, bool CF, bool SF, bool ANGLE = false>
 static int launch_tile(const GocCdklmParams* p, const StepConst& k, float dt, int rk_step,
                        const float* e0, const float* hu0, const float* hv0, float* e1, float* hu1, float* hv1,
                        float* ea, float* hua, float* hva, int pitch_f, const float* Hi, int hi_pitch_f,
                        const float* Hm, int hm_pitch_f, cudaStream_t st) {
     constexpr int HALO = 2 * NSTAGE;
     constexpr int W = kTX + 2 * HALO, H = kTY + 2 * HALO;
-    constexpr size_t smem = sizeof(TileSmem<W, H>);
-    auto kern = cdklm_tile_kernel<kTX, kTY, NSTAGE, kNT, CF, SF>;
+    constexpr size_t smem = ANGLE ? sizeof(TileSmemAngle<W, H>) : sizeof(TileSmem<W, H>);
+    auto kern = cdklm_tile_kernel<kTX, kTY, NSTAGE, kNT, CF, SF, ANGLE>;
     static bool configured = false;
     if (!configured) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -218,7 +218,7 @@ extern "C" int goc_cdklm_stage(const GocCdklmParams* p, float dt, int rk_step, c
                                const float* hu_in, const float* hv_in, float* eta_out, float* hu_out,
                                float* hv_out, float* eta_alt, float* hu_alt, float* hv_alt, int pitch,
                                const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch, void* stream) {
-    int rc = validate_params(p, "goc_cdklm_stage", true);
+    int rc = validate_params(p, "goc_cdklm_stage", true, true);
     if (rc) return rc;
     if ((rc = check_pitch(p, pitch, Hi_pitch, Hm_pitch, "goc_cdklm_stage"))) return rc;
     if (!eta_in || !hu_in || !hv_in || !eta_out || !hu_out || !hv_out || !Hi || !Hm)
@@ -232,6 +232,13 @@ extern "C" int goc_cdklm_stage(const GocCdklmParams* p, float dt, int rk_step, c
     bool cf, sf;
     cudaStream_t st = as_stream(stream);
     if ((rc = make_const(p, &k, &cf, &sf))) return rc;
+    if (p->angle_nx * p->angle_ny > 1) {
+        // a north vector per cell (angle texture): its own kernel, general
+        // Coriolis and forcing lookups
+        return launch_tile<1, false, false, true>(p, k, dt, rk_step, eta_in, hu_in, hv_in, eta_out, hu_out, hv_out,
+                                                  eta_alt, hu_alt, hv_alt, pitch / 4, Hi, Hi_pitch / 4, Hm,
+                                                  Hm_pitch / 4, st);
+    }
     return dispatch<1>(p, k, cf, sf, dt, rk_step, eta_in, hu_in, hv_in, eta_out, hu_out, hv_out, eta_alt, hu_alt,
                        hv_alt, pitch / 4, Hi, Hi_pitch / 4, Hm, Hm_pitch / 4, st);
 }

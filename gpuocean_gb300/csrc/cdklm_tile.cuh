@@ -24,6 +24,8 @@
 // multiplications by precomputed reciprocals here.
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "noise_transfer.cuh"
 #include "tma.cuh"
@@ -50,6 +52,17 @@ struct TileSmem {
     float Fx[3][H][W];   // flux through the east face of each cell
     float Gy[3][H][W];   // flux through the north face of each cell
     float Hi[H + 1][W + 1];  // corner depths, land -> kDryFlag
+};
+
+// The single-stage kernel with a north-angle texture: each cell sees the
+// faces around it with its own north vector (K/CDKLM16_kernel.cu:744-765),
+// so every face flux exists twice, once per adjacent cell: Fx / Gy hold the
+// faces as their minus (west / south) cell sees them, Fx2 / Gy2 as their
+// plus cell does.
+template <int W, int H>
+struct TileSmemAngle : TileSmem<W, H> {
+    float Fx2[3][H][W];
+    float Gy2[3][H][W];
 };
 
 __device__ __forceinline__ float minmod_raw(float b, float c, float f) {
@@ -158,7 +171,9 @@ __device__ __forceinline__ void block_cell(int idx, int ny, int& i, int& j) {
 
 // SM: the shared-memory layout; any struct with the members of TileSmem that
 // the stage code reads (D, Sx, Sy, Fx, Gy, Hi and, with a Coriolis texture, Fc).
-template <int W, int H, int NT, bool BORDER, class SM = TileSmem<W, H>>
+// ANGLE: the north vector varies by cell (angle texture; SM then has the
+// Fx2 / Gy2 planes of TileSmemAngle).
+template <int W, int H, int NT, bool BORDER, class SM = TileSmem<W, H>, bool ANGLE = false>
 struct Tile {
     SM& S;
     const GocCdklmParams& p;
@@ -169,6 +184,22 @@ struct Tile {
     float wind_X, wind_Y;     // scaled wind stress of 1x1 textures
 
     __device__ float F(int j, int i, bool const_f) const { return const_f ? f0 : S.Fc[j][i]; }
+
+    // North vector of local cell (i, j): the angle texture at the cell's
+    // (unwrapped) global index, as getNorth evaluates it
+    // (K/CDKLM16_kernel.cu:70-79), or the constant one.
+    __device__ __forceinline__ void north(int i, int j, float& ax, float& ay) const {
+        if constexpr (ANGLE) {
+            const float s = (x0 + i + 0.5f) / (p.nx + 4.0f);
+            const float t = (y0 + j + 0.5f) / (p.ny + 4.0f);
+            const float a = tex_bilinear(p.angle, p.angle_nx, p.angle_ny, s, t);
+            ax = __sinf(a);
+            ay = __cosf(a);
+        } else {
+            ax = nX;
+            ay = nY;
+        }
+    }
 
     // Start thread of the second loop of a phase whose first loop has n_first
     // items: the warps that take one item more in the first loop (from thread
@@ -203,9 +234,11 @@ struct Tile {
                 if (p.bc_east == 1) { if (gx > p.nx) rv = -rv; if (gx > p.nx + 1) cv = -cv; }
             }
             const float fL = F(j, i - 1, CONST_F), fC = F(j, i, CONST_F), fR = F(j, i + 1, CONST_F);
-            const float lfv = (nX * uL + nY * lv) * fL;
-            const float cfv = (nX * uC + nY * cv) * fC;
-            const float rfv = (nX * uR + nY * rv) * fR;
+            float cnX, cnY;
+            north(i, j, cnX, cnY);
+            const float lfv = (cnX * uL + cnY * lv) * fL;
+            const float cfv = (cnX * uC + cnY * cv) * fC;
+            const float rfv = (cnX * uR + cnY * rv) * fR;
             const float back = k.theta_g * (eC - eL - k.Vc * (cfv + lfv));
             const float cent = k.half_g * (eR - eL - k.Vc * (rfv + 2.0f * cfv + lfv));
             const float fwd = k.theta_g * (eR - eC - k.Vc * (cfv + rfv));
@@ -226,11 +259,13 @@ struct Tile {
             S.Sx[2][j][i] = Kx;
         }
         constexpr int NXY = UX1 - UX0, NYY = UY1 - UY0 + 2;
-        const float eX = nY, eY = -nX;  // east vector
         for (int idx = second_loop_thread(NXS * (NYS - skip)); idx < NXY * (NYY - skip); idx += NT) {
             int i, j;
             block_cell<NXY>(idx, NYY - skip, i, j);
             i += UX0; j += UY0 - 1 + skip;
+            float cnX, cnY;
+            north(i, j, cnX, cnY);
+            const float eX = cnY, eY = -cnX;  // east vector
             const int gy = y0 + j;
             const float eL = S.D[0][j - 1][i], eC = S.D[0][j][i], eU = S.D[0][j + 1][i];
             const float uL = S.D[1][j - 1][i], uC = S.D[1][j][i], uU = S.D[1][j + 1][i];
@@ -292,22 +327,36 @@ struct Tile {
                     if (p.bc_west == 1 && gxp == 2) vm = -vm;
                     if (p.bc_east == 1 && gxp == p.nx + 2) vp = -vp;
                 }
-                const float vpn = up * nX + vp * nY;
-                const float vmn = um * nX + vm * nY;
-                const float etap = fmaxf(-Hf, ebp - (S.Sx[2][j][i + 1] + p.dx * F(j, i + 1, CONST_F) * vpn) * k.inv_2g);
-                const float etam = fmaxf(-Hf, ebm + (S.Sx[2][j][i] + p.dx * F(j, i, CONST_F) * vmn) * k.inv_2g);
-                if (dm) {
-                    F1 = k.half_g * (etap + Hf) * (etap + Hf);
-                } else if (dp) {
-                    F1 = k.half_g * (etam + Hf) * (etam + Hf);
-                } else {
-                    cdklm_flux(p, k, etam, Rmx, Rmy, etap, Rpx, Rpy, Hf, F0, F1, F2);
+                // the face as a cell with north vector (ax, ay) sees it
+                auto face = [&](float ax, float ay, float& G0, float& G1, float& G2) {
+                    const float vpn = up * ax + vp * ay;
+                    const float vmn = um * ax + vm * ay;
+                    const float etap =
+                        fmaxf(-Hf, ebp - (S.Sx[2][j][i + 1] + p.dx * F(j, i + 1, CONST_F) * vpn) * k.inv_2g);
+                    const float etam = fmaxf(-Hf, ebm + (S.Sx[2][j][i] + p.dx * F(j, i, CONST_F) * vmn) * k.inv_2g);
+                    if (dm) {
+                        G1 = k.half_g * (etap + Hf) * (etap + Hf);
+                    } else if (dp) {
+                        G1 = k.half_g * (etam + Hf) * (etam + Hf);
+                    } else {
+                        cdklm_flux(p, k, etam, Rmx, Rmy, etap, Rpx, Rpy, Hf, G0, G1, G2);
+                    }
+                };
+                float ax, ay;
+                north(i, j, ax, ay);
+                face(ax, ay, F0, F1, F2);
+                if constexpr (ANGLE) {
+                    float P0 = 0.f, P1 = 0.f, P2 = 0.f;
+                    north(i + 1, j, ax, ay);
+                    face(ax, ay, P0, P1, P2);
+                    S.Fx2[0][j][i] = P0; S.Fx2[1][j][i] = P1; S.Fx2[2][j][i] = P2;
                 }
+            } else if constexpr (ANGLE) {
+                S.Fx2[0][j][i] = 0.f; S.Fx2[1][j][i] = 0.f; S.Fx2[2][j][i] = 0.f;
             }
             S.Fx[0][j][i] = F0; S.Fx[1][j][i] = F1; S.Fx[2][j][i] = F2;
         }
         constexpr int NXG = UX1 - UX0, NYG = UY1 - UY0 + 1;
-        const float eX = nY, eY = -nX;
         for (int idx = second_loop_thread(NXF * (NYF - skip)); idx < NXG * (NYG - skip); idx += NT) {
             int i, j;
             block_cell<NXG>(idx, NYG - skip, i, j);
@@ -328,20 +377,35 @@ struct Tile {
                     if (p.bc_south == 1 && gyp == 2) um = -um;
                     if (p.bc_north == 1 && gyp == p.ny + 2) up = -up;
                 }
-                const float upe = up * eX + vp * eY;
-                const float ume = um * eX + vm * eY;
-                const float etap = fmaxf(-Hf, ebp - (S.Sy[2][j + 1][i] - p.dy * F(j + 1, i, CONST_F) * upe) * k.inv_2g);
-                const float etam = fmaxf(-Hf, ebm + (S.Sy[2][j][i] - p.dy * F(j, i, CONST_F) * ume) * k.inv_2g);
-                if (dm) {
-                    G2 = k.half_g * (etap + Hf) * (etap + Hf);
-                } else if (dp) {
-                    G2 = k.half_g * (etam + Hf) * (etam + Hf);
-                } else {
-                    // u and v swap roles along y
-                    float a0, a1, a2;
-                    cdklm_flux(p, k, etam, Rmy, Rmx, etap, Rpy, Rpx, Hf, a0, a1, a2);
-                    G0 = a0; G1 = a2; G2 = a1;
+                // the face as a cell with east vector (eX, eY) sees it
+                auto face = [&](float eX, float eY, float& H0, float& H1, float& H2) {
+                    const float upe = up * eX + vp * eY;
+                    const float ume = um * eX + vm * eY;
+                    const float etap =
+                        fmaxf(-Hf, ebp - (S.Sy[2][j + 1][i] - p.dy * F(j + 1, i, CONST_F) * upe) * k.inv_2g);
+                    const float etam = fmaxf(-Hf, ebm + (S.Sy[2][j][i] - p.dy * F(j, i, CONST_F) * ume) * k.inv_2g);
+                    if (dm) {
+                        H2 = k.half_g * (etap + Hf) * (etap + Hf);
+                    } else if (dp) {
+                        H2 = k.half_g * (etam + Hf) * (etam + Hf);
+                    } else {
+                        // u and v swap roles along y
+                        float a0, a1, a2;
+                        cdklm_flux(p, k, etam, Rmy, Rmx, etap, Rpy, Rpx, Hf, a0, a1, a2);
+                        H0 = a0; H1 = a2; H2 = a1;
+                    }
+                };
+                float ax, ay;
+                north(i, j, ax, ay);
+                face(ay, -ax, G0, G1, G2);
+                if constexpr (ANGLE) {
+                    float P0 = 0.f, P1 = 0.f, P2 = 0.f;
+                    north(i, j + 1, ax, ay);
+                    face(ay, -ax, P0, P1, P2);
+                    S.Gy2[0][j][i] = P0; S.Gy2[1][j][i] = P1; S.Gy2[2][j][i] = P2;
                 }
+            } else if constexpr (ANGLE) {
+                S.Gy2[0][j][i] = 0.f; S.Gy2[1][j][i] = 0.f; S.Gy2[2][j][i] = 0.f;
             }
             S.Gy[0][j][i] = G0; S.Gy[1][j][i] = G1; S.Gy[2][j][i] = G2;
         }
@@ -359,13 +423,21 @@ struct Tile {
         hu = 0.0f; hv = 0.0f;
         if (hsum > p.depth_cutoff) { hu = uc * hsum; hv = vc * hsum; }
         const float fc = F(j, i, CONST_F);
-        float fd0 = (S.Fx[0][j][i] - S.Fx[0][j][i - 1]) * k.inv_dx;
-        float fd1 = (S.Fx[1][j][i] - S.Fx[1][j][i - 1]) * k.inv_dx;
-        float fd2 = (S.Fx[2][j][i] - S.Fx[2][j][i - 1]) * k.inv_dx;
+        // the west / south faces as this cell sees them: with a north-angle
+        // texture the plus-cell versions of the neighbours' faces
+        auto WF = [&](int c) -> float {
+            if constexpr (ANGLE) return S.Fx2[c][j][i - 1]; else return S.Fx[c][j][i - 1];
+        };
+        auto SF = [&](int c) -> float {
+            if constexpr (ANGLE) return S.Gy2[c][j - 1][i]; else return S.Gy[c][j - 1][i];
+        };
+        float fd0 = (S.Fx[0][j][i] - WF(0)) * k.inv_dx;
+        float fd1 = (S.Fx[1][j][i] - WF(1)) * k.inv_dx;
+        float fd2 = (S.Fx[2][j][i] - WF(2)) * k.inv_dx;
         if (!p.one_dimensional) {
-            fd0 = fd0 + (S.Gy[0][j][i] - S.Gy[0][j - 1][i]) * k.inv_dy;
-            fd1 = fd1 + (S.Gy[1][j][i] - S.Gy[1][j - 1][i]) * k.inv_dy;
-            fd2 = fd2 + (S.Gy[2][j][i] - S.Gy[2][j - 1][i]) * k.inv_dy;
+            fd0 = fd0 + (S.Gy[0][j][i] - SF(0)) * k.inv_dy;
+            fd1 = fd1 + (S.Gy[1][j][i] - SF(1)) * k.inv_dy;
+            fd2 = fd2 + (S.Gy[2][j][i] - SF(2)) * k.inv_dy;
         }
         float st1 = 0.0f, st2 = 0.0f;
         if (hsum >= p.depth_cutoff && ec != kDryFlag) {
@@ -377,6 +449,8 @@ struct Tile {
             const float RHxm = 0.5f * (S.Hi[j][i] + S.Hi[j + 1][i]);
             const float RHyp = 0.5f * (S.Hi[j + 1][i] + S.Hi[j + 1][i + 1]);
             const float RHym = 0.5f * (S.Hi[j][i] + S.Hi[j][i + 1]);
+            float nX, nY;
+            north(i, j, nX, nY);
             const float eX = nY, eY = -nX;
             const float hu_e = hu * eX + hv * eY;
             const float hv_n = hu * nX + hv * nY;
@@ -398,15 +472,28 @@ struct Tile {
                 X = p.wind_stress_factor * (p.wind_t * wxn + (1.0f - p.wind_t) * wxc);
                 Y = p.wind_stress_factor * (p.wind_t * wyn + (1.0f - p.wind_t) * wyc);
                 if (p.atm_p_nx * p.atm_p_ny > 1) {
-                    const float dxn = 1.0f / (float)(p.nx + 4), dyn = 1.0f / (float)(p.ny + 4);
                     const float pt = p.atm_p_t;
-                    auto P = [&](float ss, float tt) {
-                        const float c = tex_bilinear(p.atm_p_cur, p.atm_p_nx, p.atm_p_ny, ss, tt);
-                        const float n = tex_bilinear(p.atm_p_next, p.atm_p_nx, p.atm_p_ny, ss, tt);
-                        return pt * n + (1.0f - pt) * c;
-                    };
-                    const float pe = P(s + dxn, t), pw = P(s - dxn, t);
-                    const float pn = P(s, t + dyn), ps = P(s, t - dyn);
+                    float pe, pw, pn, ps;
+                    if (p.atm_p_direct) {
+                        // the cells the reference's direct lookup reads, its
+                        // north/south values one column east included
+                        // (K/external_forcing.cu:76-97)
+                        auto P = [&](int ii, int jj) {
+                            const size_t o = (size_t)jj * p.atm_p_nx + ii;
+                            return pt * __ldg(p.atm_p_next + o) + (1.0f - pt) * __ldg(p.atm_p_cur + o);
+                        };
+                        pn = P(gxs + 1, gys + 1); ps = P(gxs + 1, gys - 1);
+                        pe = P(gxs + 1, gys); pw = P(gxs - 1, gys);
+                    } else {
+                        const float dxn = 1.0f / (float)(p.nx + 4), dyn = 1.0f / (float)(p.ny + 4);
+                        auto P = [&](float ss, float tt) {
+                            const float c = tex_bilinear(p.atm_p_cur, p.atm_p_nx, p.atm_p_ny, ss, tt);
+                            const float n = tex_bilinear(p.atm_p_next, p.atm_p_nx, p.atm_p_ny, ss, tt);
+                            return pt * n + (1.0f - pt) * c;
+                        };
+                        pe = P(s + dxn, t); pw = P(s - dxn, t);
+                        pn = P(s, t + dyn); ps = P(s, t - dyn);
+                    }
                     ax = -(pe - pw) * hsum * k.inv_atm_x;
                     ay = -(pn - ps) * hsum * k.inv_atm_y;
                 }
@@ -523,7 +610,8 @@ constexpr int kHandRows = 4;
 // reuses.  Only the RK2 fused path (NSTAGE = 2) streams.  s1 is a run-time
 // value so that one instantiation serves both kinds of tile (the kernel's
 // code stays within the instruction cache).
-template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING, bool BORDER, bool NOISE = false>
+template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING, bool BORDER, bool NOISE = false,
+          bool ANGLE = false>
 __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const StepConst& k, float dt, int rk_step,
                                                 int tile_x, int tile_y,
                                                 const float* __restrict__ e_in, const float* __restrict__ hu_in,
@@ -536,14 +624,18 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const S
                                                 const TileNoise* nz = nullptr) {
     constexpr int HALO = 2 * NSTAGE;
     constexpr int W = TX + 2 * HALO, H = TY + 2 * HALO;
-    TileSmem<W, H>& S = *reinterpret_cast<TileSmem<W, H>*>(smem_raw);
+    static_assert(!ANGLE || NSTAGE == 1, "a north-angle texture is stepped stage by stage");
+    using SMT = std::conditional_t<ANGLE, TileSmemAngle<W, H>, TileSmem<W, H>>;
+    SMT& S = *reinterpret_cast<SMT*>(smem_raw);
 
-    Tile<W, H, NT, BORDER> T{S, p, k, 2 + tile_x * TX - HALO, 2 + tile_y * TY - HALO, 0.f, 1.f, 0.f, 0.f, 0.f};
+    Tile<W, H, NT, BORDER, SMT, ANGLE> T{S, p, k, 2 + tile_x * TX - HALO, 2 + tile_y * TY - HALO, 0.f, 1.f, 0.f, 0.f,
+                                         0.f};
     {
-        // uniform one-value textures are read once per thread
+        // uniform one-value textures are read once per thread; the north
+        // vector with the fast sine / cosine getNorth uses (K/CDKLM16_kernel.cu:78)
         const float a = __ldg(p.angle);
-        T.nX = sinf(a);
-        T.nY = cosf(a);
+        T.nX = __sinf(a);
+        T.nY = __cosf(a);
         if (CONST_F) T.f0 = __ldg(p.coriolis_f);
         if (SIMPLE_FORCING) {
             const float wt = p.wind_t;
@@ -852,7 +944,7 @@ __device__ __forceinline__ bool tile_on_border(const GocCdklmParams& p, int tile
     return x0 < 2 || y0 < 2 || x0 + TX + 2 * HALO > p.nx + 2 || y0 + TY + 2 * HALO > p.ny + 2;
 }
 
-template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING>
+template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING, bool ANGLE = false>
 __device__ __forceinline__ void cdklm_tile(const GocCdklmParams& p, const StepConst& k, float dt, int rk_step,
                                            int tile_x, int tile_y,
                                            const float* __restrict__ e_in, const float* __restrict__ hu_in,
@@ -861,11 +953,11 @@ __device__ __forceinline__ void cdklm_tile(const GocCdklmParams& p, const StepCo
                                            const float* __restrict__ Hi_g, int hi_pitch,
                                            const float* __restrict__ Hm_g, int hm_pitch, float* smem_raw) {
     if (tile_on_border<TX, TY, NSTAGE>(p, tile_x, tile_y))
-        cdklm_tile_body<TX, TY, NSTAGE, NT, CONST_F, SIMPLE_FORCING, true>(
+        cdklm_tile_body<TX, TY, NSTAGE, NT, CONST_F, SIMPLE_FORCING, true, false, ANGLE>(
             p, k, dt, rk_step, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, e_alt, hu_alt, hv_alt,
             pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw);
     else
-        cdklm_tile_body<TX, TY, NSTAGE, NT, CONST_F, SIMPLE_FORCING, false>(
+        cdklm_tile_body<TX, TY, NSTAGE, NT, CONST_F, SIMPLE_FORCING, false, false, ANGLE>(
             p, k, dt, rk_step, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, e_alt, hu_alt, hv_alt,
             pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw);
 }
@@ -899,17 +991,18 @@ __device__ __forceinline__ bool cdklm_strip_tile(const GocCdklmParams& p, const 
         pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, s1, side_in, side_out, tma, nz);
 }
 
-template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING>
-__global__ void __launch_bounds__(NT, 3)
+template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING, bool ANGLE = false>
+__global__ void __launch_bounds__(NT, ANGLE ? 2 : 3)
 cdklm_tile_kernel(const GocCdklmParams p, const StepConst k, float dt, int rk_step,
                   const float* __restrict__ e_in, const float* __restrict__ hu_in,
                   const float* __restrict__ hv_in, float* e_out, float* hu_out, float* hv_out,
                   float* e_alt, float* hu_alt, float* hv_alt, int pitch,
                   const float* __restrict__ Hi_g, int hi_pitch, const float* __restrict__ Hm_g, int hm_pitch) {
     extern __shared__ __align__(16) float smem_raw[];
-    cdklm_tile<TX, TY, NSTAGE, NT, CONST_F, SIMPLE_FORCING>(p, k, dt, rk_step, blockIdx.x, blockIdx.y, e_in, hu_in,
-                                                            hv_in, e_out, hu_out, hv_out, e_alt, hu_alt, hv_alt,
-                                                            pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw);
+    cdklm_tile<TX, TY, NSTAGE, NT, CONST_F, SIMPLE_FORCING, ANGLE>(p, k, dt, rk_step, blockIdx.x, blockIdx.y, e_in,
+                                                                   hu_in, hv_in, e_out, hu_out, hv_out, e_alt,
+                                                                   hu_alt, hv_alt, pitch, Hi_g, hi_pitch, Hm_g,
+                                                                   hm_pitch, smem_raw);
 }
 
 // Output tile of the step kernels and threads per CTA.
@@ -919,7 +1012,10 @@ constexpr int kTX = 32, kTY = 16, kNT = 256;
 // allow_open: open (sponge) boundaries, flags 3 and 4, whose ghost cells the
 // stage reads as stored - only the single-stage entry takes them, since the
 // sponge kernels act between the stages.
-inline int validate_params(const GocCdklmParams* p, const char* who, bool allow_open = false) {
+// allow_angle: a north-angle texture (more than one value), which only the
+// single-stage entry steps.
+inline int validate_params(const GocCdklmParams* p, const char* who, bool allow_open = false,
+                           bool allow_angle = false) {
     if (!p) return set_error(GOC_ERR_ARG, "%s: null params", who);
     if (p->nx < 1 || p->ny < 1) return set_error(GOC_ERR_ARG, "%s: nx, ny must be >= 1 (got %d, %d)", who, p->nx, p->ny);
     if (!(p->dx > 0.0f) || !(p->dy > 0.0f) || !(p->g > 0.0f))
@@ -936,13 +1032,19 @@ inline int validate_params(const GocCdklmParams* p, const char* who, bool allow_
         return set_error(GOC_ERR_ARG, "%s: periodic boundaries must come in opposite pairs", who);
     if (!p->coriolis_f || p->coriolis_nx < 1 || p->coriolis_ny < 1)
         return set_error(GOC_ERR_ARG, "%s: Coriolis texture missing", who);
-    if (!p->angle || p->angle_nx != 1 || p->angle_ny != 1)
-        return set_error(GOC_ERR_UNSUPPORTED, "%s: only a constant (1x1) angle texture is supported", who);
+    if (!p->angle || p->angle_nx < 1 || p->angle_ny < 1)
+        return set_error(GOC_ERR_ARG, "%s: angle texture missing", who);
+    if (!allow_angle && (p->angle_nx != 1 || p->angle_ny != 1))
+        return set_error(GOC_ERR_UNSUPPORTED,
+                         "%s: a north-angle texture is stepped stage by stage (goc_cdklm_stage); this entry takes a "
+                         "constant (1x1) angle", who);
     if (!p->wind_x_cur || !p->wind_x_next || !p->wind_y_cur || !p->wind_y_next ||
         p->wind_x_nx < 1 || p->wind_x_ny < 1 || p->wind_y_nx < 1 || p->wind_y_ny < 1)
         return set_error(GOC_ERR_ARG, "%s: wind stress textures missing", who);
     if (!p->atm_p_cur || !p->atm_p_next || p->atm_p_nx < 1 || p->atm_p_ny < 1)
         return set_error(GOC_ERR_ARG, "%s: atmospheric pressure textures missing", who);
+    if (p->atm_p_direct && (p->atm_p_nx != p->nx + 4 || p->atm_p_ny != p->ny + 4))
+        return set_error(GOC_ERR_ARG, "%s: direct lookup needs (ny+4) x (nx+4) pressure arrays", who);
     if ((p->bc_north == 2 && p->ny < 4) || (p->bc_east == 2 && p->nx < 4))
         return set_error(GOC_ERR_ARG, "%s: periodic directions need at least 4 interior cells", who);
     return GOC_OK;

@@ -61,6 +61,9 @@ class BatchedEnsemble:
         assert len(sims) > 0
         for s in sims:
             assert int(s.rk_order) == 2, "the batched engine runs the fused RK2 step"
+            if getattr(s, "angle_varies", False):
+                raise NotImplementedError("a north-angle texture is stepped stage by stage; step such members on "
+                                          "their own")
             if s.boundary_conditions.isSponge():
                 raise NotImplementedError("sponge boundaries act between the RK stages; step such members on their own")
         self.sims = list(sims)

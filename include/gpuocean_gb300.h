@@ -70,6 +70,10 @@ typedef struct GocCdklmParams {
     float wind_t;                   /* time interpolation weight in [0,1] */
     const float* atm_p_cur;  const float* atm_p_next; int32_t atm_p_nx, atm_p_ny;
     float atm_p_t;
+    /* 1: the pressure arrays are (ny+4) x (nx+4) and are read directly at the
+     * cells the central differences need instead of interpolated
+     * (USE_DIRECT_LOOKUP, K/external_forcing.cu:76-97, S/CDKLM16.py:123-133) */
+    int32_t atm_p_direct;
 } GocCdklmParams;
 
 /* ---------------- runtime plumbing (device memory, streams, timing) ------ */

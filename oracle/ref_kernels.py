@@ -54,7 +54,7 @@ def _f(x):
 def cdklm_defines(nx, ny, dx, dy, g=9.81, r=0.0, theta=1.8, rk_order=2, coriolis_shape=(1, 1),
                   angle_shape=(1, 1), desing_eps=0.1, flux_slope_eps=0.1, depth_cutoff=1e-5,
                   rho_o=1025.0, wind_stress_factor=1.0, flux_balancer=0.8, block=(12, 32),
-                  wind_shape=(1, 1), pressure_shape=(1, 1)):
+                  wind_shape=(1, 1), pressure_shape=(1, 1), direct_lookup=False):
     """S/CDKLM16.py:242-269 (one_dimensional False); texture shapes are (ny, nx)."""
     return {"block_width": block[0], "block_height": block[1],
             "KPSIMULATOR_DESING_EPS": _f(desing_eps), "KPSIMULATOR_FLUX_SLOPE_EPS": _f(flux_slope_eps),
@@ -67,7 +67,7 @@ def cdklm_defines(nx, ny, dx, dy, g=9.81, r=0.0, theta=1.8, rk_order=2, coriolis
             "ATMOS_PRES_NX": int(pressure_shape[1]), "ATMOS_PRES_NY": int(pressure_shape[0]),
             "WIND_STRESS_X_NX": int(wind_shape[1]), "WIND_STRESS_X_NY": int(wind_shape[0]),
             "WIND_STRESS_Y_NX": int(wind_shape[1]), "WIND_STRESS_Y_NY": int(wind_shape[0]),
-            "USE_DIRECT_LOOKUP": "False"}
+            "USE_DIRECT_LOOKUP": "True" if direct_lookup else "False"}
 
 
 def noise_defines(coriolis_shape=(1, 1), angle_shape=(1, 1), block=(16, 16), kl_rand=(1, 1)):
@@ -124,6 +124,11 @@ REF_CONFIGS = {
     # time-varying textured wind stress and atmospheric pressure on a 77 x 45 grid
     "cdklm_forcing77": ("CDKLM16_kernel.cu", cdklm_defines(77, 45, 150.0, 170.0, wind_shape=(5, 7),
                                                            pressure_shape=(6, 8)), CDKLM_FLAGS),
+    # a rotated grid: north-angle texture of 6 x 5 (nx x ny) values on a 64 x 48 grid
+    "cdklm_angle64": ("CDKLM16_kernel.cu", cdklm_defines(64, 48, 500.0, 500.0, angle_shape=(5, 6)), CDKLM_FLAGS),
+    # ... with a pressure array of the grid's own size read directly (S/CDKLM16.py:123-133)
+    "cdklm_direct77": ("CDKLM16_kernel.cu", cdklm_defines(77, 45, 150.0, 170.0, wind_shape=(5, 7),
+                                                          pressure_shape=(49, 81), direct_lookup=True), CDKLM_FLAGS),
     # ModelErrorKL with the default basis (1..10 x 1..10) and with the double-jet case's (2..8 x 1..7)
     "noise_kl10": ("ocean_noise.cu", noise_defines(kl_rand=(10, 20)), NOISE_FLAGS),
     "noise_kl7": ("ocean_noise.cu", noise_defines(kl_rand=(7, 14)), NOISE_FLAGS),

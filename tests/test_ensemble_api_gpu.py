@@ -167,7 +167,19 @@ def test_multilevel_step_to_observation_with_drifters(gpu_ctx):
     def levels():
         return [[mk(lv[0]) for _ in range(3)], [[mk(lv[1]) for _ in range(2)], [mk(lv[0]) for _ in range(2)]]]
 
+    class Quiet:
+        """Stands in for a model error that adds nothing: the reference's
+        dataAssimilationStep with a coarse partner calls perturbSimilarAs,
+        which needs one."""
+        def perturbSim(self, sim, **kw):
+            pass
+
+        def perturbSimSimilarAs(self, sim, **kw):
+            pass
+
     ml_sims, twin = levels(), levels()
+    for s in twin[1][0] + twin[1][1]:
+        s.model_error = Quiet()
     ml = MultiLevelOceanEnsemble(ml_sims)
     np.random.seed(9)
     start = np.array([[300e3, 400e3], [900e3, 200e3]])

@@ -41,7 +41,7 @@ def _bcdata(t, sides, n_ns, n_ew):
 
 
 def _run(ctx, config, bc_config, nx, ny, dx, dy, H, eta0, bc, sponge, bc_data, T, dt=0.0, f=0.0, wind=None,
-         pressure=None):
+         pressure=None, direct=False):
     from gpuocean_gb300.SWEsimulators import CDKLM16
     from gpuocean_gb300.utils import AtmosphericPressure, Common, WindStress
     z = np.zeros_like(eta0)
@@ -53,7 +53,7 @@ def _run(ctx, config, bc_config, nx, ny, dx, dy, H, eta0, bc, sponge, bc_data, T
                                                                             shiftValue=0)
     b = Common.BoundaryConditions(*bc, spongeCells=dict(zip(("north", "east", "south", "west"), sponge)))
     sim = CDKLM16.CDKLM16(ctx, eta0, z, z.copy(), H, nx, ny, dx, dy, dt, 9.81, f, 0.0, boundary_conditions=b,
-                          boundary_conditions_data=bc_data[0] if bc_data else None, **kw)
+                          boundary_conditions_data=bc_data[0] if bc_data else None, use_direct_lookup=direct, **kw)
     # the Coriolis and angle textures and the compensated f of the product's host
     ftex = sim.coriolis_f_arr.download(sim.gpu_stream)
     angle = sim.angle_arr.download(sim.gpu_stream)
@@ -136,4 +136,26 @@ def test_time_varying_textured_forcing(gpu_ctx):
     got, exp = _run(gpu_ctx, "cdklm_forcing77", "boundary", nx, ny, 150.0, 170.0, H, eta0, (1, 1, 1, 1),
                     (0, 0, 0, 0), None, 800.0, f=1.2e-4, wind=(tw, us, vs), pressure=(tp, ps))
     d = _report("time-varying textured wind stress and atmospheric pressure", got, exp)
+    assert max(d.values()) == 0.0
+
+
+def test_direct_lookup_pressure(gpu_ctx):
+    """use_direct_lookup: a pressure array of the grid's own size read at
+    the cells of the reference's central differences (its north and south
+    values taken one column east), against the reference kernel built with
+    USE_DIRECT_LOOKUP, two time stamps."""
+    nx, ny = 77, 45
+    rng = np.random.default_rng(12)
+    x = np.arange(nx + 4) - 2 + 0.5 - nx / 2.0
+    y = np.arange(ny + 4) - 2 + 0.5 - ny / 2.0
+    eta0 = (0.1 * np.exp(-(x[None, :] ** 2 + y[:, None] ** 2) / 80.0)).astype(np.float32)
+    H = (40.0 + 2.0 * rng.standard_normal((ny + 5, nx + 5))).astype(np.float32)
+    tw = [0.0]
+    us = [(1e-4 * rng.standard_normal((5, 7))).astype(np.float32)]
+    vs = [(1e-4 * rng.standard_normal((5, 7))).astype(np.float32)]
+    tp = [0.0, 600.0]
+    ps = [(80.0 * rng.standard_normal((ny + 4, nx + 4))).astype(np.float32) for _ in tp]
+    got, exp = _run(gpu_ctx, "cdklm_direct77", "boundary", nx, ny, 150.0, 170.0, H, eta0, (1, 1, 1, 1),
+                    (0, 0, 0, 0), None, 800.0, f=1.2e-4, wind=(tw, us, vs), pressure=(tp, ps), direct=True)
+    d = _report("atmospheric pressure by direct lookup", got, exp)
     assert max(d.values()) == 0.0
