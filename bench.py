@@ -622,7 +622,7 @@ def run_adjoint(ctx, n=256, n_steps=400, every=10, n_points=64):
         return a.elapsed_time(b) / reps
 
     t_step = timeit(lambda: adj.step(qa, qb))
-    t_vjp = timeit(lambda: adj.step_vjp(qa, qs, la, ls, ln))
+    t_vjp = timeit(lambda: adj.step_vjp(qa, qs, la, ls, ln, qb))   # qb: Q^{n+1} of qa
     out["kernels"] = {"step_ms": t_step, "step_vjp_ms": t_vjp, "vjp_over_step": t_vjp / t_step}
     sim.cleanUp()
     out["batched"] = run_adjoint_batched(ctx, ev, timeit)
@@ -677,7 +677,7 @@ def run_adjoint_batched(ctx, ev, timeit, n=128, members=128, n_steps=400, every=
     la, ls, ln = adj.zeros(), adj.zeros(), adj.zeros()
     la.normal_()
     t_step = timeit(lambda: adj.step(qa, qb))
-    t_vjp = timeit(lambda: adj.step_vjp(qa, qs, la, ls, ln))
+    t_vjp = timeit(lambda: adj.step_vjp(qa, qs, la, ls, ln, qb))   # qb: Q^{n+1} of qa
     sim.cleanUp()
     cells = members * n * n
     return {"config": f"{members} members x {n}x{n} bump, per-member wind, {n_steps} steps, (hu, hv) misfit at "

@@ -98,6 +98,11 @@ class CDKLM16(Simulator):
             assert r == 0.0, "3rd order Runge Kutta supported only without friction"
         wind = WindStress.WindStress() if wind is None else wind
         atmospheric_pressure = AtmosphericPressure.AtmosphericPressure() if atmospheric_pressure is None else atmospheric_pressure
+        # use_direct_lookup keeps the reference's shape check and nothing
+        # more: the reference passes the define as the Python literal True
+        # (U/Common.py:478), which the preprocessor's `#if USE_DIRECT_LOOKUP`
+        # (K/CDKLM16_kernel.cu:915) evaluates as 0, so its kernel always
+        # interpolates the pressure - as this step does
         if use_direct_lookup:
             assert atmospheric_pressure.P[0].shape[0] == ny + 4 and atmospheric_pressure.P[0].shape[1] == nx + 4, \
                 "Direct lookup is only supported for same sized grids"
@@ -231,7 +236,6 @@ class CDKLM16(Simulator):
         p.wind_y_nx, p.wind_y_ny = self.wind_stress_y_current_arr.nx_halo, self.wind_stress_y_current_arr.ny_halo
         p.atm_p_cur, p.atm_p_next = self.atmospheric_pressure_current_arr.ptr, self.atmospheric_pressure_next_arr.ptr
         p.atm_p_nx, p.atm_p_ny = self.atmospheric_pressure_current_arr.nx_halo, self.atmospheric_pressure_current_arr.ny_halo
-        p.atm_p_direct = int(self.use_direct_lookup)
         return p
 
     @property

@@ -46,7 +46,6 @@ class GocCdklmParams(ctypes.Structure):
         ("atm_p_cur", c_void_p), ("atm_p_next", c_void_p),
         ("atm_p_nx", ctypes.c_int32), ("atm_p_ny", ctypes.c_int32),
         ("atm_p_t", c_float),
-        ("atm_p_direct", ctypes.c_int32),
     ]
 
 
@@ -107,6 +106,11 @@ SIGNATURES = {
                                      c_void_p, c_void_p]),
     "goc_cdklm_stage_vjp": (c_int, [ctypes.POINTER(GocCdklmParams), c_float, c_int] + [c_void_p] * 18 +
                             [c_int, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
+    "goc_cdklm_stage_vjp_out": (c_int, [ctypes.POINTER(GocCdklmParams), c_float, c_int] + [c_void_p] * 21 +
+                                [c_int, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
+    "goc_cdklm_stage_vjp_members_out": (c_int, [ctypes.POINTER(GocCdklmParams), c_float, c_int] + [c_void_p] * 21 +
+                                        [c_int, ctypes.c_longlong, c_int, c_int, c_void_p, c_int, c_void_p, c_int,
+                                         c_void_p, c_void_p]),
     "goc_drift": (c_int, [c_int, c_int, c_float, c_float, c_float, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int,
                           c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_float,
                           c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_float, c_float, c_void_p]),

@@ -127,17 +127,31 @@ class StepAdjoint:
                   int(b.isPeriodicNorthSouth()), int(b.isPeriodicEastWest()), positions.shape[0], _ptr(positions), 8,
                   _ptr(pos_bar), 8, ctypes.c_float(1.0), *[_ptr(a) for a in lam], self._stream())
 
-    def step_vjp(self, q_n, q_star, lam_next, lam_star, lam_n):
+    def step_vjp(self, q_n, q_star, lam_next, lam_star, lam_n, q_next=None):
         """lam_n = (dQ^{n+1}/dQ^n)^T lam_next on interior cells; the wind-stress
-        gradient accumulates on the device (``wind_grad``)."""
+        gradient accumulates on the device (``wind_grad``).  With q_next
+        (Q^{n+1} as the forward step wrote it) the stage VJPs take the stage
+        outputs instead of recomputing the stages' fluxes."""
         s = self._stream()
         common = (self.pitch, self.Hi.ptr, int(self.Hi.pitch), self.Hm.ptr, int(self.Hm.pitch))
-        _lib.call("goc_cdklm_stage_vjp", ctypes.byref(self.params), ctypes.c_float(self.dt), 1,
-                  *[_ptr(a) for a in q_star], *[_ptr(a) for a in q_n], *[_ptr(a) for a in lam_next],
+        p = [_ptr(a) for a in q_n]
+        ps = [_ptr(a) for a in q_star]
+        if q_next is None:
+            _lib.call("goc_cdklm_stage_vjp", ctypes.byref(self.params), ctypes.c_float(self.dt), 1,
+                      *ps, *p, *[_ptr(a) for a in lam_next],
+                      None, None, None, *[_ptr(a) for a in lam_star], *[_ptr(a) for a in lam_n],
+                      *common, _ptr(self.partials[0]), s)
+            _lib.call("goc_cdklm_stage_vjp", ctypes.byref(self.params), ctypes.c_float(self.dt), 0,
+                      *p, None, None, None, *[_ptr(a) for a in lam_star],
+                      *[_ptr(a) for a in lam_n], *[_ptr(a) for a in lam_n], None, None, None,
+                      *common, _ptr(self.partials[1]), s)
+            return None
+        _lib.call("goc_cdklm_stage_vjp_out", ctypes.byref(self.params), ctypes.c_float(self.dt), 1,
+                  *ps, *p, *[_ptr(a) for a in q_next], *[_ptr(a) for a in lam_next],
                   None, None, None, *[_ptr(a) for a in lam_star], *[_ptr(a) for a in lam_n],
                   *common, _ptr(self.partials[0]), s)
-        _lib.call("goc_cdklm_stage_vjp", ctypes.byref(self.params), ctypes.c_float(self.dt), 0,
-                  *[_ptr(a) for a in q_n], None, None, None, *[_ptr(a) for a in lam_star],
+        _lib.call("goc_cdklm_stage_vjp_out", ctypes.byref(self.params), ctypes.c_float(self.dt), 0,
+                  *p, None, None, None, *ps, *[_ptr(a) for a in lam_star],
                   *[_ptr(a) for a in lam_n], *[_ptr(a) for a in lam_n], None, None, None,
                   *common, _ptr(self.partials[1]), s)
         return None
@@ -228,7 +242,7 @@ def _rollout_backward(ctx, grad, grad_pos):
             if pos_bar is not None:
                 # the drift after step n read the state after it
                 adj.drift_vjp(states[n + 1 - start], track[n], pos_bar, lam)
-            adj.step_vjp(states[n - start], stars[n - start], lam, lam_s, lam_n)
+            adj.step_vjp(states[n - start], stars[n - start], lam, lam_s, lam_n, states[n + 1 - start])
             lam, lam_n = lam_n, lam
         del states, stars
         ctx.segments[start] = None
@@ -327,18 +341,28 @@ class EnsembleStepAdjoint:
                   *self._p3(q_in), *self._p3(q_out), *self._p3(q_star), o.pitch, 3 * self.plane, self.n, 2,
                   o.Hi.ptr, int(o.Hi.pitch), o.Hm.ptr, int(o.Hm.pitch), o._stream())
 
-    def step_vjp(self, q_n, q_star, lam_next, lam_star, lam_n):
+    def step_vjp(self, q_n, q_star, lam_next, lam_star, lam_n, q_next=None):
         """lam_n = VJP of every member's step; the (n_members, 2) wind-stress
-        gradient accumulates on the device (``wind_grad``)."""
+        gradient accumulates on the device (``wind_grad``).  q_next: as in
+        ``StepAdjoint.step_vjp``."""
         o = self.one
         s = o._stream()
         common = (o.pitch, 3 * self.plane, self.n, 2, o.Hi.ptr, int(o.Hi.pitch), o.Hm.ptr, int(o.Hm.pitch))
-        _lib.call("goc_cdklm_stage_vjp_members", ctypes.byref(self.params), ctypes.c_float(self.dt), 1,
-                  *self._p3(q_star), *self._p3(q_n), *self._p3(lam_next), None, None, None, *self._p3(lam_star),
-                  *self._p3(lam_n), *common, ctypes.c_void_p(self.partials[0].data_ptr()), s)
-        _lib.call("goc_cdklm_stage_vjp_members", ctypes.byref(self.params), ctypes.c_float(self.dt), 0,
-                  *self._p3(q_n), None, None, None, *self._p3(lam_star), *self._p3(lam_n), *self._p3(lam_n),
-                  None, None, None, *common, ctypes.c_void_p(self.partials[1].data_ptr()), s)
+        w0, w1 = ctypes.c_void_p(self.partials[0].data_ptr()), ctypes.c_void_p(self.partials[1].data_ptr())
+        if q_next is None:
+            _lib.call("goc_cdklm_stage_vjp_members", ctypes.byref(self.params), ctypes.c_float(self.dt), 1,
+                      *self._p3(q_star), *self._p3(q_n), *self._p3(lam_next), None, None, None,
+                      *self._p3(lam_star), *self._p3(lam_n), *common, w0, s)
+            _lib.call("goc_cdklm_stage_vjp_members", ctypes.byref(self.params), ctypes.c_float(self.dt), 0,
+                      *self._p3(q_n), None, None, None, *self._p3(lam_star), *self._p3(lam_n), *self._p3(lam_n),
+                      None, None, None, *common, w1, s)
+            return None
+        _lib.call("goc_cdklm_stage_vjp_members_out", ctypes.byref(self.params), ctypes.c_float(self.dt), 1,
+                  *self._p3(q_star), *self._p3(q_n), *self._p3(q_next), *self._p3(lam_next), None, None, None,
+                  *self._p3(lam_star), *self._p3(lam_n), *common, w0, s)
+        _lib.call("goc_cdklm_stage_vjp_members_out", ctypes.byref(self.params), ctypes.c_float(self.dt), 0,
+                  *self._p3(q_n), None, None, None, *self._p3(q_star), *self._p3(lam_star), *self._p3(lam_n),
+                  *self._p3(lam_n), None, None, None, *common, w1, s)
         return None
 
     def reset_wind_grad(self):
@@ -405,7 +429,7 @@ class CDKLM16EnsembleRollout(torch.autograd.Function):
             for n in range(end - 1, start - 1, -1):
                 if (n + 1) % every == 0:
                     lam[:, :, 2:-2, 2:-2] += grad[(n + 1) // every - 1]
-                adj.step_vjp(states[n - start], stars[n - start], lam, lam_s, lam_n)
+                adj.step_vjp(states[n - start], stars[n - start], lam, lam_s, lam_n, states[n + 1 - start])
                 lam, lam_n = lam_n, lam
             del states, stars
             ctx.segments[start] = None
@@ -443,13 +467,14 @@ def _main(argv=None):
     for _ in range(20):
         adj.step(q0, q1, qs)
         q0, q1 = q1, q0
+    adj.step(q0, q1, qs)      # q1 = Q^{n+1}, qs = Q* of q0
     lam, ls, ln = adj.zeros(), adj.zeros(), adj.zeros()
     lam.normal_()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     torch.cuda.synchronize()
     ev[0].record()
     for _ in range(a.calls):
-        adj.step_vjp(q0, qs, lam, ls, ln)
+        adj.step_vjp(q0, qs, lam, ls, ln, q1)
     ev[1].record()
     for _ in range(a.calls):
         adj.step(q0, q1, qs)

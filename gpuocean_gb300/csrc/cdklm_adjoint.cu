@@ -2,20 +2,27 @@
 // points.  Compiled like the step (no FMA contraction) so that the forward
 // recompute inside the VJP reproduces the forward step bit for bit.
 #include <cstdio>
+#include <type_traits>
 
 #include "cdklm_adjoint.cuh"
 
 namespace goc {
 
 constexpr int kAX = 32, kAY = 16, kANT = 256;   // x-bar tile and threads per CTA
+constexpr int kAYSmall = 8;                      // tile height for grids that fill few SMs
 constexpr int kAHalo = 4;
 
-template <int TX, int TY, int NT, bool CONST_F, bool BORDER>
+// HAS_Y: the stage output y (ye, yu, yv) is given.  The cell pass then takes
+// the updated state from it instead of from the forward fluxes, and the
+// forward recompute stops after the slopes (the face pass recomputes each
+// flux it differentiates anyway).
+template <int TX, int TY, int NT, bool CONST_F, bool BORDER, bool HAS_Y>
 __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, float dt, int rk_step, int tile_x,
                                int tile_y, const float* __restrict__ xe, const float* __restrict__ xu,
                                const float* __restrict__ xv, const float* __restrict__ ae,
                                const float* __restrict__ au, const float* __restrict__ av,
-                               const float* __restrict__ ybe, const float* __restrict__ ybu,
+                               const float* __restrict__ ye, const float* __restrict__ yu,
+                               const float* __restrict__ yv, const float* __restrict__ ybe, const float* __restrict__ ybu,
                                const float* __restrict__ ybv, const float* __restrict__ bbe,
                                const float* __restrict__ bbu, const float* __restrict__ bbv, float* xbe, float* xbu,
                                float* xbv, float* abe, float* abu, float* abv, int pitch,
@@ -103,11 +110,14 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
     }
     __syncthreads();
 
-    // 3. forward recompute of the stage on the tile + 2
+    // 3. forward recompute of the stage on the tile + 2 (without y: with the
+    //    fluxes, which the cell pass needs for the updated state)
     T.template slopes<2, W - 2, 2, H - 2, CONST_F>();
     __syncthreads();
-    T.template faces<2, W - 2, 2, H - 2, CONST_F>();
-    __syncthreads();
+    if constexpr (!HAS_Y) {
+        T.template faces<2, W - 2, 2, H - 2, CONST_F>();
+        __syncthreads();
+    }
 
     // 4. cell pass: RK combination, friction and source terms in reverse.
     //    The flux-divergence adjoints stay in registers until every cell has
@@ -136,16 +146,37 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
                            gx < nx + 2 && gy < ny + 2);
         const size_t o = (size_t)gys * pitch + gxs;
         const float yb0 = __ldg(ybe + o), yb1 = __ldg(ybu + o), yb2 = __ldg(ybv + o);
-        float L1, L2, L3, ec, hu, hv, Hm, hsum;
-        T.template rhs<CONST_F, true>(i, j, gxs, gys, L1, L2, L3, ec, hu, hv, Hm, hsum);
+        float L1 = 0.f, L2 = 0.f, L3 = 0.f, ec, hu, hv, Hm, hsum;
+        if constexpr (HAS_Y)
+            T.cell_state(i, j, ec, hu, hv, Hm, hsum);
+        else
+            T.template rhs<CONST_F, true>(i, j, gxs, gys, L1, L2, L3, ec, hu, hv, Hm, hsum);
         const float C = T.friction(dt, hsum, hu, hv);
-        float ne, nhu, nhv, ecb, hub, hvb, L1b, L2b, L3b, Cb;
+        // the updated state before the final clamp, and whether the clamp
+        // dried the cell.  From y: a cell the clamp dried holds exactly
+        // (-Hm + cutoff, 0, 0) (finish_cell); a wet cell holds its updated
+        // momenta.  (A wet cell at rest whose eta the clamp raised to the
+        // same value reads as dry: a tie at the clamp's kink.)
+        bool ydry = false;
+        float ynu = 0.f, ynv = 0.f;
+        if constexpr (HAS_Y) {
+            const float ye0 = __ldg(ye + o);
+            ynu = __ldg(yu + o);
+            ynv = __ldg(yv + o);
+            ydry = (ynu == 0.0f && ynv == 0.0f && ye0 == -Hm + p.depth_cutoff);
+        }
+        float nhu, nhv, ecb, hub, hvb, L1b, L2b, L3b, Cb;
         float eab = 0.f, huab = 0.f, hvab = 0.f;
         if (rk_step == 0) {
-            ne = ec + dt * L1;
-            nhu = (hu + dt * L2) / (1.0f + C);
-            nhv = (hv + dt * L3) / (1.0f + C);
-            const bool dry = (ne + Hm <= p.depth_cutoff);
+            bool dry;
+            if constexpr (HAS_Y) {
+                nhu = ynu; nhv = ynv; dry = ydry;
+            } else {
+                const float ne = ec + dt * L1;
+                nhu = (hu + dt * L2) / (1.0f + C);
+                nhv = (hv + dt * L3) / (1.0f + C);
+                dry = (ne + Hm <= p.depth_cutoff);
+            }
             if (dry) continue;
             const float ic = 1.0f / (1.0f + C);
             ecb = yb0;
@@ -156,12 +187,17 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
             L3b = dt * hvb;
             Cb = -(yb1 * nhu + yb2 * nhv) * ic;
         } else {
-            const float ea = __ldg(ae + o), hua = __ldg(au + o), hva = __ldg(av + o);
             const float Dd = 1.0f + 0.5f * C;
-            ne = 0.5f * (ea + (ec + dt * L1));
-            nhu = 0.5f * (hua + (hu + dt * L2)) / Dd;
-            nhv = 0.5f * (hva + (hv + dt * L3)) / Dd;
-            const bool dry = (ne + Hm <= p.depth_cutoff);
+            bool dry;
+            if constexpr (HAS_Y) {
+                nhu = ynu; nhv = ynv; dry = ydry;
+            } else {
+                const float ea = __ldg(ae + o), hua = __ldg(au + o), hva = __ldg(av + o);
+                const float ne = 0.5f * (ea + (ec + dt * L1));
+                nhu = 0.5f * (hua + (hu + dt * L2)) / Dd;
+                nhv = 0.5f * (hva + (hv + dt * L3)) / Dd;
+                dry = (ne + Hm <= p.depth_cutoff);
+            }
             if (dry) {
                 if (core) {
                     abe[o] = 0.0f; abu[o] = 0.0f; abv[o] = 0.0f;
@@ -239,13 +275,24 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
     __syncthreads();
     auto FDb = [&](int c) -> float (&)[H][W] { return S.Gy[c]; };
 
+    // The reverse passes cover only what reaches the x-bar of the tile's
+    // cells (and of the wall-mirror positions that fold onto them): an x face
+    // or x slope changes the adjoints of its own row only, a y face or y
+    // slope those of its own column.  x faces and slopes therefore run on
+    // the tile's rows, y faces and slopes on its columns; along the pass
+    // direction the faces reach two cells beyond the tile, the slopes one.
+    // Faces between two ghost cells of a wall carry no adjoint (the cell
+    // pass leaves ghost cells out), so walls need no more.
+    constexpr int T0X = kAHalo, T1X = kAHalo + TX, T0Y = kAHalo, T1Y = kAHalo + TY;
+
     // 5. faces in reverse, two colours each.  x faces are coloured as a
     //    checkerboard ((i + j) even / odd): faces of one row never share a
     //    cell.  A warp takes 16 faces of a row and 16 of the next: the
     //    stride-2 accesses of one half-warp cover 32 consecutive floats, and
     //    the checkerboard puts the two rows on even and odd banks, so they do
     //    not conflict; the remaining faces of each row come afterwards.
-    constexpr int NXF = W - 3, NYF = H - 4;     // east faces of cells [1, W-2) on rows [2, H-2)
+    constexpr int FX0 = T0X - 2;                 // east faces of cells [T0X - 2, T1X + 1) on the tile's rows
+    constexpr int NXF = TX + 3, NYF = TY;
     constexpr int FPR = (NXF + 1) / 2;          // faces of one colour per row
     constexpr int FM = FPR < 16 ? FPR : 16, FR = FPR - FM;
     constexpr int NITEM = FM == 16 ? ((NYF + 1) / 2) * 32 + FR * NYF : FPR * NYF;
@@ -267,9 +314,9 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
                     row = q / (FR > 0 ? FR : 1); kf = FM + q % (FR > 0 ? FR : 1);
                 }
             }
-            const int j = 2 + row;
-            const int i = 1 + 2 * kf + ((j + colour) & 1);
-            if (i >= W - 2) continue;
+            const int j = T0Y + row;
+            const int i = FX0 + 2 * kf + ((j + colour) & 1);
+            if (i >= T1X + 1) continue;
             const float F0b = (FDb(0)[j][i] - FDb(0)[j][i + 1]) * k.inv_dx;
             const float F1b = (FDb(1)[j][i] - FDb(1)[j][i + 1]) * k.inv_dx;
             const float F2b = (FDb(2)[j][i] - FDb(2)[j][i + 1]) * k.inv_dx;
@@ -280,14 +327,14 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
     }
     // 6. x slopes in reverse (three colours); their adjoints are complete
     //    once the x faces are done
-    constexpr int NXS = W - 2, NYS = H - 4;     // x slopes of cells [1, W-1) on rows [2, H-2)
+    constexpr int NXS = TX + 2, NYS = TY;       // x slopes of cells [T0X - 1, T1X + 1) on the tile's rows
 #pragma unroll 1
     for (int colour = 0; colour < 3; ++colour) {
         constexpr int PERROW = (NXS + 2) / 3;
         for (int idx = threadIdx.x; idx < PERROW * NYS; idx += NT) {
-            const int i = 1 + colour + 3 * (idx % PERROW);
-            const int j = 2 + idx / PERROW;
-            if (i >= W - 1) continue;
+            const int i = T0X - 1 + colour + 3 * (idx % PERROW);
+            const int j = T0Y + idx / PERROW;
+            if (i >= T1X + 1) continue;
             R.template slope_x_vjp<CONST_F>(i, j);
         }
         __syncthreads();
@@ -301,13 +348,13 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
     __syncthreads();
     // 7. y faces and y slopes in reverse
     if (!p.one_dimensional) {
-        constexpr int NXG = W - 4, NYG = H - 3;   // north faces of cells [2, W-2) on rows [1, H-2)
+        constexpr int NXG = TX, NYG = TY + 3;     // north faces of rows [T0Y - 2, T1Y + 1) on the tile's columns
 #pragma unroll 1
         for (int colour = 0; colour < 2; ++colour) {
             for (int idx = threadIdx.x; idx < NXG * ((NYG + 1) / 2); idx += NT) {
-                const int i = 2 + idx % NXG;
-                const int j = 1 + colour + 2 * (idx / NXG);
-                if (j >= H - 2) continue;
+                const int i = T0X + idx % NXG;
+                const int j = T0Y - 2 + colour + 2 * (idx / NXG);
+                if (j >= T1Y + 1) continue;
                 const float G0b = (FDb(0)[j][i] - FDb(0)[j + 1][i]) * k.inv_dy;
                 const float G1b = (FDb(1)[j][i] - FDb(1)[j + 1][i]) * k.inv_dy;
                 const float G2b = (FDb(2)[j][i] - FDb(2)[j + 1][i]) * k.inv_dy;
@@ -318,24 +365,26 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
         }
     }
 
-    constexpr int NXY = W - 4, NYY = H - 2;     // y slopes of cells [2, W-2) on rows [1, H-1)
+    constexpr int NXY = TX, NYY = TY + 2;       // y slopes of rows [T0Y - 1, T1Y + 1) on the tile's columns
 #pragma unroll 1
     for (int colour = 0; colour < 3; ++colour) {
         constexpr int PERCOL = (NYY + 2) / 3;
         for (int idx = threadIdx.x; idx < NXY * PERCOL; idx += NT) {
-            const int i = 2 + idx % NXY;
-            const int j = 1 + colour + 3 * (idx / NXY);
-            if (j >= H - 1) continue;
+            const int i = T0X + idx % NXY;
+            const int j = T0Y - 1 + colour + 3 * (idx / NXY);
+            if (j >= T1Y + 1) continue;
             R.template slope_y_vjp<CONST_F>(i, j);
         }
         __syncthreads();
     }
 
-    // 8. desingularisation in reverse at every staged position, as the
-    //    adjoint of the memory cell it read (signs of the wall mirrors); the
-    //    result per position goes to the Gy planes
-    for (int idx = threadIdx.x; idx < H * W; idx += NT) {
-        const int i = idx % W, j = idx / W;
+    // 8. desingularisation in reverse at the tile's positions (border tiles:
+    //    also the two rings around it, where the wall mirrors of its cells
+    //    lie), as the adjoint of the memory cell each read (signs of the wall
+    //    mirrors); the result per position goes to the Gy planes
+    constexpr int DR = BORDER ? 2 : 0, DW = TX + 2 * DR, DH = TY + 2 * DR;
+    for (int idx = threadIdx.x; idx < DW * DH; idx += NT) {
+        const int i = T0X - DR + idx % DW, j = T0Y - DR + idx / DW;
         const float d0 = A.Db[0][j][i], d1 = A.Db[1][j][i], d2 = A.Db[2][j][i];
         float eb = 0.f, hub = 0.f, hvb = 0.f;
         if (d0 != 0.0f || d1 != 0.0f || d2 != 0.0f) {
@@ -397,25 +446,28 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
     }
 }
 
-template <bool CONST_F>
+template <bool CONST_F, bool HAS_Y, int TY>
 __global__ void __launch_bounds__(kANT, CONST_F ? 3 : 2)
 stage_vjp_kernel(const GocCdklmParams p, const StepConst k, float dt, int rk_step, const float* xe, const float* xu,
-                 const float* xv, const float* ae, const float* au, const float* av, const float* ybe,
+                 const float* xv, const float* ae, const float* au, const float* av, const float* ye,
+                 const float* yu, const float* yv, const float* ybe,
                  const float* ybu, const float* ybv, const float* bbe, const float* bbu, const float* bbv,
                  float* xbe, float* xbu, float* xbv, float* abe, float* abu, float* abv, int pitch,
                  const float* Hi_g, int hi_pitch, const float* Hm_g, int hm_pitch, float* wind_partials) {
     extern __shared__ __align__(16) float smem_raw[];
     const int tx = blockIdx.x, ty = blockIdx.y;
-    const int x0 = 2 + tx * kAX - kAHalo, y0 = 2 + ty * kAY - kAHalo;
-    const bool border = x0 < 2 || y0 < 2 || x0 + kAX + 2 * kAHalo > p.nx + 2 || y0 + kAY + 2 * kAHalo > p.ny + 2;
+    const int x0 = 2 + tx * kAX - kAHalo, y0 = 2 + ty * TY - kAHalo;
+    const bool border = x0 < 2 || y0 < 2 || x0 + kAX + 2 * kAHalo > p.nx + 2 || y0 + TY + 2 * kAHalo > p.ny + 2;
     if (border)
-        stage_vjp_body<kAX, kAY, kANT, CONST_F, true>(p, k, dt, rk_step, tx, ty, xe, xu, xv, ae, au, av, ybe, ybu,
-                                                      ybv, bbe, bbu, bbv, xbe, xbu, xbv, abe, abu, abv, pitch, Hi_g,
-                                                      hi_pitch, Hm_g, hm_pitch, wind_partials, smem_raw);
+        stage_vjp_body<kAX, TY, kANT, CONST_F, true, HAS_Y>(p, k, dt, rk_step, tx, ty, xe, xu, xv, ae, au, av, ye,
+                                                             yu, yv, ybe, ybu, ybv, bbe, bbu, bbv, xbe, xbu, xbv, abe,
+                                                             abu, abv, pitch, Hi_g, hi_pitch, Hm_g, hm_pitch,
+                                                             wind_partials, smem_raw);
     else
-        stage_vjp_body<kAX, kAY, kANT, CONST_F, false>(p, k, dt, rk_step, tx, ty, xe, xu, xv, ae, au, av, ybe, ybu,
-                                                       ybv, bbe, bbu, bbv, xbe, xbu, xbv, abe, abu, abv, pitch, Hi_g,
-                                                       hi_pitch, Hm_g, hm_pitch, wind_partials, smem_raw);
+        stage_vjp_body<kAX, TY, kANT, CONST_F, false, HAS_Y>(p, k, dt, rk_step, tx, ty, xe, xu, xv, ae, au, av, ye,
+                                                              yu, yv, ybe, ybu, ybv, bbe, bbu, bbv, xbe, xbu, xbv,
+                                                              abe, abu, abv, pitch, Hi_g, hi_pitch, Hm_g, hm_pitch,
+                                                              wind_partials, smem_raw);
 }
 
 // Tile of position q when the ntx x nty tiles are taken interior tiles first
@@ -456,11 +508,11 @@ __device__ __forceinline__ void interior_first_tile(int q, int ntx, int nty, int
 // position b / n_members of the interior-first order: while the interior
 // tiles of all members last, every CTA runs the interior code (the kernel is
 // sensitive to the instruction cache).
-template <bool CONST_F>
+template <bool CONST_F, bool HAS_Y, int TY>
 __global__ void __launch_bounds__(kANT, CONST_F ? 3 : 2)
 stage_vjp_members_kernel(const GocCdklmParams p, const StepConst k, float dt, int rk_step, const float* xe,
                          const float* xu, const float* xv, const float* ae, const float* au, const float* av,
-                         const float* ybe, const float* ybu, const float* ybv, const float* bbe, const float* bbu,
+                         const float* ye, const float* yu, const float* yv, const float* ybe, const float* ybu, const float* ybv, const float* bbe, const float* bbu,
                          const float* bbv, float* xbe, float* xbu, float* xbv, float* abe, float* abu, float* abv,
                          int pitch, long long member_stride, int wind_stride, const float* Hi_g, int hi_pitch,
                          const float* Hm_g, int hm_pitch, float* wind_partials, int partials_stride,
@@ -468,7 +520,7 @@ stage_vjp_members_kernel(const GocCdklmParams p, const StepConst k, float dt, in
     extern __shared__ __align__(16) float smem_raw[];
     const int member = (int)(blockIdx.x % (unsigned)n_members);
     int tx, ty;
-    interior_first_tile((int)(blockIdx.x / (unsigned)n_members), (p.nx + kAX - 1) / kAX, (p.ny + kAY - 1) / kAY,
+    interior_first_tile((int)(blockIdx.x / (unsigned)n_members), (p.nx + kAX - 1) / kAX, (p.ny + TY - 1) / TY,
                         inner.x, inner.y, inner.z, inner.w, tx, ty);
     const size_t o = (size_t)member * (size_t)member_stride;
     GocCdklmParams pm = p;
@@ -479,18 +531,18 @@ stage_vjp_members_kernel(const GocCdklmParams p, const StepConst k, float dt, in
     auto sh = [&](const float* q) { return q ? q + o : q; };
     auto shw = [&](float* q) { return q ? q + o : q; };
     float* wp = wind_partials ? wind_partials + (size_t)member * partials_stride : nullptr;
-    const int x0 = 2 + tx * kAX - kAHalo, y0 = 2 + ty * kAY - kAHalo;
-    const bool border = x0 < 2 || y0 < 2 || x0 + kAX + 2 * kAHalo > p.nx + 2 || y0 + kAY + 2 * kAHalo > p.ny + 2;
+    const int x0 = 2 + tx * kAX - kAHalo, y0 = 2 + ty * TY - kAHalo;
+    const bool border = x0 < 2 || y0 < 2 || x0 + kAX + 2 * kAHalo > p.nx + 2 || y0 + TY + 2 * kAHalo > p.ny + 2;
     if (border)
-        stage_vjp_body<kAX, kAY, kANT, CONST_F, true>(pm, k, dt, rk_step, tx, ty, sh(xe), sh(xu), sh(xv), sh(ae),
-                                                      sh(au), sh(av), sh(ybe), sh(ybu), sh(ybv), sh(bbe), sh(bbu),
-                                                      sh(bbv), shw(xbe), shw(xbu), shw(xbv), shw(abe), shw(abu),
-                                                      shw(abv), pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, wp, smem_raw);
+        stage_vjp_body<kAX, TY, kANT, CONST_F, true, HAS_Y>(
+            pm, k, dt, rk_step, tx, ty, sh(xe), sh(xu), sh(xv), sh(ae), sh(au), sh(av), sh(ye), sh(yu), sh(yv),
+            sh(ybe), sh(ybu), sh(ybv), sh(bbe), sh(bbu), sh(bbv), shw(xbe), shw(xbu), shw(xbv), shw(abe), shw(abu),
+            shw(abv), pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, wp, smem_raw);
     else
-        stage_vjp_body<kAX, kAY, kANT, CONST_F, false>(pm, k, dt, rk_step, tx, ty, sh(xe), sh(xu), sh(xv), sh(ae),
-                                                       sh(au), sh(av), sh(ybe), sh(ybu), sh(ybv), sh(bbe), sh(bbu),
-                                                       sh(bbv), shw(xbe), shw(xbu), shw(xbv), shw(abe), shw(abu),
-                                                       shw(abv), pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, wp, smem_raw);
+        stage_vjp_body<kAX, TY, kANT, CONST_F, false, HAS_Y>(
+            pm, k, dt, rk_step, tx, ty, sh(xe), sh(xu), sh(xv), sh(ae), sh(au), sh(av), sh(ye), sh(yu), sh(yv),
+            sh(ybe), sh(ybu), sh(ybv), sh(bbe), sh(bbu), sh(bbv), shw(xbe), shw(xbu), shw(xbv), shw(abe), shw(abu),
+            shw(abv), pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, wp, smem_raw);
 }
 
 static int vjp_check(const GocCdklmParams* p, int pitch, int Hi_pitch, int Hm_pitch, const char* who) {
@@ -512,37 +564,158 @@ static int vjp_check(const GocCdklmParams* p, int pitch, int Hi_pitch, int Hm_pi
     return GOC_OK;
 }
 
-template <bool CF>
-static int launch_vjp(const GocCdklmParams* p, const StepConst& k, float dt, int rk, const float* xe,
-                      const float* xu, const float* xv, const float* ae, const float* au, const float* av,
-                      const float* ybe, const float* ybu, const float* ybv, const float* bbe, const float* bbu,
-                      const float* bbv, float* xbe, float* xbu, float* xbv, float* abe, float* abu, float* abv,
-                      int pitch_f, const float* Hi, int hip_f, const float* Hm, int hmp_f, float* wind,
-                      cudaStream_t st) {
-    constexpr int W = kAX + 2 * kAHalo, H = kAY + 2 * kAHalo;
-    constexpr size_t smem = sizeof(AdjSmem<W, H, !CF>);
-    auto kern = stage_vjp_kernel<CF>;
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return set_error(GOC_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
-        configured = true;
+// Dynamic shared memory above 48 KB is opted into once per kernel.
+template <class K>
+static int configure_smem(K kern, size_t smem) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return set_error(GOC_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+    return GOC_OK;
+}
+
+// The buffers of one stage VJP call (device pointers; y may be null).
+struct VjpBuffers {
+    const float *xe, *xu, *xv, *ae, *au, *av, *ye, *yu, *yv, *ybe, *ybu, *ybv, *bbe, *bbu, *bbv;
+    float *xbe, *xbu, *xbv, *abe, *abu, *abv;
+};
+
+static int vjp_args(const GocCdklmParams* p, int rk_step, const VjpBuffers& b, int pitch, int Hi_pitch,
+                    int Hm_pitch, const float* Hi, const float* Hm, const char* who) {
+    int rc = vjp_check(p, pitch, Hi_pitch, Hm_pitch, who);
+    if (rc) return rc;
+    if (rk_step != 0 && rk_step != 1) return set_error(GOC_ERR_ARG, "%s: rk_step must be 0 or 1", who);
+    if (!b.xe || !b.xu || !b.xv || !b.ybe || !b.ybu || !b.ybv || !b.xbe || !b.xbu || !b.xbv || !Hi || !Hm)
+        return set_error(GOC_ERR_ARG, "%s: null buffer", who);
+    if (rk_step == 1 && (!b.ae || !b.au || !b.av || !b.abe || !b.abu || !b.abv))
+        return set_error(GOC_ERR_ARG, "%s: the second stage needs Q^n and its adjoint output", who);
+    if ((b.bbe || b.bbu || b.bbv) && !(b.bbe && b.bbu && b.bbv))
+        return set_error(GOC_ERR_ARG, "%s: base must be all three arrays or none", who);
+    if ((b.ye || b.yu || b.yv) && !(b.ye && b.yu && b.yv))
+        return set_error(GOC_ERR_ARG, "%s: the stage output must be all three arrays or none", who);
+    if (b.xbe == b.ybe || b.xbe == b.xe)
+        return set_error(GOC_ERR_ARG, "%s: x-bar must not alias x or y-bar", who);
+    return GOC_OK;
+}
+
+// Calls f(CF, HY, TY) with the three as compile-time constants
+// (std::integral_constant values): constant Coriolis, stage output given,
+// tile height.
+template <class F>
+static int dispatch_vjp(bool cf, bool hy, bool small, F&& f) {
+    using T = std::true_type;
+    using N = std::false_type;
+    using S = std::integral_constant<int, kAYSmall>;
+    using L = std::integral_constant<int, kAY>;
+    if (cf) {
+        if (hy) return small ? f(T{}, T{}, S{}) : f(T{}, T{}, L{});
+        return small ? f(T{}, N{}, S{}) : f(T{}, N{}, L{});
     }
-    dim3 grid((p->nx + kAX - 1) / kAX, (p->ny + kAY - 1) / kAY);
-    kern<<<grid, kANT, smem, st>>>(*p, k, dt, rk, xe, xu, xv, ae, au, av, ybe, ybu, ybv, bbe, bbu, bbv, xbe, xbu,
-                                   xbv, abe, abu, abv, pitch_f, Hi, hip_f, Hm, hmp_f, wind);
-    count_launch();
-    return check_launch("stage_vjp_kernel");
+    if (hy) return small ? f(N{}, T{}, S{}) : f(N{}, T{}, L{});
+    return small ? f(N{}, N{}, S{}) : f(N{}, N{}, L{});
+}
+
+// Tiles of kAY rows fill the GPU's SMs less than twice over: the launch
+// then takes tiles of kAYSmall rows, twice as many CTAs, each with about
+// 0.6 of the work (a launch of a few CTAs per SM is bound by one CTA's
+// latency, not by throughput).
+static bool small_tiles(const GocCdklmParams* p, int n_members) {
+    static int sms[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int& n = sms[dev & 63];
+    if (n == 0 && cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) n = 0;
+    const long long tiles = (long long)((p->nx + kAX - 1) / kAX) * ((p->ny + kAY - 1) / kAY) * n_members;
+    return n > 0 && tiles < 2LL * n;
+}
+
+// Wind partials: one (x, y) pair per tile of the smaller tile height, so the
+// count covers either launch.
+static int goc_cdklm_vjp_partials_count(int nx, int ny) {
+    if (nx < 1 || ny < 1) return 0;
+    return 2 * ((nx + kAX - 1) / kAX) * ((ny + kAYSmall - 1) / kAYSmall);
+}
+
+static int stage_vjp_impl(const GocCdklmParams* p, float dt, int rk_step, const VjpBuffers& b, int pitch,
+                          const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch, float* wind_partials,
+                          void* stream, const char* who) {
+    int rc = vjp_args(p, rk_step, b, pitch, Hi_pitch, Hm_pitch, Hi, Hm, who);
+    if (rc) return rc;
+    const StepConst k = make_step_const(*p);
+    const bool cf = (p->coriolis_nx == 1 && p->coriolis_ny == 1);
+    cudaStream_t st = as_stream(stream);
+    const int pf = pitch / 4, hip = Hi_pitch / 4, hmp = Hm_pitch / 4;
+    return dispatch_vjp(cf, b.ye != nullptr, small_tiles(p, 1), [&](auto CF, auto HY, auto TY) -> int {
+        constexpr int W = kAX + 2 * kAHalo, H = decltype(TY)::value + 2 * kAHalo;
+        constexpr size_t smem = sizeof(AdjSmem<W, H, !decltype(CF)::value>);
+        auto kern = stage_vjp_kernel<decltype(CF)::value, decltype(HY)::value, decltype(TY)::value>;
+        static bool configured = false;
+        if (!configured) {
+            if (int e = configure_smem(kern, smem)) return e;
+            configured = true;
+        }
+        const dim3 grid((p->nx + kAX - 1) / kAX, (p->ny + TY - 1) / TY);
+        kern<<<grid, kANT, smem, st>>>(*p, k, dt, rk_step, b.xe, b.xu, b.xv, b.ae, b.au, b.av, b.ye, b.yu, b.yv,
+                                       b.ybe, b.ybu, b.ybv, b.bbe, b.bbu, b.bbv, b.xbe, b.xbu, b.xbv, b.abe, b.abu,
+                                       b.abv, pf, Hi, hip, Hm, hmp, wind_partials);
+        count_launch();
+        return check_launch("stage_vjp_kernel");
+    });
+}
+
+static int stage_vjp_members_impl(const GocCdklmParams* p, float dt, int rk_step, const VjpBuffers& b, int pitch,
+                                  long long member_stride, int n_members, int wind_stride, const float* Hi,
+                                  int Hi_pitch, const float* Hm, int Hm_pitch, float* wind_partials, void* stream,
+                                  const char* who) {
+    int rc = vjp_args(p, rk_step, b, pitch, Hi_pitch, Hm_pitch, Hi, Hm, who);
+    if (rc) return rc;
+    if (n_members < 1 || n_members > 65535 || member_stride < (long long)(p->ny + 4) * (pitch / 4) || wind_stride < 0)
+        return set_error(GOC_ERR_ARG, "%s: bad member count or stride", who);
+    const StepConst k = make_step_const(*p);
+    const bool cf = (p->coriolis_nx == 1 && p->coriolis_ny == 1);
+    cudaStream_t st = as_stream(stream);
+    const int partials = goc_cdklm_vjp_partials_count(p->nx, p->ny);
+    const int pf = pitch / 4, hip = Hi_pitch / 4, hmp = Hm_pitch / 4;
+    return dispatch_vjp(cf, b.ye != nullptr, small_tiles(p, n_members), [&](auto CF, auto HY, auto TY) -> int {
+        constexpr int ty = decltype(TY)::value;
+        // interior tile rectangle (contiguous in x and in y)
+        const int ntx = (p->nx + kAX - 1) / kAX, nty = (p->ny + ty - 1) / ty;
+        int4 inner = make_int4(0, 0, 0, 0);
+        for (int t = 0, first = -1; t < ntx; ++t) {
+            const int x0 = 2 + t * kAX - kAHalo;
+            if (x0 >= 2 && x0 + kAX + 2 * kAHalo <= p->nx + 2) {
+                if (first < 0) first = inner.x = t;
+                inner.y = t + 1;
+            }
+        }
+        for (int t = 0, first = -1; t < nty; ++t) {
+            const int y0 = 2 + t * ty - kAHalo;
+            if (y0 >= 2 && y0 + ty + 2 * kAHalo <= p->ny + 2) {
+                if (first < 0) first = inner.z = t;
+                inner.w = t + 1;
+            }
+        }
+        constexpr int W = kAX + 2 * kAHalo, H = ty + 2 * kAHalo;
+        constexpr size_t smem = sizeof(AdjSmem<W, H, !decltype(CF)::value>);
+        auto kern = stage_vjp_members_kernel<decltype(CF)::value, decltype(HY)::value, ty>;
+        static bool configured = false;
+        if (!configured) {
+            if (int e = configure_smem(kern, smem)) return e;
+            configured = true;
+        }
+        const dim3 grid((unsigned)(ntx * nty) * (unsigned)n_members);
+        kern<<<grid, kANT, smem, st>>>(*p, k, dt, rk_step, b.xe, b.xu, b.xv, b.ae, b.au, b.av, b.ye, b.yu, b.yv,
+                                       b.ybe, b.ybu, b.ybv, b.bbe, b.bbu, b.bbv, b.xbe, b.xbu, b.xbv, b.abe, b.abu,
+                                       b.abv, pf, member_stride, wind_stride, Hi, hip, Hm, hmp, wind_partials,
+                                       partials, n_members, inner);
+        count_launch();
+        return check_launch("stage_vjp_members_kernel");
+    });
 }
 
 }  // namespace goc
 
 using namespace goc;
 
-extern "C" int goc_cdklm_vjp_partials(int nx, int ny) {
-    if (nx < 1 || ny < 1) return 0;
-    return 2 * ((nx + kAX - 1) / kAX) * ((ny + kAY - 1) / kAY);
-}
+extern "C" int goc_cdklm_vjp_partials(int nx, int ny) { return goc_cdklm_vjp_partials_count(nx, ny); }
 
 extern "C" int goc_cdklm_stage_vjp(const GocCdklmParams* p, float dt, int rk_step, const float* x_eta,
                                    const float* x_hu, const float* x_hv, const float* a_eta, const float* a_hu,
@@ -551,28 +724,25 @@ extern "C" int goc_cdklm_stage_vjp(const GocCdklmParams* p, float dt, int rk_ste
                                    float* xb_eta, float* xb_hu, float* xb_hv, float* ab_eta, float* ab_hu,
                                    float* ab_hv, int pitch, const float* Hi, int Hi_pitch, const float* Hm,
                                    int Hm_pitch, float* wind_partials, void* stream) {
-    int rc = vjp_check(p, pitch, Hi_pitch, Hm_pitch, "goc_cdklm_stage_vjp");
-    if (rc) return rc;
-    if (rk_step != 0 && rk_step != 1) return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp: rk_step must be 0 or 1");
-    if (!x_eta || !x_hu || !x_hv || !yb_eta || !yb_hu || !yb_hv || !xb_eta || !xb_hu || !xb_hv || !Hi || !Hm)
-        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp: null buffer");
-    if (rk_step == 1 && (!a_eta || !a_hu || !a_hv || !ab_eta || !ab_hu || !ab_hv))
-        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp: the second stage needs Q^n and its adjoint output");
-    if ((base_eta || base_hu || base_hv) && !(base_eta && base_hu && base_hv))
-        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp: base must be all three arrays or none");
-    if (xb_eta == yb_eta || xb_eta == x_eta)
-        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp: x-bar must not alias x or y-bar");
-    const StepConst k = make_step_const(*p);
-    const bool cf = (p->coriolis_nx == 1 && p->coriolis_ny == 1);
-    cudaStream_t st = as_stream(stream);
-    const int pf = pitch / 4, hip = Hi_pitch / 4, hmp = Hm_pitch / 4;
-    if (cf)
-        return launch_vjp<true>(p, k, dt, rk_step, x_eta, x_hu, x_hv, a_eta, a_hu, a_hv, yb_eta, yb_hu, yb_hv,
-                                base_eta, base_hu, base_hv, xb_eta, xb_hu, xb_hv, ab_eta, ab_hu, ab_hv, pf, Hi, hip,
-                                Hm, hmp, wind_partials, st);
-    return launch_vjp<false>(p, k, dt, rk_step, x_eta, x_hu, x_hv, a_eta, a_hu, a_hv, yb_eta, yb_hu, yb_hv,
-                             base_eta, base_hu, base_hv, xb_eta, xb_hu, xb_hv, ab_eta, ab_hu, ab_hv, pf, Hi, hip, Hm,
-                             hmp, wind_partials, st);
+    const VjpBuffers b{x_eta, x_hu, x_hv, a_eta, a_hu, a_hv, nullptr, nullptr, nullptr, yb_eta, yb_hu, yb_hv,
+                       base_eta, base_hu, base_hv, xb_eta, xb_hu, xb_hv, ab_eta, ab_hu, ab_hv};
+    return stage_vjp_impl(p, dt, rk_step, b, pitch, Hi, Hi_pitch, Hm, Hm_pitch, wind_partials, stream,
+                          "goc_cdklm_stage_vjp");
+}
+
+extern "C" int goc_cdklm_stage_vjp_out(const GocCdklmParams* p, float dt, int rk_step, const float* x_eta,
+                                       const float* x_hu, const float* x_hv, const float* a_eta, const float* a_hu,
+                                       const float* a_hv, const float* y_eta, const float* y_hu, const float* y_hv,
+                                       const float* yb_eta, const float* yb_hu, const float* yb_hv,
+                                       const float* base_eta, const float* base_hu, const float* base_hv,
+                                       float* xb_eta, float* xb_hu, float* xb_hv, float* ab_eta, float* ab_hu,
+                                       float* ab_hv, int pitch, const float* Hi, int Hi_pitch, const float* Hm,
+                                       int Hm_pitch, float* wind_partials, void* stream) {
+    if (!y_eta || !y_hu || !y_hv) return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp_out: null stage output");
+    const VjpBuffers b{x_eta, x_hu, x_hv, a_eta, a_hu, a_hv, y_eta, y_hu, y_hv, yb_eta, yb_hu, yb_hv,
+                       base_eta, base_hu, base_hv, xb_eta, xb_hu, xb_hv, ab_eta, ab_hu, ab_hv};
+    return stage_vjp_impl(p, dt, rk_step, b, pitch, Hi, Hi_pitch, Hm, Hm_pitch, wind_partials, stream,
+                          "goc_cdklm_stage_vjp_out");
 }
 
 extern "C" int goc_cdklm_stage_vjp_members(const GocCdklmParams* p, float dt, int rk_step, const float* x_eta,
@@ -584,64 +754,26 @@ extern "C" int goc_cdklm_stage_vjp_members(const GocCdklmParams* p, float dt, in
                                            long long member_stride, int n_members, int wind_stride,
                                            const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch,
                                            float* wind_partials, void* stream) {
-    int rc = vjp_check(p, pitch, Hi_pitch, Hm_pitch, "goc_cdklm_stage_vjp_members");
-    if (rc) return rc;
-    if (rk_step != 0 && rk_step != 1)
-        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp_members: rk_step must be 0 or 1");
-    if (!x_eta || !x_hu || !x_hv || !yb_eta || !yb_hu || !yb_hv || !xb_eta || !xb_hu || !xb_hv || !Hi || !Hm)
-        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp_members: null buffer");
-    if (rk_step == 1 && (!a_eta || !a_hu || !a_hv || !ab_eta || !ab_hu || !ab_hv))
-        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp_members: the second stage needs Q^n and its adjoint");
-    if ((base_eta || base_hu || base_hv) && !(base_eta && base_hu && base_hv))
-        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp_members: base must be all three arrays or none");
-    if (xb_eta == yb_eta || xb_eta == x_eta)
-        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp_members: x-bar must not alias x or y-bar");
-    if (n_members < 1 || n_members > 65535 || member_stride < (long long)(p->ny + 4) * (pitch / 4) || wind_stride < 0)
-        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp_members: bad member count or stride");
-    const StepConst k = make_step_const(*p);
-    const bool cf = (p->coriolis_nx == 1 && p->coriolis_ny == 1);
-    cudaStream_t st = as_stream(stream);
-    constexpr int W = kAX + 2 * kAHalo, H = kAY + 2 * kAHalo;
-    const size_t smem = cf ? sizeof(AdjSmem<W, H, false>) : sizeof(AdjSmem<W, H, true>);
-    const int partials = goc_cdklm_vjp_partials(p->nx, p->ny);
-    // interior tile rectangle (contiguous in x and in y)
-    const int ntx = (p->nx + kAX - 1) / kAX, nty = (p->ny + kAY - 1) / kAY;
-    int4 inner = make_int4(0, 0, 0, 0);
-    for (int t = 0, first = -1; t < ntx; ++t) {
-        const int x0 = 2 + t * kAX - kAHalo;
-        if (x0 >= 2 && x0 + kAX + 2 * kAHalo <= p->nx + 2) {
-            if (first < 0) first = inner.x = t;
-            inner.y = t + 1;
-        }
-    }
-    for (int t = 0, first = -1; t < nty; ++t) {
-        const int y0 = 2 + t * kAY - kAHalo;
-        if (y0 >= 2 && y0 + kAY + 2 * kAHalo <= p->ny + 2) {
-            if (first < 0) first = inner.z = t;
-            inner.w = t + 1;
-        }
-    }
-    const dim3 grid((unsigned)(ntx * nty) * (unsigned)n_members);
-    static bool configured[2] = {false, false};
-    if (!configured[cf]) {
-        cudaError_t e = cf ? cudaFuncSetAttribute(stage_vjp_members_kernel<true>,
-                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                           : cudaFuncSetAttribute(stage_vjp_members_kernel<false>,
-                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return set_error(GOC_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
-        configured[cf] = true;
-    }
-    const int pf = pitch / 4, hip = Hi_pitch / 4, hmp = Hm_pitch / 4;
-    if (cf)
-        stage_vjp_members_kernel<true><<<grid, kANT, smem, st>>>(
-            *p, k, dt, rk_step, x_eta, x_hu, x_hv, a_eta, a_hu, a_hv, yb_eta, yb_hu, yb_hv, base_eta, base_hu,
-            base_hv, xb_eta, xb_hu, xb_hv, ab_eta, ab_hu, ab_hv, pf, member_stride, wind_stride, Hi, hip, Hm, hmp,
-            wind_partials, partials, n_members, inner);
-    else
-        stage_vjp_members_kernel<false><<<grid, kANT, smem, st>>>(
-            *p, k, dt, rk_step, x_eta, x_hu, x_hv, a_eta, a_hu, a_hv, yb_eta, yb_hu, yb_hv, base_eta, base_hu,
-            base_hv, xb_eta, xb_hu, xb_hv, ab_eta, ab_hu, ab_hv, pf, member_stride, wind_stride, Hi, hip, Hm, hmp,
-            wind_partials, partials, n_members, inner);
-    count_launch();
-    return check_launch("stage_vjp_members_kernel");
+    const VjpBuffers b{x_eta, x_hu, x_hv, a_eta, a_hu, a_hv, nullptr, nullptr, nullptr, yb_eta, yb_hu, yb_hv,
+                       base_eta, base_hu, base_hv, xb_eta, xb_hu, xb_hv, ab_eta, ab_hu, ab_hv};
+    return stage_vjp_members_impl(p, dt, rk_step, b, pitch, member_stride, n_members, wind_stride, Hi, Hi_pitch,
+                                  Hm, Hm_pitch, wind_partials, stream, "goc_cdklm_stage_vjp_members");
+}
+
+extern "C" int goc_cdklm_stage_vjp_members_out(const GocCdklmParams* p, float dt, int rk_step, const float* x_eta,
+                                               const float* x_hu, const float* x_hv, const float* a_eta,
+                                               const float* a_hu, const float* a_hv, const float* y_eta,
+                                               const float* y_hu, const float* y_hv, const float* yb_eta,
+                                               const float* yb_hu, const float* yb_hv, const float* base_eta,
+                                               const float* base_hu, const float* base_hv, float* xb_eta,
+                                               float* xb_hu, float* xb_hv, float* ab_eta, float* ab_hu, float* ab_hv,
+                                               int pitch, long long member_stride, int n_members, int wind_stride,
+                                               const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch,
+                                               float* wind_partials, void* stream) {
+    if (!y_eta || !y_hu || !y_hv)
+        return set_error(GOC_ERR_ARG, "goc_cdklm_stage_vjp_members_out: null stage output");
+    const VjpBuffers b{x_eta, x_hu, x_hv, a_eta, a_hu, a_hv, y_eta, y_hu, y_hv, yb_eta, yb_hu, yb_hv,
+                       base_eta, base_hu, base_hv, xb_eta, xb_hu, xb_hv, ab_eta, ab_hu, ab_hv};
+    return stage_vjp_members_impl(p, dt, rk_step, b, pitch, member_stride, n_members, wind_stride, Hi, Hi_pitch,
+                                  Hm, Hm_pitch, wind_partials, stream, "goc_cdklm_stage_vjp_members_out");
 }

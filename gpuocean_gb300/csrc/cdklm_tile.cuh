@@ -27,6 +27,7 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "f32x2.cuh"
 #include "noise_transfer.cuh"
 #include "tma.cuh"
 
@@ -40,6 +41,7 @@ struct StepConst {
     float Vc, Uc;         // dx/(2g), dy/(2g)
     float inv_atm_x, inv_atm_y;  // 1/(2 dx rho), 1/(2 dy rho)
     int periodic_x, periodic_y;
+    float one;            // 1, a run-time value for the paired sums (f32x2.cuh)
 };
 
 template <int W, int H>
@@ -74,6 +76,22 @@ __device__ __forceinline__ float minmod_slope(float l, float c, float r, float t
     return minmod_raw((c - l) * theta, (r - l) * 0.5f, (r - c) * theta);
 }
 
+// minmod_raw and minmod_slope of two independent triples at once (paired
+// arithmetic, the same roundings; u = 1, StepConst::one).
+__device__ __forceinline__ float2 minmod_raw2(float2 b, float2 c, float2 f, float u) {
+    const float2 sb = pr(copysignf(1.0f, b.x), copysignf(1.0f, b.y));
+    const float2 sc = pr(copysignf(1.0f, c.x), copysignf(1.0f, c.y));
+    const float2 sf = pr(copysignf(1.0f, f.x), copysignf(1.0f, f.y));
+    const float2 m = pr(fminf(fminf(fabsf(b.x), fabsf(c.x)), fabsf(f.x)),
+                        fminf(fminf(fabsf(b.y), fabsf(c.y)), fabsf(f.y)));
+    return mul2(mul2(mul2(mul2(pr(0.25f), sb), add2(sb, sc, u)), add2(sc, sf, u)), m);
+}
+
+__device__ __forceinline__ float2 minmod_slope2(float2 l, float2 c, float2 r, float theta, float u) {
+    return minmod_raw2(mul2(sub2(c, l, u), pr(theta)), mul2(sub2(r, l, u), pr(0.5f)), mul2(sub2(r, c, u), pr(theta)),
+                       u);
+}
+
 // K/common.cu:664-666.  The reference's literal 0.5*eps is a double.
 __device__ __forceinline__ float desing(float h, float hu, float eps) {
     const float a = (float)((double)(h * h / (2.0f * eps)) + 0.5 * (double)eps);
@@ -105,38 +123,40 @@ __device__ __forceinline__ void desingularize_cell(const GocCdklmParams& p, floa
 __device__ __forceinline__ void cdklm_flux(const GocCdklmParams& p, const StepConst& k,
                                            float em, float um_, float vm_, float ep, float up_, float vp_,
                                            float H, float& F0, float& F1, float& F2) {
-    const float hp = ep + H;
-    const float hm = em + H;
-    float Fp0 = 0.f, Fp1 = 0.f, Fp2 = 0.f, up = 0.f, cp = 0.f;
-    if (hp > p.depth_cutoff) {
-        Fp0 = hp * up_;
-        Fp1 = hp * up_ * up_ + k.half_g * hp * hp;
-        Fp2 = hp * up_ * vp_;
-        up = up_;
-        cp = sqrtf(p.g * hp);
-    }
-    float Fm0 = 0.f, Fm1 = 0.f, Fm2 = 0.f, um = 0.f, cm = 0.f;
-    if (hm > p.depth_cutoff) {
-        Fm0 = hm * um_;
-        Fm1 = hm * um_ * um_ + k.half_g * hm * hm;
-        Fm2 = hm * um_ * vm_;
-        um = um_;
-        cm = sqrtf(p.g * hm);
-    }
-    const float am = fminf(fminf(um - cm, up - cp), 0.0f);
-    const float ap = fmaxf(fmaxf(um + cm, up + cp), 0.0f);
+    // the plus and minus sides in pairs (x: plus, y: minus); a dry side (h at
+    // or below the cutoff) contributes no flux and no wave speed
+    const float u = k.one;
+    const float2 h = add2(pr(ep, em), pr(H), u);
+    const float2 hu = mul2(h, pr(up_, um_));
+    const float2 f1 = add2(mul2(hu, pr(up_, um_)), mul2(mul2(pr(k.half_g), h), h), u);
+    const float2 f2 = mul2(hu, pr(vp_, vm_));
+    const float2 gh = mul2(pr(p.g), h);
+    const bool wp = h.x > p.depth_cutoff, wm = h.y > p.depth_cutoff;
+    const float Fp0 = wp ? hu.x : 0.f, Fp1 = wp ? f1.x : 0.f, Fp2 = wp ? f2.x : 0.f;
+    const float Fm0 = wm ? hu.y : 0.f, Fm1 = wm ? f1.y : 0.f, Fm2 = wm ? f2.y : 0.f;
+    const float up = wp ? up_ : 0.f, cp = wp ? sqrtf(gh.x) : 0.f;
+    const float um = wm ? um_ : 0.f, cm = wm ? sqrtf(gh.y) : 0.f;
+    const float2 lo = sub2(pr(um, up), pr(cm, cp), u);
+    const float2 hi = add2(pr(um, up), pr(cm, cp), u);
+    const float am = fminf(fminf(lo.x, lo.y), 0.0f);
+    const float ap = fmaxf(fmaxf(hi.x, hi.y), 0.0f);
     if (fabsf(ap - am) < p.flux_slope_eps) {
         F0 = 0.f; F1 = 0.f; F2 = 0.f;
         return;
     }
     const float inv = 1.0f / (ap - am);
     const float apam = ap * am;
-    F0 = ((ap * Fm0 - am * Fp0) + apam * (ep - em)) * inv;
-    F1 = ((ap * Fm1 - am * Fp1) + apam * (Fp0 - Fm0)) * inv;
+    // (F0, F1) = ((ap Fm - am Fp) + apam (ep - em, Fp0 - Fm0)) inv
+    const float2 t = sub2(mul2(pr(ap), pr(Fm0, Fm1)), mul2(pr(am), pr(Fp0, Fp1)), u);
+    const float2 F01 = mul2(add2(t, mul2(pr(apam), sub2(pr(ep, Fp0), pr(em, Fm0), u)), u), pr(inv));
+    F0 = F01.x;
+    F1 = F01.y;
     const float fb = p.flux_balancer;
-    float f2 = (um_ > -up_) ? fb * Fm2 : fb * Fp2;
-    f2 += (1.0f - fb) * (((ap * Fm2 - am * Fp2) + apam * (hp * vp_ - hm * vm_)) * inv);
-    F2 = f2;
+    const float2 s2 = mul2(pr(ap, am), pr(Fm2, Fp2));
+    const float2 hv = mul2(h, pr(vp_, vm_));
+    float g2 = (um_ > -up_) ? fb * Fm2 : fb * Fp2;
+    g2 += (1.0f - fb) * (((s2.x - s2.y) + apam * (hv.x - hv.y)) * inv);
+    F2 = g2;
 }
 
 // Issue the TMA copies of the (eta, hu, hv) box at (x, y) (x a multiple of
@@ -226,8 +246,9 @@ struct Tile {
             const float eL = S.D[0][j][i - 1], eC = S.D[0][j][i], eR = S.D[0][j][i + 1];
             const float uL = S.D[1][j][i - 1], uC = S.D[1][j][i], uR = S.D[1][j][i + 1];
             const float vL = S.D[2][j][i - 1], vC = S.D[2][j][i], vR = S.D[2][j][i + 1];
-            S.Sx[0][j][i] = minmod_slope(uL, uC, uR, th);
-            S.Sx[1][j][i] = minmod_slope(vL, vC, vR, th);
+            const float2 suv = minmod_slope2(pr(uL, vL), pr(uC, vC), pr(uR, vR), th, k.one);
+            S.Sx[0][j][i] = suv.x;
+            S.Sx[1][j][i] = suv.y;
             float lv = vL, cv = vC, rv = vR;
             if (BORDER) {
                 if (p.bc_west == 1) { if (gx < 3) lv = -lv; if (gx < 2) cv = -cv; }
@@ -236,13 +257,16 @@ struct Tile {
             const float fL = F(j, i - 1, CONST_F), fC = F(j, i, CONST_F), fR = F(j, i + 1, CONST_F);
             float cnX, cnY;
             north(i, j, cnX, cnY);
-            const float lfv = (cnX * uL + cnY * lv) * fL;
+            // (left, right) in pairs
+            const float2 lrfv =
+                mul2(add2(mul2(pr(cnX), pr(uL, uR)), mul2(pr(cnY), pr(lv, rv)), k.one), pr(fL, fR));
+            const float lfv = lrfv.x, rfv = lrfv.y;
             const float cfv = (cnX * uC + cnY * cv) * fC;
-            const float rfv = (cnX * uR + cnY * rv) * fR;
-            const float back = k.theta_g * (eC - eL - k.Vc * (cfv + lfv));
+            // (backward, forward) in pairs
+            const float2 bf = mul2(pr(k.theta_g), sub2(sub2(pr(eC, eR), pr(eL, eC), k.one),
+                                                       mul2(pr(k.Vc), add2(pr(cfv), pr(lfv, rfv), k.one)), k.one));
             const float cent = k.half_g * (eR - eL - k.Vc * (rfv + 2.0f * cfv + lfv));
-            const float fwd = k.theta_g * (eR - eC - k.Vc * (cfv + rfv));
-            float Kx = minmod_raw(back, cent, fwd);
+            float Kx = minmod_raw(bf.x, cent, bf.y);
             float va = vC;
             if (BORDER) {
                 if (p.bc_west == 1 && gx < 2) va = -va;
@@ -270,21 +294,25 @@ struct Tile {
             const float eL = S.D[0][j - 1][i], eC = S.D[0][j][i], eU = S.D[0][j + 1][i];
             const float uL = S.D[1][j - 1][i], uC = S.D[1][j][i], uU = S.D[1][j + 1][i];
             const float vL = S.D[2][j - 1][i], vC = S.D[2][j][i], vU = S.D[2][j + 1][i];
-            S.Sy[0][j][i] = minmod_slope(uL, uC, uU, th);
-            S.Sy[1][j][i] = minmod_slope(vL, vC, vU, th);
+            const float2 suv = minmod_slope2(pr(uL, vL), pr(uC, vC), pr(uU, vU), th, k.one);
+            S.Sy[0][j][i] = suv.x;
+            S.Sy[1][j][i] = suv.y;
             float lu = uL, cu = uC, uu = uU;
             if (BORDER) {
                 if (p.bc_south == 1) { if (gy < 3) lu = -lu; if (gy < 2) cu = -cu; }
                 if (p.bc_north == 1) { if (gy > p.ny) uu = -uu; if (gy > p.ny + 1) cu = -cu; }
             }
             const float fL = F(j - 1, i, CONST_F), fC = F(j, i, CONST_F), fU = F(j + 1, i, CONST_F);
-            const float lfu = (eX * lu + eY * vL) * fL;
+            // (lower, upper) in pairs
+            const float2 lufu =
+                mul2(add2(mul2(pr(eX), pr(lu, uu)), mul2(pr(eY), pr(vL, vU)), k.one), pr(fL, fU));
+            const float lfu = lufu.x, ufu = lufu.y;
             const float cfu = (eX * cu + eY * vC) * fC;
-            const float ufu = (eX * uu + eY * vU) * fU;
-            const float back = k.theta_g * (eC - eL + k.Uc * (cfu + lfu));
+            // (backward, forward) in pairs
+            const float2 bf = mul2(pr(k.theta_g), add2(sub2(pr(eC, eU), pr(eL, eC), k.one),
+                                                       mul2(pr(k.Uc), add2(pr(cfu), pr(lfu, ufu), k.one)), k.one));
             const float cent = k.half_g * (eU - eL + k.Uc * (ufu + 2.0f * cfu + lfu));
-            const float fwd = k.theta_g * (eU - eC + k.Uc * (cfu + ufu));
-            float Ly = minmod_raw(back, cent, fwd);
+            float Ly = minmod_raw(bf.x, cent, bf.y);
             float ua = uC;
             if (BORDER) {
                 if (p.bc_south == 1 && gy < 2) ua = -ua;
@@ -411,17 +439,25 @@ struct Tile {
         }
     }
 
-    // Right-hand side L(Q) of the cell (i,j) plus the quantities the RK
-    // combination needs; K/CDKLM16_kernel.cu:739-966.
-    template <bool CONST_F, bool SIMPLE_FORCING>
-    __device__ void rhs(int i, int j, int gxs, int gys, float& L1, float& L2, float& L3,
-                        float& ec, float& hu, float& hv, float& Hm, float& hsum) const {
+    // The state of cell (i,j) that the RK combination starts from: eta,
+    // the re-singularised momenta, the cell-mean depth and the water depth.
+    __device__ __forceinline__ void cell_state(int i, int j, float& ec, float& hu, float& hv, float& Hm,
+                                               float& hsum) const {
         ec = S.D[0][j][i];
         const float uc = S.D[1][j][i], vc = S.D[2][j][i];
         Hm = 0.25f * (S.Hi[j][i] + S.Hi[j + 1][i] + S.Hi[j][i + 1] + S.Hi[j + 1][i + 1]);
         hsum = ec + Hm;
         hu = 0.0f; hv = 0.0f;
         if (hsum > p.depth_cutoff) { hu = uc * hsum; hv = vc * hsum; }
+    }
+
+    // Right-hand side L(Q) of the cell (i,j) plus the quantities the RK
+    // combination needs; K/CDKLM16_kernel.cu:739-966.
+    template <bool CONST_F, bool SIMPLE_FORCING>
+    __device__ void rhs(int i, int j, int gxs, int gys, float& L1, float& L2, float& L3,
+                        float& ec, float& hu, float& hv, float& Hm, float& hsum) const {
+        cell_state(i, j, ec, hu, hv, Hm, hsum);
+        const float uc = S.D[1][j][i], vc = S.D[2][j][i];
         const float fc = F(j, i, CONST_F);
         // the west / south faces as this cell sees them: with a north-angle
         // texture the plus-cell versions of the neighbours' faces
@@ -473,27 +509,14 @@ struct Tile {
                 Y = p.wind_stress_factor * (p.wind_t * wyn + (1.0f - p.wind_t) * wyc);
                 if (p.atm_p_nx * p.atm_p_ny > 1) {
                     const float pt = p.atm_p_t;
-                    float pe, pw, pn, ps;
-                    if (p.atm_p_direct) {
-                        // the cells the reference's direct lookup reads, its
-                        // north/south values one column east included
-                        // (K/external_forcing.cu:76-97)
-                        auto P = [&](int ii, int jj) {
-                            const size_t o = (size_t)jj * p.atm_p_nx + ii;
-                            return pt * __ldg(p.atm_p_next + o) + (1.0f - pt) * __ldg(p.atm_p_cur + o);
-                        };
-                        pn = P(gxs + 1, gys + 1); ps = P(gxs + 1, gys - 1);
-                        pe = P(gxs + 1, gys); pw = P(gxs - 1, gys);
-                    } else {
-                        const float dxn = 1.0f / (float)(p.nx + 4), dyn = 1.0f / (float)(p.ny + 4);
-                        auto P = [&](float ss, float tt) {
-                            const float c = tex_bilinear(p.atm_p_cur, p.atm_p_nx, p.atm_p_ny, ss, tt);
-                            const float n = tex_bilinear(p.atm_p_next, p.atm_p_nx, p.atm_p_ny, ss, tt);
-                            return pt * n + (1.0f - pt) * c;
-                        };
-                        pe = P(s + dxn, t); pw = P(s - dxn, t);
-                        pn = P(s, t + dyn); ps = P(s, t - dyn);
-                    }
+                    const float dxn = 1.0f / (float)(p.nx + 4), dyn = 1.0f / (float)(p.ny + 4);
+                    auto P = [&](float ss, float tt) {
+                        const float c = tex_bilinear(p.atm_p_cur, p.atm_p_nx, p.atm_p_ny, ss, tt);
+                        const float n = tex_bilinear(p.atm_p_next, p.atm_p_nx, p.atm_p_ny, ss, tt);
+                        return pt * n + (1.0f - pt) * c;
+                    };
+                    const float pe = P(s + dxn, t), pw = P(s - dxn, t);
+                    const float pn = P(s, t + dyn), ps = P(s, t - dyn);
                     ax = -(pe - pw) * hsum * k.inv_atm_x;
                     ay = -(pn - ps) * hsum * k.inv_atm_y;
                 }
@@ -592,6 +615,9 @@ __host__ __device__ inline StepConst make_step_const(const GocCdklmParams& p) {
     k.inv_atm_y = exact_div(1.0f, 2.0f * p.dy * p.rho_o);
     k.periodic_x = (p.bc_east == 2);
     k.periodic_y = (p.bc_north == 2);
+    // 1 for every valid grid, from a run-time value so that the device
+    // compiler cannot treat it as a constant
+    k.one = p.nx >= 0 ? 1.0f : -1.0f;
     return k;
 }
 
@@ -1043,8 +1069,6 @@ inline int validate_params(const GocCdklmParams* p, const char* who, bool allow_
         return set_error(GOC_ERR_ARG, "%s: wind stress textures missing", who);
     if (!p->atm_p_cur || !p->atm_p_next || p->atm_p_nx < 1 || p->atm_p_ny < 1)
         return set_error(GOC_ERR_ARG, "%s: atmospheric pressure textures missing", who);
-    if (p->atm_p_direct && (p->atm_p_nx != p->nx + 4 || p->atm_p_ny != p->ny + 4))
-        return set_error(GOC_ERR_ARG, "%s: direct lookup needs (ny+4) x (nx+4) pressure arrays", who);
     if ((p->bc_north == 2 && p->ny < 4) || (p->bc_east == 2 && p->nx < 4))
         return set_error(GOC_ERR_ARG, "%s: periodic directions need at least 4 interior cells", who);
     return GOC_OK;

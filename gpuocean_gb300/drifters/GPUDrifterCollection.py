@@ -60,10 +60,24 @@ class GPUDrifterCollection(BaseDrifterCollection):
         return c
 
     def update_wind(self, t):
+        """Bring the current / next wind textures to the interval of time t
+        and return the time weight of t in it (D/GPUDrifterCollection.py:
+        138-174)."""
+        t0, t1 = self.wind_interval(t)
+        self.load_wind_interval(t0, t1)
+        return self.wind_weight(t, t0, t1)
+
+    def wind_interval(self, t, side="left"):
+        """Indices of the wind time stamps around t.  At a time stamp itself
+        side "left" gives the interval that ends there (as update_wind
+        chooses), "right" the one that starts there; both give t the same
+        wind (weight 1 of the one, weight 0 of the other)."""
+        last = len(self.wind.t) - 1
+        k = int(np.searchsorted(self.wind.t, t, side=side))
+        return max(0, k - 1), min(last, k)
+
+    def load_wind_interval(self, t0, t1):
         w = self.wind
-        t_max_index = len(w.t) - 1
-        t0 = max(0, np.searchsorted(w.t, t) - 1)
-        t1 = min(t_max_index, np.searchsorted(w.t, t))
         new_t0, new_t1 = w.t[t0], w.t[t1]
         old = self.wind_timestamps.get("drift", [None, None])
         self.wind_timestamps["drift"] = [new_t0, new_t1]
@@ -73,6 +87,9 @@ class GPUDrifterCollection(BaseDrifterCollection):
         if new_t1 != old[1]:
             self.wind_x_next_arr.upload(self.gpu_stream, w.wind_u[t1])
             self.wind_y_next_arr.upload(self.gpu_stream, w.wind_v[t1])
+
+    def wind_weight(self, t, t0, t1):
+        new_t0, new_t1 = self.wind.t[t0], self.wind.t[t1]
         return max(0.0, min(1.0, (t - new_t0) / max(1.0e-10, (new_t1 - new_t0))))
 
     def setDrifterPositions(self, newDrifterPositions):

@@ -252,12 +252,12 @@ class BatchedEnsemble:
         (the drift after step k reads the wind at the member's time before
         step k's increment, D/GPUDrifterCollection.py:138-174), after
         bringing each collection's current/next textures to the block's wind
-        interval.  A block may not cross a wind time stamp."""
+        interval.  A block may not cross a wind time stamp; it may start or
+        end on one (the wind there is the same from either side)."""
         table = np.zeros((len(self.sims), self.max_substeps), dtype=np.float32)
         for m in self._wind_members:
             s = self.sims[m]
             d = s.drifters
-            tw = np.asarray(d.wind.t, dtype=np.float64)
             t = float(s.t)
             times = []
             for local_dt in scheds[m]:
@@ -265,13 +265,17 @@ class BatchedEnsemble:
                 t += float(np.float64(local_dt))
             if not times:
                 continue
-            last = len(tw) - 1
-            spans = {(max(0, int(np.searchsorted(tw, x)) - 1), min(last, int(np.searchsorted(tw, x)))) for x in times}
-            if len(spans) > 1:
+            common = None
+            for x in times:
+                c = {d.wind_interval(x, "left"), d.wind_interval(x, "right")}
+                common = c if common is None else common & c
+            if not common:
                 raise NotImplementedError("a batched block crosses a wind time stamp of member %d's drifters: "
                                           "step to the time stamp first" % m)
+            t0, t1 = min(common)
+            d.load_wind_interval(t0, t1)
             for k, x in enumerate(times):
-                table[m, k] = np.float32(d.update_wind(x))
+                table[m, k] = np.float32(d.wind_weight(x, t0, t1))
         _lib.call("goc_ensemble_set_wind_times", self._handle, table.ctypes.data, self.stream.handle)
 
     def release(self):

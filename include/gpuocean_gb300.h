@@ -70,10 +70,6 @@ typedef struct GocCdklmParams {
     float wind_t;                   /* time interpolation weight in [0,1] */
     const float* atm_p_cur;  const float* atm_p_next; int32_t atm_p_nx, atm_p_ny;
     float atm_p_t;
-    /* 1: the pressure arrays are (ny+4) x (nx+4) and are read directly at the
-     * cells the central differences need instead of interpolated
-     * (USE_DIRECT_LOOKUP, K/external_forcing.cu:76-97, S/CDKLM16.py:123-133) */
-    int32_t atm_p_direct;
 } GocCdklmParams;
 
 /* ---------------- runtime plumbing (device memory, streams, timing) ------ */
@@ -322,6 +318,38 @@ int goc_cdklm_stage_vjp(const GocCdklmParams* p, float dt, int rk_step,
                         float* ab_eta, float* ab_hu, float* ab_hv, int pitch,
                         const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch,
                         float* wind_partials, void* stream);
+
+/*
+ * The same VJPs given the stage output y as well (no counterpart in the
+ * reference): rk_step 0 takes y = Q*, rk_step 1 y = Q^{n+1}, exactly as the
+ * forward step wrote them (goc_cdklm_rk2_step_stage keeps both).  The
+ * updated state and the dry clamp of each cell then come from y instead of
+ * from a recompute of the stage's fluxes, which the kernel skips; results
+ * are those of goc_cdklm_stage_vjp except where the final clamp ties (a wet
+ * cell at rest that the clamp raised to exactly -Hm + depth_cutoff reads as
+ * dried).  A rollout's backward sweep has y at hand.
+ */
+int goc_cdklm_stage_vjp_out(const GocCdklmParams* p, float dt, int rk_step,
+                            const float* x_eta, const float* x_hu, const float* x_hv,
+                            const float* a_eta, const float* a_hu, const float* a_hv,
+                            const float* y_eta, const float* y_hu, const float* y_hv,
+                            const float* yb_eta, const float* yb_hu, const float* yb_hv,
+                            const float* base_eta, const float* base_hu, const float* base_hv,
+                            float* xb_eta, float* xb_hu, float* xb_hv,
+                            float* ab_eta, float* ab_hu, float* ab_hv, int pitch,
+                            const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch,
+                            float* wind_partials, void* stream);
+int goc_cdklm_stage_vjp_members_out(const GocCdklmParams* p, float dt, int rk_step,
+                                    const float* x_eta, const float* x_hu, const float* x_hv,
+                                    const float* a_eta, const float* a_hu, const float* a_hv,
+                                    const float* y_eta, const float* y_hu, const float* y_hv,
+                                    const float* yb_eta, const float* yb_hu, const float* yb_hv,
+                                    const float* base_eta, const float* base_hu, const float* base_hv,
+                                    float* xb_eta, float* xb_hu, float* xb_hv,
+                                    float* ab_eta, float* ab_hu, float* ab_hv, int pitch,
+                                    long long member_stride, int n_members, int wind_stride,
+                                    const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch,
+                                    float* wind_partials, void* stream);
 
 /* ---------------- drifters ---------------------------------------------- */
 

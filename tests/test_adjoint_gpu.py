@@ -321,6 +321,175 @@ def test_rollout_gradient_matches_fp64_finite_differences(ctx):
     sim.cleanUp()
 
 
+def _fd_study(ctx, moving, steps, with_fd32):
+    """The 400-step rollout and loss of the FP64 finite-difference test on the
+    64 x 64 bump (at rest, or with a smooth current everywhere), its adjoint
+    gradient, and central differences along the gradient and two random
+    smooth directions with the given steps: of the FP64 oracle rollout and,
+    with with_fd32, of the FP32 forward that the adjoint differentiates (the
+    product's own step).  Each directional derivative is taken along the
+    difference that the two FP32-rounded inputs actually have.  Errors are
+    relative to the directional derivative along the gradient and to
+    |grad| |direction| along random directions."""
+    from gpuocean_gb300.adjoint import CDKLM16Rollout, StepAdjoint
+    c = _bump_case(64, moving=moving)
+    n_steps, every = 400, 10
+    sim = _sim(ctx, c, 0.0)
+    sim.updateDt(courant_number=0.45)
+    dt = float(sim.dt)
+    adj = StepAdjoint(sim)
+    dev = adj.device
+    tau = np.array([1.0e-4, 0.0], dtype=np.float32)
+    rows, cols = _misfit_setup(c, 64, 3)
+    Hm = torch.as_tensor(np.asarray(sim.downloadBathymetry()[1], dtype=np.float32)[2:-2, 2:-2], device=dev)
+    base32 = [a.detach().clone() for a in adj.state(*sim.download())]
+
+    def rollout64(q):
+        o = OracleCDKLM16(c["eta"], c["hu"], c["hv"], c["H"], c["nx"], c["ny"], c["dx"], c["dy"], dt, c["g"],
+                          c["f"], c["r"], boundary_conditions=BC(*c["bc"]))
+        Hm64 = np.asarray(o.Hm, dtype=np.float64)[2:-2, 2:-2]
+        o.Q0 = [np.asarray(a, dtype=np.float64).copy() for a in q]
+        o.Q1 = [a.copy() for a in o.Q0]
+        sh = (c["ny"] + 4, c["nx"] + 4)
+        o.wind = (np.full(sh, float(tau[0])), np.full(sh, float(tau[1])))
+        for _ in range(n_steps // every):
+            for _ in range(every):
+                o.step(dt)
+            e, hu, hv = (a[2:-2, 2:-2] for a in o.Q0)
+            h = e[rows, cols] + Hm64[rows, cols]
+            yield hu[rows, cols] / h, hv[rows, cols] / h
+
+    base64 = [a.double().cpu().numpy() for a in base32]
+    # the truth: half the bump (FP64), the same for both losses
+    truth0 = [b.copy() for b in base64]
+    truth0[0] = truth0[0] * 0.5
+    obs = list(rollout64(truth0))
+    u_obs_h = np.stack([a for a, _ in obs])
+    v_obs_h = np.stack([b for _, b in obs])
+    u_obs = torch.as_tensor(u_obs_h, device=dev)
+    v_obs = torch.as_tensor(v_obs_h, device=dev)
+
+    def loss_of(states):
+        h = (states[:, 0] + Hm).double()
+        u = states[:, 1, rows, cols].double() / h[:, rows, cols]
+        v = states[:, 2, rows, cols].double() / h[:, rows, cols]
+        return ((u - u_obs) ** 2).sum() + ((v - v_obs) ** 2).sum()
+
+    x = [a.clone().requires_grad_(True) for a in base32]
+    w = torch.tensor(tau, device=dev, requires_grad=True)
+    loss_of(CDKLM16Rollout.apply(adj, n_steps, every, *x, w)).backward()
+    grads = [a.grad.double() for a in x]
+
+    def loss32(q):
+        with torch.no_grad():
+            return float(loss_of(CDKLM16Rollout.apply(adj, n_steps, every, *q, torch.tensor(tau, device=dev))))
+
+    def loss64(q):
+        return sum(float(np.sum((a - u_obs_h[k]) ** 2) + np.sum((b - v_obs_h[k]) ** 2))
+                   for k, (a, b) in enumerate(rollout64(q)))
+
+    gmax = max(float(g.abs().max()) for g in grads)
+    gnorm = float(torch.sqrt(sum((g * g).sum() for g in grads)))
+    rng = np.random.default_rng(9)
+    directions = {"gradient": [g / gmax for g in grads]}
+    for d in range(2):
+        dd = [torch.as_tensor(_smooth(rng, base64[0].shape, s), dtype=torch.float64, device=dev)
+              for s in (1.0, 10.0, 10.0)]
+        for a in dd:
+            a[:2, :] = 0; a[-2:, :] = 0; a[:, :2] = 0; a[:, -2:] = 0
+        directions[f"random_{d}"] = dd
+    results = {}
+    for name, dd in directions.items():
+        for step in steps:
+            qp = [(b.double() + step * a).float() for b, a in zip(base32, dd)]
+            qm = [(b.double() - step * a).float() for b, a in zip(base32, dd)]
+            diff = [p.double() - m.double() for p, m in zip(qp, qm)]
+            dnorm = float(torch.sqrt(sum((a * a).sum() for a in diff)))
+            ad = float(sum((g * a).sum() for g, a in zip(grads, diff)))
+            den = abs(ad) if name == "gradient" else gnorm * dnorm
+            fd64 = loss64([p.double().cpu().numpy() for p in qp]) - loss64([m.double().cpu().numpy() for m in qm])
+            r = dict(ad=ad, fd64=fd64, err64=abs(ad - fd64) / den)
+            if with_fd32:
+                fd32 = loss32(qp) - loss32(qm)
+                r.update(fd32=fd32, err32=abs(ad - fd32) / den, fd32_vs_fd64=abs(fd32 - fd64) / den)
+            results[f"{name}@{step:g}"] = r
+    sim.cleanUp()
+    return results
+
+
+def test_rollout_fd_of_fp32_forward_matches_fp64_forward(ctx):
+    """The bump at rest: finite differences of the FP32 forward (the
+    product's step) agree with those of the FP64 oracle to ~1e-5, so the
+    rounding of the FP32 trajectory is not what separates the adjoint from
+    the FP64 finite differences.  That gap (~6e-4 along the gradient here)
+    comes from the point itself: at rest, h = 60 m + eta is quantised in FP32
+    (one ulp of 60 is 3.8e-6 m), so depths, wave speeds and limiter arguments
+    of neighbouring cells tie in FP32 where they differ in FP64, and the
+    adjoint - the derivative of the FP32 computation - takes the
+    subgradients of those ties.  The moving bump below has no ties, and
+    there the adjoint matches FP64 finite differences closely."""
+    results = _fd_study(ctx, False, (1.0e-3,), True)
+    print(json.dumps({"case": "rollout 400 steps 64x64 bump at rest, FD of FP32 and FP64 forwards",
+                      "results": results}))
+    assert max(r["fd32_vs_fd64"] for r in results.values()) <= 1e-4, results
+
+
+def test_rollout_gradient_of_moving_bump_matches_fp64_fd(ctx):
+    """The bump with a smooth current everywhere (no FP32 ties): the adjoint
+    gradient of the 400-step rollout against FP64 central differences."""
+    results = _fd_study(ctx, True, (1.0e-4, 1.0e-3), False)
+    print(json.dumps({"case": "rollout 400 steps 64x64 moving bump, FD of FP64 forward", "results": results}))
+    best = {}
+    for key, r in results.items():
+        name = key.split("@")[0]
+        best[name] = min(best.get(name, np.inf), r["err64"])
+    assert max(best.values()) <= 1e-4, results
+
+
+def test_step_vjp_from_stage_outputs_equals_recompute(ctx):
+    """The stage VJPs given the stage outputs (Q* and Q^{n+1} as the forward
+    wrote them) skip the recompute of the stages' fluxes; without dry cells
+    their results are bit-identical to the recomputing VJPs, for one
+    simulator and for a batch of members."""
+    from gpuocean_gb300.adjoint import EnsembleStepAdjoint, StepAdjoint
+    c = dict(_bump_case(64, moving=True), wind=(1.0e-4, -6.0e-5))
+    sim = _sim(ctx, c, 2.0)
+    adj = StepAdjoint(sim)
+    adj.set_wind(c["wind"])
+    q = adj.state(*sim.download())
+    q1, qs = adj.zeros(), adj.zeros()
+    adj.step_with_stage(q, q1, qs)
+    rng = np.random.default_rng(6)
+    lam = adj.zeros()
+    for a in lam:
+        a[2:-2, 2:-2] = torch.as_tensor(rng.standard_normal((c["ny"], c["nx"])), dtype=torch.float32)
+    out = []
+    for q_next in (None, q1):
+        ls, ln = adj.zeros(), adj.zeros()
+        adj.reset_wind_grad()
+        adj.step_vjp(q, qs, lam, ls, ln, q_next)
+        out.append([a.clone() for a in ln] + [adj.wind_grad().clone()])
+    for a, b in zip(*out):
+        assert torch.equal(a, b)
+    n = 3
+    eadj = EnsembleStepAdjoint(sim, n)
+    base = torch.stack([a for a in q]).unsqueeze(0).repeat(n, 1, 1, 1).contiguous()
+    base[:, 1] += torch.as_tensor(np.stack([_smooth(rng, base.shape[2:], 0.5) for _ in range(n)]),
+                                  device=base.device)
+    e1, es = eadj.zeros(), eadj.zeros()
+    eadj.step(base, e1, es)
+    elam = eadj.zeros()
+    elam.normal_()
+    out = []
+    for q_next in (None, e1):
+        ls, ln = eadj.zeros(), eadj.zeros()
+        eadj.reset_wind_grad()
+        eadj.step_vjp(base, es, elam, ls, ln, q_next)
+        out.append((ln[..., 2:-2, 2:-2].clone(), eadj.wind_grad().clone()))
+    assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])
+    sim.cleanUp()
+
+
 def test_rollout_adjoint_matches_fp64_vjp_chain(ctx):
     """100 steps of the moving bump with wind: the CUDA adjoint of the whole
     rollout (sqrt(N) checkpointing) against the chain of FP64 autograd stage

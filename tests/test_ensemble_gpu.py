@@ -297,17 +297,18 @@ def test_packed_drifter_transfers(gpu_ctx):
 
 
 def test_batched_wind_drift_equals_member_by_member(gpu_ctx):
-    """Drifters with wind drift (3 x 4 wind textures at two time stamps,
+    """Drifters with wind drift (3 x 4 wind textures at three time stamps,
     factor 0.02) in the batched engine - moved in launches of their own -
     equal the collections drifted by the plain simulators, bit for bit; the
-    members without wind keep drifting inside the step.  Blocks stay
-    between the wind's time stamps (crossing one is refused)."""
+    members without wind keep drifting inside the step.  Blocks may start or
+    end on a wind time stamp (the fourth block starts on one); a block that
+    crosses one is refused."""
     from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
     from gpuocean_gb300.drifters import GPUDrifterCollection
     from gpuocean_gb300.utils import WindStress
     rng = np.random.default_rng(8)
-    wu = [(5.0 * rng.standard_normal((4, 3))).astype(np.float32) for _ in range(2)]
-    wv = [(5.0 * rng.standard_normal((4, 3))).astype(np.float32) for _ in range(2)]
+    wu = [(5.0 * rng.standard_normal((4, 3))).astype(np.float32) for _ in range(3)]
+    wv = [(5.0 * rng.standard_normal((4, 3))).astype(np.float32) for _ in range(3)]
 
     def members():
         out = []
@@ -315,7 +316,7 @@ def test_batched_wind_drift_equals_member_by_member(gpu_ctx):
             s = _member(gpu_ctx, *spec, drifters=40)
             if i != 1:
                 old = s.drifters
-                wind = WindStress.WindStress(t=[0.0, 7200.0], wind_u=wu, wind_v=wv)
+                wind = WindStress.WindStress(t=[0.0, 1800.0, 3600.0], wind_u=wu, wind_v=wv)
                 d = GPUDrifterCollection.GPUDrifterCollection(
                     gpu_ctx, 40, boundaryConditions=s.boundary_conditions, domain_size_x=old.domain_size_x,
                     domain_size_y=old.domain_size_y, gpu_stream=s.gpu_stream, wind=wind, wind_drift_factor=0.02)
@@ -327,7 +328,7 @@ def test_batched_wind_drift_equals_member_by_member(gpu_ctx):
         return out
     a, b = members(), members()
     ens = BatchedEnsemble(a)
-    for _ in range(3):
+    for _ in range(4):
         ens.step(600.0)
         for s in b:
             s.step(600.0)
@@ -338,5 +339,5 @@ def test_batched_wind_drift_equals_member_by_member(gpu_ctx):
         for x, y in zip(sa.download(), sb.download()):
             assert np.array_equal(np.asarray(x)[2:-2, 2:-2], np.asarray(y)[2:-2, 2:-2])
     with pytest.raises(NotImplementedError):
-        ens.step(7200.0)   # would cross the wind's second time stamp
+        ens.step(1800.0)   # 2400 s -> 4200 s would cross the wind's third time stamp
     ens.release()

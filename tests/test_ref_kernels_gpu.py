@@ -430,7 +430,9 @@ def test_wind_drift_against_reference_kernel(ctx):
     dpos = float(np.max(np.abs(mine - theirs)))
     print(json.dumps({"case": "wind drift, 20 steps", "max_abs_drifter_diff_m": dpos,
                       "wind_displacement_m": moved}))
-    assert moved > 100.0                     # the wind moved the drifters
+    # the wind moved the drifters: 0.02 x ~5 m/s over 20 steps of ~20 s is
+    # tens of metres
+    assert moved > 10.0
     assert dpos <= 1e-6 * max(Lx, Ly), dpos
     for o in (rdrift, calm, ref, still):
         o.free()

@@ -140,10 +140,10 @@ def test_time_varying_textured_forcing(gpu_ctx):
 
 
 def test_direct_lookup_pressure(gpu_ctx):
-    """use_direct_lookup: a pressure array of the grid's own size read at
-    the cells of the reference's central differences (its north and south
-    values taken one column east), against the reference kernel built with
-    USE_DIRECT_LOOKUP, two time stamps."""
+    """use_direct_lookup with a pressure array of the grid's own size, two
+    time stamps, against the reference kernel built with the define its host
+    writes (USE_DIRECT_LOOKUP True, which the preprocessor reads as 0: the
+    reference interpolates the array, and so does this build)."""
     nx, ny = 77, 45
     rng = np.random.default_rng(12)
     x = np.arange(nx + 4) - 2 + 0.5 - nx / 2.0
