@@ -48,6 +48,39 @@ def step_schedule(dt, t_end):
     return out
 
 
+def step_schedules(dts, t_end, active):
+    """step_schedule for many members at once: dts (N,) float32, active
+    (N,) bool.  Returns (table (N, K) float32, n (N,) int32), row m holding
+    member m's dt sequence - the same numbers step_schedule gives, as every
+    member's arithmetic is the same sequence of float32 / float64 roundings."""
+    dts = np.asarray(dts, dtype=np.float32)
+    t_now = np.zeros(dts.shape[0], dtype=np.float64)
+    going = np.array(active, dtype=bool) & (t_now < t_end)
+    cols = []
+    n = np.zeros(dts.shape[0], dtype=np.int32)
+    while going.any():
+        local = np.minimum(dts, (t_end - t_now).astype(np.float32))
+        cols.append(np.where(going, local, np.float32(0.0)).astype(np.float32))
+        n += going
+        t_now = np.where(going, t_now + local.astype(np.float64), t_now)
+        going &= t_now < t_end
+    table = np.stack(cols, axis=1) if cols else np.zeros((dts.shape[0], 0), dtype=np.float32)
+    return table, n
+
+
+class _Schedules:
+    """Per-member dt sequences of a block, read from the (table, n) pair."""
+
+    def __init__(self, table, n):
+        self.table, self.n = table, n
+
+    def __getitem__(self, m):
+        return list(self.table[m, :self.n[m]])
+
+    def __len__(self):
+        return len(self.n)
+
+
 class BatchedEnsemble:
     """Steps a list of RK2 ``CDKLM16`` simulators together on one GPU stream.
 
@@ -405,18 +438,19 @@ class BatchedEnsemble:
     def _schedule(self, t_end, members=None):
         """Per member the dt sequence of step(t_end); members not in
         `members` (if given) take no step."""
-        chosen = set(range(len(self.sims))) if members is None else {int(m) for m in members}
-        scheds = [step_schedule(s.dt, t_end) if m in chosen else [] for m, s in enumerate(self.sims)]
-        nsub = max(len(x) for x in scheds)
+        active = np.ones(len(self.sims), dtype=bool)
+        if members is not None:
+            active[:] = False
+            active[[int(m) for m in members]] = True
+        dts = np.fromiter((s.dt for s in self.sims), dtype=np.float32, count=len(self.sims))
+        part, n = step_schedules(dts, float(t_end), active)
+        nsub = int(n.max()) if len(n) else 0
         if nsub > self.max_substeps or self._current_ptrs() != self._ptrs:
             # members stepped on their own, or a longer block: rebuild the table
             self._build(max_substeps=max(nsub, self.max_substeps))
         table = np.zeros((len(self.sims), self.max_substeps), dtype=np.float32)
-        n = np.zeros(len(self.sims), dtype=np.int32)
-        for m, sc in enumerate(scheds):
-            table[m, :len(sc)] = sc
-            n[m] = len(sc)
-        return scheds, table, n, nsub
+        table[:, :part.shape[1]] = part
+        return _Schedules(table, n), table, n, nsub
 
     # ------------------------------------------------------------------
     def set_noise(self, noises, random_pool=None, rng_seed=None, sources=None):
@@ -650,17 +684,30 @@ class BatchedEnsemble:
             self.kernels_launched += self._launch_block(nsub, with_noise, n)
         self._before_members()
         self._check_staging()
-        cells = 0
-        for m, s in enumerate(self.sims):
-            for local_dt in scheds[m]:
-                s.t += np.float64(local_dt)
-            s.num_iterations += len(scheds[m])
+        # the members' clocks: each member's dts added one by one in float64,
+        # as step does; the drifters' clocks by the sum of the block's dts
+        steps = table[:, :nsub].astype(np.float64)
+        t = np.fromiter((s.t for s in self.sims), dtype=np.float64, count=len(self.sims))
+        dsum = np.zeros(len(self.sims), dtype=np.float64)
+        for k in range(nsub):
+            on = n > k
+            t = np.where(on, t + steps[:, k], t)
+            dsum = np.where(on, dsum + steps[:, k], dsum)
+        for m in np.flatnonzero(n):
+            s = self.sims[m]
+            s.t = t[m]
+            s.num_iterations += int(n[m])
             if s.hasDrifters:
-                s.drifter_t += sum(np.float64(x) for x in scheds[m])
-            if len(scheds[m]) % 2 == 1:
+                s.drifter_t += dsum[m]
+            if n[m] % 2 == 1:
                 s.gpu_data.swap()
-            cells += len(scheds[m]) * int(s.nx) * int(s.ny)
         self._ptrs = self._current_ptrs()
+        return int(np.dot(n.astype(np.int64), self._member_cells()))
+
+    def _member_cells(self):
+        cells = getattr(self, "_cells_cache", None)
+        if cells is None or len(cells) != len(self.sims):
+            cells = self._cells_cache = np.array([int(s.nx) * int(s.ny) for s in self.sims], dtype=np.int64)
         return cells
 
     def synchronize(self):
