@@ -156,12 +156,55 @@ class StepAdjoint:
                   *common, _ptr(self.partials[1]), s)
         return None
 
+    # -- address-level calls of the rollout loops: states live in stacked
+    # (N, 3, ny+4, nx+4) buffers and are passed as three device addresses
+    # (see _triple), which keeps the host's work per step to a few ctypes
+    # calls --
+    def _bound(self):
+        b = getattr(self, "_bound_args", None)
+        if b is None:
+            lib = _lib.load()
+            b = self._bound_args = {
+                "step": lib.goc_cdklm_rk2_step, "stage": lib.goc_cdklm_rk2_step_stage,
+                "vjp": lib.goc_cdklm_stage_vjp_out,
+                "pre": (ctypes.byref(self.params), ctypes.c_float(self.dt)),
+                "common": (self.pitch, self.Hi.ptr, int(self.Hi.pitch), self.Hm.ptr, int(self.Hm.pitch)),
+                "part": (self.partials[0].data_ptr(), self.partials[1].data_ptr()),
+                "plane": 4 * (self.nx + 4) * (self.ny + 4)}
+        return b
+
+    def _step_p(self, src, dst, stream):
+        b = self._bound()
+        _lib.check(b["step"](*b["pre"], *src, *dst, *b["common"], stream), "goc_cdklm_rk2_step")
+
+    def _stage_p(self, src, dst, star, stream):
+        b = self._bound()
+        _lib.check(b["stage"](*b["pre"], *src, *dst, *star, *b["common"], stream), "goc_cdklm_rk2_step_stage")
+
+    def _vjp_p(self, qn, qs, qnext, lam_next, lam_star, lam_n, stream):
+        """step_vjp on addresses (q_next given)."""
+        b = self._bound()
+        f, pre, com = b["vjp"], b["pre"], b["common"]
+        p0, p1 = b["part"]
+        _lib.check(f(*pre, 1, *qs, *qn, *qnext, *lam_next, None, None, None, *lam_star, *lam_n, *com, p0, stream),
+                   "goc_cdklm_stage_vjp_out")
+        _lib.check(f(*pre, 0, *qn, None, None, None, *qs, *lam_star, *lam_n, *lam_n, None, None, None, *com, p1,
+                     stream), "goc_cdklm_stage_vjp_out")
+
     def reset_wind_grad(self):
         self.partials.zero_()
 
     def wind_grad(self):
         """Wind-stress gradient accumulated by step_vjp since the last reset."""
         return self.wsf * self.partials.view(2, -1, 2).sum(dim=(0, 1))
+
+
+def _triple(base, index, plane):
+    """Device addresses of (eta, hu, hv) of state `index` of a stacked
+    (N, 3, ny+4, nx+4) float32 buffer at address `base` (plane: bytes of one
+    field)."""
+    o = base + 3 * index * plane
+    return (o, o + plane, o + 2 * plane)
 
 
 def _rollout_forward(ctx, adj, n_steps, obs_every, init, wind, positions0):
@@ -172,82 +215,122 @@ def _rollout_forward(ctx, adj, n_steps, obs_every, init, wind, positions0):
         raise ValueError("n_steps must be at least obs_every")
     adj.set_wind(wind.detach())
     K = adj.segment_length(n_steps)
-    q = [a.detach().to(torch.float32).contiguous().clone() for a in init]
-    outs, pouts = [], []
-    pos = None
-    track = []
+    dev, (H, W) = adj.device, adj.shape
+    plane = adj._bound()["plane"]
+    sh = torch.cuda.current_stream(dev).cuda_stream
+    q0 = torch.stack([a.detach().to(torch.float32) for a in init])
+    n_obs = n_steps // obs_every
+    pos, track = None, None
     if positions0 is not None:
         pos = positions0.detach().to(torch.float32).contiguous().clone()
-        track = [pos.clone()]
+        track = torch.empty((n_steps + 1,) + tuple(pos.shape), dtype=torch.float32, device=dev)
+        track[0].copy_(pos)
     if K >= n_steps:
-        states, stars = [q], []
+        # the whole trajectory and its first stages
+        states = torch.empty((n_steps + 1, 3, H, W), dtype=torch.float32, device=dev)
+        stars = torch.empty((n_steps, 3, H, W), dtype=torch.float32, device=dev)
+        states[0].copy_(q0)
+        bs, bt = states.data_ptr(), stars.data_ptr()
         for n in range(n_steps):
-            nxt, qs = [torch.empty_like(a) for a in q], [torch.empty_like(a) for a in q]
-            adj.step_with_stage(states[-1], nxt, qs)
-            states.append(nxt)
-            stars.append(qs)
+            adj._stage_p(_triple(bs, n, plane), _triple(bs, n + 1, plane), _triple(bt, n, plane), sh)
             if pos is not None:
-                adj.drift(nxt, pos)
-                track.append(pos.clone())
-            if (n + 1) % obs_every == 0:
-                outs.append(torch.stack([a[2:-2, 2:-2] for a in nxt]))
-                if pos is not None:
-                    pouts.append(pos.clone())
-        ctx.segments = {0: (states, stars)}
+                adj.drift(states[n + 1], pos)
+                track[n + 1].copy_(pos)
+        outs = states[obs_every::obs_every, :, 2:-2, 2:-2][:n_obs].clone()
+        ctx.stored, ctx.ckpt = (states, stars), None
     else:
-        buf = [torch.empty_like(a) for a in q]
-        ctx.segments = {0: ([a.clone() for a in q], None)}
+        # every K-th state; the backward sweep recomputes the segments
+        n_seg = (n_steps + K - 1) // K
+        ckpt = torch.empty((n_seg, 3, H, W), dtype=torch.float32, device=dev)
+        buf = torch.empty((2, 3, H, W), dtype=torch.float32, device=dev)
+        ckpt[0].copy_(q0)
+        buf[0].copy_(q0)
+        outs = torch.empty((n_obs, 3, H - 4, W - 4), dtype=torch.float32, device=dev)
+        bb, cur = buf.data_ptr(), 0
         for n in range(n_steps):
-            adj.step(q, buf)
-            q, buf = buf, q
+            adj._step_p(_triple(bb, cur, plane), _triple(bb, 1 - cur, plane), sh)
+            cur = 1 - cur
             if pos is not None:
-                adj.drift(q, pos)
-                track.append(pos.clone())
+                adj.drift(buf[cur], pos)
+                track[n + 1].copy_(pos)
             if (n + 1) % K == 0 and n + 1 < n_steps:
-                ctx.segments[n + 1] = ([a.clone() for a in q], None)
+                ckpt[(n + 1) // K].copy_(buf[cur])
             if (n + 1) % obs_every == 0:
-                outs.append(torch.stack([a[2:-2, 2:-2] for a in q]))
-                if pos is not None:
-                    pouts.append(pos.clone())
+                outs[(n + 1) // obs_every - 1].copy_(buf[cur, :, 2:-2, 2:-2])
+        ctx.stored, ctx.ckpt = None, ckpt
     ctx.adj, ctx.K, ctx.n_steps, ctx.obs_every, ctx.track = adj, K, n_steps, obs_every, track
-    return torch.stack(outs), (torch.stack(pouts) if pos is not None else None)
+    pouts = track[obs_every::obs_every][:n_obs].clone() if track is not None else None
+    return outs, pouts
 
 
 def _rollout_backward(ctx, grad, grad_pos):
+    """The reverse sweep.  With checkpoints, segment s - 1 is recomputed on a
+    second stream while the sweep runs over segment s (two segment buffers
+    in turn): at grid sizes that leave SMs idle the two overlap."""
     adj, K, n_steps, every = ctx.adj, ctx.K, ctx.n_steps, ctx.obs_every
+    dev, (H, W) = adj.device, adj.shape
+    plane = adj._bound()["plane"]
+    main = torch.cuda.current_stream(dev)
+    mh = main.cuda_stream
     grad = grad.contiguous() if grad is not None else None
-    lam, lam_n, lam_s = adj.zeros(), adj.zeros(), adj.zeros()
+    lam, lam_n, lam_s = (torch.zeros((3, H, W), dtype=torch.float32, device=dev) for _ in range(3))
     adj.reset_wind_grad()
     track = ctx.track
-    pos_bar = torch.zeros_like(track[0]) if track else None
-    for start in sorted(ctx.segments, reverse=True):
-        end = min(start + K, n_steps)
-        states, stars = ctx.segments[start]
-        if stars is None:
-            states, stars = [states], []
-            for _ in range(start, end):
-                nxt = [torch.empty_like(a) for a in states[-1]]
-                qs = [torch.empty_like(a) for a in states[-1]]
-                adj.step_with_stage(states[-1], nxt, qs)
-                states.append(nxt)
-                stars.append(qs)
+    pos_bar = torch.zeros_like(track[0]) if track is not None else None
+
+    def sweep(start, end, states, stars):
+        nonlocal lam, lam_n, pos_bar
+        bs, bt = states.data_ptr(), stars.data_ptr()
+        ls = _triple(lam_s.data_ptr(), 0, plane)
         for n in range(end - 1, start - 1, -1):
+            i = n - start
             if (n + 1) % every == 0:
                 k = (n + 1) // every - 1
                 if grad is not None:
-                    for c in range(3):
-                        lam[c][2:-2, 2:-2] += grad[k, c]
+                    lam[:, 2:-2, 2:-2] += grad[k]
                 if pos_bar is not None and grad_pos is not None:
                     pos_bar += grad_pos[k]
             if pos_bar is not None:
                 # the drift after step n read the state after it
-                adj.drift_vjp(states[n + 1 - start], track[n], pos_bar, lam)
-            adj.step_vjp(states[n - start], stars[n - start], lam, lam_s, lam_n, states[n + 1 - start])
+                adj.drift_vjp(states[i + 1], track[n], pos_bar, lam)
+            adj._vjp_p(_triple(bs, i, plane), _triple(bt, i, plane), _triple(bs, i + 1, plane),
+                       _triple(lam.data_ptr(), 0, plane), ls, _triple(lam_n.data_ptr(), 0, plane), mh)
             lam, lam_n = lam_n, lam
-        del states, stars
-        ctx.segments[start] = None
-    ctx.segments = None
-    ctx.track = None
+
+    if ctx.ckpt is None:
+        states, stars = ctx.stored
+        sweep(0, n_steps, states, stars)
+    else:
+        ckpt = ctx.ckpt
+        order = sorted(range(0, n_steps, K), reverse=True)
+        bufs = [(torch.empty((K + 1, 3, H, W), dtype=torch.float32, device=dev),
+                 torch.empty((K, 3, H, W), dtype=torch.float32, device=dev)) for _ in range(min(2, len(order)))]
+        side = torch.cuda.Stream(dev)
+        sh = side.cuda_stream
+        ready = [torch.cuda.Event() for _ in bufs]
+        free = [torch.cuda.Event() for _ in bufs]
+        side.wait_stream(main)
+
+        def recompute(start, b):
+            st, sr = bufs[b]
+            side.wait_event(free[b])
+            with torch.cuda.stream(side):
+                st[0].copy_(ckpt[start // K])
+            bs, bt = st.data_ptr(), sr.data_ptr()
+            for i in range(min(start + K, n_steps) - start):
+                adj._stage_p(_triple(bs, i, plane), _triple(bs, i + 1, plane), _triple(bt, i, plane), sh)
+            ready[b].record(side)
+
+        recompute(order[0], 0)
+        for idx, start in enumerate(order):
+            b = idx % 2
+            if idx + 1 < len(order):
+                recompute(order[idx + 1], 1 - b)
+            main.wait_event(ready[b])
+            sweep(start, min(start + K, n_steps), *bufs[b])
+            free[b].record(main)
+        main.wait_stream(side)
+    ctx.stored = ctx.ckpt = ctx.track = None
     return lam, adj.wind_grad(), pos_bar
 
 

@@ -1,6 +1,10 @@
 // Adjoint of the CDKLM16 RK2 step: stage VJP kernels and their host entry
-// points.  Compiled like the step (no FMA contraction) so that the forward
-// recompute inside the VJP reproduces the forward step bit for bit.
+// points.  Built with FMA contraction (7 % fewer instructions than without):
+// the forward quantities the VJP recomputes (slopes, reconstructions,
+// fluxes) then differ from the forward kernel's by rounding, so where the
+// forward's limiter or clamp arguments tie to the last bit the VJP may take
+// the other side's subgradient.  Single-simulator and member-batched VJPs
+// run one kernel and agree bit for bit.
 #include <cstdio>
 #include <type_traits>
 
@@ -446,30 +450,6 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
     }
 }
 
-template <bool CONST_F, bool HAS_Y, int TY>
-__global__ void __launch_bounds__(kANT, CONST_F ? 3 : 2)
-stage_vjp_kernel(const GocCdklmParams p, const StepConst k, float dt, int rk_step, const float* xe, const float* xu,
-                 const float* xv, const float* ae, const float* au, const float* av, const float* ye,
-                 const float* yu, const float* yv, const float* ybe,
-                 const float* ybu, const float* ybv, const float* bbe, const float* bbu, const float* bbv,
-                 float* xbe, float* xbu, float* xbv, float* abe, float* abu, float* abv, int pitch,
-                 const float* Hi_g, int hi_pitch, const float* Hm_g, int hm_pitch, float* wind_partials) {
-    extern __shared__ __align__(16) float smem_raw[];
-    const int tx = blockIdx.x, ty = blockIdx.y;
-    const int x0 = 2 + tx * kAX - kAHalo, y0 = 2 + ty * TY - kAHalo;
-    const bool border = x0 < 2 || y0 < 2 || x0 + kAX + 2 * kAHalo > p.nx + 2 || y0 + TY + 2 * kAHalo > p.ny + 2;
-    if (border)
-        stage_vjp_body<kAX, TY, kANT, CONST_F, true, HAS_Y>(p, k, dt, rk_step, tx, ty, xe, xu, xv, ae, au, av, ye,
-                                                             yu, yv, ybe, ybu, ybv, bbe, bbu, bbv, xbe, xbu, xbv, abe,
-                                                             abu, abv, pitch, Hi_g, hi_pitch, Hm_g, hm_pitch,
-                                                             wind_partials, smem_raw);
-    else
-        stage_vjp_body<kAX, TY, kANT, CONST_F, false, HAS_Y>(p, k, dt, rk_step, tx, ty, xe, xu, xv, ae, au, av, ye,
-                                                              yu, yv, ybe, ybu, ybv, bbe, bbu, bbv, xbe, xbu, xbv,
-                                                              abe, abu, abv, pitch, Hi_g, hi_pitch, Hm_g, hm_pitch,
-                                                              wind_partials, smem_raw);
-}
-
 // Tile of position q when the ntx x nty tiles are taken interior tiles first
 // (the rectangle [ix0, ix1) x [iy0, iy1), row by row), then the border frame
 // (the rows below and above the rectangle, then the columns beside it).
@@ -634,33 +614,6 @@ static int goc_cdklm_vjp_partials_count(int nx, int ny) {
     return 2 * ((nx + kAX - 1) / kAX) * ((ny + kAYSmall - 1) / kAYSmall);
 }
 
-static int stage_vjp_impl(const GocCdklmParams* p, float dt, int rk_step, const VjpBuffers& b, int pitch,
-                          const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch, float* wind_partials,
-                          void* stream, const char* who) {
-    int rc = vjp_args(p, rk_step, b, pitch, Hi_pitch, Hm_pitch, Hi, Hm, who);
-    if (rc) return rc;
-    const StepConst k = make_step_const(*p);
-    const bool cf = (p->coriolis_nx == 1 && p->coriolis_ny == 1);
-    cudaStream_t st = as_stream(stream);
-    const int pf = pitch / 4, hip = Hi_pitch / 4, hmp = Hm_pitch / 4;
-    return dispatch_vjp(cf, b.ye != nullptr, small_tiles(p, 1), [&](auto CF, auto HY, auto TY) -> int {
-        constexpr int W = kAX + 2 * kAHalo, H = decltype(TY)::value + 2 * kAHalo;
-        constexpr size_t smem = sizeof(AdjSmem<W, H, !decltype(CF)::value>);
-        auto kern = stage_vjp_kernel<decltype(CF)::value, decltype(HY)::value, decltype(TY)::value>;
-        static bool configured = false;
-        if (!configured) {
-            if (int e = configure_smem(kern, smem)) return e;
-            configured = true;
-        }
-        const dim3 grid((p->nx + kAX - 1) / kAX, (p->ny + TY - 1) / TY);
-        kern<<<grid, kANT, smem, st>>>(*p, k, dt, rk_step, b.xe, b.xu, b.xv, b.ae, b.au, b.av, b.ye, b.yu, b.yv,
-                                       b.ybe, b.ybu, b.ybv, b.bbe, b.bbu, b.bbv, b.xbe, b.xbu, b.xbv, b.abe, b.abu,
-                                       b.abv, pf, Hi, hip, Hm, hmp, wind_partials);
-        count_launch();
-        return check_launch("stage_vjp_kernel");
-    });
-}
-
 static int stage_vjp_members_impl(const GocCdklmParams* p, float dt, int rk_step, const VjpBuffers& b, int pitch,
                                   long long member_stride, int n_members, int wind_stride, const float* Hi,
                                   int Hi_pitch, const float* Hm, int Hm_pitch, float* wind_partials, void* stream,
@@ -709,6 +662,16 @@ static int stage_vjp_members_impl(const GocCdklmParams* p, float dt, int rk_step
         count_launch();
         return check_launch("stage_vjp_members_kernel");
     });
+}
+
+// One simulator: the member-batched kernel with one member, so that single
+// and batched VJPs run the same code and agree bit for bit.
+static int stage_vjp_impl(const GocCdklmParams* p, float dt, int rk_step, const VjpBuffers& b, int pitch,
+                          const float* Hi, int Hi_pitch, const float* Hm, int Hm_pitch, float* wind_partials,
+                          void* stream, const char* who) {
+    const long long plane = (long long)(p->ny + 4) * (pitch / 4);
+    return stage_vjp_members_impl(p, dt, rk_step, b, pitch, plane, 1, 0, Hi, Hi_pitch, Hm, Hm_pitch, wind_partials,
+                                  stream, who);
 }
 
 }  // namespace goc

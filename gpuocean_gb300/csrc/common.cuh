@@ -59,9 +59,18 @@ __device__ __forceinline__ float tex_bilinear(const float* __restrict__ data, in
 
 // Periodic index map onto the interior range [2, n+2) of a grid with two
 // ghost cells: cell k and k +- n are the same cell.
+// Interior index (2 .. n+1) of the periodic image of index k.  Callers'
+// indices lie within a tile's halo of the interior, at most one period away,
+// so one conditional add or subtract does it; the remainder (an integer
+// division, ~20 instructions) is left for grids narrower than a tile.
 __device__ __forceinline__ int wrap_interior(int k, int n) {
-    int m = (k - 2) % n;
+    int m = k - 2;
     if (m < 0) m += n;
+    else if (m >= n) m -= n;
+    if ((unsigned)m >= (unsigned)n) {
+        m %= n;
+        if (m < 0) m += n;
+    }
     return m + 2;
 }
 
