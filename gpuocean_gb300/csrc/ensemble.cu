@@ -127,6 +127,7 @@ static void free_ensemble(Ensemble* e) {
     cudaFree(e->d_tma_err);
     if (e->h_tma_err) cudaFreeHost(const_cast<int*>(e->h_tma_err));
     cudaFree(e->d_tma_tiles);
+    cudaFree(e->d_queue);
     cudaFree(e->d_spare_pool);
     cudaFree(e->d_spare);
     cudaFree(e->d_nsub_noise);
@@ -358,6 +359,8 @@ extern "C" int goc_ensemble_create(const GocMemberDesc* members, int n_members, 
     if (err == cudaSuccess) err = cudaMemset(e->d_nsub, 0, sizeof(int) * n_members);
     if (err == cudaSuccess) err = cudaMemset(e->d_nsub_noise, 0, sizeof(int) * n_members);
     if (err == cudaSuccess) err = cudaMemset(e->d_dt, 0, sizeof(float) * (size_t)n_members * max_substeps);
+    if (err == cudaSuccess) err = cudaMalloc(&e->d_queue, sizeof(int));
+    if (err == cudaSuccess) err = cudaMemset(e->d_queue, 0, sizeof(int));
     if (err != cudaSuccess) {
         free_ensemble(e);
         return set_error(GOC_ERR_CUDA, "goc_ensemble_create: %s", cudaGetErrorString(err));

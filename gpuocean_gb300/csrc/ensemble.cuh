@@ -42,6 +42,7 @@ struct Ensemble {
     int* d_tma_err = nullptr;             // set when a staging wait ran out
     volatile int* h_tma_err = nullptr;    // pinned host copy, refreshed at the end of every block
     unsigned long long* d_tma_tiles = nullptr;  // tiles staged by TMA so far
+    int* d_queue = nullptr;               // work items taken beyond the first gridDim.x (per launch)
     int n_tma_members = 0;
     float* d_dt = nullptr;                // n_members x max_substeps
     int* d_nsub = nullptr;                // n_substeps per member
@@ -131,7 +132,8 @@ ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __res
                     float sensitivity, const CUtensorMap* __restrict__ tmaps,
                     const float* const* __restrict__ tma_base, int* tma_err,
                     unsigned long long* tma_tiles, const GocNoiseDesc* __restrict__ noise,
-                    float* const* __restrict__ spare, int noise_mode, const int* __restrict__ noise_steps) {
+                    float* const* __restrict__ spare, int noise_mode, const int* __restrict__ noise_steps,
+                    int* queue) {
     extern __shared__ __align__(128) float smem_raw[];
     // TMA writes the staging planes on 128-byte boundaries: stage only if the
     // dynamic shared memory starts on one (the pointer itself stays the
@@ -154,9 +156,19 @@ ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __res
     bool perturb = false;   // the current member takes its model error in this launch
     // Work items: the RK2 tiles of step k, then (for k >= 1) the drifter
     // chunks of step k-1, which read the input state of step k (buffer set
-    // k % 2) that no tile of this launch writes.
+    // k % 2) that no tile of this launch writes.  Each CTA takes item
+    // blockIdx.x first, then the next untaken one from a counter (zeroed
+    // before the launch): runs of different lengths and cost, and members
+    // that take no step in this launch, then even out over the CTAs.
+    __shared__ int s_next;
+    auto next_item = [&]() {
+        __syncthreads();
+        if (threadIdx.x == 0) s_next = (int)gridDim.x + atomicAdd(queue, 1);
+        __syncthreads();
+        return s_next;
+    };
     const int n_items = n_tiles + (k >= 1 ? n_chunks : 0);
-    for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+    for (int item = blockIdx.x; item < n_items; item = next_item()) {
         if (item >= n_tiles) {
             const int4 c = drift_chunks[item - n_tiles];
             const int ns = __ldg(nsub + c.x);
@@ -280,11 +292,13 @@ int launch_ensemble(Ensemble* e, int k, cudaStream_t st, const FusedNoise* fn) {
     if (rc) return rc;
     const int items = e->n_runs + (k >= 1 ? e->n_step_chunks : 0);
     const int grid = std::min(items, full);
+    cudaError_t qe = cudaMemsetAsync(e->d_queue, 0, sizeof(int), st);
+    if (qe != cudaSuccess) return set_error(GOC_ERR_CUDA, "ensemble work counter: %s", cudaGetErrorString(qe));
     kern<<<grid, kNT, smem, st>>>(e->d_members, e->d_tiles, e->n_runs, e->d_dt, e->d_nsub, e->max_substeps, k,
                                   e->d_drift_pos, e->d_step_chunks, e->n_step_chunks, e->drift_sensitivity,
                                   e->d_tmaps + (size_t)e->shape * e->n_members * 6, e->d_tma_base, e->d_tma_err,
                                   e->d_tma_tiles, fn ? fn->noise : nullptr, fn ? fn->spare : nullptr,
-                                  fn ? fn->mode : 0, e->d_nsub_noise);
+                                  fn ? fn->mode : 0, e->d_nsub_noise, e->d_queue);
     count_launch();
     return check_launch(NOISE ? "ensemble_rk2_kernel (model error)" : "ensemble_rk2_kernel");
 }
