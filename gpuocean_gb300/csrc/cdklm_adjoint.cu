@@ -115,10 +115,16 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
     __syncthreads();
 
     // 3. forward recompute of the stage on the tile + 2 (without y: with the
-    //    fluxes, which the cell pass needs for the updated state)
-    T.template slopes<2, W - 2, 2, H - 2, CONST_F>();
-    __syncthreads();
-    if constexpr (!HAS_Y) {
+    //    fluxes, which the cell pass needs for the updated state).  With y
+    //    only the slopes the face passes read: x slopes on the tile's rows
+    //    (cells two beyond it in x), y slopes on its columns
+    if constexpr (HAS_Y) {
+        T.template slopes_boxes<kAHalo - 2, kAHalo + TX + 2, kAHalo, kAHalo + TY, kAHalo, kAHalo + TX,
+                                kAHalo - 2, kAHalo + TY + 2, CONST_F>();
+        __syncthreads();
+    } else {
+        T.template slopes<2, W - 2, 2, H - 2, CONST_F>();
+        __syncthreads();
         T.template faces<2, W - 2, 2, H - 2, CONST_F>();
         __syncthreads();
     }

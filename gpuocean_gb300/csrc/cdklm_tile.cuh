@@ -236,12 +236,19 @@ struct Tile {
     // [ux0, ux1) x [uy0-1, uy1+1); `skip` leading rows are left out
     template <int UX0, int UX1, int UY0, int UY1, bool CONST_F>
     __device__ void slopes(int skip = 0) {
-        constexpr int NXS = UX1 - UX0 + 2, NYS = UY1 - UY0;
+        slopes_boxes<UX0 - 1, UX1 + 1, UY0, UY1, UX0, UX1, UY0 - 1, UY1 + 1, CONST_F>(skip);
+    }
+
+    // x slopes on [xx0, xx1) x [xy0, xy1), y slopes on [yx0, yx1) x
+    // [yy0, yy1); `skip` leading rows of each are left out
+    template <int XX0, int XX1, int XY0, int XY1, int YX0, int YX1, int YY0, int YY1, bool CONST_F>
+    __device__ void slopes_boxes(int skip = 0) {
+        constexpr int NXS = XX1 - XX0, NYS = XY1 - XY0;
         const float th = p.theta;
         for (int idx = threadIdx.x; idx < NXS * (NYS - skip); idx += NT) {
             int i, j;
             block_cell<NXS>(idx, NYS - skip, i, j);
-            i += UX0 - 1; j += UY0 + skip;
+            i += XX0; j += XY0 + skip;
             const int gx = x0 + i;
             const float eL = S.D[0][j][i - 1], eC = S.D[0][j][i], eR = S.D[0][j][i + 1];
             const float uL = S.D[1][j][i - 1], uC = S.D[1][j][i], uR = S.D[1][j][i + 1];
@@ -282,11 +289,11 @@ struct Tile {
             Kx = (he > 0.0f) ? Kx : -dxfv - k.two_g * (eC + He);
             S.Sx[2][j][i] = Kx;
         }
-        constexpr int NXY = UX1 - UX0, NYY = UY1 - UY0 + 2;
+        constexpr int NXY = YX1 - YX0, NYY = YY1 - YY0;
         for (int idx = second_loop_thread(NXS * (NYS - skip)); idx < NXY * (NYY - skip); idx += NT) {
             int i, j;
             block_cell<NXY>(idx, NYY - skip, i, j);
-            i += UX0; j += UY0 - 1 + skip;
+            i += YX0; j += YY0 + skip;
             float cnX, cnY;
             north(i, j, cnX, cnY);
             const float eX = cnY, eY = -cnX;  // east vector
