@@ -643,9 +643,15 @@ constexpr int kHandRows = 4;
 // reuses.  Only the RK2 fused path (NSTAGE = 2) streams.  s1 is a run-time
 // value so that one instantiation serves both kinds of tile (the kernel's
 // code stays within the instruction cache).
+// p: the scalar parameters the stage loops read; pm: the member's own
+// parameters, whose texture pointers the tile's set-up reads (the same
+// object for a single simulator; for an ensemble whose members share their
+// scalars, p can then live in the kernel's parameter space, where the loops
+// read it as instruction operands instead of shared-memory loads).
 template <int TX, int TY, int NSTAGE, int NT, bool CONST_F, bool SIMPLE_FORCING, bool BORDER, bool NOISE = false,
           bool ANGLE = false>
-__device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const StepConst& k, float dt, int rk_step,
+__device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const GocCdklmParams& pm,
+                                                const StepConst& k, float dt, int rk_step,
                                                 int tile_x, int tile_y,
                                                 const float* __restrict__ e_in, const float* __restrict__ hu_in,
                                                 const float* __restrict__ hv_in, float* e_out, float* hu_out,
@@ -666,14 +672,14 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const S
     {
         // uniform one-value textures are read once per thread; the north
         // vector with the fast sine / cosine getNorth uses (K/CDKLM16_kernel.cu:78)
-        const float a = __ldg(p.angle);
+        const float a = __ldg(pm.angle);
         T.nX = __sinf(a);
         T.nY = __cosf(a);
-        if (CONST_F) T.f0 = __ldg(p.coriolis_f);
+        if (CONST_F) T.f0 = __ldg(pm.coriolis_f);
         if (SIMPLE_FORCING) {
-            const float wt = p.wind_t;
-            T.wind_X = p.wind_stress_factor * (wt * __ldg(p.wind_x_next) + (1.0f - wt) * __ldg(p.wind_x_cur));
-            T.wind_Y = p.wind_stress_factor * (wt * __ldg(p.wind_y_next) + (1.0f - wt) * __ldg(p.wind_y_cur));
+            const float wt = pm.wind_t;
+            T.wind_X = pm.wind_stress_factor * (wt * __ldg(pm.wind_x_next) + (1.0f - wt) * __ldg(pm.wind_x_cur));
+            T.wind_Y = pm.wind_stress_factor * (wt * __ldg(pm.wind_y_next) + (1.0f - wt) * __ldg(pm.wind_y_cur));
         }
     }
     const int nx = p.nx, ny = p.ny;
@@ -757,13 +763,13 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const S
         desingularize_cell(p, e, hu, hv, hmb, oe, ou, ov);
         S.D[0][j][i] = oe; S.D[1][j][i] = ou; S.D[2][j][i] = ov;
         if (!CONST_F) {
-            if (p.coriolis_cell) {
-                S.Fc[j][i] = __ldg(p.coriolis_cell + (size_t)gy * (p.coriolis_cell_pitch / 4) + gx);
+            if (pm.coriolis_cell) {
+                S.Fc[j][i] = __ldg(pm.coriolis_cell + (size_t)gy * (pm.coriolis_cell_pitch / 4) + gx);
             } else {
                 const int fx = (BORDER && !px) ? T.x0 + i : gx, fy = (BORDER && !py) ? T.y0 + j : gy;
                 const float s = (fx + 0.5f) / (nx + 4.0f);
                 const float t = (fy + 0.5f) / (ny + 4.0f);
-                S.Fc[j][i] = tex_bilinear(p.coriolis_f, p.coriolis_nx, p.coriolis_ny, s, t);
+                S.Fc[j][i] = tex_bilinear(pm.coriolis_f, pm.coriolis_nx, pm.coriolis_ny, s, t);
             }
         }
     }
@@ -987,11 +993,11 @@ __device__ __forceinline__ void cdklm_tile(const GocCdklmParams& p, const StepCo
                                            const float* __restrict__ Hm_g, int hm_pitch, float* smem_raw) {
     if (tile_on_border<TX, TY, NSTAGE>(p, tile_x, tile_y))
         cdklm_tile_body<TX, TY, NSTAGE, NT, CONST_F, SIMPLE_FORCING, true, false, ANGLE>(
-            p, k, dt, rk_step, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, e_alt, hu_alt, hv_alt,
+            p, p, k, dt, rk_step, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, e_alt, hu_alt, hv_alt,
             pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw);
     else
         cdklm_tile_body<TX, TY, NSTAGE, NT, CONST_F, SIMPLE_FORCING, false, false, ANGLE>(
-            p, k, dt, rk_step, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, e_alt, hu_alt, hv_alt,
+            p, p, k, dt, rk_step, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, e_alt, hu_alt, hv_alt,
             pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw);
 }
 
@@ -1004,7 +1010,8 @@ __device__ __forceinline__ void cdklm_tile(const GocCdklmParams& p, const StepCo
 // mirrors of its first rows land in rows it does not take over.  East/west
 // borders keep the hand-over (their mirrors stay within a row).
 template <int TX, int TY, int NT, bool CONST_F, bool SIMPLE_FORCING, bool NOISE = false>
-__device__ __forceinline__ bool cdklm_strip_tile(const GocCdklmParams& p, const StepConst& k, float dt, int tile_x,
+__device__ __forceinline__ bool cdklm_strip_tile(const GocCdklmParams& p, const GocCdklmParams& pm,
+                                                 const StepConst& k, float dt, int tile_x,
                                                  int tile_y, bool reuse, const float* __restrict__ e_in,
                                                  const float* __restrict__ hu_in, const float* __restrict__ hv_in,
                                                  float* e_out, float* hu_out, float* hv_out, int pitch,
@@ -1017,10 +1024,10 @@ __device__ __forceinline__ bool cdklm_strip_tile(const GocCdklmParams& p, const 
     const int s1 = (reuse && y0 >= 2 && y0 + TY + 8 <= p.ny + 2) ? 2 + kHandRows : 2;
     if (border)
         return cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, true, NOISE>(
-            p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
+            p, pm, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
             pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, s1, side_in, side_out, tma, nz);
     return cdklm_tile_body<TX, TY, 2, NT, CONST_F, SIMPLE_FORCING, false, NOISE>(
-        p, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
+        p, pm, k, dt, 1, tile_x, tile_y, e_in, hu_in, hv_in, e_out, hu_out, hv_out, nullptr, nullptr, nullptr,
         pitch, Hi_g, hi_pitch, Hm_g, hm_pitch, smem_raw, s1, side_in, side_out, tma, nz);
 }
 

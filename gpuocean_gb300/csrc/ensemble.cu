@@ -7,6 +7,7 @@
 #include <climits>
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
 
 #include "ensemble.cuh"
 
@@ -339,6 +340,23 @@ extern "C" int goc_ensemble_create(const GocMemberDesc* members, int n_members, 
             for (int i = 0; i < bx; ++i) dt_items.push_back(make_int4(m, i, j, (int)dt_items.size()));
     }
     e->n_dt_items = (int)dt_items.size();
+    // shared scalar parameters: every member's parameters equal member 0's
+    // once the texture pointers are set aside (those stay per member)
+    auto scalars = [](GocCdklmParams q) {
+        q.coriolis_f = q.coriolis_cell = q.angle = nullptr;
+        q.wind_x_cur = q.wind_x_next = q.wind_y_cur = q.wind_y_next = nullptr;
+        q.atm_p_cur = q.atm_p_next = nullptr;
+        q.wind_t = 0.0f;
+        q.atm_p_t = 0.0f;
+        return q;
+    };
+    e->pu = scalars(e->host[0].p);
+    e->uniform = true;
+    for (int m = 1; m < n_members && e->uniform; ++m) {
+        const GocCdklmParams q = scalars(e->host[m].p);
+        e->uniform = std::memcmp(&q, &e->pu, sizeof(q)) == 0;
+    }
+    e->ku = make_step_const(e->pu);
     cudaError_t err = cudaSuccess;
     auto alloc = [&](void** p, size_t bytes) {
         if (err == cudaSuccess) err = cudaMalloc(p, bytes);

@@ -34,6 +34,11 @@ struct Ensemble {
     int max_substeps = 0;
     int n_dt_items = 0;
     bool const_f = true, simple = true;
+    // every member has the same scalar parameters (textures aside): the step
+    // then reads them from the kernel's parameter space (pu, ku)
+    bool uniform = false;
+    GocCdklmParams pu{};
+    StepConst ku{};
     std::vector<GocMemberDesc> host;      // descriptors as created (set 0 current)
     GocMemberDesc* d_members = nullptr;   // device copy, buffers swapped on device
     int4* d_tiles = nullptr;              // runs (member, tile_x, first tile_y, tiles)
@@ -124,9 +129,9 @@ enum NoiseMode : int {
 // spare: per member three buffers (eta, hu, hv) for the unperturbed state,
 // or null entries / a null table; noise_steps: per member the step count of
 // the block if the member takes model error, else 0).
-template <int TX, int TY, int MINB, bool CONST_F, bool SIMPLE_FORCING, bool NOISE>
+template <int TX, int TY, int MINB, bool CONST_F, bool SIMPLE_FORCING, bool NOISE, bool UNI>
 __global__ void __launch_bounds__(kNT, MINB)
-ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __restrict__ tiles, int n_tiles,
+ensemble_rk2_kernel(const GocCdklmParams pu, const StepConst ku, const GocMemberDesc* __restrict__ members, const int4* __restrict__ tiles, int n_tiles,
                     const float* __restrict__ dt_table, const int* __restrict__ nsub, int max_sub, int k,
                     float* const* __restrict__ drift_pos, const int4* __restrict__ drift_chunks, int n_chunks,
                     float sensitivity, const CUtensorMap* __restrict__ tmaps,
@@ -233,8 +238,12 @@ ensemble_rk2_kernel(const GocMemberDesc* __restrict__ members, const int4* __res
             // every thread gets the same answer (it comes from a barrier
             // vote): a CTA whose staged input never landed stops here, with
             // the error flag set for the host
+            // with UNI the stage loops read the shared scalar parameters
+            // from the kernel's parameter space, the member's textures from md
+            const GocCdklmParams& ps = UNI ? pu : md.p;
+            const StepConst& ks = UNI ? ku : kc;
             if (!cdklm_strip_tile<TX, TY, kNT, CONST_F, SIMPLE_FORCING, NOISE>(
-                    md.p, kc, dt, t.y, ty, r > 0, md.eta[in], md.hu[in], md.hv[in], md.eta[out], md.hu[out],
+                    ps, md.p, ks, dt, t.y, ty, r > 0, md.eta[in], md.hu[in], md.hv[in], md.eta[out], md.hu[out],
                     md.hv[out], md.pitch / 4, md.Hi, md.Hi_pitch / 4, md.Hm, md.Hm_pitch / 4, smem_raw, side_in,
                     side_out, &tma, perturb ? &tn : nullptr))
                 goto done;
@@ -255,12 +264,12 @@ constexpr size_t ensemble_smem() {
 
 // Kernel attributes and the persistent grid are set up once per variant,
 // outside any stream capture (goc_ensemble_create calls this).
-template <int TX, int TY, bool CF, bool SF, bool NOISE>
+template <int TX, int TY, bool CF, bool SF, bool NOISE, bool UNI>
 int configure_ensemble_kernel(int* grid_out) {
     constexpr size_t smem = ensemble_smem<TX, TY>();
     static int grid = 0;
     if (grid == 0) {
-        auto kern = ensemble_rk2_kernel<TX, TY, shape_min_blocks<TX, TY>(), CF, SF, NOISE>;
+        auto kern = ensemble_rk2_kernel<TX, TY, shape_min_blocks<TX, TY>(), CF, SF, NOISE, UNI>;
         cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (err != cudaSuccess) return set_error(GOC_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(err));
         int blocks = 0;
@@ -283,44 +292,57 @@ struct FusedNoise {
     int mode;
 };
 
-template <int TX, int TY, bool CF, bool SF, bool NOISE>
+template <int TX, int TY, bool CF, bool SF, bool NOISE, bool UNI>
 int launch_ensemble(Ensemble* e, int k, cudaStream_t st, const FusedNoise* fn) {
     constexpr size_t smem = ensemble_smem<TX, TY>();
-    auto kern = ensemble_rk2_kernel<TX, TY, shape_min_blocks<TX, TY>(), CF, SF, NOISE>;
+    auto kern = ensemble_rk2_kernel<TX, TY, shape_min_blocks<TX, TY>(), CF, SF, NOISE, UNI>;
     int full = 0;
-    int rc = configure_ensemble_kernel<TX, TY, CF, SF, NOISE>(&full);
+    int rc = configure_ensemble_kernel<TX, TY, CF, SF, NOISE, UNI>(&full);
     if (rc) return rc;
     const int items = e->n_runs + (k >= 1 ? e->n_step_chunks : 0);
     const int grid = std::min(items, full);
     cudaError_t qe = cudaMemsetAsync(e->d_queue, 0, sizeof(int), st);
     if (qe != cudaSuccess) return set_error(GOC_ERR_CUDA, "ensemble work counter: %s", cudaGetErrorString(qe));
-    kern<<<grid, kNT, smem, st>>>(e->d_members, e->d_tiles, e->n_runs, e->d_dt, e->d_nsub, e->max_substeps, k,
-                                  e->d_drift_pos, e->d_step_chunks, e->n_step_chunks, e->drift_sensitivity,
-                                  e->d_tmaps + (size_t)e->shape * e->n_members * 6, e->d_tma_base, e->d_tma_err,
-                                  e->d_tma_tiles, fn ? fn->noise : nullptr, fn ? fn->spare : nullptr,
-                                  fn ? fn->mode : 0, e->d_nsub_noise, e->d_queue);
+    kern<<<grid, kNT, smem, st>>>(e->pu, e->ku, e->d_members, e->d_tiles, e->n_runs, e->d_dt, e->d_nsub,
+                                  e->max_substeps, k, e->d_drift_pos, e->d_step_chunks, e->n_step_chunks,
+                                  e->drift_sensitivity, e->d_tmaps + (size_t)e->shape * e->n_members * 6,
+                                  e->d_tma_base, e->d_tma_err, e->d_tma_tiles, fn ? fn->noise : nullptr,
+                                  fn ? fn->spare : nullptr, fn ? fn->mode : 0, e->d_nsub_noise, e->d_queue);
     count_launch();
     return check_launch(NOISE ? "ensemble_rk2_kernel (model error)" : "ensemble_rk2_kernel");
+}
+
+// The variants an ensemble can launch: constant or textured Coriolis,
+// uniform or textured forcing, with or without fused model error, and (with
+// uniform forcing) shared scalar parameters in parameter space.
+template <int TX, int TY, bool CF, bool SF>
+int configure_variants(const Ensemble* e, int* grid) {
+    int g2 = 0;
+    if (SF && e->uniform) {
+        int rc = configure_ensemble_kernel<TX, TY, CF, SF, false, SF>(grid);
+        return rc ? rc : configure_ensemble_kernel<TX, TY, CF, SF, true, SF>(&g2);
+    }
+    int rc = configure_ensemble_kernel<TX, TY, CF, SF, false, false>(grid);
+    return rc ? rc : configure_ensemble_kernel<TX, TY, CF, SF, true, false>(&g2);
 }
 
 // Launchers of one tile shape (explicitly instantiated per shape).
 template <int TX, int TY>
 int ensemble_configure_shape(const Ensemble* e, int* grid) {
-    int g2 = 0, rc;
-    if (e->const_f && e->simple) {
-        rc = configure_ensemble_kernel<TX, TY, true, true, false>(grid);
-        return rc ? rc : configure_ensemble_kernel<TX, TY, true, true, true>(&g2);
-    }
-    if (e->const_f) {
-        rc = configure_ensemble_kernel<TX, TY, true, false, false>(grid);
-        return rc ? rc : configure_ensemble_kernel<TX, TY, true, false, true>(&g2);
-    }
-    if (e->simple) {
-        rc = configure_ensemble_kernel<TX, TY, false, true, false>(grid);
-        return rc ? rc : configure_ensemble_kernel<TX, TY, false, true, true>(&g2);
-    }
-    rc = configure_ensemble_kernel<TX, TY, false, false, false>(grid);
-    return rc ? rc : configure_ensemble_kernel<TX, TY, false, false, true>(&g2);
+    if (e->const_f && e->simple) return configure_variants<TX, TY, true, true>(e, grid);
+    if (e->const_f) return configure_variants<TX, TY, true, false>(e, grid);
+    if (e->simple) return configure_variants<TX, TY, false, true>(e, grid);
+    return configure_variants<TX, TY, false, false>(e, grid);
+}
+
+template <int TX, int TY, bool CF, bool SF>
+int launch_variant(Ensemble* e, int k, cudaStream_t st, const FusedNoise* fn) {
+    const bool noise = fn && fn->noise;
+    if (SF && e->uniform)
+        return noise ? launch_ensemble<TX, TY, CF, SF, true, SF>(e, k, st, fn)
+                     : launch_ensemble<TX, TY, CF, SF, false, SF>(e, k, st, fn);
+    return noise ? launch_ensemble<TX, TY, CF, SF, true, false>(e, k, st, fn)
+                 : launch_ensemble<TX, TY, CF, SF, false, false>(e, k, st, fn);
 }
 
 // fn: the model error of this launch (null: none); fn->noise null means no
@@ -328,16 +350,10 @@ int ensemble_configure_shape(const Ensemble* e, int* grid) {
 // members drift with an unperturbed copy (the plain variant runs then).
 template <int TX, int TY>
 int ensemble_launch_shape(Ensemble* e, int k, cudaStream_t st, const FusedNoise* fn) {
-    if (fn && fn->noise) {
-        if (e->const_f && e->simple) return launch_ensemble<TX, TY, true, true, true>(e, k, st, fn);
-        if (e->const_f) return launch_ensemble<TX, TY, true, false, true>(e, k, st, fn);
-        if (e->simple) return launch_ensemble<TX, TY, false, true, true>(e, k, st, fn);
-        return launch_ensemble<TX, TY, false, false, true>(e, k, st, fn);
-    }
-    if (e->const_f && e->simple) return launch_ensemble<TX, TY, true, true, false>(e, k, st, fn);
-    if (e->const_f) return launch_ensemble<TX, TY, true, false, false>(e, k, st, fn);
-    if (e->simple) return launch_ensemble<TX, TY, false, true, false>(e, k, st, fn);
-    return launch_ensemble<TX, TY, false, false, false>(e, k, st, fn);
+    if (e->const_f && e->simple) return launch_variant<TX, TY, true, true>(e, k, st, fn);
+    if (e->const_f) return launch_variant<TX, TY, true, false>(e, k, st, fn);
+    if (e->simple) return launch_variant<TX, TY, false, true>(e, k, st, fn);
+    return launch_variant<TX, TY, false, false>(e, k, st, fn);
 }
 
 #define GOC_ENSEMBLE_SHAPE_EXTERN(TX, TY)                                           \
