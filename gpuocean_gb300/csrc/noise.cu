@@ -338,8 +338,13 @@ __global__ void kl_xorwow_batched_kernel(const GocKLDesc* __restrict__ kl, const
     }
 }
 
+// Roller set of a perturbation at `substep`: 0 for the perturbations after a
+// block (substep -1: all members, -2: the members that stepped), k + 1 after
+// RK2 step k of a block.
+__host__ __device__ __forceinline__ int kl_roll_set(int substep) { return substep < 0 ? 0 : substep + 1; }
+
 // Rollers of the source members that perturb at `substep`, drawn on the
-// device (one XORWOW state per member): set substep + 1.
+// device (one XORWOW state per member) into roller set kl_roll_set(substep).
 __global__ void kl_roll_batched_kernel(const int* __restrict__ src, curandStateXORWOW_t* states, float4* rollers,
                                        int n, const int* __restrict__ nsub, int substep) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
@@ -347,7 +352,7 @@ __global__ void kl_roll_batched_kernel(const int* __restrict__ src, curandStateX
     if (m >= n || src[m] != m || !member_set(nsub, m, substep, &set)) return;
     curandStateXORWOW_t st = states[m];
     const float a = curand_uniform(&st), b = curand_uniform(&st), c = curand_uniform(&st), d = curand_uniform(&st);
-    rollers[(size_t)(substep + 1) * n + m] = make_float4(a, b, c, d);
+    rollers[(size_t)kl_roll_set(substep) * n + m] = make_float4(a, b, c, d);
     states[m] = st;
 }
 
@@ -721,7 +726,7 @@ extern "C" int goc_kl_batch_generate(void* batch, void* ensemble, int substep, v
     if (!batch || !ensemble) return set_error(GOC_ERR_ARG, "goc_kl_batch_generate: null handle");
     KLBatch* b = static_cast<KLBatch*>(batch);
     if (!b->d_states) return set_error(GOC_ERR_ARG, "goc_kl_batch_generate: call goc_kl_batch_seed first");
-    if (substep + 1 < 0 || substep + 1 >= b->max_sets)
+    if (substep < -2 || kl_roll_set(substep) >= b->max_sets)
         return set_error(GOC_ERR_ARG, "goc_kl_batch_generate: substep %d outside the roller sets", substep);
     cudaStream_t st = as_stream(stream);
     const int* nsub = ensemble_device_noise_steps(ensemble);
@@ -764,12 +769,12 @@ extern "C" int goc_kl_batch_perturb(void* batch, void* ensemble, float perturbat
     int n = 0;
     ensemble_host_members(ensemble, &n);
     if (n != b->n) return set_error(GOC_ERR_ARG, "goc_kl_batch_perturb: ensemble has %d members, batch %d", n, b->n);
-    if (substep + 1 < 0 || substep + 1 >= b->max_sets)
+    if (substep < -2 || kl_roll_set(substep) >= b->max_sets)
         return set_error(GOC_ERR_ARG, "goc_kl_batch_perturb: substep %d outside the roller sets", substep);
     cudaStream_t st = as_stream(stream);
     const int* nsub = ensemble_device_noise_steps(ensemble);
     const GocMemberDesc* dm = ensemble_device_members(ensemble);
-    kl_table_batched_kernel<<<b->n_tab, 128, 0, st>>>(b->d_kl, b->d_src, b->d_rollers, b->n, substep + 1, dm,
+    kl_table_batched_kernel<<<b->n_tab, 128, 0, st>>>(b->d_kl, b->d_src, b->d_rollers, b->n, kl_roll_set(substep), dm,
                                                       b->d_tab_items, nsub, substep);
     count_launch();
     int rc = check_launch("kl_table_batched_kernel");

@@ -3,7 +3,9 @@
 
 All members advance together through the batched engine: one persistent
 launch per RK2 step for the whole ensemble, SOAR model error for all members
-in two launches, drifters advected inside the step launch.
+in two launches, drifters advected inside the step launch.  Members that the
+batched engine does not take (sponge boundaries, a north-angle texture) step
+one by one through their own CUDA path, as the reference's ensemble does.
 """
 from __future__ import annotations
 
@@ -38,8 +40,8 @@ class OceanModelEnsemble:
             self.particles[i] = CDKLM16.CDKLM16(gpu_ctx, **sim_args, **data_args, local_particle_id=i)
             if 'small_scale_perturbation_amplitude' in model_error_args:
                 self.particles[i].setSOARModelError(**model_error_args)
-            elif model_error_args:
-                raise NotImplementedError("only SOAR model error is supported")
+            elif 'kl_scaling' in model_error_args:
+                self.particles[i].setKLModelError(**model_error_args)
             if initialization_variance_factor_ocean_field != 0.0:
                 self.particles[i].perturbState(q0_scale=initialization_variance_factor_ocean_field)
         self.nx, self.ny = self.particles[0].nx, self.particles[0].ny
@@ -50,11 +52,18 @@ class OceanModelEnsemble:
         self.rng_seed = rng_seed if rng_seed is not None else 1234 + 7919 * rank
 
     def _engine(self):
+        """The batched engine over all particles, or None when they step one
+        by one (members the engine rejects)."""
         if self.engine is None:
-            self.engine = BatchedEnsemble(self.particles)
+            try:
+                self.engine = BatchedEnsemble(self.particles)
+            except NotImplementedError as e:
+                self.logger.info("particles step one by one: %s", e)
+                self.engine = False
+                return None
             if all(p.model_error is not None for p in self.particles):
                 self.engine.set_noise([p.model_error for p in self.particles], rng_seed=self.rng_seed)
-        return self.engine
+        return self.engine or None
 
     def attachDrifters(self, drifter_positions):
         for i in range(self.numParticles):
@@ -66,11 +75,11 @@ class OceanModelEnsemble:
                                          domain_size_y=self.data_args['ny'] * self.data_args['dy'])
                 d.setDrifterPositions(drifter_positions)
                 self.particles[i].attachDrifters(d)
-        if self.engine is not None:
+        if self.engine:
             self.engine._build(self.engine.max_substeps)
 
     def cleanUp(self):
-        if self.engine is not None:
+        if self.engine:
             self.engine.release()
         for p in self.particles:
             if p is not None:
@@ -86,6 +95,11 @@ class OceanModelEnsemble:
         from ..SWEsimulators.ObservationSchedule import blocks_to_observation, refresh_dt_after
         eng = self._engine()
         p0 = self.particles[0]
+        if eng is None:
+            for p in self.particles:
+                p.dataAssimilationStep(observation_time, write_now=write_now, courant_number=courant_number)
+            self.t = observation_time
+            return
         plan = blocks_to_observation(observation_time - p0.t, p0.model_time_step)
         eng.updateDt(courant_number=courant_number)
         noisy = eng._noise is not None
@@ -102,6 +116,13 @@ class OceanModelEnsemble:
 
     def modelStep(self, sub_t, rank="", update_dt=True):
         eng = self._engine()
+        if eng is None:
+            for p in self.particles:
+                p.step(sub_t, apply_stochastic_term=p.model_error is not None)
+                if update_dt:
+                    p.updateDt()
+            self.t = self.particles[0].t
+            return self.t
         eng.step(sub_t, apply_stochastic_term=eng._noise is not None, noise_cadence="step")
         if update_dt:
             eng.updateDt()
@@ -109,7 +130,12 @@ class OceanModelEnsemble:
         return self.t
 
     def updateDt(self):
-        self._engine().updateDt()
+        eng = self._engine()
+        if eng is None:
+            for p in self.particles:
+                p.updateDt()
+        else:
+            eng.updateDt()
 
     def observeParticles(self, drifter_positions):
         """hu, hv of every particle at the cells of the given positions,
@@ -119,15 +145,24 @@ class OceanModelEnsemble:
         dx, dy = float(self.data_args['dx']), float(self.data_args['dy'])
         ix = np.floor(pos[:, 0] / dx)
         iy = np.floor(pos[:, 1] / dy)
+        eng = self._engine()
+        if eng is None:
+            out = np.empty((len(self.particles), len(pos), 2))
+            jx, jy = ix.astype(np.int64), iy.astype(np.int64)
+            for k, p in enumerate(self.particles):
+                _, hu, hv = p.download(interior_domain_only=True)
+                out[k, :, 0] = np.asarray(hu)[jy, jx]
+                out[k, :, 1] = np.asarray(hv)[jy, jx]
+            return out
         centres = np.stack([(ix + 0.5) * dx, (iy + 0.5) * dy], axis=1)
-        obs = self._engine().observe(centres, first=0, count=len(self.particles))
+        obs = eng.observe(centres, first=0, count=len(self.particles))
         return obs[:, :, 1:].astype(np.float64)
 
     def getNumParticles(self):
         return self.numParticles
 
     def syncGPU(self):
-        if self.engine is not None:
+        if self.engine:
             self.engine.synchronize()
         for p in self.particles:
             p.gpu_stream.synchronize()

@@ -694,9 +694,10 @@ int goc_kl_perturb(const GocKLDesc* kl, int nx, int ny, float dx, float dy, floa
  * perturbSimilarAs, S/CDKLM16.py:782-790).  goc_kl_batch_seed seeds XORWOW
  * states for every source member's normals and rollers; goc_kl_batch_generate draws new
  * normals and rollers on the device (substep rule of
- * goc_noise_batch_perturb; the rollers go to set substep + 1);
+ * goc_noise_batch_perturb; the rollers go to set 0 for substep -1 or -2,
+ * set substep + 1 otherwise);
  * goc_kl_batch_set_rollers uploads n_sets x n_members x 4 rollers (host;
- * set 0 is used with substep -1, set k + 1 with substep k);
+ * set 0 is used with substep -1 and -2, set k + 1 with substep k);
  * goc_kl_batch_set_random copies host normals for member m's source.
  */
 int goc_kl_batch_create(void* ensemble, const GocKLDesc* kl, const int* source, int max_sets, void** batch);

@@ -231,6 +231,74 @@ def test_ensemble_classes_run(gpu_ctx):
     assert est.shape == (3, 40, 64) and np.all(np.isfinite(est))
 
 
+def test_ocean_model_ensemble_kl_model_error(gpu_ctx):
+    """KL model-error arguments (``kl_scaling`` present) give every particle a
+    KL model error, as E/OceanModelEnsemble.py's constructor does; the batched
+    engine perturbs all members in its block launches.  Two ensembles with
+    the same seed step to identical states, members differ from one another
+    and from the unperturbed run."""
+    from gpuocean_gb300.ensembles.OceanModelEnsemble import OceanModelEnsemble
+    from gpuocean_gb300.SWEsimulators.ModelErrorKL import ModelErrorKL
+    from gpuocean_gb300.utils import BenchmarkCases, Common
+    c = BenchmarkCases.double_jet_case(nx=64, ny=40)
+    sim_args = dict(dt=0.0, g=c["g"], f=c["f"], r=0.0, coriolis_beta=c["coriolis_beta"], model_time_step=60.0)
+    data_args = dict(eta0=c["eta0"], hu0=c["hu0"], hv0=c["hv0"], H=c["H"], nx=64, ny=40, dx=c["dx"], dy=c["dy"],
+                     boundary_conditions=Common.BoundaryConditions(1, 2, 1, 2))
+    kl = dict(kl_decay=1.25, kl_scaling=0.025, basis_x_start=2, basis_x_end=8, basis_y_start=1, basis_y_end=7)
+    runs = []
+    for args in (kl, kl, {}):
+        ens = OceanModelEnsemble(gpu_ctx, sim_args, data_args, args, 3, rng_seed=5)
+        if args:
+            assert all(isinstance(p.model_error, ModelErrorKL) for p in ens.particles)
+        ens.stepToObservation(300.0)
+        ens.syncGPU()
+        assert all(abs(p.t - 300.0) < 1e-6 for p in ens.particles)
+        runs.append([np.asarray(p.download()[0]) for p in ens.particles])
+        ens.cleanUp()
+    assert all(np.array_equal(x, y) for x, y in zip(runs[0], runs[1]))
+    assert all(np.all(np.isfinite(x)) for x in runs[0])
+    assert not np.array_equal(runs[0][0], runs[0][1])
+    assert all(not np.array_equal(x, y) for x, y in zip(runs[0], runs[2]))
+
+
+def test_ocean_model_ensemble_sponge_members_step_one_by_one(gpu_ctx):
+    """Particles with sponge boundaries (not taken by the batched engine)
+    step one by one, each through its own dataAssimilationStep: the states
+    equal a lone simulator's and the observation operator reads their hu, hv
+    at the drifters' cells (E/OceanModelEnsemble.py:168-198)."""
+    from gpuocean_gb300.ensembles.OceanModelEnsemble import OceanModelEnsemble
+    from gpuocean_gb300.SWEsimulators import CDKLM16
+    from gpuocean_gb300.utils import Common
+    nx, ny, dx, dy = 50, 70, 200.0, 200.0
+    x = np.arange(nx + 4) - 2 + 0.5 - nx / 2.0
+    y = np.arange(ny + 4) - 2 + 0.5 - ny / 2.0
+    eta0 = (0.5 * np.exp(-(x[None, :] ** 2 + y[:, None] ** 2) / 50.0)).astype(np.float32)
+    z = np.zeros_like(eta0)
+    H = np.full((ny + 5, nx + 5), 10.0, np.float32)
+    bc = Common.BoundaryConditions(4, 4, 4, 4, spongeCells=dict(north=6, east=6, south=6, west=6))
+    sim_args = dict(dt=0.0, g=9.81, f=0.0, r=0.0, model_time_step=60.0)
+    data_args = dict(eta0=eta0, hu0=z, hv0=z.copy(), H=H, nx=nx, ny=ny, dx=dx, dy=dy, boundary_conditions=bc)
+    ens = OceanModelEnsemble(gpu_ctx, sim_args, data_args, {}, 2)
+    ens.stepToObservation(300.0)
+    assert ens.engine is False
+    lone = CDKLM16.CDKLM16(gpu_ctx, **sim_args, **data_args)
+    lone.dataAssimilationStep(300.0)
+    want = [np.asarray(a) for a in lone.download()]
+    for p in ens.particles:
+        assert abs(p.t - 300.0) < 1e-6
+        for a, b in zip(p.download(), want):
+            assert np.array_equal(np.asarray(a), b)
+    pos = np.array([[1234.0, 4321.0], [9000.0, 100.0]])
+    obs = ens.observeParticles(pos)
+    _, hu, hv = lone.download(interior_domain_only=True)
+    jx, jy = (pos[:, 0] // dx).astype(int), (pos[:, 1] // dy).astype(int)
+    assert obs.shape == (2, 2, 2)
+    assert np.array_equal(obs[1, :, 0], np.asarray(hu)[jy, jx]) and np.array_equal(obs[1, :, 1], np.asarray(hv)[jy, jx])
+    assert np.abs(obs).max() > 0
+    ens.cleanUp()
+    lone.cleanUp()
+
+
 def test_every_tile_shape_gives_identical_states(gpu_ctx):
     """The autotuner may pick any tile shape: each computes bit-identical
     states (the per-cell arithmetic does not depend on the tiling)."""

@@ -131,6 +131,65 @@ def test_kl_batched_equals_single(gpu_ctx):
     ens.release()
 
 
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_kl_block_cadence_equals_member_by_member(gpu_ctx, use_graph):
+    """dataAssimilationStep cadence with KL model error: each block of RK2
+    steps, then one KL perturbation of the members that stepped (roller set
+    0), equals step + perturbSim member by member with the same normals and
+    rollers from twin generators."""
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
+    a = _kl_members(gpu_ctx, 3, 64, 40, 200)
+    b = _kl_members(gpu_ctx, 3, 64, 40, 200)
+    rng = np.random.default_rng(6)
+    normals = [rng.standard_normal((14, 7)).astype(np.float32) for _ in a]
+    for s, t, r in zip(a, b, normals):
+        s.model_error.setRandomNumbers(r)
+        t.model_error.setRandomNumbers(r)
+    ens = BatchedEnsemble(a, autotune=False, use_graph=use_graph)
+    ens.set_noise([s.model_error for s in a])
+    for _ in range(3):
+        ens.step(60.0, apply_stochastic_term=True)
+        for s in b:
+            s.step(60.0, apply_stochastic_term=False)
+            s.model_error.perturbSim(s, update_random_field=False)
+    ens.synchronize()
+    for sa, sb in zip(a, b):
+        assert sa.t == sb.t
+        for x, y in zip(sa.download(), sb.download()):
+            assert np.array_equal(np.asarray(x)[2:-2, 2:-2], np.asarray(y)[2:-2, 2:-2])
+    ens.release()
+
+
+def test_kl_step_cadence_equals_member_by_member(gpu_ctx, monkeypatch):
+    """CDKLM16.step cadence with KL model error: a perturbation after every
+    RK2 step of each member (roller set k + 1 for step k of the block), as
+    CDKLM16.step with the stochastic term does, with the current normals."""
+    from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
+    from gpuocean_gb300.SWEsimulators import CDKLM16
+    a = _kl_members(gpu_ctx, 2, 64, 40, 300)
+    b = _kl_members(gpu_ctx, 2, 64, 40, 300)
+    rng = np.random.default_rng(7)
+    normals = [rng.standard_normal((14, 7)).astype(np.float32) for _ in a]
+    for s, t, r in zip(a, b, normals):
+        s.model_error.setRandomNumbers(r)
+        t.model_error.setRandomNumbers(r)
+    orig = CDKLM16.CDKLM16.perturbState
+    monkeypatch.setattr(CDKLM16.CDKLM16, "perturbState",
+                        lambda self, **kw: orig(self, update_random_field=False))
+    ens = BatchedEnsemble(a, autotune=False)
+    ens.set_noise([s.model_error for s in a])
+    for _ in range(2):
+        ens.step(60.0, apply_stochastic_term=True, noise_cadence="step")
+        for s in b:
+            s.step(60.0, apply_stochastic_term=True)
+    ens.synchronize()
+    for sa, sb in zip(a, b):
+        assert sa.t == sb.t and sa.num_iterations == sb.num_iterations
+        for x, y in zip(sa.download(), sb.download()):
+            assert np.array_equal(np.asarray(x)[2:-2, 2:-2], np.asarray(y)[2:-2, 2:-2])
+    ens.release()
+
+
 def test_kl_multilevel_partner_coupling(gpu_ctx):
     """With sources, the coarse partner is perturbed with its fine partner's
     normals and rollers - what perturbSimSimilarAs does in
