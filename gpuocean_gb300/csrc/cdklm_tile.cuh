@@ -42,18 +42,26 @@ struct StepConst {
     float inv_atm_x, inv_atm_y;  // 1/(2 dx rho), 1/(2 dy rho)
     int periodic_x, periodic_y;
     float one;            // 1, a run-time value for the paired sums (f32x2.cuh)
+    // operands of the paired arithmetic as pairs of equal halves, so that
+    // each is one 64-bit operand read instead of two register moves
+    float2 one2, none2;   // (1, 1), (-1, -1)
+    float2 quarter2, half2;
+    float2 theta2, theta_g2, half_g2, g2, Vc2, Uc2;
 };
 
 template <int W, int H>
 struct TileSmem {
     float D[3][H][W];    // (eta, u, v) after desingularisation
-    float Hmb[H][W];     // cell mean depth (initBm semantics)
+    float Hmb[H][W];     // cell mean depth (initBm semantics); [j][i + 2] holds cell (i, j)
     float Fc[H][W];      // Coriolis f per cell
     float Sx[3][H][W];   // u_x, v_x, dx*Kx at each cell
     float Sy[3][H][W];   // u_y, v_y, dy*Ly at each cell
     float Fx[3][H][W];   // flux through the east face of each cell
     float Gy[3][H][W];   // flux through the north face of each cell
-    float Hi[H + 1][W + 1];  // corner depths, land -> kDryFlag
+    // depth at the south-west corner of each cell, land -> kDryFlag (the
+    // stage code reads corners (j, i) with j < H, i < W only: the corners
+    // north and east of the last row and column are not needed)
+    float Hi[H][W];
 };
 
 // The single-stage kernel with a north-angle texture: each cell sees the
@@ -77,19 +85,21 @@ __device__ __forceinline__ float minmod_slope(float l, float c, float r, float t
 }
 
 // minmod_raw and minmod_slope of two independent triples at once (paired
-// arithmetic, the same roundings; u = 1, StepConst::one).
-__device__ __forceinline__ float2 minmod_raw2(float2 b, float2 c, float2 f, float u) {
+// arithmetic, the same roundings; the unit factors and constants as pairs
+// from the step constants).
+__device__ __forceinline__ float2 minmod_raw2(float2 b, float2 c, float2 f, const StepConst& k) {
     const float2 sb = pr(copysignf(1.0f, b.x), copysignf(1.0f, b.y));
     const float2 sc = pr(copysignf(1.0f, c.x), copysignf(1.0f, c.y));
     const float2 sf = pr(copysignf(1.0f, f.x), copysignf(1.0f, f.y));
     const float2 m = pr(fminf(fminf(fabsf(b.x), fabsf(c.x)), fabsf(f.x)),
                         fminf(fminf(fabsf(b.y), fabsf(c.y)), fabsf(f.y)));
-    return mul2(mul2(mul2(mul2(pr(0.25f), sb), add2(sb, sc, u)), add2(sc, sf, u)), m);
+    return mul2(mul2(mul2(mul2(k.quarter2, sb), add2(sb, sc, k.one2)), add2(sc, sf, k.one2)), m);
 }
 
-__device__ __forceinline__ float2 minmod_slope2(float2 l, float2 c, float2 r, float theta, float u) {
-    return minmod_raw2(mul2(sub2(c, l, u), pr(theta)), mul2(sub2(r, l, u), pr(0.5f)), mul2(sub2(r, c, u), pr(theta)),
-                       u);
+// with theta = p.theta (StepConst::theta2)
+__device__ __forceinline__ float2 minmod_slope2(float2 l, float2 c, float2 r, const StepConst& k) {
+    return minmod_raw2(mul2(sub2n(c, l, k.none2), k.theta2), mul2(sub2n(r, l, k.none2), k.half2),
+                       mul2(sub2n(r, c, k.none2), k.theta2), k);
 }
 
 // K/common.cu:664-666.  The reference's literal 0.5*eps is a double.
@@ -99,22 +109,27 @@ __device__ __forceinline__ float desing(float h, float hu, float eps) {
 }
 
 // Desingularised (eta, u, v) of a raw state, K/CDKLM16_kernel.cu:614-656.
+// Every lane evaluates the wet cell's division; land and shallow cells
+// (rare) are redone under a branch that a warp takes only when one of its
+// lanes has such a cell, so the common case runs without a divergent branch.
 __device__ __forceinline__ void desingularize_cell(const GocCdklmParams& p, float eta, float hu, float hv,
                                                    float Hm, float& oe, float& ou, float& ov) {
     const float h = eta + Hm;
-    if (fabsf(Hm - p.land_value) <= kDryEps) {
-        oe = kDryFlag; ou = 0.0f; ov = 0.0f;
-    } else if (h < p.desing_eps) {
-        if (h <= p.depth_cutoff) {
-            oe = -Hm + p.depth_cutoff; ou = 0.0f; ov = 0.0f;
-        } else {
-            oe = eta;
-            ou = desing(h, hu, p.desing_eps);
-            ov = desing(h, hv, p.desing_eps);
+    const float ih = 1.0f / h;
+    oe = eta; ou = hu * ih; ov = hv * ih;
+    const bool land = fabsf(Hm - p.land_value) <= kDryEps;
+    const bool shallow = h < p.desing_eps;
+    if (__any_sync(__activemask(), land || shallow)) {
+        if (land) {
+            oe = kDryFlag; ou = 0.0f; ov = 0.0f;
+        } else if (shallow) {
+            if (h <= p.depth_cutoff) {
+                oe = -Hm + p.depth_cutoff; ou = 0.0f; ov = 0.0f;
+            } else {
+                ou = desing(h, hu, p.desing_eps);
+                ov = desing(h, hv, p.desing_eps);
+            }
         }
-    } else {
-        const float ih = 1.0f / h;
-        oe = eta; ou = hu * ih; ov = hv * ih;
     }
 }
 
@@ -125,30 +140,28 @@ __device__ __forceinline__ void cdklm_flux(const GocCdklmParams& p, const StepCo
                                            float H, float& F0, float& F1, float& F2) {
     // the plus and minus sides in pairs (x: plus, y: minus); a dry side (h at
     // or below the cutoff) contributes no flux and no wave speed
-    const float u = k.one;
-    const float2 h = add2(pr(ep, em), pr(H), u);
+    const float2 h = add2(pr(ep, em), pr(H), k.one2);
     const float2 hu = mul2(h, pr(up_, um_));
-    const float2 f1 = add2(mul2(hu, pr(up_, um_)), mul2(mul2(pr(k.half_g), h), h), u);
+    const float2 f1 = add2(mul2(hu, pr(up_, um_)), mul2(mul2(k.half_g2, h), h), k.one2);
     const float2 f2 = mul2(hu, pr(vp_, vm_));
-    const float2 gh = mul2(pr(p.g), h);
+    const float2 gh = mul2(k.g2, h);
     const bool wp = h.x > p.depth_cutoff, wm = h.y > p.depth_cutoff;
     const float Fp0 = wp ? hu.x : 0.f, Fp1 = wp ? f1.x : 0.f, Fp2 = wp ? f2.x : 0.f;
     const float Fm0 = wm ? hu.y : 0.f, Fm1 = wm ? f1.y : 0.f, Fm2 = wm ? f2.y : 0.f;
     const float up = wp ? up_ : 0.f, cp = wp ? sqrtf(gh.x) : 0.f;
     const float um = wm ? um_ : 0.f, cm = wm ? sqrtf(gh.y) : 0.f;
-    const float2 lo = sub2(pr(um, up), pr(cm, cp), u);
-    const float2 hi = add2(pr(um, up), pr(cm, cp), u);
+    const float2 lo = sub2n(pr(um, up), pr(cm, cp), k.none2);
+    const float2 hi = add2(pr(um, up), pr(cm, cp), k.one2);
     const float am = fminf(fminf(lo.x, lo.y), 0.0f);
     const float ap = fmaxf(fmaxf(hi.x, hi.y), 0.0f);
-    if (fabsf(ap - am) < p.flux_slope_eps) {
-        F0 = 0.f; F1 = 0.f; F2 = 0.f;
-        return;
-    }
+    // no flux where both wave speeds vanish (near-dry faces, rare): the
+    // general expression is evaluated on every lane and replaced there
+    const bool still = fabsf(ap - am) < p.flux_slope_eps;
     const float inv = 1.0f / (ap - am);
     const float apam = ap * am;
     // (F0, F1) = ((ap Fm - am Fp) + apam (ep - em, Fp0 - Fm0)) inv
-    const float2 t = sub2(mul2(pr(ap), pr(Fm0, Fm1)), mul2(pr(am), pr(Fp0, Fp1)), u);
-    const float2 F01 = mul2(add2(t, mul2(pr(apam), sub2(pr(ep, Fp0), pr(em, Fm0), u)), u), pr(inv));
+    const float2 t = sub2n(mul2(pr(ap), pr(Fm0, Fm1)), mul2(pr(am), pr(Fp0, Fp1)), k.none2);
+    const float2 F01 = mul2(add2(t, mul2(pr(apam), sub2n(pr(ep, Fp0), pr(em, Fm0), k.none2)), k.one2), pr(inv));
     F0 = F01.x;
     F1 = F01.y;
     const float fb = p.flux_balancer;
@@ -157,18 +170,33 @@ __device__ __forceinline__ void cdklm_flux(const GocCdklmParams& p, const StepCo
     float g2 = (um_ > -up_) ? fb * Fm2 : fb * Fp2;
     g2 += (1.0f - fb) * (((s2.x - s2.y) + apam * (hv.x - hv.y)) * inv);
     F2 = g2;
+    if (still) {
+        F0 = 0.f; F1 = 0.f; F2 = 0.f;
+    }
 }
 
-// Issue the TMA copies of the (eta, hu, hv) box at (x, y) (x a multiple of
-// 4) into the staging planes Sx[0], Sx[1], Sy[0].  The caller is one thread,
-// after a barrier that ended every generic access of those planes.
+// Issue the TMA copies of the input boxes of the tile whose staged region
+// starts at (x + 2, y) (x a multiple of 4): eta, hu, hv into the planes
+// Sx[0], Sx[1], Sy[0] (columns x .. x + W) and the edge area (columns
+// x + W .. x + W + 4); with `aux` also the cell-mean depth into the Hmb
+// plane and the Coriolis f into Sy[1] (the same column origin x), with their
+// east boxes.  The caller is one thread, after a barrier that ended every
+// generic access of those planes.
 template <int W, int H>
-__device__ __forceinline__ void tma_stage_tile(TileTma& t, TileSmem<W, H>& S, int x, int y) {
+__device__ __forceinline__ void tma_stage_tile(TileTma& t, TileSmem<W, H>& S, int x, int y, bool aux) {
+    constexpr uint32_t kBox = W * H * sizeof(float), kEdge = 4 * H * sizeof(float);
+    const int naux = aux ? (t.aux_coriolis ? 2 : 1) : 0;
     fence_proxy_async_shared();
-    mbar_arrive_expect_tx(t.bar, 3u * W * H * sizeof(float));
-    tma_load_2d(&S.Sx[0][0][0], t.in_maps + 0, x, y, t.bar);
-    tma_load_2d(&S.Sx[1][0][0], t.in_maps + 1, x, y, t.bar);
-    tma_load_2d(&S.Sy[0][0][0], t.in_maps + 2, x, y, t.bar);
+    mbar_arrive_expect_tx(t.bar, (uint32_t)(3 + naux) * (kBox + kEdge));
+    float* const dst[5] = {&S.Sx[0][0][0], &S.Sx[1][0][0], &S.Sy[0][0][0], &S.Hmb[0][0], &S.Sy[1][0][0]};
+    for (int c = 0; c < 3; ++c) {
+        tma_load_2d(dst[c], t.in_maps + c, x, y, t.bar);
+        tma_load_2d(t.edge + c * 4 * H, t.edge_maps + c, x + W, y, t.bar);
+    }
+    for (int c = 0; c < naux; ++c) {
+        tma_load_2d(dst[3 + c], t.aux_maps + 2 * c, x, y, t.bar);
+        tma_load_2d(t.edge + (3 + c) * 4 * H, t.aux_maps + 2 * c + 1, x + W, y, t.bar);
+    }
 }
 
 // Cell (i, j) of item `idx` of a loop over an NX x ny block of cells.  The
@@ -244,7 +272,6 @@ struct Tile {
     template <int XX0, int XX1, int XY0, int XY1, int YX0, int YX1, int YY0, int YY1, bool CONST_F>
     __device__ void slopes_boxes(int skip = 0) {
         constexpr int NXS = XX1 - XX0, NYS = XY1 - XY0;
-        const float th = p.theta;
         for (int idx = threadIdx.x; idx < NXS * (NYS - skip); idx += NT) {
             int i, j;
             block_cell<NXS>(idx, NYS - skip, i, j);
@@ -253,7 +280,7 @@ struct Tile {
             const float eL = S.D[0][j][i - 1], eC = S.D[0][j][i], eR = S.D[0][j][i + 1];
             const float uL = S.D[1][j][i - 1], uC = S.D[1][j][i], uR = S.D[1][j][i + 1];
             const float vL = S.D[2][j][i - 1], vC = S.D[2][j][i], vR = S.D[2][j][i + 1];
-            const float2 suv = minmod_slope2(pr(uL, vL), pr(uC, vC), pr(uR, vR), th, k.one);
+            const float2 suv = minmod_slope2(pr(uL, vL), pr(uC, vC), pr(uR, vR), k);
             S.Sx[0][j][i] = suv.x;
             S.Sx[1][j][i] = suv.y;
             float lv = vL, cv = vC, rv = vR;
@@ -266,12 +293,12 @@ struct Tile {
             north(i, j, cnX, cnY);
             // (left, right) in pairs
             const float2 lrfv =
-                mul2(add2(mul2(pr(cnX), pr(uL, uR)), mul2(pr(cnY), pr(lv, rv)), k.one), pr(fL, fR));
+                mul2(add2(mul2(pr(cnX), pr(uL, uR)), mul2(pr(cnY), pr(lv, rv)), k.one2), pr(fL, fR));
             const float lfv = lrfv.x, rfv = lrfv.y;
             const float cfv = (cnX * uC + cnY * cv) * fC;
             // (backward, forward) in pairs
-            const float2 bf = mul2(pr(k.theta_g), sub2(sub2(pr(eC, eR), pr(eL, eC), k.one),
-                                                       mul2(pr(k.Vc), add2(pr(cfv), pr(lfv, rfv), k.one)), k.one));
+            const float2 bf = mul2(k.theta_g2, sub2n(sub2n(pr(eC, eR), pr(eL, eC), k.none2),
+                                                     mul2(k.Vc2, add2(pr(cfv), pr(lfv, rfv), k.one2)), k.none2));
             const float cent = k.half_g * (eR - eL - k.Vc * (rfv + 2.0f * cfv + lfv));
             float Kx = minmod_raw(bf.x, cent, bf.y);
             float va = vC;
@@ -301,7 +328,7 @@ struct Tile {
             const float eL = S.D[0][j - 1][i], eC = S.D[0][j][i], eU = S.D[0][j + 1][i];
             const float uL = S.D[1][j - 1][i], uC = S.D[1][j][i], uU = S.D[1][j + 1][i];
             const float vL = S.D[2][j - 1][i], vC = S.D[2][j][i], vU = S.D[2][j + 1][i];
-            const float2 suv = minmod_slope2(pr(uL, vL), pr(uC, vC), pr(uU, vU), th, k.one);
+            const float2 suv = minmod_slope2(pr(uL, vL), pr(uC, vC), pr(uU, vU), k);
             S.Sy[0][j][i] = suv.x;
             S.Sy[1][j][i] = suv.y;
             float lu = uL, cu = uC, uu = uU;
@@ -312,12 +339,12 @@ struct Tile {
             const float fL = F(j - 1, i, CONST_F), fC = F(j, i, CONST_F), fU = F(j + 1, i, CONST_F);
             // (lower, upper) in pairs
             const float2 lufu =
-                mul2(add2(mul2(pr(eX), pr(lu, uu)), mul2(pr(eY), pr(vL, vU)), k.one), pr(fL, fU));
+                mul2(add2(mul2(pr(eX), pr(lu, uu)), mul2(pr(eY), pr(vL, vU)), k.one2), pr(fL, fU));
             const float lfu = lufu.x, ufu = lufu.y;
             const float cfu = (eX * cu + eY * vC) * fC;
             // (backward, forward) in pairs
-            const float2 bf = mul2(pr(k.theta_g), add2(sub2(pr(eC, eU), pr(eL, eC), k.one),
-                                                       mul2(pr(k.Uc), add2(pr(cfu), pr(lfu, ufu), k.one)), k.one));
+            const float2 bf = mul2(k.theta_g2, add2(sub2n(pr(eC, eU), pr(eL, eC), k.none2),
+                                                    mul2(k.Uc2, add2(pr(cfu), pr(lfu, ufu), k.one2)), k.one2));
             const float cent = k.half_g * (eU - eL + k.Uc * (ufu + 2.0f * cfu + lfu));
             float Ly = minmod_raw(bf.x, cent, bf.y);
             float ua = uC;
@@ -350,7 +377,39 @@ struct Tile {
             const float ebm = S.D[0][j][i], ebp = S.D[0][j][i + 1];
             float F0 = 0.f, F1 = 0.f, F2 = 0.f;
             const bool dm = (ebm == kDryFlag), dp = (ebp == kDryFlag);
-            if (!(dm && dp)) {
+            if constexpr (!ANGLE) {
+                // the wet face's flux on every lane; a face with a dry side
+                // (rare) is redone under a branch that a warp takes only when
+                // one of its lanes has one (values of a dry side's
+                // reconstruction are not used)
+                const float um = S.D[1][j][i], up = S.D[1][j][i + 1];
+                float vm = S.D[2][j][i], vp = S.D[2][j][i + 1];
+                const float Rpx = up - 0.5f * S.Sx[0][j][i + 1];
+                const float Rpy = vp - 0.5f * S.Sx[1][j][i + 1];
+                const float Rmx = um + 0.5f * S.Sx[0][j][i];
+                const float Rmy = vm + 0.5f * S.Sx[1][j][i];
+                const float Hf = 0.5f * (S.Hi[j][i + 1] + S.Hi[j + 1][i + 1]);
+                if (BORDER) {
+                    if (p.bc_west == 1 && gxp == 2) vm = -vm;
+                    if (p.bc_east == 1 && gxp == p.nx + 2) vp = -vp;
+                }
+                float ax, ay;
+                north(i, j, ax, ay);
+                const float vpn = up * ax + vp * ay;
+                const float vmn = um * ax + vm * ay;
+                const float etap =
+                    fmaxf(-Hf, ebp - (S.Sx[2][j][i + 1] + p.dx * F(j, i + 1, CONST_F) * vpn) * k.inv_2g);
+                const float etam = fmaxf(-Hf, ebm + (S.Sx[2][j][i] + p.dx * F(j, i, CONST_F) * vmn) * k.inv_2g);
+                cdklm_flux(p, k, etam, Rmx, Rmy, etap, Rpx, Rpy, Hf, F0, F1, F2);
+                // a dry side (rare): no flux but the pressure of the wet side
+                if (__any_sync(__activemask(), dm || dp)) {
+                    if (dm || dp) {
+                        F0 = 0.f; F2 = 0.f;
+                        F1 = (dm && dp) ? 0.f
+                             : dm ? k.half_g * (etap + Hf) * (etap + Hf) : k.half_g * (etam + Hf) * (etam + Hf);
+                    }
+                }
+            } else if (!(dm && dp)) {
                 const float um = S.D[1][j][i], up = S.D[1][j][i + 1];
                 float vm = S.D[2][j][i], vp = S.D[2][j][i + 1];
                 const float Rpx = up - 0.5f * S.Sx[0][j][i + 1];
@@ -400,7 +459,37 @@ struct Tile {
             const float ebm = S.D[0][j][i], ebp = S.D[0][j + 1][i];
             float G0 = 0.f, G1 = 0.f, G2 = 0.f;
             const bool dm = (ebm == kDryFlag), dp = (ebp == kDryFlag);
-            if (!(dm && dp)) {
+            if constexpr (!ANGLE) {
+                float um = S.D[1][j][i], up = S.D[1][j + 1][i];
+                const float vm = S.D[2][j][i], vp = S.D[2][j + 1][i];
+                const float Rpx = up - 0.5f * S.Sy[0][j + 1][i];
+                const float Rpy = vp - 0.5f * S.Sy[1][j + 1][i];
+                const float Rmx = um + 0.5f * S.Sy[0][j][i];
+                const float Rmy = vm + 0.5f * S.Sy[1][j][i];
+                const float Hf = 0.5f * (S.Hi[j + 1][i] + S.Hi[j + 1][i + 1]);
+                if (BORDER) {
+                    if (p.bc_south == 1 && gyp == 2) um = -um;
+                    if (p.bc_north == 1 && gyp == p.ny + 2) up = -up;
+                }
+                float ax, ay;
+                north(i, j, ax, ay);
+                const float eX = ay, eY = -ax;
+                const float upe = up * eX + vp * eY;
+                const float ume = um * eX + vm * eY;
+                const float etap =
+                    fmaxf(-Hf, ebp - (S.Sy[2][j + 1][i] - p.dy * F(j + 1, i, CONST_F) * upe) * k.inv_2g);
+                const float etam = fmaxf(-Hf, ebm + (S.Sy[2][j][i] - p.dy * F(j, i, CONST_F) * ume) * k.inv_2g);
+                float a0, a1, a2;
+                cdklm_flux(p, k, etam, Rmy, Rmx, etap, Rpy, Rpx, Hf, a0, a1, a2);
+                G0 = a0; G1 = a2; G2 = a1;
+                if (__any_sync(__activemask(), dm || dp)) {
+                    if (dm || dp) {
+                        G0 = 0.f; G1 = 0.f;
+                        G2 = (dm && dp) ? 0.f
+                             : dm ? k.half_g * (etap + Hf) * (etap + Hf) : k.half_g * (etam + Hf) * (etam + Hf);
+                    }
+                }
+            } else if (!(dm && dp)) {
                 float um = S.D[1][j][i], up = S.D[1][j + 1][i];
                 const float vm = S.D[2][j][i], vp = S.D[2][j + 1][i];
                 const float Rpx = up - 0.5f * S.Sy[0][j + 1][i];
@@ -482,8 +571,11 @@ struct Tile {
             fd1 = fd1 + (S.Gy[1][j][i] - SF(1)) * k.inv_dy;
             fd2 = fd2 + (S.Gy[2][j][i] - SF(2)) * k.inv_dy;
         }
-        float st1 = 0.0f, st2 = 0.0f;
-        if (hsum >= p.depth_cutoff && ec != kDryFlag) {
+        // source terms of a wet cell, evaluated on every lane; dry and land
+        // cells (rare) have none
+        const bool wet = hsum >= p.depth_cutoff && ec != kDryFlag;
+        float st1, st2;
+        {
             const float tx = (S.Sx[2][j][i] + p.dx * fc * vc) * k.inv_2g;
             const float ty = (S.Sy[2][j][i] - p.dy * fc * uc) * k.inv_2g;
             const float eta_we = 0.5f * ((ec - tx) + (ec + tx));
@@ -533,10 +625,20 @@ struct Tile {
             st1 = X + hu_cor + ax + bath1 * k.inv_dx;
             st2 = Y + hv_cor + ay + bath2 * k.inv_dy;
         }
+        if (!wet) {
+            st1 = 0.0f; st2 = 0.0f;
+        }
         L1 = -fd0;
         L2 = -fd1 + st1;
         L3 = -fd2 + st2;
     }
+
+    // Whether the semi-implicit friction term acts (the same for every cell
+    // of a launch).  Without it C = 0 and the reference's division of the
+    // updated momenta by 1 + C (or 1 + C / 2) is a division by one, which
+    // the fused step leaves out: the approximate division (-prec-div=false)
+    // returns its dividend exactly for a divisor of one.
+    __device__ __forceinline__ bool has_friction() const { return p.r > 0.0f && p.rk_order < 3; }
 
     // Semi-implicit friction coefficient C (K/CDKLM16_kernel.cu:971-983).
     __device__ float friction(float dt, float hsum, float hu, float hv) const {
@@ -625,6 +727,16 @@ __host__ __device__ inline StepConst make_step_const(const GocCdklmParams& p) {
     // 1 for every valid grid, from a run-time value so that the device
     // compiler cannot treat it as a constant
     k.one = p.nx >= 0 ? 1.0f : -1.0f;
+    k.one2 = make_float2(k.one, k.one);
+    k.none2 = make_float2(-k.one, -k.one);
+    k.quarter2 = make_float2(0.25f, 0.25f);
+    k.half2 = make_float2(0.5f, 0.5f);
+    k.theta2 = make_float2(p.theta, p.theta);
+    k.theta_g2 = make_float2(k.theta_g, k.theta_g);
+    k.half_g2 = make_float2(k.half_g, k.half_g);
+    k.g2 = make_float2(p.g, p.g);
+    k.Vc2 = make_float2(k.Vc, k.Vc);
+    k.Uc2 = make_float2(k.Uc, k.Uc);
     return k;
 }
 
@@ -685,19 +797,15 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
     const int nx = p.nx, ny = p.ny;
     const bool px = k.periodic_x, py = k.periodic_y;
 
-    // 1. corner depths, land marked with the dry flag (K/CDKLM16_kernel.cu:571-587)
-    for (int idx = threadIdx.x; idx < (H + 1) * (W + 1); idx += NT) {
-        const int i = idx % (W + 1), j = idx / (W + 1);
-        const int gc = T.x0 + i, gr = T.y0 + j;
-        const int cc = !BORDER ? gc : px ? wrap_interior(gc, nx) : clampi(gc, 0, nx + 4);
-        const int cr = !BORDER ? gr : py ? wrap_interior(gr, ny) : clampi(gr, 0, ny + 4);
-        float v = __ldg(Hi_g + (size_t)cr * hi_pitch + cc);
-        if (fabsf(v - p.land_value) < kDryEps) v = kDryFlag;
-        S.Hi[j][i] = v;
-    }
-    // no barrier here: the loads below do not read the corner depths, so both
-    // phases' global loads are in flight together (the barrier after them
-    // covers both)
+    // A tile whose first stage-1 rows come from the previous tile of its
+    // strip (s1 = 6) reads its halo's south rows only in part: stage 1 reads
+    // Q^n from row 4 on (rows [2, 6) then take the handed-over stage-1
+    // values), stage 2's south-most y slopes read corner-depth rows from 3 on
+    // and Coriolis rows (with a per-cell Coriolis f) from 2 on.  The rows
+    // below are not loaded.
+    const int qr0 = (NSTAGE == 2 && s1 != 2) ? 4 : 0;
+    const int hr0 = (NSTAGE == 2 && s1 != 2) ? 3 : 0;
+    const int fr0 = (NSTAGE == 2 && s1 != 2) ? (CONST_F ? 4 : 2) : 0;
 
     // Q^n of an interior tile may have been staged by TMA into the planes
     // Sx[0], Sx[1], Sy[0] (box from column x0 - 2: TMA boxes start on 16-byte
@@ -719,11 +827,34 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
         }
         tma->phase ^= 1u;
     }
+    // staged depth and Coriolis boxes (launches whose last phase does not
+    // use their planes as model-error scratch)
+    const bool aux = staged && tma->aux;
+    const bool aux_f = aux && tma->aux_coriolis;
+    // field c of local cell (i, j) from its staged boxes: the main box holds
+    // columns from x0 - 2 (plane column i + 2), the east box the last two
+    auto staged_at = [&](const float (&P)[H][W], int c, int i, int j) -> float {
+        const bool east = i >= W - 2;
+        const float* a = east ? tma->edge + (c * H + j) * 4 + (i - (W - 2)) : &P[j][i + 2];
+        return *a;
+    };
 
     // 2. Q^n with wall mirrors and periodic images, desingularised with the
     //    cell-mean depth of the (unmirrored) cell (K/CDKLM16_kernel.cu:614-656)
-    for (int idx = threadIdx.x; idx < H * W; idx += NT) {
-        const int i = idx % W, j = idx / W;
+    //    One loop over the cells from row r0 also loads each cell's corner
+    //    depth (from row hr0; land marked with the dry flag,
+    //    K/CDKLM16_kernel.cu:571-587) and Coriolis f (from row fr0).
+    const int r0 = hr0 < fr0 ? hr0 : fr0;
+    for (int idx = threadIdx.x; idx < (H - r0) * W; idx += NT) {
+        const int i = idx % W, j = r0 + idx / W;
+        if (j >= hr0) {
+            const int gc = T.x0 + i, gr = T.y0 + j;
+            const int cc = !BORDER ? gc : px ? wrap_interior(gc, nx) : clampi(gc, 0, nx + 4);
+            const int cr = !BORDER ? gr : py ? wrap_interior(gr, ny) : clampi(gr, 0, ny + 4);
+            float v = __ldg(Hi_g + (size_t)cr * hi_pitch + cc);
+            if (fabsf(v - p.land_value) < kDryEps) v = kDryFlag;
+            S.Hi[j][i] = v;
+        }
         int gx = T.x0 + i, gy = T.y0 + j;
         int mx = gx, my = gy;
         float su = 1.0f, sv = 1.0f;
@@ -746,24 +877,32 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
             gx = clampi(gx, 0, nx + 3);
             gy = clampi(gy, 0, ny + 3);
         }
-        float e, hu, hv;
-        if (!BORDER && staged && i < W - 2) {
-            e = S.Sx[0][j][i + 2];
-            hu = S.Sx[1][j][i + 2];
-            hv = S.Sy[0][j][i + 2];
-        } else {
-            const size_t o = (size_t)my * pitch + mx;
-            e = __ldg(e_in + o);
-            hu = su * __ldg(hu_in + o);
-            hv = sv * __ldg(hv_in + o);
+        if (j >= qr0) {
+            float e, hu, hv, hmb;
+            if (!BORDER && staged) {
+                e = staged_at(S.Sx[0], 0, i, j);
+                hu = staged_at(S.Sx[1], 1, i, j);
+                hv = staged_at(S.Sy[0], 2, i, j);
+            } else {
+                const size_t o = (size_t)my * pitch + mx;
+                e = __ldg(e_in + o);
+                hu = su * __ldg(hu_in + o);
+                hv = sv * __ldg(hv_in + o);
+            }
+            if (!BORDER && aux) {
+                hmb = staged_at(S.Hmb, 3, i, j);
+            } else {
+                hmb = __ldg(Hm_g + (size_t)gy * hm_pitch + gx);
+                if (i < W - 2) S.Hmb[j][i + 2] = hmb;
+            }
+            float oe, ou, ov;
+            desingularize_cell(p, e, hu, hv, hmb, oe, ou, ov);
+            S.D[0][j][i] = oe; S.D[1][j][i] = ou; S.D[2][j][i] = ov;
         }
-        const float hmb = __ldg(Hm_g + (size_t)gy * hm_pitch + gx);
-        S.Hmb[j][i] = hmb;
-        float oe, ou, ov;
-        desingularize_cell(p, e, hu, hv, hmb, oe, ou, ov);
-        S.D[0][j][i] = oe; S.D[1][j][i] = ou; S.D[2][j][i] = ov;
-        if (!CONST_F) {
-            if (pm.coriolis_cell) {
+        if (!CONST_F && j >= fr0) {
+            if (!BORDER && aux_f) {
+                S.Fc[j][i] = staged_at(S.Sy[1], 4, i, j);
+            } else if (pm.coriolis_cell) {
                 S.Fc[j][i] = __ldg(pm.coriolis_cell + (size_t)gy * (pm.coriolis_cell_pitch / 4) + gx);
             } else {
                 const int fx = (BORDER && !px) ? T.x0 + i : gx, fy = (BORDER && !py) ? T.y0 + j : gy;
@@ -798,10 +937,14 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
             if (!ok) continue;
             float L1, L2, L3, ec, hu, hv, Hm, hsum;
             T.template rhs<CONST_F, SIMPLE_FORCING>(i, j, gxs, gys, L1, L2, L3, ec, hu, hv, Hm, hsum);
-            const float C = T.friction(dt, hsum, hu, hv);
             float ne = ec + dt * L1;
-            float nhu = (hu + dt * L2) / (1.0f + C);
-            float nhv = (hv + dt * L3) / (1.0f + C);
+            float nhu = hu + dt * L2;
+            float nhv = hv + dt * L3;
+            if (T.has_friction()) {
+                const float C = T.friction(dt, hsum, hu, hv);
+                nhu = nhu / (1.0f + C);
+                nhv = nhv / (1.0f + C);
+            }
             finish_cell(p, Hm, ne, nhu, nhv);
             S.Sx[0][j][i] = ne; S.Sx[1][j][i] = nhu; S.Sy[0][j][i] = nhv;
         }
@@ -822,14 +965,14 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
                 e_alt[os] = qe; hu_alt[os] = qu; hv_alt[os] = qv;
             }
             float oe, ou, ov;
-            desingularize_cell(p, qe, qu, qv, S.Hmb[j][i], oe, ou, ov);
+            desingularize_cell(p, qe, qu, qv, S.Hmb[j][i + 2], oe, ou, ov);
             S.D[0][j][i] = oe; S.D[1][j][i] = ou; S.D[2][j][i] = ov;
             if (BORDER) {
                 // wall ghosts of the stage result (K/CDKLM16_kernel.cu:420-470)
                 auto mirror = [&](int ii, int jj, float e, float hu, float hv) {
                     if (ii < 2 || ii >= W - 2 || jj < 2 || jj >= H - 2) return;
                     float me, mu, mv;
-                    desingularize_cell(p, e, hu, hv, S.Hmb[jj][ii], me, mu, mv);
+                    desingularize_cell(p, e, hu, hv, S.Hmb[jj][ii + 2], me, mu, mv);
                     S.D[0][jj][ii] = me; S.D[1][jj][ii] = mu; S.D[2][jj][ii] = mv;
                 };
                 const int gxs = px ? wrap_interior(gx, nx) : gx;
@@ -875,7 +1018,7 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
         // the last phase reads neither Sx[0..1] nor Sy[0..1]: stage the next
         // tile of the strip there meanwhile
         if (tma && tma->next_tile_y >= 0 && threadIdx.x == 0 && *tma->off == 0)
-            tma_stage_tile<W, H>(*tma, S, T.x0 - 2, 2 + tma->next_tile_y * TY - HALO);
+            tma_stage_tile<W, H>(*tma, S, T.x0 - 2, 2 + tma->next_tile_y * TY - HALO, tma->next_aux);
         // model error: the eta perturbation on the tile + 1 ring, into Sy[1]
         // (dead after the faces; the staging above does not touch it), with
         // the cell-mean depths' plane (dead since stage 1) as scratch
@@ -898,10 +1041,14 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
             const float ea = __ldg(e_in + o), hua = __ldg(hu_in + o), hva = __ldg(hv_in + o);
             float L1, L2, L3, ec, hu, hv, Hm, hsum;
             T.template rhs<CONST_F, SIMPLE_FORCING>(i, j, gx, gy, L1, L2, L3, ec, hu, hv, Hm, hsum);
-            const float C = T.friction(dt, hsum, hu, hv);
             float ne = 0.5f * (ea + (ec + dt * L1));
-            float nhu = 0.5f * (hua + (hu + dt * L2)) / (1.0f + 0.5f * C);
-            float nhv = 0.5f * (hva + (hv + dt * L3)) / (1.0f + 0.5f * C);
+            float nhu = 0.5f * (hua + (hu + dt * L2));
+            float nhv = 0.5f * (hva + (hv + dt * L3));
+            if (T.has_friction()) {
+                const float C = T.friction(dt, hsum, hu, hv);
+                nhu = nhu / (1.0f + 0.5f * C);
+                nhv = nhv / (1.0f + 0.5f * C);
+            }
             finish_cell(p, Hm, ne, nhu, nhv);
             if constexpr (NOISE) {
                 if (nz) {

@@ -125,6 +125,7 @@ static void free_ensemble(Ensemble* e) {
     cudaFree(e->d_drift_n);
     cudaFree(e->d_tmaps);
     cudaFree(e->d_tma_base);
+    cudaFree(e->d_tma_aux);
     cudaFree(e->d_tma_err);
     if (e->h_tma_err) cudaFreeHost(const_cast<int*>(e->h_tma_err));
     cudaFree(e->d_tma_tiles);
@@ -154,16 +155,23 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     return fn;
 }
 
-// TMA maps of every member's (eta, hu, hv) in both buffer sets, one box per
-// tile shape (the shape's tile + 4 cells on each side).  A member is staged
-// by TMA when every buffer starts on a 16-byte boundary, its row pitch is a
-// multiple of 16 bytes and every map encodes; otherwise its tiles load Q^n
-// with ordinary loads.
+// TMA maps of every member's (eta, hu, hv) in both buffer sets, one main box
+// per tile shape (the shape's tile + 4 cells on each side, from two columns
+// west of it) and one east box of 4 columns; and of the cell-mean depth and
+// the per-cell Coriolis table (main and east boxes), which the kernel stages
+// with the state when it can.  A member is staged by TMA when every state
+// buffer starts on a 16-byte boundary, its row pitch is a multiple of 16
+// bytes and every map encodes; otherwise its tiles load Q^n with ordinary
+// loads.  The depth (and Coriolis) boxes follow the same rules.
 static int build_tma_maps(Ensemble* e) {
     const int n = e->n_members;
-    std::vector<CUtensorMap> maps((size_t)kNumEnsembleShapes * n * 6);
+    std::vector<CUtensorMap> maps((size_t)kNumEnsembleShapes * n * kTmaMapsPerMember);
     std::vector<const float*> base(n, nullptr);
+    std::vector<int> aux(n, 0);
     const PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    auto aligned = [](const void* p, size_t pitch) {
+        return p != nullptr && reinterpret_cast<uintptr_t>(p) % 16 == 0 && pitch % 16 == 0;
+    };
     e->n_tma_members = 0;
     for (int m = 0; m < n; ++m) {
         const GocMemberDesc& d = e->host[m];
@@ -171,31 +179,46 @@ static int build_tma_maps(Ensemble* e) {
         bool ok = encode != nullptr && d.pitch % 16 == 0;
         for (int set = 0; set < 2; ++set)
             for (int c = 0; c < 3; ++c) ok = ok && reinterpret_cast<uintptr_t>(buf[set][c]) % 16 == 0;
+        bool depth = ok && aligned(d.Hm, (size_t)d.Hm_pitch);
+        bool cor = depth && !e->const_f && aligned(d.p.coriolis_cell, (size_t)d.p.coriolis_cell_pitch);
+        const cuuint64_t dims[2] = {(cuuint64_t)d.p.nx + 4, (cuuint64_t)d.p.ny + 4};
+        const cuuint32_t unit[2] = {1, 1};
+        auto enc = [&](CUtensorMap* map, const void* ptr, size_t pitch, cuuint32_t bx, cuuint32_t by) {
+            const cuuint64_t strides[1] = {(cuuint64_t)pitch};
+            const cuuint32_t box[2] = {bx, by};
+            return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(ptr), dims, strides, box, unit,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+        };
         for (int sh = 0; ok && sh < kNumEnsembleShapes; ++sh) {
-            const cuuint64_t dims[2] = {(cuuint64_t)d.p.nx + 4, (cuuint64_t)d.p.ny + 4};
-            const cuuint64_t strides[1] = {(cuuint64_t)d.pitch};
-            const cuuint32_t box[2] = {(cuuint32_t)kEnsembleShapes[sh].tx + 8, (cuuint32_t)kEnsembleShapes[sh].ty + 8};
-            const cuuint32_t unit[2] = {1, 1};
+            CUtensorMap* mm = &maps[((size_t)sh * n + m) * kTmaMapsPerMember];
+            const cuuint32_t bx = (cuuint32_t)kEnsembleShapes[sh].tx + 8, by = (cuuint32_t)kEnsembleShapes[sh].ty + 8;
             for (int set = 0; ok && set < 2; ++set)
                 for (int c = 0; ok && c < 3; ++c)
-                    ok = encode(&maps[(((size_t)sh * n + m) * 2 + set) * 3 + c], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
-                                buf[set][c], dims, strides, box, unit, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+                    ok = enc(mm + set * 3 + c, buf[set][c], (size_t)d.pitch, bx, by) &&
+                         enc(mm + 6 + set * 3 + c, buf[set][c], (size_t)d.pitch, 4, by);
+            if (depth)
+                depth = enc(mm + 12, d.Hm, (size_t)d.Hm_pitch, bx, by) && enc(mm + 13, d.Hm, (size_t)d.Hm_pitch, 4, by);
+            if (cor)
+                cor = enc(mm + 14, d.p.coriolis_cell, (size_t)d.p.coriolis_cell_pitch, bx, by) &&
+                      enc(mm + 15, d.p.coriolis_cell, (size_t)d.p.coriolis_cell_pitch, 4, by);
         }
         if (ok) {
             base[m] = d.eta[0];
+            aux[m] = depth ? (cor ? 3 : 1) : 0;
             ++e->n_tma_members;
         }
     }
     cudaError_t err = cudaMalloc(&e->d_tmaps, sizeof(CUtensorMap) * maps.size());
     if (err == cudaSuccess) err = cudaMalloc(&e->d_tma_base, sizeof(const float*) * n);
+    if (err == cudaSuccess) err = cudaMalloc(&e->d_tma_aux, sizeof(int) * n);
     if (err == cudaSuccess) err = cudaMalloc(&e->d_tma_err, sizeof(int));
     if (err == cudaSuccess) err = cudaMalloc(&e->d_tma_tiles, sizeof(unsigned long long));
     if (err == cudaSuccess)
         err = cudaMemcpy(e->d_tmaps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice);
     if (err == cudaSuccess)
         err = cudaMemcpy(e->d_tma_base, base.data(), sizeof(const float*) * n, cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMemcpy(e->d_tma_aux, aux.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
     if (err == cudaSuccess) err = cudaMemset(e->d_tma_err, 0, sizeof(int));
     if (err == cudaSuccess) {
         int* h = nullptr;

@@ -18,12 +18,14 @@ namespace goc {
 struct TileShape { int tx, ty; };
 constexpr TileShape kEnsembleShapes[] = {{32, 16}, {32, 8}, {16, 16}, {64, 8}, {32, 24}};
 constexpr int kNumEnsembleShapes = sizeof(kEnsembleShapes) / sizeof(kEnsembleShapes[0]);
+constexpr int kTmaMapsPerMember = 16;
 
 // CTAs per SM the shared memory of a shape allows (at most 3), used as the
 // launch-bounds occupancy target of its kernel.
 template <int TX, int TY>
 constexpr int shape_min_blocks() {
-    constexpr size_t b = sizeof(TileSmem<TX + 8, TY + 8>) + 2 * 3 * kHandRows * (TX + 8) * sizeof(float) + 1024;
+    constexpr size_t b = sizeof(TileSmem<TX + 8, TY + 8>) + 2 * 3 * kHandRows * (TX + 8) * sizeof(float) +
+                         5 * (TY + 8) * 4 * sizeof(float) + 1024;
     return (int)(3 * b <= 228 * 1024 ? 3 : 2 * b <= 228 * 1024 ? 2 : 1);
 }
 
@@ -42,8 +44,12 @@ struct Ensemble {
     std::vector<GocMemberDesc> host;      // descriptors as created (set 0 current)
     GocMemberDesc* d_members = nullptr;   // device copy, buffers swapped on device
     int4* d_tiles = nullptr;              // runs (member, tile_x, first tile_y, tiles)
-    CUtensorMap* d_tmaps = nullptr;       // [shape][member][buffer set][eta, hu, hv] TMA maps of the state
+    // [shape][member][kTmaMapsPerMember] TMA maps: eta, hu, hv main boxes of
+    // buffer sets 0 and 1, their east boxes, then the cell-mean depth and the
+    // Coriolis table (main, east)
+    CUtensorMap* d_tmaps = nullptr;
     const float** d_tma_base = nullptr;   // per member: set-0 eta buffer (null: member not staged by TMA)
+    int* d_tma_aux = nullptr;             // per member: bit 0 depth boxes staged, bit 1 Coriolis boxes too
     int* d_tma_err = nullptr;             // set when a staging wait ran out
     volatile int* h_tma_err = nullptr;    // pinned host copy, refreshed at the end of every block
     unsigned long long* d_tma_tiles = nullptr;  // tiles staged by TMA so far
@@ -135,7 +141,7 @@ ensemble_rk2_kernel(const GocCdklmParams pu, const StepConst ku, const GocMember
                     const float* __restrict__ dt_table, const int* __restrict__ nsub, int max_sub, int k,
                     float* const* __restrict__ drift_pos, const int4* __restrict__ drift_chunks, int n_chunks,
                     float sensitivity, const CUtensorMap* __restrict__ tmaps,
-                    const float* const* __restrict__ tma_base, int* tma_err,
+                    const float* const* __restrict__ tma_base, const int* __restrict__ tma_aux, int* tma_err,
                     unsigned long long* tma_tiles, const GocNoiseDesc* __restrict__ noise,
                     float* const* __restrict__ spare, int noise_mode, const int* __restrict__ noise_steps,
                     int* queue) {
@@ -154,7 +160,7 @@ ensemble_rk2_kernel(const GocCdklmParams pu, const StepConst ku, const GocMember
         tma_off = 0;
     }
     __syncthreads();
-    TileTma tma{nullptr, &tma_bar, 0u, false, -1, &tma_off, tma_err};
+    TileTma tma{nullptr, nullptr, nullptr, false, nullptr, &tma_bar, 0u, false, false, false, -1, &tma_off, tma_err};
     unsigned staged_tiles = 0;  // counted by thread 0
     int cur = -1;
     TileNoise tn{&nd, nullptr, nullptr, nullptr};
@@ -218,7 +224,18 @@ ensemble_rk2_kernel(const GocCdklmParams pu, const StepConst ku, const GocMember
         // is read after a barrier, so the choice is the same in every thread
         const float* base = tma_base[m];
         const bool use_tma = base != nullptr && tma_off == 0 && smem_aligned;
-        tma.in_maps = use_tma ? tmaps + ((size_t)m * 2 + (md.eta[in] == base ? 0 : 1)) * 3 : nullptr;
+        const CUtensorMap* mm = tmaps + (size_t)m * kTmaMapsPerMember;
+        const int set = md.eta[in] == base ? 0 : 1;
+        tma.in_maps = use_tma ? mm + set * 3 : nullptr;
+        tma.edge_maps = mm + 6 + set * 3;
+        const int auxf = use_tma ? __ldg(tma_aux + m) : 0;
+        tma.aux_maps = (auxf & 1) ? mm + 12 : nullptr;
+        tma.aux_coriolis = (auxf & 2) != 0;
+        tma.edge = side + 2 * NSIDE;
+        // depth and Coriolis boxes of a run's later tiles are staged during the
+        // previous tile's last phase, whose planes the fused model error uses
+        // as scratch when this member perturbs in this launch
+        tma.next_aux = tma.aux_maps != nullptr && !perturb;
         bool pending = false;  // the previous tile of the run staged this one
         for (int r = 0; r < t.w; ++r) {
             const int ty = t.z + r;
@@ -226,10 +243,13 @@ ensemble_rk2_kernel(const GocCdklmParams pu, const StepConst ku, const GocMember
             // staging point and read here after a barrier: a copy of this
             // tile was issued exactly when `pending` and tma_off is still 0
             tma.staged = use_tma && tma_off == 0 && !tile_on_border<TX, TY, 2>(md.p, t.y, ty);
+            // its depth / Coriolis boxes: staged with the first tile of a run,
+            // or by the previous tile when that could
+            tma.aux = tma.staged && tma.aux_maps != nullptr && (pending ? tma.next_aux : true);
             staged_tiles += tma.staged ? 1u : 0u;
             if (tma.staged && !pending && threadIdx.x == 0)
                 tma_stage_tile<TX + 8, TY + 8>(tma, *reinterpret_cast<TileSmem<TX + 8, TY + 8>*>(smem_raw),
-                                               t.y * TX - 4, 2 + ty * TY - 4);
+                                               t.y * TX - 4, 2 + ty * TY - 4, tma.aux);
             tma.next_tile_y =
                 (use_tma && r + 1 < t.w && !tile_on_border<TX, TY, 2>(md.p, t.y, ty + 1)) ? ty + 1 : -1;
             // stage-1 rows handed along the run through two alternating buffers
@@ -255,11 +275,13 @@ done:
     if (threadIdx.x == 0 && staged_tiles) atomicAdd(tma_tiles, (unsigned long long)staged_tiles);
 }
 
-// Dynamic shared memory of the persistent kernel: the tile planes plus two
-// hand-over buffers of stage-1 rows.
+// Dynamic shared memory of the persistent kernel: the tile planes, two
+// hand-over buffers of stage-1 rows and the east boxes of the TMA staging
+// (5 fields x rows x 4 columns).
 template <int TX, int TY>
 constexpr size_t ensemble_smem() {
-    return sizeof(TileSmem<TX + 8, TY + 8>) + 2 * 3 * kHandRows * (TX + 8) * sizeof(float);
+    return sizeof(TileSmem<TX + 8, TY + 8>) + 2 * 3 * kHandRows * (TX + 8) * sizeof(float) +
+           5 * (TY + 8) * 4 * sizeof(float);
 }
 
 // Kernel attributes and the persistent grid are set up once per variant,
@@ -305,8 +327,9 @@ int launch_ensemble(Ensemble* e, int k, cudaStream_t st, const FusedNoise* fn) {
     if (qe != cudaSuccess) return set_error(GOC_ERR_CUDA, "ensemble work counter: %s", cudaGetErrorString(qe));
     kern<<<grid, kNT, smem, st>>>(e->pu, e->ku, e->d_members, e->d_tiles, e->n_runs, e->d_dt, e->d_nsub,
                                   e->max_substeps, k, e->d_drift_pos, e->d_step_chunks, e->n_step_chunks,
-                                  e->drift_sensitivity, e->d_tmaps + (size_t)e->shape * e->n_members * 6,
-                                  e->d_tma_base, e->d_tma_err, e->d_tma_tiles, fn ? fn->noise : nullptr,
+                                  e->drift_sensitivity,
+                                  e->d_tmaps + (size_t)e->shape * e->n_members * kTmaMapsPerMember,
+                                  e->d_tma_base, e->d_tma_aux, e->d_tma_err, e->d_tma_tiles, fn ? fn->noise : nullptr,
                                   fn ? fn->spare : nullptr, fn ? fn->mode : 0, e->d_nsub_noise, e->d_queue);
     count_launch();
     return check_launch(NOISE ? "ensemble_rk2_kernel (model error)" : "ensemble_rk2_kernel");

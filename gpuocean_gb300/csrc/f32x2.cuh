@@ -51,4 +51,9 @@ __device__ __forceinline__ float2 add2(float2 a, float2 b, float u) { return fma
 // a - b (u = 1 at run time): b * (-1) + a
 __device__ __forceinline__ float2 sub2(float2 a, float2 b, float u) { return fma2(b, pr(-u), a); }
 
+// The same with the unit factor given as a pair, u2 = (u, u) and
+// nu2 = (-u, -u), read from memory as one 64-bit operand.
+__device__ __forceinline__ float2 add2(float2 a, float2 b, float2 u2) { return fma2(a, u2, b); }
+__device__ __forceinline__ float2 sub2n(float2 a, float2 b, float2 nu2) { return fma2(b, nu2, a); }
+
 }  // namespace goc

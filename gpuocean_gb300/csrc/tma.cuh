@@ -74,15 +74,25 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
 // Time after which a staging wait gives up (far longer than any copy takes).
 constexpr uint64_t kTmaWaitLimitNs = 200000000ull;  // 0.2 s
 
-// Per-CTA state of the staging of one tile's (eta, hu, hv) (Q^n) by TMA.
+// Per-CTA state of the staging of one tile's inputs by TMA: Q^n (eta, hu,
+// hv) and, when `aux` is set, the cell-mean depth and the per-cell Coriolis
+// f.  Each field comes as a main box of the tile's width starting two
+// columns west of the tile (x on a 16-byte boundary) and a 4-column box east
+// of it for the last two columns.
 struct TileTma {
-    const CUtensorMap* in_maps;  // eta, hu, hv maps of the input buffer set (null: no staging)
-    uint64_t* bar;               // completes when a staged tile has landed
-    uint32_t phase;              // parity of the barrier phase to wait for next
-    bool staged;                 // this tile's Q^n is (being) staged
-    int next_tile_y;             // tile row to stage during this tile's last phase (-1: none)
-    int* off;                    // shared flag: a wait ran out, the CTA stops staging
-    int* err;                    // global flag the host reads
+    const CUtensorMap* in_maps;    // eta, hu, hv main boxes of the input set (null: no staging)
+    const CUtensorMap* edge_maps;  // eta, hu, hv east boxes of the input set
+    const CUtensorMap* aux_maps;   // cell-mean depth main + east, Coriolis main + east (null: none)
+    bool aux_coriolis;             // aux_maps has the Coriolis boxes
+    float* edge;                   // shared [5][rows][4]: east boxes of eta, hu, hv, depth, Coriolis
+    uint64_t* bar;                 // completes when a staged tile has landed
+    uint32_t phase;                // parity of the barrier phase to wait for next
+    bool staged;                   // this tile's Q^n is (being) staged
+    bool aux;                      // ... and its depth / Coriolis boxes too
+    bool next_aux;                 // stage the next tile's depth / Coriolis boxes as well
+    int next_tile_y;               // tile row to stage during this tile's last phase (-1: none)
+    int* off;                      // shared flag: a wait ran out, the CTA stops staging
+    int* err;                      // global flag the host reads
 };
 
 }  // namespace goc

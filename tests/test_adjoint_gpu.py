@@ -449,8 +449,16 @@ def test_rollout_gradient_of_moving_bump_matches_fp64_fd(ctx):
 def test_step_vjp_from_stage_outputs_equals_recompute(ctx):
     """The stage VJPs given the stage outputs (Q* and Q^{n+1} as the forward
     wrote them) skip the recompute of the stages' fluxes; without dry cells
-    their results are bit-identical to the recomputing VJPs, for one
-    simulator and for a batch of members."""
+    their results agree with the recomputing VJPs to rounding, for one
+    simulator and for a batch of members.  The adjoint translation unit
+    contracts multiply-adds and the two kernel variants recompute the
+    forward slopes on different boxes, so the compiler may contract them
+    differently: measured differences are a few ulps (2.9e-6 at values up
+    to 27)."""
+
+    def close(a, b):
+        torch.testing.assert_close(a, b, rtol=2e-6, atol=2e-6 * float(b.abs().max()))
+
     from gpuocean_gb300.adjoint import EnsembleStepAdjoint, StepAdjoint
     c = dict(_bump_case(64, moving=True), wind=(1.0e-4, -6.0e-5))
     sim = _sim(ctx, c, 2.0)
@@ -470,7 +478,7 @@ def test_step_vjp_from_stage_outputs_equals_recompute(ctx):
         adj.step_vjp(q, qs, lam, ls, ln, q_next)
         out.append([a.clone() for a in ln] + [adj.wind_grad().clone()])
     for a, b in zip(*out):
-        assert torch.equal(a, b)
+        close(a, b)
     n = 3
     eadj = EnsembleStepAdjoint(sim, n)
     base = torch.stack([a for a in q]).unsqueeze(0).repeat(n, 1, 1, 1).contiguous()
@@ -486,7 +494,8 @@ def test_step_vjp_from_stage_outputs_equals_recompute(ctx):
         eadj.reset_wind_grad()
         eadj.step_vjp(base, es, elam, ls, ln, q_next)
         out.append((ln[..., 2:-2, 2:-2].clone(), eadj.wind_grad().clone()))
-    assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])
+    close(out[0][0], out[1][0])
+    close(out[0][1], out[1][1])
     sim.cleanUp()
 
 

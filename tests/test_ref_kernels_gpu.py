@@ -168,6 +168,45 @@ def test_friction_odd_grid_random_state(ctx):
     sim.cleanUp()
 
 
+def test_land_and_drying_beach_bit_identical(ctx):
+    """An island of land cells (masked depths) and a beach that starts dry
+    (eta = -H) and floods under a wave from the east: the land, dry-face and
+    shallow-cell (desingularised) paths of the step against the reference
+    kernel, bit for bit, with bottom friction."""
+    nx, ny = 77, 45
+    x = np.arange(nx + 5, dtype=np.float32)[None, :]
+    H = (10.0 * (0.02 + np.clip((x - 8.0) / 25.0, 0.0, 1.0)) * np.ones((ny + 5, 1), np.float32)).astype(np.float32)
+    H = np.ma.array(H, mask=np.zeros(H.shape, bool))
+    H.mask[20:26, 40:46] = True
+    xc = np.arange(nx + 4)[None, :] - 2 + 0.5
+    yc = np.arange(ny + 4)[:, None] - 2 + 0.5
+    eta = (0.6 * np.exp(-((xc - 30.0) ** 2 + (yc - 22.0) ** 2) / 40.0)).astype(np.float32)
+    eta[:, :10] = -np.float32(0.2)   # the beach's cells (depth 0.2 m) start dry
+    z = np.zeros_like(eta)
+    c = dict(eta0=eta, hu0=z, hv0=z.copy(), H=H, nx=nx, ny=ny, dx=150.0, dy=170.0, g=9.81, f=1.0e-4, r=2.4e-3,
+             coriolis_beta=0.0, boundary=(1, 1, 1, 1))
+    sim = _product(ctx, c, 0.0)
+    sim.updateDt(courant_number=0.5)
+    dt = float(sim.dt)
+    ref = _reference("cdklm_fric77", c, dt, sim)
+    for _ in range(300):
+        sim.step(dt)
+        ref.step(dt)
+    (de, dhu, dhv), theirs = _diffs(sim, ref, nx, ny)
+    e = np.ma.getdata(theirs[0]).astype(np.float64)
+    Hm = np.asarray(sim.downloadBathymetry()[1])[2:ny + 2, 2:nx + 2].astype(np.float64)
+    land = Hm > 1e10
+    h = np.where(land, np.nan, e + Hm)
+    n_dry = int(np.sum(h <= 1e-5))
+    n_shallow = int(np.sum((h > 1e-5) & (h < 0.1)))
+    print(json.dumps({"case": "land + drying beach 77x45, 300 steps", "max_abs_diff": [de, dhu, dhv],
+                      "land": int(land.sum()), "dry": n_dry, "shallow": n_shallow}))
+    assert land.sum() > 0 and n_dry > 0 and n_shallow > 0
+    assert de == 0.0 and dhu == 0.0 and dhv == 0.0, (de, dhu, dhv)
+    ref.free()
+    sim.cleanUp()
+
+
 def _soar_q0(L_cells=8.0, std=0.003):
     oy, ox = np.mgrid[-2:3, -2:3]
     d = np.sqrt(ox ** 2 + oy ** 2) / L_cells
