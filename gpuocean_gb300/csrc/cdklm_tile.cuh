@@ -921,11 +921,12 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
         T.template faces<2, W - 2, 2, H - 2, CONST_F>(s1 - 2);
         __syncthreads();
         const int nu = (W - 4) * (H - 2 - s1);
-        // Results go to the planes Sx[0], Sx[1], Sy[0] (dead after the faces:
-        // the cell update reads only Sx[2] and Sy[2]) and become D* once
-        // every thread has read its cell of D^n.  A rolled loop keeps one copy
-        // of the cell update in the kernel (the step is sensitive to the
-        // instruction cache).
+        // The update of a cell reads D^n of that cell only (its neighbours
+        // enter through the flux and slope planes), so each result is
+        // desingularised into D* at once; the wall mirrors write ghost cells,
+        // whose own update is skipped.  A rolled loop keeps one copy of the
+        // cell update in the kernel (the step is sensitive to the instruction
+        // cache).
         for (int idx = threadIdx.x; idx < nu; idx += NT) {
             int i, j;
             block_cell<W - 4>(idx, H - 2 - s1, i, j);
@@ -937,27 +938,15 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
             if (!ok) continue;
             float L1, L2, L3, ec, hu, hv, Hm, hsum;
             T.template rhs<CONST_F, SIMPLE_FORCING>(i, j, gxs, gys, L1, L2, L3, ec, hu, hv, Hm, hsum);
-            float ne = ec + dt * L1;
-            float nhu = hu + dt * L2;
-            float nhv = hv + dt * L3;
+            float qe = ec + dt * L1;
+            float qu = hu + dt * L2;
+            float qv = hv + dt * L3;
             if (T.has_friction()) {
                 const float C = T.friction(dt, hsum, hu, hv);
-                nhu = nhu / (1.0f + C);
-                nhv = nhv / (1.0f + C);
+                qu = qu / (1.0f + C);
+                qv = qv / (1.0f + C);
             }
-            finish_cell(p, Hm, ne, nhu, nhv);
-            S.Sx[0][j][i] = ne; S.Sx[1][j][i] = nhu; S.Sy[0][j][i] = nhv;
-        }
-        __syncthreads();
-        for (int idx = threadIdx.x; idx < nu; idx += NT) {
-            int i, j;
-            block_cell<W - 4>(idx, H - 2 - s1, i, j);
-            i += 2; j += s1;
-            const int gx = T.x0 + i, gy = T.y0 + j;
-            const bool okx = !BORDER || px || (gx >= 2 && gx < nx + 2);
-            const bool oky = !BORDER || py || (gy >= 2 && gy < ny + 2);
-            if (!(okx && oky)) continue;
-            const float qe = S.Sx[0][j][i], qu = S.Sx[1][j][i], qv = S.Sy[0][j][i];
+            finish_cell(p, Hm, qe, qu, qv);
             // the first-stage state of the tile's own cells, when asked for
             // (the adjoint's second-stage VJP reads it)
             if (e_alt && i >= HALO && i < HALO + TX && j >= HALO && j < HALO + TY && gx < nx + 2 && gy < ny + 2) {
@@ -969,14 +958,12 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
             S.D[0][j][i] = oe; S.D[1][j][i] = ou; S.D[2][j][i] = ov;
             if (BORDER) {
                 // wall ghosts of the stage result (K/CDKLM16_kernel.cu:420-470)
-                auto mirror = [&](int ii, int jj, float e, float hu, float hv) {
+                auto mirror = [&](int ii, int jj, float me0, float mu0, float mv0) {
                     if (ii < 2 || ii >= W - 2 || jj < 2 || jj >= H - 2) return;
                     float me, mu, mv;
-                    desingularize_cell(p, e, hu, hv, S.Hmb[jj][ii + 2], me, mu, mv);
+                    desingularize_cell(p, me0, mu0, mv0, S.Hmb[jj][ii + 2], me, mu, mv);
                     S.D[0][jj][ii] = me; S.D[1][jj][ii] = mu; S.D[2][jj][ii] = mv;
                 };
-                const int gxs = px ? wrap_interior(gx, nx) : gx;
-                const int gys = py ? wrap_interior(gy, ny) : gy;
                 if (p.bc_north == 1) {
                     if (gys == ny + 1) mirror(i, j + 1, qe, qu, -qv);
                     if (gys == ny) mirror(i, j + 3, qe, qu, -qv);
