@@ -50,16 +50,6 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
     const int nx = p.nx, ny = p.ny;
     const bool px = k.periodic_x, py = k.periodic_y;
 
-    // 1. corner depths (as the forward kernel)
-    for (int idx = threadIdx.x; idx < (H + 1) * (W + 1); idx += NT) {
-        const int i = idx % (W + 1), j = idx / (W + 1);
-        const int gc = T.x0 + i, gr = T.y0 + j;
-        const int cc = !BORDER ? gc : px ? wrap_interior(gc, nx) : clampi(gc, 0, nx + 4);
-        const int cr = !BORDER ? gr : py ? wrap_interior(gr, ny) : clampi(gr, 0, ny + 4);
-        float v = __ldg(Hi_g + (size_t)cr * hi_pitch + cc);
-        if (fabsf(v - p.land_value) < kDryEps) v = kDryFlag;
-        S.Hi[j][i] = v;
-    }
     // staged position -> memory cell it reads, with the wall-mirror signs
     auto source = [&](int i, int j, int& mx, int& my, int& hx, int& hy, float& su, float& sv) {
         int gx = T.x0 + i, gy = T.y0 + j;
@@ -85,9 +75,18 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
         }
         hx = gx; hy = gy;
     };
-    // 2. x on the tile + 4, desingularised; adjoint accumulators cleared
+    // 1. x on the tile + 4, desingularised, and the corner depths (as the
+    //    forward kernel); adjoint accumulators cleared
     for (int idx = threadIdx.x; idx < H * W; idx += NT) {
         const int i = idx % W, j = idx / W;
+        {
+            const int gc = T.x0 + i, gr = T.y0 + j;
+            const int cc = !BORDER ? gc : px ? wrap_interior(gc, nx) : clampi(gc, 0, nx + 4);
+            const int cr = !BORDER ? gr : py ? wrap_interior(gr, ny) : clampi(gr, 0, ny + 4);
+            float v = __ldg(Hi_g + (size_t)cr * hi_pitch + cc);
+            if (fabsf(v - p.land_value) < kDryEps) v = kDryFlag;
+            S.Hi[j][i] = v;
+        }
         int mx, my, hx, hy;
         float su, sv;
         source(i, j, mx, my, hx, hy, su, sv);
@@ -114,7 +113,7 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
     }
     __syncthreads();
 
-    // 3. forward recompute of the stage on the tile + 2 (without y: with the
+    // 2. forward recompute of the stage on the tile + 2 (without y: with the
     //    fluxes, which the cell pass needs for the updated state).  With y
     //    only the slopes the face passes read: x slopes on the tile's rows
     //    (cells two beyond it in x), y slopes on its columns
@@ -129,7 +128,7 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
         __syncthreads();
     }
 
-    // 4. cell pass: RK combination, friction and source terms in reverse.
+    // 3. cell pass: RK combination, friction and source terms in reverse.
     //    The flux-divergence adjoints stay in registers until every cell has
     //    read the fluxes, then replace them in the Gy planes.
     float wXb = 0.0f, wYb = 0.0f;
@@ -295,7 +294,7 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
     // pass leaves ghost cells out), so walls need no more.
     constexpr int T0X = kAHalo, T1X = kAHalo + TX, T0Y = kAHalo, T1Y = kAHalo + TY;
 
-    // 5. faces in reverse, two colours each.  x faces are coloured as a
+    // 4. faces in reverse, two colours each.  x faces are coloured as a
     //    checkerboard ((i + j) even / odd): faces of one row never share a
     //    cell.  A warp takes 16 faces of a row and 16 of the next: the
     //    stride-2 accesses of one half-warp cover 32 consecutive floats, and
@@ -335,7 +334,7 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
         }
         __syncthreads();
     }
-    // 6. x slopes in reverse (three colours); their adjoints are complete
+    // 5. x slopes in reverse (three colours); their adjoints are complete
     //    once the x faces are done
     constexpr int NXS = TX + 2, NYS = TY;       // x slopes of cells [T0X - 1, T1X + 1) on the tile's rows
 #pragma unroll 1
@@ -356,7 +355,7 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
         for (int c = 0; c < 3; ++c) S.Fx[c][j][i] = 0.0f;
     }
     __syncthreads();
-    // 7. y faces and y slopes in reverse
+    // 6. y faces and y slopes in reverse
     if (!p.one_dimensional) {
         constexpr int NXG = TX, NYG = TY + 3;     // north faces of rows [T0Y - 2, T1Y + 1) on the tile's columns
 #pragma unroll 1
@@ -388,7 +387,7 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
         __syncthreads();
     }
 
-    // 8. desingularisation in reverse at the tile's positions (border tiles:
+    // 7. desingularisation in reverse at the tile's positions (border tiles:
     //    also the two rings around it, where the wall mirrors of its cells
     //    lie), as the adjoint of the memory cell each read (signs of the wall
     //    mirrors); the result per position goes to the Gy planes
@@ -414,7 +413,7 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
     }
     __syncthreads();
 
-    // 9. x-bar of the tile's interior cells: own position plus the wall
+    // 8. x-bar of the tile's interior cells: own position plus the wall
     //    mirror positions that read it
     for (int idx = threadIdx.x; idx < TX * TY; idx += NT) {
         const int i = kAHalo + idx % TX, j = kAHalo + idx / TX;
@@ -436,7 +435,7 @@ __device__ void stage_vjp_body(const GocCdklmParams& p, const StepConst& k, floa
         xbe[o] = s0; xbu[o] = s1; xbv[o] = s2;
     }
 
-    // 10. wind-stress adjoint of the tile's cells
+    // 9. wind-stress adjoint of the tile's cells
     if (wind_partials) {
         __shared__ float red[2][NT / 32];
         for (int off = 16; off > 0; off >>= 1) {

@@ -37,7 +37,7 @@ struct AdjSmem {
     float Fx[3][H][W];
     float Gy[3][H][W];
     float Db[3][H][W];      // adjoint of the desingularised (eta, u, v)
-    float Hi[H + 1][W + 1];
+    float Hi[H][W];         // south-west corner depth of each cell (the passes read corners < (H, W))
     float Fc[HAS_FC ? H : 1][HAS_FC ? W : 1];
 };
 
