@@ -801,11 +801,10 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
     // strip (s1 = 6) reads its halo's south rows only in part: stage 1 reads
     // Q^n from row 4 on (rows [2, 6) then take the handed-over stage-1
     // values), stage 2's south-most y slopes read corner-depth rows from 3 on
-    // and Coriolis rows (with a per-cell Coriolis f) from 2 on.  The rows
-    // below are not loaded.
-    const int qr0 = (NSTAGE == 2 && s1 != 2) ? 4 : 0;
-    const int hr0 = (NSTAGE == 2 && s1 != 2) ? 3 : 0;
-    const int fr0 = (NSTAGE == 2 && s1 != 2) ? (CONST_F ? 4 : 2) : 0;
+    // and Coriolis rows (with a per-cell Coriolis f) from 2 on.  All fields
+    // are loaded from row 2 on (the rows below are not loaded): one row start
+    // for every field costs less than a test per cell and field.
+    const int r0 = (NSTAGE == 2 && s1 != 2) ? 2 : 0;
 
     // Q^n of an interior tile may have been staged by TMA into the planes
     // Sx[0], Sx[1], Sy[0] (box from column x0 - 2: TMA boxes start on 16-byte
@@ -842,12 +841,11 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
     // 2. Q^n with wall mirrors and periodic images, desingularised with the
     //    cell-mean depth of the (unmirrored) cell (K/CDKLM16_kernel.cu:614-656)
     //    One loop over the cells from row r0 also loads each cell's corner
-    //    depth (from row hr0; land marked with the dry flag,
-    //    K/CDKLM16_kernel.cu:571-587) and Coriolis f (from row fr0).
-    const int r0 = hr0 < fr0 ? hr0 : fr0;
+    //    depth (land marked with the dry flag, K/CDKLM16_kernel.cu:571-587)
+    //    and Coriolis f.
     for (int idx = threadIdx.x; idx < (H - r0) * W; idx += NT) {
         const int i = idx % W, j = r0 + idx / W;
-        if (j >= hr0) {
+        {
             const int gc = T.x0 + i, gr = T.y0 + j;
             const int cc = !BORDER ? gc : px ? wrap_interior(gc, nx) : clampi(gc, 0, nx + 4);
             const int cr = !BORDER ? gr : py ? wrap_interior(gr, ny) : clampi(gr, 0, ny + 4);
@@ -877,7 +875,7 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
             gx = clampi(gx, 0, nx + 3);
             gy = clampi(gy, 0, ny + 3);
         }
-        if (j >= qr0) {
+        {
             float e, hu, hv, hmb;
             if (!BORDER && staged) {
                 e = staged_at(S.Sx[0], 0, i, j);
@@ -899,7 +897,7 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
             desingularize_cell(p, e, hu, hv, hmb, oe, ou, ov);
             S.D[0][j][i] = oe; S.D[1][j][i] = ou; S.D[2][j][i] = ov;
         }
-        if (!CONST_F && j >= fr0) {
+        if (!CONST_F) {
             if (!BORDER && aux_f) {
                 S.Fc[j][i] = staged_at(S.Sy[1], 4, i, j);
             } else if (pm.coriolis_cell) {
