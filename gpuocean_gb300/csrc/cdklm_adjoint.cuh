@@ -111,35 +111,28 @@ __device__ __forceinline__ void desingularize_cell_vjp(const GocCdklmParams& p, 
     }
 }
 
-// Reverse of cdklm_flux (H constant).
+// Reverse of cdklm_flux (H constant).  Branch-free: a dry side's terms and
+// the case of vanishing wave speeds are evaluated on every lane and replaced
+// by selects (the adjoint is checked against FP64 autograd, not for bits).
 __device__ __forceinline__ void cdklm_flux_vjp(const GocCdklmParams& p, const StepConst& k, float em, float um_,
                                                float vm_, float ep, float up_, float vp_, float H, float F0b,
                                                float F1b, float F2b, float& emb, float& umb, float& vmb,
                                                float& epb, float& upb, float& vpb) {
-    emb = umb = vmb = epb = upb = vpb = 0.0f;
     const float hp = ep + H;
     const float hm = em + H;
     const bool wp = hp > p.depth_cutoff, wm = hm > p.depth_cutoff;
-    float Fp0 = 0.f, Fp1 = 0.f, Fp2 = 0.f, up = 0.f, cp = 0.f;
-    if (wp) {
-        Fp0 = hp * up_;
-        Fp1 = hp * up_ * up_ + k.half_g * hp * hp;
-        Fp2 = hp * up_ * vp_;
-        up = up_;
-        cp = sqrtf(p.g * hp);
-    }
-    float Fm0 = 0.f, Fm1 = 0.f, Fm2 = 0.f, um = 0.f, cm = 0.f;
-    if (wm) {
-        Fm0 = hm * um_;
-        Fm1 = hm * um_ * um_ + k.half_g * hm * hm;
-        Fm2 = hm * um_ * vm_;
-        um = um_;
-        cm = sqrtf(p.g * hm);
-    }
+    const float Fp0 = wp ? hp * up_ : 0.f;
+    const float Fp1 = wp ? hp * up_ * up_ + k.half_g * hp * hp : 0.f;
+    const float Fp2 = wp ? hp * up_ * vp_ : 0.f;
+    const float up = wp ? up_ : 0.f, cp = wp ? sqrtf(p.g * hp) : 0.f;
+    const float Fm0 = wm ? hm * um_ : 0.f;
+    const float Fm1 = wm ? hm * um_ * um_ + k.half_g * hm * hm : 0.f;
+    const float Fm2 = wm ? hm * um_ * vm_ : 0.f;
+    const float um = wm ? um_ : 0.f, cm = wm ? sqrtf(p.g * hm) : 0.f;
     const float A = um + cm, B = up + cp, C = um - cm, D = up - cp;
     const float am = fminf(fminf(C, D), 0.0f);
     const float ap = fmaxf(fmaxf(A, B), 0.0f);
-    if (fabsf(ap - am) < p.flux_slope_eps) return;
+    const bool still = fabsf(ap - am) < p.flux_slope_eps;
     const float inv = 1.0f / (ap - am);
     const float apam = ap * am;
     const float fb = p.flux_balancer;
@@ -149,8 +142,8 @@ __device__ __forceinline__ void cdklm_flux_vjp(const GocCdklmParams& p, const St
     const float N2 = (ap * Fm2 - am * Fp2) + apam * dv;
     const float N0b = F0b * inv, N1b = F1b * inv, N2b = F2b * (1.0f - fb) * inv;
     const float invb = F0b * N0 + F1b * N1 + F2b * (1.0f - fb) * N2;
-    float Fm2b = 0.f, Fp2b = 0.f;
-    if (um_ > -up_) Fm2b = F2b * fb; else Fp2b = F2b * fb;
+    const bool upwind_m = um_ > -up_;
+    float Fm2b = upwind_m ? F2b * fb : 0.f, Fp2b = upwind_m ? 0.f : F2b * fb;
     float apb = N0b * Fm0 + N1b * Fm1 + N2b * Fm2;
     float amb = -(N0b * Fp0 + N1b * Fp1 + N2b * Fp2);
     const float apamb = N0b * (ep - em) + N1b * (Fp0 - Fm0) + N2b * dv;
@@ -158,11 +151,11 @@ __device__ __forceinline__ void cdklm_flux_vjp(const GocCdklmParams& p, const St
     const float Fm1b = N1b * ap, Fp1b = -N1b * am;
     Fm2b += N2b * ap;
     Fp2b += -N2b * am;
-    epb = N0b * apam;
-    emb = -N0b * apam;
+    float ep_b = N0b * apam;
+    float em_b = -N0b * apam;
     float hpb = N2b * apam * vp_, hmb = -N2b * apam * vm_;
-    vpb = N2b * apam * hp;
-    vmb = -N2b * apam * hm;
+    float vp_b = N2b * apam * hp;
+    float vm_b = -N2b * apam * hm;
     apb += apamb * am;
     amb += apamb * ap;
     apb -= invb * inv * inv;
@@ -177,22 +170,28 @@ __device__ __forceinline__ void cdklm_flux_vjp(const GocCdklmParams& p, const St
     const float Cb = amb * ws * wC, Db = amb * ws * (1.0f - wC);
     const float umb_m = Ab + Cb, cmb = Ab - Cb;
     const float upb_m = Bb + Db, cpb = Bb - Db;
-    if (wm) {
-        umb += umb_m;
-        if (cm > 0.0f) hmb += cmb * 0.5f * p.g / cm;
-        hmb += Fm0b * um_ + Fm1b * (um_ * um_ + p.g * hm) + Fm2b * um_ * vm_;
-        umb += Fm0b * hm + Fm1b * 2.0f * hm * um_ + Fm2b * hm * vm_;
-        vmb += Fm2b * hm * um_;
+    // the wet sides' terms (a dry side has none)
+    float um_b = 0.f, up_b = 0.f;
+    {
+        const float hmb_w = (cm > 0.0f ? cmb * 0.5f * p.g / cm : 0.0f) + Fm0b * um_ +
+                            Fm1b * (um_ * um_ + p.g * hm) + Fm2b * um_ * vm_;
+        const float umb_w = umb_m + Fm0b * hm + Fm1b * 2.0f * hm * um_ + Fm2b * hm * vm_;
+        const float vmb_w = Fm2b * hm * um_;
+        if (wm) { hmb += hmb_w; um_b += umb_w; vm_b += vmb_w; }
+        const float hpb_w = (cp > 0.0f ? cpb * 0.5f * p.g / cp : 0.0f) + Fp0b * up_ +
+                            Fp1b * (up_ * up_ + p.g * hp) + Fp2b * up_ * vp_;
+        const float upb_w = upb_m + Fp0b * hp + Fp1b * 2.0f * hp * up_ + Fp2b * hp * vp_;
+        const float vpb_w = Fp2b * hp * up_;
+        if (wp) { hpb += hpb_w; up_b += upb_w; vp_b += vpb_w; }
     }
-    if (wp) {
-        upb += upb_m;
-        if (cp > 0.0f) hpb += cpb * 0.5f * p.g / cp;
-        hpb += Fp0b * up_ + Fp1b * (up_ * up_ + p.g * hp) + Fp2b * up_ * vp_;
-        upb += Fp0b * hp + Fp1b * 2.0f * hp * up_ + Fp2b * hp * vp_;
-        vpb += Fp2b * hp * up_;
-    }
-    epb += hpb;
-    emb += hmb;
+    ep_b += hpb;
+    em_b += hmb;
+    emb = still ? 0.f : em_b;
+    umb = still ? 0.f : um_b;
+    vmb = still ? 0.f : vm_b;
+    epb = still ? 0.f : ep_b;
+    upb = still ? 0.f : up_b;
+    vpb = still ? 0.f : vp_b;
 }
 
 // Reverse of Tile::friction: C-bar -> (hsum, hu, hv)-bar (adds).
@@ -253,7 +252,6 @@ struct AdjTile {
         SM& S = A;
         const float ebm = S.D[0][j][i], ebp = S.D[0][j][i + 1];
         const bool dm = (ebm == kDryFlag), dp = (ebp == kDryFlag);
-        if (dm && dp) return;
         const int gxp = T.x0 + i + 1;
         const float um = S.D[1][j][i], up = S.D[1][j][i + 1];
         float vm = S.D[2][j][i], vp = S.D[2][j][i + 1];
@@ -276,15 +274,16 @@ struct AdjTile {
         const float xm = ebm + (S.Sx[2][j][i] + p.dx * fm * vmn) * k.inv_2g;
         const float etap = fmaxf(-Hf, xp);
         const float etam = fmaxf(-Hf, xm);
-        float etapb = 0.f, etamb = 0.f;
-        float Rpxb = 0.f, Rpyb = 0.f, Rmxb = 0.f, Rmyb = 0.f;
-        if (dm) {
-            etapb = F1b * p.g * (etap + Hf);
-        } else if (dp) {
-            etamb = F1b * p.g * (etam + Hf);
-        } else {
-            cdklm_flux_vjp(p, k, etam, Rmx, Rmy, etap, Rpx, Rpy, Hf, F0b, F1b, F2b, etamb, Rmxb, Rmyb, etapb, Rpxb,
-                           Rpyb);
+        // the wet face on every lane; a face with a land side (rare) is redone
+        // under a branch that a warp takes only when one of its lanes has one
+        float etapb, etamb, Rpxb, Rpyb, Rmxb, Rmyb;
+        cdklm_flux_vjp(p, k, etam, Rmx, Rmy, etap, Rpx, Rpy, Hf, F0b, F1b, F2b, etamb, Rmxb, Rmyb, etapb, Rpxb, Rpyb);
+        if (__any_sync(__activemask(), dm || dp)) {
+            if (dm || dp) {
+                Rpxb = 0.f; Rpyb = 0.f; Rmxb = 0.f; Rmyb = 0.f;
+                etapb = (dm && !dp) ? F1b * p.g * (etap + Hf) : 0.f;
+                etamb = (dp && !dm) ? F1b * p.g * (etam + Hf) : 0.f;
+            }
         }
         // etap = max(-Hf, xp): xp-bar only where xp is taken
         const float xpb = etapb * (xp > -Hf ? 1.0f : (xp == -Hf ? 0.5f : 0.0f));
@@ -313,7 +312,6 @@ struct AdjTile {
         SM& S = A;
         const float ebm = S.D[0][j][i], ebp = S.D[0][j + 1][i];
         const bool dm = (ebm == kDryFlag), dp = (ebp == kDryFlag);
-        if (dm && dp) return;
         const int gyp = T.y0 + j + 1;
         const float eX = T.nY, eY = -T.nX;
         float um = S.D[1][j][i], up = S.D[1][j + 1][i];
@@ -337,16 +335,16 @@ struct AdjTile {
         const float xm = ebm + (S.Sy[2][j][i] - p.dy * fm * ume) * k.inv_2g;
         const float etap = fmaxf(-Hf, xp);
         const float etam = fmaxf(-Hf, xm);
-        float etapb = 0.f, etamb = 0.f;
-        float Rpxb = 0.f, Rpyb = 0.f, Rmxb = 0.f, Rmyb = 0.f;
-        if (dm) {
-            etapb = G2b * p.g * (etap + Hf);
-        } else if (dp) {
-            etamb = G2b * p.g * (etam + Hf);
-        } else {
-            // forward: cdklm_flux(etam, Rmy, Rmx, etap, Rpy, Rpx) -> (a0, a1, a2), G = (a0, a2, a1)
-            cdklm_flux_vjp(p, k, etam, Rmy, Rmx, etap, Rpy, Rpx, Hf, G0b, G2b, G1b, etamb, Rmyb, Rmxb, etapb, Rpyb,
-                           Rpxb);
+        // forward: cdklm_flux(etam, Rmy, Rmx, etap, Rpy, Rpx) -> (a0, a1, a2), G = (a0, a2, a1);
+        // the wet face on every lane, land faces under a warp vote
+        float etapb, etamb, Rpxb, Rpyb, Rmxb, Rmyb;
+        cdklm_flux_vjp(p, k, etam, Rmy, Rmx, etap, Rpy, Rpx, Hf, G0b, G2b, G1b, etamb, Rmyb, Rmxb, etapb, Rpyb, Rpxb);
+        if (__any_sync(__activemask(), dm || dp)) {
+            if (dm || dp) {
+                Rpxb = 0.f; Rpyb = 0.f; Rmxb = 0.f; Rmyb = 0.f;
+                etapb = (dm && !dp) ? G2b * p.g * (etap + Hf) : 0.f;
+                etamb = (dp && !dm) ? G2b * p.g * (etam + Hf) : 0.f;
+            }
         }
         const float xpb = etapb * (xp > -Hf ? 1.0f : (xp == -Hf ? 0.5f : 0.0f));
         const float xmb = etamb * (xm > -Hf ? 1.0f : (xm == -Hf ? 0.5f : 0.0f));
