@@ -52,17 +52,17 @@ struct AdjSmem {
 // sign, else 0.
 __device__ __forceinline__ void minmod_raw_vjp(float b, float c, float f, float gb, float& bb, float& cb,
                                                float& fb) {
-    bb = cb = fb = 0.0f;
     const float sb = copysignf(1.0f, b), sc = copysignf(1.0f, c), sf = copysignf(1.0f, f);
-    if (!(sb == sc && sc == sf)) return;
+    // no adjoint where the signs differ (branch-free: selects)
+    const float g = (sb == sc && sc == sf) ? gb : 0.0f;
     const float ab = fabsf(b), ac = fabsf(c), af = fabsf(f);
     // inner min(|b|, |c|), outer min(., |f|)
     const float wb1 = ab < ac ? 1.0f : (ab == ac ? 0.5f : 0.0f);
     const float m1 = fminf(ab, ac);
     const float wm = m1 < af ? 1.0f : (m1 == af ? 0.5f : 0.0f);
-    if (b != 0.0f) bb = gb * wb1 * wm;
-    if (c != 0.0f) cb = gb * (1.0f - wb1) * wm;
-    if (f != 0.0f) fb = gb * (1.0f - wm);
+    bb = b != 0.0f ? g * wb1 * wm : 0.0f;
+    cb = c != 0.0f ? g * (1.0f - wb1) * wm : 0.0f;
+    fb = f != 0.0f ? g * (1.0f - wm) : 0.0f;
 }
 
 __device__ __forceinline__ void minmod_slope_vjp(float l, float c, float r, float theta, float gs, float& lb,
@@ -93,21 +93,24 @@ __device__ __forceinline__ void desing_vjp(float h, float q, float eps, float rb
 __device__ __forceinline__ void desingularize_cell_vjp(const GocCdklmParams& p, float eta, float hu, float hv,
                                                        float Hm, float oeb, float oub, float ovb, float& eb,
                                                        float& hub, float& hvb) {
-    eb = hub = hvb = 0.0f;
     const float h = eta + Hm;
-    if (fabsf(Hm - p.land_value) <= kDryEps) return;
-    if (h < p.desing_eps) {
-        if (h <= p.depth_cutoff) return;
-        float hb1, hb2;
-        desing_vjp(h, hu, p.desing_eps, oub, hb1, hub);
-        desing_vjp(h, hv, p.desing_eps, ovb, hb2, hvb);
-        eb = oeb + hb1 + hb2;
-    } else {
-        const float ih = 1.0f / h;
-        hub = oub * ih;
-        hvb = ovb * ih;
-        const float ihb = oub * hu + ovb * hv;
-        eb = oeb - ihb * ih * ih;
+    // the wet cell on every lane; land and shallow cells (rare) are redone
+    // under a branch that a warp takes only when one of its lanes has one
+    const float ih = 1.0f / h;
+    hub = oub * ih;
+    hvb = ovb * ih;
+    eb = oeb - (oub * hu + ovb * hv) * ih * ih;
+    const bool land = fabsf(Hm - p.land_value) <= kDryEps;
+    const bool shallow = h < p.desing_eps;
+    if (__any_sync(__activemask(), land || shallow)) {
+        if (land || (shallow && h <= p.depth_cutoff)) {
+            eb = 0.0f; hub = 0.0f; hvb = 0.0f;
+        } else if (shallow) {
+            float hb1, hb2;
+            desing_vjp(h, hu, p.desing_eps, oub, hb1, hub);
+            desing_vjp(h, hv, p.desing_eps, ovb, hb2, hvb);
+            eb = oeb + hb1 + hb2;
+        }
     }
 }
 
@@ -400,9 +403,12 @@ struct AdjTile {
         const float t = (K0 + dxfv) * k.inv_2g;
         const float hw = eC + Hw - t;
         const float he = eC + He + t;
-        float K1b = 0.f, K0b = 0.f, dxfvb = 0.f;
-        if (he > 0.0f) K1b = g2; else { dxfvb -= g2; eCb -= k.two_g * g2; }
-        if (hw > 0.0f) K0b = K1b; else { dxfvb -= K1b; eCb += k.two_g * K1b; }
+        // the clamps of adjustSlopes in reverse (selects)
+        const bool pe = he > 0.0f, pw = hw > 0.0f;
+        const float K1b = pe ? g2 : 0.f;
+        const float K0b = pw ? K1b : 0.f;
+        const float dxfvb = (pe ? 0.f : -g2) - (pw ? 0.f : K1b);
+        eCb += (pe ? 0.f : -k.two_g * g2) + (pw ? 0.f : k.two_g * K1b);
         vCb += dxfvb * p.dx * fC * sa;
         float bb, cb, fb;
         minmod_raw_vjp(back, cent, fwd, K0b, bb, cb, fb);
@@ -456,9 +462,12 @@ struct AdjTile {
         const float t = (L0 - dyfu) * k.inv_2g;
         const float hs = eC + Hs - t;
         const float hn = eC + Hn + t;
-        float L1b = 0.f, L0b = 0.f, dyfub = 0.f;
-        if (hn > 0.0f) L1b = g2; else { dyfub += g2; eCb -= k.two_g * g2; }
-        if (hs > 0.0f) L0b = L1b; else { dyfub += L1b; eCb += k.two_g * L1b; }
+        // the clamps of adjustSlopes in reverse (selects)
+        const bool pn = hn > 0.0f, ps = hs > 0.0f;
+        const float L1b = pn ? g2 : 0.f;
+        const float L0b = ps ? L1b : 0.f;
+        const float dyfub = (pn ? 0.f : g2) + (ps ? 0.f : L1b);
+        eCb += (pn ? 0.f : -k.two_g * g2) + (ps ? 0.f : k.two_g * L1b);
         uCb += dyfub * p.dy * fC * sa;
         float bb, cb, fb;
         minmod_raw_vjp(back, cent, fwd, L0b, bb, cb, fb);
