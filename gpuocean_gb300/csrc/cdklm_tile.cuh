@@ -75,9 +75,19 @@ struct TileSmemAngle : TileSmem<W, H> {
     float Gy2[3][H][W];
 };
 
+// 0.25 sb (sb + sc) (sc + sf) min(|b|, |c|, |f|) with sb, sc, sf the signs
+// (+-1) of b, c, f, evaluated on the sign bits: with all three signs equal
+// the product is sb * min exactly; otherwise it is a zero whose sign the
+// product's factors give - + when sb = sc, - when sb != sc = sf, sb's sign
+// when sb != sc != sf.  The same bits as the floating-point expression for
+// finite arguments.
 __device__ __forceinline__ float minmod_raw(float b, float c, float f) {
-    const float sb = copysignf(1.0f, b), sc = copysignf(1.0f, c), sf = copysignf(1.0f, f);
-    return 0.25f * sb * (sb + sc) * (sc + sf) * fminf(fminf(fabsf(b), fabsf(c)), fabsf(f));
+    const float m = fminf(fminf(fabsf(b), fabsf(c)), fabsf(f));
+    const unsigned B = __float_as_uint(b), C = __float_as_uint(c), F = __float_as_uint(f);
+    const unsigned x1 = B ^ C, x2 = C ^ F;
+    const unsigned zero = (x1 & (~x2 | B)) & 0x80000000u;
+    const unsigned same = __float_as_uint(m) | (B & 0x80000000u);
+    return __uint_as_float(((x1 | x2) & 0x80000000u) ? zero : same);
 }
 
 __device__ __forceinline__ float minmod_slope(float l, float c, float r, float theta) {
