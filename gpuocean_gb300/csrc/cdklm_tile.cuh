@@ -144,8 +144,10 @@ __device__ __forceinline__ void desingularize_cell(const GocCdklmParams& p, floa
 }
 
 // Central-upwind flux with the flux balancer, K/CDKLM16_kernel.cu:82-151.
-// Q = (eta, u_normal, v_transverse).
-__device__ __forceinline__ void cdklm_flux(const GocCdklmParams& p, const StepConst& k,
+// Q = (eta, u_normal, v_transverse).  Returns true where both wave speeds
+// vanish (near-dry faces, rare): the reference's flux is zero there, and the
+// caller replaces the general expression computed here.
+__device__ __forceinline__ bool cdklm_flux(const GocCdklmParams& p, const StepConst& k,
                                            float em, float um_, float vm_, float ep, float up_, float vp_,
                                            float H, float& F0, float& F1, float& F2) {
     // the plus and minus sides in pairs (x: plus, y: minus); a dry side (h at
@@ -164,8 +166,6 @@ __device__ __forceinline__ void cdklm_flux(const GocCdklmParams& p, const StepCo
     const float2 hi = add2(pr(um, up), pr(cm, cp), k.one2);
     const float am = fminf(fminf(lo.x, lo.y), 0.0f);
     const float ap = fmaxf(fmaxf(hi.x, hi.y), 0.0f);
-    // no flux where both wave speeds vanish (near-dry faces, rare): the
-    // general expression is evaluated on every lane and replaced there
     const bool still = fabsf(ap - am) < p.flux_slope_eps;
     const float inv = 1.0f / (ap - am);
     const float apam = ap * am;
@@ -180,9 +180,7 @@ __device__ __forceinline__ void cdklm_flux(const GocCdklmParams& p, const StepCo
     float g2 = (um_ > -up_) ? fb * Fm2 : fb * Fp2;
     g2 += (1.0f - fb) * (((s2.x - s2.y) + apam * (hv.x - hv.y)) * inv);
     F2 = g2;
-    if (still) {
-        F0 = 0.f; F1 = 0.f; F2 = 0.f;
-    }
+    return still;
 }
 
 // Issue the TMA copies of the input boxes of the tile whose staged region
@@ -410,9 +408,13 @@ struct Tile {
                 const float etap =
                     fmaxf(-Hf, ebp - (S.Sx[2][j][i + 1] + p.dx * F(j, i + 1, CONST_F) * vpn) * k.inv_2g);
                 const float etam = fmaxf(-Hf, ebm + (S.Sx[2][j][i] + p.dx * F(j, i, CONST_F) * vmn) * k.inv_2g);
-                cdklm_flux(p, k, etam, Rmx, Rmy, etap, Rpx, Rpy, Hf, F0, F1, F2);
-                // a dry side (rare): no flux but the pressure of the wet side
-                if (__any_sync(__activemask(), dm || dp)) {
+                const bool still = cdklm_flux(p, k, etam, Rmx, Rmy, etap, Rpx, Rpy, Hf, F0, F1, F2);
+                // vanishing wave speeds: no flux; a land side: no flux but
+                // the pressure of the other side (both rare)
+                if (__any_sync(__activemask(), dm || dp || still)) {
+                    if (still) {
+                        F0 = 0.f; F1 = 0.f; F2 = 0.f;
+                    }
                     if (dm || dp) {
                         F0 = 0.f; F2 = 0.f;
                         F1 = (dm && dp) ? 0.f
@@ -443,7 +445,9 @@ struct Tile {
                     } else if (dp) {
                         G1 = k.half_g * (etam + Hf) * (etam + Hf);
                     } else {
-                        cdklm_flux(p, k, etam, Rmx, Rmy, etap, Rpx, Rpy, Hf, G0, G1, G2);
+                        if (cdklm_flux(p, k, etam, Rmx, Rmy, etap, Rpx, Rpy, Hf, G0, G1, G2)) {
+                            G0 = 0.f; G1 = 0.f; G2 = 0.f;
+                        }
                     }
                 };
                 float ax, ay;
@@ -490,9 +494,12 @@ struct Tile {
                     fmaxf(-Hf, ebp - (S.Sy[2][j + 1][i] - p.dy * F(j + 1, i, CONST_F) * upe) * k.inv_2g);
                 const float etam = fmaxf(-Hf, ebm + (S.Sy[2][j][i] - p.dy * F(j, i, CONST_F) * ume) * k.inv_2g);
                 float a0, a1, a2;
-                cdklm_flux(p, k, etam, Rmy, Rmx, etap, Rpy, Rpx, Hf, a0, a1, a2);
+                const bool still = cdklm_flux(p, k, etam, Rmy, Rmx, etap, Rpy, Rpx, Hf, a0, a1, a2);
                 G0 = a0; G1 = a2; G2 = a1;
-                if (__any_sync(__activemask(), dm || dp)) {
+                if (__any_sync(__activemask(), dm || dp || still)) {
+                    if (still) {
+                        G0 = 0.f; G1 = 0.f; G2 = 0.f;
+                    }
                     if (dm || dp) {
                         G0 = 0.f; G1 = 0.f;
                         G2 = (dm && dp) ? 0.f
@@ -525,7 +532,9 @@ struct Tile {
                     } else {
                         // u and v swap roles along y
                         float a0, a1, a2;
-                        cdklm_flux(p, k, etam, Rmy, Rmx, etap, Rpy, Rpx, Hf, a0, a1, a2);
+                        if (cdklm_flux(p, k, etam, Rmy, Rmx, etap, Rpy, Rpx, Hf, a0, a1, a2)) {
+                            a0 = 0.f; a1 = 0.f; a2 = 0.f;
+                        }
                         H0 = a0; H1 = a2; H2 = a1;
                     }
                 };
