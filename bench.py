@@ -34,14 +34,14 @@ NOISE_FACTOR = 8          # coarse grid every 8 cells
 NOISE_L_COARSE = 8.0      # SOAR length scale in coarse cells
 NOISE_STD = 0.003         # target std of the SOAR eta perturbation [m]
 # DRAM bytes (read + write) per member-cell-step of ensemble_rk2_kernel, from
-# one ncu capture of a 96-member C3 launch (220.9 MB read + 148.6 MB written
+# one ncu capture of a 96-member C3 launch (221.0 MB read + 148.7 MB written
 # over 96 x 512 x 300 member-cell-steps, step built without FMA contraction);
 # traffic of a bench launch is scaled by its member-cells.
-NCU_DRAM_BYTES_PER_MEMBER_CELL = 369.6e6 / (96 * 512 * 300)
+NCU_DRAM_BYTES_PER_MEMBER_CELL = 369.7e6 / (96 * 512 * 300)
 # Warp instructions per member-cell-step of the same capture
-# (smsp__inst_executed.sum = 0.900e9): the step is bound by instruction issue,
+# (smsp__inst_executed.sum = 0.883e9): the step is bound by instruction issue,
 # whose ceiling is 4 warp instructions per cycle per SM.
-NCU_WARP_INST_PER_MEMBER_CELL = 0.900e9 / (96 * 512 * 300)
+NCU_WARP_INST_PER_MEMBER_CELL = 0.883e9 / (96 * 512 * 300)
 SM_COUNT = 152
 
 
