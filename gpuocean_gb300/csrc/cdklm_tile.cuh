@@ -1064,10 +1064,11 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
                             nz->spare_e[o] = ne; nz->spare_u[o] = nhu; nz->spare_v[o] = nhv;
                         }
                     }
-                    const float* h0 = Hi_g + (size_t)gy * hi_pitch + gx;
-                    const float hc[4] = {__ldg(h0), __ldg(h0 + 1), __ldg(h0 + hi_pitch), __ldg(h0 + hi_pitch + 1)};
+                    // the cell's corner depths from the tile's plane (land
+                    // corners hold the dry flag there)
+                    const float hc[4] = {S.Hi[j][i], S.Hi[j][i + 1], S.Hi[j + 1][i], S.Hi[j + 1][i + 1]};
                     const int ox = T.x0 + HALO - 1, oy = T.y0 + HALO - 1;
-                    perturbed_state(*nz->d, nx, ny, p.dx, p.dy, p.land_value, gx, gy, nz->d->interpolation_factor <= 1,
+                    perturbed_state(*nz->d, nx, ny, p.dx, p.dy, kDryFlag, gx, gy, nz->d->interpolation_factor <= 1,
                                     [&](int jj, int ii) { return de[(jj - oy) * DW + (ii - ox)]; }, ne, nhu, nhv, hc);
                 }
             }
