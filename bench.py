@@ -255,39 +255,74 @@ def run_reference(args, spec, rank, world):
 
 def run_multilevel(ctx, args, levels=((128, 64, 512), (256, 128, 128), (512, 256, 32)), blocks=5):
     """All levels share one physical domain (2560 km x 1500 km) and the
-    double-jet physics with SOAR model error; every member of every level
-    advances in one persistent launch per RK2 step.  Returns the batched and
-    the member-by-member member-cell-steps/s."""
+    double-jet physics with SOAR model error (independent per member).  The
+    members of each grid advance in one persistent launch per RK2 step of
+    their own engine, the three engines on their own streams (each engine's
+    members share their scalar parameters, which its kernel then reads from
+    the parameter space, and the levels' launches overlap); for comparison
+    all 672 members also run as one engine.  Returns the batched and the
+    member-by-member member-cell-steps/s."""
     from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
     from gpuocean_gb300.SWEsimulators import CDKLM16
     from gpuocean_gb300.SWEsimulators.OceanStateNoise import OceanStateNoise
     from gpuocean_gb300.utils import BenchmarkCases, Common
     Lx, Ly = 2560e3, 1500e3
-    sims = []
     bc = Common.BoundaryConditions(1, 2, 1, 2)
-    for nx, ny, n in levels:
-        c = BenchmarkCases.double_jet_case(nx=nx, ny=ny, dx=Lx / nx, dy=Ly / ny)
-        for m in range(n):
-            s = CDKLM16.CDKLM16(ctx, c["eta0"], c["hu0"], c["hv0"], c["H"], nx, ny, c["dx"], c["dy"], 0.0, c["g"],
-                                c["f"], 0.0, coriolis_beta=c["coriolis_beta"], boundary_conditions=bc,
-                                model_time_step=MODEL_TIME_STEP)
-            s.model_error = OceanStateNoise.fromsim(s, soar_q0=soar_q0(), soar_L=NOISE_L_COARSE * c["dx"] * NOISE_FACTOR,
-                                                    interpolation_factor=NOISE_FACTOR, strict_odd_factor=False)
-            sims.append(s)
-    ens = BatchedEnsemble(sims)
-    ens.set_noise([s.model_error for s in sims], rng_seed=77)
-    ens.updateDt(courant_number=0.8)
-    for _ in range(2):
-        ens.step(MODEL_TIME_STEP, apply_stochastic_term=True)
-    ens.synchronize()
-    t0 = time.perf_counter()
-    cells = 0
-    for _ in range(blocks):
-        cells += ens.step(MODEL_TIME_STEP, apply_stochastic_term=True)
-    ens.synchronize()
-    batched = cells / (time.perf_counter() - t0)
-    shape = list(ens.tile_shape)
-    ens.release()
+
+    def make():
+        per_level = []
+        for nx, ny, n in levels:
+            c = BenchmarkCases.double_jet_case(nx=nx, ny=ny, dx=Lx / nx, dy=Ly / ny)
+            lv = []
+            for m in range(n):
+                s = CDKLM16.CDKLM16(ctx, c["eta0"], c["hu0"], c["hv0"], c["H"], nx, ny, c["dx"], c["dy"], 0.0,
+                                    c["g"], c["f"], 0.0, coriolis_beta=c["coriolis_beta"], boundary_conditions=bc,
+                                    model_time_step=MODEL_TIME_STEP)
+                s.model_error = OceanStateNoise.fromsim(s, soar_q0=soar_q0(),
+                                                        soar_L=NOISE_L_COARSE * c["dx"] * NOISE_FACTOR,
+                                                        interpolation_factor=NOISE_FACTOR, strict_odd_factor=False)
+                lv.append(s)
+            per_level.append(lv)
+        return per_level
+
+    def timed(engines):
+        for e in engines:
+            e.updateDt(courant_number=0.8)
+        for _ in range(2):
+            for e in engines:
+                e.step(MODEL_TIME_STEP, apply_stochastic_term=True)
+        for e in engines:
+            e.synchronize()
+        t0 = time.perf_counter()
+        cells = 0
+        for _ in range(blocks):
+            for e in engines:
+                cells += e.step(MODEL_TIME_STEP, apply_stochastic_term=True)
+        for e in engines:
+            e.synchronize()
+        return cells / (time.perf_counter() - t0)
+
+    # all members as one engine
+    per_level = make()
+    sims = [s for lv in per_level for s in lv]
+    one = BatchedEnsemble(sims)
+    one.set_noise([s.model_error for s in sims], rng_seed=77)
+    one_engine = timed([one])
+    one.release()
+    for s in sims:
+        s.cleanUp(do_gc=False)
+    # one engine per grid, each on its own stream
+    per_level = make()
+    sims = [s for lv in per_level for s in lv]
+    engines = []
+    for k, lv in enumerate(per_level):
+        e = BatchedEnsemble(lv)
+        e.set_noise([s.model_error for s in lv], rng_seed=77 + k)
+        engines.append(e)
+    batched = timed(engines)
+    shape = [list(e.tile_shape) for e in engines]
+    for e in engines:
+        e.release()
     # member by member: a sample of every level, stepped from Python
     sample = [s for lv in range(len(levels)) for s in sims[sum(l[2] for l in levels[:lv]):][:8]]
     for s in sample:
@@ -309,6 +344,7 @@ def run_multilevel(ctx, args, levels=((128, 64, 512), (256, 128, 128), (512, 256
         s.cleanUp(do_gc=False)
     return {"workload": "c4", "levels": [list(l) for l in levels], "members": len(sims),
             "value": batched, "unit": "member-cell-steps/s", "blocks": blocks,
+            "engines": "one per grid, each on its own stream", "one_engine_value": one_engine,
             "per_member_baseline": per_member, "batched_over_per_member": batched / per_member,
             "per_member_sample": len(sample), "tile_shape": shape}
 
