@@ -39,9 +39,9 @@ NOISE_STD = 0.003         # target std of the SOAR eta perturbation [m]
 # traffic of a bench launch is scaled by its member-cells.
 NCU_DRAM_BYTES_PER_MEMBER_CELL = 369.7e6 / (96 * 512 * 300)
 # Warp instructions per member-cell-step of the same capture
-# (smsp__inst_executed.sum = 0.883e9): the step is bound by instruction issue,
+# (smsp__inst_executed.sum = 0.880e9): the step is bound by instruction issue,
 # whose ceiling is 4 warp instructions per cycle per SM.
-NCU_WARP_INST_PER_MEMBER_CELL = 0.883e9 / (96 * 512 * 300)
+NCU_WARP_INST_PER_MEMBER_CELL = 0.880e9 / (96 * 512 * 300)
 SM_COUNT = 152
 
 

@@ -768,6 +768,29 @@ __host__ __device__ inline StepConst make_step_const(const GocCdklmParams& p) {
 // the next tile's rows [2, 6).
 constexpr int kHandRows = 4;
 
+// Copy kHandRows consecutive rows of each of the three state planes (width
+// W, plane strides dst_plane / src_plane floats) between a tile's planes and
+// a packed hand-over buffer [3][kHandRows][W].  The rows of one plane are
+// contiguous, so with W and H even every block starts on a 16-byte boundary
+// and moves as float4.  Items are taken from the last thread down: the first
+// warps carry the extra items of the loops the copy runs beside.
+template <int W, int H, int NT>
+__device__ __forceinline__ void copy_hand_rows(float* dst, int dst_plane, const float* src, int src_plane) {
+    constexpr int NH = kHandRows * W;
+    if constexpr (W % 2 == 0 && H % 2 == 0) {
+        constexpr int N4 = NH / 4;
+        for (int q = NT - 1 - (int)threadIdx.x; q < 3 * N4; q += NT) {
+            const int c = q / N4, r = q - c * N4;
+            reinterpret_cast<float4*>(dst + c * dst_plane)[r] = reinterpret_cast<const float4*>(src + c * src_plane)[r];
+        }
+    } else {
+        for (int q = NT - 1 - (int)threadIdx.x; q < 3 * NH; q += NT) {
+            const int c = q / NH, r = q - c * NH;
+            dst[c * dst_plane + r] = src[c * src_plane + r];
+        }
+    }
+}
+
 // s1: first local row of the stage-1 region the body computes (2: all of it;
 // 6: the rows [2, 6) come from `side_in`, the previous tile of the strip).
 // side_out (if not null) receives the stage-1 rows the next tile of the strip
@@ -943,7 +966,10 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
         // desingularised into D* at once; the wall mirrors write ghost cells,
         // whose own update is skipped.  A rolled loop keeps one copy of the
         // cell update in the kernel (the step is sensitive to the instruction
-        // cache).
+        // cache).  The previous tile's stage-1 rows become this tile's rows
+        // [2, 6) meanwhile: the update neither reads nor writes them (its
+        // rows start at s1 = 6 and read the state planes at their own cell).
+        if (s1 != 2) copy_hand_rows<W, H, NT>(&S.D[0][2][0], H * W, side_in, kHandRows * W);
         for (int idx = threadIdx.x; idx < nu; idx += NT) {
             int i, j;
             block_cell<W - 4>(idx, H - 2 - s1, i, j);
@@ -1000,20 +1026,9 @@ __device__ __forceinline__ bool cdklm_tile_body(const GocCdklmParams& p, const G
             }
         }
         __syncthreads();
-        if (s1 != 2 || side_out) {
-            // stage-1 rows handed over along the strip: take the previous
-            // tile's rows [2, 6), keep this tile's rows [H - 6, H - 2)
-            constexpr int NH = kHandRows * W;
-            for (int q = threadIdx.x; q < NH; q += NT) {
-                const int j = q / W, i = q % W;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    if (s1 != 2) S.D[c][2 + j][i] = side_in[c * NH + q];
-                    if (side_out) side_out[c * NH + q] = S.D[c][H - 2 - kHandRows + j][i];
-                }
-            }
-            if (s1 != 2) __syncthreads();
-        }
+        // this tile's stage-1 rows [H - 6, H - 2) for the next tile of the
+        // strip, beside the slopes below (which only read the state planes)
+        if (side_out) copy_hand_rows<W, H, NT>(side_out, kHandRows * W, &S.D[0][H - 2 - kHandRows][0], H * W);
         // ---- stage 2 on the tile ----
         T.template slopes<4, W - 4, 4, H - 4, CONST_F>();
         __syncthreads();
