@@ -253,15 +253,17 @@ def run_reference(args, spec, rank, world):
 # uneven multi-level ensemble (512 x 64x128, 128 x 128x256, 32 x 256x512)
 # ---------------------------------------------------------------------------
 
-def run_multilevel(ctx, args, levels=((128, 64, 512), (256, 128, 128), (512, 256, 32)), blocks=5):
+def run_multilevel(ctx, args, levels=((128, 64, 512), (256, 128, 128), (512, 256, 32)), blocks=10, reps=3):
     """All levels share one physical domain (2560 km x 1500 km) and the
     double-jet physics with SOAR model error (independent per member).  The
     members of each grid advance in one persistent launch per RK2 step of
     their own engine, the three engines on their own streams (each engine's
     members share their scalar parameters, which its kernel then reads from
     the parameter space, and the levels' launches overlap); for comparison
-    all 672 members also run as one engine.  Returns the batched and the
-    member-by-member member-cell-steps/s."""
+    all 672 members also run as one engine.  Each configuration is timed
+    `reps` times over `blocks` blocks (a repetition takes a few tens of
+    milliseconds, so one host-side stall can dominate it) and reports the
+    median.  Returns the batched and the member-by-member member-cell-steps/s."""
     from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
     from gpuocean_gb300.SWEsimulators import CDKLM16
     from gpuocean_gb300.SWEsimulators.OceanStateNoise import OceanStateNoise
@@ -293,21 +295,24 @@ def run_multilevel(ctx, args, levels=((128, 64, 512), (256, 128, 128), (512, 256
                 e.step(MODEL_TIME_STEP, apply_stochastic_term=True)
         for e in engines:
             e.synchronize()
-        t0 = time.perf_counter()
-        cells = 0
-        for _ in range(blocks):
+        rates = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            cells = 0
+            for _ in range(blocks):
+                for e in engines:
+                    cells += e.step(MODEL_TIME_STEP, apply_stochastic_term=True)
             for e in engines:
-                cells += e.step(MODEL_TIME_STEP, apply_stochastic_term=True)
-        for e in engines:
-            e.synchronize()
-        return cells / (time.perf_counter() - t0)
+                e.synchronize()
+            rates.append(cells / (time.perf_counter() - t0))
+        return float(np.median(rates)), rates
 
     # all members as one engine
     per_level = make()
     sims = [s for lv in per_level for s in lv]
     one = BatchedEnsemble(sims)
     one.set_noise([s.model_error for s in sims], rng_seed=77)
-    one_engine = timed([one])
+    one_engine, one_engine_reps = timed([one])
     one.release()
     for s in sims:
         s.cleanUp(do_gc=False)
@@ -319,7 +324,7 @@ def run_multilevel(ctx, args, levels=((128, 64, 512), (256, 128, 128), (512, 256
         e = BatchedEnsemble(lv)
         e.set_noise([s.model_error for s in lv], rng_seed=77 + k)
         engines.append(e)
-    batched = timed(engines)
+    batched, batched_reps = timed(engines)
     shape = [list(e.tile_shape) for e in engines]
     for e in engines:
         e.release()
@@ -343,8 +348,9 @@ def run_multilevel(ctx, args, levels=((128, 64, 512), (256, 128, 128), (512, 256
     for s in sims:
         s.cleanUp(do_gc=False)
     return {"workload": "c4", "levels": [list(l) for l in levels], "members": len(sims),
-            "value": batched, "unit": "member-cell-steps/s", "blocks": blocks,
-            "engines": "one per grid, each on its own stream", "one_engine_value": one_engine,
+            "value": batched, "unit": "member-cell-steps/s", "blocks": blocks, "repetitions": reps,
+            "value_per_repetition": batched_reps, "engines": "one per grid, each on its own stream",
+            "one_engine_value": one_engine, "one_engine_value_per_repetition": one_engine_reps,
             "per_member_baseline": per_member, "batched_over_per_member": batched / per_member,
             "per_member_sample": len(sample), "tile_shape": shape}
 
