@@ -45,6 +45,21 @@ NCU_WARP_INST_PER_MEMBER_CELL = 0.880e9 / (96 * 512 * 300)
 SM_COUNT = 152
 
 
+def sample_extras(spec):
+    """What the oracle's timed member block runs beside the step."""
+    extras = [w for w, on in (("its SOAR model error", spec["noise"]),
+                              (f"{spec['drifters']} drifters per member", spec["drifters"])) if on]
+    return " with " + " and ".join(extras) if extras else ""
+
+
+def model_error_text(spec):
+    """The workload's model error as the bench lines describe it."""
+    if not spec["noise"]:
+        return None
+    return (f"SOAR every {MODEL_TIME_STEP:.0f} s, coarse factor {NOISE_FACTOR}, L={NOISE_L_COARSE:g} coarse cells, "
+            f"std {NOISE_STD} m")
+
+
 def soar_q0(L_cells=NOISE_L_COARSE, std=NOISE_STD):
     """q0 such that the SOAR field sum_{5x5} Q xi has standard deviation `std`
     for unit normals: q0 = std / sqrt(sum s(d)^2), s(d) = (1 + d/L) exp(-d/L)."""
@@ -197,13 +212,38 @@ def _oracle_member_block(args):
     sim = OracleCDKLM16(case["eta0"], case["hu0"], case["hv0"], case["H"], case["nx"], case["ny"], case["dx"],
                         case["dy"], 0.0, case["g"], case["f"], case["r"],
                         coriolis_beta=case.get("coriolis_beta", 0.0), boundary_conditions=BC(*case["boundary"]))
+    nx, ny, dx, dy = case["nx"], case["ny"], case["dx"], case["dy"]
+    bc = BC(*case["boundary"])
+    rng = np.random.default_rng(1000 + m)
+    pos = None
+    if spec["drifters"]:
+        pos = np.stack([rng.uniform(0, nx * dx, spec["drifters"] + 1), rng.uniform(0, ny * dy, spec["drifters"] + 1)],
+                       axis=1)
     t0 = time.perf_counter()
     steps = 0
     for _ in range(n_blocks):
         before = sim.num_iterations
         sim.step(MODEL_TIME_STEP)
-        steps += sim.num_iterations - before
-    return steps * case["nx"] * case["ny"], time.perf_counter() - t0
+        taken = sim.num_iterations - before
+        steps += taken
+        if spec["noise"]:
+            # the block's SOAR model error (normals from numpy: only the work
+            # is timed here, the draws are not the engine's)
+            from oracle.noise_oracle import bicubic_perturbation, soar_coarse
+            cnx, cny = -(-nx // NOISE_FACTOR), -(-ny // NOISE_FACTOR)
+            cdx, cdy = dx * NOISE_FACTOR, dy * NOISE_FACTOR
+            pns, pew = bc.north == 2, bc.east == 2
+            xi = rng.standard_normal((cny if pns else cny + 8, cnx if pew else cnx + 8))
+            coarse = soar_coarse(xi, cnx, cny, cdx, cdy, soar_q0(), NOISE_L_COARSE * cdx, pns, pew)
+            bicubic_perturbation(sim.Q0[0], sim.Q0[1], sim.Q0[2], coarse, sim.Hi, nx, ny, dx, dy, cnx, cny, cdx, cdy,
+                                 float(sim.f), float(sim.coriolis_beta), case["g"])
+        if pos is not None:
+            # one drifter step per model step of the block
+            from oracle.noise_oracle import drift
+            for _ in range(taken):
+                pos = drift(pos, sim.Q0[0], sim.Q0[1], sim.Q0[2], sim.Hm, nx, ny, dx, dy, sim.dt,
+                            bc.north == 2, bc.east == 2)
+    return steps * nx * ny, time.perf_counter() - t0
 
 
 def cpu_reference_rate(spec, n_members, n_blocks, cores):
@@ -236,12 +276,15 @@ def run_reference(args, spec, rank, world):
         walls.append(w)
     value = statistics.median(rates)
     wall = statistics.median(walls)
-    sample = (f"{n_members} members x 1 block of {MODEL_TIME_STEP:.0f} s of the {spec['name']} workload per step, "
-              f"FP64 NumPy restatement (the reference has no CPU step), one member per process")
+    sample = (f"{n_members} of the {spec['members']} members x 1 block of {MODEL_TIME_STEP:.0f} s of the "
+              f"{spec['name']} workload per step{sample_extras(spec)}, FP64 NumPy restatement (the reference has no "
+              f"CPU step), one member per process")
     line = {"metric": "member-cell-steps/s", "value": value, "unit": "member-cell-steps/s", "n_gpus": world,
             "steps": len(rates), "warmup": args.warmup, "ms_per_step": 1000.0 * wall, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": spec["name"], "members": n_members, "nx": spec["nx"], "ny": spec["ny"]},
+            "config": {"workload": spec["name"], "members": spec["members"], "nx": spec["nx"], "ny": spec["ny"],
+                       "drifters_per_member": spec["drifters"], "block_seconds": MODEL_TIME_STEP,
+                       "model_error": model_error_text(spec)},
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "member-cell-steps/s", "cores": cores, "kind": "port",
                              "sample": sample},
@@ -927,8 +970,8 @@ def main():
         n_cpu_members = 2
         rate, wall_cpu = cpu_reference_rate(spec, n_cpu_members, 1, 1)
         cpu = {"value": rate, "unit": "member-cell-steps/s", "cores": 1, "kind": "port",
-               "sample": f"{n_cpu_members} members x 1 block of {MODEL_TIME_STEP:.0f} s ({wall_cpu:.1f} s), FP64 NumPy "
-                         f"restatement of the reference step on one core"}
+               "sample": f"{n_cpu_members} members x 1 block of {MODEL_TIME_STEP:.0f} s{sample_extras(spec)} "
+                         f"({wall_cpu:.1f} s), FP64 NumPy restatement of the reference step on one core"}
 
     if rank == 0:
         line = {
@@ -938,8 +981,7 @@ def main():
             "data": "synthetic",
             "config": {"workload": spec["name"], "members": len(sims), "nx": spec["nx"], "ny": spec["ny"],
                        "drifters_per_member": n_d, "block_seconds": MODEL_TIME_STEP,
-                       "model_error": (f"SOAR every {MODEL_TIME_STEP:.0f} s, coarse factor {NOISE_FACTOR}, "
-                                       f"L={NOISE_L_COARSE:g} coarse cells, std {NOISE_STD} m") if noise else None,
+                       "model_error": model_error_text(spec),
                        "substeps_per_block": int(sched[3]), "l2": "inputs larger than L2"
                        if 24 * sum(int(s.nx) * int(s.ny) for s in sims) > 129e6 else "inputs smaller than L2",
                        "parallelism": f"replicas x{world}",

@@ -96,42 +96,48 @@ _B = np.array([[1., 0., 0., 0.], [0., 0., 1., 0.], [-3., 3., -2., -1.], [2., -2.
 
 def bicubic_eta(coarse, nx, ny, dx, dy, cnx, cny, cdx, cdy, offset_i=0, offset_j=0):
     """d_eta on the fine cells [1, nx+3) x [1, ny+3) (interior + one ring) by
-    bicubic interpolation of the coarse field (K/ocean_noise.cu:497-586)."""
+    bicubic interpolation of the coarse field (K/ocean_noise.cu:497-586).
+    Every fine cell at once: its coarse cell (cj, ci) and fractions (ry, rx)
+    per row and column, the 4x4 table of values, x / y differences and the
+    cross difference gathered from the clamped coarse field, then
+    [1 rx rx^2 rx^3] B F B^T [1 ry ry^2 ry^3]^T."""
     c = np.asarray(coarse, dtype=np.float64)
     out = np.zeros((ny + 4, nx + 4))
-    for j in range(1, ny + 3):
-        y = (j - 2 + 0.5 + offset_j) * dy
-        cj = int(math.floor(y / cdy + 2 - 0.5))
-        if cj > cny + 1:
-            cj -= 1
-        ry = (y - (cj - 2 + 0.5) * cdy) / cdy
-        for i in range(1, nx + 3):
-            x = (i - 2 + 0.5 + offset_i) * dx
-            ci = int(math.floor(x / cdx + 2 - 0.5))
-            if ci > cnx + 1:
-                ci -= 1
-            rx = (x - (ci - 2 + 0.5) * cdx) / cdx
+    j = np.arange(1, ny + 3, dtype=np.float64)
+    i = np.arange(1, nx + 3, dtype=np.float64)
+    y = (j - 2 + 0.5 + offset_j) * dy
+    x = (i - 2 + 0.5 + offset_i) * dx
+    cj = np.floor(y / cdy + 2 - 0.5).astype(np.int64)
+    ci = np.floor(x / cdx + 2 - 0.5).astype(np.int64)
+    cj = np.where(cj > cny + 1, cj - 1, cj)
+    ci = np.where(ci > cnx + 1, ci - 1, ci)
+    ry = (y - (cj - 2 + 0.5) * cdy) / cdy
+    rx = (x - (ci - 2 + 0.5) * cdx) / cdx
 
-            def C(jj, ii):
-                return c[min(max(jj, 0), cny + 3), min(max(ii, 0), cnx + 3)]
-            f00, f01, f10, f11 = C(cj, ci), C(cj + 1, ci), C(cj, ci + 1), C(cj + 1, ci + 1)
-            fx00 = (C(cj, ci + 1) - C(cj, ci - 1)) / 2
-            fx01 = (C(cj + 1, ci + 1) - C(cj + 1, ci - 1)) / 2
-            fx10 = (C(cj, ci + 2) - C(cj, ci)) / 2
-            fx11 = (C(cj + 1, ci + 2) - C(cj + 1, ci)) / 2
-            fy00 = (C(cj + 1, ci) - C(cj - 1, ci)) / 2
-            fy01 = (C(cj + 2, ci) - C(cj, ci)) / 2
-            fy10 = (C(cj + 1, ci + 1) - C(cj - 1, ci + 1)) / 2
-            fy11 = (C(cj + 2, ci + 1) - C(cj, ci + 1)) / 2
-            fy_10 = (C(cj + 1, ci - 1) - C(cj - 1, ci - 1)) / 2
-            fy_11 = (C(cj + 2, ci - 1) - C(cj, ci - 1)) / 2
-            fy20 = (C(cj + 1, ci + 2) - C(cj - 1, ci + 2)) / 2
-            fy21 = (C(cj + 2, ci + 2) - C(cj, ci + 2)) / 2
-            F = np.array([[f00, f01, fy00, fy01], [f10, f11, fy10, fy11],
-                          [fx00, fx01, (fy10 - fy_10) / 2, (fy11 - fy_11) / 2],
-                          [fx10, fx11, (fy20 - fy00) / 2, (fy21 - fy01) / 2]])
-            A = _B @ F @ _B.T
-            out[j, i] = np.array([1.0, rx, rx * rx, rx ** 3]) @ A @ np.array([1.0, ry, ry * ry, ry ** 3])
+    def C(dj, di):
+        rows = np.clip(cj + dj, 0, cny + 3)[:, None]
+        cols = np.clip(ci + di, 0, cnx + 3)[None, :]
+        return c[rows, cols]
+    f00, f01, f10, f11 = C(0, 0), C(1, 0), C(0, 1), C(1, 1)
+    fx00 = (C(0, 1) - C(0, -1)) / 2
+    fx01 = (C(1, 1) - C(1, -1)) / 2
+    fx10 = (C(0, 2) - C(0, 0)) / 2
+    fx11 = (C(1, 2) - C(1, 0)) / 2
+    fy00 = (C(1, 0) - C(-1, 0)) / 2
+    fy01 = (C(2, 0) - C(0, 0)) / 2
+    fy10 = (C(1, 1) - C(-1, 1)) / 2
+    fy11 = (C(2, 1) - C(0, 1)) / 2
+    fy_10 = (C(1, -1) - C(-1, -1)) / 2
+    fy_11 = (C(2, -1) - C(0, -1)) / 2
+    fy20 = (C(1, 2) - C(-1, 2)) / 2
+    fy21 = (C(2, 2) - C(0, 2)) / 2
+    F = np.stack([np.stack([f00, f01, fy00, fy01], -1), np.stack([f10, f11, fy10, fy11], -1),
+                  np.stack([fx00, fx01, (fy10 - fy_10) / 2, (fy11 - fy_11) / 2], -1),
+                  np.stack([fx10, fx11, (fy20 - fy00) / 2, (fy21 - fy01) / 2], -1)], -2)
+    A = _B @ F @ _B.T
+    px = np.stack([np.ones_like(rx), rx, rx * rx, rx ** 3], -1)      # (nx+2, 4)
+    py = np.stack([np.ones_like(ry), ry, ry * ry, ry ** 3], -1)      # (ny+2, 4)
+    out[1:ny + 3, 1:nx + 3] = np.einsum("xa,yxab,yb->yx", px, A, py)
     return out
 
 
