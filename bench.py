@@ -208,12 +208,12 @@ def algorithmic_bytes_per_launch(sims, n_active, distinct_bathymetry):
 def _oracle_member_block(args):
     spec, m, n_blocks = args
     from oracle.cdklm16_oracle import BC, OracleCDKLM16
+    from oracle.noise_oracle import bicubic_perturbation, drift, soar_coarse
     case = make_case(spec)
-    sim = OracleCDKLM16(case["eta0"], case["hu0"], case["hv0"], case["H"], case["nx"], case["ny"], case["dx"],
-                        case["dy"], 0.0, case["g"], case["f"], case["r"],
-                        coriolis_beta=case.get("coriolis_beta", 0.0), boundary_conditions=BC(*case["boundary"]))
     nx, ny, dx, dy = case["nx"], case["ny"], case["dx"], case["dy"]
     bc = BC(*case["boundary"])
+    sim = OracleCDKLM16(case["eta0"], case["hu0"], case["hv0"], case["H"], nx, ny, dx, dy, 0.0, case["g"], case["f"],
+                        case["r"], coriolis_beta=case.get("coriolis_beta", 0.0), boundary_conditions=bc)
     rng = np.random.default_rng(1000 + m)
     pos = None
     if spec["drifters"]:
@@ -229,7 +229,6 @@ def _oracle_member_block(args):
         if spec["noise"]:
             # the block's SOAR model error (normals from numpy: only the work
             # is timed here, the draws are not the engine's)
-            from oracle.noise_oracle import bicubic_perturbation, soar_coarse
             cnx, cny = -(-nx // NOISE_FACTOR), -(-ny // NOISE_FACTOR)
             cdx, cdy = dx * NOISE_FACTOR, dy * NOISE_FACTOR
             pns, pew = bc.north == 2, bc.east == 2
@@ -239,7 +238,6 @@ def _oracle_member_block(args):
                                  float(sim.f), float(sim.coriolis_beta), case["g"])
         if pos is not None:
             # one drifter step per model step of the block
-            from oracle.noise_oracle import drift
             for _ in range(taken):
                 pos = drift(pos, sim.Q0[0], sim.Q0[1], sim.Q0[2], sim.Hm, nx, ny, dx, dy, sim.dt,
                             bc.north == 2, bc.east == 2)
