@@ -301,10 +301,10 @@ def run_multilevel(ctx, args, levels=((128, 64, 512), (256, 128, 128), (512, 256
     their own engine, the three engines on their own streams (each engine's
     members share their scalar parameters, which its kernel then reads from
     the parameter space, and the levels' launches overlap); for comparison
-    all 672 members also run as one engine.  Each configuration is timed
-    `reps` times over `blocks` blocks (a repetition takes a few tens of
-    milliseconds, so one host-side stall can dominate it) and reports the
-    median.  Returns the batched and the member-by-member member-cell-steps/s."""
+    all 672 members also run as one engine.  Each configuration, and the
+    member-by-member sample, is timed `reps` times (a repetition takes a few
+    tens of milliseconds, so one host-side stall can dominate it) and reports
+    the median.  Returns the batched and the member-by-member member-cell-steps/s."""
     from gpuocean_gb300.ensembles.BatchedEnsemble import BatchedEnsemble
     from gpuocean_gb300.SWEsimulators import CDKLM16
     from gpuocean_gb300.SWEsimulators.OceanStateNoise import OceanStateNoise
@@ -376,23 +376,27 @@ def run_multilevel(ctx, args, levels=((128, 64, 512), (256, 128, 128), (512, 256
         s.perturbState()
     for s in sample:
         s.gpu_stream.synchronize()
-    t0 = time.perf_counter()
-    pm = 0
-    for s in sample:
-        before = s.num_iterations
-        s.step(MODEL_TIME_STEP, apply_stochastic_term=False)
-        s.perturbState()
-        pm += (s.num_iterations - before) * int(s.nx) * int(s.ny)
-    for s in sample:
-        s.gpu_stream.synchronize()
-    per_member = pm / (time.perf_counter() - t0)
+    pm_rates = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        pm = 0
+        for s in sample:
+            before = s.num_iterations
+            s.step(MODEL_TIME_STEP, apply_stochastic_term=False)
+            s.perturbState()
+            pm += (s.num_iterations - before) * int(s.nx) * int(s.ny)
+        for s in sample:
+            s.gpu_stream.synchronize()
+        pm_rates.append(pm / (time.perf_counter() - t0))
+    per_member = float(np.median(pm_rates))
     for s in sims:
         s.cleanUp(do_gc=False)
     return {"workload": "c4", "levels": [list(l) for l in levels], "members": len(sims),
             "value": batched, "unit": "member-cell-steps/s", "blocks": blocks, "repetitions": reps,
             "value_per_repetition": batched_reps, "engines": "one per grid, each on its own stream",
             "one_engine_value": one_engine, "one_engine_value_per_repetition": one_engine_reps,
-            "per_member_baseline": per_member, "batched_over_per_member": batched / per_member,
+            "per_member_baseline": per_member, "per_member_baseline_per_repetition": pm_rates,
+            "batched_over_per_member": batched / per_member,
             "per_member_sample": len(sample), "tile_shape": shape}
 
 
